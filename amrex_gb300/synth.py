@@ -58,7 +58,7 @@ def gaussian_random_field(shape_zyx, seed, sigma_cells=5.0):
     kx = np.fft.rfftfreq(shape_zyx[2])[None, None, :]
     # Fourier transform of a unit-mass Gaussian with std sigma (in cells)
     filt = np.exp(-2.0 * (np.pi * sigma_cells) ** 2 * (kx * kx + ky * ky + kz * kz))
-    g = np.fft.irfftn(np.fft.rfftn(noise) * filt, s=shape_zyx)
+    g = np.fft.irfftn(np.fft.rfftn(noise) * filt, s=shape_zyx, axes=(0, 1, 2))
     g -= g.mean()
     g /= g.std()
     return g

@@ -1,0 +1,56 @@
+"""The CPU oracle (oracle/mlmg_oracle.c) against the golden fixtures made by
+the reference AMReX CPU MLMG itself (tests/golden/make_golden.py)."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tests.golden import cases, load
+
+
+@pytest.mark.parametrize("name", load.names("hier_"))
+def test_hierarchy_matches_reference(name):
+    g = load.load(name)
+    assert oracle.hierarchy(g["case"]) == g["hier"]
+
+
+@pytest.mark.parametrize("name", load.names("hier_"))
+def test_python_max_size_matches_reference(name):
+    g = load.load(name)
+    c = g["case"]
+    if "boxes" in c:
+        pytest.skip("explicit boxes")
+    assert cases.max_size_boxes(c["n"], c["max_grid_size"]) == \
+        [((b[0], b[1], b[2]), (b[3], b[4], b[5])) for b in g["hier"][0]]
+    assert oracle.max_size(c["n"], c["max_grid_size"]) == g["hier"][0]
+
+
+@pytest.mark.parametrize("name", load.names("fb_"))
+def test_fill_boundary_bit_exact(name):
+    g = load.load(name)
+    out = oracle.fill_boundary(g["case"], g["fb_in"], g["case"]["cross"])
+    assert np.array_equal(out, g["fb_out"])
+
+
+@pytest.mark.parametrize("name", load.names("apply_"))
+def test_apply_matches_reference(name):
+    g = load.load(name)
+    c = g["case"]
+    out = oracle.apply(c, cases.inputs(c))
+    ref = g["out"].reshape(out.shape)
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(out, ref, rtol=0, atol=1e-13 * scale)
+
+
+@pytest.mark.parametrize("name", load.names("solve_"))
+def test_solve_matches_reference(name):
+    g = load.load(name)
+    c = g["case"]
+    phi, info = oracle.solve(c, cases.inputs(c))
+    ref = g["phi"].reshape(phi.shape)
+    r = g["result"]
+    assert info["status"] == 0
+    assert info["niters"] == r["niters"]
+    assert info["cg_iters"] == r["cg_iters"]
+    np.testing.assert_allclose(info["history"], r["history"], rtol=1e-6)
+    # phi agrees to 1e-10 relative (max norm)
+    assert np.abs(phi - ref).max() <= 1e-10 * np.abs(ref).max()
