@@ -1,0 +1,373 @@
+"""GB300-native MLMG (cell-centred MLPoisson / MLABecLaplacian) -- Python host API.
+
+A thin mirror of the reference's C++ interface for this path (amrex::BoxArray,
+DistributionMapping, Geometry, MultiFab, LPInfo, MLPoisson, MLABecLaplacian,
+MLMG), implemented over the C ABI of ``libamrex_gb300.so``
+(include/mlmg_capi.h).  All compute runs in hand-written sm_103a kernels;
+importing this package never falls back to a CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import capi
+from .capi import MLMGError, check
+
+__all__ = ["Box", "BoxArray", "DistributionMapping", "Geometry", "MultiFab", "LPInfo", "LinOpBCType",
+           "MLPoisson", "MLABecLaplacian", "MLMG", "MLMGError", "solve_batched", "kernel_launches"]
+
+
+class LinOpBCType:
+    """LinOpBCType codes (Src/Boundary/AMReX_LO_BCTYPES.H:5-35)."""
+    interior = 0
+    Dirichlet = 101
+    Neumann = 102
+    reflect_odd = 103
+    Periodic = 200
+
+
+def _i3(v):
+    return capi.I3(*[int(x) for x in v])
+
+
+def _d3(v):
+    return capi.D3(*[float(x) for x in v])
+
+
+class Box:
+    def __init__(self, lo, hi):
+        self.lo = tuple(int(x) for x in lo)
+        self.hi = tuple(int(x) for x in hi)
+
+    def length(self, d=None):
+        ln = tuple(self.hi[i] - self.lo[i] + 1 for i in range(3))
+        return ln if d is None else ln[d]
+
+    def numPts(self):
+        n = self.length()
+        return n[0] * n[1] * n[2]
+
+    def __eq__(self, o):
+        return isinstance(o, Box) and self.lo == o.lo and self.hi == o.hi
+
+    def __repr__(self):
+        return f"Box({self.lo}, {self.hi})"
+
+
+class BoxArray:
+    """amrex::BoxArray: BoxArray(domain) or BoxArray(list_of_boxes); maxSize."""
+
+    def __init__(self, boxes):
+        h = ctypes.c_void_p()
+        if isinstance(boxes, Box):
+            check(capi.lib().mlmg_boxarray_new_domain(_i3(boxes.lo), _i3(boxes.hi), ctypes.byref(h)))
+        else:
+            flat = np.array([list(b.lo) + list(b.hi) for b in boxes], dtype=np.int32).ravel()
+            check(capi.lib().mlmg_boxarray_new(flat.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(boxes),
+                                               ctypes.byref(h)))
+        self._h = h
+
+    def maxSize(self, chunk):
+        if np.isscalar(chunk):
+            chunk = (chunk, chunk, chunk)
+        check(capi.lib().mlmg_boxarray_maxsize(self._h, _i3(chunk)))
+        return self
+
+    def size(self):
+        return capi.lib().mlmg_boxarray_size(self._h)
+
+    def __len__(self):
+        return self.size()
+
+    def __getitem__(self, i):
+        lo, hi = capi.I3(), capi.I3()
+        check(capi.lib().mlmg_boxarray_get(self._h, int(i), lo, hi))
+        return Box(tuple(lo), tuple(hi))
+
+    def boxes(self):
+        return [self[i] for i in range(self.size())]
+
+    def __del__(self):
+        if getattr(self, "_h", None) and capi._lib is not None:
+            capi.lib().mlmg_boxarray_delete(self._h)
+
+
+class DistributionMapping:
+    """amrex::DistributionMapping(const BoxArray&): one GPU owns every box."""
+
+    def __init__(self, ba):
+        h = ctypes.c_void_p()
+        check(capi.lib().mlmg_distromap_new(ba._h, ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and capi._lib is not None:
+            capi.lib().mlmg_distromap_delete(self._h)
+
+
+class Geometry:
+    """amrex::Geometry(domain, RealBox, coord=cartesian, is_periodic)."""
+
+    def __init__(self, domain, prob_lo=(0.0, 0.0, 0.0), prob_hi=(1.0, 1.0, 1.0), is_periodic=(0, 0, 0)):
+        h = ctypes.c_void_p()
+        check(capi.lib().mlmg_geometry_new(_i3(domain.lo), _i3(domain.hi), _d3(prob_lo), _d3(prob_hi),
+                                           _i3(is_periodic), ctypes.byref(h)))
+        self._h = h
+        self.domain = domain
+        self.is_periodic = tuple(is_periodic)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and capi._lib is not None:
+            capi.lib().mlmg_geometry_delete(self._h)
+
+
+class MultiFab:
+    """amrex::MultiFab(ba, dm, ncomp, ngrow) on the GPU; ``nodal_dir`` makes a
+    face-centred MultiFab (amrex::convert(ba, IntVect::TheDimensionVector(d))),
+    ``precision`` 8 (double) or 4 (float)."""
+
+    def __init__(self, ba, dm, ncomp=1, ngrow=0, nodal_dir=-1, precision=8):
+        h = ctypes.c_void_p()
+        check(capi.lib().mlmg_multifab_new(ba._h, dm._h, ncomp, ngrow, nodal_dir, precision, ctypes.byref(h)))
+        self._h = h
+        self.ba, self.ncomp, self.ngrow, self.nodal_dir, self.precision = ba, ncomp, ngrow, nodal_dir, precision
+        self.dtype = np.float64 if precision == 8 else np.float32
+
+    def __del__(self):
+        if getattr(self, "_h", None) and capi._lib is not None:
+            capi.lib().mlmg_multifab_delete(self._h)
+
+    def fab_box(self, i):
+        b = self.ba[i]
+        lo = [x - self.ngrow for x in b.lo]
+        hi = [x + self.ngrow for x in b.hi]
+        if self.nodal_dir >= 0:
+            hi[self.nodal_dir] += 1
+        return Box(lo, hi)
+
+    def fab_shape(self, i):
+        n = self.fab_box(i).length()
+        return (self.ncomp, n[2], n[1], n[0]) if self.ncomp > 1 else (n[2], n[1], n[0])
+
+    def set_fab(self, i, arr):
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        assert a.size == int(np.prod(self.fab_shape(i)))
+        check(capi.lib().mlmg_multifab_upload(self._h, int(i), a.ctypes.data))
+
+    def get_fab(self, i):
+        a = np.empty(self.fab_shape(i), dtype=self.dtype)
+        check(capi.lib().mlmg_multifab_download(self._h, int(i), a.ctypes.data))
+        return a
+
+    def set_global(self, arr, lo=(0, 0, 0)):
+        """Fill every FAB from a whole-domain array (nz, ny, nx) whose lowest
+        cell is ``lo`` (ghost cells are filled where the array covers them)."""
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        n = (a.shape[2], a.shape[1], a.shape[0])
+        check(capi.lib().mlmg_multifab_upload_global(self._h, a.ctypes.data, _i3(lo), _i3(n)))
+
+    def get_global(self, shape_zyx, lo=(0, 0, 0), out=None):
+        a = out if out is not None else np.zeros(shape_zyx, dtype=self.dtype)
+        n = (a.shape[2], a.shape[1], a.shape[0])
+        check(capi.lib().mlmg_multifab_download_global(self._h, a.ctypes.data, _i3(lo), _i3(n)))
+        return a
+
+    def setVal(self, v):
+        check(capi.lib().mlmg_multifab_setval(self._h, float(v)))
+
+    def FillBoundary(self, geom, cross=False):
+        check(capi.lib().mlmg_multifab_fill_boundary(self._h, geom._h, int(bool(cross))))
+
+    def norminf(self):
+        v = ctypes.c_double()
+        check(capi.lib().mlmg_multifab_norminf(self._h, ctypes.byref(v)))
+        return v.value
+
+
+class LPInfo:
+    """amrex::LPInfo (Src/LinearSolvers/MLMG/AMReX_MLLinOp.H:34-83)."""
+
+    def __init__(self):
+        self.agglomeration, self.consolidation = True, True
+        self.agg_grid_size, self.con_grid_size = -1, -1
+        self.max_coarsening_level = 30
+
+    def setAgglomeration(self, x):
+        self.agglomeration = bool(x); return self
+
+    def setConsolidation(self, x):
+        self.consolidation = bool(x); return self
+
+    def setAgglomerationGridSize(self, x):
+        self.agg_grid_size = int(x); return self
+
+    def setConsolidationGridSize(self, x):
+        self.con_grid_size = int(x); return self
+
+    def setMaxCoarseningLevel(self, n):
+        self.max_coarsening_level = int(n); return self
+
+    def _c(self):
+        return capi.LPInfoC(int(self.agglomeration), int(self.consolidation), self.agg_grid_size,
+                            self.con_grid_size, self.max_coarsening_level)
+
+
+class _LinOp:
+    _ctor = None
+
+    def __init__(self, geom, ba, dm, info=None):
+        geoms = geom if isinstance(geom, (list, tuple)) else [geom]
+        bas = ba if isinstance(ba, (list, tuple)) else [ba]
+        dms = dm if isinstance(dm, (list, tuple)) else [dm]
+        n = len(geoms)
+        G = (ctypes.c_void_p * n)(*[g._h for g in geoms])
+        B = (ctypes.c_void_p * n)(*[b._h for b in bas])
+        D = (ctypes.c_void_p * n)(*[d._h for d in dms])
+        h = ctypes.c_void_p()
+        inf = (info or LPInfo())._c()
+        check(getattr(capi.lib(), self._ctor)(n, G, B, D, ctypes.byref(inf), ctypes.byref(h)))
+        self._h = h
+        self._keep = (geoms, bas, dms)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and capi._lib is not None:
+            capi.lib().mlmg_linop_delete(self._h)
+
+    def setDomainBC(self, lobc, hibc):
+        check(capi.lib().mlmg_linop_set_domain_bc(self._h, _i3(lobc), _i3(hibc)))
+
+    def setLevelBC(self, amrlev, mf):
+        check(capi.lib().mlmg_linop_set_level_bc(self._h, amrlev, None if mf is None else mf._h))
+
+    def setMaxOrder(self, o):
+        check(capi.lib().mlmg_linop_set_maxorder(self._h, int(o)))
+
+    def NMGLevels(self, amrlev=0):
+        return capi.lib().mlmg_linop_num_mg_levels(self._h)
+
+
+class MLPoisson(_LinOp):
+    _ctor = "mlmg_linop_new_poisson"
+
+
+class MLABecLaplacian(_LinOp):
+    """alpha a phi - beta div(b grad phi)."""
+    _ctor = "mlmg_linop_new_abeclap"
+
+    def setScalars(self, a, b):
+        check(capi.lib().mlmg_abeclap_set_scalars(self._h, float(a), float(b)))
+
+    def setACoeffs(self, amrlev, a):
+        if isinstance(a, MultiFab):
+            check(capi.lib().mlmg_abeclap_set_acoeffs(self._h, amrlev, a._h))
+        else:
+            check(capi.lib().mlmg_abeclap_set_acoeffs_const(self._h, amrlev, float(a)))
+
+    def setBCoeffs(self, amrlev, b):
+        if isinstance(b, (list, tuple)):
+            arr = (ctypes.c_void_p * 3)(*[x._h for x in b])
+            check(capi.lib().mlmg_abeclap_set_bcoeffs(self._h, amrlev, arr))
+        else:
+            check(capi.lib().mlmg_abeclap_set_bcoeffs_const(self._h, amrlev, float(b)))
+
+
+class MLMG:
+    """amrex::MLMG(linop): solve, apply, setters and getters."""
+
+    def __init__(self, linop):
+        h = ctypes.c_void_p()
+        check(capi.lib().mlmg_new(linop._h, ctypes.byref(h)))
+        self._h = h
+        self.linop = linop
+
+    def __del__(self):
+        if getattr(self, "_h", None) and capi._lib is not None:
+            capi.lib().mlmg_delete(self._h)
+
+    def _set(self, name, v):
+        check(getattr(capi.lib(), name)(self._h, v))
+
+    def setVerbose(self, v): self._set("mlmg_set_verbose", int(v))
+    def setMaxIter(self, n): self._set("mlmg_set_max_iter", int(n))
+    def setMaxFmgIter(self, n): self._set("mlmg_set_max_fmg_iter", int(n))
+    def setFixedIter(self, n): self._set("mlmg_set_fixed_iter", int(n))
+    def setPreSmooth(self, n): self._set("mlmg_set_pre_smooth", int(n))
+    def setPostSmooth(self, n): self._set("mlmg_set_post_smooth", int(n))
+    def setFinalSmooth(self, n): self._set("mlmg_set_final_smooth", int(n))
+    def setBottomSmooth(self, n): self._set("mlmg_set_bottom_smooth", int(n))
+    def setBottomSolver(self, s): self._set("mlmg_set_bottom_solver", int(s))
+    def setBottomMaxIter(self, n): self._set("mlmg_set_bottom_max_iter", int(n))
+    def setBottomTolerance(self, t): self._set("mlmg_set_bottom_tolerance", float(t))
+    def setBottomToleranceAbs(self, t): self._set("mlmg_set_bottom_tolerance_abs", float(t))
+    def setAlwaysUseBNorm(self, f): self._set("mlmg_set_always_use_bnorm", int(f))
+    def setPrecision(self, mode): self._set("mlmg_set_precision", {"fp64": 0, "mixed": 1}.get(mode, mode))
+    def setGraph(self, on): self._set("mlmg_set_graph", int(bool(on)))
+    def setFusedSmoother(self, on): self._set("mlmg_set_fused_smoother", int(bool(on)))
+
+    def solve(self, sol, rhs, tol_rel, tol_abs):
+        """Returns the final residual max-norm; raises MLMGError unless the
+        solve converged (or ran its fixed iteration count)."""
+        sols = sol if isinstance(sol, (list, tuple)) else [sol]
+        rhss = rhs if isinstance(rhs, (list, tuple)) else [rhs]
+        r = ctypes.c_double()
+        rc = capi.lib().mlmg_solve(self._h, sols[0]._h, rhss[0]._h, float(tol_rel), float(tol_abs), ctypes.byref(r))
+        if rc != 0:
+            raise MLMGError(rc, capi.lib().mlmg_last_error().decode())
+        return r.value
+
+    def solve_status(self, sol, rhs, tol_rel, tol_abs):
+        r = ctypes.c_double()
+        rc = capi.lib().mlmg_solve(self._h, sol._h, rhs._h, float(tol_rel), float(tol_abs), ctypes.byref(r))
+        return rc, r.value
+
+    def apply(self, out, inp):
+        outs = out if isinstance(out, (list, tuple)) else [out]
+        ins = inp if isinstance(inp, (list, tuple)) else [inp]
+        check(capi.lib().mlmg_apply(self._h, outs[0]._h, ins[0]._h))
+
+    def getNumIters(self):
+        return capi.lib().mlmg_get_num_iters(self._h)
+
+    def getResidualHistory(self):
+        n = self.getNumIters()
+        a = (ctypes.c_double * max(n, 1))()
+        capi.lib().mlmg_get_residual_history(self._h, a, n)
+        return list(a[:n])
+
+    def getNumCGIters(self):
+        n = self.getNumIters()
+        a = (ctypes.c_int * max(n, 1))()
+        capi.lib().mlmg_get_num_cg_iters(self._h, a, n)
+        return list(a[:n])
+
+    def getInitResidual(self):
+        return capi.lib().mlmg_get_init_residual(self._h)
+
+    def getFinalResidual(self):
+        return capi.lib().mlmg_get_final_residual(self._h)
+
+    def getInitRHS(self):
+        return capi.lib().mlmg_get_init_rhs(self._h)
+
+    def solveTimeMs(self):
+        return capi.lib().mlmg_get_solve_time_ms(self._h)
+
+
+def solve_batched(solvers, sols, rhss, tol_rel, tol_abs):
+    """Independent solves run together (one launch per V-cycle stage).
+    Returns the per-solve statuses."""
+    n = len(solvers)
+    S = (ctypes.c_void_p * n)(*[s._h for s in solvers])
+    X = (ctypes.c_void_p * n)(*[m._h for m in sols])
+    B = (ctypes.c_void_p * n)(*[m._h for m in rhss])
+    st = (ctypes.c_int * n)()
+    rc = capi.lib().mlmg_solve_batched(n, S, X, B, float(tol_rel), float(tol_abs), st)
+    if rc < 0 and rc != -2 and all(v == 0 for v in st):
+        raise MLMGError(rc, capi.lib().mlmg_last_error().decode())
+    return list(st)
+
+
+def kernel_launches(reset=False):
+    return capi.lib().mlmg_kernel_launches(int(bool(reset)))

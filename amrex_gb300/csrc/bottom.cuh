@@ -1,0 +1,254 @@
+// Bottom solve: one thread block per solve runs the whole Jacobi-
+// preconditioned BiCGStab of MLCGSolverT::solve_bicgstab
+// (AMReX_MLCGSolver.H:96-273) and the follow-up smoothing of
+// MLMGT::actualBottomSolve (AMReX_MLMG.H:1500-1610) on the solve's coarsest
+// level, with FP64 arithmetic, dot products and norms, and no host round
+// trip.  The coarsest level is tiny (2^3..8^3 cells for the benchmark
+// configurations), so one block is the right size.
+#pragma once
+
+#include "stage_kernels.cuh"
+
+namespace mlmg {
+
+constexpr int BOTTOM_THREADS = 512;
+
+struct BottomLevelPtrs {       // one level that is the bottom of some solve
+    DevLevel L;
+    const CopyTag* tags;
+    double *x, *b, *p, *r, *rh, *v, *t;    // FP64 work arrays (level layout)
+    const double *a, *bx, *by, *bz;        // FP64 coefficients
+    void* x_out;                           // working-precision cor of the level
+    const void* b_in;                      // working-precision res of the level
+};
+
+struct BottomJob {
+    int lev;                   // index into the BottomLevelPtrs table
+    int solve;
+    int p0, np;                // the solve's patches at that level
+    int t0, nt;                // the solve's ghost-copy tags at that level
+    int singular;
+    double volinv;
+};
+
+struct BottomParams {
+    int maxiter;
+    double eps_rel, eps_abs;
+    int nub, nuf;
+    int smoother_only;         // bottom_solver == smoother
+};
+
+namespace bottom_detail {
+
+// flat loop over the valid cells of patches [p0, p0+np)
+template <typename F>
+__device__ __forceinline__ void for_cells (const DevLevel& L, int p0, int np, F&& f)
+{
+    for (int p = p0; p < p0 + np; ++p) {
+        const PatchDesc& P = L.P[p];
+        const int nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1, nz = P.hi[2] - P.lo[2] + 1;
+        const long long n = (long long)nx * ny * nz;
+        for (long long u = threadIdx.x; u < n; u += blockDim.x) {
+            const int i = P.lo[0] + (int)(u % nx);
+            const int j = P.lo[1] + (int)((u / nx) % ny);
+            const int k = P.lo[2] + (int)(u / ((long long)nx * ny));
+            f(P, i, j, k, cidx(P, i, j, k));
+        }
+    }
+}
+
+__device__ void ghost_fill (const BottomLevelPtrs& B, const BottomJob& J, double* phi)
+{
+    __syncthreads();
+    for (int p = J.p0; p < J.p0 + J.np; ++p) {
+        const PatchDesc& P = B.L.P[p];
+        for (int f = 0; f < 6; ++f) {
+            const int d = f % 3;
+            const int e0 = (d == 0) ? 1 : 0, e1 = (d == 2) ? 1 : 2;
+            const long long n = (long long)(P.hi[e0] - P.lo[e0] + 1) * (P.hi[e1] - P.lo[e1] + 1);
+            for (long long u = threadIdx.x; u < n; u += blockDim.x) {
+                int i, j, k;
+                face_cell(P, f, u, i, j, k);
+                if (face_mask(B.L, P, f, i, j, k) > 0) {
+                    const long long stride = (d == 0) ? 1 : ((d == 1) ? (long long)P.sx : P.sxy);
+                    bc_ghost<double>(P, f, cidx(P, i, j, k), (f >= 3) ? -stride : stride, phi, 0, nullptr, u);
+                }
+            }
+        }
+    }
+    for (int w = J.t0; w < J.t0 + J.nt; ++w) {
+        const CopyTag& C = B.tags[w];
+        const int nx = C.box.hi[0] - C.box.lo[0] + 1, ny = C.box.hi[1] - C.box.lo[1] + 1;
+        const long long n = (long long)nx * ny * (C.box.hi[2] - C.box.lo[2] + 1);
+        for (long long u = threadIdx.x; u < n; u += blockDim.x) {
+            const int i = C.box.lo[0] + (int)(u % nx);
+            const int j = C.box.lo[1] + (int)((u / nx) % ny);
+            const int k = C.box.lo[2] + (int)(u / ((long long)nx * ny));
+            phi[cidx(B.L.P[C.dst], i, j, k)] =
+                phi[cidx(B.L.P[C.src], i - C.shift[0], j - C.shift[1], k - C.shift[2])];
+        }
+    }
+    __syncthreads();
+}
+
+template <bool ABEC>
+__device__ void apply_normalize (const BottomLevelPtrs& B, const BottomJob& J, double* out, double* in)
+{
+    ghost_fill(B, J, in);
+    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc& P, int, int, int, long long q) {
+        double v = adotx_cell<double, ABEC>(P, q, in, B.a, B.bx, B.by, B.bz);
+        if constexpr (ABEC) { v /= abec_diag<double>(P, q, B.a, B.bx, B.by, B.bz); }
+        out[q] = v;
+    });
+    __syncthreads();
+}
+
+__device__ double reduce (const BottomLevelPtrs& B, const BottomJob& J, const double* x, const double* y, int op)
+{
+    __shared__ double sm[32];
+    __shared__ double result;
+    double acc = 0.0;
+    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
+        if (op == RED_MAXABS) { acc = fmax(acc, fabs(x[q])); }
+        else if (op == RED_DOT) { acc += x[q] * y[q]; }
+        else { acc += x[q]; }
+    });
+    const double r = block_reduce(acc, op, sm);
+    if (threadIdx.x == 0) { result = r; }
+    __syncthreads();
+    const double out = result;
+    __syncthreads();
+    return out;
+}
+
+template <bool ABEC>
+__device__ void smooth (const BottomLevelPtrs& B, const BottomJob& J, double* x, const double* b)
+{
+    for (int rb = 0; rb < 2; ++rb) {
+        ghost_fill(B, J, x);
+        for_cells(B.L, J.p0, J.np, [&] (const PatchDesc& P, int i, int j, int k, long long) {
+            if (((i + j + k + rb) & 1) == 0) {
+                gsrb_cell<double, ABEC>(B.L, P, i, j, k, x, b, B.a, B.bx, B.by, B.bz);
+            }
+        });
+        __syncthreads();
+    }
+}
+
+} // namespace bottom_detail
+
+template <typename T, bool ABEC>
+__global__ void __launch_bounds__(BOTTOM_THREADS)
+k_bottom (const BottomLevelPtrs* __restrict__ levels, const BottomJob* __restrict__ jobs, BottomParams prm,
+          const int* __restrict__ active, int* __restrict__ out_iters, int* __restrict__ out_ret)
+{
+    using namespace bottom_detail;
+    const BottomJob J = jobs[blockIdx.x];
+    if (active != nullptr && !active[J.solve]) { return; }
+    const BottomLevelPtrs& B = levels[J.lev];
+    double *x = B.x, *b = B.b, *p = B.p, *r = B.r, *rh = B.rh, *v = B.v, *t = B.t;
+    const T* bin = static_cast<const T*>(B.b_in);
+    T* xout = static_cast<T*>(B.x_out);
+
+    // x = 0 (ghosts included), b = res (valid)
+    for (int pp = J.p0; pp < J.p0 + J.np; ++pp) {
+        const PatchDesc& P = B.L.P[pp];
+        const long long n0 = P.base - P.sxy - P.sx - 1;
+        const long long n = P.sxy * (P.hi[2] - P.lo[2] + 3);
+        for (long long u = threadIdx.x; u < n; u += blockDim.x) {
+            x[n0 + u] = 0.0; p[n0 + u] = 0.0; r[n0 + u] = 0.0;
+        }
+    }
+    __syncthreads();
+    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { b[q] = (double)bin[q]; });
+    __syncthreads();
+
+    int ret = 0, iter = 0;
+    if (prm.smoother_only) {
+        for (int i = 0; i < prm.nuf; ++i) { smooth<ABEC>(B, J, x, b); }
+    } else {
+        // the solve's b, made solvable for a singular operator (a private copy)
+        const double* bb = b;
+        if (J.singular) {
+            const double off = reduce(B, J, b, nullptr, RED_SUM) * J.volinv;
+            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { t[q] = b[q] + (-off); });
+            __syncthreads();
+            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { rh[q] = t[q]; });
+            __syncthreads();
+            bb = rh;   // rh is reloaded below from r, so borrow it to hold b'
+        }
+        // r = b ; normalize ; rh = r
+        for_cells(B.L, J.p0, J.np, [&] (const PatchDesc& P, int, int, int, long long q) {
+            double val = bb[q];
+            if constexpr (ABEC) { val /= abec_diag<double>(P, q, B.a, B.bx, B.by, B.bz); }
+            r[q] = val;
+        });
+        __syncthreads();
+        for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { rh[q] = r[q]; });
+        __syncthreads();
+        double rnorm = reduce(B, J, r, nullptr, RED_MAXABS);
+        const double rnorm0 = rnorm;
+        double rho_1 = 0, alpha = 0, omega = 0;
+        iter = 1;
+        if (!(rnorm0 == 0 || rnorm0 < prm.eps_abs)) {
+            for (; iter <= prm.maxiter; ++iter) {
+                const double rho = reduce(B, J, rh, r, RED_DOT);
+                if (rho == 0) { ret = 1; break; }
+                if (iter == 1) {
+                    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { p[q] = r[q]; });
+                } else {
+                    const double beta = (rho / rho_1) * (alpha / omega);
+                    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
+                        double pv = p[q] + (-omega) * v[q];   // Saxpy
+                        p[q] = r[q] + beta * pv;              // Xpay
+                    });
+                }
+                __syncthreads();
+                apply_normalize<ABEC>(B, J, v, p);
+                const double rhTv = reduce(B, J, rh, v, RED_DOT);
+                if (rhTv != 0.0) { alpha = rho / rhTv; } else { ret = 2; break; }
+                for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
+                    x[q] += alpha * p[q];
+                    r[q] += (-alpha) * v[q];
+                });
+                __syncthreads();
+                rnorm = reduce(B, J, r, nullptr, RED_MAXABS);
+                if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
+                apply_normalize<ABEC>(B, J, t, r);
+                const double tt = reduce(B, J, t, t, RED_DOT);
+                const double tr = reduce(B, J, t, r, RED_DOT);
+                if (tt != 0.0) { omega = tr / tt; } else { ret = 3; break; }
+                for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
+                    x[q] += omega * r[q];
+                    r[q] += (-omega) * t[q];
+                });
+                __syncthreads();
+                rnorm = reduce(B, J, r, nullptr, RED_MAXABS);
+                if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
+                if (omega == 0) { ret = 4; break; }
+                rho_1 = rho;
+            }
+            if (ret == 0 && rnorm > prm.eps_rel * rnorm0 && rnorm > prm.eps_abs) { ret = 8; }
+            if ((ret == 0 || ret == 8) && (rnorm < rnorm0)) {
+                if (ret == 8) { ret = 9; }
+            } else {
+                for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { x[q] = 0.0; });
+                __syncthreads();
+            }
+        }
+        if (ret != 0 && ret != 9) {
+            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { x[q] = 0.0; });
+            __syncthreads();
+        }
+        const int n = (ret == 0) ? prm.nub : prm.nuf;
+        for (int i = 0; i < n; ++i) { smooth<ABEC>(B, J, x, b); }
+    }
+    __syncthreads();
+    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { xout[q] = T(x[q]); });
+    if (threadIdx.x == 0) {
+        out_iters[J.solve] = iter;
+        out_ret[J.solve] = ret;
+    }
+}
+
+} // namespace mlmg

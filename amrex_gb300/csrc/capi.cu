@@ -1,0 +1,937 @@
+// C ABI of the GB300 MLMG library (declared in include/mlmg_capi.h).
+#include "../../include/mlmg_capi.h"
+#include "solver.hpp"
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+
+using namespace mlmg;
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<long long> g_launches{0};
+cudaStream_t g_stream = nullptr;
+std::mutex g_mutex;
+
+cudaStream_t lib_stream ()
+{
+    std::lock_guard<std::mutex> lk(g_mutex);
+    if (g_stream == nullptr) {
+        MLMG_CUDA_CHECK(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+    }
+    return g_stream;
+}
+
+int fail (int code, const std::string& msg) { g_err = msg; return code; }
+
+#define API_BEGIN try {
+#define API_END                                                        \
+    } catch (const ::mlmg::Error& e) { return fail(e.code, e.what()); }  \
+    catch (const std::exception& e) { return fail(ERR_INTERNAL, e.what()); } \
+    return OK;
+
+// --------------------------------------------------------- user MultiFab ---
+struct FabInfo {          // device description of one FAB
+    long long off;
+    int lo[3];            // lower corner of the grown (nodal-extended) box
+    int hi[3];
+    int sx;
+    long long sxy;
+};
+
+struct FabTag {           // copy `box` of FAB dst from FAB src at (index - shift)
+    int dst, src;
+    int shift[3];
+    Box3 box;
+};
+
+template <typename T>
+__global__ void k_fab_tags (const FabInfo* __restrict__ fi, const FabTag* __restrict__ tags,
+                            const long long* __restrict__ start, int ntag, long long n, T* __restrict__ data)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) { return; }
+    int lo = 0, hi = ntag - 1;
+    while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (start[mid] <= t) { lo = mid; } else { hi = mid - 1; } }
+    const FabTag& C = tags[lo];
+    const long long u = t - start[lo];
+    const int nx = C.box.hi[0] - C.box.lo[0] + 1, ny = C.box.hi[1] - C.box.lo[1] + 1;
+    const int i = C.box.lo[0] + (int)(u % nx);
+    const int j = C.box.lo[1] + (int)((u / nx) % ny);
+    const int k = C.box.lo[2] + (int)(u / ((long long)nx * ny));
+    const FabInfo& D = fi[C.dst];
+    const FabInfo& S = fi[C.src];
+    const int si = i - C.shift[0], sj = j - C.shift[1], sk = k - C.shift[2];
+    data[D.off + (long long)(k - D.lo[2]) * D.sxy + (long long)(j - D.lo[1]) * D.sx + (i - D.lo[0])] =
+        data[S.off + (long long)(sk - S.lo[2]) * S.sxy + (long long)(sj - S.lo[1]) * S.sx + (si - S.lo[0])];
+}
+
+// global array <-> FAB cells.  dir 0: global -> FAB (cells of the grown box
+// inside the global array); dir 1: FAB valid cells -> global
+template <typename T>
+__global__ void k_fab_global (const FabInfo* __restrict__ fi, const Box3* __restrict__ regions,
+                              const long long* __restrict__ start, int nbox, long long n, T* __restrict__ data,
+                              T* __restrict__ glob, int g0, int g1, int g2, int gnx, int gny, int dir)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) { return; }
+    int lo = 0, hi = nbox - 1;
+    while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (start[mid] <= t) { lo = mid; } else { hi = mid - 1; } }
+    const Box3& R = regions[lo];
+    const FabInfo& F = fi[lo];
+    const long long u = t - start[lo];
+    const int nx = R.hi[0] - R.lo[0] + 1, ny = R.hi[1] - R.lo[1] + 1;
+    const int i = R.lo[0] + (int)(u % nx);
+    const int j = R.lo[1] + (int)((u / nx) % ny);
+    const int k = R.lo[2] + (int)(u / ((long long)nx * ny));
+    const long long qf = F.off + (long long)(k - F.lo[2]) * F.sxy + (long long)(j - F.lo[1]) * F.sx + (i - F.lo[0]);
+    const long long qg = ((long long)(k - g2) * gny + (j - g1)) * gnx + (i - g0);
+    if (dir == 0) { data[qf] = glob[qg]; } else { glob[qg] = data[qf]; }
+}
+
+template <typename T>
+__global__ void k_fab_maxabs (const FabInfo* __restrict__ fi, const Box3* __restrict__ regions,
+                              const long long* __restrict__ start, int nbox, long long n, const T* __restrict__ data,
+                              unsigned long long* __restrict__ out)
+{
+    double m = 0.0;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nbox - 1;
+        while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (start[mid] <= t) { lo = mid; } else { hi = mid - 1; } }
+        const Box3& R = regions[lo];
+        const FabInfo& F = fi[lo];
+        const long long u = t - start[lo];
+        const int nx = R.hi[0] - R.lo[0] + 1, ny = R.hi[1] - R.lo[1] + 1;
+        const int i = R.lo[0] + (int)(u % nx);
+        const int j = R.lo[1] + (int)((u / nx) % ny);
+        const int k = R.lo[2] + (int)(u / ((long long)nx * ny));
+        m = fmax(m, fabs((double)data[F.off + (long long)(k - F.lo[2]) * F.sxy + (long long)(j - F.lo[1]) * F.sx + (i - F.lo[0])]));
+    }
+    for (int o = 16; o > 0; o >>= 1) { m = fmax(m, __shfl_down_sync(0xffffffffu, m, o)); }
+    // max of non-negative doubles == max of their bit patterns
+    if ((threadIdx.x & 31) == 0) { atomicMax(out, (unsigned long long)__double_as_longlong(m)); }
+}
+
+template <typename T>
+__global__ void k_fill (long long n, T* __restrict__ p, T v)
+{
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        p[q] = v;
+    }
+}
+
+unsigned grid_for (long long n, int threads) { return (unsigned)std::max<long long>(1, (n + threads - 1) / threads); }
+
+} // namespace
+
+struct mlmg_boxarray_s { std::vector<Box3> boxes; };
+struct mlmg_distromap_s { int nbox; };
+struct mlmg_geometry_s { GeomC g; };
+
+struct mlmg_multifab_s {
+    std::vector<Box3> boxes;
+    int ncomp = 1, ngrow = 0, nodal_dir = -1, prec = 8;
+    std::vector<long long> off;
+    std::vector<FabInfo> info;
+    long long total = 0;
+    DevBuf<char> data;
+    DevBuf<FabInfo> dinfo;
+    Box3 fab_box (int b) const {
+        Box3 f = grow(boxes[b], ngrow);
+        if (nodal_dir >= 0) { f.hi[nodal_dir] += 1; }
+        return f;
+    }
+    FabSet fabset () const {
+        FabSet fs;
+        fs.data = data.p; fs.prec = prec; fs.ngrow = ngrow; fs.nodal_dir = nodal_dir;
+        fs.boxes = boxes; fs.off = off;
+        return fs;
+    }
+};
+
+namespace {
+
+template <typename T>
+void fab_run_tags (mlmg_multifab_s& mf, const std::vector<FabTag>& tags)
+{
+    if (tags.empty()) { return; }
+    std::vector<long long> start{0};
+    for (const auto& t : tags) { start.push_back(start.back() + t.box.npts()); }
+    DevBuf<FabTag> dt; DevBuf<long long> ds;
+    cudaStream_t st = lib_stream();
+    dt.upload(tags, st);
+    ds.upload(start, st);
+    k_fab_tags<T><<<grid_for(start.back(), 256), 256, 0, st>>>(mf.dinfo.p, dt.p, ds.p, (int)tags.size(), start.back(),
+                                                              (T*)mf.data.p);
+    g_launches++;
+    MLMG_CUDA_CHECK(cudaGetLastError());
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+}
+
+// FillBoundary tags: every ghost cell of every FAB covered by the valid
+// region of a box (periodic images included).  On one rank the reference's
+// local copies are not trimmed to the cross stencil
+// (Src/Base/AMReX_FabArrayBase.cpp:745-790 vs the trimming of the MPI tags at
+// :814-870), so edge and corner ghosts are filled whatever `cross` is.
+std::vector<FabTag> fill_boundary_tags (const mlmg_multifab_s& mf, const GeomC& geom)
+{
+    std::vector<FabTag> tags;
+    const int nb = (int)mf.boxes.size();
+    std::vector<int> shifts;
+    for (int sz = -1; sz <= 1; ++sz) for (int sy = -1; sy <= 1; ++sy) for (int sx = -1; sx <= 1; ++sx) {
+        const int sv[3] = {sx, sy, sz};
+        bool ok = true;
+        for (int d = 0; d < 3; ++d) { if (sv[d] != 0 && !geom.periodic[d]) { ok = false; } }
+        if (ok) { for (int d = 0; d < 3; ++d) { shifts.push_back(sv[d] * geom.domain.len(d)); } }
+    }
+    for (int b = 0; b < nb; ++b) {
+        const Box3 vb = mf.boxes[b];
+        Box3 vbn = vb;
+        if (mf.nodal_dir >= 0) { vbn.hi[mf.nodal_dir] += 1; }
+        const Box3 gb = mf.fab_box(b);
+        // shell of the grown box minus the valid box: z slabs (full x,y), then
+        // y slabs (full x, valid z), then x slabs (valid y, z)
+        std::vector<Box3> shell;
+        for (int d = 2; d >= 0; --d) {
+            for (int side = 0; side < 2; ++side) {
+                Box3 s = gb;
+                for (int e = 0; e < d; ++e) { (void)e; }
+                for (int e = d + 1; e < 3; ++e) { s.lo[e] = vbn.lo[e]; s.hi[e] = vbn.hi[e]; }
+                if (side == 0) { s.hi[d] = vbn.lo[d] - 1; } else { s.lo[d] = vbn.hi[d] + 1; }
+                if (s.ok()) { shell.push_back(s); }
+            }
+        }
+        for (const Box3& s : shell) {
+            for (size_t q = 0; q < shifts.size(); q += 3) {
+                const int sh[3] = {shifts[q], shifts[q + 1], shifts[q + 2]};
+                for (int src = 0; src < nb; ++src) {
+                    Box3 sv = mf.boxes[src];
+                    if (mf.nodal_dir >= 0) { sv.hi[mf.nodal_dir] += 1; }
+                    const Box3 isect = intersect(s, shift(sv, sh));
+                    if (!isect.ok()) { continue; }
+                    FabTag t;
+                    t.dst = b; t.src = src;
+                    for (int d = 0; d < 3; ++d) { t.shift[d] = sh[d]; }
+                    t.box = isect;
+                    tags.push_back(t);
+                }
+            }
+        }
+    }
+    return tags;
+}
+
+template <typename T>
+void fab_global (mlmg_multifab_s& mf, void* host, const int glo[3], const int gn[3], int dir)
+{
+    cudaStream_t st = lib_stream();
+    const Box3 gbox{{glo[0], glo[1], glo[2]}, {glo[0] + gn[0] - 1, glo[1] + gn[1] - 1, glo[2] + gn[2] - 1}};
+    std::vector<Box3> regions;
+    std::vector<long long> start{0};
+    for (int b = 0; b < (int)mf.boxes.size(); ++b) {
+        Box3 r;
+        if (dir == 0) {
+            r = intersect(mf.fab_box(b), gbox);
+        } else {
+            Box3 v = mf.boxes[b];
+            if (mf.nodal_dir >= 0) { v.hi[mf.nodal_dir] += 1; }
+            r = intersect(v, gbox);
+        }
+        if (!r.ok()) { r = Box3{{0, 0, 0}, {-1, -1, -1}}; }
+        regions.push_back(r);
+        start.push_back(start.back() + (r.ok() ? r.npts() : 0));
+    }
+    const long long ng = (long long)gn[0] * gn[1] * gn[2];
+    DevBuf<T> stage(ng);
+    DevBuf<Box3> dr; DevBuf<long long> ds;
+    dr.upload(regions, st);
+    ds.upload(start, st);
+    if (dir == 0) { MLMG_CUDA_CHECK(cudaMemcpyAsync(stage.p, host, ng * sizeof(T), cudaMemcpyHostToDevice, st)); }
+    if (start.back() > 0) {
+        k_fab_global<T><<<grid_for(start.back(), 256), 256, 0, st>>>(mf.dinfo.p, dr.p, ds.p, (int)regions.size(),
+            start.back(), (T*)mf.data.p, stage.p, glo[0], glo[1], glo[2], gn[0], gn[1], dir);
+        g_launches++;
+    }
+    if (dir == 1) { MLMG_CUDA_CHECK(cudaMemcpyAsync(host, stage.p, ng * sizeof(T), cudaMemcpyDeviceToHost, st)); }
+    MLMG_CUDA_CHECK(cudaGetLastError());
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+}
+
+} // namespace
+
+// --------------------------------------------------------------- linop ----
+struct mlmg_linop_s {
+    int is_abec = 0;
+    GeomC geom;
+    std::vector<Box3> boxes;
+    LPInfoC info;
+    int lobc[3] = {BC_DIRICHLET, BC_DIRICHLET, BC_DIRICHLET};
+    int hibc[3] = {BC_DIRICHLET, BC_DIRICHLET, BC_DIRICHLET};
+    int maxorder = 3;
+    double alpha = std::nan(""), beta = std::nan("");
+    std::unique_ptr<mlmg_multifab_s> acoef, bcoef[3], levelbc;
+    FabSet acoef_fs, bcoef_fs[3], levelbc_fs;
+    int struct_version = 0, coef_version = 0;
+    std::vector<LevelGrids> levels;
+    void regrid () { levels = define_grids(geom, boxes, info); ++struct_version; }
+};
+
+struct mlmg_solver_s {
+    mlmg_linop op = nullptr;
+    EngineOptions opt;
+    std::unique_ptr<Engine> eng;
+    int eng_struct = -1, eng_coef = -1, eng_prec = -1, eng_merge = -1;
+    SolveReport last;
+    double last_ms = 0;
+    // batch engine cached on the first solver of a batch
+    std::unique_ptr<Engine> batch_eng;
+    std::vector<mlmg_linop> batch_ops;
+    std::vector<int> batch_struct, batch_coef;
+    int batch_prec = -1;
+};
+
+namespace {
+
+std::unique_ptr<mlmg_multifab_s> new_mf (const std::vector<Box3>& boxes, int ncomp, int ngrow, int nodal_dir, int prec)
+{
+    MLMG_REQUIRE(prec == 8 || prec == 4, ERR_ARGS, "precision must be 8 or 4 bytes");
+    MLMG_REQUIRE(ncomp >= 1 && ngrow >= 0 && nodal_dir >= -1 && nodal_dir <= 2, ERR_ARGS, "bad MultiFab shape");
+    auto mf = std::make_unique<mlmg_multifab_s>();
+    mf->boxes = boxes; mf->ncomp = ncomp; mf->ngrow = ngrow; mf->nodal_dir = nodal_dir; mf->prec = prec;
+    long long off = 0;
+    for (int b = 0; b < (int)boxes.size(); ++b) {
+        const Box3 f = mf->fab_box(b);
+        FabInfo fi{};
+        fi.off = off;
+        for (int d = 0; d < 3; ++d) { fi.lo[d] = f.lo[d]; fi.hi[d] = f.hi[d]; }
+        fi.sx = f.len(0);
+        fi.sxy = (long long)f.len(0) * f.len(1);
+        mf->info.push_back(fi);
+        mf->off.push_back(off);
+        off += f.npts() * ncomp;
+    }
+    mf->total = off;
+    mf->data.alloc((size_t)std::max<long long>(off, 1) * prec);
+    cudaStream_t st = lib_stream();
+    MLMG_CUDA_CHECK(cudaMemsetAsync(mf->data.p, 0, (size_t)std::max<long long>(off, 1) * prec, st));
+    mf->dinfo.upload(mf->info, st);
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+    return mf;
+}
+
+std::unique_ptr<mlmg_multifab_s> clone_mf (const mlmg_multifab_s& src)
+{
+    auto mf = new_mf(src.boxes, src.ncomp, src.ngrow, src.nodal_dir, src.prec);
+    cudaStream_t st = lib_stream();
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(mf->data.p, src.data.p, (size_t)src.total * src.prec, cudaMemcpyDeviceToDevice, st));
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+    return mf;
+}
+
+SolveProblem make_problem (mlmg_linop op)
+{
+    SolveProblem pr;
+    SolveSpec& S = pr.spec;
+    S.geom = op->geom;
+    S.levels = op->levels;
+    for (int d = 0; d < 3; ++d) {
+        S.lobc[d] = op->lobc[d]; S.hibc[d] = op->hibc[d];
+        S.dx0[d] = (op->geom.prob_hi[d] - op->geom.prob_lo[d]) / (double)op->geom.domain.len(d);
+    }
+    S.maxorder = op->maxorder;
+    S.is_abec = op->is_abec;
+    if (op->is_abec) {
+        MLMG_REQUIRE(!std::isnan(op->alpha) && !std::isnan(op->beta), ERR_ARGS,
+                     "MLABecLaplacian: setScalars has not been called");
+        S.alpha = op->alpha; S.beta = op->beta;
+    } else {
+        S.alpha = 0.0; S.beta = 1.0;
+    }
+    pr.boxes = op->boxes;
+    if (op->acoef) { op->acoef_fs = op->acoef->fabset(); pr.acoef = &op->acoef_fs; }
+    for (int d = 0; d < 3; ++d) {
+        if (op->bcoef[d]) { op->bcoef_fs[d] = op->bcoef[d]->fabset(); pr.bcoef[d] = &op->bcoef_fs[d]; }
+    }
+    if (op->levelbc) { op->levelbc_fs = op->levelbc->fabset(); pr.levelbc = &op->levelbc_fs; }
+    return pr;
+}
+
+Engine& engine_for (mlmg_solver s)
+{
+    mlmg_linop op = s->op;
+    if (!s->eng || s->eng_struct != op->struct_version || s->eng_prec != s->opt.precision ||
+        s->eng_merge != s->opt.merge_boxes) {
+        s->eng.reset();
+        std::vector<SolveProblem> probs{make_problem(op)};
+        s->eng = std::make_unique<Engine>(std::move(probs), s->opt, lib_stream());
+        s->eng_struct = op->struct_version;
+        s->eng_coef = op->coef_version;
+        s->eng_prec = s->opt.precision;
+        s->eng_merge = s->opt.merge_boxes;
+    } else if (s->eng_coef != op->coef_version) {
+        make_problem(op);     // refresh the FabSets
+        s->eng->set_coefficients();
+        s->eng_coef = op->coef_version;
+    }
+    s->eng->options() = s->opt;
+    return *s->eng;
+}
+
+void count_launches (Engine& e) { g_launches += e.kernel_launches(); e.reset_launch_count(); }
+
+void check_solver_mf (mlmg_solver s, mlmg_multifab mf)
+{
+    MLMG_REQUIRE(s != nullptr && mf != nullptr, ERR_ARGS, "null handle");
+    MLMG_REQUIRE(mf->ncomp == 1, ERR_UNSUPPORTED, "only single-component MultiFabs are solved");
+    MLMG_REQUIRE(mf->nodal_dir == -1, ERR_ARGS, "solution and rhs must be cell-centred");
+    MLMG_REQUIRE(mf->prec == 8, ERR_UNSUPPORTED, "solution and rhs must be double precision");
+    MLMG_REQUIRE(mf->boxes == s->op->boxes, ERR_ARGS, "MultiFab BoxArray differs from the operator's");
+}
+
+} // namespace
+
+extern "C" {
+
+const char* mlmg_last_error (void) { return g_err.c_str(); }
+int mlmg_version (void) { return 10000; }
+void* mlmg_stream (void)
+{
+    try { return (void*)lib_stream(); } catch (...) { return nullptr; }
+}
+long long mlmg_kernel_launches (int reset)
+{
+    const long long v = g_launches.load();
+    if (reset) { g_launches = 0; }
+    return v;
+}
+
+// ------------------------------------------------------------- BoxArray --
+int mlmg_boxarray_new (const int* boxes, int nbox, mlmg_boxarray* out)
+{
+    API_BEGIN
+    MLMG_REQUIRE(out != nullptr && nbox >= 0 && (nbox == 0 || boxes != nullptr), ERR_ARGS, "bad arguments");
+    auto ba = std::make_unique<mlmg_boxarray_s>();
+    for (int b = 0; b < nbox; ++b) {
+        Box3 x;
+        for (int d = 0; d < 3; ++d) { x.lo[d] = boxes[6 * b + d]; x.hi[d] = boxes[6 * b + 3 + d]; }
+        MLMG_REQUIRE(x.ok(), ERR_ARGS, "empty box");
+        ba->boxes.push_back(x);
+    }
+    // boxes of a BoxArray must be disjoint
+    for (int b = 0; b < nbox; ++b) {
+        for (int c = b + 1; c < nbox; ++c) {
+            MLMG_REQUIRE(!intersect(ba->boxes[b], ba->boxes[c]).ok(), ERR_ARGS, "overlapping boxes in BoxArray");
+        }
+    }
+    *out = ba.release();
+    API_END
+}
+
+int mlmg_boxarray_new_domain (const int lo[3], const int hi[3], mlmg_boxarray* out)
+{
+    const int b[6] = {lo[0], lo[1], lo[2], hi[0], hi[1], hi[2]};
+    return mlmg_boxarray_new(b, 1, out);
+}
+
+int mlmg_boxarray_maxsize (mlmg_boxarray ba, const int chunk[3])
+{
+    API_BEGIN
+    MLMG_REQUIRE(ba != nullptr && chunk != nullptr && chunk[0] > 0 && chunk[1] > 0 && chunk[2] > 0, ERR_ARGS,
+                 "bad arguments");
+    ba->boxes = max_size(ba->boxes, chunk);
+    API_END
+}
+
+int mlmg_boxarray_size (mlmg_boxarray ba) { return ba ? (int)ba->boxes.size() : ERR_ARGS; }
+
+int mlmg_boxarray_get (mlmg_boxarray ba, int i, int lo[3], int hi[3])
+{
+    API_BEGIN
+    MLMG_REQUIRE(ba != nullptr && i >= 0 && i < (int)ba->boxes.size(), ERR_ARGS, "bad box index");
+    for (int d = 0; d < 3; ++d) { lo[d] = ba->boxes[i].lo[d]; hi[d] = ba->boxes[i].hi[d]; }
+    API_END
+}
+
+int mlmg_boxarray_delete (mlmg_boxarray ba) { delete ba; return OK; }
+
+int mlmg_distromap_new (mlmg_boxarray ba, mlmg_distromap* out)
+{
+    API_BEGIN
+    MLMG_REQUIRE(ba != nullptr && out != nullptr, ERR_ARGS, "null handle");
+    *out = new mlmg_distromap_s{(int)ba->boxes.size()};
+    API_END
+}
+
+int mlmg_distromap_delete (mlmg_distromap dm) { delete dm; return OK; }
+
+int mlmg_geometry_new (const int lo[3], const int hi[3], const double prob_lo[3], const double prob_hi[3],
+                       const int is_periodic[3], mlmg_geometry* out)
+{
+    API_BEGIN
+    MLMG_REQUIRE(out != nullptr && lo && hi && prob_lo && prob_hi, ERR_ARGS, "bad arguments");
+    auto g = std::make_unique<mlmg_geometry_s>();
+    for (int d = 0; d < 3; ++d) {
+        g->g.domain.lo[d] = lo[d]; g->g.domain.hi[d] = hi[d];
+        g->g.prob_lo[d] = prob_lo[d]; g->g.prob_hi[d] = prob_hi[d];
+        g->g.periodic[d] = is_periodic ? (is_periodic[d] != 0) : 0;
+        MLMG_REQUIRE(hi[d] >= lo[d] && prob_hi[d] > prob_lo[d], ERR_ARGS, "empty domain");
+    }
+    *out = g.release();
+    API_END
+}
+
+int mlmg_geometry_delete (mlmg_geometry g) { delete g; return OK; }
+
+// ------------------------------------------------------------- MultiFab --
+int mlmg_multifab_new (mlmg_boxarray ba, mlmg_distromap dm, int ncomp, int ngrow, int nodal_dir, int precision,
+                       mlmg_multifab* out)
+{
+    API_BEGIN
+    MLMG_REQUIRE(ba != nullptr && dm != nullptr && out != nullptr, ERR_ARGS, "null handle");
+    MLMG_REQUIRE(dm->nbox == (int)ba->boxes.size(), ERR_ARGS, "DistributionMapping does not match BoxArray");
+    *out = new_mf(ba->boxes, ncomp, ngrow, nodal_dir, precision).release();
+    API_END
+}
+
+int mlmg_multifab_delete (mlmg_multifab mf) { delete mf; return OK; }
+
+int mlmg_multifab_fab_size (mlmg_multifab mf, int box, size_t* nelem)
+{
+    API_BEGIN
+    MLMG_REQUIRE(mf && box >= 0 && box < (int)mf->boxes.size() && nelem, ERR_ARGS, "bad arguments");
+    *nelem = (size_t)(mf->fab_box(box).npts() * mf->ncomp);
+    API_END
+}
+
+int mlmg_multifab_fab_ptr (mlmg_multifab mf, int box, void** dptr)
+{
+    API_BEGIN
+    MLMG_REQUIRE(mf && box >= 0 && box < (int)mf->boxes.size() && dptr, ERR_ARGS, "bad arguments");
+    *dptr = mf->data.p + (size_t)mf->off[box] * mf->prec;
+    API_END
+}
+
+int mlmg_multifab_upload (mlmg_multifab mf, int box, const void* host)
+{
+    API_BEGIN
+    MLMG_REQUIRE(mf && box >= 0 && box < (int)mf->boxes.size() && host, ERR_ARGS, "bad arguments");
+    cudaStream_t st = lib_stream();
+    const size_t n = (size_t)(mf->fab_box(box).npts() * mf->ncomp) * mf->prec;
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(mf->data.p + (size_t)mf->off[box] * mf->prec, host, n, cudaMemcpyHostToDevice, st));
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+    API_END
+}
+
+int mlmg_multifab_download (mlmg_multifab mf, int box, void* host)
+{
+    API_BEGIN
+    MLMG_REQUIRE(mf && box >= 0 && box < (int)mf->boxes.size() && host, ERR_ARGS, "bad arguments");
+    cudaStream_t st = lib_stream();
+    const size_t n = (size_t)(mf->fab_box(box).npts() * mf->ncomp) * mf->prec;
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(host, mf->data.p + (size_t)mf->off[box] * mf->prec, n, cudaMemcpyDeviceToHost, st));
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+    API_END
+}
+
+int mlmg_multifab_upload_global (mlmg_multifab mf, const void* host, const int glo[3], const int gn[3])
+{
+    API_BEGIN
+    MLMG_REQUIRE(mf && host && glo && gn && mf->ncomp == 1, ERR_ARGS, "bad arguments");
+    if (mf->prec == 8) { fab_global<double>(*mf, const_cast<void*>(host), glo, gn, 0); }
+    else { fab_global<float>(*mf, const_cast<void*>(host), glo, gn, 0); }
+    API_END
+}
+
+int mlmg_multifab_download_global (mlmg_multifab mf, void* host, const int glo[3], const int gn[3])
+{
+    API_BEGIN
+    MLMG_REQUIRE(mf && host && glo && gn && mf->ncomp == 1, ERR_ARGS, "bad arguments");
+    if (mf->prec == 8) { fab_global<double>(*mf, host, glo, gn, 1); }
+    else { fab_global<float>(*mf, host, glo, gn, 1); }
+    API_END
+}
+
+int mlmg_multifab_setval (mlmg_multifab mf, double v)
+{
+    API_BEGIN
+    MLMG_REQUIRE(mf != nullptr, ERR_ARGS, "null handle");
+    cudaStream_t st = lib_stream();
+    const long long n = mf->total;
+    const unsigned nb = (unsigned)std::min<long long>(grid_for(n, 256), 152 * 32);
+    if (mf->prec == 8) { k_fill<double><<<nb, 256, 0, st>>>(n, (double*)mf->data.p, v); }
+    else { k_fill<float><<<nb, 256, 0, st>>>(n, (float*)mf->data.p, (float)v); }
+    g_launches++;
+    MLMG_CUDA_CHECK(cudaGetLastError());
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+    API_END
+}
+
+int mlmg_multifab_fill_boundary (mlmg_multifab mf, mlmg_geometry geom, int cross)
+{
+    API_BEGIN
+    (void)cross;
+    MLMG_REQUIRE(mf != nullptr && geom != nullptr, ERR_ARGS, "null handle");
+    MLMG_REQUIRE(mf->ncomp == 1, ERR_UNSUPPORTED, "FillBoundary of multi-component MultiFabs");
+    if (mf->ngrow == 0) { return OK; }
+    const auto tags = fill_boundary_tags(*mf, geom->g);
+    if (mf->prec == 8) { fab_run_tags<double>(*mf, tags); } else { fab_run_tags<float>(*mf, tags); }
+    API_END
+}
+
+int mlmg_multifab_norminf (mlmg_multifab mf, double* out)
+{
+    API_BEGIN
+    MLMG_REQUIRE(mf != nullptr && out != nullptr, ERR_ARGS, "bad arguments");
+    cudaStream_t st = lib_stream();
+    std::vector<Box3> regions;
+    std::vector<long long> start{0};
+    for (int b = 0; b < (int)mf->boxes.size(); ++b) {
+        Box3 v = mf->boxes[b];
+        if (mf->nodal_dir >= 0) { v.hi[mf->nodal_dir] += 1; }
+        regions.push_back(v);
+        start.push_back(start.back() + v.npts());
+    }
+    DevBuf<Box3> dr; DevBuf<long long> ds; DevBuf<unsigned long long> dm(1);
+    dr.upload(regions, st);
+    ds.upload(start, st);
+    dm.zero(st);
+    const unsigned nb = (unsigned)std::min<long long>(grid_for(start.back(), 256), 152 * 8);
+    if (mf->prec == 8) {
+        k_fab_maxabs<double><<<nb, 256, 0, st>>>(mf->dinfo.p, dr.p, ds.p, (int)regions.size(), start.back(),
+                                                 (const double*)mf->data.p, dm.p);
+    } else {
+        k_fab_maxabs<float><<<nb, 256, 0, st>>>(mf->dinfo.p, dr.p, ds.p, (int)regions.size(), start.back(),
+                                                (const float*)mf->data.p, dm.p);
+    }
+    g_launches++;
+    unsigned long long bits = 0;
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(&bits, dm.p, sizeof(bits), cudaMemcpyDeviceToHost, st));
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+    double v;
+    std::memcpy(&v, &bits, sizeof(v));
+    *out = v;
+    API_END
+}
+
+// --------------------------------------------------------------- linop ----
+static int linop_new (int is_abec, int nlev, const mlmg_geometry* geom, const mlmg_boxarray* ba,
+                      const mlmg_distromap* dm, const mlmg_lpinfo* info, mlmg_linop* out)
+{
+    API_BEGIN
+    MLMG_REQUIRE(out && geom && ba && dm && geom[0] && ba[0] && dm[0], ERR_ARGS, "null handle");
+    MLMG_REQUIRE(nlev == 1, ERR_UNSUPPORTED, "composite (multi-AMR-level) solves are not implemented");
+    auto op = std::make_unique<mlmg_linop_s>();
+    op->is_abec = is_abec;
+    op->geom = geom[0]->g;
+    op->boxes = ba[0]->boxes;
+    MLMG_REQUIRE(dm[0]->nbox == (int)op->boxes.size(), ERR_ARGS, "DistributionMapping does not match BoxArray");
+    for (const auto& b : op->boxes) {
+        for (int d = 0; d < 3; ++d) {
+            MLMG_REQUIRE(b.lo[d] >= op->geom.domain.lo[d] && b.hi[d] <= op->geom.domain.hi[d], ERR_ARGS,
+                         "box outside the domain");
+        }
+    }
+    if (info) {
+        op->info.agg = info->agglomeration;
+        op->info.con = info->consolidation;
+        op->info.agg_grid_size = info->agg_grid_size > 0 ? info->agg_grid_size : 32;
+        op->info.con_grid_size = info->con_grid_size > 0 ? info->con_grid_size : 32;
+        op->info.max_coarsening_level = info->max_coarsening_level >= 0 ? info->max_coarsening_level : 30;
+    }
+    for (int d = 0; d < 3; ++d) {
+        if (op->geom.periodic[d]) { op->lobc[d] = op->hibc[d] = BC_PERIODIC; }
+    }
+    op->regrid();
+    *out = op.release();
+    API_END
+}
+
+int mlmg_linop_new_poisson (int nlev, const mlmg_geometry* geom, const mlmg_boxarray* ba, const mlmg_distromap* dm,
+                            const mlmg_lpinfo* info, mlmg_linop* out)
+{
+    return linop_new(0, nlev, geom, ba, dm, info, out);
+}
+
+int mlmg_linop_new_abeclap (int nlev, const mlmg_geometry* geom, const mlmg_boxarray* ba, const mlmg_distromap* dm,
+                            const mlmg_lpinfo* info, mlmg_linop* out)
+{
+    return linop_new(1, nlev, geom, ba, dm, info, out);
+}
+
+int mlmg_linop_delete (mlmg_linop op) { delete op; return OK; }
+
+int mlmg_linop_set_domain_bc (mlmg_linop op, const int lobc[3], const int hibc[3])
+{
+    API_BEGIN
+    MLMG_REQUIRE(op && lobc && hibc, ERR_ARGS, "bad arguments");
+    for (int d = 0; d < 3; ++d) {
+        for (int v : {lobc[d], hibc[d]}) {
+            MLMG_REQUIRE(v == BC_DIRICHLET || v == BC_NEUMANN || v == BC_REFLECT_ODD || v == BC_PERIODIC,
+                         ERR_UNSUPPORTED, "BC type " + std::to_string(v) + " is not implemented");
+        }
+        MLMG_REQUIRE((lobc[d] == BC_PERIODIC) == (op->geom.periodic[d] != 0) &&
+                     (hibc[d] == BC_PERIODIC) == (op->geom.periodic[d] != 0), ERR_ARGS,
+                     "periodic BCs must match the Geometry's periodicity");
+        op->lobc[d] = lobc[d]; op->hibc[d] = hibc[d];
+    }
+    ++op->struct_version;
+    API_END
+}
+
+int mlmg_linop_set_level_bc (mlmg_linop op, int amrlev, mlmg_multifab levelbc)
+{
+    API_BEGIN
+    MLMG_REQUIRE(op && amrlev == 0, ERR_ARGS, "bad arguments");
+    if (levelbc == nullptr) { op->levelbc.reset(); }
+    else {
+        MLMG_REQUIRE(levelbc->ngrow >= 1 && levelbc->boxes == op->boxes && levelbc->nodal_dir == -1, ERR_ARGS,
+                     "level BC MultiFab must share the BoxArray and have a ghost cell");
+        op->levelbc = clone_mf(*levelbc);    // values are taken at this call (setPhysBndryValues)
+    }
+    ++op->coef_version;
+    API_END
+}
+
+int mlmg_linop_set_maxorder (mlmg_linop op, int maxorder)
+{
+    API_BEGIN
+    MLMG_REQUIRE(op && maxorder >= 1 && maxorder <= 4, ERR_ARGS, "maxorder must be in 1..4");
+    op->maxorder = maxorder;
+    ++op->struct_version;
+    API_END
+}
+
+int mlmg_abeclap_set_scalars (mlmg_linop op, double alpha, double beta)
+{
+    API_BEGIN
+    MLMG_REQUIRE(op && op->is_abec, ERR_ARGS, "not an ABecLaplacian");
+    op->alpha = alpha; op->beta = beta;
+    ++op->struct_version;      // scalars live in the patch descriptors
+    API_END
+}
+
+int mlmg_abeclap_set_acoeffs (mlmg_linop op, int amrlev, mlmg_multifab a)
+{
+    API_BEGIN
+    MLMG_REQUIRE(op && op->is_abec && amrlev == 0 && a, ERR_ARGS, "bad arguments");
+    MLMG_REQUIRE(a->boxes == op->boxes && a->nodal_dir == -1 && a->ncomp == 1, ERR_ARGS,
+                 "a must be a one-component cell-centred MultiFab on the operator's BoxArray");
+    op->acoef = clone_mf(*a);
+    ++op->coef_version;
+    API_END
+}
+
+int mlmg_abeclap_set_acoeffs_const (mlmg_linop op, int amrlev, double a)
+{
+    API_BEGIN
+    MLMG_REQUIRE(op && op->is_abec && amrlev == 0, ERR_ARGS, "bad arguments");
+    op->acoef = new_mf(op->boxes, 1, 0, -1, 8);
+    mlmg_multifab_setval(op->acoef.get(), a);
+    ++op->coef_version;
+    API_END
+}
+
+int mlmg_abeclap_set_bcoeffs (mlmg_linop op, int amrlev, const mlmg_multifab b[3])
+{
+    API_BEGIN
+    MLMG_REQUIRE(op && op->is_abec && amrlev == 0 && b && b[0] && b[1] && b[2], ERR_ARGS, "bad arguments");
+    for (int d = 0; d < 3; ++d) {
+        MLMG_REQUIRE(b[d]->boxes == op->boxes && b[d]->nodal_dir == d && b[d]->ncomp == 1, ERR_ARGS,
+                     "b[d] must be a one-component face MultiFab (nodal in d) on the operator's BoxArray");
+    }
+    for (int d = 0; d < 3; ++d) { op->bcoef[d] = clone_mf(*b[d]); }
+    ++op->coef_version;
+    API_END
+}
+
+int mlmg_abeclap_set_bcoeffs_const (mlmg_linop op, int amrlev, double b)
+{
+    API_BEGIN
+    MLMG_REQUIRE(op && op->is_abec && amrlev == 0, ERR_ARGS, "bad arguments");
+    for (int d = 0; d < 3; ++d) {
+        op->bcoef[d] = new_mf(op->boxes, 1, 0, d, 8);
+        mlmg_multifab_setval(op->bcoef[d].get(), b);
+    }
+    ++op->coef_version;
+    API_END
+}
+
+int mlmg_linop_num_mg_levels (mlmg_linop op) { return op ? (int)op->levels.size() : ERR_ARGS; }
+
+// --------------------------------------------------------------- solver ---
+int mlmg_new (mlmg_linop op, mlmg_solver* out)
+{
+    API_BEGIN
+    MLMG_REQUIRE(op && out, ERR_ARGS, "null handle");
+    auto s = std::make_unique<mlmg_solver_s>();
+    s->op = op;
+    *out = s.release();
+    API_END
+}
+
+int mlmg_delete (mlmg_solver s) { delete s; return OK; }
+
+#define SETTER(name, field, type, check)                      \
+    int name (mlmg_solver s, type v)                          \
+    {                                                         \
+        API_BEGIN                                             \
+        MLMG_REQUIRE(s != nullptr && (check), ERR_ARGS, "bad value for " #name); \
+        s->opt.field = v;                                     \
+        API_END                                               \
+    }
+
+SETTER(mlmg_set_verbose, verbose, int, true)
+SETTER(mlmg_set_max_iter, max_iter, int, v >= 1)
+SETTER(mlmg_set_fixed_iter, fixed_iter, int, v >= 0)
+SETTER(mlmg_set_pre_smooth, nu1, int, v >= 0)
+SETTER(mlmg_set_post_smooth, nu2, int, v >= 0)
+SETTER(mlmg_set_final_smooth, nuf, int, v >= 0)
+SETTER(mlmg_set_bottom_smooth, nub, int, v >= 0)
+SETTER(mlmg_set_bottom_max_iter, bottom_maxiter, int, v >= 1)
+SETTER(mlmg_set_bottom_tolerance, bottom_reltol, double, v > 0)
+SETTER(mlmg_set_bottom_tolerance_abs, bottom_abstol, double, true)
+SETTER(mlmg_set_always_use_bnorm, always_use_bnorm, int, true)
+SETTER(mlmg_set_precision, precision, int, v == 0 || v == 1)
+SETTER(mlmg_set_graph, use_graph, int, true)
+SETTER(mlmg_set_fused_smoother, fused_smoother, int, true)
+
+int mlmg_set_max_fmg_iter (mlmg_solver s, int n)
+{
+    API_BEGIN
+    MLMG_REQUIRE(s != nullptr, ERR_ARGS, "null handle");
+    MLMG_REQUIRE(n == 0, ERR_UNSUPPORTED, "F-cycles (max_fmg_iter > 0) are not implemented");
+    API_END
+}
+
+int mlmg_set_bottom_solver (mlmg_solver s, int which)
+{
+    API_BEGIN
+    MLMG_REQUIRE(s != nullptr, ERR_ARGS, "null handle");
+    MLMG_REQUIRE(which == 0 || which == 1 || which == 2, ERR_UNSUPPORTED,
+                 "bottom solver must be 0 (default), 1 (smoother) or 2 (bicgstab)");
+    s->opt.bottom_solver = (which == 0) ? 2 : which;
+    API_END
+}
+
+int mlmg_solve (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, double tol_rel, double tol_abs,
+                double* final_resid)
+{
+    API_BEGIN
+    check_solver_mf(s, sol);
+    check_solver_mf(s, rhs);
+    Engine& e = engine_for(s);
+    FabSet fs_sol = sol->fabset(), fs_rhs = rhs->fabset();
+    e.solve({&fs_sol}, {&fs_sol}, {&fs_rhs}, tol_rel, tol_abs);
+    count_launches(e);
+    s->last = e.reports()[0];
+    s->last_ms = e.last_solve_ms();
+    if (sol->ngrow >= 1) {
+        // ghost cells between boxes, as the reference's final FillBoundary leaves them
+        GeomC g = s->op->geom;
+        const auto tags = fill_boundary_tags(*sol, g);
+        fab_run_tags<double>(*sol, tags);
+    }
+    if (final_resid) { *final_resid = s->last.final_resid; }
+    if (s->last.status == NOT_CONVERGED) { g_err = "MLMG failed to converge"; }
+    if (s->last.status == ERR_DIVERGED) { g_err = "MLMG blew up"; }
+    if (s->last.status == ERR_NONFINITE) { g_err = "MLMG residual is not finite"; }
+    return s->last.status;
+    API_END
+}
+
+int mlmg_apply (mlmg_solver s, mlmg_multifab out, mlmg_multifab in)
+{
+    API_BEGIN
+    check_solver_mf(s, out);
+    check_solver_mf(s, in);
+    Engine& e = engine_for(s);
+    FabSet fi = in->fabset(), fo = out->fabset();
+    e.apply(fi, fo);
+    count_launches(e);
+    API_END
+}
+
+int mlmg_get_num_iters (mlmg_solver s) { return s ? s->last.niters : ERR_ARGS; }
+
+int mlmg_get_residual_history (mlmg_solver s, double* out, int max)
+{
+    if (!s || !out) { return ERR_ARGS; }
+    const int n = std::min(max, (int)s->last.history.size());
+    for (int i = 0; i < n; ++i) { out[i] = s->last.history[i]; }
+    return (int)s->last.history.size();
+}
+
+int mlmg_get_num_cg_iters (mlmg_solver s, int* out, int max)
+{
+    if (!s || !out) { return ERR_ARGS; }
+    const int n = std::min(max, (int)s->last.cg_iters.size());
+    for (int i = 0; i < n; ++i) { out[i] = s->last.cg_iters[i]; }
+    return (int)s->last.cg_iters.size();
+}
+
+double mlmg_get_init_residual (mlmg_solver s) { return s ? s->last.init_resid : -1.0; }
+double mlmg_get_final_residual (mlmg_solver s) { return s ? s->last.final_resid : -1.0; }
+double mlmg_get_init_rhs (mlmg_solver s) { return s ? s->last.rhs_norm : -1.0; }
+double mlmg_get_solve_time_ms (mlmg_solver s) { return s ? s->last_ms : -1.0; }
+int mlmg_get_num_mg_levels (mlmg_solver s) { return (s && s->op) ? (int)s->op->levels.size() : ERR_ARGS; }
+
+int mlmg_solve_batched (int n, const mlmg_solver* solvers, const mlmg_multifab* sols, const mlmg_multifab* rhss,
+                        double tol_rel, double tol_abs, int* status)
+{
+    API_BEGIN
+    MLMG_REQUIRE(n >= 1 && solvers && sols && rhss, ERR_ARGS, "bad arguments");
+    for (int i = 0; i < n; ++i) { check_solver_mf(solvers[i], sols[i]); check_solver_mf(solvers[i], rhss[i]); }
+    mlmg_solver s0 = solvers[0];
+    bool rebuild = !s0->batch_eng || (int)s0->batch_ops.size() != n || s0->batch_prec != s0->opt.precision;
+    if (!rebuild) {
+        for (int i = 0; i < n; ++i) {
+            if (s0->batch_ops[i] != solvers[i]->op || s0->batch_struct[i] != solvers[i]->op->struct_version ||
+                s0->batch_coef[i] != solvers[i]->op->coef_version) { rebuild = true; }
+        }
+    }
+    if (rebuild) {
+        s0->batch_eng.reset();
+        std::vector<SolveProblem> probs;
+        s0->batch_ops.clear(); s0->batch_struct.clear(); s0->batch_coef.clear();
+        for (int i = 0; i < n; ++i) {
+            probs.push_back(make_problem(solvers[i]->op));
+            s0->batch_ops.push_back(solvers[i]->op);
+            s0->batch_struct.push_back(solvers[i]->op->struct_version);
+            s0->batch_coef.push_back(solvers[i]->op->coef_version);
+        }
+        s0->batch_eng = std::make_unique<Engine>(std::move(probs), s0->opt, lib_stream());
+        s0->batch_prec = s0->opt.precision;
+    }
+    Engine& e = *s0->batch_eng;
+    e.options() = s0->opt;
+    std::vector<FabSet> fsol(n), frhs(n);
+    std::vector<const FabSet*> pin(n), prhs(n);
+    std::vector<FabSet*> pout(n);
+    for (int i = 0; i < n; ++i) {
+        fsol[i] = sols[i]->fabset(); frhs[i] = rhss[i]->fabset();
+        pin[i] = &fsol[i]; pout[i] = &fsol[i]; prhs[i] = &frhs[i];
+    }
+    e.solve(pin, pout, prhs, tol_rel, tol_abs);
+    count_launches(e);
+    int worst = OK;
+    for (int i = 0; i < n; ++i) {
+        solvers[i]->last = e.reports()[i];
+        solvers[i]->last_ms = e.last_solve_ms();
+        if (status) { status[i] = e.reports()[i].status; }
+        if (e.reports()[i].status != OK) { worst = (worst == OK || e.reports()[i].status < worst) ? e.reports()[i].status : worst; }
+        if (sols[i]->ngrow >= 1) {
+            const auto tags = fill_boundary_tags(*sols[i], solvers[i]->op->geom);
+            fab_run_tags<double>(*sols[i], tags);
+        }
+    }
+    return worst;
+    API_END
+}
+
+} // extern "C"

@@ -1,0 +1,89 @@
+// Host-side grid metadata: MG hierarchy, patch levels, masks, BC records and
+// ghost-copy tags.  No device code.
+#pragma once
+
+#include "common.hpp"
+
+#include <array>
+#include <memory>
+
+namespace mlmg {
+
+struct LPInfoC {
+    int agg = 1, con = 1;
+    int agg_grid_size = 32, con_grid_size = 32;   // the reference's GPU-build defaults
+    int max_coarsening_level = 30;
+};
+
+struct GeomC {
+    Box3 domain;
+    double prob_lo[3] = {0, 0, 0}, prob_hi[3] = {1, 1, 1};
+    int periodic[3] = {0, 0, 0};
+    void cell_size (double dx[3], double dxinv[3]) const {
+        for (int d = 0; d < 3; ++d) {
+            // Geometry cell size (Src/Base/AMReX_Geometry.H:406-407)
+            dx[d] = (prob_hi[d] - prob_lo[d]) / (double)domain.len(d);
+            dxinv[d] = 1.0 / dx[d];
+        }
+    }
+};
+
+struct LevelGrids {
+    GeomC geom;
+    std::vector<Box3> boxes;
+};
+
+// MLLinOpT::defineGrids for AMR level 0 (Src/LinearSolvers/MLMG/AMReX_MLLinOp.H:793-1165)
+std::vector<LevelGrids> define_grids (const GeomC& geom, const std::vector<Box3>& ba, const LPInfoC& info);
+
+// Description of one solve's operator, as seen by the patch builder.
+struct SolveSpec {
+    GeomC geom;                       // level-0 geometry
+    std::vector<LevelGrids> levels;   // MG levels
+    int lobc[3], hibc[3];             // domain BC types
+    int maxorder = 3;
+    double alpha = 0.0, beta = 1.0;
+    int is_abec = 0;
+    double dx0[3];                    // level-0 cell size (BC location of internal faces)
+};
+
+// Ghost-copy tag: copy region `box` (destination index space) of patch `dst`
+// from patch `src`, whose source index is destination index - shift.
+struct CopyTag {
+    int dst, src;
+    int shift[3];
+    Box3 box;
+};
+
+// One joint level of a batch: the patches of MG level `lev` of every solve
+// that has such a level.
+struct PatchLevel {
+    int lev = 0;
+    std::vector<PatchDesc> patches;
+    std::vector<int> patch_is_bottom;      // 1 if this level is the owning solve's bottom level
+    std::vector<int8_t> masks;             // per-cell masks of faces whose mask is not uniform
+    std::vector<CopyTag> tags;             // intra-level ghost copies (faces only)
+    long long nelem = 0;                   // elements per field
+    std::vector<int> solve_first_patch;    // first patch index of each solve at this level (-1 if absent)
+    std::vector<int> solve_npatch;
+};
+
+struct BoxToPatch {                        // level-0 user box -> patch location
+    int patch;
+};
+
+// Build the patch layout of level `lev` for every solve in `solves`.
+// Boxes of one solve's level are merged into one patch when their union is
+// their bounding box and the merge leaves every Dirichlet closure unchanged.
+PatchLevel build_patch_level (const std::vector<const SolveSpec*>& solves, int lev, bool allow_merge);
+
+// index of cell (i,j,k) of patch p
+inline long long pidx (const PatchDesc& p, int i, int j, int k)
+{
+    return p.base + (long long)(k - p.lo[2]) * p.sxy + (long long)(j - p.lo[1]) * p.sx + (i - p.lo[0]);
+}
+
+// poly_interp_coeff (Src/Boundary/AMReX_LOUtil_K.H:22-37)
+void poly_interp_coeff (double xInt, const double* x, int N, double* c);
+
+} // namespace mlmg

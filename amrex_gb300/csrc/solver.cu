@@ -1,0 +1,799 @@
+// The batched MLMG engine: host orchestration of the V-cycle stages.
+#include "solver.hpp"
+#include "bottom.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace mlmg {
+
+namespace {
+
+struct SubsetData {
+    DevBuf<int> plist, tstart, solve_begin;
+    std::vector<int> h_plist, h_tstart, h_solve_begin;
+    int n = 0, ntiles = 0;
+    Subset dev () const { return Subset{plist.p, tstart.p, n, ntiles}; }
+};
+
+int tiles_of (const PatchDesc& P)
+{
+    const int nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1, nz = P.hi[2] - P.lo[2] + 1;
+    return ((nx + TILE_X - 1) / TILE_X) * ((ny + TILE_Y - 1) / TILE_Y) * ((nz + TILE_Z - 1) / TILE_Z);
+}
+
+void build_subset (SubsetData& S, const PatchLevel& PL, const std::vector<int>& plist, int nsolve,
+                   cudaStream_t st)
+{
+    S.h_plist = plist;
+    S.n = (int)plist.size();
+    S.h_tstart.assign(S.n + 1, 0);
+    for (int q = 0; q < S.n; ++q) { S.h_tstart[q + 1] = S.h_tstart[q] + tiles_of(PL.patches[plist[q]]); }
+    S.ntiles = S.h_tstart[S.n];
+    S.h_solve_begin.assign(nsolve + 1, 0);
+    // tiles of solve s are [begin[s], begin[s+1]) (patches are grouped by solve)
+    int q = 0;
+    for (int s = 0; s < nsolve; ++s) {
+        S.h_solve_begin[s] = S.h_tstart[q];
+        while (q < S.n && PL.patches[plist[q]].solve == s) { ++q; }
+    }
+    S.h_solve_begin[nsolve] = S.ntiles;
+    if (S.n > 0) {
+        S.plist.upload(S.h_plist, st);
+        S.tstart.upload(S.h_tstart, st);
+    }
+    S.solve_begin.upload(S.h_solve_begin, st);
+}
+
+} // namespace
+
+struct LevelData {
+    PatchLevel meta;
+    DevBuf<PatchDesc> P;
+    DevBuf<int8_t> masks;
+    DevBuf<int> sfirst, snp;
+    DevBuf<CopyTag> tags;
+    DevBuf<int2> faces;
+    DevBuf<long long> fstart, tstart;
+    GhostWork gw{};
+    SubsetData all, mg;
+    DevLevel dl{};
+    // FP64 fields
+    DevBuf<double> cor, res, rescor, a, bx, by, bz;
+    DevBuf<double> sol, rhs, bcval;                 // level 0 only
+    // FP32 fields (mixed precision)
+    DevBuf<float> cor32, res32, rescor32, a32, bx32, by32, bz32;
+    // bottom work arrays
+    DevBuf<double> bw[7];
+    bool has_bottom = false;
+    std::vector<int> solve_tag_first, solve_tag_n;  // tags grouped per solve
+};
+
+struct Engine::Impl {
+    Engine& E;
+    int nsolve = 0;
+    int nlev_max = 0;
+    bool abec = false;
+    std::vector<LevelData> lev;
+    std::vector<int> singular;
+    std::vector<double> volinv0, volinv_bottom;
+    DevBuf<double> partial, red_out, volinv0_d;
+    DevBuf<int> active_d, bot_iters, bot_ret;
+    PinnedBuf<double> h_red;
+    PinnedBuf<int> h_iters;
+    DevBuf<BottomLevelPtrs> bot_levels;
+    DevBuf<BottomJob> bot_jobs;
+    int njobs = 0;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_key = -1;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    explicit Impl (Engine& e) : E(e) {}
+    ~Impl () {
+        if (graph_exec) { cudaGraphExecDestroy(graph_exec); }
+        if (ev0) { cudaEventDestroy(ev0); }
+        if (ev1) { cudaEventDestroy(ev1); }
+    }
+
+    cudaStream_t st () const { return E.m_stream; }
+    bool mixed () const { return E.m_opt.precision == 1; }
+    void launched (int n = 1) { E.m_launches += n; }
+
+    // ------------------------------------------------------------ setup --
+    void build ();
+    void build_bottom_tables ();
+    void load_level0_field (const FabSet* fs, double* field, double defval, int nodal_dir, int s);
+    void xfer (const std::vector<XferItem>& items, const FabSet& fs, void* field, bool field_is_f32, int dir);
+    std::vector<XferItem> items_for (const FabSet& fs, int s, int ghost_mode, int nodal_dir) const;
+
+    // ------------------------------------------------------- operations --
+    template <typename T> void ghost (int l, T* phi, bool inhomog, bool do_copy);
+    template <typename T> void smooth (int l, T* cor, const T* res, bool skip_fb);
+    template <typename T> void vcycle ();
+    template <typename T> T* field_cor (int l);
+    template <typename T> T* field_res (int l);
+    template <typename T> T* field_rescor (int l);
+    template <typename T> const T* coef (int l, int which);
+    void reduce_per_solve (int l, const SubsetData& S, int op, const double* x, const double* y);
+    void residual0 (bool to32);   // res[0] (FP64, or FP32 in mixed) and per-block max|r|
+    void one_iteration ();
+};
+
+// -------------------------------------------------------------- fields ----
+template <> double* Engine::Impl::field_cor<double> (int l) { return lev[l].cor.p; }
+template <> double* Engine::Impl::field_res<double> (int l) { return lev[l].res.p; }
+template <> double* Engine::Impl::field_rescor<double> (int l) { return lev[l].rescor.p; }
+template <> float* Engine::Impl::field_cor<float> (int l) { return lev[l].cor32.p; }
+template <> float* Engine::Impl::field_res<float> (int l) { return lev[l].res32.p; }
+template <> float* Engine::Impl::field_rescor<float> (int l) { return lev[l].rescor32.p; }
+template <> const double* Engine::Impl::coef<double> (int l, int w)
+{
+    const LevelData& L = lev[l];
+    return w == 0 ? L.a.p : (w == 1 ? L.bx.p : (w == 2 ? L.by.p : L.bz.p));
+}
+template <> const float* Engine::Impl::coef<float> (int l, int w)
+{
+    const LevelData& L = lev[l];
+    return w == 0 ? L.a32.p : (w == 1 ? L.bx32.p : (w == 2 ? L.by32.p : L.bz32.p));
+}
+
+// --------------------------------------------------------------- build ----
+void Engine::Impl::build ()
+{
+    nsolve = (int)E.m_problems.size();
+    MLMG_REQUIRE(nsolve > 0, ERR_ARGS, "empty batch");
+    abec = E.m_problems[0].spec.is_abec != 0;
+    std::vector<const SolveSpec*> specs;
+    for (auto& pr : E.m_problems) {
+        MLMG_REQUIRE((pr.spec.is_abec != 0) == abec, ERR_UNSUPPORTED, "a batch must hold one operator type");
+        specs.push_back(&pr.spec);
+        nlev_max = std::max(nlev_max, (int)pr.spec.levels.size());
+    }
+    lev.resize(nlev_max);
+    size_t max_tiles = 1;
+    for (int l = 0; l < nlev_max; ++l) {
+        LevelData& L = lev[l];
+        L.meta = build_patch_level(specs, l, E.m_opt.merge_boxes != 0);
+        PatchLevel& M = L.meta;
+        // level-0 Dirichlet values: one slot per face cell of every level-0 patch face
+        if (l == 0) {
+            long long off = 0;
+            for (auto& P : M.patches) {
+                for (int f = 0; f < 6; ++f) {
+                    const int d = f % 3;
+                    const int e0 = (d == 0) ? 1 : 0, e1 = (d == 2) ? 1 : 2;
+                    P.face[f].bcval_off = off;
+                    off += (long long)(P.hi[e0] - P.lo[e0] + 1) * (P.hi[e1] - P.lo[e1] + 1);
+                }
+            }
+            L.bcval.alloc((size_t)std::max<long long>(off, 1));
+            L.bcval.zero(st());
+        }
+        L.P.upload(M.patches, st());
+        if (!M.masks.empty()) { L.masks.upload(M.masks, st()); }
+        std::vector<int> sfirst(nsolve), snp(nsolve);
+        for (int s = 0; s < nsolve; ++s) { sfirst[s] = M.solve_first_patch[s]; snp[s] = M.solve_npatch[s]; }
+        L.sfirst.upload(sfirst, st());
+        L.snp.upload(snp, st());
+        // tags grouped per solve (they are generated solve by solve)
+        L.solve_tag_first.assign(nsolve, 0);
+        L.solve_tag_n.assign(nsolve, 0);
+        for (size_t t = 0; t < M.tags.size(); ++t) {
+            const int s = M.patches[M.tags[t].dst].solve;
+            if (L.solve_tag_n[s] == 0) { L.solve_tag_first[s] = (int)t; }
+            L.solve_tag_n[s]++;
+        }
+        // ghost work
+        std::vector<int2> faces;
+        std::vector<long long> fstart{0}, tstart{0};
+        for (int p = 0; p < (int)M.patches.size(); ++p) {
+            const PatchDesc& P = M.patches[p];
+            for (int f = 0; f < 6; ++f) {
+                const int d = f % 3;
+                const int e0 = (d == 0) ? 1 : 0, e1 = (d == 2) ? 1 : 2;
+                faces.push_back(make_int2(p, f));
+                fstart.push_back(fstart.back() + (long long)(P.hi[e0] - P.lo[e0] + 1) * (P.hi[e1] - P.lo[e1] + 1));
+            }
+        }
+        for (const auto& t : M.tags) { tstart.push_back(tstart.back() + t.box.npts()); }
+        L.faces.upload(faces, st());
+        L.fstart.upload(fstart, st());
+        if (!M.tags.empty()) { L.tags.upload(M.tags, st()); }
+        L.tstart.upload(tstart, st());
+        L.gw = GhostWork{L.faces.p, L.fstart.p, (int)faces.size(), L.tags.p, L.tstart.p, (int)M.tags.size(),
+                         fstart.back(), tstart.back()};
+        L.dl = DevLevel{L.P.p, L.masks.p, L.sfirst.p, L.snp.p, (int)M.patches.size()};
+        std::vector<int> all(M.patches.size()), mg;
+        std::iota(all.begin(), all.end(), 0);
+        for (int p = 0; p < (int)M.patches.size(); ++p) {
+            if (!M.patch_is_bottom[p]) { mg.push_back(p); } else { L.has_bottom = true; }
+        }
+        build_subset(L.all, M, all, nsolve, st());
+        build_subset(L.mg, M, mg, nsolve, st());
+        max_tiles = std::max(max_tiles, (size_t)L.all.ntiles);
+        // fields
+        const size_t n = (size_t)M.nelem;
+        auto alloc0 = [&] (DevBuf<double>& b) { b.alloc(n); b.zero(st()); };
+        auto alloc0f = [&] (DevBuf<float>& b) { b.alloc(n); b.zero(st()); };
+        if (abec) { alloc0(L.a); alloc0(L.bx); alloc0(L.by); alloc0(L.bz); }
+        if (l == 0) { alloc0(L.sol); alloc0(L.rhs); alloc0(L.res); }
+        if (mixed()) {
+            alloc0f(L.cor32); alloc0f(L.res32); alloc0f(L.rescor32);
+            if (abec) { alloc0f(L.a32); alloc0f(L.bx32); alloc0f(L.by32); alloc0f(L.bz32); }
+        } else {
+            alloc0(L.cor); if (l > 0) { alloc0(L.res); } alloc0(L.rescor);
+        }
+        if (L.has_bottom) { for (auto& b : L.bw) { alloc0(b); } }
+    }
+    partial.alloc(max_tiles + 1);
+    red_out.alloc((size_t)nsolve * 4 + 4);
+    h_red.alloc((size_t)nsolve * 4 + 4);
+    h_iters.alloc((size_t)nsolve * 2 + 2);
+    bot_iters.alloc(nsolve);
+    bot_ret.alloc(nsolve);
+    active_d.alloc(nsolve);
+
+    // singular operators (update_singular_flags, AMReX_MLABecLaplacian.H:714-773;
+    // MLPoissonT::prepareForSolve, AMReX_MLPoisson.H:138-178) and the
+    // solvability volumes (AMReX_MLCellLinOp.H:1941-1995)
+    singular.assign(nsolve, 0);
+    volinv0.assign(nsolve, 0.0);
+    volinv_bottom.assign(nsolve, 0.0);
+    for (int s = 0; s < nsolve; ++s) {
+        const SolveSpec& S = E.m_problems[s].spec;
+        bool dir = false;
+        for (int d = 0; d < 3; ++d) { if (S.lobc[d] == BC_DIRICHLET || S.hibc[d] == BC_DIRICHLET) { dir = true; } }
+        long long np = 0;
+        for (const auto& b : S.levels[0].boxes) { np += b.npts(); }
+        const bool covered = (np == S.levels[0].geom.domain.npts());
+        singular[s] = (!dir && covered && (!abec || S.alpha == 0.0)) ? 1 : 0;
+        volinv0[s] = 1.0 / (double)S.levels[0].geom.domain.npts();
+        volinv_bottom[s] = 1.0 / (double)S.levels.back().geom.domain.npts();
+    }
+    volinv0_d.upload(volinv0, st());
+    build_bottom_tables();
+    MLMG_CUDA_CHECK(cudaEventCreate(&ev0));
+    MLMG_CUDA_CHECK(cudaEventCreate(&ev1));
+}
+
+void Engine::Impl::build_bottom_tables ()
+{
+    std::vector<BottomLevelPtrs> tab(nlev_max);
+    std::vector<BottomJob> jobs;
+    for (int l = 0; l < nlev_max; ++l) {
+        LevelData& L = lev[l];
+        BottomLevelPtrs& B = tab[l];
+        B.L = L.dl;
+        B.tags = L.tags.p;
+        if (L.has_bottom) {
+            B.x = L.bw[0].p; B.b = L.bw[1].p; B.p = L.bw[2].p; B.r = L.bw[3].p;
+            B.rh = L.bw[4].p; B.v = L.bw[5].p; B.t = L.bw[6].p;
+        }
+        B.a = L.a.p; B.bx = L.bx.p; B.by = L.by.p; B.bz = L.bz.p;
+        B.x_out = mixed() ? (void*)L.cor32.p : (void*)L.cor.p;
+        B.b_in = mixed() ? (const void*)L.res32.p : (const void*)L.res.p;
+    }
+    for (int s = 0; s < nsolve; ++s) {
+        const int l = (int)E.m_problems[s].spec.levels.size() - 1;
+        BottomJob J{};
+        J.lev = l; J.solve = s;
+        J.p0 = lev[l].meta.solve_first_patch[s];
+        J.np = lev[l].meta.solve_npatch[s];
+        J.t0 = lev[l].solve_tag_first[s];
+        J.nt = lev[l].solve_tag_n[s];
+        J.singular = singular[s];
+        J.volinv = volinv_bottom[s];
+        jobs.push_back(J);
+    }
+    njobs = (int)jobs.size();
+    bot_levels.upload(tab, st());
+    bot_jobs.upload(jobs, st());
+}
+
+// ----------------------------------------------------- user data transfer --
+std::vector<XferItem> Engine::Impl::items_for (const FabSet& fs, int s, int ghost_mode, int nodal_dir) const
+{
+    // ghost_mode 0: valid cells (nodal-extended for faces); 1: valid + the
+    // face-ghost layers that lie inside the owning patch's ghost shell
+    std::vector<XferItem> items;
+    const PatchLevel& M = lev[0].meta;
+    const int p0 = M.solve_first_patch[s], np = M.solve_npatch[s];
+    for (size_t b = 0; b < fs.boxes.size(); ++b) {
+        const Box3& vb = fs.boxes[b];
+        int pid = -1;
+        for (int p = p0; p < p0 + np; ++p) {
+            Box3 pb; for (int d = 0; d < 3; ++d) { pb.lo[d] = M.patches[p].lo[d]; pb.hi[d] = M.patches[p].hi[d]; }
+            if (pb.contains(vb.lo[0], vb.lo[1], vb.lo[2])) { pid = p; break; }
+        }
+        MLMG_REQUIRE(pid >= 0, ERR_ARGS, "MultiFab box outside the operator's BoxArray");
+        Box3 fab = grow(vb, fs.ngrow);
+        if (fs.nodal_dir >= 0) { fab.hi[fs.nodal_dir] += 1; }
+        XferItem X{};
+        X.patch = pid;
+        X.src_off = fs.off[b];
+        for (int d = 0; d < 3; ++d) { X.flo[d] = fab.lo[d]; }
+        X.fsx = fab.len(0);
+        X.fsxy = (long long)fab.len(0) * fab.len(1);
+        Box3 reg = vb;
+        if (nodal_dir >= 0) { reg.hi[nodal_dir] += 1; }
+        X.region = reg;
+        items.push_back(X);
+        if (ghost_mode == 1 && fs.ngrow >= 1) {
+            const PatchDesc& P = M.patches[pid];
+            for (int f = 0; f < 6; ++f) {
+                const int d = f % 3;
+                Box3 g = vb;
+                if (f >= 3) { g.lo[d] = g.hi[d] = vb.hi[d] + 1; } else { g.lo[d] = g.hi[d] = vb.lo[d] - 1; }
+                // only ghost layers on the patch boundary (the rest are valid cells of the patch)
+                const bool on_patch_face = (f >= 3) ? (vb.hi[d] == P.hi[d]) : (vb.lo[d] == P.lo[d]);
+                if (!on_patch_face) { continue; }
+                X.region = g;
+                items.push_back(X);
+            }
+        }
+    }
+    return items;
+}
+
+void Engine::Impl::xfer (const std::vector<XferItem>& items, const FabSet& fs, void* field, bool field_is_f32,
+                         int dir)
+{
+    if (items.empty()) { return; }
+    std::vector<long long> start{0};
+    for (const auto& X : items) { start.push_back(start.back() + X.region.npts()); }
+    DevBuf<XferItem> d_items;
+    DevBuf<long long> d_start;
+    d_items.upload(items, st());
+    d_start.upload(start, st());
+    const long long n = start.back();
+    const int threads = 256;
+    const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+    const DevLevel& dl = lev[0].dl;
+    if (fs.prec == 8 && !field_is_f32) {
+        k_xfer<double, double><<<blocks, threads, 0, st()>>>(dl, d_items.p, d_start.p, (int)items.size(), n,
+            (double*)const_cast<void*>(fs.data), (double*)field, dir);
+    } else if (fs.prec == 4 && !field_is_f32) {
+        k_xfer<float, double><<<blocks, threads, 0, st()>>>(dl, d_items.p, d_start.p, (int)items.size(), n,
+            (float*)const_cast<void*>(fs.data), (double*)field, dir);
+    } else {
+        MLMG_REQUIRE(false, ERR_UNSUPPORTED, "unsupported transfer precision");
+    }
+    launched();
+    MLMG_CUDA_CHECK(cudaGetLastError());
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st()));   // items are freed on return
+}
+
+void Engine::Impl::load_level0_field (const FabSet* fs, double* field, double defval, int nodal_dir, int s)
+{
+    if (fs == nullptr) {
+        // constant value over the solve's level-0 patches (valid + nodal layer)
+        const PatchLevel& M = lev[0].meta;
+        std::vector<double> h((size_t)M.nelem, 0.0);
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(h.data(), field, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st()));
+        MLMG_CUDA_CHECK(cudaStreamSynchronize(st()));
+        for (int p = M.solve_first_patch[s]; p < M.solve_first_patch[s] + M.solve_npatch[s]; ++p) {
+            const PatchDesc& P = M.patches[p];
+            Box3 r; for (int d = 0; d < 3; ++d) { r.lo[d] = P.lo[d]; r.hi[d] = P.hi[d]; }
+            if (nodal_dir >= 0) { r.hi[nodal_dir] += 1; }
+            for (int k = r.lo[2]; k <= r.hi[2]; ++k)
+            for (int j = r.lo[1]; j <= r.hi[1]; ++j)
+            for (int i = r.lo[0]; i <= r.hi[0]; ++i) { h[(size_t)pidx(P, i, j, k)] = defval; }
+        }
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(field, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, st()));
+        MLMG_CUDA_CHECK(cudaStreamSynchronize(st()));
+        return;
+    }
+    MLMG_REQUIRE(fs->nodal_dir == nodal_dir, ERR_ARGS, "coefficient MultiFab has the wrong index type");
+    xfer(items_for(*fs, s, 0, nodal_dir), *fs, field, false, 0);
+}
+
+// ------------------------------------------------------------ operations --
+static const dim3 kTileBlock(32, TILE_Y);
+
+template <typename T>
+void Engine::Impl::ghost (int l, T* phi, bool inhomog, bool do_copy)
+{
+    const LevelData& L = lev[l];
+    const long long n = L.gw.nfacecells + (do_copy ? L.gw.ntagcells : 0);
+    if (n == 0) { return; }
+    const int threads = 256;
+    k_ghost<T><<<(unsigned)((n + threads - 1) / threads), threads, 0, st()>>>(
+        L.dl, L.gw, phi, inhomog ? 1 : 0, (l == 0) ? L.bcval.p : nullptr, do_copy ? 1 : 0);
+    launched();
+}
+
+template <typename T>
+void Engine::Impl::smooth (int l, T* cor, const T* res, bool skip_fb)
+{
+    // MLCellLinOpT::smooth (AMReX_MLCellLinOp.H:1204-1217): per colour, applyBC then Fsmooth
+    const LevelData& L = lev[l];
+    for (int rb = 0; rb < 2; ++rb) {
+        ghost<T>(l, cor, false, !skip_fb);
+        skip_fb = false;
+        if (abec) {
+            k_gsrb<T, true><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, coef<T>(l, 0),
+                coef<T>(l, 1), coef<T>(l, 2), coef<T>(l, 3), rb);
+        } else {
+            k_gsrb<T, false><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, nullptr, nullptr,
+                nullptr, nullptr, rb);
+        }
+        launched();
+    }
+}
+
+// MLMGT::mgVcycle (AMReX_MLMG.H:1306-1415), one stage per launch for every
+// patch of every solve at that level.
+template <typename T>
+void Engine::Impl::vcycle ()
+{
+    const EngineOptions& o = E.m_opt;
+    for (int l = 0; l + 1 < nlev_max; ++l) {
+        LevelData& L = lev[l];
+        if (L.mg.n == 0) { continue; }
+        T* cor = field_cor<T>(l);
+        T* res = field_res<T>(l);
+        T* rescor = field_rescor<T>(l);
+        MLMG_CUDA_CHECK(cudaMemsetAsync(cor, 0, (size_t)L.meta.nelem * sizeof(T), st()));
+        for (int i = 0; i < o.nu1; ++i) { smooth<T>(l, cor, res, i == 0); }
+        // rescor = res - L(cor), homogeneous BC (computeResOfCorrection)
+        ghost<T>(l, cor, false, true);
+        if (abec) {
+            k_residual<T, T, true><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
+                coef<T>(l, 0), coef<T>(l, 1), coef<T>(l, 2), coef<T>(l, 3), nullptr);
+        } else {
+            k_residual<T, T, false><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
+                nullptr, nullptr, nullptr, nullptr, nullptr);
+        }
+        launched();
+        LevelData& C = lev[l + 1];
+        k_restrict<T><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), rescor, field_res<T>(l + 1));
+        launched();
+    }
+    BottomParams prm{o.bottom_maxiter, o.bottom_reltol, o.bottom_abstol, o.nub, o.nuf, o.bottom_solver == 1 ? 1 : 0};
+    if (abec) {
+        k_bottom<T, true><<<njobs, BOTTOM_THREADS, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
+                                                              bot_iters.p, bot_ret.p);
+    } else {
+        k_bottom<T, false><<<njobs, BOTTOM_THREADS, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
+                                                               bot_iters.p, bot_ret.p);
+    }
+    launched();
+    for (int l = nlev_max - 2; l >= 0; --l) {
+        LevelData& L = lev[l];
+        if (L.mg.n == 0) { continue; }
+        T* cor = field_cor<T>(l);
+        k_interp_add<T><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), lev[l + 1].dl, field_cor<T>(l + 1), cor);
+        launched();
+        for (int i = 0; i < o.nu2; ++i) { smooth<T>(l, cor, field_res<T>(l), false); }
+    }
+}
+
+void Engine::Impl::reduce_per_solve (int l, const SubsetData& S, int op, const double* x, const double* y)
+{
+    const LevelData& L = lev[l];
+    k_reduce<double><<<S.ntiles, kTileBlock, 0, st()>>>(L.dl, S.dev(), x, y, op, partial.p);
+    k_reduce_final<<<nsolve, 256, 0, st()>>>(partial.p, S.solve_begin.p, op, red_out.p);
+    launched(2);
+}
+
+// res[0] = rhs - L(sol) with the solution's BCs (solutionResidual,
+// AMReX_MLCellLinOp.H:1219-1236) and per-solve max|res| into red_out
+void Engine::Impl::residual0 (bool to32)
+{
+    LevelData& L = lev[0];
+    ghost<double>(0, L.sol.p, true, true);
+    const double *a = L.a.p, *bx = L.bx.p, *by = L.by.p, *bz = L.bz.p;
+    if (to32) {
+        if (abec) {
+            k_residual<double, float, true><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res32.p,
+                L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
+        } else {
+            k_residual<double, float, false><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res32.p,
+                L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
+        }
+    } else {
+        if (abec) {
+            k_residual<double, double, true><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res.p,
+                L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
+        } else {
+            k_residual<double, double, false><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res.p,
+                L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
+        }
+    }
+    k_reduce_final<<<nsolve, 256, 0, st()>>>(partial.p, L.all.solve_begin.p, RED_MAXABS, red_out.p);
+    launched(2);
+}
+
+// MLMGT::oneIter (AMReX_MLMG.H:1227-1293), single AMR level, followed by the
+// convergence residual of MLMGT::solve (:436-441)
+void Engine::Impl::one_iteration ()
+{
+    LevelData& L0 = lev[0];
+    bool any_singular = false;
+    for (int s : singular) { if (s) { any_singular = true; } }
+    if (mixed()) {
+        if (any_singular) {
+            // makeSolvable on the (FP32) residual: offsets from FP64 sums
+            k_reduce<float><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.res32.p, nullptr,
+                                                                    RED_SUM, partial.p);
+            k_reduce_final<<<nsolve, 256, 0, st()>>>(partial.p, L0.all.solve_begin.p, RED_SUM, red_out.p + nsolve);
+            k_minus_offset<float><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.res32.p,
+                                                                         red_out.p + nsolve, volinv0_d.p);
+            launched(3);
+        }
+        vcycle<float>();
+        k_add_to<double, float><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.sol.p, L0.cor32.p,
+                                                                        active_d.p);
+        launched();
+        residual0(true);
+    } else {
+        if (any_singular) {
+            k_reduce<double><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.res.p, nullptr,
+                                                                     RED_SUM, partial.p);
+            k_reduce_final<<<nsolve, 256, 0, st()>>>(partial.p, L0.all.solve_begin.p, RED_SUM, red_out.p + nsolve);
+            k_minus_offset<double><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.res.p,
+                                                                          red_out.p + nsolve, volinv0_d.p);
+            launched(3);
+        }
+        vcycle<double>();
+        k_add_to<double, double><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.sol.p, L0.cor.p,
+                                                                         active_d.p);
+        launched();
+        residual0(false);
+    }
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(h_red.p, red_out.p, sizeof(double) * nsolve, cudaMemcpyDeviceToHost, st()));
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(h_iters.p, bot_iters.p, sizeof(int) * nsolve, cudaMemcpyDeviceToHost, st()));
+}
+
+// ---------------------------------------------------------------- Engine ---
+Engine::Engine (std::vector<SolveProblem> problems, const EngineOptions& opt, cudaStream_t stream)
+    : m_problems(std::move(problems)), m_opt(opt), m_stream(stream)
+{
+    m_impl = std::make_unique<Impl>(*this);
+    m_impl->build();
+    set_coefficients();
+}
+
+Engine::~Engine () = default;
+
+void Engine::set_coefficients ()
+{
+    Impl& I = *m_impl;
+    LevelData& L0 = I.lev[0];
+    for (int s = 0; s < I.nsolve; ++s) {
+        const SolveProblem& pr = m_problems[s];
+        if (I.abec) {
+            I.load_level0_field(pr.acoef, L0.a.p, 1.0, -1, s);
+            for (int d = 0; d < 3; ++d) {
+                double* dst = d == 0 ? L0.bx.p : (d == 1 ? L0.by.p : L0.bz.p);
+                I.load_level0_field(pr.bcoef[d], dst, 1.0, d, s);
+            }
+        }
+        // Dirichlet values: ghost cells of the level-BC MultiFab on the
+        // domain faces (MLCellLinOpT::setLevelBC, AMReX_MLCellLinOp.H:552-649)
+        if (pr.levelbc != nullptr) {
+            const FabSet& fs = *pr.levelbc;
+            MLMG_REQUIRE(fs.ngrow >= 1, ERR_ARGS, "level BC MultiFab needs one ghost cell");
+            const PatchLevel& M = L0.meta;
+            std::vector<double> hb(L0.bcval.n, 0.0);
+            MLMG_CUDA_CHECK(cudaMemcpyAsync(hb.data(), L0.bcval.p, hb.size() * sizeof(double), cudaMemcpyDeviceToHost, m_stream));
+            // pull the whole BC MultiFab to the host (setup only)
+            long long total = 0;
+            for (size_t b = 0; b < fs.boxes.size(); ++b) { total = std::max(total, fs.off[b] + grow(fs.boxes[b], fs.ngrow).npts()); }
+            std::vector<double> hm((size_t)total);
+            if (fs.prec == 8) {
+                MLMG_CUDA_CHECK(cudaMemcpyAsync(hm.data(), fs.data, (size_t)total * 8, cudaMemcpyDeviceToHost, m_stream));
+                MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
+            } else {
+                std::vector<float> hf((size_t)total);
+                MLMG_CUDA_CHECK(cudaMemcpyAsync(hf.data(), fs.data, (size_t)total * 4, cudaMemcpyDeviceToHost, m_stream));
+                MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
+                for (size_t q = 0; q < hf.size(); ++q) { hm[q] = hf[q]; }
+            }
+            const Box3 dom = pr.spec.levels[0].geom.domain;
+            for (int p = M.solve_first_patch[s]; p < M.solve_first_patch[s] + M.solve_npatch[s]; ++p) {
+                const PatchDesc& P = M.patches[p];
+                for (int f = 0; f < 6; ++f) {
+                    const int d = f % 3;
+                    const bool hi = f >= 3;
+                    const int e0 = (d == 0) ? 1 : 0, e1 = (d == 2) ? 1 : 2;
+                    const int nx0 = P.hi[e0] - P.lo[e0] + 1;
+                    const int g = hi ? P.hi[d] + 1 : P.lo[d] - 1;
+                    if (g >= dom.lo[d] && g <= dom.hi[d]) { continue; }     // not a physical face
+                    for (size_t b = 0; b < fs.boxes.size(); ++b) {
+                        const Box3& vb = fs.boxes[b];
+                        if ((hi ? vb.hi[d] : vb.lo[d]) != (hi ? P.hi[d] : P.lo[d])) { continue; }
+                        const Box3 fab = grow(vb, fs.ngrow);
+                        for (int v1 = vb.lo[e1]; v1 <= vb.hi[e1]; ++v1)
+                        for (int v0 = vb.lo[e0]; v0 <= vb.hi[e0]; ++v0) {
+                            int c[3];
+                            c[d] = g; c[e0] = v0; c[e1] = v1;
+                            const long long qm = fs.off[b] + ((long long)(c[2] - fab.lo[2]) * fab.len(1)
+                                               + (c[1] - fab.lo[1])) * fab.len(0) + (c[0] - fab.lo[0]);
+                            const long long u = (long long)(v1 - P.lo[e1]) * nx0 + (v0 - P.lo[e0]);
+                            hb[(size_t)(P.face[f].bcval_off + u)] = hm[(size_t)qm];
+                        }
+                    }
+                }
+            }
+            MLMG_CUDA_CHECK(cudaMemcpyAsync(L0.bcval.p, hb.data(), hb.size() * sizeof(double), cudaMemcpyHostToDevice, m_stream));
+            MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
+        }
+    }
+    // restrict a and b to every MG level (averageDownCoeffsSameAmrLevel)
+    if (I.abec) {
+        int a_zero = 1;
+        for (auto& pr : m_problems) { if (pr.spec.alpha != 0.0) { a_zero = 0; } }
+        if (a_zero) { MLMG_CUDA_CHECK(cudaMemsetAsync(L0.a.p, 0, L0.a.n * sizeof(double), m_stream)); }
+        for (int l = 1; l < I.nlev_max; ++l) {
+            LevelData& F = I.lev[l - 1];
+            LevelData& C = I.lev[l];
+            k_restrict_coef<double><<<C.all.ntiles, kTileBlock, 0, m_stream>>>(F.dl, C.dl, C.all.dev(), F.a.p, F.bx.p,
+                F.by.p, F.bz.p, C.a.p, C.bx.p, C.by.p, C.bz.p, a_zero);
+            I.launched();
+        }
+        if (I.mixed()) {
+            for (int l = 0; l < I.nlev_max; ++l) {
+                LevelData& L = I.lev[l];
+                const long long n = L.meta.nelem;
+                const unsigned nb = (unsigned)std::min<long long>((n + 255) / 256, 152 * 16);
+                k_convert<float, double><<<nb, 256, 0, m_stream>>>(n, L.a32.p, L.a.p);
+                k_convert<float, double><<<nb, 256, 0, m_stream>>>(n, L.bx32.p, L.bx.p);
+                k_convert<float, double><<<nb, 256, 0, m_stream>>>(n, L.by32.p, L.by.p);
+                k_convert<float, double><<<nb, 256, 0, m_stream>>>(n, L.bz32.p, L.bz.p);
+                I.launched(4);
+            }
+        }
+    }
+    MLMG_CUDA_CHECK(cudaGetLastError());
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
+}
+
+void Engine::apply (const FabSet& in, FabSet& out)
+{
+    Impl& I = *m_impl;
+    MLMG_REQUIRE(I.nsolve == 1, ERR_UNSUPPORTED, "apply works on a single solve");
+    LevelData& L0 = I.lev[0];
+    I.xfer(I.items_for(in, 0, 0, -1), in, L0.sol.p, false, 0);
+    I.ghost<double>(0, L0.sol.p, true, true);
+    if (I.abec) {
+        k_residual<double, double, true><<<L0.all.ntiles, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.res.p,
+            L0.sol.p, nullptr, L0.a.p, L0.bx.p, L0.by.p, L0.bz.p, nullptr);
+    } else {
+        k_residual<double, double, false><<<L0.all.ntiles, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.res.p,
+            L0.sol.p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    }
+    I.launched();
+    I.xfer(I.items_for(out, 0, 0, -1), out, L0.res.p, false, 1);
+}
+
+void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<FabSet*>& sol_out,
+                    const std::vector<const FabSet*>& rhs, double tol_rel, double tol_abs)
+{
+    Impl& I = *m_impl;
+    const int ns = I.nsolve;
+    MLMG_REQUIRE((int)sol_in.size() == ns && (int)sol_out.size() == ns && (int)rhs.size() == ns, ERR_ARGS,
+                 "one sol and one rhs per solve");
+    LevelData& L0 = I.lev[0];
+    m_reports.assign(ns, SolveReport{});
+    // initial guess (valid cells) and rhs; the solution's ghosts come from BCs
+    MLMG_CUDA_CHECK(cudaMemsetAsync(L0.sol.p, 0, L0.sol.n * sizeof(double), m_stream));
+    MLMG_CUDA_CHECK(cudaMemsetAsync(L0.rhs.p, 0, L0.rhs.n * sizeof(double), m_stream));
+    for (int s = 0; s < ns; ++s) {
+        I.xfer(I.items_for(*sol_in[s], s, 0, -1), *sol_in[s], L0.sol.p, false, 0);
+        I.xfer(I.items_for(*rhs[s], s, 0, -1), *rhs[s], L0.rhs.p, false, 0);
+    }
+    MLMG_CUDA_CHECK(cudaEventRecord(I.ev0, m_stream));
+    // enforce solvability of singular problems (MLMGT::makeSolvable, AMReX_MLMG.H:1844-1858)
+    bool any_singular = false;
+    for (int s : I.singular) { if (s) { any_singular = true; } }
+    if (any_singular) {
+        k_reduce<double><<<L0.all.ntiles, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.rhs.p, nullptr, RED_SUM,
+                                                                    I.partial.p);
+        k_reduce_final<<<ns, 256, 0, m_stream>>>(I.partial.p, L0.all.solve_begin.p, RED_SUM, I.red_out.p + ns);
+        k_minus_offset<double><<<L0.all.ntiles, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.rhs.p,
+                                                                          I.red_out.p + ns, I.volinv0_d.p);
+        I.launched(3);
+    }
+    // initial residual and norms (AMReX_MLMG.H:391-420)
+    I.residual0(false);
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(I.h_red.p, I.red_out.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, m_stream));
+    I.reduce_per_solve(0, L0.all, RED_MAXABS, L0.rhs.p, nullptr);
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(I.h_red.p + ns, I.red_out.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, m_stream));
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
+    std::vector<double> target(ns), max_norm(ns);
+    std::vector<int> active(ns, 1);
+    for (int s = 0; s < ns; ++s) {
+        SolveReport& R = m_reports[s];
+        R.init_resid = I.h_red.p[s];
+        R.rhs_norm = I.h_red.p[ns + s];
+        max_norm[s] = (m_opt.always_use_bnorm || R.rhs_norm >= R.init_resid) ? R.rhs_norm : R.init_resid;
+        target[s] = std::max(tol_abs, std::max(tol_rel, 1.e-16) * max_norm[s]);
+        R.final_resid = R.init_resid;
+        if (R.init_resid <= target[s]) { active[s] = 0; }
+        if (m_opt.verbose >= 1) {
+            std::printf("MLMG: Initial rhs               = %.10g\nMLMG: Initial residual (resid0) = %.10g\n",
+                        R.rhs_norm, R.init_resid);
+        }
+    }
+    // when the first residual already meets the target, the mixed path needs
+    // its FP32 copy of the residual for the next iteration anyway
+    if (I.mixed()) { I.residual0(true); }
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(I.active_d.p, active.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, m_stream));
+    const int niters = m_opt.fixed_iter ? m_opt.fixed_iter : m_opt.max_iter;
+    bool any_active = false;
+    for (int a : active) { if (a) { any_active = true; } }
+    int per_iter_launches = 0;
+    for (int iter = 0; iter < niters && any_active; ++iter) {
+        if (m_opt.use_graph) {
+            if (I.graph_exec == nullptr) {
+                const int before = m_launches;
+                cudaGraph_t g;
+                MLMG_CUDA_CHECK(cudaStreamBeginCapture(m_stream, cudaStreamCaptureModeThreadLocal));
+                I.one_iteration();
+                MLMG_CUDA_CHECK(cudaStreamEndCapture(m_stream, &g));
+                MLMG_CUDA_CHECK(cudaGraphInstantiate(&I.graph_exec, g, 0));
+                MLMG_CUDA_CHECK(cudaGraphDestroy(g));
+                per_iter_launches = m_launches - before;
+                m_launches = before;
+            } else if (per_iter_launches == 0) {
+                per_iter_launches = 0;
+            }
+            MLMG_CUDA_CHECK(cudaGraphLaunch(I.graph_exec, m_stream));
+            m_launches += per_iter_launches;
+        } else {
+            I.one_iteration();
+        }
+        MLMG_CUDA_CHECK(cudaGetLastError());
+        MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
+        bool changed = false;
+        for (int s = 0; s < ns; ++s) {
+            if (!active[s]) { continue; }
+            SolveReport& R = m_reports[s];
+            const double fine = I.h_red.p[s];
+            R.history.push_back(fine);
+            R.cg_iters.push_back(I.h_iters.p[s]);
+            R.niters++;
+            R.final_resid = fine;
+            if (m_opt.verbose >= 2) {
+                std::printf("MLMG: Iteration %3d Fine resid/%s = %.10g\n", iter + 1,
+                            (max_norm[s] == R.rhs_norm) ? "bnorm" : "resid0", fine / max_norm[s]);
+            }
+            if (!std::isfinite(fine)) {
+                R.status = ERR_NONFINITE; active[s] = 0; changed = true;
+            } else if (fine <= target[s]) {
+                R.status = OK; active[s] = 0; changed = true;
+            } else if (fine > 1.e20 * max_norm[s]) {
+                R.status = ERR_DIVERGED; active[s] = 0; changed = true;
+            }
+        }
+        if (changed) {
+            MLMG_CUDA_CHECK(cudaMemcpyAsync(I.active_d.p, active.data(), sizeof(int) * ns, cudaMemcpyHostToDevice,
+                                            m_stream));
+        }
+        any_active = false;
+        for (int a : active) { if (a) { any_active = true; } }
+    }
+    MLMG_CUDA_CHECK(cudaEventRecord(I.ev1, m_stream));
+    for (int s = 0; s < ns; ++s) {
+        if (active[s] && m_opt.fixed_iter == 0) { m_reports[s].status = NOT_CONVERGED; }
+        if (m_opt.verbose >= 1) {
+            std::printf("MLMG: Final Iter. %d resid, resid/bnorm = %.10g, %.10g\n", m_reports[s].niters,
+                        m_reports[s].final_resid, m_reports[s].final_resid / max_norm[s]);
+        }
+    }
+    // write back the solution: valid cells and, for one-ghost MultiFabs, the
+    // physical-boundary ghost layer left by the last residual evaluation
+    for (int s = 0; s < ns; ++s) {
+        FabSet& out = *sol_out[s];
+        I.xfer(I.items_for(out, s, out.ngrow >= 1 ? 1 : 0, -1), out, L0.sol.p, false, 1);
+    }
+    MLMG_CUDA_CHECK(cudaEventSynchronize(I.ev1));
+    float ms = 0;
+    MLMG_CUDA_CHECK(cudaEventElapsedTime(&ms, I.ev0, I.ev1));
+    m_last_ms = ms;
+}
+
+} // namespace mlmg

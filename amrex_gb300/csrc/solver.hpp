@@ -1,0 +1,95 @@
+// The GB300 MLMG engine: a batch of N >= 1 independent cell-centred
+// MLPoisson / MLABecLaplacian solves (single AMR level each), run V-cycle
+// stage by V-cycle stage with one launch per stage covering every patch of
+// every solve.  A single MLMG::solve is a batch of one.
+#pragma once
+
+#include "devbuf.hpp"
+#include "hierarchy.hpp"
+
+#include <memory>
+
+namespace mlmg {
+
+// A user MultiFab as the engine sees it: per-box FABs (box grown by ngrow,
+// x fastest) in one device allocation.
+struct FabSet {
+    const void* data = nullptr;
+    int prec = 8;               // bytes per value
+    int ngrow = 0;
+    int nodal_dir = -1;         // -1 cell-centred, 0..2 face-centred in that direction
+    std::vector<Box3> boxes;    // valid boxes, cell-centred index space
+    std::vector<long long> off; // element offset of each FAB
+};
+
+struct EngineOptions {
+    int max_iter = 200;
+    int fixed_iter = 0;
+    int nu1 = 2, nu2 = 2, nuf = 8, nub = 0;
+    int bottom_solver = 2;      // 1 smoother, 2 bicgstab
+    int bottom_maxiter = 200;
+    double bottom_reltol = 1.e-4;
+    double bottom_abstol = -1.0;
+    int always_use_bnorm = 0;
+    int verbose = 0;
+    int precision = 0;          // 0: FP64 throughout; 1: FP32 V-cycle inside FP64 refinement
+    int use_graph = 0;          // capture one iteration in a CUDA graph and replay it
+    int fused_smoother = 0;     // fused two-colour sweeps where a level allows
+    int merge_boxes = 1;        // merge a level's boxes into one patch where exact
+};
+
+struct SolveProblem {           // one solve of a batch
+    SolveSpec spec;             // geometry, MG grids, BCs, scalars
+    std::vector<Box3> boxes;    // level-0 user boxes
+    const FabSet* acoef = nullptr;       // cell-centred a (ABec); null = 1
+    const FabSet* bcoef[3] = {nullptr, nullptr, nullptr};  // face b (ABec); null = 1
+    const FabSet* levelbc = nullptr;     // Dirichlet values in its ghost cells; null = 0
+};
+
+struct SolveReport {
+    int status = 0;
+    int niters = 0;
+    double init_resid = 0, rhs_norm = 0, final_resid = 0;
+    std::vector<double> history;
+    std::vector<int> cg_iters;
+};
+
+class Engine {
+public:
+    Engine (std::vector<SolveProblem> problems, const EngineOptions& opt, cudaStream_t stream);
+    ~Engine ();
+    Engine (const Engine&) = delete;
+    Engine& operator= (const Engine&) = delete;
+
+    // (Re)load coefficients and BC values from the problems' FabSets and
+    // restrict them to every MG level.
+    void set_coefficients ();
+
+    // MLMGT::solve on every solve of the batch.  sol[s] (ngrow >= 0) holds the
+    // initial guess and receives the solution; rhs[s] the right-hand side.
+    void solve (const std::vector<const FabSet*>& sol_in, const std::vector<FabSet*>& sol_out,
+                const std::vector<const FabSet*>& rhs, double tol_rel, double tol_abs);
+
+    // out = L(in) with inhomogeneous BCs (MLMGT::apply)
+    void apply (const FabSet& in, FabSet& out);
+
+    const std::vector<SolveReport>& reports () const { return m_reports; }
+    int nlevels (int s) const { return (int)m_problems[s].spec.levels.size(); }
+    const EngineOptions& options () const { return m_opt; }
+    EngineOptions& options () { return m_opt; }
+    double last_solve_ms () const { return m_last_ms; }
+    int kernel_launches () const { return m_launches; }
+    void reset_launch_count () { m_launches = 0; }
+
+    struct Impl;
+private:
+    std::vector<SolveProblem> m_problems;
+    EngineOptions m_opt;
+    cudaStream_t m_stream;
+    std::vector<SolveReport> m_reports;
+    double m_last_ms = 0;
+    int m_launches = 0;
+    std::unique_ptr<Impl> m_impl;
+};
+
+} // namespace mlmg

@@ -1,0 +1,434 @@
+// Global kernels of the V-cycle stages, ghost fill, reductions, transfers.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace mlmg {
+
+// ------------------------------------------------------------ reductions --
+enum RedOp : int { RED_MAXABS = 0, RED_DOT = 1, RED_SUM = 2 };
+
+__device__ __forceinline__ double red_combine (int op, double a, double b)
+{
+    return (op == RED_MAXABS) ? fmax(a, b) : a + b;
+}
+
+// deterministic block reduction over TILE_THREADS (or any multiple of 32 up to 1024) threads
+__device__ __forceinline__ double block_reduce (double v, int op, double* sm)
+{
+    const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+    const int warp = (threadIdx.y * blockDim.x + threadIdx.x) >> 5;
+    const int nwarp = (blockDim.x * blockDim.y + 31) >> 5;
+    for (int o = 16; o > 0; o >>= 1) { v = red_combine(op, v, __shfl_down_sync(0xffffffffu, v, o)); }
+    __syncthreads();
+    if (lane == 0) { sm[warp] = v; }
+    __syncthreads();
+    double r = (op == RED_MAXABS) ? 0.0 : 0.0;
+    if (warp == 0) {
+        r = (lane < nwarp) ? sm[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) { r = red_combine(op, r, __shfl_down_sync(0xffffffffu, r, o)); }
+    }
+    return r;   // valid in thread 0
+}
+
+// --------------------------------------------------------------- smoother --
+template <typename T, bool ABEC>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_gsrb (DevLevel L, Subset S, T* __restrict__ phi, const T* __restrict__ rhs, const T* __restrict__ a,
+        const T* __restrict__ bx, const T* __restrict__ by, const T* __restrict__ bz, int rb)
+{
+    const TileCoord c = decode_tile(L, S, blockIdx.x);
+    const PatchDesc& P = L.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    if (j > P.hi[1]) { return; }
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > P.hi[2]) { break; }
+        const int i = c.x0 + ((c.x0 + j + k + rb) & 1) + 2 * threadIdx.x;
+        if (i <= P.hi[0]) { gsrb_cell<T, ABEC>(L, P, i, j, k, phi, rhs, a, bx, by, bz); }
+    }
+}
+
+// r = b - A x (b != null) or r = A x (b == null); optional per-block max|r|
+template <typename T, typename TO, bool ABEC>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_residual (DevLevel L, Subset S, TO* __restrict__ r, const T* __restrict__ x, const T* __restrict__ b,
+            const T* __restrict__ a, const T* __restrict__ bx, const T* __restrict__ by,
+            const T* __restrict__ bz, double* __restrict__ partial)
+{
+    __shared__ double sm[32];
+    const TileCoord c = decode_tile(L, S, blockIdx.x);
+    const PatchDesc& P = L.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    double mx = 0.0;
+    if (j <= P.hi[1]) {
+        for (int kk = 0; kk < TILE_Z; ++kk) {
+            const int k = c.z0 + kk;
+            if (k > P.hi[2]) { break; }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int i = c.x0 + threadIdx.x + 32 * h;
+                if (i > P.hi[0]) { continue; }
+                const long long q = cidx(P, i, j, k);
+                const T ax = adotx_cell<T, ABEC>(P, q, x, a, bx, by, bz);
+                // MF::Xpay(resid, -1, b): resid = b + (-1)*resid
+                const T v = (b != nullptr) ? T(b[q] + T(-1.0) * ax) : ax;
+                r[q] = TO(v);
+                mx = fmax(mx, fabs((double)v));
+            }
+        }
+    }
+    if (partial != nullptr) {
+        const double red = block_reduce(mx, RED_MAXABS, sm);
+        if (threadIdx.x == 0 && threadIdx.y == 0) { partial[blockIdx.x] = red; }
+    }
+}
+
+// ------------------------------------------------------------- ghost fill --
+struct GhostWork {
+    const int2* faces;          // (patch, face)
+    const long long* fstart;    // prefix over face cell counts (nface+1)
+    int nface;
+    const CopyTag* tags;
+    const long long* tstart;    // prefix over tag cell counts (ntag+1)
+    int ntag;
+    long long nfacecells, ntagcells;
+};
+
+template <typename P_>
+__device__ __forceinline__ int bsearch_ll (const long long* start, int n, long long v)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= v) { lo = mid; } else { hi = mid - 1; }
+    }
+    return lo;
+}
+
+// face-cell coordinates of local index u on face f of patch P (the outside layer)
+__device__ __forceinline__ void face_cell (const PatchDesc& P, int f, long long u, int& i, int& j, int& k)
+{
+    const int d = f % 3;
+    const int nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1;
+    const int g = (f >= 3) ? P.hi[d] + 1 : P.lo[d] - 1;
+    if (d == 0) { i = g; j = P.lo[1] + (int)(u % ny); k = P.lo[2] + (int)(u / ny); }
+    else if (d == 1) { j = g; i = P.lo[0] + (int)(u % nx); k = P.lo[2] + (int)(u / nx); }
+    else { k = g; i = P.lo[0] + (int)(u % nx); j = P.lo[1] + (int)(u / nx); }
+}
+
+// FillBoundary (face ghosts) + physical/coarse-fine BC closure, one launch:
+// MLCellLinOpT::applyBC (AMReX_MLCellLinOp.H:682-893).  The two parts write
+// disjoint ghost cells (mask > 0 vs covered) and read only valid cells.
+template <typename T>
+__global__ void k_ghost (DevLevel L, GhostWork W, T* __restrict__ phi, int inhomog,
+                         const double* __restrict__ bcval, int do_copy)
+{
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid < W.nfacecells) {
+        const int w = bsearch_ll<int>(W.fstart, W.nface, tid);
+        const int2 pf = W.faces[w];
+        const PatchDesc& P = L.P[pf.x];
+        const int f = pf.y;
+        const long long u = tid - W.fstart[w];
+        int i, j, k;
+        face_cell(P, f, u, i, j, k);
+        if (face_mask(L, P, f, i, j, k) > 0) {
+            const int d = f % 3;
+            const long long stride = (d == 0) ? 1 : ((d == 1) ? (long long)P.sx : P.sxy);
+            const long long step = (f >= 3) ? -stride : stride;
+            bc_ghost<T>(P, f, cidx(P, i, j, k), step, phi, inhomog, bcval, u);
+        }
+    } else if (do_copy) {
+        const long long t = tid - W.nfacecells;
+        if (t >= W.ntagcells) { return; }
+        const int w = bsearch_ll<int>(W.tstart, W.ntag, t);
+        const CopyTag& C = W.tags[w];
+        const long long u = t - W.tstart[w];
+        const int nx = C.box.hi[0] - C.box.lo[0] + 1, ny = C.box.hi[1] - C.box.lo[1] + 1;
+        const int i = C.box.lo[0] + (int)(u % nx);
+        const int j = C.box.lo[1] + (int)((u / nx) % ny);
+        const int k = C.box.lo[2] + (int)(u / ((long long)nx * ny));
+        const PatchDesc& D = L.P[C.dst];
+        const PatchDesc& Sp = L.P[C.src];
+        phi[cidx(D, i, j, k)] = phi[cidx(Sp, i - C.shift[0], j - C.shift[1], k - C.shift[2])];
+    }
+}
+
+// ---------------------------------------------------- inter-level transfer --
+// patch of solve s at level L containing cell (i,j,k) (linear search; levels
+// are almost always a single patch per solve)
+__device__ __forceinline__ int find_patch (const DevLevel& L, int s, int i, int j, int k)
+{
+    const int p0 = L.sfirst[s], np = L.snp[s];
+    for (int p = p0; p < p0 + np; ++p) {
+        const PatchDesc& P = L.P[p];
+        if (i >= P.lo[0] && i <= P.hi[0] && j >= P.lo[1] && j <= P.hi[1] && k >= P.lo[2] && k <= P.hi[2]) {
+            return p;
+        }
+    }
+    return p0;
+}
+
+// crse = average of 2x2x2 fine: amrex_avgdown (Src/Base/AMReX_MultiFabUtil_3D_C.H:375-392)
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_restrict (DevLevel Lf, DevLevel Lc, Subset Sc, const T* __restrict__ fine, T* __restrict__ crse)
+{
+    const TileCoord c = decode_tile(Lc, Sc, blockIdx.x);
+    const PatchDesc& C = Lc.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    if (j > C.hi[1]) { return; }
+    const int s = C.solve;
+    const T volfrac = T(1.0) / T(8);
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > C.hi[2]) { break; }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = c.x0 + threadIdx.x + 32 * h;
+            if (i > C.hi[0]) { continue; }
+            const PatchDesc& F = Lf.P[find_patch(Lf, s, 2 * i, 2 * j, 2 * k)];
+            const long long qf = cidx(F, 2 * i, 2 * j, 2 * k);
+            const long long sx = F.sx, sxy = F.sxy;
+            T v = 0;
+            v += fine[qf];           v += fine[qf + 1];
+            v += fine[qf + sx];      v += fine[qf + sx + 1];
+            v += fine[qf + sxy];     v += fine[qf + sxy + 1];
+            v += fine[qf + sxy + sx]; v += fine[qf + sxy + sx + 1];
+            crse[cidx(C, i, j, k)] = volfrac * v;
+        }
+    }
+}
+
+// fine += crse(i/2,j/2,k/2): MLCellLinOpT::interpolation (AMReX_MLCellLinOp.H:954-999)
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_interp_add (DevLevel Lf, Subset Sf, DevLevel Lc, const T* __restrict__ crse, T* __restrict__ fine)
+{
+    const TileCoord c = decode_tile(Lf, Sf, blockIdx.x);
+    const PatchDesc& F = Lf.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    if (j > F.hi[1]) { return; }
+    const int s = F.solve;
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > F.hi[2]) { break; }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = c.x0 + threadIdx.x + 32 * h;
+            if (i > F.hi[0]) { continue; }
+            const int ic = i >> 1, jc = j >> 1, kc = k >> 1;
+            const PatchDesc& C = Lc.P[find_patch(Lc, s, ic, jc, kc)];
+            fine[cidx(F, i, j, k)] += crse[cidx(C, ic, jc, kc)];
+        }
+    }
+}
+
+// dst += src over valid cells (LocalAdd), with precision conversion; solves
+// whose `active` flag is 0 are left untouched
+template <typename TD, typename TS>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_add_to (DevLevel L, Subset S, TD* __restrict__ dst, const TS* __restrict__ src, const int* __restrict__ active)
+{
+    const TileCoord c = decode_tile(L, S, blockIdx.x);
+    const PatchDesc& P = L.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    if (j > P.hi[1]) { return; }
+    if (active != nullptr && !active[P.solve]) { return; }
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > P.hi[2]) { break; }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = c.x0 + threadIdx.x + 32 * h;
+            if (i > P.hi[0]) { continue; }
+            const long long q = cidx(P, i, j, k);
+            dst[q] += TD(src[q]);
+        }
+    }
+}
+
+// per-block partial of max|x|, sum x*y or sum x over valid cells
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_reduce (DevLevel L, Subset S, const T* __restrict__ x, const T* __restrict__ y, int op,
+          double* __restrict__ partial)
+{
+    __shared__ double sm[32];
+    const TileCoord c = decode_tile(L, S, blockIdx.x);
+    const PatchDesc& P = L.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    double acc = 0.0;
+    if (j <= P.hi[1]) {
+        for (int kk = 0; kk < TILE_Z; ++kk) {
+            const int k = c.z0 + kk;
+            if (k > P.hi[2]) { break; }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int i = c.x0 + threadIdx.x + 32 * h;
+                if (i > P.hi[0]) { continue; }
+                const long long q = cidx(P, i, j, k);
+                const double xv = (double)x[q];
+                if (op == RED_MAXABS) { acc = fmax(acc, fabs(xv)); }
+                else if (op == RED_DOT) { acc += xv * (double)y[q]; }
+                else { acc += xv; }
+            }
+        }
+    }
+    const double red = block_reduce(acc, op, sm);
+    if (threadIdx.x == 0 && threadIdx.y == 0) { partial[blockIdx.x] = red; }
+}
+
+// one block per solve: combine the partials of blocks [begin[s], begin[s+1])
+__global__ void k_reduce_final (const double* __restrict__ partial, const int* __restrict__ begin, int op,
+                                double* __restrict__ out)
+{
+    __shared__ double sm[32];
+    const int s = blockIdx.x;
+    double acc = 0.0;
+    for (int b = begin[s] + (int)threadIdx.x; b < begin[s + 1]; b += blockDim.x) {
+        acc = red_combine(op, acc, partial[b]);
+    }
+    const double red = block_reduce(acc, op, sm);
+    if (threadIdx.x == 0) { out[s] = red; }
+}
+
+// x -= offset[solve] * scale over valid cells (fixSolvabilityByOffset)
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_minus_offset (DevLevel L, Subset S, T* __restrict__ x, const double* __restrict__ sums,
+                const double* __restrict__ volinv)
+{
+    const TileCoord c = decode_tile(L, S, blockIdx.x);
+    const PatchDesc& P = L.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    if (j > P.hi[1]) { return; }
+    const T off = T(sums[P.solve] * volinv[P.solve]);
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > P.hi[2]) { break; }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = c.x0 + threadIdx.x + 32 * h;
+            if (i > P.hi[0]) { continue; }
+            x[cidx(P, i, j, k)] += -off;
+        }
+    }
+}
+
+template <typename TD, typename TS>
+__global__ void k_convert (long long n, TD* __restrict__ dst, const TS* __restrict__ src)
+{
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+         q += (long long)gridDim.x * blockDim.x) {
+        dst[q] = TD(src[q]);
+    }
+}
+
+// ------------------------------------------- user MultiFab <-> patch field --
+struct XferItem {
+    int patch;
+    Box3 region;          // cells (in the FAB's index space) to move
+    long long src_off;    // FAB offset in the MultiFab allocation
+    int flo[3];           // lower corner of the FAB box (grown, nodal-extended)
+    int fsx;              // FAB x extent
+    long long fsxy;       // FAB x*y extent
+};
+
+// dir 0: MultiFab -> patch field ; dir 1: patch field -> MultiFab
+template <typename TM, typename TP>
+__global__ void k_xfer (DevLevel L, const XferItem* __restrict__ items, const long long* __restrict__ start,
+                        int nitem, long long ncell, TM* __restrict__ mf, TP* __restrict__ field, int dir)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell) { return; }
+    const int w = bsearch_ll<int>(start, nitem, t);
+    const XferItem& X = items[w];
+    const long long u = t - start[w];
+    const int nx = X.region.hi[0] - X.region.lo[0] + 1, ny = X.region.hi[1] - X.region.lo[1] + 1;
+    const int i = X.region.lo[0] + (int)(u % nx);
+    const int j = X.region.lo[1] + (int)((u / nx) % ny);
+    const int k = X.region.lo[2] + (int)(u / ((long long)nx * ny));
+    const long long qm = X.src_off + (long long)(k - X.flo[2]) * X.fsxy + (long long)(j - X.flo[1]) * X.fsx
+                       + (i - X.flo[0]);
+    const long long qp = cidx(L.P[X.patch], i, j, k);
+    if (dir == 0) { field[qp] = TP(mf[qm]); } else { mf[qm] = TM(field[qp]); }
+}
+
+// ------------------------------------------------- coefficient restriction --
+// patch of solve s holding face (i,j,k) of direction d: the one whose cells
+// include (i,j,k) or, at a high face, (i,j,k) - e_d
+__device__ __forceinline__ int find_face_patch (const DevLevel& L, int s, int d, int i, int j, int k)
+{
+    const int p0 = L.sfirst[s], np = L.snp[s];
+    for (int p = p0; p < p0 + np; ++p) {
+        const PatchDesc& P = L.P[p];
+        const int c[3] = {i, j, k};
+        bool in = true;
+        for (int e = 0; e < 3; ++e) {
+            const int hi = (e == d) ? P.hi[e] + 1 : P.hi[e];
+            if (c[e] < P.lo[e] || c[e] > hi) { in = false; }
+        }
+        if (in) { return p; }
+    }
+    return p0;
+}
+
+template <typename T>
+__device__ __forceinline__ void restrict_face (const DevLevel& Lf, const PatchDesc& C, int s, int d, int i, int j,
+                                               int k, const T* __restrict__ bf, T* __restrict__ bc)
+{
+    const int fi = 2 * i, fj = 2 * j, fk = 2 * k;
+    const PatchDesc& F = Lf.P[find_face_patch(Lf, s, d, fi, fj, fk)];
+    const long long qf = cidx(F, fi, fj, fk);
+    long long s0, s1;
+    if (d == 0) { s0 = F.sx; s1 = F.sxy; } else if (d == 1) { s0 = 1; s1 = F.sxy; } else { s0 = 1; s1 = F.sx; }
+    // amrex_avgdown_faces sums the outer index slowest: (r1, r0) = (k,j) / (k,i) / (j,i)
+    T v = T(0.);
+    v += bf[qf]; v += bf[qf + s0]; v += bf[qf + s1]; v += bf[qf + s1 + s0];
+    bc[cidx(C, i, j, k)] = v * (T(1.0) / T(4));
+}
+
+// cell a: amrex_avgdown ; faces: amrex_avgdown_faces
+// (Src/Base/AMReX_MultiFabUtil_3D_C.H:170-225, 375-392)
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_restrict_coef (DevLevel Lf, DevLevel Lc, Subset Sc, const T* __restrict__ af, const T* __restrict__ bxf,
+                 const T* __restrict__ byf, const T* __restrict__ bzf, T* __restrict__ ac, T* __restrict__ bxc,
+                 T* __restrict__ byc, T* __restrict__ bzc, int a_zero)
+{
+    const TileCoord c = decode_tile(Lc, Sc, blockIdx.x);
+    const PatchDesc& C = Lc.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    const int s = C.solve;
+    if (j > C.hi[1]) { return; }
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > C.hi[2]) { break; }
+        for (int h = 0; h < 2; ++h) {
+            const int i = c.x0 + threadIdx.x + 32 * h;
+            if (i > C.hi[0]) { continue; }
+            const long long qc = cidx(C, i, j, k);
+            if (a_zero) {
+                ac[qc] = T(0);
+            } else {
+                const PatchDesc& F = Lf.P[find_patch(Lf, s, 2 * i, 2 * j, 2 * k)];
+                const long long qf = cidx(F, 2 * i, 2 * j, 2 * k);
+                const long long sx = F.sx, sxy = F.sxy;
+                T v = 0;
+                v += af[qf]; v += af[qf + 1]; v += af[qf + sx]; v += af[qf + sx + 1];
+                v += af[qf + sxy]; v += af[qf + sxy + 1]; v += af[qf + sxy + sx]; v += af[qf + sxy + sx + 1];
+                ac[qc] = (T(1.0) / T(8)) * v;
+            }
+            restrict_face<T>(Lf, C, s, 0, i, j, k, bxf, bxc);
+            restrict_face<T>(Lf, C, s, 1, i, j, k, byf, byc);
+            restrict_face<T>(Lf, C, s, 2, i, j, k, bzf, bzc);
+            if (i == C.hi[0]) { restrict_face<T>(Lf, C, s, 0, i + 1, j, k, bxf, bxc); }
+            if (j == C.hi[1]) { restrict_face<T>(Lf, C, s, 1, i, j + 1, k, byf, byc); }
+            if (k == C.hi[2]) { restrict_face<T>(Lf, C, s, 2, i, j, k + 1, bzf, bzc); }
+        }
+    }
+}
+
+} // namespace mlmg

@@ -1,0 +1,183 @@
+/*
+ * mlmg_capi.h -- C ABI of the GB300-native MLMG cell-centred solver.
+ *
+ * Drop-in boundary for AMReX's MLMG path (MLPoisson / MLABecLaplacian on
+ * MultiFab data).  The entry points mirror the reference's own C ABI for
+ * this path -- the Fortran-interface layer Src/F_Interfaces/ (files below are
+ * relative to the AMReX source tree) -- with opaque handles, caller-owned
+ * handle arrays, LinOpBCType codes (101 Dirichlet, 102 Neumann, 103
+ * reflect_odd, 200 periodic) and an int status instead of amrex::Abort:
+ *
+ *    0  converged / ok            1  not converged within max_iter
+ *   -1  bad argument or handle   -2  residual blew up (> 1e20 * norm)
+ *   -3  CUDA error               -4  unsupported request
+ *   -5  NaN/Inf in the residual  -6  internal error   -7  device wait timed out
+ *
+ * mlmg_last_error() returns the message of the last failing call on the
+ * calling thread.  Handles are not thread-safe; distinct solver handles may
+ * be used from distinct host threads.  Every call returns after its device
+ * work has completed (like the reference, which synchronises its stream after
+ * every Fsmooth/Fapply).
+ *
+ * Data layout of a MultiFab box (FAB): the box grown by ngrow (plus one cell
+ * in the nodal direction of a face MultiFab), x fastest, then y, z, then
+ * component -- the layout of amrex::BaseFab (Src/Base/AMReX_Array4.H:60-100).
+ */
+#ifndef MLMG_CAPI_H_
+#define MLMG_CAPI_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+typedef struct mlmg_boxarray_s* mlmg_boxarray;
+typedef struct mlmg_distromap_s* mlmg_distromap;
+typedef struct mlmg_geometry_s* mlmg_geometry;
+typedef struct mlmg_multifab_s* mlmg_multifab;
+typedef struct mlmg_linop_s* mlmg_linop;
+typedef struct mlmg_solver_s* mlmg_solver;
+
+/* LPInfo (Src/LinearSolvers/MLMG/AMReX_MLLinOp.H:34-83).  agg/con grid size
+ * <= 0 selects the reference's GPU-build default (32). */
+typedef struct {
+    int agglomeration;
+    int consolidation;
+    int agg_grid_size;
+    int con_grid_size;
+    int max_coarsening_level;
+} mlmg_lpinfo;
+
+/* ------------------------------------------------------------ library ---- */
+const char* mlmg_last_error(void);
+int mlmg_version(void);
+/* the CUDA stream the library works on (a cudaStream_t) */
+void* mlmg_stream(void);
+/* number of kernels this library has launched since the last reset */
+long long mlmg_kernel_launches(int reset);
+
+/* ----------------------------------------------------------- BoxArray ----
+ * replaces amrex_fi_new_boxarray / amrex_fi_boxarray_maxsize / ..._get_box
+ * (Src/F_Interfaces/Base/AMReX_boxarray_fi.cpp:10,16,44) */
+int mlmg_boxarray_new(const int* boxes, int nbox, mlmg_boxarray* out);  /* boxes: lo[3],hi[3] per box */
+int mlmg_boxarray_new_domain(const int lo[3], const int hi[3], mlmg_boxarray* out);  /* BoxArray(const Box&) */
+int mlmg_boxarray_maxsize(mlmg_boxarray ba, const int chunk[3]);       /* BoxArray::maxSize */
+int mlmg_boxarray_size(mlmg_boxarray ba);
+int mlmg_boxarray_get(mlmg_boxarray ba, int i, int lo[3], int hi[3]);
+int mlmg_boxarray_delete(mlmg_boxarray ba);
+
+/* ------------------------------------------------ DistributionMapping ----
+ * replaces amrex_fi_new_distromap (Src/F_Interfaces/Base/AMReX_distromap_fi.cpp:9,14);
+ * one GPU: every box is local */
+int mlmg_distromap_new(mlmg_boxarray ba, mlmg_distromap* out);
+int mlmg_distromap_delete(mlmg_distromap dm);
+
+/* ----------------------------------------------------------- Geometry ----
+ * replaces amrex_fi_new_geometry (Src/F_Interfaces/Base/AMReX_geometry_fi.cpp:7) */
+int mlmg_geometry_new(const int lo[3], const int hi[3], const double prob_lo[3], const double prob_hi[3],
+                      const int is_periodic[3], mlmg_geometry* out);
+int mlmg_geometry_delete(mlmg_geometry g);
+
+/* ----------------------------------------------------------- MultiFab ----
+ * replaces amrex_fi_new_multifab (Src/F_Interfaces/Base/AMReX_multifab_fi.cpp:10).
+ * nodal_dir: -1 cell-centred, 0..2 face-centred; precision: 8 (double) or 4 (float) */
+int mlmg_multifab_new(mlmg_boxarray ba, mlmg_distromap dm, int ncomp, int ngrow, int nodal_dir, int precision,
+                      mlmg_multifab* out);
+int mlmg_multifab_delete(mlmg_multifab mf);
+/* FAB of box i: element count, device pointer */
+int mlmg_multifab_fab_size(mlmg_multifab mf, int box, size_t* nelem);
+int mlmg_multifab_fab_ptr(mlmg_multifab mf, int box, void** dptr);
+/* copy one FAB (box grown by ngrow) from / to host memory */
+int mlmg_multifab_upload(mlmg_multifab mf, int box, const void* host);
+int mlmg_multifab_download(mlmg_multifab mf, int box, void* host);
+/* copy a whole-domain host array (x fastest; lower corner glo, extents gn)
+ * into every box's cells (ghosts included where the array covers them) or
+ * out of every box's valid cells -- one host<->device copy and one kernel */
+int mlmg_multifab_upload_global(mlmg_multifab mf, const void* host, const int glo[3], const int gn[3]);
+int mlmg_multifab_download_global(mlmg_multifab mf, void* host, const int glo[3], const int gn[3]);
+int mlmg_multifab_setval(mlmg_multifab mf, double v);                    /* FabArray::setVal, ghosts included */
+/* FabArray::FillBoundary (Src/Base/AMReX_FabArray.H:1000-1044), one rank */
+int mlmg_multifab_fill_boundary(mlmg_multifab mf, mlmg_geometry geom, int cross);
+int mlmg_multifab_norminf(mlmg_multifab mf, double* out);                /* valid cells */
+
+/* ------------------------------------------------- linear operators -----
+ * replace amrex_fi_new_poisson (Src/F_Interfaces/LinearSolvers/AMReX_poisson_fi.cpp:8-30)
+ * and amrex_fi_new_abeclaplacian (AMReX_abeclaplacian_fi.cpp:8-49); nlev must be 1 */
+int mlmg_linop_new_poisson(int nlev, const mlmg_geometry* geom, const mlmg_boxarray* ba, const mlmg_distromap* dm,
+                           const mlmg_lpinfo* info, mlmg_linop* out);
+int mlmg_linop_new_abeclap(int nlev, const mlmg_geometry* geom, const mlmg_boxarray* ba, const mlmg_distromap* dm,
+                           const mlmg_lpinfo* info, mlmg_linop* out);
+int mlmg_linop_delete(mlmg_linop op);
+/* amrex_fi_linop_set_domain_bc / _level_bc / _maxorder (AMReX_linop_fi.cpp:8-40) */
+int mlmg_linop_set_domain_bc(mlmg_linop op, const int lobc[3], const int hibc[3]);
+int mlmg_linop_set_level_bc(mlmg_linop op, int amrlev, mlmg_multifab levelbc);  /* NULL: homogeneous */
+int mlmg_linop_set_maxorder(mlmg_linop op, int maxorder);
+/* amrex_fi_abeclap_set_scalars / _acoeffs / _bcoeffs (AMReX_abeclaplacian_fi.cpp:20-49) */
+int mlmg_abeclap_set_scalars(mlmg_linop op, double alpha, double beta);
+int mlmg_abeclap_set_acoeffs(mlmg_linop op, int amrlev, mlmg_multifab a);
+int mlmg_abeclap_set_acoeffs_const(mlmg_linop op, int amrlev, double a);
+int mlmg_abeclap_set_bcoeffs(mlmg_linop op, int amrlev, const mlmg_multifab b[3]);
+int mlmg_abeclap_set_bcoeffs_const(mlmg_linop op, int amrlev, double b);
+/* number of MG levels of AMR level 0 (built from the LPInfo) */
+int mlmg_linop_num_mg_levels(mlmg_linop op);
+
+/* ------------------------------------------------------------- solver ----
+ * replace amrex_fi_new_multigrid / amrex_fi_multigrid_solve / setters
+ * (Src/F_Interfaces/LinearSolvers/AMReX_multigrid_fi.cpp:8-112), with the
+ * setters of MLMGT (Src/LinearSolvers/MLMG/AMReX_MLMG.H:116-142) */
+int mlmg_new(mlmg_linop op, mlmg_solver* out);
+int mlmg_delete(mlmg_solver s);
+int mlmg_set_verbose(mlmg_solver s, int v);
+int mlmg_set_max_iter(mlmg_solver s, int n);
+int mlmg_set_max_fmg_iter(mlmg_solver s, int n);        /* only 0 (V-cycles) is implemented */
+int mlmg_set_fixed_iter(mlmg_solver s, int n);
+int mlmg_set_pre_smooth(mlmg_solver s, int n);
+int mlmg_set_post_smooth(mlmg_solver s, int n);
+int mlmg_set_final_smooth(mlmg_solver s, int n);
+int mlmg_set_bottom_smooth(mlmg_solver s, int n);
+int mlmg_set_bottom_solver(mlmg_solver s, int which);   /* 0 default, 1 smoother, 2 bicgstab */
+int mlmg_set_bottom_max_iter(mlmg_solver s, int n);
+int mlmg_set_bottom_tolerance(mlmg_solver s, double t);
+int mlmg_set_bottom_tolerance_abs(mlmg_solver s, double t);
+int mlmg_set_always_use_bnorm(mlmg_solver s, int flag);
+/* GB300 additions: 0 = FP64 throughout, 1 = FP32 V-cycles inside FP64
+ * iterative refinement (residual, update, bottom solve and norms in FP64) */
+int mlmg_set_precision(mlmg_solver s, int mode);
+int mlmg_set_graph(mlmg_solver s, int on);               /* replay each iteration as a CUDA graph */
+int mlmg_set_fused_smoother(mlmg_solver s, int on);      /* fused two-colour Gauss-Seidel sweeps */
+
+/* MLMGT::solve (AMReX_MLMG.H:44-51): sol holds the initial guess, rhs the
+ * right-hand side; returns a status, final_resid gets the final max-norm */
+int mlmg_solve(mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, double tol_rel, double tol_abs,
+               double* final_resid);
+/* MLMGT::apply (AMReX_MLMG.H:858-932): out = L(in) with the level BC values */
+int mlmg_apply(mlmg_solver s, mlmg_multifab out, mlmg_multifab in);
+/* getters (AMReX_MLMG.H:220-228) and the device time of the last solve */
+int mlmg_get_num_iters(mlmg_solver s);
+int mlmg_get_residual_history(mlmg_solver s, double* out, int max);
+int mlmg_get_num_cg_iters(mlmg_solver s, int* out, int max);
+double mlmg_get_init_residual(mlmg_solver s);
+double mlmg_get_final_residual(mlmg_solver s);
+double mlmg_get_init_rhs(mlmg_solver s);
+double mlmg_get_solve_time_ms(mlmg_solver s);
+int mlmg_get_num_mg_levels(mlmg_solver s);
+
+/* n independent solves (each with its own operator, solver settings taken
+ * from solvers[0]) run together: every V-cycle stage is one launch over all
+ * solves' patches.  Per-solve statuses go to status[] (may be NULL); the
+ * return value is the worst status. */
+int mlmg_solve_batched(int n, const mlmg_solver* solvers, const mlmg_multifab* sols, const mlmg_multifab* rhss,
+                       double tol_rel, double tol_abs, int* status);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MLMG_CAPI_H_ */
