@@ -305,6 +305,15 @@ class MLMG:
     def setPrecision(self, mode): self._set("mlmg_set_precision", {"fp64": 0, "mixed": 1}.get(mode, mode))
     def setGraph(self, on): self._set("mlmg_set_graph", int(bool(on)))
     def setFusedSmoother(self, on): self._set("mlmg_set_fused_smoother", int(bool(on)))
+    def setTimeKernels(self, on): self._set("mlmg_set_time_kernels", int(bool(on)))
+
+    def smootherStats(self, reset=False):
+        """(total ms, launches, algorithmic bytes per launch) of the
+        finest-level smoother since the last reset."""
+        ms, n, b = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
+        check(capi.lib().mlmg_get_smoother_stats(self._h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(b),
+                                                 int(bool(reset))))
+        return ms.value, n.value, b.value
 
     def solve(self, sol, rhs, tol_rel, tol_abs):
         """Returns the final residual max-norm; raises MLMGError unless the

@@ -80,6 +80,8 @@ SIGNATURES = {
     "mlmg_set_precision": (c_int, [c_void_p, c_int]),
     "mlmg_set_graph": (c_int, [c_void_p, c_int]),
     "mlmg_set_fused_smoother": (c_int, [c_void_p, c_int]),
+    "mlmg_set_time_kernels": (c_int, [c_void_p, c_int]),
+    "mlmg_get_smoother_stats": (c_int, [c_void_p, P(c_double), P(ctypes.c_longlong), P(c_double), c_int]),
     "mlmg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_double, P(c_double)]),
     "mlmg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),
     "mlmg_get_num_iters": (c_int, [c_void_p]),

@@ -800,6 +800,22 @@ SETTER(mlmg_set_always_use_bnorm, always_use_bnorm, int, true)
 SETTER(mlmg_set_precision, precision, int, v == 0 || v == 1)
 SETTER(mlmg_set_graph, use_graph, int, true)
 SETTER(mlmg_set_fused_smoother, fused_smoother, int, true)
+SETTER(mlmg_set_time_kernels, time_kernels, int, true)
+
+int mlmg_get_smoother_stats (mlmg_solver s, double* total_ms, long long* launches, double* bytes_per_launch,
+                             int reset)
+{
+    API_BEGIN
+    MLMG_REQUIRE(s != nullptr, ERR_ARGS, "null handle");
+    Engine* e = s->eng ? s->eng.get() : s->batch_eng.get();
+    MLMG_REQUIRE(e != nullptr, ERR_ARGS, "no solve has run on this solver");
+    const KernelStats& k = e->smoother_stats();
+    if (total_ms) { *total_ms = k.total_ms; }
+    if (launches) { *launches = k.launches; }
+    if (bytes_per_launch) { *bytes_per_launch = k.bytes_per_launch; }
+    if (reset) { e->reset_smoother_stats(); }
+    API_END
+}
 
 int mlmg_set_max_fmg_iter (mlmg_solver s, int n)
 {

@@ -87,14 +87,44 @@ struct Engine::Impl {
     DevBuf<BottomJob> bot_jobs;
     int njobs = 0;
     cudaGraphExec_t graph_exec = nullptr;
-    int graph_key = -1;
+    int graph_launches = 0;      // kernels in one replay of the iteration graph
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // event pairs around the finest-level smoother launches of one iteration
+    std::vector<cudaEvent_t> kev;
+    int kev_used = 0;
+    bool capturing = false;
 
     explicit Impl (Engine& e) : E(e) {}
     ~Impl () {
         if (graph_exec) { cudaGraphExecDestroy(graph_exec); }
         if (ev0) { cudaEventDestroy(ev0); }
         if (ev1) { cudaEventDestroy(ev1); }
+        for (auto e : kev) { cudaEventDestroy(e); }
+    }
+
+    void kev_record ()
+    {
+        if (kev_used >= (int)kev.size()) {
+            cudaEvent_t e;
+            MLMG_CUDA_CHECK(cudaEventCreate(&e));
+            kev.push_back(e);
+        }
+        cudaEvent_t e = kev[kev_used++];
+        if (capturing) {
+            MLMG_CUDA_CHECK(cudaEventRecordWithFlags(e, st(), cudaEventRecordExternal));
+        } else {
+            MLMG_CUDA_CHECK(cudaEventRecord(e, st()));
+        }
+    }
+
+    void kev_harvest ()
+    {
+        for (int q = 0; q + 1 < kev_used; q += 2) {
+            float ms = 0;
+            MLMG_CUDA_CHECK(cudaEventElapsedTime(&ms, kev[q], kev[q + 1]));
+            E.m_kstats.total_ms += ms;
+            E.m_kstats.launches += 1;
+        }
     }
 
     cudaStream_t st () const { return E.m_stream; }
@@ -254,6 +284,18 @@ void Engine::Impl::build ()
     }
     volinv0_d.upload(volinv0, st());
     build_bottom_tables();
+    // algorithmic bytes of one finest-level smoother launch (one colour pass
+    // reads phi, rhs and, for ABec, a, bX, bY, bZ over the whole level and
+    // writes phi: 7 words per cell; Poisson: 3)
+    {
+        double cells = 0;
+        for (int p : lev[0].mg.h_plist) {
+            const PatchDesc& P = lev[0].meta.patches[p];
+            cells += (double)(P.hi[0] - P.lo[0] + 1) * (P.hi[1] - P.lo[1] + 1) * (P.hi[2] - P.lo[2] + 1);
+        }
+        E.m_kstats.cells_per_launch = cells;
+        E.m_kstats.bytes_per_launch = cells * (abec ? 7.0 : 3.0) * (mixed() ? 4.0 : 8.0);
+    }
     MLMG_CUDA_CHECK(cudaEventCreate(&ev0));
     MLMG_CUDA_CHECK(cudaEventCreate(&ev1));
 }
@@ -409,9 +451,11 @@ void Engine::Impl::smooth (int l, T* cor, const T* res, bool skip_fb)
 {
     // MLCellLinOpT::smooth (AMReX_MLCellLinOp.H:1204-1217): per colour, applyBC then Fsmooth
     const LevelData& L = lev[l];
+    const bool timed = E.m_opt.time_kernels && l == 0;
     for (int rb = 0; rb < 2; ++rb) {
         ghost<T>(l, cor, false, !skip_fb);
         skip_fb = false;
+        if (timed) { kev_record(); }
         if (abec) {
             k_gsrb<T, true><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, coef<T>(l, 0),
                 coef<T>(l, 1), coef<T>(l, 2), coef<T>(l, 3), rb);
@@ -420,6 +464,7 @@ void Engine::Impl::smooth (int l, T* cor, const T* res, bool skip_fb)
                 nullptr, nullptr, rb);
         }
         launched();
+        if (timed) { kev_record(); }
     }
 }
 
@@ -511,6 +556,7 @@ void Engine::Impl::residual0 (bool to32)
 void Engine::Impl::one_iteration ()
 {
     LevelData& L0 = lev[0];
+    kev_used = 0;
     bool any_singular = false;
     for (int s : singular) { if (s) { any_singular = true; } }
     if (mixed()) {
@@ -725,21 +771,21 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
     const int niters = m_opt.fixed_iter ? m_opt.fixed_iter : m_opt.max_iter;
     bool any_active = false;
     for (int a : active) { if (a) { any_active = true; } }
-    int per_iter_launches = 0;
+    int& per_iter_launches = I.graph_launches;
     for (int iter = 0; iter < niters && any_active; ++iter) {
         if (m_opt.use_graph) {
             if (I.graph_exec == nullptr) {
                 const int before = m_launches;
                 cudaGraph_t g;
                 MLMG_CUDA_CHECK(cudaStreamBeginCapture(m_stream, cudaStreamCaptureModeThreadLocal));
+                I.capturing = true;
                 I.one_iteration();
+                I.capturing = false;
                 MLMG_CUDA_CHECK(cudaStreamEndCapture(m_stream, &g));
                 MLMG_CUDA_CHECK(cudaGraphInstantiate(&I.graph_exec, g, 0));
                 MLMG_CUDA_CHECK(cudaGraphDestroy(g));
                 per_iter_launches = m_launches - before;
                 m_launches = before;
-            } else if (per_iter_launches == 0) {
-                per_iter_launches = 0;
             }
             MLMG_CUDA_CHECK(cudaGraphLaunch(I.graph_exec, m_stream));
             m_launches += per_iter_launches;
@@ -748,6 +794,7 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
         }
         MLMG_CUDA_CHECK(cudaGetLastError());
         MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
+        if (m_opt.time_kernels) { I.kev_harvest(); }
         bool changed = false;
         for (int s = 0; s < ns; ++s) {
             if (!active[s]) { continue; }

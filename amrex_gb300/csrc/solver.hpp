@@ -36,6 +36,15 @@ struct EngineOptions {
     int use_graph = 0;          // capture one iteration in a CUDA graph and replay it
     int fused_smoother = 0;     // fused two-colour sweeps where a level allows
     int merge_boxes = 1;        // merge a level's boxes into one patch where exact
+    int time_kernels = 0;       // time every finest-level smoother launch with CUDA events
+};
+
+// Live timing of the dominant kernel (the finest-level smoother).
+struct KernelStats {
+    double total_ms = 0;        // summed device time of the timed launches
+    long long launches = 0;
+    double bytes_per_launch = 0;  // algorithmic bytes moved by one launch
+    double cells_per_launch = 0;
 };
 
 struct SolveProblem {           // one solve of a batch
@@ -80,6 +89,8 @@ public:
     double last_solve_ms () const { return m_last_ms; }
     int kernel_launches () const { return m_launches; }
     void reset_launch_count () { m_launches = 0; }
+    const KernelStats& smoother_stats () const { return m_kstats; }
+    void reset_smoother_stats () { m_kstats.total_ms = 0; m_kstats.launches = 0; }
 
     struct Impl;
 private:
@@ -89,6 +100,7 @@ private:
     std::vector<SolveReport> m_reports;
     double m_last_ms = 0;
     int m_launches = 0;
+    KernelStats m_kstats;
     std::unique_ptr<Impl> m_impl;
 };
 

@@ -1,0 +1,346 @@
+#!/usr/bin/env python
+"""Benchmark: MLMG time to a 1e-10 relative residual on the 256^3
+variable-coefficient MLABecLaplacian (alpha = a = beta = 1, face b =
+exp(kappa g) of a smoothed Gaussian random field with max/min contrast 1e3,
+Gaussian-blob RHS, homogeneous Dirichlet, max_grid_size 64), mixed precision
+(FP32 V-cycles inside FP64 refinement, CUDA-graph replay) on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One step = one full solve from a zero initial guess.  Inputs (256^3 FP64
+arrays of 134 MB, larger than the 129 MB L2) stay resident in HBM for the
+device-timed `value`; `e2e` repeats the step through the C ABI with host
+buffers (RHS upload and solution download inside the timed region).  Under
+torchrun every rank solves its own replica (no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 256
+MGS = 64
+RHS_SEED, B_SEED = 1001, 2001
+TOL_REL = 1e-10
+# V-cycles the reference AMReX CPU MLMG needs on this workload (measured with
+# the reference built from its sources, 16 iterations to 2.67e-11); used to
+# scale the CPU baseline's timed sample of V-cycles to a full solve
+REF_ITERS = 16
+CPU_SAMPLE_VCYCLES = 2
+METRIC = "MLMG time-to-1e-10 residual, 256^3 variable-coefficient ABecLaplacian, mixed FP32/FP64"
+
+
+def workload_config():
+    return {"workload": f"MLABecLaplacian {N}^3, max_grid_size {MGS} ({(N // MGS) ** 3} boxes), log-normal b "
+                        f"(contrast 1e3, 5-cell Gaussian field), Gaussian-blob RHS, Dirichlet, tol_rel 1e-10",
+            "n": N, "max_grid_size": MGS, "rhs_seed": RHS_SEED, "b_seed": B_SEED,
+            "precision": "FP32 V-cycle in FP64 iterative refinement", "cuda_graph": True,
+            "l2": "inputs larger than L2 (134 MB FP64 arrays vs 129 MB L2), no flush"}
+
+
+def make_inputs():
+    from amrex_gb300 import synth
+    rhs = synth.gaussian_rhs(N, RHS_SEED)
+    bx, by, bz = synth.lognormal_bcoef(N, B_SEED, sigma_cells=5.0, max_ratio=1e3)
+    return rhs, (bx, by, bz)
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def barrier_max(v, ws):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return None
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                try:
+                    rows.append((float(p[1]), float(p[2]), p[5], p[6], p[7], p[8]))
+                except ValueError:
+                    pass
+        if not rows:
+            return None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[2:]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch(mode):
+    """dram bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/traffic.json), scaled to this workload; None if absent."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    e = d.get(mode)
+    if not e:
+        return None
+    return float(e["bytes_per_cell"]) * N ** 3
+
+
+def cpu_baseline(rhs, bcoef):
+    """The C restatement of the reference MLMG (oracle) on the host cores:
+    a sample of CPU_SAMPLE_VCYCLES V-cycles of the same solve, scaled to the
+    reference's REF_ITERS V-cycles."""
+    import multiprocessing
+    cores = multiprocessing.cpu_count()
+    from oracle import oracle
+    from tests.golden import cases
+    c = cases._c(mode="solve", op="abec", n=(N, N, N), max_grid_size=MGS, fixed_iter=CPU_SAMPLE_VCYCLES)
+    arrays = {"sol": np.zeros((N + 2,) * 3), "rhs": rhs, "a": np.ones((N,) * 3),
+              "bx": bcoef[0], "by": bcoef[1], "bz": bcoef[2]}
+    _, info = oracle.solve(c, arrays)
+    per_iter = info["iter_seconds"] / CPU_SAMPLE_VCYCLES
+    return {"value": per_iter * REF_ITERS * 1e3, "unit": "ms", "cores": cores, "kind": "port",
+            "sample": f"{CPU_SAMPLE_VCYCLES} V-cycles of the {N}^3 FP64 solve (setup excluded), OpenMP on "
+                      f"{cores} threads, scaled to the reference's {REF_ITERS} V-cycles"}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    import multiprocessing
+    os.environ.setdefault("OMP_NUM_THREADS", str(multiprocessing.cpu_count()))
+    rhs, bcoef = make_inputs()
+    vals = []
+    for s in range(args.warmup + args.steps):
+        cb = cpu_baseline(rhs, bcoef)
+        if s >= args.warmup:
+            vals.append(cb["value"])
+    v = statistics.median(vals)
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": workload_config(),
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, ws, rank, local):
+    import torch
+    import amrex_gb300 as ag
+    from amrex_gb300 import capi
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA GPU")
+    torch.cuda.set_device(local)
+    rhs_h, bcoef_h = make_inputs()
+    domain = ag.Box((0, 0, 0), (N - 1, N - 1, N - 1))
+    ba = ag.BoxArray(domain).maxSize(MGS)
+    dm = ag.DistributionMapping(ba)
+    geom = ag.Geometry(domain)
+    sol = ag.MultiFab(ba, dm, 1, 1)
+    rhs = ag.MultiFab(ba, dm, 1, 0)
+    rhs.set_global(rhs_h)
+    op = ag.MLABecLaplacian(geom, ba, dm)
+    op.setDomainBC((101,) * 3, (101,) * 3)
+    op.setLevelBC(0, None)
+    op.setScalars(1.0, 1.0)
+    op.setACoeffs(0, 1.0)
+    faces = []
+    for d in range(3):
+        f = ag.MultiFab(ba, dm, 1, 0, nodal_dir=d)
+        f.set_global(bcoef_h[d])
+        faces.append(f)
+    op.setBCoeffs(0, faces)
+    mixed = ag.MLMG(op)
+    mixed.setPrecision("mixed")
+    mixed.setGraph(True)
+    mixed.setTimeKernels(True)
+    fp64 = ag.MLMG(op)
+    fp64.setPrecision("fp64")
+    fp64.setTimeKernels(True)
+
+    stream = torch.cuda.ExternalStream(capi.lib().mlmg_stream())
+
+    def step(m):
+        sol.setVal(0.0)
+        m.solve(sol, rhs, TOL_REL, 0.0)
+
+    # --- plain FP64 GPU MLMG (the comparator), also the phi reference
+    for _ in range(2):
+        step(fp64)
+    fp64.smootherStats(reset=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nfp = max(2, min(args.steps, 5))
+    barrier(ws)
+    e0.record(stream)
+    for _ in range(nfp):
+        step(fp64)
+    e1.record(stream)
+    e1.synchronize()
+    fp64_ms = e0.elapsed_time(e1) / nfp
+    fp64_iters = fp64.getNumIters()
+    fp64_sm = fp64.smootherStats(reset=True)
+    phi64 = sol.get_global((N, N, N))
+
+    # --- mixed + graph: the headline
+    for _ in range(args.warmup):
+        step(mixed)
+    mixed.smootherStats(reset=True)
+    ag.kernel_launches(reset=True)
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(mixed)
+        e1.record(stream)
+        e1.synchronize()
+    launches = ag.kernel_launches()
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = barrier_max(ms, ws)
+    sm_ms, sm_n, sm_bytes = mixed.smootherStats(reset=True)
+    iters = mixed.getNumIters()
+    phim = sol.get_global((N, N, N))
+    rel_diff = float(np.abs(phim - phi64).max() / np.abs(phi64).max())
+
+    # --- end to end through the C ABI with host buffers
+    sol_h = np.zeros((N, N, N))
+    ne2e = max(2, min(args.steps, 5))
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(ne2e):
+        rhs.set_global(rhs_h)               # host -> device
+        sol.setVal(0.0)
+        mixed.solve(sol, rhs, TOL_REL, 0.0)
+        sol.get_global((N, N, N), out=sol_h)  # device -> host
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / ne2e
+    e2e_ms = barrier_max(e2e_ms, ws)
+
+    peak, peak_kind = peaks()
+    avg_launch_ms = sm_ms / max(sm_n, 1)
+    achieved = sm_bytes / (avg_launch_ms * 1e-3) / 1e9 if sm_n else None
+    traffic = traffic_per_launch("mixed")
+    line = {
+        "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 V-cycle / f64 residual", "data": "synthetic (seeded generators, no dataset)",
+        "config": workload_config(),
+        "iters": iters, "fp64_ms": fp64_ms, "fp64_iters": fp64_iters, "speedup_vs_fp64": fp64_ms / ms,
+        "phi_rel_diff_vs_fp64": rel_diff,
+        "roofline": {"kernel": "finest-level red-black Gauss-Seidel colour pass (FP32)", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
+                     "traffic": traffic, "bytes_per_launch": sm_bytes, "avg_launch_ms": avg_launch_ms,
+                     "launches_timed": sm_n,
+                     "fp64_smoother": {"avg_launch_ms": fp64_sm[0] / max(fp64_sm[1], 1),
+                                       "achieved": (fp64_sm[2] / (fp64_sm[0] / max(fp64_sm[1], 1) * 1e-3) / 1e9)
+                                       if fp64_sm[1] else None}},
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(rhs_h.nbytes),
+                "d2h_bytes_per_step": int(sol_h.nbytes)},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        import multiprocessing
+        os.environ.setdefault("OMP_NUM_THREADS", str(multiprocessing.cpu_count()))
+        line["cpu_baseline"] = cpu_baseline(rhs_h, bcoef_h)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_gb300(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -149,6 +149,11 @@ int mlmg_set_always_use_bnorm(mlmg_solver s, int flag);
 int mlmg_set_precision(mlmg_solver s, int mode);
 int mlmg_set_graph(mlmg_solver s, int on);               /* replay each iteration as a CUDA graph */
 int mlmg_set_fused_smoother(mlmg_solver s, int on);      /* fused two-colour Gauss-Seidel sweeps */
+/* time every finest-level smoother launch with CUDA events on the library
+ * stream (graph replays included); the stats accumulate until reset */
+int mlmg_set_time_kernels(mlmg_solver s, int on);
+int mlmg_get_smoother_stats(mlmg_solver s, double* total_ms, long long* launches, double* bytes_per_launch,
+                            int reset);
 
 /* MLMGT::solve (AMReX_MLMG.H:44-51): sol holds the initial guess, rhs the
  * right-hand side; returns a status, final_resid gets the final max-norm */

@@ -22,6 +22,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "mlmg_oracle.h"
 
@@ -96,6 +97,15 @@ static void mf_setval(MF* m, double v) {
     }
 }
 #define FOR_VALID(f, i, j, k) \
+    for (int k = (f)->bx.lo[2]; k <= (f)->bx.hi[2]; ++k) \
+    for (int j = (f)->bx.lo[1]; j <= (f)->bx.hi[1]; ++j) \
+    for (int i = (f)->bx.lo[0]; i <= (f)->bx.hi[0]; ++i)
+
+/* The same loop with the k planes spread over OpenMP threads.  Used only
+ * where every iteration writes its own cell and reads cells nobody writes
+ * in that loop, so results do not depend on the thread count. */
+#define FOR_VALID_PAR(f, i, j, k) \
+    _Pragma("omp parallel for schedule(static)") \
     for (int k = (f)->bx.lo[2]; k <= (f)->bx.hi[2]; ++k) \
     for (int j = (f)->bx.lo[1]; j <= (f)->bx.hi[1]; ++j) \
     for (int i = (f)->bx.lo[0]; i <= (f)->bx.hi[0]; ++i)
@@ -477,7 +487,7 @@ static void fapply(const Hier* H, const Level* L, MF* out, const MF* in) {
             const Fab* bX = &L->bcoef[0].fab[b];
             const Fab* bY = &L->bcoef[1].fab[b];
             const Fab* bZ = &L->bcoef[2].fab[b];
-            FOR_VALID(y, i, j, k) {
+            FOR_VALID_PAR(y, i, j, k) {
                 A(y, i, j, k) = H->alpha * A(a, i, j, k) * A(x, i, j, k)
                     - dhx * (A(bX, i + 1, j, k) * (A(x, i + 1, j, k) - A(x, i, j, k))
                            - A(bX, i, j, k) * (A(x, i, j, k) - A(x, i - 1, j, k)))
@@ -490,7 +500,7 @@ static void fapply(const Hier* H, const Level* L, MF* out, const MF* in) {
             const double dhx = L->dxinv[0] * L->dxinv[0];
             const double dhy = L->dxinv[1] * L->dxinv[1];
             const double dhz = L->dxinv[2] * L->dxinv[2];
-            FOR_VALID(y, i, j, k) {
+            FOR_VALID_PAR(y, i, j, k) {
                 A(y, i, j, k) = dhx * (A(x, i - 1, j, k) - 2.0 * A(x, i, j, k) + A(x, i + 1, j, k))
                     + dhy * (A(x, i, j - 1, k) - 2.0 * A(x, i, j, k) + A(x, i, j + 1, k))
                     + dhz * (A(x, i, j, k - 1) - 2.0 * A(x, i, j, k) + A(x, i, j, k + 1));
@@ -520,7 +530,7 @@ static void fsmooth(const Hier* H, const Level* L, MF* sol, const MF* rhs, int r
             dhy = L->dxinv[1] * L->dxinv[1];
             dhz = L->dxinv[2] * L->dxinv[2];
         }
-        FOR_VALID(r, i, j, k) {
+        FOR_VALID_PAR(r, i, j, k) {
             if ((i + j + k + redblack) % 2 != 0) continue;
             double cf0 = (i == vb->lo[0] && A(m[0], vb->lo[0] - 1, j, k) > 0) ? A(fc[0], vb->lo[0], j, k) : 0.0;
             double cf1 = (j == vb->lo[1] && A(m[1], i, vb->lo[1] - 1, k) > 0) ? A(fc[1], i, vb->lo[1], k) : 0.0;
@@ -573,6 +583,7 @@ static void normalize(const Hier* H, const Level* L, MF* x) {
         const Fab* bY = &L->bcoef[1].fab[b];
         const Fab* bZ = &L->bcoef[2].fab[b];
         Box vb = L->boxes[b];
+#pragma omp parallel for schedule(static)
         for (int k = vb.lo[2]; k <= vb.hi[2]; ++k)
         for (int j = vb.lo[1]; j <= vb.hi[1]; ++j)
         for (int i = vb.lo[0]; i <= vb.hi[0]; ++i) {
@@ -623,6 +634,7 @@ static void mf_axpy(const Level* L, MF* dst, double a, const MF* src, int op) {
         Box vb = L->boxes[b];
         Fab* d = &dst->fab[b];
         const Fab* s = &src->fab[b];
+#pragma omp parallel for schedule(static)
         for (int k = vb.lo[2]; k <= vb.hi[2]; ++k)
         for (int j = vb.lo[1]; j <= vb.hi[1]; ++j)
         for (int i = vb.lo[0]; i <= vb.hi[0]; ++i) {
@@ -653,6 +665,7 @@ static void restriction(const Hier* H, const Level* Lf, const MF* fine, const Le
     for (int b = 0; b < crse->nbox; ++b) {
         Fab* c = &crse->fab[b];
         Box vb = Lc->boxes[b];
+#pragma omp parallel for schedule(static)
         for (int k = vb.lo[2]; k <= vb.hi[2]; ++k)
         for (int j = vb.lo[1]; j <= vb.hi[1]; ++j)
         for (int i = vb.lo[0]; i <= vb.hi[0]; ++i) {
@@ -675,6 +688,7 @@ static void interp_add(const Hier* H, const Level* Lc, const MF* crse, const Lev
     for (int b = 0; b < fine->nbox; ++b) {
         Fab* f = &fine->fab[b];
         Box vb = Lf->boxes[b];
+#pragma omp parallel for schedule(static)
         for (int k = vb.lo[2]; k <= vb.hi[2]; ++k)
         for (int j = vb.lo[1]; j <= vb.hi[1]; ++j)
         for (int i = vb.lo[0]; i <= vb.hi[0]; ++i) {
@@ -1099,6 +1113,8 @@ int oracle_solve(const OracleProblem* P, const OracleOptions* o, double* phi_out
     double res_target = o->tol_abs > tr * max_norm ? o->tol_abs : tr * max_norm;
     R->init_resid = resnorm0; R->rhs_norm = rhsnorm0; R->niters = 0; R->status = 0;
     double composite = resnorm0;
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
     if (resnorm0 > res_target) {
         int converged = 0;
         int niters = o->fixed_iter ? o->fixed_iter : o->max_iter;
@@ -1117,6 +1133,8 @@ int oracle_solve(const OracleProblem* P, const OracleOptions* o, double* phi_out
         }
         if (!converged && o->fixed_iter == 0 && R->status == 0) R->status = 1;
     }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    R->iter_seconds = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
     R->final_resid = composite;
     R->nlev = H->nlev;
     copy_mf_to_global(L0, &S->sol, phi_out);

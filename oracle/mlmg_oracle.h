@@ -35,6 +35,7 @@ typedef struct {
 typedef struct {
     int status, niters, nlev;
     double init_resid, rhs_norm, final_resid;
+    double iter_seconds;   /* wall time of the iteration loop (setup excluded) */
     double history[ORACLE_MAX_HIST];
     int cg_iters[ORACLE_MAX_HIST];
 } OracleResult;

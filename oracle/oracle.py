@@ -24,8 +24,8 @@ def build(force=False):
             os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "mlmg_oracle.h"))):
         return LIB
     tmp = LIB + ".tmp.%d" % os.getpid()
-    subprocess.run(["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-o", tmp, SRC, "-lm"],
-                   check=True)
+    subprocess.run(["gcc", "-O2", "-std=gnu11", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off", "-o", tmp,
+                    SRC, "-lm"], check=True)
     os.replace(tmp, LIB)
     return LIB
 
@@ -52,6 +52,7 @@ class Options(ctypes.Structure):
 class Result(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("niters", ctypes.c_int), ("nlev", ctypes.c_int),
                 ("init_resid", ctypes.c_double), ("rhs_norm", ctypes.c_double), ("final_resid", ctypes.c_double),
+                ("iter_seconds", ctypes.c_double),
                 ("history", ctypes.c_double * MAX_HIST), ("cg_iters", ctypes.c_int * MAX_HIST)]
 
 
@@ -166,6 +167,7 @@ def solve(case, arrays):
     r = Result()
     lib().oracle_solve(ctypes.byref(p), ctypes.byref(o), _dp(phi), ctypes.byref(r))
     info = dict(status=r.status, niters=r.niters, nlev=r.nlev, init_resid=r.init_resid, rhs_norm=r.rhs_norm,
-                final_resid=r.final_resid, history=list(r.history[:min(r.niters, MAX_HIST)]),
+                final_resid=r.final_resid, iter_seconds=r.iter_seconds,
+                history=list(r.history[:min(r.niters, MAX_HIST)]),
                 cg_iters=list(r.cg_iters[:min(r.niters, MAX_HIST)]))
     return phi, info

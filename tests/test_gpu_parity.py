@@ -66,7 +66,10 @@ def test_fp64_solve_matches_reference(name):
     r = g["result"]
     assert prob["mlmg"].getNumIters() == r["niters"]
     assert prob["mlmg"].getNumCGIters() == r["cg_iters"]
-    np.testing.assert_allclose(prob["mlmg"].getResidualHistory(), r["history"], rtol=1e-6)
+    # the last residuals sit near the rounding floor; FMA contraction on the
+    # GPU moves them by ~1e-15 of the initial norm
+    np.testing.assert_allclose(prob["mlmg"].getResidualHistory(), r["history"], rtol=1e-6,
+                               atol=1e-13 * max(r["rhs_norm"], r["init_resid"]))
     assert np.abs(phi - ref).max() <= 1e-10 * np.abs(ref).max()
 
 
