@@ -50,6 +50,7 @@ SIGNATURES = {
     "mlmg_multifab_setval": (c_int, [c_void_p, c_double]),
     "mlmg_multifab_fill_boundary": (c_int, [c_void_p, c_void_p, c_int]),
     "mlmg_multifab_norminf": (c_int, [c_void_p, P(c_double)]),
+    "mlmg_multifab_norminf_noalloc": (c_int, [c_void_p, P(c_double)]),
     "mlmg_linop_new_poisson": (c_int, [c_int, P(c_void_p), P(c_void_p), P(c_void_p), P(LPInfoC), P(c_void_p)]),
     "mlmg_linop_new_abeclap": (c_int, [c_int, P(c_void_p), P(c_void_p), P(c_void_p), P(LPInfoC), P(c_void_p)]),
     "mlmg_linop_delete": (c_int, [c_void_p]),

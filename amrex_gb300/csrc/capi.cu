@@ -619,6 +619,100 @@ int mlmg_multifab_norminf (mlmg_multifab mf, double* out)
     API_END
 }
 
+} // extern "C"
+
+// ------------------------------------------------ allocation-free max-norm --
+// mlmg_multifab_norminf_noalloc keeps its scratch -- the per-box table of
+// valid regions, the prefix of their cell counts and the result word -- in
+// this file-scope device array instead of memory allocated per call.  Every
+// GPU that loads the library holds the array until the process exits.
+namespace {
+
+constexpr int kNoAllocMaxBoxes = 4096;
+constexpr size_t kNoAllocRegionsOff = 0;
+constexpr size_t kNoAllocStartOff = ((kNoAllocMaxBoxes * sizeof(Box3) + 255) / 256) * 256;
+constexpr size_t kNoAllocResultOff =
+    ((kNoAllocStartOff + (kNoAllocMaxBoxes + 1) * sizeof(long long) + 255) / 256) * 256;
+constexpr size_t kNoAllocBytes = kNoAllocResultOff + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mutex;
+constexpr int kNoAllocMaxDevices = 256;
+void* g_noalloc_dptr[kNoAllocMaxDevices] = {};      // device address of the array, per device
+Box3 g_noalloc_regions[kNoAllocMaxBoxes];            // host staging of the tables
+long long g_noalloc_start[kNoAllocMaxBoxes + 1];
+
+// first call on a device: look up the array's device address with that
+// device current (the array's name is only a stand-in in host code)
+char* noalloc_scratch_for_current_device ()
+{
+    int dev = -1;
+    MLMG_CUDA_CHECK(cudaGetDevice(&dev));
+    MLMG_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, ERR_UNSUPPORTED, "device index out of range");
+    if (g_noalloc_dptr[dev] == nullptr) {
+        void* p = nullptr;
+        MLMG_CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        MLMG_REQUIRE(p != nullptr, ERR_CUDA, "cudaGetSymbolAddress returned a null address");
+        g_noalloc_dptr[dev] = p;
+    }
+    return static_cast<char*>(g_noalloc_dptr[dev]);
+}
+
+} // namespace
+
+extern "C" {
+
+int mlmg_multifab_norminf_noalloc (mlmg_multifab mf, double* out)
+{
+    API_BEGIN
+    MLMG_REQUIRE(mf != nullptr && out != nullptr, ERR_ARGS, "bad arguments");
+    const int nbox = (int)mf->boxes.size();
+    MLMG_REQUIRE(nbox <= kNoAllocMaxBoxes, ERR_ARGS,
+                 "mlmg_multifab_norminf_noalloc handles at most 4096 boxes; this MultiFab has " +
+                 std::to_string(nbox));
+    std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+    char* base = noalloc_scratch_for_current_device();
+    Box3* d_regions = reinterpret_cast<Box3*>(base + kNoAllocRegionsOff);
+    long long* d_start = reinterpret_cast<long long*>(base + kNoAllocStartOff);
+    unsigned long long* d_result = reinterpret_cast<unsigned long long*>(base + kNoAllocResultOff);
+    g_noalloc_start[0] = 0;
+    for (int b = 0; b < nbox; ++b) {
+        Box3 v = mf->boxes[b];
+        if (mf->nodal_dir >= 0) { v.hi[mf->nodal_dir] += 1; }
+        g_noalloc_regions[b] = v;
+        g_noalloc_start[b + 1] = g_noalloc_start[b] + v.npts();
+    }
+    const long long n = g_noalloc_start[nbox];
+    cudaStream_t st = lib_stream();
+    if (nbox > 0) {
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(d_regions, g_noalloc_regions, sizeof(Box3) * nbox, cudaMemcpyHostToDevice, st));
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(d_start, g_noalloc_start, sizeof(long long) * (nbox + 1),
+                                        cudaMemcpyHostToDevice, st));
+    }
+    // the array keeps the previous call's result: the maximum starts at zero
+    MLMG_CUDA_CHECK(cudaMemsetAsync(d_result, 0, sizeof(unsigned long long), st));
+    if (n > 0) {
+        const unsigned nb = (unsigned)std::min<long long>(grid_for(n, 256), 152 * 8);
+        if (mf->prec == 8) {
+            k_fab_maxabs<double><<<nb, 256, 0, st>>>(mf->dinfo.p, d_regions, d_start, nbox, n,
+                                                     (const double*)mf->data.p, d_result);
+        } else {
+            k_fab_maxabs<float><<<nb, 256, 0, st>>>(mf->dinfo.p, d_regions, d_start, nbox, n,
+                                                    (const float*)mf->data.p, d_result);
+        }
+        g_launches++;
+        MLMG_CUDA_CHECK(cudaGetLastError());
+    }
+    unsigned long long bits = 0;
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(&bits, d_result, sizeof(bits), cudaMemcpyDeviceToHost, st));
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+    double v;
+    std::memcpy(&v, &bits, sizeof(v));
+    *out = v;
+    API_END
+}
+
 // --------------------------------------------------------------- linop ----
 static int linop_new (int is_abec, int nlev, const mlmg_geometry* geom, const mlmg_boxarray* ba,
                       const mlmg_distromap* dm, const mlmg_lpinfo* info, mlmg_linop* out)

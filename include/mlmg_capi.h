@@ -103,6 +103,20 @@ int mlmg_multifab_setval(mlmg_multifab mf, double v);                    /* FabA
 /* FabArray::FillBoundary (Src/Base/AMReX_FabArray.H:1000-1044), one rank */
 int mlmg_multifab_fill_boundary(mlmg_multifab mf, mlmg_geometry geom, int cross);
 int mlmg_multifab_norminf(mlmg_multifab mf, double* out);                /* valid cells */
+/* Same result as mlmg_multifab_norminf, for callers that must not allocate
+ * device memory: a caller whose device memory is already fully claimed by its
+ * own allocator (a framework's caching allocator holding the HBM), or a time-
+ * step loop where a cudaMalloc/cudaFree -- which can synchronise the whole
+ * device -- is not acceptable.  No counterpart in the reference.  The call
+ * allocates nothing: its scratch (box table and result word) is a static
+ * device array of 131,584 bytes that every GPU loading the library keeps
+ * until the process exits.  At most 4096 boxes (more returns -1 with a
+ * message).  The first call on a device looks up that array's device address
+ * with the device current; make that first call before any stream capture.
+ * Every call shares the array, which keeps the last call's contents; each
+ * call clears the result word before use, and calls that overlap on the GPU
+ * race (calls through this library are serialised by a lock). */
+int mlmg_multifab_norminf_noalloc(mlmg_multifab mf, double* out);
 
 /* ------------------------------------------------- linear operators -----
  * replace amrex_fi_new_poisson (Src/F_Interfaces/LinearSolvers/AMReX_poisson_fi.cpp:8-30)
