@@ -11,7 +11,7 @@
 
 namespace mlmg {
 
-constexpr int BOTTOM_THREADS = 512;
+constexpr int BOTTOM_THREADS = 128;
 
 struct BottomLevelPtrs {       // one level that is the bottom of some solve
     DevLevel L;

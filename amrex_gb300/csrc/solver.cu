@@ -1,6 +1,8 @@
 // The batched MLMG engine: host orchestration of the V-cycle stages.
 #include "solver.hpp"
 #include "bottom.cuh"
+#include "stencil_kernels.cuh"
+#include "fused_sweep.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -64,7 +66,16 @@ struct LevelData {
     DevBuf<double> cor, res, rescor, a, bx, by, bz;
     DevBuf<double> sol, rhs, bcval;                 // level 0 only
     // FP32 fields (mixed precision)
-    DevBuf<float> cor32, res32, rescor32, a32, bx32, by32, bz32;
+    DevBuf<float> cor32, res32, rescor32;
+    // stencil form of the ABec operator (mixed path): FP64 on every level,
+    // FP32 copies for the FP32 V-cycle
+    DevBuf<double> D, sx, sy, sz;
+    DevBuf<float> D32, sx32, sy32, sz32;
+    bool inline_bc = false;   // ghost values computed inside the stencil kernels
+    // fused two-colour sweeps (mixed path): tile map and the second buffer
+    bool fused = false;
+    SubsetData fz;
+    DevBuf<float> cor32b;
     // bottom work arrays
     DevBuf<double> bw[7];
     bool has_bottom = false;
@@ -147,6 +158,11 @@ struct Engine::Impl {
     template <typename T> T* field_rescor (int l);
     template <typename T> const T* coef (int l, int which);
     void reduce_per_solve (int l, const SubsetData& S, int op, const double* x, const double* y);
+    StencilPtrs stencil32 (int l) const;
+    StencilPtrs stencil64 (int l) const;
+    void gsrb32 (int l, float* cor, const float* res, int rb);
+    void smooth_fused (int l, int n);
+    void resid32 (int l, float* rescor, float* cor, const float* res);
     void residual0 (bool to32);   // res[0] (FP64, or FP32 in mixed) and per-block max|r|
     void one_iteration ();
 };
@@ -162,11 +178,6 @@ template <> const double* Engine::Impl::coef<double> (int l, int w)
 {
     const LevelData& L = lev[l];
     return w == 0 ? L.a.p : (w == 1 ? L.bx.p : (w == 2 ? L.by.p : L.bz.p));
-}
-template <> const float* Engine::Impl::coef<float> (int l, int w)
-{
-    const LevelData& L = lev[l];
-    return w == 0 ? L.a32.p : (w == 1 ? L.bx32.p : (w == 2 ? L.by32.p : L.bz32.p));
 }
 
 // --------------------------------------------------------------- build ----
@@ -243,6 +254,29 @@ void Engine::Impl::build ()
         build_subset(L.all, M, all, nsolve, st());
         build_subset(L.mg, M, mg, nsolve, st());
         max_tiles = std::max(max_tiles, (size_t)L.all.ntiles);
+        // inline ghost values: no intra-level copies, and every face closed by
+        // a BC of at most two interior cells
+        L.inline_bc = M.tags.empty();
+        for (const auto& P : M.patches) {
+            for (int f = 0; f < 6; ++f) {
+                const FaceBC& F = P.face[f];
+                const bool closure = (F.type == BC_DIRICHLET && F.nx <= 3) || F.type == BC_NEUMANN ||
+                                     F.type == BC_REFLECT_ODD;
+                if (F.mask_uniform < 1 || !closure) { L.inline_bc = false; }
+            }
+        }
+        L.fused = E.m_opt.fused_smoother && mixed() && L.inline_bc && !mg.empty();
+        if (L.fused) {
+            // same patches as the mg subset, tiled for the fused sweep
+            SubsetData& S = L.fz;
+            S.h_plist = mg;
+            S.n = (int)mg.size();
+            S.h_tstart.assign(S.n + 1, 0);
+            for (int q = 0; q < S.n; ++q) { S.h_tstart[q + 1] = S.h_tstart[q] + fused_tiles_of(M.patches[mg[q]]); }
+            S.ntiles = S.h_tstart[S.n];
+            S.plist.upload(S.h_plist, st());
+            S.tstart.upload(S.h_tstart, st());
+        }
         // fields
         const size_t n = (size_t)M.nelem;
         auto alloc0 = [&] (DevBuf<double>& b) { b.alloc(n); b.zero(st()); };
@@ -251,7 +285,11 @@ void Engine::Impl::build ()
         if (l == 0) { alloc0(L.sol); alloc0(L.rhs); alloc0(L.res); }
         if (mixed()) {
             alloc0f(L.cor32); alloc0f(L.res32); alloc0f(L.rescor32);
-            if (abec) { alloc0f(L.a32); alloc0f(L.bx32); alloc0f(L.by32); alloc0f(L.bz32); }
+            if (L.fused) { alloc0f(L.cor32b); }
+            if (abec) {
+                alloc0(L.D); alloc0(L.sx); alloc0(L.sy); alloc0(L.sz);
+                alloc0f(L.D32); alloc0f(L.sx32); alloc0f(L.sy32); alloc0f(L.sz32);
+            }
         } else {
             alloc0(L.cor); if (l > 0) { alloc0(L.res); } alloc0(L.rescor);
         }
@@ -446,6 +484,87 @@ void Engine::Impl::ghost (int l, T* phi, bool inhomog, bool do_copy)
     launched();
 }
 
+StencilPtrs Engine::Impl::stencil32 (int l) const
+{
+    const LevelData& L = lev[l];
+    return StencilPtrs{L.D32.p, L.sx32.p, L.sy32.p, L.sz32.p};
+}
+
+StencilPtrs Engine::Impl::stencil64 (int l) const
+{
+    const LevelData& L = lev[l];
+    return StencilPtrs{L.D.p, L.sx.p, L.sy.p, L.sz.p};
+}
+
+// one FP32 colour pass in stencil form (mixed path)
+void Engine::Impl::gsrb32 (int l, float* cor, const float* res, int rb)
+{
+    const LevelData& L = lev[l];
+    const StencilPtrs S = stencil32(l);
+    const unsigned g = (unsigned)L.mg.ntiles;
+    if (abec) {
+        if (L.inline_bc) { k_gsrb_s<float, true, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, S, rb); }
+        else { k_gsrb_s<float, true, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, S, rb); }
+    } else {
+        if (L.inline_bc) { k_gsrb_s<float, false, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, S, rb); }
+        else { k_gsrb_s<float, false, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, S, rb); }
+    }
+    launched();
+}
+
+// rescor = res - L(cor), homogeneous BCs, FP32 stencil form (mixed path)
+void Engine::Impl::resid32 (int l, float* rescor, float* cor, const float* res)
+{
+    const LevelData& L = lev[l];
+    if (!L.inline_bc) { ghost<float>(l, cor, false, true); }
+    const StencilPtrs S = stencil32(l);
+    const unsigned g = (unsigned)L.mg.ntiles;
+    if (abec) {
+        if (L.inline_bc) {
+            k_residual_s<float, float, true, true, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor,
+                                                                                       res, S, nullptr, nullptr);
+        } else {
+            k_residual_s<float, float, true, false, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor,
+                                                                                        res, S, nullptr, nullptr);
+        }
+    } else {
+        if (L.inline_bc) {
+            k_residual_s<float, float, false, true, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor,
+                                                                                        res, S, nullptr, nullptr);
+        } else {
+            k_residual_s<float, float, false, false, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor,
+                                                                                         res, S, nullptr, nullptr);
+        }
+    }
+    launched();
+}
+
+// n fused two-colour sweeps on level l (mixed path), ping-ponging between
+// cor32 and cor32b and ending in cor32
+void Engine::Impl::smooth_fused (int l, int n)
+{
+    LevelData& L = lev[l];
+    const bool timed = E.m_opt.time_kernels && l == 0;
+    float* a = L.cor32.p;
+    float* b = L.cor32b.p;
+    const StencilPtrs S = stencil32(l);
+    for (int i = 0; i < n; ++i) {
+        if (timed) { kev_record(); }
+        if (abec) {
+            k_sweep_fused<true><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);
+        } else {
+            k_sweep_fused<false><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);
+        }
+        launched();
+        if (timed) { kev_record(); }
+        std::swap(a, b);
+    }
+    if (a != L.cor32.p) {
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(L.cor32.p, a, sizeof(float) * (size_t)L.meta.nelem, cudaMemcpyDeviceToDevice,
+                                        st()));
+    }
+}
+
 template <typename T>
 void Engine::Impl::smooth (int l, T* cor, const T* res, bool skip_fb)
 {
@@ -453,17 +572,25 @@ void Engine::Impl::smooth (int l, T* cor, const T* res, bool skip_fb)
     const LevelData& L = lev[l];
     const bool timed = E.m_opt.time_kernels && l == 0;
     for (int rb = 0; rb < 2; ++rb) {
-        ghost<T>(l, cor, false, !skip_fb);
+        if constexpr (std::is_same_v<T, float>) {
+            if (!L.inline_bc) { ghost<T>(l, cor, false, !skip_fb); }
+        } else {
+            ghost<T>(l, cor, false, !skip_fb);
+        }
         skip_fb = false;
         if (timed) { kev_record(); }
-        if (abec) {
-            k_gsrb<T, true><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, coef<T>(l, 0),
-                coef<T>(l, 1), coef<T>(l, 2), coef<T>(l, 3), rb);
+        if constexpr (std::is_same_v<T, float>) {
+            gsrb32(l, cor, res, rb);
         } else {
-            k_gsrb<T, false><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, nullptr, nullptr,
-                nullptr, nullptr, rb);
+            if (abec) {
+                k_gsrb<T, true><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, coef<T>(l, 0),
+                    coef<T>(l, 1), coef<T>(l, 2), coef<T>(l, 3), rb);
+            } else {
+                k_gsrb<T, false><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, nullptr, nullptr,
+                    nullptr, nullptr, rb);
+            }
+            launched();
         }
-        launched();
         if (timed) { kev_record(); }
     }
 }
@@ -481,17 +608,25 @@ void Engine::Impl::vcycle ()
         T* res = field_res<T>(l);
         T* rescor = field_rescor<T>(l);
         MLMG_CUDA_CHECK(cudaMemsetAsync(cor, 0, (size_t)L.meta.nelem * sizeof(T), st()));
-        for (int i = 0; i < o.nu1; ++i) { smooth<T>(l, cor, res, i == 0); }
-        // rescor = res - L(cor), homogeneous BC (computeResOfCorrection)
-        ghost<T>(l, cor, false, true);
-        if (abec) {
-            k_residual<T, T, true><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
-                coef<T>(l, 0), coef<T>(l, 1), coef<T>(l, 2), coef<T>(l, 3), nullptr);
+        if (std::is_same_v<T, float> && L.fused) {
+            smooth_fused(l, o.nu1);
         } else {
-            k_residual<T, T, false><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
-                nullptr, nullptr, nullptr, nullptr, nullptr);
+            for (int i = 0; i < o.nu1; ++i) { smooth<T>(l, cor, res, i == 0); }
         }
-        launched();
+        // rescor = res - L(cor), homogeneous BC (computeResOfCorrection)
+        if constexpr (std::is_same_v<T, float>) {
+            resid32(l, rescor, cor, res);
+        } else {
+            ghost<T>(l, cor, false, true);
+            if (abec) {
+                k_residual<T, T, true><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
+                    coef<T>(l, 0), coef<T>(l, 1), coef<T>(l, 2), coef<T>(l, 3), nullptr);
+            } else {
+                k_residual<T, T, false><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
+                    nullptr, nullptr, nullptr, nullptr, nullptr);
+            }
+            launched();
+        }
         LevelData& C = lev[l + 1];
         k_restrict<T><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), rescor, field_res<T>(l + 1));
         launched();
@@ -511,7 +646,11 @@ void Engine::Impl::vcycle ()
         T* cor = field_cor<T>(l);
         k_interp_add<T><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), lev[l + 1].dl, field_cor<T>(l + 1), cor);
         launched();
-        for (int i = 0; i < o.nu2; ++i) { smooth<T>(l, cor, field_res<T>(l), false); }
+        if (std::is_same_v<T, float> && L.fused) {
+            smooth_fused(l, o.nu2);
+        } else {
+            for (int i = 0; i < o.nu2; ++i) { smooth<T>(l, cor, field_res<T>(l), false); }
+        }
     }
 }
 
@@ -528,9 +667,36 @@ void Engine::Impl::reduce_per_solve (int l, const SubsetData& S, int op, const d
 void Engine::Impl::residual0 (bool to32)
 {
     LevelData& L = lev[0];
+    if (to32) {
+        // mixed path: FP64 residual in stencil form, FP32 copy for the V-cycle,
+        // per-solve max-norm by atomic max (zeroed first)
+        MLMG_CUDA_CHECK(cudaMemsetAsync(red_out.p, 0, sizeof(double) * nsolve, st()));
+        if (!L.inline_bc) { ghost<double>(0, L.sol.p, true, true); }
+        const StencilPtrs S = stencil64(0);
+        const unsigned g = (unsigned)L.all.ntiles;
+        if (abec) {
+            if (L.inline_bc) {
+                k_residual_s<double, float, true, true, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res32.p,
+                    L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
+            } else {
+                k_residual_s<double, float, true, false, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(),
+                    L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
+            }
+        } else {
+            if (L.inline_bc) {
+                k_residual_s<double, float, false, true, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(),
+                    L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
+            } else {
+                k_residual_s<double, float, false, false, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(),
+                    L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
+            }
+        }
+        launched();
+        return;
+    }
     ghost<double>(0, L.sol.p, true, true);
     const double *a = L.a.p, *bx = L.bx.p, *by = L.by.p, *bz = L.bz.p;
-    if (to32) {
+    if (false) {
         if (abec) {
             k_residual<double, float, true><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res32.p,
                 L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
@@ -681,15 +847,12 @@ void Engine::set_coefficients ()
             I.launched();
         }
         if (I.mixed()) {
+            // stencil form on every level: D, s in FP64 and FP32
             for (int l = 0; l < I.nlev_max; ++l) {
                 LevelData& L = I.lev[l];
-                const long long n = L.meta.nelem;
-                const unsigned nb = (unsigned)std::min<long long>((n + 255) / 256, 152 * 16);
-                k_convert<float, double><<<nb, 256, 0, m_stream>>>(n, L.a32.p, L.a.p);
-                k_convert<float, double><<<nb, 256, 0, m_stream>>>(n, L.bx32.p, L.bx.p);
-                k_convert<float, double><<<nb, 256, 0, m_stream>>>(n, L.by32.p, L.by.p);
-                k_convert<float, double><<<nb, 256, 0, m_stream>>>(n, L.bz32.p, L.bz.p);
-                I.launched(4);
+                k_build_stencil<<<L.all.ntiles, kTileBlock, 0, m_stream>>>(L.dl, L.all.dev(), L.a.p, L.bx.p, L.by.p,
+                    L.bz.p, L.D.p, L.sx.p, L.sy.p, L.sz.p, L.D32.p, L.sx32.p, L.sy32.p, L.sz32.p);
+                I.launched();
             }
         }
     }

@@ -64,6 +64,15 @@ CASES = {
                               lobc=(101, 102, 101), hibc=(102, 101, 101), sol_seed=3004),
     "solve_abec_agg8": _c(mode="solve", op="abec", n=(32, 32, 32), max_grid_size=8, rhs_seed=1005,
                           b_seed=2005, agg_grid_size=8, con_grid_size=8),
+    # singular operators (solvability fix) and a 4-point Dirichlet closure
+    "solve_poisson_periodic": _c(mode="solve", n=(32, 32, 32), max_grid_size=16, rhs_seed=1006,
+                                 periodic=(1, 1, 1), lobc=(200,) * 3, hibc=(200,) * 3),
+    "solve_abec_neumann_singular": _c(mode="solve", op="abec", n=(32, 32, 32), max_grid_size=16, rhs_seed=1007,
+                                      b_seed=2007, alpha=0.0, lobc=(102,) * 3, hibc=(102,) * 3),
+    "solve_abec_mo4": _c(mode="solve", op="abec", n=(32, 32, 32), max_grid_size=16, rhs_seed=1008, b_seed=2008,
+                         maxorder=4),
+    "solve_poisson_periodic_x": _c(mode="solve", n=(32, 24, 16), max_grid_size=8, rhs_seed=1009,
+                                   periodic=(1, 0, 0), lobc=(200, 101, 102), hibc=(200, 102, 101)),
 }
 
 

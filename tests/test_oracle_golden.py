@@ -51,6 +51,9 @@ def test_solve_matches_reference(name):
     assert info["status"] == 0
     assert info["niters"] == r["niters"]
     assert info["cg_iters"] == r["cg_iters"]
-    np.testing.assert_allclose(info["history"], r["history"], rtol=1e-6)
+    # near the rounding floor the residuals move with the summation order of
+    # the reference's OpenMP reductions (solvability offsets, bottom dots)
+    np.testing.assert_allclose(info["history"], r["history"], rtol=1e-6,
+                               atol=1e-13 * max(r["rhs_norm"], r["init_resid"]))
     # phi agrees to 1e-10 relative (max norm)
     assert np.abs(phi - ref).max() <= 1e-10 * np.abs(ref).max()
