@@ -307,6 +307,10 @@ class MLMG:
     def setFusedSmoother(self, on): self._set("mlmg_set_fused_smoother", int(bool(on)))
     def setTimeKernels(self, on): self._set("mlmg_set_time_kernels", int(bool(on)))
 
+    def setOption(self, name, value):
+        """Engine tuning knob (coarse_block, coarse_cells, merge_boxes, fuse_resid_restrict)."""
+        check(capi.lib().mlmg_set_option(self._h, name.encode(), float(value)))
+
     def smootherStats(self, reset=False):
         """(total ms, launches, algorithmic bytes per launch) of the
         finest-level smoother since the last reset."""

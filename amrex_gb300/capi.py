@@ -82,6 +82,7 @@ SIGNATURES = {
     "mlmg_set_graph": (c_int, [c_void_p, c_int]),
     "mlmg_set_fused_smoother": (c_int, [c_void_p, c_int]),
     "mlmg_set_time_kernels": (c_int, [c_void_p, c_int]),
+    "mlmg_set_option": (c_int, [c_void_p, ctypes.c_char_p, c_double]),
     "mlmg_get_smoother_stats": (c_int, [c_void_p, P(c_double), P(ctypes.c_longlong), P(c_double), c_int]),
     "mlmg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_double, P(c_double)]),
     "mlmg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),

@@ -4,7 +4,8 @@
 // MLMGT::actualBottomSolve (AMReX_MLMG.H:1500-1610) on the solve's coarsest
 // level, with FP64 arithmetic, dot products and norms, and no host round
 // trip.  The coarsest level is tiny (2^3..8^3 cells for the benchmark
-// configurations), so one block is the right size.
+// configurations), so one block is the right size.  The block-level helpers
+// here are also used by the coarse-level V-cycle kernel.
 #pragma once
 
 #include "stage_kernels.cuh"
@@ -47,45 +48,47 @@ __device__ __forceinline__ void for_cells (const DevLevel& L, int p0, int np, F&
     for (int p = p0; p < p0 + np; ++p) {
         const PatchDesc& P = L.P[p];
         const int nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1, nz = P.hi[2] - P.lo[2] + 1;
-        const long long n = (long long)nx * ny * nz;
-        for (long long u = threadIdx.x; u < n; u += blockDim.x) {
-            const int i = P.lo[0] + (int)(u % nx);
-            const int j = P.lo[1] + (int)((u / nx) % ny);
-            const int k = P.lo[2] + (int)(u / ((long long)nx * ny));
+        const int n = nx * ny * nz;
+        for (int u = threadIdx.x; u < n; u += blockDim.x) {
+            const int i = P.lo[0] + u % nx;
+            const int j = P.lo[1] + (u / nx) % ny;
+            const int k = P.lo[2] + u / (nx * ny);
             f(P, i, j, k, cidx(P, i, j, k));
         }
     }
 }
 
-__device__ void ghost_fill (const BottomLevelPtrs& B, const BottomJob& J, double* phi)
+// applyBC (homogeneous) for one solve's patches of a level: BC closures
+// where the mask is > 0, then copies from neighbouring patches
+template <typename T>
+__device__ void ghost_fill (const DevLevel& L, const CopyTag* tags, int p0, int np, int t0, int nt, T* phi)
 {
     __syncthreads();
-    for (int p = J.p0; p < J.p0 + J.np; ++p) {
-        const PatchDesc& P = B.L.P[p];
+    for (int p = p0; p < p0 + np; ++p) {
+        const PatchDesc& P = L.P[p];
         for (int f = 0; f < 6; ++f) {
             const int d = f % 3;
             const int e0 = (d == 0) ? 1 : 0, e1 = (d == 2) ? 1 : 2;
-            const long long n = (long long)(P.hi[e0] - P.lo[e0] + 1) * (P.hi[e1] - P.lo[e1] + 1);
-            for (long long u = threadIdx.x; u < n; u += blockDim.x) {
+            const int n = (P.hi[e0] - P.lo[e0] + 1) * (P.hi[e1] - P.lo[e1] + 1);
+            for (int u = threadIdx.x; u < n; u += blockDim.x) {
                 int i, j, k;
                 face_cell(P, f, u, i, j, k);
-                if (face_mask(B.L, P, f, i, j, k) > 0) {
+                if (face_mask(L, P, f, i, j, k) > 0) {
                     const long long stride = (d == 0) ? 1 : ((d == 1) ? (long long)P.sx : P.sxy);
-                    bc_ghost<double>(P, f, cidx(P, i, j, k), (f >= 3) ? -stride : stride, phi, 0, nullptr, u);
+                    bc_ghost<T>(P, f, cidx(P, i, j, k), (f >= 3) ? -stride : stride, phi, 0, nullptr, u);
                 }
             }
         }
     }
-    for (int w = J.t0; w < J.t0 + J.nt; ++w) {
-        const CopyTag& C = B.tags[w];
+    for (int w = t0; w < t0 + nt; ++w) {
+        const CopyTag& C = tags[w];
         const int nx = C.box.hi[0] - C.box.lo[0] + 1, ny = C.box.hi[1] - C.box.lo[1] + 1;
-        const long long n = (long long)nx * ny * (C.box.hi[2] - C.box.lo[2] + 1);
-        for (long long u = threadIdx.x; u < n; u += blockDim.x) {
-            const int i = C.box.lo[0] + (int)(u % nx);
-            const int j = C.box.lo[1] + (int)((u / nx) % ny);
-            const int k = C.box.lo[2] + (int)(u / ((long long)nx * ny));
-            phi[cidx(B.L.P[C.dst], i, j, k)] =
-                phi[cidx(B.L.P[C.src], i - C.shift[0], j - C.shift[1], k - C.shift[2])];
+        const int n = nx * ny * (C.box.hi[2] - C.box.lo[2] + 1);
+        for (int u = threadIdx.x; u < n; u += blockDim.x) {
+            const int i = C.box.lo[0] + u % nx;
+            const int j = C.box.lo[1] + (u / nx) % ny;
+            const int k = C.box.lo[2] + u / (nx * ny);
+            phi[cidx(L.P[C.dst], i, j, k)] = phi[cidx(L.P[C.src], i - C.shift[0], j - C.shift[1], k - C.shift[2])];
         }
     }
     __syncthreads();
@@ -94,7 +97,7 @@ __device__ void ghost_fill (const BottomLevelPtrs& B, const BottomJob& J, double
 template <bool ABEC>
 __device__ void apply_normalize (const BottomLevelPtrs& B, const BottomJob& J, double* out, double* in)
 {
-    ghost_fill(B, J, in);
+    ghost_fill<double>(B.L, B.tags, J.p0, J.np, J.t0, J.nt, in);
     for_cells(B.L, J.p0, J.np, [&] (const PatchDesc& P, int, int, int, long long q) {
         double v = adotx_cell<double, ABEC>(P, q, in, B.a, B.bx, B.by, B.bz);
         if constexpr (ABEC) { v /= abec_diag<double>(P, q, B.a, B.bx, B.by, B.bz); }
@@ -103,12 +106,12 @@ __device__ void apply_normalize (const BottomLevelPtrs& B, const BottomJob& J, d
     __syncthreads();
 }
 
-__device__ double reduce (const BottomLevelPtrs& B, const BottomJob& J, const double* x, const double* y, int op)
+__device__ double reduce (const DevLevel& L, int p0, int np, const double* x, const double* y, int op)
 {
     __shared__ double sm[32];
     __shared__ double result;
     double acc = 0.0;
-    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
+    for_cells(L, p0, np, [&] (const PatchDesc&, int, int, int, long long q) {
         if (op == RED_MAXABS) { acc = fmax(acc, fabs(x[q])); }
         else if (op == RED_DOT) { acc += x[q] * y[q]; }
         else { acc += x[q]; }
@@ -125,7 +128,7 @@ template <bool ABEC>
 __device__ void smooth (const BottomLevelPtrs& B, const BottomJob& J, double* x, const double* b)
 {
     for (int rb = 0; rb < 2; ++rb) {
-        ghost_fill(B, J, x);
+        ghost_fill<double>(B.L, B.tags, J.p0, J.np, J.t0, J.nt, x);
         for_cells(B.L, J.p0, J.np, [&] (const PatchDesc& P, int i, int j, int k, long long) {
             if (((i + j + k + rb) & 1) == 0) {
                 gsrb_cell<double, ABEC>(B.L, P, i, j, k, x, b, B.a, B.bx, B.by, B.bz);
@@ -137,15 +140,12 @@ __device__ void smooth (const BottomLevelPtrs& B, const BottomJob& J, double* x,
 
 } // namespace bottom_detail
 
+// the bottom solve of one solve, executed by the calling block
 template <typename T, bool ABEC>
-__global__ void __launch_bounds__(BOTTOM_THREADS)
-k_bottom (const BottomLevelPtrs* __restrict__ levels, const BottomJob* __restrict__ jobs, BottomParams prm,
-          const int* __restrict__ active, int* __restrict__ out_iters, int* __restrict__ out_ret)
+__device__ void bottom_solve_block (const BottomLevelPtrs& B, const BottomJob& J, const BottomParams& prm,
+                                    int* __restrict__ out_iters, int* __restrict__ out_ret)
 {
     using namespace bottom_detail;
-    const BottomJob J = jobs[blockIdx.x];
-    if (active != nullptr && !active[J.solve]) { return; }
-    const BottomLevelPtrs& B = levels[J.lev];
     double *x = B.x, *b = B.b, *p = B.p, *r = B.r, *rh = B.rh, *v = B.v, *t = B.t;
     const T* bin = static_cast<const T*>(B.b_in);
     T* xout = static_cast<T*>(B.x_out);
@@ -153,7 +153,7 @@ k_bottom (const BottomLevelPtrs* __restrict__ levels, const BottomJob* __restric
     // x = 0 (ghosts included), b = res (valid)
     for (int pp = J.p0; pp < J.p0 + J.np; ++pp) {
         const PatchDesc& P = B.L.P[pp];
-        const long long n0 = P.base - P.sxy - P.sx - 1;
+        const long long n0 = P.base - P.sxy - P.sx - XOFF;   // the patch's whole allocation
         const long long n = P.sxy * (P.hi[2] - P.lo[2] + 3);
         for (long long u = threadIdx.x; u < n; u += blockDim.x) {
             x[n0 + u] = 0.0; p[n0 + u] = 0.0; r[n0 + u] = 0.0;
@@ -170,7 +170,7 @@ k_bottom (const BottomLevelPtrs* __restrict__ levels, const BottomJob* __restric
         // the solve's b, made solvable for a singular operator (a private copy)
         const double* bb = b;
         if (J.singular) {
-            const double off = reduce(B, J, b, nullptr, RED_SUM) * J.volinv;
+            const double off = reduce(B.L, J.p0, J.np, b, nullptr, RED_SUM) * J.volinv;
             for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { t[q] = b[q] + (-off); });
             __syncthreads();
             for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { rh[q] = t[q]; });
@@ -186,13 +186,13 @@ k_bottom (const BottomLevelPtrs* __restrict__ levels, const BottomJob* __restric
         __syncthreads();
         for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { rh[q] = r[q]; });
         __syncthreads();
-        double rnorm = reduce(B, J, r, nullptr, RED_MAXABS);
+        double rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
         const double rnorm0 = rnorm;
         double rho_1 = 0, alpha = 0, omega = 0;
         iter = 1;
         if (!(rnorm0 == 0 || rnorm0 < prm.eps_abs)) {
             for (; iter <= prm.maxiter; ++iter) {
-                const double rho = reduce(B, J, rh, r, RED_DOT);
+                const double rho = reduce(B.L, J.p0, J.np, rh, r, RED_DOT);
                 if (rho == 0) { ret = 1; break; }
                 if (iter == 1) {
                     for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { p[q] = r[q]; });
@@ -205,25 +205,25 @@ k_bottom (const BottomLevelPtrs* __restrict__ levels, const BottomJob* __restric
                 }
                 __syncthreads();
                 apply_normalize<ABEC>(B, J, v, p);
-                const double rhTv = reduce(B, J, rh, v, RED_DOT);
+                const double rhTv = reduce(B.L, J.p0, J.np, rh, v, RED_DOT);
                 if (rhTv != 0.0) { alpha = rho / rhTv; } else { ret = 2; break; }
                 for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
                     x[q] += alpha * p[q];
                     r[q] += (-alpha) * v[q];
                 });
                 __syncthreads();
-                rnorm = reduce(B, J, r, nullptr, RED_MAXABS);
+                rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
                 if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
                 apply_normalize<ABEC>(B, J, t, r);
-                const double tt = reduce(B, J, t, t, RED_DOT);
-                const double tr = reduce(B, J, t, r, RED_DOT);
+                const double tt = reduce(B.L, J.p0, J.np, t, t, RED_DOT);
+                const double tr = reduce(B.L, J.p0, J.np, t, r, RED_DOT);
                 if (tt != 0.0) { omega = tr / tt; } else { ret = 3; break; }
                 for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
                     x[q] += omega * r[q];
                     r[q] += (-omega) * t[q];
                 });
                 __syncthreads();
-                rnorm = reduce(B, J, r, nullptr, RED_MAXABS);
+                rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
                 if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
                 if (omega == 0) { ret = 4; break; }
                 rho_1 = rho;
@@ -249,6 +249,17 @@ k_bottom (const BottomLevelPtrs* __restrict__ levels, const BottomJob* __restric
         out_iters[J.solve] = iter;
         out_ret[J.solve] = ret;
     }
+    __syncthreads();
+}
+
+template <typename T, bool ABEC>
+__global__ void __launch_bounds__(BOTTOM_THREADS)
+k_bottom (const BottomLevelPtrs* __restrict__ levels, const BottomJob* __restrict__ jobs, BottomParams prm,
+          const int* __restrict__ active, int* __restrict__ out_iters, int* __restrict__ out_ret)
+{
+    const BottomJob J = jobs[blockIdx.x];
+    if (active != nullptr && !active[J.solve]) { return; }
+    bottom_solve_block<T, ABEC>(levels[J.lev], J, prm, out_iters, out_ret);
 }
 
 } // namespace mlmg

@@ -896,6 +896,25 @@ SETTER(mlmg_set_graph, use_graph, int, true)
 SETTER(mlmg_set_fused_smoother, fused_smoother, int, true)
 SETTER(mlmg_set_time_kernels, time_kernels, int, true)
 
+int mlmg_set_option (mlmg_solver s, const char* name, double value)
+{
+    API_BEGIN
+    MLMG_REQUIRE(s != nullptr && name != nullptr, ERR_ARGS, "bad arguments");
+    const std::string n(name);
+    if (n == "coarse_block") { s->opt.coarse_block = value != 0.0; }
+    else if (n == "coarse_cells") {
+        MLMG_REQUIRE(value >= 0, ERR_ARGS, "coarse_cells must be >= 0");
+        s->opt.coarse_cells = (int)value;
+    }
+    else if (n == "merge_boxes") { s->opt.merge_boxes = value != 0.0; }
+    else if (n == "fuse_resid_restrict") { s->opt.fuse_resid_restrict = value != 0.0; }
+    else { MLMG_REQUIRE(false, ERR_UNSUPPORTED, "unknown option " + n); }
+    // layout-changing knobs take effect at the next engine build
+    s->eng.reset();
+    s->batch_eng.reset();
+    API_END
+}
+
 int mlmg_get_smoother_stats (mlmg_solver s, double* total_ms, long long* launches, double* bytes_per_launch,
                              int reset)
 {

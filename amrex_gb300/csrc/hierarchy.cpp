@@ -205,7 +205,10 @@ PatchLevel build_patch_level (const std::vector<const SolveSpec*>& solves, int l
             PatchDesc P{};
             for (int d = 0; d < 3; ++d) { P.lo[d] = pb.lo[d]; P.hi[d] = pb.hi[d]; }
             const int nx = pb.len(0), ny = pb.len(1), nz = pb.len(2);
-            P.sx = ((XOFF + nx + 1 + XALIGN - 1) / XALIGN) * XALIGN;
+            // row: XOFF cells before lo, the patch, and at least 7 cells after
+            // hi, so 16-byte staged copies of any row chunk touching the patch
+            // stay inside the row
+            P.sx = ((XOFF + nx + 8 + XALIGN - 1) / XALIGN) * XALIGN;
             P.sxy = (long long)P.sx * (ny + 2);
             cursor = ((cursor + XALIGN - 1) / XALIGN) * XALIGN;
             P.base = cursor + P.sxy + P.sx + XOFF;

@@ -3,6 +3,7 @@
 #include "bottom.cuh"
 #include "stencil_kernels.cuh"
 #include "fused_sweep.cuh"
+#include "coarse_vcycle.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -76,6 +77,7 @@ struct LevelData {
     bool fused = false;
     SubsetData fz;
     DevBuf<float> cor32b;
+    DevBuf<int> tfirst_d, tn_d;    // per-solve tag ranges (coarse-level kernel)
     // bottom work arrays
     DevBuf<double> bw[7];
     bool has_bottom = false;
@@ -97,6 +99,12 @@ struct Engine::Impl {
     DevBuf<BottomLevelPtrs> bot_levels;
     DevBuf<BottomJob> bot_jobs;
     int njobs = 0;
+    // one warp when every bottom level is tiny (its block barriers are then
+    // nearly free), else BOTTOM_THREADS
+    int bot_threads = BOTTOM_THREADS;
+    // levels >= lc run inside k_coarse_vcycle (one block per solve); -1: none
+    int lc = -1;
+    DevBuf<CoarseLevelPtrs> coarse_lv;
     cudaGraphExec_t graph_exec = nullptr;
     int graph_launches = 0;      // kernels in one replay of the iteration graph
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -368,7 +376,45 @@ void Engine::Impl::build_bottom_tables ()
         jobs.push_back(J);
     }
     njobs = (int)jobs.size();
+    long long max_cells = 0;
+    for (const auto& J : jobs) {
+        long long c = 0;
+        for (int p = J.p0; p < J.p0 + J.np; ++p) {
+            const PatchDesc& P = lev[J.lev].meta.patches[p];
+            c += (long long)(P.hi[0] - P.lo[0] + 1) * (P.hi[1] - P.lo[1] + 1) * (P.hi[2] - P.lo[2] + 1);
+        }
+        max_cells = std::max(max_cells, c);
+    }
+    bot_threads = (max_cells <= 512) ? 32 : BOTTOM_THREADS;
     bot_levels.upload(tab, st());
+    // coarse levels: from the bottom up, every level on which each solve has
+    // at most coarse_cells cells (mixed path)
+    lc = -1;
+    if (mixed() && E.m_opt.coarse_block) {
+        for (int l = nlev_max - 1; l >= 0; --l) {
+            const PatchLevel& M = lev[l].meta;
+            bool small = true;
+            for (int s = 0; s < nsolve; ++s) {
+                long long c = 0;
+                for (int p = M.solve_first_patch[s]; p >= 0 && p < M.solve_first_patch[s] + M.solve_npatch[s]; ++p) {
+                    const PatchDesc& P = M.patches[p];
+                    c += (long long)(P.hi[0] - P.lo[0] + 1) * (P.hi[1] - P.lo[1] + 1) * (P.hi[2] - P.lo[2] + 1);
+                }
+                if (c > E.m_opt.coarse_cells) { small = false; }
+            }
+            if (!small) { break; }
+            lc = l;
+        }
+        std::vector<CoarseLevelPtrs> ct(nlev_max);
+        for (int l = 0; l < nlev_max; ++l) {
+            LevelData& L = lev[l];
+            L.tfirst_d.upload(L.solve_tag_first, st());
+            L.tn_d.upload(L.solve_tag_n, st());
+            ct[l] = CoarseLevelPtrs{L.dl, L.tags.p, L.tfirst_d.p, L.tn_d.p, L.cor32.p, L.res32.p, L.rescor32.p,
+                                    stencil32(l)};
+        }
+        coarse_lv.upload(ct, st());
+    }
     bot_jobs.upload(jobs, st());
 }
 
@@ -601,7 +647,10 @@ template <typename T>
 void Engine::Impl::vcycle ()
 {
     const EngineOptions& o = E.m_opt;
-    for (int l = 0; l + 1 < nlev_max; ++l) {
+    // levels >= top_end run in the coarse-level kernel (mixed path)
+    const bool coarse = std::is_same_v<T, float> && lc >= 0;
+    const int top_end = coarse ? lc : nlev_max - 1;
+    for (int l = 0; l < top_end; ++l) {
         LevelData& L = lev[l];
         if (L.mg.n == 0) { continue; }
         T* cor = field_cor<T>(l);
@@ -615,6 +664,20 @@ void Engine::Impl::vcycle ()
         }
         // rescor = res - L(cor), homogeneous BC (computeResOfCorrection)
         if constexpr (std::is_same_v<T, float>) {
+            if (L.inline_bc && E.m_opt.fuse_resid_restrict) {
+                // fused with the restriction below: the fine residual is never stored
+                LevelData& C = lev[l + 1];
+                const StencilPtrs S = stencil32(l);
+                if (abec) {
+                    k_resid_restrict<true><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), cor, res, S,
+                                                                                 field_res<T>(l + 1));
+                } else {
+                    k_resid_restrict<false><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), cor, res, S,
+                                                                                  field_res<T>(l + 1));
+                }
+                launched();
+                continue;
+            }
             resid32(l, rescor, cor, res);
         } else {
             ghost<T>(l, cor, false, true);
@@ -632,15 +695,23 @@ void Engine::Impl::vcycle ()
         launched();
     }
     BottomParams prm{o.bottom_maxiter, o.bottom_reltol, o.bottom_abstol, o.nub, o.nuf, o.bottom_solver == 1 ? 1 : 0};
-    if (abec) {
-        k_bottom<T, true><<<njobs, BOTTOM_THREADS, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
+    if (coarse) {
+        if (abec) {
+            k_coarse_vcycle<true><<<njobs, COARSE_THREADS, 0, st()>>>(coarse_lv.p, lc, bot_levels.p, bot_jobs.p, prm,
+                                                                      o.nu1, o.nu2, bot_iters.p, bot_ret.p);
+        } else {
+            k_coarse_vcycle<false><<<njobs, COARSE_THREADS, 0, st()>>>(coarse_lv.p, lc, bot_levels.p, bot_jobs.p, prm,
+                                                                       o.nu1, o.nu2, bot_iters.p, bot_ret.p);
+        }
+    } else if (abec) {
+        k_bottom<T, true><<<njobs, bot_threads, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
                                                               bot_iters.p, bot_ret.p);
     } else {
-        k_bottom<T, false><<<njobs, BOTTOM_THREADS, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
+        k_bottom<T, false><<<njobs, bot_threads, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
                                                                bot_iters.p, bot_ret.p);
     }
     launched();
-    for (int l = nlev_max - 2; l >= 0; --l) {
+    for (int l = top_end - 1; l >= 0; --l) {
         LevelData& L = lev[l];
         if (L.mg.n == 0) { continue; }
         T* cor = field_cor<T>(l);

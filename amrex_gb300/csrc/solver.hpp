@@ -37,6 +37,11 @@ struct EngineOptions {
     int fused_smoother = 0;     // fused two-colour sweeps where a level allows
     int merge_boxes = 1;        // merge a level's boxes into one patch where exact
     int time_kernels = 0;       // time every finest-level smoother launch with CUDA events
+    int fuse_resid_restrict = 0;  // correction residual and restriction in one kernel (slower on GB300)
+    int coarse_block = 0;       // run the coarse levels of each V-cycle in one thread block per solve
+                                // (slower than graph-replayed grid-wide launches on GB300 at every
+                                // threshold from 2^3 to 32^3 cells)
+    int coarse_cells = 512;     // a level is coarse when every solve has at most this many cells on it
 };
 
 // Live timing of the dominant kernel (the finest-level smoother).

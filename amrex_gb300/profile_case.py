@@ -1,6 +1,6 @@
 """A fixed solve for profilers (ncu launch lists and single-kernel captures).
 
-    python -m amrex_gb300.profile_case --n 256 --mode mixed --solves 1 [--graph] [--fused]
+    python -m amrex_gb300.profile_case --n 256 --mode mixed --solves 1 [--graph] [--fused] [--opt name=value]
 
 Builds the benchmark workload (variable-coefficient MLABecLaplacian, log-normal
 b with contrast 1e3, Gaussian-blob RHS, max_grid_size 64) at n^3 and runs
@@ -25,6 +25,7 @@ def main():
     ap.add_argument("--solves", type=int, default=1)
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--fused", action="store_true")
+    ap.add_argument("--opt", action="append", default=[], help="engine option name=value (repeatable)")
     args = ap.parse_args()
     n = args.n
     rhs_h = synth.gaussian_rhs(n, 1001)
@@ -50,6 +51,9 @@ def main():
     m.setPrecision(args.mode)
     m.setGraph(args.graph)
     m.setFusedSmoother(args.fused)
+    for kv in args.opt:
+        k, v = kv.split("=")
+        m.setOption(k, float(v))
     for s in range(args.solves):
         sol.setVal(0.0)
         t = time.perf_counter()

@@ -163,6 +163,11 @@ int mlmg_set_always_use_bnorm(mlmg_solver s, int flag);
 int mlmg_set_precision(mlmg_solver s, int mode);
 int mlmg_set_graph(mlmg_solver s, int on);               /* replay each iteration as a CUDA graph */
 int mlmg_set_fused_smoother(mlmg_solver s, int on);      /* fused two-colour Gauss-Seidel sweeps */
+/* engine tuning knobs by name: "coarse_block" (0/1: run the coarse levels of
+ * each V-cycle in one thread block per solve), "coarse_cells" (a level is
+ * coarse when every solve has at most this many cells on it),
+ * "merge_boxes" (0/1), "fuse_resid_restrict" (0/1); -4 for an unknown name */
+int mlmg_set_option(mlmg_solver s, const char* name, double value);
 /* time every finest-level smoother launch with CUDA events on the library
  * stream (graph replays included); the stats accumulate until reset */
 int mlmg_set_time_kernels(mlmg_solver s, int on);

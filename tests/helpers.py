@@ -8,7 +8,7 @@ import numpy as np
 import amrex_gb300 as ag
 
 
-def make_problem(case, arrays, precision=None, graph=False, fused=False):
+def make_problem(case, arrays, precision=None, graph=False, fused=False, options=None):
     nx, ny, nz = case["n"]
     domain = ag.Box((0, 0, 0), (nx - 1, ny - 1, nz - 1))
     if case.get("boxes"):
@@ -53,6 +53,8 @@ def make_problem(case, arrays, precision=None, graph=False, fused=False):
         mlmg.setPrecision(precision)
     mlmg.setGraph(graph)
     mlmg.setFusedSmoother(fused)
+    for k, v in (options or {}).items():
+        mlmg.setOption(k, v)
     return dict(ba=ba, dm=dm, geom=geom, sol=sol, rhs=rhs, op=op, mlmg=mlmg, keep=keep, domain=domain)
 
 

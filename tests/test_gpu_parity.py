@@ -79,15 +79,17 @@ MIXED_CASES = ["solve_poisson_32", "solve_abec_32", "solve_abec_48", "solve_abec
 
 
 @pytest.mark.parametrize("name", MIXED_CASES)
-@pytest.mark.parametrize("graph,fused", [(False, False), (True, False), (True, True)])
-def test_mixed_solve_reaches_target(name, graph, fused):
+@pytest.mark.parametrize("graph,fused,coarse", [(False, False, 1), (True, False, 1), (True, True, 1),
+                                                (False, False, 0), (True, True, 0)])
+def test_mixed_solve_reaches_target(name, graph, fused, coarse):
     """FP32 V-cycles inside FP64 refinement reach the same 1e-10 relative
     residual (the residual is evaluated in FP64); phi agrees with the
     reference's FP64 answer to the accuracy that residual implies (up to the
     constant null-space component for singular problems)."""
     g = load.load(name)
     c = g["case"]
-    prob = helpers.make_problem(c, cases.inputs(c), precision="mixed", graph=graph, fused=fused)
+    prob = helpers.make_problem(c, cases.inputs(c), precision="mixed", graph=graph, fused=fused,
+                                options={"coarse_block": coarse})
     resid = prob["mlmg"].solve(prob["sol"], prob["rhs"], c["tol_rel"], c["tol_abs"])
     r = g["result"]
     target = c["tol_rel"] * max(r["rhs_norm"], r["init_resid"])
@@ -115,6 +117,27 @@ def test_fused_sweep_matches_colour_passes(name):
     np.testing.assert_allclose(h2, h1, rtol=1e-5, atol=1e-13 * h1[0])
     a, b = helpers.solution(p1, c), helpers.solution(p2, c)
     assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
+
+
+@pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_48", "solve_abec_mixed_bc",
+                                  "solve_abec_agg8", "solve_poisson_periodic"])
+@pytest.mark.parametrize("cells", [512, 32768])
+def test_coarse_block_vcycle_matches_grid_kernels(name, cells):
+    """Running the coarse levels inside one block per solve performs the same
+    FP32 stage arithmetic as the grid-wide kernels: the same iteration count
+    and residual history up to FP32 summation order."""
+    c = load.load(name)["case"]
+    inp = cases.inputs(c)
+    p1 = helpers.make_problem(c, inp, precision="mixed", options={"coarse_block": 0})
+    p2 = helpers.make_problem(c, inp, precision="mixed", options={"coarse_block": 1, "coarse_cells": cells})
+    p1["mlmg"].solve(p1["sol"], p1["rhs"], 1e-10, 0)
+    p2["mlmg"].solve(p2["sol"], p2["rhs"], 1e-10, 0)
+    assert abs(p1["mlmg"].getNumIters() - p2["mlmg"].getNumIters()) <= 1
+    h1, h2 = np.array(p1["mlmg"].getResidualHistory()), np.array(p2["mlmg"].getResidualHistory())
+    n = min(len(h1), len(h2), 4)
+    np.testing.assert_allclose(h2[:n], h1[:n], rtol=1e-3, atol=1e-12 * h1[0])
+    a, b = helpers.solution(p1, c), helpers.solution(p2, c)
+    assert np.abs(a - b).max() <= 1e-8 * np.abs(a).max()
 
 
 def test_graph_replay_is_bitwise_identical():
