@@ -325,7 +325,9 @@ void Engine::Impl::build ()
         for (const auto& b : S.levels[0].boxes) { np += b.npts(); }
         const bool covered = (np == S.levels[0].geom.domain.npts());
         singular[s] = (!dir && covered && (!abec || S.alpha == 0.0)) ? 1 : 0;
-        volinv0[s] = 1.0 / (double)S.levels[0].geom.domain.npts();
+        // zero for a regular solve, so that the mean removal launched for the
+        // singular solves of a batch leaves the other solves unchanged
+        volinv0[s] = singular[s] ? 1.0 / (double)S.levels[0].geom.domain.npts() : 0.0;
         volinv_bottom[s] = 1.0 / (double)S.levels.back().geom.domain.npts();
     }
     volinv0_d.upload(volinv0, st());

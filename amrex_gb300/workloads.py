@@ -1,0 +1,54 @@
+"""Seeded benchmark workloads built through the public API.
+
+* ``abec_problem(n, mgs, rhs_seed, b_seed)``: the variable-coefficient
+  MLABecLaplacian on an n^3 unit cube (alpha = a = beta = 1, face b from a
+  log-normal random field with max/min contrast 1e3, Gaussian-blob RHS,
+  homogeneous Dirichlet on every face, boxes of at most ``mgs`` cells).
+* ``batch_specs(nsolve, seed)``: the batch of independent solves of uneven
+  sizes -- cube edges drawn uniformly from {32, 48, ..., 128}, solve i with
+  RHS and b seeds ``seed + 1 + i``.
+"""
+from __future__ import annotations
+
+from collections import namedtuple
+
+import numpy as np
+
+import amrex_gb300 as ag
+from amrex_gb300 import synth
+
+BatchSolveSpec = namedtuple("BatchSolveSpec", "n rhs_seed b_seed")
+
+BATCH_EDGES = (32, 48, 64, 80, 96, 112, 128)
+
+
+def batch_specs(nsolve=64, seed=4000):
+    rng = np.random.default_rng(seed)
+    edges = rng.choice(np.array(BATCH_EDGES), size=nsolve)
+    return [BatchSolveSpec(int(e), seed + 1 + i, seed + 1 + i) for i, e in enumerate(edges)]
+
+
+def abec_problem(n, mgs, rhs_seed, b_seed, rhs_host=None, bcoef_host=None):
+    """Operator, solution (1 ghost) and RHS MultiFabs of one solve; the host
+    inputs are returned too (``rhs_h``, ``b_h``)."""
+    rhs_h = synth.gaussian_rhs(n, rhs_seed) if rhs_host is None else rhs_host
+    b_h = synth.lognormal_bcoef(n, b_seed, sigma_cells=5.0, max_ratio=1e3) if bcoef_host is None else bcoef_host
+    domain = ag.Box((0, 0, 0), (n - 1, n - 1, n - 1))
+    ba = ag.BoxArray(domain).maxSize(mgs)
+    dm = ag.DistributionMapping(ba)
+    geom = ag.Geometry(domain)
+    sol = ag.MultiFab(ba, dm, 1, 1)
+    rhs = ag.MultiFab(ba, dm, 1, 0)
+    rhs.set_global(rhs_h)
+    op = ag.MLABecLaplacian(geom, ba, dm)
+    op.setDomainBC((101,) * 3, (101,) * 3)
+    op.setLevelBC(0, None)
+    op.setScalars(1.0, 1.0)
+    op.setACoeffs(0, 1.0)
+    faces = []
+    for d in range(3):
+        f = ag.MultiFab(ba, dm, 1, 0, nodal_dir=d)
+        f.set_global(b_h[d])
+        faces.append(f)
+    op.setBCoeffs(0, faces)
+    return dict(n=n, ba=ba, dm=dm, geom=geom, sol=sol, rhs=rhs, op=op, faces=faces, rhs_h=rhs_h, b_h=b_h)

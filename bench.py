@@ -200,6 +200,72 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def bench_batch(stream, nsolve=64):
+    """The batch of independent solves of uneven sizes (cube edges from
+    {32, 48, ..., 128}, max_grid_size 32, per-solve seeded b and RHS), mixed
+    precision in one batched call, against the same solves run one after
+    another through plain FP64 MLMG.  Device time on the library stream."""
+    import torch
+    import amrex_gb300 as ag
+    from amrex_gb300 import workloads
+    specs = workloads.batch_specs(nsolve, 4000)
+    probs = [workloads.abec_problem(s.n, 32, s.rhs_seed, s.b_seed) for s in specs]
+    cells = sum(s.n ** 3 for s in specs)
+    mixed = []
+    for p in probs:
+        m = ag.MLMG(p["op"])
+        m.setPrecision("mixed")
+        m.setGraph(True)
+        m.setFusedSmoother(True)
+        mixed.append(m)
+    sols, rhss = [p["sol"] for p in probs], [p["rhs"] for p in probs]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def batched():
+        for x in sols:
+            x.setVal(0.0)
+        return ag.solve_batched(mixed, sols, rhss, TOL_REL, 0.0)
+
+    batched()
+    reps = 3
+    e0.record(stream)
+    for _ in range(reps):
+        st = batched()
+    e1.record(stream)
+    e1.synchronize()
+    batch_ms = e0.elapsed_time(e1) / reps
+    iters_b = [m.getNumIters() for m in mixed]
+    phib = [x.get_global((s.n,) * 3) for x, s in zip(sols, specs)]
+    fp64 = []
+    for p in probs:
+        m = ag.MLMG(p["op"])
+        m.setPrecision("fp64")
+        fp64.append(m)
+
+    def sequential():
+        for m, x, b in zip(fp64, sols, rhss):
+            x.setVal(0.0)
+            m.solve(x, b, TOL_REL, 0.0)
+
+    sequential()
+    e0.record(stream)
+    sequential()
+    e1.record(stream)
+    e1.synchronize()
+    seq_ms = e0.elapsed_time(e1)
+    err = max(float(np.abs(a - x.get_global((s.n,) * 3)).max() / np.abs(x.get_global((s.n,) * 3)).max())
+              for a, x, s in zip(phib, sols, specs))
+    return {"workload": f"{nsolve} independent MLABecLaplacian solves, cube edges uniform in {{32,48,...,128}} "
+                        f"(seed 4000), max_grid_size 32, per-solve seeds 4001..{4000 + nsolve}, tol_rel 1e-10",
+            "nsolve": nsolve, "cells": cells, "edges": [s.n for s in specs],
+            "batched_mixed_ms": batch_ms, "solves_per_s": nsolve / (batch_ms * 1e-3),
+            "sequential_fp64_ms": seq_ms, "sequential_fp64_solves_per_s": nsolve / (seq_ms * 1e-3),
+            "speedup": seq_ms / batch_ms, "all_converged": all(v == 0 for v in st),
+            "iters_mixed": [min(iters_b), max(iters_b)],
+            "iters_fp64": [min(m.getNumIters() for m in fp64), max(m.getNumIters() for m in fp64)],
+            "phi_rel_diff_vs_fp64_max": err}
+
+
 def run_gb300(args, ws, rank, local):
     import torch
     import amrex_gb300 as ag
@@ -318,6 +384,8 @@ def run_gb300(args, ws, rank, local):
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
+    if not args.no_batch:
+        line["batch"] = bench_batch(stream)
     if rank == 0 and ws == 1 and not args.no_cpu:
         import multiprocessing
         os.environ.setdefault("OMP_NUM_THREADS", str(multiprocessing.cpu_count()))
@@ -333,6 +401,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
