@@ -335,6 +335,20 @@ class MLMG:
         rc = capi.lib().mlmg_solve(self._h, sol._h, rhs._h, float(tol_rel), float(tol_abs), ctypes.byref(r))
         return rc, r.value
 
+    def adjointGrad(self, sol, dJdphi, tol_rel, tol_abs, dJdf, dJdb=None, dJda=None):
+        """Adjoint gradients of J(phi) at the solution ``sol``: solves
+        A^T lambda = dJdphi, writes dJ/df = lambda into ``dJdf`` and, for
+        MLABecLaplacian, dJ/db into the three face MultiFabs ``dJdb`` and
+        dJ/da into ``dJda``.  Returns the adjoint solve's final residual."""
+        B = None
+        if dJdb is not None:
+            B = (ctypes.c_void_p * 3)(*[(m._h if m is not None else None) for m in dJdb])
+        rc = capi.lib().mlmg_adjoint_grad(self._h, sol._h, dJdphi._h, float(tol_rel), float(tol_abs), dJdf._h, B,
+                                          dJda._h if dJda is not None else None)
+        if rc != 0:
+            raise MLMGError(rc, capi.lib().mlmg_last_error().decode())
+        return capi.lib().mlmg_get_final_residual(self._h)
+
     def apply(self, out, inp):
         outs = out if isinstance(out, (list, tuple)) else [out]
         ins = inp if isinstance(inp, (list, tuple)) else [inp]

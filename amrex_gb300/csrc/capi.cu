@@ -294,6 +294,9 @@ struct mlmg_solver_s {
     std::vector<mlmg_linop> batch_ops;
     std::vector<int> batch_struct, batch_coef;
     int batch_prec = -1;
+    // transposed-operator engine of the adjoint (its own graph and buffers)
+    std::unique_ptr<Engine> adj_eng;
+    int adj_struct = -1, adj_coef = -1, adj_prec = -1, adj_merge = -1;
 };
 
 namespace {
@@ -381,6 +384,29 @@ Engine& engine_for (mlmg_solver s)
     }
     s->eng->options() = s->opt;
     return *s->eng;
+}
+
+Engine& adjoint_engine_for (mlmg_solver s)
+{
+    mlmg_linop op = s->op;
+    EngineOptions o = s->opt;
+    o.transpose = 1;
+    if (!s->adj_eng || s->adj_struct != op->struct_version || s->adj_prec != o.precision ||
+        s->adj_merge != o.merge_boxes) {
+        s->adj_eng.reset();
+        std::vector<SolveProblem> probs{make_problem(op)};
+        s->adj_eng = std::make_unique<Engine>(std::move(probs), o, lib_stream());
+        s->adj_struct = op->struct_version;
+        s->adj_coef = op->coef_version;
+        s->adj_prec = o.precision;
+        s->adj_merge = o.merge_boxes;
+    } else if (s->adj_coef != op->coef_version) {
+        make_problem(op);
+        s->adj_eng->set_coefficients();
+        s->adj_coef = op->coef_version;
+    }
+    s->adj_eng->options() = o;
+    return *s->adj_eng;
 }
 
 void count_launches (Engine& e) { g_launches += e.kernel_launches(); e.reset_launch_count(); }
@@ -970,6 +996,53 @@ int mlmg_solve (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, double tol_
     if (s->last.status == NOT_CONVERGED) { g_err = "MLMG failed to converge"; }
     if (s->last.status == ERR_DIVERGED) { g_err = "MLMG blew up"; }
     if (s->last.status == ERR_NONFINITE) { g_err = "MLMG residual is not finite"; }
+    return s->last.status;
+    API_END
+}
+
+int mlmg_adjoint_grad (mlmg_solver s, mlmg_multifab sol, mlmg_multifab dJdphi, double tol_rel, double tol_abs,
+                       mlmg_multifab out_dJdf, const mlmg_multifab* out_dJdb, mlmg_multifab out_dJda)
+{
+    API_BEGIN
+    check_solver_mf(s, sol);
+    check_solver_mf(s, dJdphi);
+    check_solver_mf(s, out_dJdf);
+    MLMG_REQUIRE(out_dJdf != dJdphi, ERR_ARGS, "dJ/df must not alias dJ/dphi");
+    FabSet fb[3];
+    FabSet* pb[3] = {nullptr, nullptr, nullptr};
+    FabSet fa;
+    FabSet* pa = nullptr;
+    const bool want_coef = (out_dJdb != nullptr) || (out_dJda != nullptr);
+    MLMG_REQUIRE(!want_coef || s->op->is_abec, ERR_UNSUPPORTED, "coefficient gradients need MLABecLaplacian");
+    if (out_dJdb != nullptr) {
+        for (int d = 0; d < 3; ++d) {
+            mlmg_multifab m = out_dJdb[d];
+            if (m == nullptr) { continue; }
+            MLMG_REQUIRE(m->ncomp == 1 && m->prec == 8 && m->nodal_dir == d && m->boxes == s->op->boxes, ERR_ARGS,
+                         "dJ/db[d] must be an FP64 MultiFab on the operator's BoxArray, face-centred in d");
+            fb[d] = m->fabset();
+            pb[d] = &fb[d];
+        }
+    }
+    if (out_dJda != nullptr) {
+        check_solver_mf(s, out_dJda);
+        fa = out_dJda->fabset();
+        pa = &fa;
+    }
+    Engine& e = adjoint_engine_for(s);
+    // lambda = A^{-T} dJ/dphi from a zero initial guess, written to dJ/df
+    cudaStream_t st = lib_stream();
+    MLMG_CUDA_CHECK(cudaMemsetAsync(out_dJdf->data.p, 0, (size_t)out_dJdf->total * out_dJdf->prec, st));
+    FabSet fl = out_dJdf->fabset(), fg = dJdphi->fabset(), fphi = sol->fabset();
+    e.solve({&fl}, {&fl}, {&fg}, tol_rel, tol_abs);
+    s->last = e.reports()[0];
+    s->last_ms = e.last_solve_ms();
+    if (want_coef) { e.adjoint_gradient(fphi, pb, pa); }
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+    count_launches(e);
+    if (s->last.status == NOT_CONVERGED) { g_err = "adjoint MLMG failed to converge"; }
+    if (s->last.status == ERR_DIVERGED) { g_err = "adjoint MLMG blew up"; }
+    if (s->last.status == ERR_NONFINITE) { g_err = "adjoint MLMG residual is not finite"; }
     return s->last.status;
     API_END
 }

@@ -123,7 +123,7 @@ struct FaceBC {
     int type;            // BC type code (only used where the mask is > 0)
     int nx;              // number of interpolation points of the Dirichlet closure
     int mask_uniform;    // uniform mask value of the face, or -1 if per-cell
-    int pad_;
+    int on_domain;       // 1 if the patch face lies on the domain boundary (periodic or not)
     long long mask_off;  // offset of the per-cell mask (int8) in the level's mask array
     long long bcval_off; // offset of the face's Dirichlet values in the level's bcval array, -1 if none
     double coef[4];      // closure coefficients (coef[0] multiplies the boundary value)

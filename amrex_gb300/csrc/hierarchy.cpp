@@ -233,6 +233,7 @@ PatchLevel build_patch_level (const std::vector<const SolveSpec*>& solves, int l
                 const bool hi = f >= 3;
                 FaceBC& F = P.face[f];
                 const bool on_domain = hi ? (LG.geom.domain.hi[d] == pb.hi[d]) : (LG.geom.domain.lo[d] == pb.lo[d]);
+                F.on_domain = on_domain ? 1 : 0;
                 double bcl;
                 // MLMGBndryT::setBoxBC (Src/LinearSolvers/MLMG/AMReX_MLMGBndry.H:106-150)
                 if (on_domain && !LG.geom.periodic[d]) {

@@ -4,6 +4,7 @@
 #include "stencil_kernels.cuh"
 #include "fused_sweep.cuh"
 #include "coarse_vcycle.cuh"
+#include "adjoint_kernels.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -66,6 +67,8 @@ struct LevelData {
     // FP64 fields
     DevBuf<double> cor, res, rescor, a, bx, by, bz;
     DevBuf<double> sol, rhs, bcval;                 // level 0 only
+    DevBuf<double> adj_phi, adj_g[4];               // level 0, adjoint gradients (on demand)
+    DevBuf<double> partner;                         // level 0, periodic image face coefficients (A^T)
     // FP32 fields (mixed precision)
     DevBuf<float> cor32, res32, rescor32;
     // stencil form of the ABec operator (mixed path): FP64 on every level,
@@ -740,6 +743,32 @@ void Engine::Impl::reduce_per_solve (int l, const SubsetData& S, int op, const d
 void Engine::Impl::residual0 (bool to32)
 {
     LevelData& L = lev[0];
+    if (E.m_opt.transpose) {
+        // adjoint solve: r = rhs - A^T sol, FP64, homogeneous BCs
+        MLMG_CUDA_CHECK(cudaMemsetAsync(red_out.p, 0, sizeof(double) * nsolve, st()));
+        ghost<double>(0, L.sol.p, false, true);
+        const unsigned g = (unsigned)L.all.ntiles;
+        const double *a = L.a.p, *bx = L.bx.p, *by = L.by.p, *bz = L.bz.p;
+        if (to32) {
+            if (abec) {
+                k_residual_transpose<float, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res32.p, L.sol.p,
+                    L.rhs.p, a, bx, by, bz, L.partner.p, red_out.p);
+            } else {
+                k_residual_transpose<float, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res32.p, L.sol.p,
+                    L.rhs.p, a, bx, by, bz, L.partner.p, red_out.p);
+            }
+        } else {
+            if (abec) {
+                k_residual_transpose<double, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res.p, L.sol.p,
+                    L.rhs.p, a, bx, by, bz, L.partner.p, red_out.p);
+            } else {
+                k_residual_transpose<double, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res.p, L.sol.p,
+                    L.rhs.p, a, bx, by, bz, L.partner.p, red_out.p);
+            }
+        }
+        launched();
+        return;
+    }
     if (to32) {
         // mixed path: FP64 residual in stencil form, FP32 copy for the V-cycle,
         // per-solve max-norm by atomic max (zeroed first)
@@ -769,22 +798,12 @@ void Engine::Impl::residual0 (bool to32)
     }
     ghost<double>(0, L.sol.p, true, true);
     const double *a = L.a.p, *bx = L.bx.p, *by = L.by.p, *bz = L.bz.p;
-    if (false) {
-        if (abec) {
-            k_residual<double, float, true><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res32.p,
-                L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
-        } else {
-            k_residual<double, float, false><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res32.p,
-                L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
-        }
+    if (abec) {
+        k_residual<double, double, true><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res.p,
+            L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
     } else {
-        if (abec) {
-            k_residual<double, double, true><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res.p,
-                L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
-        } else {
-            k_residual<double, double, false><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res.p,
-                L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
-        }
+        k_residual<double, double, false><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res.p,
+            L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
     }
     k_reduce_final<<<nsolve, 256, 0, st()>>>(partial.p, L.all.solve_begin.p, RED_MAXABS, red_out.p);
     launched(2);
@@ -951,6 +970,38 @@ void Engine::apply (const FabSet& in, FabSet& out)
     I.xfer(I.items_for(out, 0, 0, -1), out, L0.res.p, false, 1);
 }
 
+void Engine::adjoint_gradient (const FabSet& phi, FabSet* const grad_b[3], FabSet* grad_a)
+{
+    Impl& I = *m_impl;
+    MLMG_REQUIRE(I.nsolve == 1 && m_opt.transpose, ERR_INTERNAL, "adjoint_gradient needs a transposed engine of one solve");
+    MLMG_REQUIRE(I.abec, ERR_UNSUPPORTED, "coefficient gradients need MLABecLaplacian");
+    LevelData& L0 = I.lev[0];
+    const size_t n = (size_t)L0.meta.nelem;
+    if (L0.adj_phi.n != n) {
+        L0.adj_phi.alloc(n);
+        for (auto& g : L0.adj_g) { g.alloc(n); }
+    }
+    // phi with the ghosts of the inhomogeneous applyBC; lambda (the last
+    // transposed solution, valid cells) with copies between patches
+    L0.adj_phi.zero(m_stream);
+    I.xfer(I.items_for(phi, 0, 0, -1), phi, L0.adj_phi.p, false, 0);
+    I.ghost<double>(0, L0.adj_phi.p, true, true);
+    I.ghost<double>(0, L0.sol.p, false, true);
+    double* g[3];
+    for (int d = 0; d < 3; ++d) { g[d] = grad_b[d] ? L0.adj_g[d].p : nullptr; }
+    k_face_grad<<<L0.all.ntiles, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.adj_phi.p, L0.sol.p, g[0], g[1],
+                                                            g[2], grad_a ? L0.adj_g[3].p : nullptr);
+    I.launched();
+    MLMG_CUDA_CHECK(cudaGetLastError());
+    for (int d = 0; d < 3; ++d) {
+        if (grad_b[d]) {
+            MLMG_REQUIRE(grad_b[d]->nodal_dir == d, ERR_ARGS, "dJ/db MultiFabs must be face-centred in x, y, z");
+            I.xfer(I.items_for(*grad_b[d], 0, 0, d), *grad_b[d], L0.adj_g[d].p, false, 1);
+        }
+    }
+    if (grad_a) { I.xfer(I.items_for(*grad_a, 0, 0, -1), *grad_a, L0.adj_g[3].p, false, 1); }
+}
+
 void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<FabSet*>& sol_out,
                     const std::vector<const FabSet*>& rhs, double tol_rel, double tol_abs)
 {
@@ -971,6 +1022,15 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
     // enforce solvability of singular problems (MLMGT::makeSolvable, AMReX_MLMG.H:1844-1858)
     bool any_singular = false;
     for (int s : I.singular) { if (s) { any_singular = true; } }
+    MLMG_REQUIRE(!(any_singular && m_opt.transpose), ERR_UNSUPPORTED,
+                 "adjoint solves of singular operators are not supported");
+    if (m_opt.transpose && I.abec && L0.gw.ntagcells > 0) {
+        if (L0.partner.n != (size_t)L0.meta.nelem) { L0.partner.alloc((size_t)L0.meta.nelem); }
+        L0.partner.zero(m_stream);
+        k_partner_faces<<<(unsigned)((L0.gw.ntagcells + 255) / 256), 256, 0, m_stream>>>(L0.dl, L0.gw, L0.bx.p,
+            L0.by.p, L0.bz.p, L0.partner.p);
+        I.launched();
+    }
     if (any_singular) {
         k_reduce<double><<<L0.all.ntiles, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.rhs.p, nullptr, RED_SUM,
                                                                     I.partial.p);

@@ -42,6 +42,8 @@ struct EngineOptions {
                                 // (slower than graph-replayed grid-wide launches on GB300 at every
                                 // threshold from 2^3 to 32^3 cells)
     int coarse_cells = 512;     // a level is coarse when every solve has at most this many cells on it
+    int transpose = 0;          // solve A^T x = rhs (homogeneous BCs): the outer residual uses A^T,
+                                // the V-cycle of A is the correction operator (adjoint solves)
 };
 
 // Live timing of the dominant kernel (the finest-level smoother).
@@ -86,6 +88,13 @@ public:
 
     // out = L(in) with inhomogeneous BCs (MLMGT::apply)
     void apply (const FabSet& in, FabSet& out);
+
+    // After a transposed solve (options().transpose) of a batch of one, whose
+    // solution lambda solves A^T lambda = dJ/dphi: the face-gradient
+    // contraction dJ/db[d] = -beta dxinv_d^2 (phi_c - phi_{c-1})(lam_c - lam_{c-1})
+    // and dJ/da = -alpha lam phi for the forward solution phi (MLABecLaplacian).
+    // Null outputs are skipped.
+    void adjoint_gradient (const FabSet& phi, FabSet* const grad_b[3], FabSet* grad_a);
 
     const std::vector<SolveReport>& reports () const { return m_reports; }
     int nlevels (int s) const { return (int)m_problems[s].spec.levels.size(); }

@@ -52,3 +52,13 @@ def abec_problem(n, mgs, rhs_seed, b_seed, rhs_host=None, bcoef_host=None):
         faces.append(f)
     op.setBCoeffs(0, faces)
     return dict(n=n, ba=ba, dm=dm, geom=geom, sol=sol, rhs=rhs, op=op, faces=faces, rhs_h=rhs_h, b_h=b_h)
+
+
+def adjoint_objective(n, phi_scale, target_seed=3003):
+    """J = 0.5 * sum over the central half-width cube [n/4, 3n/4)^3 of
+    (phi - phi_t)^2, phi_t = phi_scale * (a smooth random field, 5-cell
+    Gaussian, unit variance).  Returns (phi_t, region slices z-major)."""
+    tgt = phi_scale * synth.smooth_field(n, target_seed)
+    q = n // 4
+    region = (slice(q, n - q),) * 3
+    return tgt, region

@@ -197,6 +197,20 @@ int mlmg_get_num_mg_levels(mlmg_solver s);
 int mlmg_solve_batched(int n, const mlmg_solver* solvers, const mlmg_multifab* sols, const mlmg_multifab* rhss,
                        double tol_rel, double tol_abs, int* status);
 
+/* Adjoint gradients of J(phi) for the solution phi = sol of A phi = f (no
+ * counterpart in the reference; the face-gradient contraction is the one of
+ * MLMG::getGradSolution / compFlux, AMReX_MLMG.H:553-761).  Solves
+ * A^T lambda = dJdphi (homogeneous BCs, same MLMG settings and precision as
+ * s, to tol_rel/tol_abs) and writes dJ/df = lambda into out_dJdf.  For
+ * MLABecLaplacian, out_dJdb[3] (face-centred MultiFabs, entries may be NULL,
+ * or the pointer NULL) receive dJ/db = -beta dxinv^2 (phi_c - phi_{c-1})
+ * (lambda_c - lambda_{c-1}) per face (lambda = 0 outside the domain, phi's
+ * ghosts from the level BC), and out_dJda (may be NULL) dJ/da = -alpha
+ * lambda phi.  Returns the adjoint solve's status; the solver's getters then
+ * report the adjoint solve.  Singular operators are rejected (-4). */
+int mlmg_adjoint_grad(mlmg_solver s, mlmg_multifab sol, mlmg_multifab dJdphi, double tol_rel, double tol_abs,
+                      mlmg_multifab out_dJdf, const mlmg_multifab* out_dJdb, mlmg_multifab out_dJda);
+
 #if defined(__GNUC__)
 #pragma GCC visibility pop
 #endif
