@@ -335,6 +335,16 @@ class MLMG:
         rc = capi.lib().mlmg_solve(self._h, sol._h, rhs._h, float(tol_rel), float(tol_abs), ctypes.byref(r))
         return rc, r.value
 
+    def getFluxes(self, flux, sol):
+        """MLMG::getFluxes of ``sol`` into three face-centred MultiFabs."""
+        F = (ctypes.c_void_p * 3)(*[(m._h if m is not None else None) for m in flux])
+        check(capi.lib().mlmg_get_fluxes(self._h, sol._h, F))
+
+    def getGradSolution(self, grad, sol):
+        """MLMG::getGradSolution of ``sol`` into three face-centred MultiFabs."""
+        G = (ctypes.c_void_p * 3)(*[(m._h if m is not None else None) for m in grad])
+        check(capi.lib().mlmg_get_grad_solution(self._h, sol._h, G))
+
     def adjointGrad(self, sol, dJdphi, tol_rel, tol_abs, dJdf, dJdb=None, dJda=None):
         """Adjoint gradients of J(phi) at the solution ``sol``: solves
         A^T lambda = dJdphi, writes dJ/df = lambda into ``dJdf`` and, for

@@ -86,6 +86,8 @@ SIGNATURES = {
     "mlmg_get_smoother_stats": (c_int, [c_void_p, P(c_double), P(ctypes.c_longlong), P(c_double), c_int]),
     "mlmg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_double, P(c_double)]),
     "mlmg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "mlmg_get_fluxes": (c_int, [c_void_p, c_void_p, P(c_void_p)]),
+    "mlmg_get_grad_solution": (c_int, [c_void_p, c_void_p, P(c_void_p)]),
     "mlmg_get_num_iters": (c_int, [c_void_p]),
     "mlmg_get_residual_history": (c_int, [c_void_p, P(c_double), c_int]),
     "mlmg_get_num_cg_iters": (c_int, [c_void_p, P(c_int), c_int]),

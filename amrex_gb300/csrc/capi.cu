@@ -1047,6 +1047,44 @@ int mlmg_adjoint_grad (mlmg_solver s, mlmg_multifab sol, mlmg_multifab dJdphi, d
     API_END
 }
 
+namespace {
+int face_fluxes_impl (mlmg_solver s, mlmg_multifab sol, const mlmg_multifab* out, int mode)
+{
+    check_solver_mf(s, sol);
+    MLMG_REQUIRE(out != nullptr, ERR_ARGS, "null output array");
+    FabSet fo[3];
+    FabSet* po[3] = {nullptr, nullptr, nullptr};
+    for (int d = 0; d < 3; ++d) {
+        mlmg_multifab m = out[d];
+        if (m == nullptr) { continue; }
+        MLMG_REQUIRE(m->ncomp == 1 && m->prec == 8 && m->nodal_dir == d && m->boxes == s->op->boxes, ERR_ARGS,
+                     "output[d] must be an FP64 MultiFab on the operator's BoxArray, face-centred in d");
+        fo[d] = m->fabset();
+        po[d] = &fo[d];
+    }
+    Engine& e = engine_for(s);
+    FabSet fs = sol->fabset();
+    e.face_fluxes(fs, po, mode);
+    count_launches(e);
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(lib_stream()));
+    return OK;
+}
+} // namespace
+
+int mlmg_get_fluxes (mlmg_solver s, mlmg_multifab sol, const mlmg_multifab* flux)
+{
+    API_BEGIN
+    return face_fluxes_impl(s, sol, flux, 1);
+    API_END
+}
+
+int mlmg_get_grad_solution (mlmg_solver s, mlmg_multifab sol, const mlmg_multifab* grad)
+{
+    API_BEGIN
+    return face_fluxes_impl(s, sol, grad, 0);
+    API_END
+}
+
 int mlmg_apply (mlmg_solver s, mlmg_multifab out, mlmg_multifab in)
 {
     API_BEGIN

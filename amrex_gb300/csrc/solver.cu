@@ -5,6 +5,7 @@
 #include "fused_sweep.cuh"
 #include "coarse_vcycle.cuh"
 #include "adjoint_kernels.cuh"
+#include "flux_kernels.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -67,7 +68,8 @@ struct LevelData {
     // FP64 fields
     DevBuf<double> cor, res, rescor, a, bx, by, bz;
     DevBuf<double> sol, rhs, bcval;                 // level 0 only
-    DevBuf<double> adj_phi, adj_g[4];               // level 0, adjoint gradients (on demand)
+    DevBuf<double> face_phi, face_out[4];           // level 0 scratch: a solution with ghosts and face outputs
+                                                    // (adjoint gradients, fluxes), allocated on demand
     DevBuf<double> partner;                         // level 0, periodic image face coefficients (A^T)
     // FP32 fields (mixed precision)
     DevBuf<float> cor32, res32, rescor32;
@@ -970,6 +972,43 @@ void Engine::apply (const FabSet& in, FabSet& out)
     I.xfer(I.items_for(out, 0, 0, -1), out, L0.res.p, false, 1);
 }
 
+void Engine::face_fluxes (const FabSet& phi, FabSet* const out[3], int mode)
+{
+    Impl& I = *m_impl;
+    MLMG_REQUIRE(I.nsolve == 1, ERR_UNSUPPORTED, "fluxes are computed for a single solve");
+    MLMG_REQUIRE(mode == 0 || mode == 1, ERR_ARGS, "mode must be 0 (gradient) or 1 (flux)");
+    LevelData& L0 = I.lev[0];
+    const size_t n = (size_t)L0.meta.nelem;
+    if (L0.face_phi.n != n) {
+        L0.face_phi.alloc(n);
+        for (auto& g : L0.face_out) { g.alloc(n); }
+    }
+    L0.face_phi.zero(m_stream);
+    I.xfer(I.items_for(phi, 0, 0, -1), phi, L0.face_phi.p, false, 0);
+    I.ghost<double>(0, L0.face_phi.p, true, true);
+    double* o[3] = {L0.face_out[0].p, L0.face_out[1].p, L0.face_out[2].p};
+    const unsigned g = (unsigned)L0.all.ntiles;
+    const double *bx = L0.bx.p, *by = L0.by.p, *bz = L0.bz.p;
+    if (mode == 0) {
+        k_face_flux<0, false><<<g, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.face_phi.p, bx, by, bz, o[0],
+                                                              o[1], o[2]);
+    } else if (I.abec) {
+        k_face_flux<1, true><<<g, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.face_phi.p, bx, by, bz, o[0],
+                                                             o[1], o[2]);
+    } else {
+        k_face_flux<1, false><<<g, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.face_phi.p, bx, by, bz, o[0],
+                                                              o[1], o[2]);
+    }
+    I.launched();
+    MLMG_CUDA_CHECK(cudaGetLastError());
+    for (int d = 0; d < 3; ++d) {
+        if (out[d]) {
+            MLMG_REQUIRE(out[d]->nodal_dir == d, ERR_ARGS, "face MultiFabs must be face-centred in x, y, z");
+            I.xfer(I.items_for(*out[d], 0, 0, d), *out[d], L0.face_out[d].p, false, 1);
+        }
+    }
+}
+
 void Engine::adjoint_gradient (const FabSet& phi, FabSet* const grad_b[3], FabSet* grad_a)
 {
     Impl& I = *m_impl;
@@ -977,29 +1016,29 @@ void Engine::adjoint_gradient (const FabSet& phi, FabSet* const grad_b[3], FabSe
     MLMG_REQUIRE(I.abec, ERR_UNSUPPORTED, "coefficient gradients need MLABecLaplacian");
     LevelData& L0 = I.lev[0];
     const size_t n = (size_t)L0.meta.nelem;
-    if (L0.adj_phi.n != n) {
-        L0.adj_phi.alloc(n);
-        for (auto& g : L0.adj_g) { g.alloc(n); }
+    if (L0.face_phi.n != n) {
+        L0.face_phi.alloc(n);
+        for (auto& g : L0.face_out) { g.alloc(n); }
     }
     // phi with the ghosts of the inhomogeneous applyBC; lambda (the last
     // transposed solution, valid cells) with copies between patches
-    L0.adj_phi.zero(m_stream);
-    I.xfer(I.items_for(phi, 0, 0, -1), phi, L0.adj_phi.p, false, 0);
-    I.ghost<double>(0, L0.adj_phi.p, true, true);
+    L0.face_phi.zero(m_stream);
+    I.xfer(I.items_for(phi, 0, 0, -1), phi, L0.face_phi.p, false, 0);
+    I.ghost<double>(0, L0.face_phi.p, true, true);
     I.ghost<double>(0, L0.sol.p, false, true);
     double* g[3];
-    for (int d = 0; d < 3; ++d) { g[d] = grad_b[d] ? L0.adj_g[d].p : nullptr; }
-    k_face_grad<<<L0.all.ntiles, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.adj_phi.p, L0.sol.p, g[0], g[1],
-                                                            g[2], grad_a ? L0.adj_g[3].p : nullptr);
+    for (int d = 0; d < 3; ++d) { g[d] = grad_b[d] ? L0.face_out[d].p : nullptr; }
+    k_face_grad<<<L0.all.ntiles, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.face_phi.p, L0.sol.p, g[0], g[1],
+                                                            g[2], grad_a ? L0.face_out[3].p : nullptr);
     I.launched();
     MLMG_CUDA_CHECK(cudaGetLastError());
     for (int d = 0; d < 3; ++d) {
         if (grad_b[d]) {
             MLMG_REQUIRE(grad_b[d]->nodal_dir == d, ERR_ARGS, "dJ/db MultiFabs must be face-centred in x, y, z");
-            I.xfer(I.items_for(*grad_b[d], 0, 0, d), *grad_b[d], L0.adj_g[d].p, false, 1);
+            I.xfer(I.items_for(*grad_b[d], 0, 0, d), *grad_b[d], L0.face_out[d].p, false, 1);
         }
     }
-    if (grad_a) { I.xfer(I.items_for(*grad_a, 0, 0, -1), *grad_a, L0.adj_g[3].p, false, 1); }
+    if (grad_a) { I.xfer(I.items_for(*grad_a, 0, 0, -1), *grad_a, L0.face_out[3].p, false, 1); }
 }
 
 void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<FabSet*>& sol_out,

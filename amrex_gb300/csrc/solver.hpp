@@ -96,6 +96,11 @@ public:
     // Null outputs are skipped.
     void adjoint_gradient (const FabSet& phi, FabSet* const grad_b[3], FabSet* grad_a);
 
+    // MLMG::getGradSolution (mode 0) / MLMG::getFluxes (mode 1) of the
+    // solution phi of a batch of one: face arrays of every box, phi's ghosts
+    // from applyBC with the level's boundary values.  Null outputs are skipped.
+    void face_fluxes (const FabSet& phi, FabSet* const out[3], int mode);
+
     const std::vector<SolveReport>& reports () const { return m_reports; }
     int nlevels (int s) const { return (int)m_problems[s].spec.levels.size(); }
     const EngineOptions& options () const { return m_opt; }

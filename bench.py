@@ -266,6 +266,45 @@ def bench_batch(stream, nsolve=64):
             "phi_rel_diff_vs_fp64_max": err}
 
 
+def bench_adjoint(stream, n=128):
+    """Adjoint gradients dJ/db (all faces) and dJ/df of J = 0.5 |phi - phi_t|^2
+    over the central (n/2)^3 for the n^3 variable-coefficient ABecLaplacian:
+    one mlmg_adjoint_grad call (transposed solve to 1e-10 plus the fused
+    face-gradient contraction), FP64 and mixed, device time."""
+    import torch
+    import amrex_gb300 as ag
+    from amrex_gb300 import workloads
+    p = workloads.abec_problem(n, 64, 1003, 2003)
+    out = {"workload": f"adjoint of MLABecLaplacian {n}^3 (log-normal b, contrast 1e3), J over the central "
+                       f"{n // 2}^3, tol_rel 1e-10"}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for prec in ("fp64", "mixed"):
+        m = ag.MLMG(p["op"])
+        m.setPrecision(prec)
+        m.setGraph(prec == "mixed")
+        m.setFusedSmoother(prec == "mixed")
+        p["sol"].setVal(0.0)
+        m.solve(p["sol"], p["rhs"], TOL_REL, 0.0)
+        phi = p["sol"].get_global((n, n, n))
+        tgt, region = workloads.adjoint_objective(n, float(phi.std()))
+        g = np.zeros_like(phi)
+        g[region] = phi[region] - tgt[region]
+        gm = ag.MultiFab(p["ba"], p["dm"], 1, 0)
+        gm.set_global(g)
+        lam = ag.MultiFab(p["ba"], p["dm"], 1, 0)
+        gb = [ag.MultiFab(p["ba"], p["dm"], 1, 0, nodal_dir=d) for d in range(3)]
+        m.adjointGrad(p["sol"], gm, TOL_REL, 0.0, lam, gb)
+        reps = 3
+        e0.record(stream)
+        for _ in range(reps):
+            m.adjointGrad(p["sol"], gm, TOL_REL, 0.0, lam, gb)
+        e1.record(stream)
+        e1.synchronize()
+        out[f"{prec}_ms"] = e0.elapsed_time(e1) / reps
+        out[f"{prec}_iters"] = m.getNumIters()
+    return out
+
+
 def run_gb300(args, ws, rank, local):
     import torch
     import amrex_gb300 as ag
@@ -386,6 +425,7 @@ def run_gb300(args, ws, rank, local):
     }
     if not args.no_batch:
         line["batch"] = bench_batch(stream)
+        line["adjoint"] = bench_adjoint(stream)
     if rank == 0 and ws == 1 and not args.no_cpu:
         import multiprocessing
         os.environ.setdefault("OMP_NUM_THREADS", str(multiprocessing.cpu_count()))

@@ -180,6 +180,16 @@ int mlmg_solve(mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, double tol_r
                double* final_resid);
 /* MLMGT::apply (AMReX_MLMG.H:858-932): out = L(in) with the level BC values */
 int mlmg_apply(mlmg_solver s, mlmg_multifab out, mlmg_multifab in);
+/* MLMGT::getFluxes(a_flux, a_sol, loc) (AMReX_MLMG.H:627-655) and
+ * MLMGT::getGradSolution (AMReX_MLMG.H:553-572): face-centred FP64 MultiFabs
+ * flux[3] / grad[3] (entries may be NULL) of the solution sol, whose ghost
+ * values come from the operator's boundary conditions and level BC values.
+ * flux = -b dphi/dn (MLABecLaplacian, after the 1/beta scaling of
+ * MLCellABecLapT::getFluxes) or -dphi/dn (MLPoisson); grad = dphi/dn.  The
+ * reference's variants read the solver's internal solution; here the
+ * solution is passed explicitly (the one given to mlmg_solve). */
+int mlmg_get_fluxes(mlmg_solver s, mlmg_multifab sol, const mlmg_multifab* flux);
+int mlmg_get_grad_solution(mlmg_solver s, mlmg_multifab sol, const mlmg_multifab* grad);
 /* getters (AMReX_MLMG.H:220-228) and the device time of the last solve */
 int mlmg_get_num_iters(mlmg_solver s);
 int mlmg_get_residual_history(mlmg_solver s, double* out, int max);

@@ -1072,6 +1072,62 @@ int oracle_apply(const OracleProblem* P, const OracleOptions* o, double* out) {
     return 0;
 }
 
+/* MLMGT::getGradSolution -> MLCellLinOpT::compGrad (AMReX_MLCellLinOp.H:1392-1442)
+ * for mode 0; MLMGT::getFluxes -> MLCellABecLapT::getFluxes
+ * (AMReX_MLCellABecLap.H:272-291) -> compFlux (AMReX_MLCellLinOp.H:1348-1390)
+ * -> FFlux (mlabeclap_flux_x, AMReX_MLABecLap_3D_K.H:79-97; mlpoisson_flux_x,
+ * AMReX_MLPoisson_3D_K.H:36-50) then the 1/beta scaling for mode 1.  The
+ * solution's ghosts come from applyBC with the level's Dirichlet values.
+ * Outputs are global face arrays (n_d + 1 along d), written box by box over
+ * each box's surrounding nodes. */
+int oracle_fluxes(const OracleProblem* P, const OracleOptions* o, int mode, double* fx, double* fy, double* fz) {
+    Solver* S = (Solver*)calloc(1, sizeof(Solver));
+    OracleOptions oo = *o; oo.max_coarsening_level = 0;
+    setup(S, P, &oo);
+    set_coeffs(S, P);
+    Hier* H = &S->H;
+    Level* L = &H->lev[0];
+    S->bcval.v = P->sol; for (int d = 0; d < 3; ++d) S->bcval.n[d] = P->n[d];
+    MF x;
+    mf_define(&x, L->nbox, L->boxes, 1, -1);
+    copy_global_to_mf(L, &x, P->sol, 1, -1);
+    apply_bc(H, L, &x, 1, &S->bcval, 0);
+    double* out[3] = {fx, fy, fz};
+    const double bscalar = H->is_abec ? H->beta : -1.0;   /* MLPoissonT::getBScalar is -1 */
+    const double betainv = 1.0 / bscalar;
+    for (int b = 0; b < L->nbox; ++b) {
+        const Box* vb = &L->boxes[b];
+        const Fab* s = &x.fab[b];
+        for (int d = 0; d < 3; ++d) {
+            int e[3] = {P->n[0], P->n[1], P->n[2]};
+            e[d] += 1;
+            const int di = (d == 0), dj = (d == 1), dk = (d == 2);
+            const double dxi = L->dxinv[d];
+            for (int k = vb->lo[2]; k <= vb->hi[2] + dk; ++k)
+            for (int j = vb->lo[1]; j <= vb->hi[1] + dj; ++j)
+            for (int i = vb->lo[0]; i <= vb->hi[0] + di; ++i) {
+                const double ds = A(s, i, j, k) - A(s, i - di, j - dj, k - dk);
+                double v;
+                if (mode == 0) {
+                    v = dxi * ds;
+                } else if (H->is_abec) {
+                    const double fac = H->beta * dxi;
+                    v = -fac * A(&L->bcoef[d].fab[b], i, j, k) * ds;
+                    if (betainv != 1.0) v *= betainv;
+                } else {
+                    v = dxi * ds;
+                    v *= betainv;
+                }
+                out[d][((size_t)k * e[1] + j) * e[0] + i] = v;
+            }
+        }
+    }
+    mf_free(&x);
+    free_solver(S);
+    free(S);
+    return 0;
+}
+
 void oracle_default_options(OracleOptions* o) {
     memset(o, 0, sizeof(*o));
     o->agg = 1; o->con = 1; o->agg_grid_size = 32; o->con_grid_size = 32; o->max_coarsening_level = 30;

@@ -46,6 +46,8 @@ int oracle_hierarchy(const OracleProblem* P, const OracleOptions* o, int* nbox_p
                      int max_boxes);
 int oracle_fill_boundary(const OracleProblem* P, int cross, double* data);
 int oracle_apply(const OracleProblem* P, const OracleOptions* o, double* out);
+/* mode 0: getGradSolution, mode 1: getFluxes; global face arrays */
+int oracle_fluxes(const OracleProblem* P, const OracleOptions* o, int mode, double* fx, double* fy, double* fz);
 int oracle_solve(const OracleProblem* P, const OracleOptions* o, double* phi_out, OracleResult* R);
 
 #ifdef __cplusplus

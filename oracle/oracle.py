@@ -69,6 +69,8 @@ def lib():
         _lib.oracle_hierarchy.argtypes = [P(Problem), P(Options), P(ctypes.c_int), P(ctypes.c_int), ctypes.c_int]
         _lib.oracle_fill_boundary.argtypes = [P(Problem), ctypes.c_int, P(ctypes.c_double)]
         _lib.oracle_apply.argtypes = [P(Problem), P(Options), P(ctypes.c_double)]
+        _lib.oracle_fluxes.argtypes = [P(Problem), P(Options), ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double),
+                                       P(ctypes.c_double)]
         _lib.oracle_solve.argtypes = [P(Problem), P(Options), P(ctypes.c_double), P(Result)]
     return _lib
 
@@ -155,6 +157,19 @@ def apply(case, arrays):
     nx, ny, nz = case["n"]
     out = np.zeros((nz, ny, nx))
     lib().oracle_apply(ctypes.byref(p), ctypes.byref(o), _dp(out))
+    return out
+
+
+def fluxes(case, arrays, mode):
+    """mode "grad" (MLMG::getGradSolution) or "flux" (MLMG::getFluxes) of the
+    solution in arrays["sol"] (valid cells + level BC values in the ghosts);
+    returns the three global face arrays, z-major."""
+    p, keep = make_problem(case, arrays)
+    o = make_options(case)
+    nx, ny, nz = case["n"]
+    out = [np.zeros((nz, ny, nx + 1)), np.zeros((nz, ny + 1, nx)), np.zeros((nz + 1, ny, nx))]
+    lib().oracle_fluxes(ctypes.byref(p), ctypes.byref(o), 0 if mode == "grad" else 1, _dp(out[0]), _dp(out[1]),
+                        _dp(out[2]))
     return out
 
 

@@ -11,6 +11,7 @@
 //            fb     : FillBoundary on a MultiFab with 1 ghost      -> fb_out.bin
 //            apply  : MLMG::apply (out = L phi, inhomogeneous BC)  -> out.bin
 //            solve  : MLMG::solve                                  -> phi.bin, result.txt
+//            flux   : solve, then getFluxes / getGradSolution    -> also f[xyz].bin, g[xyz].bin
 //
 // case.txt holds "key value..." lines; binary inputs are little-endian
 // float64 arrays over the whole domain, x fastest.
@@ -307,6 +308,26 @@ int main (int argc, char* argv[])
                     Global go{nx, ny, nz, 0, 0, 0, std::vector<double>((size_t)nx*ny*nz)};
                     copy_to_global(sol, go);
                     write_bin(dir + "/phi.bin", go.v);
+                    if (mode == "flux") {
+                        // MLMG::getFluxes (with the solution passed explicitly) and
+                        // MLMG::getGradSolution on face MultiFabs
+                        Array<MultiFab,3> flux, grad;
+                        for (int d = 0; d < 3; ++d) {
+                            const BoxArray fba = amrex::convert(ba, IntVect::TheDimensionVector(d));
+                            flux[d].define(fba, dm, 1, 0);
+                            grad[d].define(fba, dm, 1, 0);
+                        }
+                        mlmg.getFluxes({amrex::GetArrOfPtrs(flux)}, {&sol}, MLMG::Location::FaceCenter);
+                        mlmg.getGradSolution({amrex::GetArrOfPtrs(grad)});
+                        for (int d = 0; d < 3; ++d) {
+                            Global gf{nx + (d==0), ny + (d==1), nz + (d==2), 0, 0, 0, {}};
+                            gf.v.assign((size_t)gf.nx*gf.ny*gf.nz, 0.0);
+                            copy_to_global(flux[d], gf);
+                            write_bin(dir + "/f" + char('x'+d) + ".bin", gf.v);
+                            copy_to_global(grad[d], gf);
+                            write_bin(dir + "/g" + char('x'+d) + ".bin", gf.v);
+                        }
+                    }
                     res << "final_resid " << resid << "\n";
                     res << "init_resid " << mlmg.getInitResidual() << "\n";
                     res << "rhs_norm " << mlmg.getInitRHS() << "\n";

@@ -73,6 +73,15 @@ CASES = {
                          maxorder=4),
     "solve_poisson_periodic_x": _c(mode="solve", n=(32, 24, 16), max_grid_size=8, rhs_seed=1009,
                                    periodic=(1, 0, 0), lobc=(200, 101, 102), hibc=(200, 102, 101)),
+    # --- MLMG::getFluxes / getGradSolution after a solve ----------------------
+    "flux_abec_32": _c(mode="flux", op="abec", n=(32, 32, 32), max_grid_size=16, rhs_seed=1011, b_seed=2011,
+                       beta=2.0),
+    "flux_abec_mixed_bc": _c(mode="flux", op="abec", n=(32, 24, 16), max_grid_size=8, rhs_seed=1012,
+                             b_seed=2012, a_seed=3012, sol_seed=3013, alpha=1.0, beta=0.5,
+                             lobc=(101, 102, 101), hibc=(102, 101, 101)),
+    "flux_poisson_32": _c(mode="flux", n=(32, 32, 32), max_grid_size=16, rhs_seed=1013, sol_seed=3014),
+    "flux_poisson_periodic_x": _c(mode="flux", n=(32, 24, 16), max_grid_size=8, rhs_seed=1014,
+                                  periodic=(1, 0, 0), lobc=(200, 101, 102), hibc=(200, 102, 101)),
 }
 
 
@@ -84,7 +93,7 @@ def sol_grown(case):
         return np.zeros((nz + 2, ny + 2, nx + 2))
     rng = np.random.Generator(np.random.PCG64(case["sol_seed"]))
     v = rng.uniform(-1.0, 1.0, size=(nz + 2, ny + 2, nx + 2))
-    if case["mode"] == "solve":
+    if case["mode"] in ("solve", "flux"):
         v[1:-1, 1:-1, 1:-1] = 0.0
     return v
 

@@ -3,7 +3,7 @@ CPU MLMG (built from the reference sources by ``oracle/ref/Makefile`` into
 ``oracle/_ref/ref_driver``) on seeded synthetic inputs.
 
     make -C oracle/ref -j8          # needs the reference source tree
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name-prefix ...]
 
 Each fixture is a ``.npz`` holding the case description (as the text of the
 driver's case file), the inputs that are not regenerated from seeds, and the
@@ -40,7 +40,7 @@ def run_case(mode, case):
         res = os.path.join(d, "result.txt")
         if os.path.exists(res):
             out["result"] = open(res).read()
-        for name in ("phi.bin", "out.bin", "fb_out.bin"):
+        for name in ("phi.bin", "out.bin", "fb_out.bin", "fx.bin", "fy.bin", "fz.bin", "gx.bin", "gy.bin", "gz.bin"):
             p = os.path.join(d, name)
             if os.path.exists(p):
                 out[name[:-4]] = np.fromfile(p, dtype=np.float64)
@@ -53,7 +53,10 @@ def run_case(mode, case):
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("build the reference driver first: make -C oracle/ref -j8")
+    only = sys.argv[1:]          # optional name prefixes to regenerate
     for name, case in cases.CASES.items():
+        if only and not any(name.startswith(p) for p in only):
+            continue
         mode = case["mode"]
         out = run_case(mode, case)
         payload = {"case": np.array(repr(case))}
@@ -61,7 +64,7 @@ def main():
             payload["result"] = np.array(out["result"])
         if "hier" in out:
             payload["hier"] = np.array(out["hier"])
-        for k in ("phi", "out", "fb_out"):
+        for k in ("phi", "out", "fb_out", "fx", "fy", "fz", "gx", "gy", "gz"):
             if k in out:
                 payload[k] = out[k]
         if mode == "fb":

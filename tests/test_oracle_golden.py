@@ -57,3 +57,22 @@ def test_solve_matches_reference(name):
                                atol=1e-13 * max(r["rhs_norm"], r["init_resid"]))
     # phi agrees to 1e-10 relative (max norm)
     assert np.abs(phi - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", load.names("flux_"))
+def test_oracle_fluxes_match_reference(name):
+    """getFluxes / getGradSolution of the reference's own solution: the
+    oracle's restatement reproduces the reference bit for bit."""
+    g = load.load(name)
+    c = g["case"]
+    nx, ny, nz = c["n"]
+    arr = cases.inputs(c)
+    sol = arr["sol"].copy()
+    sol[1:-1, 1:-1, 1:-1] = g["phi"].reshape(nz, ny, nx)
+    arr["sol"] = sol
+    shapes = [(nz, ny, nx + 1), (nz, ny + 1, nx), (nz + 1, ny, nx)]
+    for mode, keys in (("flux", ("fx", "fy", "fz")), ("grad", ("gx", "gy", "gz"))):
+        out = oracle.fluxes(c, arr, mode)
+        for d, k in enumerate(keys):
+            ref = g[k].reshape(shapes[d])
+            assert np.array_equal(out[d], ref), (mode, d, np.abs(out[d] - ref).max())
