@@ -374,7 +374,10 @@ class MLMG:
         return list(a[:n])
 
     def getNumCGIters(self):
-        n = self.getNumIters()
+        """BiCGStab iterations of every bottom solve (F-cycles make several
+        per MLMG iteration), as MLMG::getNumCGIters."""
+        one = (ctypes.c_int * 1)()
+        n = capi.lib().mlmg_get_num_cg_iters(self._h, one, 0)
         a = (ctypes.c_int * max(n, 1))()
         capi.lib().mlmg_get_num_cg_iters(self._h, a, n)
         return list(a[:n])

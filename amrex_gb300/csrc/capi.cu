@@ -959,8 +959,8 @@ int mlmg_get_smoother_stats (mlmg_solver s, double* total_ms, long long* launche
 int mlmg_set_max_fmg_iter (mlmg_solver s, int n)
 {
     API_BEGIN
-    MLMG_REQUIRE(s != nullptr, ERR_ARGS, "null handle");
-    MLMG_REQUIRE(n == 0, ERR_UNSUPPORTED, "F-cycles (max_fmg_iter > 0) are not implemented");
+    MLMG_REQUIRE(s != nullptr && n >= 0, ERR_ARGS, "bad arguments");
+    s->opt.max_fmg_iter = n;
     API_END
 }
 

@@ -121,6 +121,7 @@ std::vector<LevelGrids> define_grids (const GeomC& geom, const std::vector<Box3>
                 if (!all_coarsenable(out.back().boxes, cr, 1)) { break; }
                 const int chunk[3] = {info.agg_grid_size, info.agg_grid_size, info.agg_grid_size};
                 L.boxes = max_size({boundboxes[lev]}, chunk);
+                L.derived = 0;
                 agged = true;
             }
             L.geom = make_geom(domainboxes[lev]);
@@ -173,11 +174,18 @@ PatchLevel build_patch_level (const std::vector<const SolveSpec*>& solves, int l
     PL.lev = lev;
     PL.solve_first_patch.assign(solves.size(), -1);
     PL.solve_npatch.assign(solves.size(), 0);
+    PL.solve_rbox_first.assign(solves.size(), 0);
+    PL.solve_rbox_n.assign(solves.size(), 0);
+    PL.solve_derived.assign(solves.size(), 0);
     long long cursor = 0;
     for (size_t s = 0; s < solves.size(); ++s) {
         const SolveSpec& S = *solves[s];
         if (lev >= (int)S.levels.size()) { continue; }
         const LevelGrids& LG = S.levels[lev];
+        PL.solve_rbox_first[s] = (int)PL.rboxes.size();
+        PL.solve_rbox_n[s] = (int)LG.boxes.size();
+        PL.solve_derived[s] = LG.derived;
+        PL.rboxes.insert(PL.rboxes.end(), LG.boxes.begin(), LG.boxes.end());
         const bool is_bottom = (lev == (int)S.levels.size() - 1);
         double dx[3], dxinv[3];
         LG.geom.cell_size(dx, dxinv);

@@ -31,6 +31,10 @@ struct GeomC {
 struct LevelGrids {
     GeomC geom;
     std::vector<Box3> boxes;
+    // grids made by coarsening the level-0 BoxArray (BoxArray::coarsen shares
+    // the data, so amrex::isMFIterSafe holds between two such levels);
+    // agglomerated levels are new BoxArrays
+    int derived = 1;
 };
 
 // MLLinOpT::defineGrids for AMR level 0 (Src/LinearSolvers/MLMG/AMReX_MLLinOp.H:793-1165)
@@ -66,6 +70,9 @@ struct PatchLevel {
     long long nelem = 0;                   // elements per field
     std::vector<int> solve_first_patch;    // first patch index of each solve at this level (-1 if absent)
     std::vector<int> solve_npatch;
+    std::vector<Box3> rboxes;              // the solves' own (unmerged) boxes of this level, solve by solve
+    std::vector<int> solve_rbox_first, solve_rbox_n;
+    std::vector<int> solve_derived;        // LevelGrids::derived of each solve (0 if absent)
 };
 
 struct BoxToPatch {                        // level-0 user box -> patch location

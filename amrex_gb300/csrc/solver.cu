@@ -6,6 +6,7 @@
 #include "coarse_vcycle.cuh"
 #include "adjoint_kernels.cuh"
 #include "flux_kernels.cuh"
+#include "fmg_kernels.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -83,6 +84,12 @@ struct LevelData {
     SubsetData fz;
     DevBuf<float> cor32b;
     DevBuf<int> tfirst_d, tn_d;    // per-solve tag ranges (coarse-level kernel)
+    // F-cycles: the solves' own boxes of this level, interpolation data for
+    // this level as the fine one, and the saved corrections (on demand)
+    DevBuf<Box3> rbox;
+    DevBuf<FmgSolveInfo> fmg;
+    DevBuf<double> cor_hold;
+    DevBuf<float> cor_hold32;
     // bottom work arrays
     DevBuf<double> bw[7];
     bool has_bottom = false;
@@ -117,6 +124,7 @@ struct Engine::Impl {
     std::vector<cudaEvent_t> kev;
     int kev_used = 0;
     bool capturing = false;
+    int bslot = 0;               // bottom solves issued in the current iteration
 
     explicit Impl (Engine& e) : E(e) {}
     ~Impl () {
@@ -165,7 +173,10 @@ struct Engine::Impl {
     // ------------------------------------------------------- operations --
     template <typename T> void ghost (int l, T* phi, bool inhomog, bool do_copy);
     template <typename T> void smooth (int l, T* cor, const T* res, bool skip_fb);
-    template <typename T> void vcycle ();
+    template <typename T> void vcycle (int top);
+    template <typename T> void fcycle ();
+    template <typename T> void correction_residual (int l);
+    void bottom_done ();
     template <typename T> T* field_cor (int l);
     template <typename T> T* field_res (int l);
     template <typename T> T* field_rescor (int l);
@@ -177,7 +188,7 @@ struct Engine::Impl {
     void smooth_fused (int l, int n);
     void resid32 (int l, float* rescor, float* cor, const float* res);
     void residual0 (bool to32);   // res[0] (FP64, or FP32 in mixed) and per-block max|r|
-    void one_iteration ();
+    void one_iteration (bool fmg);
 };
 
 // -------------------------------------------------------------- fields ----
@@ -311,7 +322,7 @@ void Engine::Impl::build ()
     partial.alloc(max_tiles + 1);
     red_out.alloc((size_t)nsolve * 4 + 4);
     h_red.alloc((size_t)nsolve * 4 + 4);
-    h_iters.alloc((size_t)nsolve * 2 + 2);
+    h_iters.alloc((size_t)nsolve * (nlev_max + 2) + 2);
     bot_iters.alloc(nsolve);
     bot_ret.alloc(nsolve);
     active_d.alloc(nsolve);
@@ -337,6 +348,26 @@ void Engine::Impl::build ()
     }
     volinv0_d.upload(volinv0, st());
     build_bottom_tables();
+    // F-cycle interpolation tables: level l as the fine level of level l+1
+    for (int l = 0; l < nlev_max; ++l) {
+        LevelData& L = lev[l];
+        if (!L.meta.rboxes.empty()) { L.rbox.upload(L.meta.rboxes, st()); }
+        if (l + 1 >= nlev_max) { continue; }
+        std::vector<FmgSolveInfo> info(nsolve);
+        for (int s = 0; s < nsolve; ++s) {
+            const SolveSpec& S = E.m_problems[s].spec;
+            FmgSolveInfo I{};
+            if (l + 1 < (int)S.levels.size()) {
+                I.cdom = S.levels[l + 1].geom.domain;
+                for (int d = 0; d < 3; ++d) { I.per[d] = S.geom.periodic[d]; }
+                I.safe = (S.levels[l].derived && S.levels[l + 1].derived) ? 1 : 0;
+                I.rbox0 = L.meta.solve_rbox_first[s];
+                I.nrbox = L.meta.solve_rbox_n[s];
+            }
+            info[s] = I;
+        }
+        L.fmg.upload(info, st());
+    }
     // algorithmic bytes of one finest-level smoother launch (one colour pass
     // reads phi, rhs and, for ABec, a, bX, bY, bZ over the whole level and
     // writes phi: 7 words per cell; Poisson: 3)
@@ -648,16 +679,51 @@ void Engine::Impl::smooth (int l, T* cor, const T* res, bool skip_fb)
     }
 }
 
-// MLMGT::mgVcycle (AMReX_MLMG.H:1306-1415), one stage per launch for every
-// patch of every solve at that level.
+// rescor = res - L(cor), homogeneous BCs (MLMGT::computeResOfCorrection,
+// AMReX_MLMG.H:1796-1803)
 template <typename T>
-void Engine::Impl::vcycle ()
+void Engine::Impl::correction_residual (int l)
+{
+    LevelData& L = lev[l];
+    T* cor = field_cor<T>(l);
+    T* res = field_res<T>(l);
+    T* rescor = field_rescor<T>(l);
+    if constexpr (std::is_same_v<T, float>) {
+        resid32(l, rescor, cor, res);
+    } else {
+        ghost<T>(l, cor, false, true);
+        if (abec) {
+            k_residual<T, T, true><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
+                coef<T>(l, 0), coef<T>(l, 1), coef<T>(l, 2), coef<T>(l, 3), nullptr);
+        } else {
+            k_residual<T, T, false><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
+                nullptr, nullptr, nullptr, nullptr, nullptr);
+        }
+        launched();
+    }
+}
+
+// the bottom solve's BiCGStab iteration counts of this iteration's bottom
+// solve number bslot, to the host (MLMGT::m_niters_cg keeps one per solve)
+void Engine::Impl::bottom_done ()
+{
+    if (bslot < nlev_max + 2) {
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(h_iters.p + (size_t)bslot * nsolve, bot_iters.p, sizeof(int) * nsolve,
+                                        cudaMemcpyDeviceToHost, st()));
+    }
+    ++bslot;
+}
+
+// MLMGT::mgVcycle (AMReX_MLMG.H:1306-1415) from MG level `top`, one stage per
+// launch for every patch of every solve at that level.
+template <typename T>
+void Engine::Impl::vcycle (int top)
 {
     const EngineOptions& o = E.m_opt;
     // levels >= top_end run in the coarse-level kernel (mixed path)
-    const bool coarse = std::is_same_v<T, float> && lc >= 0;
+    const bool coarse = std::is_same_v<T, float> && lc >= 0 && top <= lc;
     const int top_end = coarse ? lc : nlev_max - 1;
-    for (int l = 0; l < top_end; ++l) {
+    for (int l = top; l < top_end; ++l) {
         LevelData& L = lev[l];
         if (L.mg.n == 0) { continue; }
         T* cor = field_cor<T>(l);
@@ -669,7 +735,6 @@ void Engine::Impl::vcycle ()
         } else {
             for (int i = 0; i < o.nu1; ++i) { smooth<T>(l, cor, res, i == 0); }
         }
-        // rescor = res - L(cor), homogeneous BC (computeResOfCorrection)
         if constexpr (std::is_same_v<T, float>) {
             if (L.inline_bc && E.m_opt.fuse_resid_restrict) {
                 // fused with the restriction below: the fine residual is never stored
@@ -679,24 +744,14 @@ void Engine::Impl::vcycle ()
                     k_resid_restrict<true><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), cor, res, S,
                                                                                  field_res<T>(l + 1));
                 } else {
-                    k_resid_restrict<false><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), cor, res, S,
-                                                                                  field_res<T>(l + 1));
+                    k_resid_restrict<false><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), cor, res,
+                                                                                  S, field_res<T>(l + 1));
                 }
                 launched();
                 continue;
             }
-            resid32(l, rescor, cor, res);
-        } else {
-            ghost<T>(l, cor, false, true);
-            if (abec) {
-                k_residual<T, T, true><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
-                    coef<T>(l, 0), coef<T>(l, 1), coef<T>(l, 2), coef<T>(l, 3), nullptr);
-            } else {
-                k_residual<T, T, false><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
-                    nullptr, nullptr, nullptr, nullptr, nullptr);
-            }
-            launched();
         }
+        correction_residual<T>(l);
         LevelData& C = lev[l + 1];
         k_restrict<T><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), rescor, field_res<T>(l + 1));
         launched();
@@ -718,7 +773,8 @@ void Engine::Impl::vcycle ()
                                                                bot_iters.p, bot_ret.p);
     }
     launched();
-    for (int l = top_end - 1; l >= 0; --l) {
+    bottom_done();
+    for (int l = top_end - 1; l >= top; --l) {
         LevelData& L = lev[l];
         if (L.mg.n == 0) { continue; }
         T* cor = field_cor<T>(l);
@@ -729,6 +785,65 @@ void Engine::Impl::vcycle ()
         } else {
             for (int i = 0; i < o.nu2; ++i) { smooth<T>(l, cor, field_res<T>(l), false); }
         }
+    }
+}
+
+// MLMGT::mgFcycle (AMReX_MLMG.H:1420-1457): restrict the residual to every
+// level, solve the bottom, then on each level from the coarsest up: assign the
+// trilinear prolongation of the coarser correction, take its residual as the
+// level's right-hand side, run a V-cycle from that level and add the
+// prolongation back.  All solves of the batch have the same number of levels.
+template <typename T>
+void Engine::Impl::fcycle ()
+{
+    const int nb = nlev_max - 1;
+    for (int l = 1; l <= nb; ++l) {
+        LevelData& C = lev[l];
+        // avgDownResMG (AMReX_MLLinOp.H:1563-1584)
+        k_restrict<T><<<C.all.ntiles, kTileBlock, 0, st()>>>(lev[l - 1].dl, C.dl, C.all.dev(), field_res<T>(l - 1),
+                                                             field_res<T>(l));
+        launched();
+    }
+    {
+        const EngineOptions& o = E.m_opt;
+        BottomParams prm{o.bottom_maxiter, o.bottom_reltol, o.bottom_abstol, o.nub, o.nuf, o.bottom_solver == 1 ? 1 : 0};
+        if (abec) {
+            k_bottom<T, true><<<njobs, bot_threads, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
+                                                                  bot_iters.p, bot_ret.p);
+        } else {
+            k_bottom<T, false><<<njobs, bot_threads, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
+                                                                   bot_iters.p, bot_ret.p);
+        }
+        launched();
+        bottom_done();
+    }
+    for (int l = nb - 1; l >= 0; --l) {
+        LevelData& L = lev[l];
+        T* cor = field_cor<T>(l);
+        const size_t bytes = (size_t)L.meta.nelem * sizeof(T);
+        if constexpr (std::is_same_v<T, float>) {
+            // inline-BC levels keep no ghost values: give the coarse
+            // correction the ghosts applyBC would have left
+            if (lev[l + 1].inline_bc) { ghost<float>(l + 1, field_cor<float>(l + 1), false, true); }
+        }
+        k_interp_assign<T><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), lev[l + 1].dl, L.fmg.p, L.rbox.p,
+                                                                 field_cor<T>(l + 1), cor);
+        launched();
+        correction_residual<T>(l);
+        k_copy_valid<T><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), field_res<T>(l), field_rescor<T>(l));
+        launched();
+        T* hold;
+        if constexpr (std::is_same_v<T, float>) {
+            if (L.cor_hold32.n != (size_t)L.meta.nelem) { L.cor_hold32.alloc((size_t)L.meta.nelem); }
+            hold = L.cor_hold32.p;
+        } else {
+            if (L.cor_hold.n != (size_t)L.meta.nelem) { L.cor_hold.alloc((size_t)L.meta.nelem); }
+            hold = L.cor_hold.p;
+        }
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(hold, cor, bytes, cudaMemcpyDeviceToDevice, st()));
+        vcycle<T>(l);
+        k_add_to<T, T><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, hold, nullptr);
+        launched();
     }
 }
 
@@ -813,10 +928,11 @@ void Engine::Impl::residual0 (bool to32)
 
 // MLMGT::oneIter (AMReX_MLMG.H:1227-1293), single AMR level, followed by the
 // convergence residual of MLMGT::solve (:436-441)
-void Engine::Impl::one_iteration ()
+void Engine::Impl::one_iteration (bool fmg)
 {
     LevelData& L0 = lev[0];
     kev_used = 0;
+    bslot = 0;
     bool any_singular = false;
     for (int s : singular) { if (s) { any_singular = true; } }
     if (mixed()) {
@@ -829,7 +945,7 @@ void Engine::Impl::one_iteration ()
                                                                          red_out.p + nsolve, volinv0_d.p);
             launched(3);
         }
-        vcycle<float>();
+        if (fmg) { fcycle<float>(); } else { vcycle<float>(0); }
         k_add_to<double, float><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.sol.p, L0.cor32.p,
                                                                         active_d.p);
         launched();
@@ -843,14 +959,13 @@ void Engine::Impl::one_iteration ()
                                                                           red_out.p + nsolve, volinv0_d.p);
             launched(3);
         }
-        vcycle<double>();
+        if (fmg) { fcycle<double>(); } else { vcycle<double>(0); }
         k_add_to<double, double><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.sol.p, L0.cor.p,
                                                                          active_d.p);
         launched();
         residual0(false);
     }
     MLMG_CUDA_CHECK(cudaMemcpyAsync(h_red.p, red_out.p, sizeof(double) * nsolve, cudaMemcpyDeviceToHost, st()));
-    MLMG_CUDA_CHECK(cudaMemcpyAsync(h_iters.p, bot_iters.p, sizeof(int) * nsolve, cudaMemcpyDeviceToHost, st()));
 }
 
 // ---------------------------------------------------------------- Engine ---
@@ -1107,15 +1222,26 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
     bool any_active = false;
     for (int a : active) { if (a) { any_active = true; } }
     int& per_iter_launches = I.graph_launches;
+    if (m_opt.max_fmg_iter > 0) {
+        for (int s = 0; s < ns; ++s) {
+            MLMG_REQUIRE((int)m_problems[s].spec.levels.size() == I.nlev_max, ERR_UNSUPPORTED,
+                         "F-cycles need every solve of a batch to have the same number of MG levels");
+        }
+    }
+    int graph_bslots = 1;
     for (int iter = 0; iter < niters && any_active; ++iter) {
-        if (m_opt.use_graph) {
+        if (iter < m_opt.max_fmg_iter) {
+            // F-cycles run eagerly: they differ from the replayed V-cycle iteration
+            I.one_iteration(true);
+        } else if (m_opt.use_graph) {
             if (I.graph_exec == nullptr) {
                 const int before = m_launches;
                 cudaGraph_t g;
                 MLMG_CUDA_CHECK(cudaStreamBeginCapture(m_stream, cudaStreamCaptureModeThreadLocal));
                 I.capturing = true;
-                I.one_iteration();
+                I.one_iteration(false);
                 I.capturing = false;
+                graph_bslots = I.bslot;
                 MLMG_CUDA_CHECK(cudaStreamEndCapture(m_stream, &g));
                 MLMG_CUDA_CHECK(cudaGraphInstantiate(&I.graph_exec, g, 0));
                 MLMG_CUDA_CHECK(cudaGraphDestroy(g));
@@ -1124,8 +1250,9 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
             }
             MLMG_CUDA_CHECK(cudaGraphLaunch(I.graph_exec, m_stream));
             m_launches += per_iter_launches;
+            I.bslot = graph_bslots;
         } else {
-            I.one_iteration();
+            I.one_iteration(false);
         }
         MLMG_CUDA_CHECK(cudaGetLastError());
         MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
@@ -1136,7 +1263,9 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
             SolveReport& R = m_reports[s];
             const double fine = I.h_red.p[s];
             R.history.push_back(fine);
-            R.cg_iters.push_back(I.h_iters.p[s]);
+            for (int q = 0; q < I.bslot && q < I.nlev_max + 2; ++q) {
+                R.cg_iters.push_back(I.h_iters.p[(size_t)q * ns + s]);
+            }
             R.niters++;
             R.final_resid = fine;
             if (m_opt.verbose >= 2) {

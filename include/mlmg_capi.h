@@ -147,7 +147,7 @@ int mlmg_new(mlmg_linop op, mlmg_solver* out);
 int mlmg_delete(mlmg_solver s);
 int mlmg_set_verbose(mlmg_solver s, int v);
 int mlmg_set_max_iter(mlmg_solver s, int n);
-int mlmg_set_max_fmg_iter(mlmg_solver s, int n);        /* only 0 (V-cycles) is implemented */
+int mlmg_set_max_fmg_iter(mlmg_solver s, int n);        /* F-cycles for the first n iterations */
 int mlmg_set_fixed_iter(mlmg_solver s, int n);
 int mlmg_set_pre_smooth(mlmg_solver s, int n);
 int mlmg_set_post_smooth(mlmg_solver s, int n);

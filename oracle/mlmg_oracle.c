@@ -159,6 +159,8 @@ typedef struct {
     double* bcl_p;      /* per box, per face: BC location */
     Fab* mask;          /* [nbox*6]: over the face-adjacent outside cells */
     Fab* fco;           /* [nbox*6]: f coefficient over the face-adjacent inside cells */
+    int derived;        /* grids made by coarsening the level-0 BoxArray (they share its data,
+                           so MFIter over two such levels is safe: amrex::isMFIterSafe) */
     MF acoef, bcoef[3];
 } Level;
 
@@ -198,6 +200,7 @@ static int define_grids(Hier* H, const Box* ba, int nba, const OracleOptions* o)
     Level* L0 = &H->lev[nlev++];
     L0->nbox = nba; L0->boxes = (Box*)malloc(sizeof(Box) * nba);
     memcpy(L0->boxes, ba, sizeof(Box) * nba);
+    L0->derived = 1;
     level_geom(L0, &dom, H);
 
     Box aggbox; int aggable = 0;
@@ -237,12 +240,14 @@ static int define_grids(Hier* H, const Box* ba, int nba, const OracleOptions* o)
             if (!agged && !agg_flag[lev] && all_coarsenable(ba, nba, accum[lev], mg_box_min_width)) {
                 L->nbox = nba; L->boxes = (Box*)malloc(sizeof(Box) * nba);
                 for (int b = 0; b < nba; ++b) L->boxes[b] = bcoarsen(ba[b], accum[lev]);
+                L->derived = 1;
             } else {
                 int cr = blen(&domainboxes[lev - 1], 0) / blen(&domainboxes[lev], 0);
                 if (!all_coarsenable(Lp->boxes, Lp->nbox, cr, 1)) break;
                 Box* nb = NULL;
                 L->nbox = max_size(&boundboxes[lev], 1, o->agg_grid_size, &nb);
                 L->boxes = nb;
+                L->derived = 0;
                 agged = 1;
             }
             level_geom(L, &domainboxes[lev], H);
@@ -258,6 +263,7 @@ static int define_grids(Hier* H, const Box* ba, int nba, const OracleOptions* o)
             Box cd = bcoarsen(dom, rr);
             L->nbox = nba; L->boxes = (Box*)malloc(sizeof(Box) * nba);
             for (int b = 0; b < nba; ++b) L->boxes[b] = bcoarsen(ba[b], rr);
+            L->derived = 1;
             level_geom(L, &cd, H);
             nlev++;
         }
@@ -745,8 +751,10 @@ static void restrict_coeffs(const Hier* H, Level* Lf, Level* Lc) {
 typedef struct {
     Hier H;
     OracleOptions o;
-    MF cor[32], res[32], rescor[32];
+    MF cor[32], res[32], rescor[32], cor_hold[32];
     MF sol, rhs;
+    int cg_log[ORACLE_MAX_HIST];   /* BiCGStab iterations of every bottom solve (MLMGT::m_niters_cg) */
+    int ncg;
     GrownGlobal bcval;
     int bottom_cg_iters_total;
     int singular;
@@ -851,7 +859,7 @@ done:
 }
 
 /* MLMGT::actualBottomSolve, AMReX_MLMG.H:1500-1610 */
-static void bottom_solve(Solver* S, int* cg_iters) {
+static void bottom_solve(Solver* S) {
     int lev = S->H.nlev - 1;
     Level* L = &S->H.lev[lev];
     MF* x = &S->cor[lev];
@@ -860,7 +868,8 @@ static void bottom_solve(Solver* S, int* cg_iters) {
     if (S->o.bottom_solver == 1) { /* smoother */
         int skip = 1;
         for (int i = 0; i < S->o.nuf; ++i) { smooth(S, lev, x, b, skip); skip = 0; }
-        *cg_iters = 0;
+        if (S->ncg < ORACLE_MAX_HIST) S->cg_log[S->ncg] = 0;
+        S->ncg++;
         return;
     }
     MF bb; int own = 0;
@@ -873,27 +882,108 @@ static void bottom_solve(Solver* S, int* cg_iters) {
     }
     int it = 0;
     int ret = bicgstab(S, lev, x, bottom_b, S->o.bottom_reltol, -1.0, S->o.bottom_maxiter, &it);
-    *cg_iters = it;
+    if (S->ncg < ORACLE_MAX_HIST) S->cg_log[S->ncg] = it;
+    S->ncg++;
     if (ret != 0 && ret != 9) mf_setval(x, 0.0);
     int n = (ret == 0) ? S->o.nub : S->o.nuf;
     for (int i = 0; i < n; ++i) smooth(S, lev, x, b, 0);
     if (own) mf_free(&bb);
 }
 
-/* MLMGT::mgVcycle, AMReX_MLMG.H:1306-1415 */
-static void vcycle(Solver* S, int* cg_iters) {
+/* MLMGT::mgVcycle, AMReX_MLMG.H:1306-1415, from MG level `top` down */
+static void vcycle(Solver* S, int top) {
     int bottom = S->H.nlev - 1;
-    for (int lev = 0; lev < bottom; ++lev) {
+    for (int lev = top; lev < bottom; ++lev) {
         mf_setval(&S->cor[lev], 0.0);
         int skip = 1;
         for (int i = 0; i < S->o.nu1; ++i) { smooth(S, lev, &S->cor[lev], &S->res[lev], skip); skip = 0; }
         correction_residual(S, lev, &S->rescor[lev], &S->cor[lev], &S->res[lev]);
         restriction(&S->H, &S->H.lev[lev], &S->rescor[lev], &S->H.lev[lev + 1], &S->res[lev + 1]);
     }
-    bottom_solve(S, cg_iters);
-    for (int lev = bottom - 1; lev >= 0; --lev) {
+    bottom_solve(S);
+    for (int lev = bottom - 1; lev >= top; --lev) {
         interp_add(&S->H, &S->H.lev[lev + 1], &S->cor[lev + 1], &S->H.lev[lev], &S->cor[lev]);
         for (int i = 0; i < S->o.nu2; ++i) smooth(S, lev, &S->cor[lev], &S->res[lev], 0);
+    }
+}
+
+/* MLCellLinOpT::interpAssign, AMReX_MLCellLinOp.H:1003-1100, with
+ * mlmg_lin_cc_interp_r2 (AMReX_MLMG_3D_K.H:7-37): cor[lev] = trilinear
+ * prolongation of cor[lev+1] on every fine box.  When MFIter over both
+ * levels is safe the coarse ghosts are refreshed by FillBoundary and the
+ * ghosts outside the domain keep what the last applyBC (or setVal) left in
+ * them; otherwise the coarse data is copied into zeroed FABs over the
+ * coarsened fine boxes (ParallelCopy). */
+static void interp_assign(Solver* S, int lev) {
+    Hier* H = &S->H;
+    const Level* Lf = &H->lev[lev];
+    const Level* Lc = &H->lev[lev + 1];
+    MF* crse = &S->cor[lev + 1];
+    MF* fine = &S->cor[lev];
+    MF tmp;
+    const MF* cm = crse;
+    int own = 0;
+    /* isMFIterSafe(crse, fine): both levels' BoxArrays come from the level-0
+     * BoxArray by BoxArray::coarsen (lazy, shared data), MLLinOpT::defineGrids
+     * (AMReX_MLLinOp.H:995-1000, 1076-1077); agglomerated levels are new
+     * BoxArrays (:1006) */
+    if (Lf->derived && Lc->derived) {
+        fill_boundary(Lc, H->periodic, crse, 0);
+    } else {
+        Box* cb = (Box*)malloc(sizeof(Box) * (size_t)Lf->nbox);
+        for (int b = 0; b < Lf->nbox; ++b) cb[b] = bcoarsen(Lf->boxes[b], 2);
+        mf_define(&tmp, Lf->nbox, cb, 1, -1);
+        mf_setval(&tmp, 0.0);
+        for (int b = 0; b < Lf->nbox; ++b) {
+            Fab* t = &tmp.fab[b];
+            for (int k = cb[b].lo[2] - 1; k <= cb[b].hi[2] + 1; ++k)
+            for (int j = cb[b].lo[1] - 1; j <= cb[b].hi[1] + 1; ++j)
+            for (int i = cb[b].lo[0] - 1; i <= cb[b].hi[0] + 1; ++i) {
+                int wi, wj, wk;
+                int src = locate(Lc, H->periodic, i, j, k, &wi, &wj, &wk);
+                if (src >= 0) A(t, i, j, k) = A(&crse->fab[src], wi, wj, wk);
+            }
+        }
+        free(cb);
+        cm = &tmp; own = 1;
+    }
+    for (int b = 0; b < fine->nbox; ++b) {
+        Fab* ff = &fine->fab[b];
+        const Fab* cc = &cm->fab[b];
+        FOR_VALID(ff, i, j, k) {
+            const int kc = k / 2, koff = 2 * (k - kc * 2) - 1;
+            const int jc = j / 2, joff = 2 * (j - jc * 2) - 1;
+            const int ic = i / 2, ioff = 2 * (i - ic * 2) - 1;
+            A(ff, i, j, k) = 0.421875 * A(cc, ic, jc, kc)
+                + 0.140625 * A(cc, ic + ioff, jc, kc)
+                + 0.140625 * A(cc, ic, jc + joff, kc)
+                + 0.140625 * A(cc, ic, jc, kc + koff)
+                + 0.046875 * A(cc, ic, jc + joff, kc + koff)
+                + 0.046875 * A(cc, ic + ioff, jc, kc + koff)
+                + 0.046875 * A(cc, ic + ioff, jc + joff, kc)
+                + 0.015625 * A(cc, ic + ioff, jc + joff, kc + koff);
+        }
+    }
+    if (own) mf_free(&tmp);
+}
+
+/* MLMGT::mgFcycle, AMReX_MLMG.H:1420-1457 */
+static void fcycle(Solver* S) {
+    Hier* H = &S->H;
+    int bottom = H->nlev - 1;
+    for (int lev = 1; lev <= bottom; ++lev) {
+        /* avgDownResMG, AMReX_MLLinOp.H:1563-1584 */
+        restriction(H, &H->lev[lev - 1], &S->res[lev - 1], &H->lev[lev], &S->res[lev]);
+    }
+    bottom_solve(S);
+    for (int lev = bottom - 1; lev >= 0; --lev) {
+        Level* L = &H->lev[lev];
+        interp_assign(S, lev);
+        correction_residual(S, lev, &S->rescor[lev], &S->cor[lev], &S->res[lev]);
+        mf_axpy(L, &S->res[lev], 0, &S->rescor[lev], 0);
+        MF t = S->cor[lev]; S->cor[lev] = S->cor_hold[lev]; S->cor_hold[lev] = t;
+        vcycle(S, lev);
+        mf_axpy(L, &S->cor[lev], 1.0, &S->cor_hold[lev], 1);
     }
 }
 
@@ -964,6 +1054,7 @@ static void free_solver(Solver* S) {
         if (S->cor[l].fab) mf_free(&S->cor[l]);
         if (S->res[l].fab) mf_free(&S->res[l]);
         if (S->rescor[l].fab) mf_free(&S->rescor[l]);
+        if (S->cor_hold[l].fab) mf_free(&S->cor_hold[l]);
     }
     if (S->sol.fab) mf_free(&S->sol);
     if (S->rhs.fab) mf_free(&S->rhs);
@@ -1134,6 +1225,7 @@ void oracle_default_options(OracleOptions* o) {
     o->maxorder = 3; o->nu1 = 2; o->nu2 = 2; o->nuf = 8; o->nub = 0;
     o->max_iter = 200; o->fixed_iter = 0; o->bottom_solver = 2; o->bottom_maxiter = 200;
     o->bottom_reltol = 1.e-4; o->tol_rel = 1.e-10; o->tol_abs = 0.0;
+    o->max_fmg_iter = 0;
 }
 
 /* MLMGT::solve, AMReX_MLMG.H:353-541, single AMR level */
@@ -1159,6 +1251,8 @@ int oracle_solve(const OracleProblem* P, const OracleOptions* o, double* phi_out
         mf_define(&S->cor[l], L->nbox, L->boxes, 1, -1);
         mf_define(&S->res[l], L->nbox, L->boxes, 0, -1);
         mf_define(&S->rescor[l], L->nbox, L->boxes, 0, -1);
+        mf_define(&S->cor_hold[l], L->nbox, L->boxes, 1, -1);
+        mf_setval(&S->cor_hold[l], 0.0);
     }
     if (S->singular) make_solvable(S, 0, &S->rhs);
     solution_residual(S, &S->res[0], &S->sol, &S->rhs);
@@ -1176,12 +1270,11 @@ int oracle_solve(const OracleProblem* P, const OracleOptions* o, double* phi_out
         int niters = o->fixed_iter ? o->fixed_iter : o->max_iter;
         for (int iter = 0; iter < niters; ++iter) {
             if (S->singular) make_solvable(S, 0, &S->res[0]);
-            int cg = 0;
-            vcycle(S, &cg);
+            if (iter < o->max_fmg_iter) { fcycle(S); } else { vcycle(S, 0); }
             mf_axpy(L0, &S->sol, 1.0, &S->cor[0], 1);
             solution_residual(S, &S->res[0], &S->sol, &S->rhs);
             double fine = mf_norminf(L0, &S->res[0]);
-            if (R->niters < ORACLE_MAX_HIST) { R->history[R->niters] = fine; R->cg_iters[R->niters] = cg; }
+            if (R->niters < ORACLE_MAX_HIST) { R->history[R->niters] = fine; }
             R->niters++;
             composite = fine;
             if (fine <= res_target) { converged = 1; break; }
@@ -1193,6 +1286,8 @@ int oracle_solve(const OracleProblem* P, const OracleOptions* o, double* phi_out
     R->iter_seconds = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
     R->final_resid = composite;
     R->nlev = H->nlev;
+    R->ncg = S->ncg;
+    for (int q = 0; q < S->ncg && q < ORACLE_MAX_HIST; ++q) R->cg_iters[q] = S->cg_log[q];
     copy_mf_to_global(L0, &S->sol, phi_out);
     free_solver(S);
     free(S);

@@ -30,6 +30,7 @@ typedef struct {
     int maxorder, nu1, nu2, nuf, nub;
     int max_iter, fixed_iter, bottom_solver, bottom_maxiter;
     double bottom_reltol, tol_rel, tol_abs;
+    int max_fmg_iter;      /* F-cycles for the first max_fmg_iter iterations */
 } OracleOptions;
 
 typedef struct {
@@ -37,7 +38,8 @@ typedef struct {
     double init_resid, rhs_norm, final_resid;
     double iter_seconds;   /* wall time of the iteration loop (setup excluded) */
     double history[ORACLE_MAX_HIST];
-    int cg_iters[ORACLE_MAX_HIST];
+    int cg_iters[ORACLE_MAX_HIST];   /* one entry per bottom solve (F-cycles make several per iteration) */
+    int ncg;
 } OracleResult;
 
 void oracle_default_options(OracleOptions* o);

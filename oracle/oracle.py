@@ -46,14 +46,16 @@ class Options(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int) for k in ("agg", "con", "agg_grid_size", "con_grid_size",
                                             "max_coarsening_level", "maxorder", "nu1", "nu2", "nuf", "nub",
                                             "max_iter", "fixed_iter", "bottom_solver", "bottom_maxiter")] + \
-               [(k, ctypes.c_double) for k in ("bottom_reltol", "tol_rel", "tol_abs")]
+               [(k, ctypes.c_double) for k in ("bottom_reltol", "tol_rel", "tol_abs")] + \
+               [("max_fmg_iter", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("niters", ctypes.c_int), ("nlev", ctypes.c_int),
                 ("init_resid", ctypes.c_double), ("rhs_norm", ctypes.c_double), ("final_resid", ctypes.c_double),
                 ("iter_seconds", ctypes.c_double),
-                ("history", ctypes.c_double * MAX_HIST), ("cg_iters", ctypes.c_int * MAX_HIST)]
+                ("history", ctypes.c_double * MAX_HIST), ("cg_iters", ctypes.c_int * MAX_HIST),
+                ("ncg", ctypes.c_int)]
 
 
 _lib = None
@@ -114,7 +116,7 @@ def make_options(case):
     o = Options()
     lib().oracle_default_options(ctypes.byref(o))
     for k in ("agg", "con", "agg_grid_size", "con_grid_size", "maxorder", "max_iter", "fixed_iter",
-              "max_coarsening_level"):
+              "max_coarsening_level", "max_fmg_iter"):
         if k in case:
             setattr(o, k, int(case[k]))
     for k in ("tol_rel", "tol_abs"):
@@ -184,5 +186,5 @@ def solve(case, arrays):
     info = dict(status=r.status, niters=r.niters, nlev=r.nlev, init_resid=r.init_resid, rhs_norm=r.rhs_norm,
                 final_resid=r.final_resid, iter_seconds=r.iter_seconds,
                 history=list(r.history[:min(r.niters, MAX_HIST)]),
-                cg_iters=list(r.cg_iters[:min(r.niters, MAX_HIST)]))
+                cg_iters=list(r.cg_iters[:min(r.ncg, MAX_HIST)]))
     return phi, info

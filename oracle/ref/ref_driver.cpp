@@ -283,6 +283,7 @@ int main (int argc, char* argv[])
                 MLMG mlmg(*linop);
                 mlmg.setVerbose(c.geti("verbose", 0));
                 mlmg.setMaxIter(c.geti("max_iter", 200));
+                mlmg.setMaxFmgIter(c.geti("max_fmg_iter", 0));
                 if (c.geti("fixed_iter", 0) > 0) { mlmg.setFixedIter(c.geti("fixed_iter", 0)); }
                 mlmg.setBottomSolver(static_cast<MLMG::BottomSolver>(c.geti("bottom_solver", 2)));
                 mlmg.setBottomVerbose(0);

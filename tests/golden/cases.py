@@ -73,6 +73,18 @@ CASES = {
                          maxorder=4),
     "solve_poisson_periodic_x": _c(mode="solve", n=(32, 24, 16), max_grid_size=8, rhs_seed=1009,
                                    periodic=(1, 0, 0), lobc=(200, 101, 102), hibc=(200, 102, 101)),
+    # --- F-cycles (max_fmg_iter > 0): mgFcycle with trilinear interpAssign ---
+    "solve_abec_32_fmg": _c(mode="solve", op="abec", n=(32, 32, 32), max_grid_size=16, rhs_seed=1001,
+                            b_seed=2001, max_fmg_iter=200),
+    "solve_poisson_c0_fmg": _c(mode="solve", n=(64, 64, 64), max_grid_size=32, rhs_seed=1000, max_fmg_iter=2),
+    "solve_abec_mixed_bc_fmg": _c(mode="solve", op="abec", n=(32, 24, 16), max_grid_size=8, rhs_seed=1003,
+                                  b_seed=2003, a_seed=3003, lobc=(101, 102, 101), hibc=(102, 101, 101),
+                                  sol_seed=3004, max_fmg_iter=200),
+    "solve_poisson_periodic_x_fmg": _c(mode="solve", n=(32, 24, 16), max_grid_size=8, rhs_seed=1009,
+                                       periodic=(1, 0, 0), lobc=(200, 101, 102), hibc=(200, 102, 101),
+                                       max_fmg_iter=200),
+    "solve_abec_agg8_fmg": _c(mode="solve", op="abec", n=(32, 32, 32), max_grid_size=8, rhs_seed=1005,
+                              b_seed=2005, agg_grid_size=8, con_grid_size=8, max_fmg_iter=200),
     # --- MLMG::getFluxes / getGradSolution after a solve ----------------------
     "flux_abec_32": _c(mode="flux", op="abec", n=(32, 32, 32), max_grid_size=16, rhs_seed=1011, b_seed=2011,
                        beta=2.0),
@@ -195,7 +207,7 @@ def case_text(case, files):
     lines = []
     for k in ("op", "n", "max_grid_size", "lobc", "hibc", "maxorder", "agg", "agg_grid_size", "con",
               "con_grid_size", "periodic", "alpha", "beta", "tol_rel", "tol_abs", "max_iter", "fixed_iter",
-              "cross"):
+              "cross", "max_fmg_iter"):
         if k in case:
             v = case[k]
             lines.append(k + " " + (" ".join(str(x) for x in v) if isinstance(v, (tuple, list)) else str(v)))

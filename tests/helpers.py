@@ -49,6 +49,8 @@ def make_problem(case, arrays, precision=None, graph=False, fused=False, options
     mlmg.setMaxIter(case.get("max_iter", 200))
     if case.get("fixed_iter", 0):
         mlmg.setFixedIter(case["fixed_iter"])
+    if case.get("max_fmg_iter", 0):
+        mlmg.setMaxFmgIter(case["max_fmg_iter"])
     if precision is not None:
         mlmg.setPrecision(precision)
     mlmg.setGraph(graph)
