@@ -934,6 +934,11 @@ int mlmg_set_option (mlmg_solver s, const char* name, double value)
     }
     else if (n == "merge_boxes") { s->opt.merge_boxes = value != 0.0; }
     else if (n == "fuse_resid_restrict") { s->opt.fuse_resid_restrict = value != 0.0; }
+    else if (n == "march_sweep") { s->opt.march_sweep = value != 0.0; }
+    else if (n == "march_min_tiles") {
+        MLMG_REQUIRE(value >= 0, ERR_ARGS, "march_min_tiles must be >= 0");
+        s->opt.march_min_tiles = (int)value;
+    }
     else { MLMG_REQUIRE(false, ERR_UNSUPPORTED, "unknown option " + n); }
     // layout-changing knobs take effect at the next engine build
     s->eng.reset();

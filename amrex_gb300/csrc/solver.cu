@@ -3,6 +3,7 @@
 #include "bottom.cuh"
 #include "stencil_kernels.cuh"
 #include "fused_sweep.cuh"
+#include "march_sweep.cuh"
 #include "coarse_vcycle.cuh"
 #include "adjoint_kernels.cuh"
 #include "flux_kernels.cuh"
@@ -82,6 +83,8 @@ struct LevelData {
     // fused two-colour sweeps (mixed path): tile map and the second buffer
     bool fused = false;
     SubsetData fz;
+    bool march = false;           // fused sweeps by the z-marching kernel
+    SubsetData mz;
     DevBuf<float> cor32b;
     DevBuf<int> tfirst_d, tn_d;    // per-solve tag ranges (coarse-level kernel)
     // F-cycles: the solves' own boxes of this level, interpolation data for
@@ -300,6 +303,26 @@ void Engine::Impl::build ()
             S.ntiles = S.h_tstart[S.n];
             S.plist.upload(S.h_plist, st());
             S.tstart.upload(S.h_tstart, st());
+            // the z-marching sweep where the level has enough columns to fill the GPU
+            SubsetData& Z = L.mz;
+            Z.h_plist = mg;
+            Z.n = (int)mg.size();
+            Z.h_tstart.assign(Z.n + 1, 0);
+            for (int q = 0; q < Z.n; ++q) { Z.h_tstart[q + 1] = Z.h_tstart[q] + march_tiles_of(M.patches[mg[q]]); }
+            Z.ntiles = Z.h_tstart[Z.n];
+            L.march = E.m_opt.march_sweep && Z.ntiles >= E.m_opt.march_min_tiles;
+            if (L.march) {
+                Z.plist.upload(Z.h_plist, st());
+                Z.tstart.upload(Z.h_tstart, st());
+                static bool attr_set = false;
+                if (!attr_set) {
+                    MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_march<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         march_smem_floats(true) * (int)sizeof(float)));
+                    MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_march<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         march_smem_floats(false) * (int)sizeof(float)));
+                    attr_set = true;
+                }
+            }
         }
         // fields
         const size_t n = (size_t)M.nelem;
@@ -634,7 +657,16 @@ void Engine::Impl::smooth_fused (int l, int n)
     const StencilPtrs S = stencil32(l);
     for (int i = 0; i < n; ++i) {
         if (timed) { kev_record(); }
-        if (abec) {
+        if (L.march) {
+            const dim3 blk(MS_TX / 2, MS_TY);
+            if (abec) {
+                k_sweep_march<true><<<L.mz.ntiles, blk, march_smem_floats(true) * sizeof(float), st()>>>(
+                    L.dl, L.mz.dev(), a, b, L.res32.p, S);
+            } else {
+                k_sweep_march<false><<<L.mz.ntiles, blk, march_smem_floats(false) * sizeof(float), st()>>>(
+                    L.dl, L.mz.dev(), a, b, L.res32.p, S);
+            }
+        } else if (abec) {
             k_sweep_fused<true><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);
         } else {
             k_sweep_fused<false><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);

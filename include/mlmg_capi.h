@@ -166,7 +166,9 @@ int mlmg_set_fused_smoother(mlmg_solver s, int on);      /* fused two-colour Gau
 /* engine tuning knobs by name: "coarse_block" (0/1: run the coarse levels of
  * each V-cycle in one thread block per solve), "coarse_cells" (a level is
  * coarse when every solve has at most this many cells on it),
- * "merge_boxes" (0/1), "fuse_resid_restrict" (0/1); -4 for an unknown name */
+ * "merge_boxes" (0/1), "fuse_resid_restrict" (0/1), "march_sweep" (0/1: fused
+ * sweeps by the z-marching kernel), "march_min_tiles" (levels with fewer
+ * marching tiles use the tiled fused sweep); -4 for an unknown name */
 int mlmg_set_option(mlmg_solver s, const char* name, double value);
 /* time every finest-level smoother launch with CUDA events on the library
  * stream (graph replays included); the stats accumulate until reset */

@@ -80,17 +80,19 @@ MIXED_CASES = ["solve_poisson_32", "solve_abec_32", "solve_abec_48", "solve_abec
 
 
 @pytest.mark.parametrize("name", MIXED_CASES)
-@pytest.mark.parametrize("graph,fused,coarse", [(False, False, 1), (True, False, 1), (True, True, 1),
-                                                (False, False, 0), (True, True, 0)])
-def test_mixed_solve_reaches_target(name, graph, fused, coarse):
+@pytest.mark.parametrize("graph,fused,coarse,march", [(False, False, 1, 0), (True, False, 1, 0), (True, True, 1, 0),
+                                                      (False, False, 0, 0), (True, True, 0, 0), (True, True, 0, 1)])
+def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
     """FP32 V-cycles inside FP64 refinement reach the same 1e-10 relative
     residual (the residual is evaluated in FP64); phi agrees with the
     reference's FP64 answer to the accuracy that residual implies (up to the
     constant null-space component for singular problems)."""
     g = load.load(name)
     c = g["case"]
-    prob = helpers.make_problem(c, cases.inputs(c), precision="mixed", graph=graph, fused=fused,
-                                options={"coarse_block": coarse})
+    opts = {"coarse_block": coarse}
+    if march:
+        opts["march_min_tiles"] = 0          # the z-marching sweep on every fused level
+    prob = helpers.make_problem(c, cases.inputs(c), precision="mixed", graph=graph, fused=fused, options=opts)
     resid = prob["mlmg"].solve(prob["sol"], prob["rhs"], c["tol_rel"], c["tol_abs"])
     r = g["result"]
     target = c["tol_rel"] * max(r["rhs_norm"], r["init_resid"])
@@ -103,14 +105,17 @@ def test_mixed_solve_reaches_target(name, graph, fused, coarse):
     assert np.abs(phi - ref).max() <= 1e-8 * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_mixed_bc", "solve_abec_48"])
-def test_fused_sweep_matches_colour_passes(name):
-    """The fused two-colour sweep performs the same arithmetic as two colour
-    passes with ghost refreshes in between."""
+@pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_mixed_bc", "solve_abec_48",
+                                  "solve_poisson_periodic_x", "solve_abec_mo4"])
+@pytest.mark.parametrize("march", [0, 1])
+def test_fused_sweep_matches_colour_passes(name, march):
+    """The fused two-colour sweep (tiled, or marching along z) performs the
+    same arithmetic as two colour passes with ghost refreshes in between."""
     c = load.load(name)["case"]
     inp = cases.inputs(c)
     p1 = helpers.make_problem(c, inp, precision="mixed", fused=False)
-    p2 = helpers.make_problem(c, inp, precision="mixed", fused=True)
+    p2 = helpers.make_problem(c, inp, precision="mixed", fused=True,
+                              options={"march_sweep": march, "march_min_tiles": 0})
     p1["mlmg"].solve(p1["sol"], p1["rhs"], 1e-10, 0)
     p2["mlmg"].solve(p2["sol"], p2["rhs"], 1e-10, 0)
     assert p1["mlmg"].getNumIters() == p2["mlmg"].getNumIters()
