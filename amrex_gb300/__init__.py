@@ -335,6 +335,13 @@ class MLMG:
         rc = capi.lib().mlmg_solve(self._h, sol._h, rhs._h, float(tol_rel), float(tol_abs), ctypes.byref(r))
         return rc, r.value
 
+    def autotune(self, sol, rhs, vcycles=2):
+        """Time the candidate smoother layouts on this problem and keep the
+        fastest.  Returns (best ms for `vcycles` V-cycles, report text)."""
+        ms = ctypes.c_double()
+        check(capi.lib().mlmg_autotune(self._h, sol._h, rhs._h, int(vcycles), ctypes.byref(ms)))
+        return ms.value, capi.lib().mlmg_autotune_report(self._h).decode()
+
     def getFluxes(self, flux, sol):
         """MLMG::getFluxes of ``sol`` into three face-centred MultiFabs."""
         F = (ctypes.c_void_p * 3)(*[(m._h if m is not None else None) for m in flux])

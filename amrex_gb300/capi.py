@@ -97,6 +97,8 @@ SIGNATURES = {
     "mlmg_get_solve_time_ms": (c_double, [c_void_p]),
     "mlmg_get_num_mg_levels": (c_int, [c_void_p]),
     "mlmg_solve_batched": (c_int, [c_int, P(c_void_p), P(c_void_p), P(c_void_p), c_double, c_double, P(c_int)]),
+    "mlmg_autotune": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(c_double)]),
+    "mlmg_autotune_report": (ctypes.c_char_p, [c_void_p]),
     "mlmg_adjoint_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_double, c_void_p, P(c_void_p),
                                   c_void_p]),
 }

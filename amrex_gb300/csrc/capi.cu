@@ -6,9 +6,11 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <string>
 
 using namespace mlmg;
 
@@ -252,7 +254,11 @@ void fab_global (mlmg_multifab_s& mf, void* host, const int glo[3], const int gn
     DevBuf<Box3> dr; DevBuf<long long> ds;
     dr.upload(regions, st);
     ds.upload(start, st);
-    if (dir == 0) { MLMG_CUDA_CHECK(cudaMemcpyAsync(stage.p, host, ng * sizeof(T), cudaMemcpyHostToDevice, st)); }
+    // the host array enters the stage for an upload, and for a download that
+    // leaves cells of the array uncovered (those keep the host's values)
+    if (dir == 0 || start.back() < ng) {
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(stage.p, host, ng * sizeof(T), cudaMemcpyHostToDevice, st));
+    }
     if (start.back() > 0) {
         k_fab_global<T><<<grid_for(start.back(), 256), 256, 0, st>>>(mf.dinfo.p, dr.p, ds.p, (int)regions.size(),
             start.back(), (T*)mf.data.p, stage.p, glo[0], glo[1], glo[2], gn[0], gn[1], dir);
@@ -294,6 +300,7 @@ struct mlmg_solver_s {
     std::vector<mlmg_linop> batch_ops;
     std::vector<int> batch_struct, batch_coef;
     int batch_prec = -1;
+    std::string tune_report;     // last mlmg_autotune: one line per candidate
     // transposed-operator engine of the adjoint (its own graph and buffers)
     std::unique_ptr<Engine> adj_eng;
     int adj_struct = -1, adj_coef = -1, adj_prec = -1, adj_merge = -1;
@@ -935,6 +942,10 @@ int mlmg_set_option (mlmg_solver s, const char* name, double value)
     else if (n == "merge_boxes") { s->opt.merge_boxes = value != 0.0; }
     else if (n == "fuse_resid_restrict") { s->opt.fuse_resid_restrict = value != 0.0; }
     else if (n == "march_sweep") { s->opt.march_sweep = value != 0.0; }
+    else if (n == "march_tz") {
+        MLMG_REQUIRE(value >= 1 && value <= 4096, ERR_ARGS, "march_tz must be in 1..4096");
+        s->opt.march_tz = (int)value;
+    }
     else if (n == "march_min_tiles") {
         MLMG_REQUIRE(value >= 0, ERR_ARGS, "march_min_tiles must be >= 0");
         s->opt.march_min_tiles = (int)value;
@@ -1089,6 +1100,71 @@ int mlmg_get_grad_solution (mlmg_solver s, mlmg_multifab sol, const mlmg_multifa
     return face_fluxes_impl(s, sol, grad, 0);
     API_END
 }
+
+int mlmg_autotune (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, int vcycles, double* best_ms)
+{
+    API_BEGIN
+    check_solver_mf(s, sol);
+    check_solver_mf(s, rhs);
+    MLMG_REQUIRE(vcycles >= 1, ERR_ARGS, "vcycles must be >= 1");
+    struct Cand { const char* name; int fused, march, tz, coarse, cells; };
+    static const Cand cands[] = {
+        {"colour passes", 0, 0, 16, 0, 512},
+        {"fused sweep, 32x8x8 tiles", 1, 0, 16, 0, 512},
+        {"fused sweep, 64x16 columns, z-slab 8", 1, 1, 8, 0, 512},
+        {"fused sweep, 64x16 columns, z-slab 16", 1, 1, 16, 0, 512},
+        {"fused sweep, 64x16 columns, z-slab 32", 1, 1, 32, 0, 512},
+        {"fused sweep, 32x8x8 tiles, coarse levels <= 8^3 in one block", 1, 0, 16, 1, 512},
+        {"fused sweep, 32x8x8 tiles, coarse levels <= 16^3 in one block", 1, 0, 16, 1, 4096},
+    };
+    const EngineOptions saved = s->opt;
+    auto scratch = clone_mf(*sol);
+    FabSet ft = scratch->fabset(), fr = rhs->fabset();
+    cudaStream_t st = lib_stream();
+    std::string report;
+    double best = 1e300;
+    int bi = 0;
+    const int ncand = (saved.precision == 1) ? (int)(sizeof(cands) / sizeof(cands[0])) : 1;
+    for (int c = 0; c < ncand; ++c) {
+        s->opt = saved;
+        s->opt.fused_smoother = cands[c].fused;
+        s->opt.march_sweep = cands[c].march;
+        s->opt.march_tz = cands[c].tz;
+        s->opt.coarse_block = cands[c].coarse;
+        s->opt.coarse_cells = cands[c].cells;
+        s->opt.fixed_iter = vcycles;
+        s->eng.reset();
+        Engine& e = engine_for(s);
+        double ms = 0;
+        for (int rep = 0; rep < 2; ++rep) {       // the first run captures the graph
+            MLMG_CUDA_CHECK(cudaMemcpyAsync(scratch->data.p, sol->data.p, (size_t)sol->total * sol->prec,
+                                            cudaMemcpyDeviceToDevice, st));
+            MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+            e.solve({&ft}, {&ft}, {&fr}, 0.0, 0.0);
+            ms = e.last_solve_ms();
+        }
+        count_launches(e);
+        char line[160];
+        std::snprintf(line, sizeof(line), "%-64s %9.3f ms / %d V-cycles\n", cands[c].name, ms, vcycles);
+        report += line;
+        if (ms < best) { best = ms; bi = c; }
+    }
+    s->opt = saved;
+    if (saved.precision == 1) {
+        s->opt.fused_smoother = cands[bi].fused;
+        s->opt.march_sweep = cands[bi].march;
+        s->opt.march_tz = cands[bi].tz;
+        s->opt.coarse_block = cands[bi].coarse;
+        s->opt.coarse_cells = cands[bi].cells;
+    }
+    s->eng.reset();
+    report += std::string("chosen: ") + cands[bi].name + "\n";
+    s->tune_report = report;
+    if (best_ms) { *best_ms = best; }
+    API_END
+}
+
+const char* mlmg_autotune_report (mlmg_solver s) { return s ? s->tune_report.c_str() : ""; }
 
 int mlmg_apply (mlmg_solver s, mlmg_multifab out, mlmg_multifab in)
 {

@@ -5,7 +5,7 @@
 // abec_gsrb / mlpoisson_gsrb and the inline ghost closures), organised to
 // keep HBM busy instead of the issue slots:
 //
-// * a block owns an MS_TX x MS_TY column of cells and walks MS_TZ planes of
+// * a block owns an MS_TX x MS_TY column of cells and walks tz planes of
 //   it; the first colour is recomputed only on a one-cell ring in x and y and
 //   on one plane above and below the chunk, not on a halo around every tile;
 // * every array (phi_in, rhs, D, sX, sY, sZ) is staged plane by plane into
@@ -25,7 +25,7 @@ namespace mlmg {
 
 constexpr int MS_TX = 64;                  // column width in x (32 thread pairs)
 constexpr int MS_TY = 16;                  // rows of the column
-constexpr int MS_TZ = 16;                  // planes per chunk
+constexpr int MS_TZ = 16;                  // default planes per chunk (the slab depth tz is a launch parameter)
 constexpr int MS_THREADS = (MS_TX / 2) * MS_TY;
 constexpr int MS_RP = MS_TX + 8;           // shared row: x0-4 .. x0+MS_TX+3 (16-byte chunks)
 constexpr int MS_CH = MS_RP / 4;           // 16-byte chunks per row
@@ -47,13 +47,13 @@ constexpr int march_smem_floats (bool varc)
            (varc ? MS_ZS * MS_CPLANE : 0);
 }
 
-inline int march_tiles_of (const PatchDesc& P)
+inline int march_tiles_of (const PatchDesc& P, int tz)
 {
     const int nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1, nz = P.hi[2] - P.lo[2] + 1;
-    return ((nx + MS_TX - 1) / MS_TX) * ((ny + MS_TY - 1) / MS_TY) * ((nz + MS_TZ - 1) / MS_TZ);
+    return ((nx + MS_TX - 1) / MS_TX) * ((ny + MS_TY - 1) / MS_TY) * ((nz + tz - 1) / tz);
 }
 
-__device__ __forceinline__ TileCoord decode_march_tile (const DevLevel& L, const Subset& S, int b)
+__device__ __forceinline__ TileCoord decode_march_tile (const DevLevel& L, const Subset& S, int b, int tz)
 {
     int lo = 0, hi = S.n - 1;
     while (lo < hi) {
@@ -68,7 +68,7 @@ __device__ __forceinline__ TileCoord decode_march_tile (const DevLevel& L, const
     const int nty = (P.hi[1] - P.lo[1] + MS_TY) / MS_TY;
     c.x0 = P.lo[0] + (t % ntx) * MS_TX;
     c.y0 = P.lo[1] + ((t / ntx) % nty) * MS_TY;
-    c.z0 = P.lo[2] + (t / (ntx * nty)) * MS_TZ;
+    c.z0 = P.lo[2] + (t / (ntx * nty)) * tz;
     return c;
 }
 
@@ -121,7 +121,7 @@ __device__ __forceinline__ float ms_update (const PatchLite& P, int i, int j, in
 template <bool VARC>
 __global__ void __launch_bounds__(MS_THREADS, 1)
 k_sweep_march (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
-               const float* __restrict__ rhs, StencilPtrs Sc)
+               const float* __restrict__ rhs, StencilPtrs Sc, int tz)
 {
     extern __shared__ __align__(16) float ms_smem[];
     __shared__ PatchLite SP;
@@ -132,7 +132,7 @@ k_sweep_march (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __
     const int tid = threadIdx.y * (MS_TX / 2) + threadIdx.x;
     int x0, y0, z0;
     {
-        const TileCoord c = decode_march_tile(L, S, blockIdx.x);
+        const TileCoord c = decode_march_tile(L, S, blockIdx.x, tz);
         x0 = c.x0; y0 = c.y0; z0 = c.z0;
         if (tid == 0) {
             const PatchDesc& Q = L.P[c.p];
@@ -151,7 +151,7 @@ k_sweep_march (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __
     __syncthreads();
     const PatchLite& P = SP;
     const int lo0 = P.lo[0], lo1 = P.lo[1], lo2 = P.lo[2], hi0 = P.hi[0], hi1 = P.hi[1], hi2 = P.hi[2];
-    const int ks = z0, ke = min(z0 + MS_TZ, hi2 + 1);                 // output planes [ks, ke)
+    const int ks = z0, ke = min(z0 + tz, hi2 + 1);                    // output planes [ks, ke)
     const float* const Dg = static_cast<const float*>(Sc.D);
     const float* const SXg = static_cast<const float*>(Sc.sx);
     const float* const SYg = static_cast<const float*>(Sc.sy);

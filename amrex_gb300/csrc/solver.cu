@@ -308,7 +308,7 @@ void Engine::Impl::build ()
             Z.h_plist = mg;
             Z.n = (int)mg.size();
             Z.h_tstart.assign(Z.n + 1, 0);
-            for (int q = 0; q < Z.n; ++q) { Z.h_tstart[q + 1] = Z.h_tstart[q] + march_tiles_of(M.patches[mg[q]]); }
+            for (int q = 0; q < Z.n; ++q) { Z.h_tstart[q + 1] = Z.h_tstart[q] + march_tiles_of(M.patches[mg[q]], E.m_opt.march_tz); }
             Z.ntiles = Z.h_tstart[Z.n];
             L.march = E.m_opt.march_sweep && Z.ntiles >= E.m_opt.march_min_tiles;
             if (L.march) {
@@ -661,10 +661,10 @@ void Engine::Impl::smooth_fused (int l, int n)
             const dim3 blk(MS_TX / 2, MS_TY);
             if (abec) {
                 k_sweep_march<true><<<L.mz.ntiles, blk, march_smem_floats(true) * sizeof(float), st()>>>(
-                    L.dl, L.mz.dev(), a, b, L.res32.p, S);
+                    L.dl, L.mz.dev(), a, b, L.res32.p, S, E.m_opt.march_tz);
             } else {
                 k_sweep_march<false><<<L.mz.ntiles, blk, march_smem_floats(false) * sizeof(float), st()>>>(
-                    L.dl, L.mz.dev(), a, b, L.res32.p, S);
+                    L.dl, L.mz.dev(), a, b, L.res32.p, S, E.m_opt.march_tz);
             }
         } else if (abec) {
             k_sweep_fused<true><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);

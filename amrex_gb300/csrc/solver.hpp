@@ -45,6 +45,7 @@ struct EngineOptions {
     int march_sweep = 0;        // fused sweeps marching along z on levels with enough columns
                                 // (measured slower than the tiled fused sweep: 0.27 vs 0.18 ms at 256^3)
     int march_min_tiles = 304;  // ... at least this many (column, z-chunk) tiles
+    int march_tz = 16;          // planes per z-slab of the marching sweep
     int max_fmg_iter = 0;       // F-cycles (MLMGT::mgFcycle) for the first max_fmg_iter iterations
     int transpose = 0;          // solve A^T x = rhs (homogeneous BCs): the outer residual uses A^T,
                                 // the V-cycle of A is the correction operator (adjoint solves)

@@ -200,6 +200,19 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def _tuned_options(chosen):
+    """engine options of an autotuner choice (the report's last line)"""
+    march = "columns" in chosen
+    opts = [("march_sweep", 1 if march else 0)]
+    if march:
+        opts.append(("march_tz", int(chosen.rsplit(" ", 1)[-1])))
+    if "one block" in chosen:
+        opts += [("coarse_block", 1), ("coarse_cells", 512 if "8^3" in chosen else 4096)]
+    else:
+        opts.append(("coarse_block", 0))
+    return opts
+
+
 def bench_batch(stream, nsolve=64):
     """The batch of independent solves of uneven sizes (cube edges from
     {32, 48, ..., 128}, max_grid_size 32, per-solve seeded b and RHS), mixed
@@ -219,6 +232,14 @@ def bench_batch(stream, nsolve=64):
         m.setFusedSmoother(True)
         mixed.append(m)
     sols, rhss = [p["sol"] for p in probs], [p["rhs"] for p in probs]
+    # tile / slab shapes picked by the autotuner on the largest solve of the
+    # batch; the batch runs with the settings of its first solver
+    big = max(range(nsolve), key=lambda q: specs[q].n)
+    _, tune_report = mixed[big].autotune(sols[big], rhss[big], vcycles=2)
+    chosen = tune_report.strip().splitlines()[-1].replace("chosen: ", "")
+    mixed[0].setFusedSmoother(not chosen.startswith("colour passes"))
+    for name, val in _tuned_options(chosen):
+        mixed[0].setOption(name, val)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def batched():
@@ -263,7 +284,7 @@ def bench_batch(stream, nsolve=64):
             "speedup": seq_ms / batch_ms, "all_converged": all(v == 0 for v in st),
             "iters_mixed": [min(iters_b), max(iters_b)],
             "iters_fp64": [min(m.getNumIters() for m in fp64), max(m.getNumIters() for m in fp64)],
-            "phi_rel_diff_vs_fp64_max": err}
+            "phi_rel_diff_vs_fp64_max": err, "autotuned": chosen}
 
 
 def bench_adjoint(stream, n=128):

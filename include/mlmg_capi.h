@@ -209,6 +209,17 @@ int mlmg_get_num_mg_levels(mlmg_solver s);
 int mlmg_solve_batched(int n, const mlmg_solver* solvers, const mlmg_multifab* sols, const mlmg_multifab* rhss,
                        double tol_rel, double tol_abs, int* status);
 
+/* Autotuner (no counterpart in the reference): times `vcycles` fixed
+ * iterations of this solver's problem (sol is the initial guess and is left
+ * unchanged, rhs the right-hand side) under each candidate smoother layout --
+ * two colour passes, the fused sweep on 32x8x8 tiles, the z-marching fused
+ * sweep on 64x16 columns with z-slabs of 8, 16 or 32 planes, and the coarse
+ * levels run in one block per solve -- keeps the fastest in the solver's
+ * options and reports its time.  FP64 solvers have one layout.  The text of
+ * the last report (one line per candidate) comes from mlmg_autotune_report. */
+int mlmg_autotune(mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, int vcycles, double* best_ms);
+const char* mlmg_autotune_report(mlmg_solver s);
+
 /* Adjoint gradients of J(phi) for the solution phi = sol of A phi = f (no
  * counterpart in the reference; the face-gradient contraction is the one of
  * MLMG::getGradSolution / compFlux, AMReX_MLMG.H:553-761).  Solves
