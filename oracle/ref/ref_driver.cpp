@@ -12,6 +12,8 @@
 //            apply  : MLMG::apply (out = L phi, inhomogeneous BC)  -> out.bin
 //            solve  : MLMG::solve                                  -> phi.bin, result.txt
 //            flux   : solve, then getFluxes / getGradSolution    -> also f[xyz].bin, g[xyz].bin
+//            amrgrids : AmrMesh::MakeNewGrids tagging |rhs_l| > thresh_l -> grids.txt
+//            amrsolve : composite multi-level MLPoisson solve          -> phi_l<lev>.bin, result.txt
 //
 // case.txt holds "key value..." lines; binary inputs are little-endian
 // float64 arrays over the whole domain, x fastest.
@@ -21,6 +23,8 @@
 #include <AMReX_MLABecLaplacian.H>
 #include <AMReX_MLPoisson.H>
 #include <AMReX_ParmParse.H>
+#include <AMReX_AmrMesh.H>
+#include <AMReX_TagBox.H>
 
 #include <omp.h>
 
@@ -164,6 +168,134 @@ LPInfo make_info (const Case& c)
     return info;
 }
 
+// AmrMesh whose ErrorEst tags cells where |rhs_l| > thresh_l (rhs of each
+// level given on the level's whole domain)
+struct TagMesh : AmrMesh {
+    std::vector<std::vector<double>> rhs;   // per level, x fastest
+    std::vector<double> thresh;
+    std::vector<Box> dom;
+    TagMesh (Geometry const& g, AmrInfo const& info) : AmrMesh(g, info) {}
+    void ErrorEst (int lev, TagBoxArray& tags, Real, int) override {
+        const Box& d = dom[lev];
+        const int nx = d.length(0), ny = d.length(1);
+        for (MFIter mfi(tags); mfi.isValid(); ++mfi) {
+            const Box& bx = mfi.validbox();
+            auto t = tags.array(mfi);
+            const auto lo = lbound(bx), hi = ubound(bx);
+            for (int k = lo.z; k <= hi.z; ++k)
+            for (int j = lo.y; j <= hi.y; ++j)
+            for (int i = lo.x; i <= hi.x; ++i) {
+                const double v = rhs[lev][((size_t)k * ny + j) * nx + i];
+                if (std::abs(v) > thresh[lev]) { t(i,j,k) = TagBox::SET; }
+            }
+        }
+    }
+};
+
+void read_boxes (const Case& c, const std::string& key, BoxList& bl)
+{
+    const auto& v = c.kv.at(key);
+    for (size_t m = 0; m + 5 < v.size(); m += 6) {
+        bl.push_back(Box(IntVect(std::stoi(v[m]), std::stoi(v[m+1]), std::stoi(v[m+2])),
+                         IntVect(std::stoi(v[m+3]), std::stoi(v[m+4]), std::stoi(v[m+5]))));
+    }
+}
+
+// amrgrids: AmrMesh::MakeNewGrids with |rhs| tagging -> grids.txt
+// amrsolve: composite MLPoisson solve on the given per-level grids
+//           -> phi_l<lev>.bin (level domain, cells of the level's boxes), result.txt
+int run_amr (const std::string& mode, const std::string& dir)
+{
+    Case c{read_case(dir)};
+    const int nlev = c.geti("nlev", 1);
+    const int nx = c.geti("n", 32, 0), ny = c.geti("n", 32, 1), nz = c.geti("n", 32, 2);
+    RealBox rb({0., 0., 0.}, {1., 1., 1.});
+    Array<int,3> is_per{0, 0, 0};
+    std::vector<Box> dom;
+    Vector<Geometry> geom;
+    for (int l = 0; l < nlev; ++l) {
+        const int r = 1 << l;
+        dom.emplace_back(IntVect(0), IntVect(nx*r-1, ny*r-1, nz*r-1));
+        geom.emplace_back(dom.back(), rb, CoordSys::cartesian, is_per);
+    }
+    if (mode == "amrgrids") {
+        AmrInfo info;
+        info.max_level = nlev - 1;
+        info.ref_ratio = Vector<IntVect>(nlev, IntVect(2));
+        info.blocking_factor = Vector<IntVect>(nlev, IntVect(c.geti("blocking_factor", 8)));
+        info.max_grid_size = Vector<IntVect>(nlev, IntVect(c.geti("max_grid_size", 64)));
+        info.n_error_buf = Vector<IntVect>(nlev, IntVect(c.geti("n_error_buf", 1)));
+        info.grid_eff = c.getd("grid_eff", 0.7);
+        TagMesh mesh(geom[0], info);
+        mesh.dom = dom;
+        for (int l = 0; l < nlev; ++l) {
+            mesh.rhs.push_back(read_bin(dir + "/rhs_l" + std::to_string(l) + ".bin", (size_t)dom[l].numPts()));
+            mesh.thresh.push_back(c.getd("thresh", 0.0, l));
+        }
+        mesh.MakeNewGrids(0.0);
+        std::ofstream gs(dir + "/grids.txt");
+        for (int l = 0; l <= mesh.finestLevel(); ++l) {
+            const BoxArray& g = mesh.boxArray(l);
+            gs << "level " << l << " " << g.size() << "\n";
+            for (int b = 0; b < g.size(); ++b) {
+                gs << g[b].smallEnd(0) << " " << g[b].smallEnd(1) << " " << g[b].smallEnd(2) << " "
+                   << g[b].bigEnd(0) << " " << g[b].bigEnd(1) << " " << g[b].bigEnd(2) << "\n";
+            }
+        }
+        return 0;
+    }
+    // composite solve
+    Vector<BoxArray> ba(nlev);
+    Vector<DistributionMapping> dm(nlev);
+    for (int l = 0; l < nlev; ++l) {
+        BoxList bl;
+        read_boxes(c, "boxes_l" + std::to_string(l), bl);
+        ba[l] = BoxArray(bl);
+        dm[l] = DistributionMapping(ba[l]);
+    }
+    LPInfo info = make_info(c);
+    MLPoisson pois(geom, ba, dm, info);
+    setup_op(pois, c);
+    Vector<MultiFab> sol(nlev), rhs(nlev);
+    for (int l = 0; l < nlev; ++l) {
+        sol[l].define(ba[l], dm[l], 1, 1);
+        rhs[l].define(ba[l], dm[l], 1, 0);
+        const int gx = dom[l].length(0), gy = dom[l].length(1), gz = dom[l].length(2);
+        Global gs{gx+2, gy+2, gz+2, -1, -1, -1, std::vector<double>((size_t)(gx+2)*(gy+2)*(gz+2), 0.0)};
+        fill_from_global(sol[l], gs, 1);
+        Global gr{gx, gy, gz, 0, 0, 0, read_bin(dir + "/rhs_l" + std::to_string(l) + ".bin", (size_t)gx*gy*gz)};
+        fill_from_global(rhs[l], gr, 0);
+        pois.setLevelBC(l, &sol[l]);
+    }
+    MLMG mlmg(pois);
+    mlmg.setVerbose(c.geti("verbose", 0));
+    mlmg.setMaxIter(c.geti("max_iter", 200));
+    if (c.geti("fixed_iter", 0) > 0) { mlmg.setFixedIter(c.geti("fixed_iter", 0)); }
+    auto t0 = std::chrono::steady_clock::now();
+    const Real resid = mlmg.solve(GetVecOfPtrs(sol), GetVecOfConstPtrs(rhs), c.getd("tol_rel", 1e-10),
+                                  c.getd("tol_abs", 0.0));
+    auto t1 = std::chrono::steady_clock::now();
+    for (int l = 0; l < nlev; ++l) {
+        const int gx = dom[l].length(0), gy = dom[l].length(1), gz = dom[l].length(2);
+        Global go{gx, gy, gz, 0, 0, 0, std::vector<double>((size_t)gx*gy*gz, 0.0)};
+        copy_to_global(sol[l], go);
+        write_bin(dir + "/phi_l" + std::to_string(l) + ".bin", go.v);
+    }
+    std::ofstream res(dir + "/result.txt");
+    res.precision(17);
+    res << "final_resid " << resid << "\n";
+    res << "init_resid " << mlmg.getInitResidual() << "\n";
+    res << "rhs_norm " << mlmg.getInitRHS() << "\n";
+    res << "niters " << mlmg.getNumIters() << "\n";
+    res << "history";
+    for (auto h : mlmg.getResidualHistory()) { res << " " << h; }
+    res << "\ncg_iters";
+    for (auto h : mlmg.getNumCGIters()) { res << " " << h; }
+    res << "\nsolve_seconds " << std::chrono::duration<double>(t1 - t0).count();
+    res << "\nthreads " << omp_get_max_threads() << "\n";
+    return 0;
+}
+
 } // namespace
 
 int main (int argc, char* argv[])
@@ -179,6 +311,11 @@ int main (int argc, char* argv[])
         pp.add("verbose", 0);
         pp.add("signal_handling", 0);
     });
+    if (mode == "amrgrids" || mode == "amrsolve") {
+        const int rc = run_amr(mode, dir);
+        amrex::Finalize();
+        return rc;
+    }
     {
         Case c{read_case(dir)};
         const int nx = c.geti("n", 32, 0), ny = c.geti("n", 32, 1), nz = c.geti("n", 32, 2);

@@ -1,0 +1,70 @@
+"""AMR composite-solve cases: a base level of n^3 cells, refinement ratio 2,
+levels tagged where |RHS| exceeds the 90th percentile of |RHS| on that level
+(RHS: the seeded sum of 16 Gaussian blobs sampled at each level's cell
+centres), homogeneous Dirichlet on the domain, MLPoisson.  Grids come from the
+reference's AmrMesh (tests/golden/make_amr_golden.py)."""
+from __future__ import annotations
+
+import ast
+import os
+
+import numpy as np
+
+from amrex_gb300 import synth
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+CASES = {
+    # the 3-level composite configuration: base 128^3, max_grid_size 64 (grids only)
+    "c2": dict(n=128, nlev=3, max_grid_size=64, rhs_seed=1002, solve=False),
+    # small composite solves for parity
+    "c2_n32": dict(n=32, nlev=3, max_grid_size=16, rhs_seed=1002),
+    "c2_n16_2lev": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1012),
+}
+
+
+def level_rhs(case, lev):
+    """RHS on the whole domain of level lev, shape (m, m, m), m = n 2^lev."""
+    return synth.gaussian_rhs(case["n"] << lev, case["rhs_seed"])
+
+
+def parse_grids(text):
+    levels = []
+    for line in text.strip().splitlines():
+        p = line.split()
+        if p[0] == "level":
+            levels.append([])
+        else:
+            levels[-1].append(tuple(int(v) for v in p))
+    return levels
+
+
+def pack_boxes(arr, boxes):
+    """values of a whole-domain array (z, y, x) on the cells of `boxes`, box by
+    box, x fastest"""
+    out = []
+    for b in boxes:
+        out.append(arr[b[2]:b[5] + 1, b[1]:b[4] + 1, b[0]:b[3] + 1].ravel())
+    return np.concatenate(out)
+
+
+def unpack_boxes(flat, boxes, m):
+    arr = np.zeros((m, m, m))
+    q = 0
+    for b in boxes:
+        shp = (b[5] - b[2] + 1, b[4] - b[1] + 1, b[3] - b[0] + 1)
+        sz = shp[0] * shp[1] * shp[2]
+        arr[b[2]:b[5] + 1, b[1]:b[4] + 1, b[0]:b[3] + 1] = flat[q:q + sz].reshape(shp)
+        q += sz
+    return arr
+
+
+def load(kind, name):
+    z = np.load(os.path.join(HERE, f"{kind}_{name}.npz"))
+    out = {k: z[k] for k in z.files}
+    out["case"] = ast.literal_eval(str(out["case"]))
+    out["grids"] = parse_grids(str(out["grids"]))
+    if "result" in out:
+        from tests.golden.load import parse_result
+        out["result"] = parse_result(str(out["result"]))
+    return out
