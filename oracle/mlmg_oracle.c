@@ -175,6 +175,7 @@ typedef struct {
     int is_abec;
     double alpha, beta;
     double dx0[3];
+    int crse_ratio;     /* refinement ratio to the next coarser AMR level (1 at AMR level 0) */
 } Hier;
 
 static void level_geom(Level* L, const Box* dom, const Hier* H) {
@@ -356,7 +357,9 @@ static void define_bc(Hier* H, Level* L, const OracleOptions* o) {
                 *bct = hi ? H->hibc[d] : H->lobc[d];
             } else {
                 *bct = LO_DIRICHLET; /* default coarse/fine BC type */
-                *bcl = 0.5 * 1.0 * H->dx0[d];  /* ratio 1 at amr level 0, level-0 cell size */
+                /* MLMGBndryT::setBoxBC (AMReX_MLMGBndry.H:106-150): 0.5 * ratio * dx of the
+                   AMR level (ratio 1 at AMR level 0) */
+                *bcl = 0.5 * (double)(H->crse_ratio > 0 ? H->crse_ratio : 1) * H->dx0[d];
             }
             Box ab = adj_cell(bx, f);
             Fab* m = &L->mask[6 * b + f];
@@ -437,7 +440,7 @@ static double gg_at(const GrownGlobal* g, int i, int j, int k) {
 }
 
 static void apply_bc(const Hier* H, const Level* L, MF* m, int inhomog, const GrownGlobal* bcval,
-                     int skip_fillboundary) {
+                     int skip_fillboundary, const Fab* bfab) {
     if (!skip_fillboundary) fill_boundary(L, H->periodic, m, 1);
     for (int b = 0; b < m->nbox; ++b) {
         Fab* phi = &m->fab[b];
@@ -468,7 +471,10 @@ static void apply_bc(const Hier* H, const Level* L, MF* m, int inhomog, const Gr
                     for (int q = 1; q < NX; ++q) tmp += A(phi, i + q * di, j + q * dj, k + q * dk) * coef[q];
                     A(phi, i, j, k) = tmp;
                     if (inhomog) {
-                        double bv = bcval ? gg_at(bcval, i, j, k) : 0.0;
+                        /* boundary values per box face (a fine AMR level: coarse/fine
+                           values from InterpBndryData, physical values from the level BC),
+                           or the level-0 values in the ghosts of a grown global array */
+                        double bv = bfab ? A(&bfab[6 * b + f], i, j, k) : (bcval ? gg_at(bcval, i, j, k) : 0.0);
                         A(phi, i, j, k) += bv * coef[0];
                     }
                 }
@@ -764,7 +770,7 @@ typedef struct {
 static void smooth(Solver* S, int lev, MF* sol, const MF* rhs, int skip_fb) {
     /* MLCellLinOpT::smooth, AMReX_MLCellLinOp.H:1204-1217 */
     for (int rb = 0; rb < 2; ++rb) {
-        apply_bc(&S->H, &S->H.lev[lev], sol, 0, NULL, skip_fb);
+        apply_bc(&S->H, &S->H.lev[lev], sol, 0, NULL, skip_fb, NULL);
         fsmooth(&S->H, &S->H.lev[lev], sol, rhs, rb);
         skip_fb = 0;
     }
@@ -772,14 +778,14 @@ static void smooth(Solver* S, int lev, MF* sol, const MF* rhs, int skip_fb) {
 
 /* correctionResidual (homogeneous): r = b - A x, AMReX_MLCellLinOp.H:1246-1270 */
 static void correction_residual(Solver* S, int lev, MF* r, MF* x, const MF* b) {
-    apply_bc(&S->H, &S->H.lev[lev], x, 0, NULL, 0);
+    apply_bc(&S->H, &S->H.lev[lev], x, 0, NULL, 0, NULL);
     fapply(&S->H, &S->H.lev[lev], r, x);
     mf_axpy(&S->H.lev[lev], r, -1.0, b, 3);
 }
 
 /* solutionResidual, AMReX_MLCellLinOp.H:1219-1236 */
 static void solution_residual(Solver* S, MF* r, MF* x, const MF* b) {
-    apply_bc(&S->H, &S->H.lev[0], x, 1, &S->bcval, 0);
+    apply_bc(&S->H, &S->H.lev[0], x, 1, &S->bcval, 0, NULL);
     fapply(&S->H, &S->H.lev[0], r, x);
     mf_axpy(&S->H.lev[0], r, -1.0, b, 3);
 }
@@ -823,7 +829,7 @@ static int bicgstab(Solver* S, int lev, MF* sol, const MF* rhs, double eps_rel, 
             mf_axpy(L, &p, -omega, &v, 2);
             mf_axpy(L, &p, beta, &r, 3);
         }
-        apply_bc(H, L, &p, 0, NULL, 0);
+        apply_bc(H, L, &p, 0, NULL, 0, NULL);
         fapply(H, L, &v, &p);
         normalize(H, L, &v);
         double rhTv = mf_dot(L, &rh, &v);
@@ -833,7 +839,7 @@ static int bicgstab(Solver* S, int lev, MF* sol, const MF* rhs, double eps_rel, 
         mf_axpy(L, &r, -alpha, &v, 2);
         rnorm = mf_norminf(L, &r);
         if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
-        apply_bc(H, L, &r, 0, NULL, 0);
+        apply_bc(H, L, &r, 0, NULL, 0, NULL);
         fapply(H, L, &t, &r);
         normalize(H, L, &t);
         double tt = mf_dot(L, &t, &t), tr = mf_dot(L, &t, &r);
@@ -1012,10 +1018,13 @@ static void copy_mf_to_global(const Level* L, const MF* m, double* g) {
     }
 }
 
-static int setup(Solver* S, const OracleProblem* P, const OracleOptions* o) {
+static int setup_ratio(Solver* S, const OracleProblem* P, const OracleOptions* o, int crse_ratio);
+static int setup(Solver* S, const OracleProblem* P, const OracleOptions* o) { return setup_ratio(S, P, o, 1); }
+static int setup_ratio(Solver* S, const OracleProblem* P, const OracleOptions* o, int crse_ratio) {
     memset(S, 0, sizeof(*S));
     S->o = *o;
     Hier* H = &S->H;
+    H->crse_ratio = crse_ratio;
     for (int d = 0; d < 3; ++d) {
         H->n[d] = P->n[d]; H->periodic[d] = P->periodic[d];
         H->prob_lo[d] = P->prob_lo[d]; H->prob_hi[d] = P->prob_hi[d];
@@ -1182,7 +1191,7 @@ int oracle_fluxes(const OracleProblem* P, const OracleOptions* o, int mode, doub
     MF x;
     mf_define(&x, L->nbox, L->boxes, 1, -1);
     copy_global_to_mf(L, &x, P->sol, 1, -1);
-    apply_bc(H, L, &x, 1, &S->bcval, 0);
+    apply_bc(H, L, &x, 1, &S->bcval, 0, NULL);
     double* out[3] = {fx, fy, fz};
     const double bscalar = H->is_abec ? H->beta : -1.0;   /* MLPoissonT::getBScalar is -1 */
     const double betainv = 1.0 / bscalar;
@@ -1292,4 +1301,128 @@ int oracle_solve(const OracleProblem* P, const OracleOptions* o, double* phi_out
     free_solver(S);
     free(S);
     return R->status;
+}
+
+/* ======================================================================
+ * AMR composite solve: MLMGT::solve over several AMR levels
+ * (AMReX_MLMG.H:353-541, oneIter :1227-1293), MLPoisson, refinement ratio 2.
+ * AMR level 0 keeps its full MG hierarchy; finer AMR levels have one MG level
+ * (MLLinOpT::defineGrids, AMReX_MLLinOp.H:843-880).
+ * ====================================================================== */
+#define AMR_MAX 4
+
+typedef struct {
+    int nlev;
+    Solver S[AMR_MAX];
+    Fab* bsol[AMR_MAX];     /* [6*nbox] boundary values of the solution (m_bndry_sol) */
+    Fab* bcor[AMR_MAX];     /* [6*nbox] boundary values of the correction (m_bndry_cor) */
+    MF cor_hold[AMR_MAX];
+} Amr;
+
+/* mask value (MultiMask, Src/Boundary/AMReX_MultiMask.cpp:25-69) of cell
+ * (i,j,k) at a level: outside the domain, covered by a box of the level
+ * (periodic images included) or not covered */
+static int level_mask(const Hier* H, const Level* L, int i, int j, int k) {
+    int c[3] = {i, j, k};
+    for (int q = 0; q < 3; ++q)
+        if (!H->periodic[q] && (c[q] < L->domain.lo[q] || c[q] > L->domain.hi[q])) return MASK_OUTSIDE;
+    int wi, wj, wk;
+    return (locate(L, H->periodic, i, j, k, &wi, &wj, &wk) >= 0) ? MASK_COVERED : MASK_NOT_COVERED;
+}
+
+/* value of a valid cell of MF m on level L (periodic images included), or 0
+ * where no box holds it (BndryRegisterT::copyFrom / ParallelCopy semantics) */
+static double cell_value(const Hier* H, const Level* L, const MF* m, int i, int j, int k) {
+    int wi, wj, wk;
+    int b = locate(L, H->periodic, i, j, k, &wi, &wj, &wk);
+    return (b >= 0) ? A(&m->fab[b], wi, wj, wk) : 0.0;
+}
+
+static int cdiv2(int a) { return (a >= 0) ? a / 2 : -((-a + 1) / 2); }
+
+/* InterpBndryDataT::setBndryValues / updateBndryValues (Src/Boundary/
+ * AMReX_InterpBndryData.H:158-252) with interpbndrydata_{x,y,z}_o3
+ * (AMReX_InterpBndryData_3D_K.H:20-120), ratio 2: boundary values of fine
+ * level l on every box face.  Faces off the non-periodic domain boundary get
+ * the coarse values (crse, level l-1) at the ghost cell's coarse cell plus
+ * tangential slopes and curvatures where the neighbouring fine ghost cells are
+ * not covered; faces on it get the level's BC values (phys != 0) or zero. */
+static void interp_bndry(Amr* A, int l, const MF* crse, int phys, Fab* dst) {
+    Solver* Sf = &A->S[l];
+    const Hier* Hf = &Sf->H;
+    const Level* Lf = &Hf->lev[0];
+    const Hier* Hc = &A->S[l - 1].H;
+    const Level* Lc = &Hc->lev[0];
+    const int r = 2;
+    for (int b = 0; b < Lf->nbox; ++b) {
+        const Box* bx = &Lf->boxes[b];
+        for (int f = 0; f < 6; ++f) {
+            const int d = f % 3, hi = f >= 3;
+            Fab* out = &dst[6 * b + f];
+            if (out->p == NULL) fab_define(out, adj_cell(bx, f), 0);
+            const int on_domain = hi ? (Lf->domain.hi[d] == bx->hi[d]) : (Lf->domain.lo[d] == bx->lo[d]);
+            if (on_domain && !Hf->periodic[d]) {
+                FOR_VALID(out, i, j, k) {
+                    A(out, i, j, k) = (phys && Sf->bcval.v) ? gg_at(&Sf->bcval, i, j, k) : 0.0;
+                }
+                continue;
+            }
+            const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;   /* tangential directions */
+            FOR_VALID(out, i, j, k) {
+                int c[3] = {i, j, k};
+                int cc[3] = {cdiv2(i), cdiv2(j), cdiv2(k)};
+#define CRS(a, bb, e) cell_value(Hc, Lc, crse, (a), (bb), (e))
+#define MSK(a, bb, e) level_mask(Hf, Lf, (a), (bb), (e))
+                double slope[2], curv[2];
+                int tdir[2] = {t1, t2};
+                for (int q = 0; q < 2; ++q) {
+                    const int t = tdir[q];
+                    int cm[3] = {c[0], c[1], c[2]}, cp[3] = {c[0], c[1], c[2]};
+                    cm[t] -= r; cp[t] += r;
+                    const int lo = (MSK(cm[0], cm[1], cm[2]) == MASK_NOT_COVERED) ? cc[t] - 1 : cc[t];
+                    const int hi2 = (MSK(cp[0], cp[1], cp[2]) == MASK_NOT_COVERED) ? cc[t] + 1 : cc[t];
+                    const double fac = (hi2 == lo + 1) ? 1.0 : 0.5;
+                    int ch[3] = {cc[0], cc[1], cc[2]}, cl[3] = {cc[0], cc[1], cc[2]};
+                    ch[t] = hi2; cl[t] = lo;
+                    slope[q] = fac * (CRS(ch[0], ch[1], ch[2]) - CRS(cl[0], cl[1], cl[2]));
+                    if (hi2 == lo + 2) {
+                        int cpp[3] = {cc[0], cc[1], cc[2]}, cmm[3] = {cc[0], cc[1], cc[2]};
+                        cpp[t] += 1; cmm[t] -= 1;
+                        curv[q] = 0.5 * (CRS(cpp[0], cpp[1], cpp[2]) - 2.0 * CRS(cc[0], cc[1], cc[2])
+                                         + CRS(cmm[0], cmm[1], cmm[2]));
+                    } else {
+                        curv[q] = 0.0;
+                    }
+                }
+                /* cross term: all four diagonal fine ghost cells not covered */
+                double cross = 0.0;
+                {
+                    int a[3];
+                    int ok = 1;
+                    for (int s1 = -1; s1 <= 1; s1 += 2)
+                        for (int s2 = -1; s2 <= 1; s2 += 2) {
+                            a[0] = c[0]; a[1] = c[1]; a[2] = c[2];
+                            a[t1] += s1 * r; a[t2] += s2 * r;
+                            if (MSK(a[0], a[1], a[2]) != MASK_NOT_COVERED) ok = 0;
+                        }
+                    if (ok) {
+                        int pp[3] = {cc[0], cc[1], cc[2]}, mp[3] = {cc[0], cc[1], cc[2]};
+                        int mm[3] = {cc[0], cc[1], cc[2]}, pm[3] = {cc[0], cc[1], cc[2]};
+                        pp[t1] += 1; pp[t2] += 1;
+                        mp[t1] -= 1; mp[t2] += 1;
+                        mm[t1] -= 1; mm[t2] -= 1;
+                        pm[t1] += 1; pm[t2] -= 1;
+                        cross = 0.25 * (CRS(pp[0], pp[1], pp[2]) - CRS(mp[0], mp[1], mp[2])
+                                        + CRS(mm[0], mm[1], mm[2]) - CRS(pm[0], pm[1], pm[2]));
+                    }
+                }
+                const double y = -0.5 + ((double)(c[t1] - cc[t1] * r) + 0.5) / (double)r;
+                const double z = -0.5 + ((double)(c[t2] - cc[t2] * r) + 0.5) / (double)r;
+                A(out, i, j, k) = CRS(cc[0], cc[1], cc[2]) + y * slope[0] + (y * y) * curv[0]
+                                  + z * slope[1] + (z * z) * curv[1] + y * z * cross;
+#undef CRS
+#undef MSK
+            }
+        }
+    }
 }
