@@ -1303,20 +1303,22 @@ int oracle_solve(const OracleProblem* P, const OracleOptions* o, double* phi_out
     return R->status;
 }
 
+
 /* ======================================================================
  * AMR composite solve: MLMGT::solve over several AMR levels
- * (AMReX_MLMG.H:353-541, oneIter :1227-1293), MLPoisson, refinement ratio 2.
- * AMR level 0 keeps its full MG hierarchy; finer AMR levels have one MG level
- * (MLLinOpT::defineGrids, AMReX_MLLinOp.H:843-880).
+ * (AMReX_MLMG.H:353-541, oneIter :1227-1293), MLPoisson, refinement ratio 2,
+ * non-periodic domain.  AMR level 0 keeps its full MG hierarchy; each finer
+ * AMR level has one MG level (MLLinOpT::defineGrids, AMReX_MLLinOp.H:843-880),
+ * so its mini-cycle is nu1 smoothing sweeps from zero (mgVcycle,
+ * AMReX_MLMG.H:1306-1415, amrlev > 0 branch).
  * ====================================================================== */
 #define AMR_MAX 4
 
 typedef struct {
     int nlev;
-    Solver S[AMR_MAX];
+    Solver S[AMR_MAX];      /* S[l].sol/rhs/res[0]/rescor[0]/cor[0]/cor_hold[0] are the AMR level's data */
     Fab* bsol[AMR_MAX];     /* [6*nbox] boundary values of the solution (m_bndry_sol) */
     Fab* bcor[AMR_MAX];     /* [6*nbox] boundary values of the correction (m_bndry_cor) */
-    MF cor_hold[AMR_MAX];
 } Amr;
 
 /* mask value (MultiMask, Src/Boundary/AMReX_MultiMask.cpp:25-69) of cell
@@ -1331,7 +1333,7 @@ static int level_mask(const Hier* H, const Level* L, int i, int j, int k) {
 }
 
 /* value of a valid cell of MF m on level L (periodic images included), or 0
- * where no box holds it (BndryRegisterT::copyFrom / ParallelCopy semantics) */
+ * where no box holds it (ParallelCopy of valid cells into zeroed data) */
 static double cell_value(const Hier* H, const Level* L, const MF* m, int i, int j, int k) {
     int wi, wj, wk;
     int b = locate(L, H->periodic, i, j, k, &wi, &wj, &wk);
@@ -1340,18 +1342,29 @@ static double cell_value(const Hier* H, const Level* L, const MF* m, int i, int 
 
 static int cdiv2(int a) { return (a >= 0) ? a / 2 : -((-a + 1) / 2); }
 
+/* coarse cell (i,j,k) of AMR level l lies under a box of level l+1 (boxes of
+ * a finer level are aligned to the refinement ratio) */
+static int covered_by_fine(const Amr* M, int l, int i, int j, int k) {
+    if (l + 1 >= M->nlev) return 0;
+    const Hier* Hf = &M->S[l + 1].H;
+    int wi, wj, wk;
+    return locate(&Hf->lev[0], Hf->periodic, 2 * i, 2 * j, 2 * k, &wi, &wj, &wk) >= 0;
+}
+
 /* InterpBndryDataT::setBndryValues / updateBndryValues (Src/Boundary/
- * AMReX_InterpBndryData.H:158-252) with interpbndrydata_{x,y,z}_o3
- * (AMReX_InterpBndryData_3D_K.H:20-120), ratio 2: boundary values of fine
- * level l on every box face.  Faces off the non-periodic domain boundary get
- * the coarse values (crse, level l-1) at the ghost cell's coarse cell plus
- * tangential slopes and curvatures where the neighbouring fine ghost cells are
- * not covered; faces on it get the level's BC values (phys != 0) or zero. */
-static void interp_bndry(Amr* A, int l, const MF* crse, int phys, Fab* dst) {
-    Solver* Sf = &A->S[l];
+ * AMReX_InterpBndryData.H:158-267) with interpbndrydata_{x,y,z}_o3
+ * (Src/Boundary/AMReX_InterpBndryData_3D_K.H:20-120), ratio 2: boundary
+ * values of AMR level l on every box face.  A face off the non-periodic
+ * domain boundary gets the coarse value (crse on level l-1, valid cells) at
+ * the ghost cell's coarse cell plus tangential slopes and curvatures, one-sided
+ * where a neighbouring fine ghost cell is not "not covered"; a face on it
+ * keeps the level's BC values (phys != 0: the solution) or zero (the
+ * correction, whose register is zeroed before the solve). */
+static void interp_bndry(Amr* M, int l, const MF* crse, int phys, Fab* dst) {
+    Solver* Sf = &M->S[l];
     const Hier* Hf = &Sf->H;
     const Level* Lf = &Hf->lev[0];
-    const Hier* Hc = &A->S[l - 1].H;
+    const Hier* Hc = &M->S[l - 1].H;
     const Level* Lc = &Hc->lev[0];
     const int r = 2;
     for (int b = 0; b < Lf->nbox; ++b) {
@@ -1369,60 +1382,433 @@ static void interp_bndry(Amr* A, int l, const MF* crse, int phys, Fab* dst) {
             }
             const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;   /* tangential directions */
             FOR_VALID(out, i, j, k) {
-                int c[3] = {i, j, k};
-                int cc[3] = {cdiv2(i), cdiv2(j), cdiv2(k)};
-#define CRS(a, bb, e) cell_value(Hc, Lc, crse, (a), (bb), (e))
-#define MSK(a, bb, e) level_mask(Hf, Lf, (a), (bb), (e))
+                const int c[3] = {i, j, k};
+                const int cc[3] = {cdiv2(i), cdiv2(j), cdiv2(k)};
+#define CRS(v) cell_value(Hc, Lc, crse, (v)[0], (v)[1], (v)[2])
+#define NOTCOV(v) (level_mask(Hf, Lf, (v)[0], (v)[1], (v)[2]) == MASK_NOT_COVERED)
                 double slope[2], curv[2];
-                int tdir[2] = {t1, t2};
+                const int tdir[2] = {t1, t2};
                 for (int q = 0; q < 2; ++q) {
                     const int t = tdir[q];
-                    int cm[3] = {c[0], c[1], c[2]}, cp[3] = {c[0], c[1], c[2]};
-                    cm[t] -= r; cp[t] += r;
-                    const int lo = (MSK(cm[0], cm[1], cm[2]) == MASK_NOT_COVERED) ? cc[t] - 1 : cc[t];
-                    const int hi2 = (MSK(cp[0], cp[1], cp[2]) == MASK_NOT_COVERED) ? cc[t] + 1 : cc[t];
+                    int fm[3] = {c[0], c[1], c[2]}, fp[3] = {c[0], c[1], c[2]};
+                    fm[t] -= r; fp[t] += r;
+                    const int lo = NOTCOV(fm) ? cc[t] - 1 : cc[t];
+                    const int hi2 = NOTCOV(fp) ? cc[t] + 1 : cc[t];
                     const double fac = (hi2 == lo + 1) ? 1.0 : 0.5;
                     int ch[3] = {cc[0], cc[1], cc[2]}, cl[3] = {cc[0], cc[1], cc[2]};
                     ch[t] = hi2; cl[t] = lo;
-                    slope[q] = fac * (CRS(ch[0], ch[1], ch[2]) - CRS(cl[0], cl[1], cl[2]));
+                    slope[q] = fac * (CRS(ch) - CRS(cl));
                     if (hi2 == lo + 2) {
-                        int cpp[3] = {cc[0], cc[1], cc[2]}, cmm[3] = {cc[0], cc[1], cc[2]};
-                        cpp[t] += 1; cmm[t] -= 1;
-                        curv[q] = 0.5 * (CRS(cpp[0], cpp[1], cpp[2]) - 2.0 * CRS(cc[0], cc[1], cc[2])
-                                         + CRS(cmm[0], cmm[1], cmm[2]));
+                        int cp[3] = {cc[0], cc[1], cc[2]}, cm[3] = {cc[0], cc[1], cc[2]};
+                        cp[t] += 1; cm[t] -= 1;
+                        curv[q] = 0.5 * (CRS(cp) - 2.0 * CRS(cc) + CRS(cm));
                     } else {
                         curv[q] = 0.0;
                     }
                 }
-                /* cross term: all four diagonal fine ghost cells not covered */
-                double cross = 0.0;
-                {
-                    int a[3];
-                    int ok = 1;
-                    for (int s1 = -1; s1 <= 1; s1 += 2)
-                        for (int s2 = -1; s2 <= 1; s2 += 2) {
-                            a[0] = c[0]; a[1] = c[1]; a[2] = c[2];
-                            a[t1] += s1 * r; a[t2] += s2 * r;
-                            if (MSK(a[0], a[1], a[2]) != MASK_NOT_COVERED) ok = 0;
-                        }
-                    if (ok) {
-                        int pp[3] = {cc[0], cc[1], cc[2]}, mp[3] = {cc[0], cc[1], cc[2]};
-                        int mm[3] = {cc[0], cc[1], cc[2]}, pm[3] = {cc[0], cc[1], cc[2]};
-                        pp[t1] += 1; pp[t2] += 1;
-                        mp[t1] -= 1; mp[t2] += 1;
-                        mm[t1] -= 1; mm[t2] -= 1;
-                        pm[t1] += 1; pm[t2] -= 1;
-                        cross = 0.25 * (CRS(pp[0], pp[1], pp[2]) - CRS(mp[0], mp[1], mp[2])
-                                        + CRS(mm[0], mm[1], mm[2]) - CRS(pm[0], pm[1], pm[2]));
+                /* cross term when the four diagonal fine ghost cells are not covered */
+                int ok = 1;
+                for (int s1 = -1; s1 <= 1; s1 += 2)
+                    for (int s2 = -1; s2 <= 1; s2 += 2) {
+                        int a[3] = {c[0], c[1], c[2]};
+                        a[t1] += s1 * r; a[t2] += s2 * r;
+                        if (!NOTCOV(a)) ok = 0;
                     }
+                double cross = 0.0;
+                if (ok) {
+                    int pp[3] = {cc[0], cc[1], cc[2]}, mp[3] = {cc[0], cc[1], cc[2]};
+                    int mm[3] = {cc[0], cc[1], cc[2]}, pm[3] = {cc[0], cc[1], cc[2]};
+                    pp[t1] += 1; pp[t2] += 1;
+                    mp[t1] -= 1; mp[t2] += 1;
+                    mm[t1] -= 1; mm[t2] -= 1;
+                    pm[t1] += 1; pm[t2] -= 1;
+                    cross = 0.25 * (CRS(pp) - CRS(mp) + CRS(mm) - CRS(pm));
                 }
                 const double y = -0.5 + ((double)(c[t1] - cc[t1] * r) + 0.5) / (double)r;
                 const double z = -0.5 + ((double)(c[t2] - cc[t2] * r) + 0.5) / (double)r;
-                A(out, i, j, k) = CRS(cc[0], cc[1], cc[2]) + y * slope[0] + (y * y) * curv[0]
+                A(out, i, j, k) = CRS(cc) + y * slope[0] + (y * y) * curv[0]
                                   + z * slope[1] + (z * z) * curv[1] + y * z * cross;
 #undef CRS
-#undef MSK
+#undef NOTCOV
             }
         }
     }
+}
+
+/* MLCellLinOpT::solutionResidual (AMReX_MLCellLinOp.H:1219-1236): at a fine
+ * AMR level the boundary values come from the coarser level's solution
+ * (updateSolBC, :651-664) when update != 0 */
+static void amr_solution_residual(Amr* M, int l, MF* r, MF* x, const MF* b, int update) {
+    Solver* S = &M->S[l];
+    if (l == 0) { solution_residual(S, r, x, b); return; }
+    if (update) interp_bndry(M, l, &M->S[l - 1].sol, 1, M->bsol[l]);
+    apply_bc(&S->H, &S->H.lev[0], x, 1, NULL, 0, M->bsol[l]);
+    fapply(&S->H, &S->H.lev[0], r, x);
+    mf_axpy(&S->H.lev[0], r, -1.0, b, 3);
+}
+
+/* MLCellLinOpT::correctionResidual, inhomogeneous with the coarser level's
+ * correction as boundary data (updateCorBC, AMReX_MLCellLinOp.H:666-680,
+ * 1246-1270) */
+static void amr_correction_residual_inhomog(Amr* M, int l, MF* r, MF* x, const MF* b) {
+    Solver* S = &M->S[l];
+    interp_bndry(M, l, &M->S[l - 1].cor[0], 0, M->bcor[l]);
+    apply_bc(&S->H, &S->H.lev[0], x, 1, NULL, 0, M->bcor[l]);
+    fapply(&S->H, &S->H.lev[0], r, x);
+    mf_axpy(&S->H.lev[0], r, -1.0, b, 3);
+}
+
+/* amrex::average_down of the valid fine cells onto the covered coarse cells
+ * (amrex_avgdown, Src/Base/AMReX_MultiFabUtil_3D_C.H:375-392) */
+static void amr_average_down(Amr* M, int c, const MF* fine, MF* crse) {
+    const Hier* Hc = &M->S[c].H;
+    const Level* Lc = &Hc->lev[0];
+    const Level* Lf = &M->S[c + 1].H.lev[0];
+    for (int b = 0; b < crse->nbox; ++b) {
+        Fab* cf = &crse->fab[b];
+        Box vb = Lc->boxes[b];
+        for (int k = vb.lo[2]; k <= vb.hi[2]; ++k)
+        for (int j = vb.lo[1]; j <= vb.hi[1]; ++j)
+        for (int i = vb.lo[0]; i <= vb.hi[0]; ++i) {
+            if (!covered_by_fine(M, c, i, j, k)) continue;
+            double s = 0;
+            for (int kr = 0; kr < 2; ++kr)
+            for (int jr = 0; jr < 2; ++jr)
+            for (int ir = 0; ir < 2; ++ir) {
+                int wi, wj, wk;
+                int fb = locate(Lf, Hc->periodic, 2 * i + ir, 2 * j + jr, 2 * k + kr, &wi, &wj, &wk);
+                s += A(&fine->fab[fb], wi, wj, wk);
+            }
+            A(cf, i, j, k) = 0.125 * s;
+        }
+    }
+}
+
+/* MLCellLinOpT::reflux (AMReX_MLCellLinOp.H:1272-1346) through YAFluxRegister
+ * (Src/Boundary/AMReX_YAFluxRegister.H:125-335, 343-560; yafluxreg_crseadd /
+ * yafluxreg_fineadd, AMReX_YAFluxRegister_3D_K.H): every coarse cell of level
+ * c next to level c+1 trades its coarse face flux for the mean of the fine
+ * face fluxes, res += (F_crse - <F_fine>) / dx_crse with MLPoisson's flux
+ * F = (phi_hi - phi_lo) / dx.  The fine solution's ghosts come from applyBC
+ * with the level's solution boundary values. */
+static void amr_reflux(Amr* M, int c, MF* res) {
+    Solver* Sc = &M->S[c];
+    Solver* Sf = &M->S[c + 1];
+    const Hier* Hc = &Sc->H;
+    const Level* Lc = &Hc->lev[0];
+    const Hier* Hf = &Sf->H;
+    const Level* Lf = &Hf->lev[0];
+    apply_bc(Hf, Lf, &Sf->sol, 1, NULL, 0, M->bsol[c + 1]);
+    MF data;
+    mf_define(&data, Lc->nbox, Lc->boxes, 0, -1);
+    mf_setval(&data, 0.0);
+    /* coarse side (CrseAdd, dt = 1) */
+    for (int b = 0; b < Lc->nbox; ++b) {
+        Fab* d = &data.fab[b];
+        Box vb = Lc->boxes[b];
+        for (int k = vb.lo[2]; k <= vb.hi[2]; ++k)
+        for (int j = vb.lo[1]; j <= vb.hi[1]; ++j)
+        for (int i = vb.lo[0]; i <= vb.hi[0]; ++i) {
+            if (covered_by_fine(M, c, i, j, k)) continue;
+            const int c0[3] = {i, j, k};
+            for (int q = 0; q < 3; ++q) {
+                const double dtdx = 1.0 / Lc->dx[q];
+                for (int side = 0; side < 2; ++side) {
+                    int n[3] = {c0[0], c0[1], c0[2]};
+                    n[q] += side ? 1 : -1;
+                    if (!covered_by_fine(M, c, n[0], n[1], n[2])) continue;
+                    const double vc = cell_value(Hc, Lc, &Sc->sol, i, j, k);
+                    const double vn = cell_value(Hc, Lc, &Sc->sol, n[0], n[1], n[2]);
+                    /* face flux on the face between the cell and its neighbour */
+                    const double fx = side ? Lc->dxinv[q] * (vn - vc) : Lc->dxinv[q] * (vc - vn);
+                    if (side) A(d, i, j, k) += dtdx * fx; else A(d, i, j, k) -= dtdx * fx;
+                }
+            }
+        }
+    }
+    /* fine side (FineAdd, one coarse/fine patch per fine box, then added) */
+    for (int fb = 0; fb < Lf->nbox; ++fb) {
+        const Box cb = bcoarsen(Lf->boxes[fb], 2);
+        Box gb = cb;
+        for (int q = 0; q < 3; ++q) { gb.lo[q] -= 1; gb.hi[q] += 1; }
+        Fab patch;
+        fab_define(&patch, gb, 0);
+        memset(patch.p, 0, sizeof(double) * fab_size(&patch));
+        const Fab* fs = &Sf->sol.fab[fb];
+        for (int q = 0; q < 3; ++q) {
+            const double dtdx = 1.0 / (Lf->dx[q] * 8.0);
+            for (int side = 0; side < 2; ++side) {
+                Box ab = adj_cell(&cb, q + 3 * side);
+                for (int k = ab.lo[2]; k <= ab.hi[2]; ++k)
+                for (int j = ab.lo[1]; j <= ab.hi[1]; ++j)
+                for (int i = ab.lo[0]; i <= ab.hi[0]; ++i) {
+                    const int cc3[3] = {i, j, k};
+                    int indom = 1;
+                    for (int e = 0; e < 3; ++e)
+                        if (cc3[e] < Lc->domain.lo[e] || cc3[e] > Lc->domain.hi[e]) indom = 0;
+                    if (!indom || covered_by_fine(M, c, i, j, k)) continue;
+                    /* the rr^2 fine faces on the coarse cell's face shared with the fine box */
+                    const int t1 = (q == 0) ? 1 : 0, t2 = (q == 2) ? 1 : 2;
+                    const int face = side ? 2 * cc3[q] : 2 * (cc3[q] + 1);
+                    for (int o2 = 0; o2 < 2; ++o2)
+                    for (int o1 = 0; o1 < 2; ++o1) {
+                        int fi[3];
+                        fi[q] = face;
+                        fi[t1] = 2 * cc3[t1] + o1;
+                        fi[t2] = 2 * cc3[t2] + o2;
+                        int lo3[3] = {fi[0], fi[1], fi[2]};
+                        lo3[q] -= 1;
+                        const double ff = Lf->dxinv[q] * (A(fs, fi[0], fi[1], fi[2]) - A(fs, lo3[0], lo3[1], lo3[2]));
+                        const double tmp = side ? dtdx * ff : -dtdx * ff;
+                        A(&patch, i, j, k) += tmp;
+                    }
+                }
+            }
+        }
+        /* add the patch into the register over the uncovered cells of grow(cb,1) */
+        FOR_VALID(&patch, i, j, k) {
+            const int cc3[3] = {i, j, k};
+            int indom = 1;
+            for (int e = 0; e < 3; ++e)
+                if (cc3[e] < Lc->domain.lo[e] || cc3[e] > Lc->domain.hi[e]) indom = 0;
+            if (!indom || covered_by_fine(M, c, i, j, k)) continue;
+            int wi, wj, wk;
+            int db = locate(Lc, Hc->periodic, i, j, k, &wi, &wj, &wk);
+            if (db >= 0) A(&data.fab[db], wi, wj, wk) += A(&patch, i, j, k);
+        }
+        free(patch.p);
+    }
+    mf_axpy(Lc, res, 1.0, &data, 1);
+    mf_free(&data);
+}
+
+/* MLMGT::interpCorrection(alev) (AMReX_MLMG.H:1719-1750) with
+ * MLCellLinOpT::interpolationAmr (AMReX_MLCellLinOp.H:1094-1181) and
+ * mlmg_lin_cc_interp_r2: the coarser level's correction is copied (valid
+ * cells) into zeroed FABs over the coarsened fine boxes grown by one, then
+ * interpolated trilinearly onto the fine level's valid cells. */
+static void amr_interp_correction(Amr* M, int l) {
+    const Hier* Hc = &M->S[l - 1].H;
+    const Level* Lc = &Hc->lev[0];
+    const Level* Lf = &M->S[l].H.lev[0];
+    const MF* crse = &M->S[l - 1].cor[0];
+    MF* fine = &M->S[l].cor[0];
+    for (int b = 0; b < Lf->nbox; ++b) {
+        Box cb = bcoarsen(Lf->boxes[b], 2);
+        Fab t;
+        fab_define(&t, cb, 1);
+        for (int k = cb.lo[2] - 1; k <= cb.hi[2] + 1; ++k)
+        for (int j = cb.lo[1] - 1; j <= cb.hi[1] + 1; ++j)
+        for (int i = cb.lo[0] - 1; i <= cb.hi[0] + 1; ++i)
+            A(&t, i, j, k) = cell_value(Hc, Lc, crse, i, j, k);
+        Fab* ff = &fine->fab[b];
+        FOR_VALID(ff, i, j, k) {
+            const int kc = k / 2, koff = 2 * (k - kc * 2) - 1;
+            const int jc = j / 2, joff = 2 * (j - jc * 2) - 1;
+            const int ic = i / 2, ioff = 2 * (i - ic * 2) - 1;
+            A(ff, i, j, k) = 0.421875 * A(&t, ic, jc, kc)
+                + 0.140625 * A(&t, ic + ioff, jc, kc)
+                + 0.140625 * A(&t, ic, jc + joff, kc)
+                + 0.140625 * A(&t, ic, jc, kc + koff)
+                + 0.046875 * A(&t, ic, jc + joff, kc + koff)
+                + 0.046875 * A(&t, ic + ioff, jc, kc + koff)
+                + 0.046875 * A(&t, ic + ioff, jc + joff, kc)
+                + 0.015625 * A(&t, ic + ioff, jc + joff, kc + koff);
+        }
+        free(t.p);
+    }
+}
+
+/* MLCellLinOpT::normInf (AMReX_MLCellLinOp.H:2006-2101): the finest level
+ * counts every cell; a coarser level only the cells no finer box covers */
+static double amr_norminf(const Amr* M, int l, const MF* m) {
+    const Level* L = &M->S[l].H.lev[0];
+    if (l == M->nlev - 1) return mf_norminf(L, m);
+    double r = 0.0;
+    for (int b = 0; b < m->nbox; ++b) {
+        Box vb = L->boxes[b];
+        const Fab* f = &m->fab[b];
+        for (int k = vb.lo[2]; k <= vb.hi[2]; ++k)
+        for (int j = vb.lo[1]; j <= vb.hi[1]; ++j)
+        for (int i = vb.lo[0]; i <= vb.hi[0]; ++i) {
+            if (covered_by_fine(M, l, i, j, k)) continue;
+            double v = fabs(A(f, i, j, k));
+            if (v > r) r = v;
+        }
+    }
+    return r;
+}
+
+/* MLMGT::computeMLResidual, AMReX_MLMG.H:1632-1648 */
+static void amr_compute_ml_residual(Amr* M, int lmax) {
+    for (int l = lmax; l >= 0; --l) {
+        Solver* S = &M->S[l];
+        amr_solution_residual(M, l, &S->res[0], &S->sol, &S->rhs, 1);
+        if (l < M->nlev - 1) amr_reflux(M, l, &S->res[0]);
+    }
+}
+
+static double amr_ml_norminf(const Amr* M, int lmax, int rhs) {
+    double r = 0.0;
+    for (int l = 0; l <= lmax; ++l) {
+        double v = amr_norminf(M, l, rhs ? &M->S[l].rhs : &M->S[l].res[0]);
+        if (v > r) r = v;
+    }
+    return r;
+}
+
+/* nu1 smoothing sweeps from zero: the mini-cycle of a fine AMR level */
+static void amr_mini_cycle(Amr* M, int l) {
+    Solver* S = &M->S[l];
+    mf_setval(&S->cor[0], 0.0);
+    int skip = 1;
+    for (int i = 0; i < S->o.nu1; ++i) { smooth(S, 0, &S->cor[0], &S->res[0], skip); skip = 0; }
+}
+
+/* MLMGT::oneIter, AMReX_MLMG.H:1227-1293 */
+static void amr_one_iter(Amr* M, int iter) {
+    const int finest = M->nlev - 1;
+    for (int l = finest; l > 0; --l) {
+        Solver* S = &M->S[l];
+        Solver* C = &M->S[l - 1];
+        amr_mini_cycle(M, l);
+        mf_axpy(&S->H.lev[0], &S->sol, 1.0, &S->cor[0], 1);
+        /* computeResWithCrseSolFineCor(l-1, l), AMReX_MLMG.H:1660-1690 */
+        amr_solution_residual(M, l - 1, &C->res[0], &C->sol, &C->rhs, 1);
+        correction_residual(S, 0, &S->rescor[0], &S->cor[0], &S->res[0]);
+        mf_axpy(&S->H.lev[0], &S->res[0], 0, &S->rescor[0], 0);
+        amr_reflux(M, l - 1, &C->res[0]);
+        amr_average_down(M, l - 1, &S->res[0], &C->res[0]);
+        if (l != finest) { MF t = S->cor_hold[0]; S->cor_hold[0] = S->cor[0]; S->cor[0] = t; }
+    }
+    {
+        Solver* S = &M->S[0];
+        if (iter < S->o.max_fmg_iter) fcycle(S); else vcycle(S, 0);
+        mf_axpy(&S->H.lev[0], &S->sol, 1.0, &S->cor[0], 1);
+    }
+    for (int l = 1; l <= finest; ++l) {
+        Solver* S = &M->S[l];
+        const Level* L = &S->H.lev[0];
+        amr_interp_correction(M, l);
+        mf_axpy(L, &S->sol, 1.0, &S->cor[0], 1);
+        if (l != finest) mf_axpy(L, &S->cor_hold[0], 1.0, &S->cor[0], 1);
+        /* computeResWithCrseCorFineCor(l), AMReX_MLMG.H:1693-1715 */
+        amr_correction_residual_inhomog(M, l, &S->rescor[0], &S->cor[0], &S->res[0]);
+        mf_axpy(L, &S->res[0], 0, &S->rescor[0], 0);
+        amr_mini_cycle(M, l);
+        mf_axpy(L, &S->sol, 1.0, &S->cor[0], 1);
+        if (l != finest) mf_axpy(L, &S->cor[0], 1.0, &S->cor_hold[0], 1);
+    }
+    /* averageDownAndSync, AMReX_MLCellLinOp.H:2102-2122 */
+    for (int l = finest; l > 0; --l) amr_average_down(M, l - 1, &M->S[l].sol, &M->S[l - 1].sol);
+}
+
+/* MLMGT::solve, AMReX_MLMG.H:353-541, several AMR levels (refinement ratio 2,
+ * MLPoisson, non-periodic).  P[l] describes AMR level l: its domain
+ * (n = n_0 2^l), boxes, right-hand side over its domain and initial guess
+ * with boundary values in the ghosts (grown domain).  phi_out[l] receives the
+ * level's solution on its boxes' cells (level-domain array). */
+int oracle_solve_amr(int nlev, const OracleProblem* P, const OracleOptions* o, double** phi_out,
+                     OracleResult* R) {
+    if (nlev < 1 || nlev > AMR_MAX) return -1;
+    for (int l = 0; l < nlev; ++l) {
+        if (P[l].is_abec) return -2;
+        for (int d = 0; d < 3; ++d) if (P[l].periodic[d]) return -3;
+    }
+    Amr* M = (Amr*)calloc(1, sizeof(Amr));
+    M->nlev = nlev;
+    for (int l = 0; l < nlev; ++l) {
+        Solver* S = &M->S[l];
+        OracleOptions ol = *o;
+        if (l > 0) ol.max_coarsening_level = 0;
+        setup_ratio(S, &P[l], &ol, l > 0 ? 2 : 1);
+        set_coeffs(S, &P[l]);
+        Hier* H = &S->H;
+        Level* L0 = &H->lev[0];
+        S->bcval.v = P[l].sol; for (int d = 0; d < 3; ++d) S->bcval.n[d] = P[l].n[d];
+        mf_define(&S->sol, L0->nbox, L0->boxes, 1, -1);
+        copy_global_to_mf(L0, &S->sol, P[l].sol, 1, -1);
+        mf_define(&S->rhs, L0->nbox, L0->boxes, 0, -1);
+        copy_global_to_mf(L0, &S->rhs, P[l].rhs, 0, -1);
+        S->volinv0 = 1.0 / (double)bnpts(&L0->domain);
+        S->volinv_bottom = 1.0 / (double)bnpts(&H->lev[H->nlev - 1].domain);
+        for (int q = 0; q < H->nlev; ++q) {
+            Level* L = &H->lev[q];
+            mf_define(&S->cor[q], L->nbox, L->boxes, 1, -1);
+            mf_define(&S->res[q], L->nbox, L->boxes, 0, -1);
+            mf_define(&S->rescor[q], L->nbox, L->boxes, 0, -1);
+            mf_define(&S->cor_hold[q], L->nbox, L->boxes, 1, -1);
+            mf_setval(&S->cor[q], 0.0);
+            mf_setval(&S->res[q], 0.0);
+            mf_setval(&S->rescor[q], 0.0);
+            mf_setval(&S->cor_hold[q], 0.0);
+        }
+        if (l > 0) {
+            M->bsol[l] = (Fab*)calloc((size_t)6 * L0->nbox, sizeof(Fab));
+            M->bcor[l] = (Fab*)calloc((size_t)6 * L0->nbox, sizeof(Fab));
+        }
+    }
+    Solver* S0 = &M->S[0];
+    S0->singular = is_singular(S0);
+    const int finest = nlev - 1;
+    /* prepareForSolve: averageDownSolutionRHS, AMReX_MLMG.H:1025-1028 */
+    for (int l = finest; l > 0; --l) {
+        amr_average_down(M, l - 1, &M->S[l].sol, &M->S[l - 1].sol);
+        amr_average_down(M, l - 1, &M->S[l].rhs, &M->S[l - 1].rhs);
+    }
+    if (S0->singular) make_solvable(S0, 0, &S0->rhs);
+    amr_compute_ml_residual(M, finest);
+    const double resnorm0 = amr_ml_norminf(M, finest, 0);
+    const double rhsnorm0 = amr_ml_norminf(M, finest, 1);
+    const double max_norm = (rhsnorm0 >= resnorm0) ? rhsnorm0 : resnorm0;
+    const double tr = o->tol_rel > 1.e-16 ? o->tol_rel : 1.e-16;
+    const double res_target = o->tol_abs > tr * max_norm ? o->tol_abs : tr * max_norm;
+    R->init_resid = resnorm0; R->rhs_norm = rhsnorm0; R->niters = 0; R->status = 0;
+    double composite = resnorm0;
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    if (resnorm0 > res_target) {
+        int converged = 0;
+        const int niters = o->fixed_iter ? o->fixed_iter : o->max_iter;
+        for (int iter = 0; iter < niters; ++iter) {
+            if (S0->singular) make_solvable(S0, 0, &S0->res[0]);
+            amr_one_iter(M, iter);
+            /* computeResidual(finest): no reflux, boundary data from the coarser solution */
+            Solver* Sf = &M->S[finest];
+            amr_solution_residual(M, finest, &Sf->res[0], &Sf->sol, &Sf->rhs, 1);
+            const double fine = amr_norminf(M, finest, &Sf->res[0]);
+            if (R->niters < ORACLE_MAX_HIST) R->history[R->niters] = fine;
+            R->niters++;
+            composite = fine;
+            const int fine_converged = fine <= res_target;
+            if (nlev == 1 && fine_converged) {
+                converged = 1;
+            } else if (fine_converged) {
+                amr_compute_ml_residual(M, finest - 1);
+                const double crse = amr_ml_norminf(M, finest - 1, 0);
+                converged = crse <= res_target;
+                composite = fine > crse ? fine : crse;
+            }
+            if (converged) break;
+            if (composite > 1.e20 * max_norm) { R->status = -2; break; }
+        }
+        if (!converged && o->fixed_iter == 0 && R->status == 0) R->status = 1;
+    }
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    R->iter_seconds = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+    R->final_resid = composite;
+    R->nlev = S0->H.nlev;
+    R->ncg = S0->ncg;
+    for (int q = 0; q < S0->ncg && q < ORACLE_MAX_HIST; ++q) R->cg_iters[q] = S0->cg_log[q];
+    for (int l = 0; l < nlev; ++l) {
+        copy_mf_to_global(&M->S[l].H.lev[0], &M->S[l].sol, phi_out[l]);
+        if (l > 0) {
+            const int nf = 6 * M->S[l].H.lev[0].nbox;
+            for (int q = 0; q < nf; ++q) { free(M->bsol[l][q].p); free(M->bcor[l][q].p); }
+            free(M->bsol[l]); free(M->bcor[l]);
+        }
+        free_solver(&M->S[l]);
+    }
+    free(M);
+    return R->status;
 }

@@ -51,6 +51,11 @@ int oracle_apply(const OracleProblem* P, const OracleOptions* o, double* out);
 /* mode 0: getGradSolution, mode 1: getFluxes; global face arrays */
 int oracle_fluxes(const OracleProblem* P, const OracleOptions* o, int mode, double* fx, double* fy, double* fz);
 int oracle_solve(const OracleProblem* P, const OracleOptions* o, double* phi_out, OracleResult* R);
+/* composite solve over nlev AMR levels (ratio 2, MLPoisson): P[l] is level l
+ * (n = n_0 2^l, its boxes, rhs over its domain, initial guess + boundary
+ * values over its grown domain); phi_out[l] gets level l's solution */
+int oracle_solve_amr(int nlev, const OracleProblem* P, const OracleOptions* o, double** phi_out,
+                     OracleResult* R);
 
 #ifdef __cplusplus
 }

@@ -74,6 +74,7 @@ def lib():
         _lib.oracle_fluxes.argtypes = [P(Problem), P(Options), ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double),
                                        P(ctypes.c_double)]
         _lib.oracle_solve.argtypes = [P(Problem), P(Options), P(ctypes.c_double), P(Result)]
+        _lib.oracle_solve_amr.argtypes = [ctypes.c_int, P(Problem), P(Options), P(P(ctypes.c_double)), P(Result)]
     return _lib
 
 
@@ -188,3 +189,34 @@ def solve(case, arrays):
                 history=list(r.history[:min(r.niters, MAX_HIST)]),
                 cg_iters=list(r.cg_iters[:min(r.ncg, MAX_HIST)]))
     return phi, info
+
+
+def solve_amr(case, levels):
+    """Composite solve over AMR levels (ratio 2, MLPoisson).  ``case`` holds
+    the level-0 settings (n, bc, solver options); ``levels`` is a list of
+    dicts with "boxes", "rhs" (level domain, z-major) and optionally "sol"
+    (grown level domain: initial guess + boundary values; zero by default).
+    Returns (list of level-domain phi arrays, info dict)."""
+    nlev = len(levels)
+    probs = (Problem * nlev)()
+    keep = []
+    phis = []
+    for lev, L in enumerate(levels):
+        n = [v << lev for v in case["n"]]
+        c = dict(case, n=tuple(n), boxes=L["boxes"])
+        sol = L.get("sol")
+        if sol is None:
+            sol = np.zeros((n[2] + 2, n[1] + 2, n[0] + 2))
+        p, k = make_problem(c, {"sol": sol, "rhs": L["rhs"]})
+        keep.append(k)
+        probs[lev] = p
+        phis.append(np.zeros((n[2], n[1], n[0])))
+    ptrs = (ctypes.POINTER(ctypes.c_double) * nlev)(*[_dp(a) for a in phis])
+    o = make_options(case)
+    r = Result()
+    lib().oracle_solve_amr(nlev, probs, ctypes.byref(o), ptrs, ctypes.byref(r))
+    info = dict(status=r.status, niters=r.niters, nlev=r.nlev, init_resid=r.init_resid, rhs_norm=r.rhs_norm,
+                final_resid=r.final_resid, iter_seconds=r.iter_seconds,
+                history=list(r.history[:min(r.niters, MAX_HIST)]),
+                cg_iters=list(r.cg_iters[:min(r.ncg, MAX_HIST)]))
+    return phis, info

@@ -1,0 +1,63 @@
+"""The oracle's AMR composite solve (MLMG over several AMR levels, refinement
+ratio 2, MLPoisson) against the reference's own composite solves on
+AmrMesh-generated grids (tests/golden/amrsolve_*.npz)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tests.golden import amr_cases as ac
+
+
+def oracle_case(case):
+    n = case["n"]
+    return dict(n=(n, n, n), tol_rel=case.get("tol_rel", 1e-10), tol_abs=0.0,
+                agg_grid_size=case.get("agg_grid_size", 32), con_grid_size=case.get("con_grid_size", 32))
+
+
+def levels_of(case, grids):
+    return [dict(boxes=grids[lev], rhs=ac.level_rhs(case, lev)) for lev in range(len(grids))]
+
+
+@pytest.mark.parametrize("name", ["c2_n16_2lev", "c2_n32"])
+def test_oracle_amr_matches_reference(name):
+    g = ac.load("amrsolve", name)
+    case, grids, ref = g["case"], g["grids"], g["result"]
+    phis, info = oracle.solve_amr(oracle_case(case), levels_of(case, grids))
+    assert info["status"] == 0
+    assert info["niters"] == ref["niters"]
+    assert info["cg_iters"] == ref["cg_iters"]
+    assert info["init_resid"] == pytest.approx(ref["init_resid"], rel=1e-13)
+    assert info["rhs_norm"] == pytest.approx(ref["rhs_norm"], rel=1e-13)
+    # residuals near 1e-10 carry roundoff from the order of the flux-register sums
+    np.testing.assert_allclose(info["history"], ref["history"], rtol=1e-4, atol=1e-14 * ref["rhs_norm"])
+    for lev in range(len(grids)):
+        want = g[f"phi_l{lev}"]
+        got = ac.pack_boxes(phis[lev], grids[lev])
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-12 * np.abs(want).max())
+
+
+def test_amr_grids_are_properly_nested():
+    """Every fixture's finer boxes sit inside the next coarser level grown by
+    one coarse cell (AmrMesh proper nesting), the premise of the oracle's and
+    the engine's coarse/fine boundary interpolation."""
+    for name in ("c2", "c2_n32", "c2_n16_2lev"):
+        g = ac.load("amrgrids", name)
+        n = g["case"]["n"]
+        grids = g["grids"]
+        for lev in range(1, len(grids)):
+            m = n << (lev - 1)
+            cov = np.zeros((m + 2,) * 3, dtype=bool)
+            for b in grids[lev - 1]:
+                cov[b[2] + 1:b[5] + 2, b[1] + 1:b[4] + 2, b[0] + 1:b[3] + 2] = True
+            # cells outside the domain count as covered
+            cov[0, :, :] = cov[-1, :, :] = True
+            cov[:, 0, :] = cov[:, -1, :] = True
+            cov[:, :, 0] = cov[:, :, -1] = True
+            for b in grids[lev]:
+                lo = [v // 2 for v in b[:3]]
+                hi = [v // 2 for v in b[3:]]
+                assert all(v % 2 == 0 for v in b[:3]) and all(v % 2 == 1 for v in b[3:])
+                blk = cov[lo[2]:hi[2] + 3, lo[1]:hi[1] + 3, lo[0]:hi[0] + 3]
+                assert blk.all(), (name, lev, b)
