@@ -247,6 +247,9 @@ class _LinOp:
     def NMGLevels(self, amrlev=0):
         return capi.lib().mlmg_linop_num_mg_levels(self._h)
 
+    def NAMRLevels(self):
+        return capi.lib().mlmg_linop_num_amr_levels(self._h)
+
 
 class MLPoisson(_LinOp):
     _ctor = "mlmg_linop_new_poisson"
@@ -325,7 +328,14 @@ class MLMG:
         sols = sol if isinstance(sol, (list, tuple)) else [sol]
         rhss = rhs if isinstance(rhs, (list, tuple)) else [rhs]
         r = ctypes.c_double()
-        rc = capi.lib().mlmg_solve(self._h, sols[0]._h, rhss[0]._h, float(tol_rel), float(tol_abs), ctypes.byref(r))
+        if len(sols) > 1:
+            # composite solve over the AMR levels (MLMG::solve with one MultiFab per level)
+            S = (ctypes.c_void_p * len(sols))(*[m._h for m in sols])
+            R = (ctypes.c_void_p * len(rhss))(*[m._h for m in rhss])
+            rc = capi.lib().mlmg_solve_levels(self._h, S, R, float(tol_rel), float(tol_abs), ctypes.byref(r))
+        else:
+            rc = capi.lib().mlmg_solve(self._h, sols[0]._h, rhss[0]._h, float(tol_rel), float(tol_abs),
+                                       ctypes.byref(r))
         if rc != 0:
             raise MLMGError(rc, capi.lib().mlmg_last_error().decode())
         return r.value

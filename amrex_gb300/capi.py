@@ -63,6 +63,7 @@ SIGNATURES = {
     "mlmg_abeclap_set_bcoeffs": (c_int, [c_void_p, c_int, P(c_void_p)]),
     "mlmg_abeclap_set_bcoeffs_const": (c_int, [c_void_p, c_int, c_double]),
     "mlmg_linop_num_mg_levels": (c_int, [c_void_p]),
+    "mlmg_linop_num_amr_levels": (c_int, [c_void_p]),
     "mlmg_new": (c_int, [c_void_p, P(c_void_p)]),
     "mlmg_delete": (c_int, [c_void_p]),
     "mlmg_set_verbose": (c_int, [c_void_p, c_int]),
@@ -85,6 +86,7 @@ SIGNATURES = {
     "mlmg_set_option": (c_int, [c_void_p, ctypes.c_char_p, c_double]),
     "mlmg_get_smoother_stats": (c_int, [c_void_p, P(c_double), P(ctypes.c_longlong), P(c_double), c_int]),
     "mlmg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_double, P(c_double)]),
+    "mlmg_solve_levels": (c_int, [c_void_p, P(c_void_p), P(c_void_p), c_double, c_double, P(c_double)]),
     "mlmg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),
     "mlmg_get_fluxes": (c_int, [c_void_p, c_void_p, P(c_void_p)]),
     "mlmg_get_grad_solution": (c_int, [c_void_p, c_void_p, P(c_void_p)]),

@@ -44,7 +44,7 @@ __device__ __forceinline__ double ghost_weight (const PatchDesc& P, int f, long 
 // For every periodic ghost cell (a copy tag with a non-zero shift) this puts
 // the face coefficient that the image cell's row uses for the same coupling
 // at the ghost's index.  ABec only.
-__global__ void k_partner_faces (DevLevel L, GhostWork W, const double* __restrict__ bx,
+static __global__ void k_partner_faces (DevLevel L, GhostWork W, const double* __restrict__ bx,
                                  const double* __restrict__ by, const double* __restrict__ bz,
                                  double* __restrict__ out)
 {
@@ -157,7 +157,7 @@ k_residual_transpose (DevLevel L, Subset S, TO* __restrict__ r, const double* __
 // coefficients; a face shared by two boxes gets its full (two-row) value in
 // both boxes' copies.
 // dJ/da = -alpha * lam * phi per cell.  MLABecLaplacian only.
-__global__ void __launch_bounds__(TILE_THREADS)
+static __global__ void __launch_bounds__(TILE_THREADS)
 k_face_grad (DevLevel L, Subset S, const double* __restrict__ phi, const double* __restrict__ lam,
              double* __restrict__ gx, double* __restrict__ gy, double* __restrict__ gz, double* __restrict__ ga)
 {

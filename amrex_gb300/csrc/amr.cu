@@ -1,0 +1,737 @@
+// AMR composite MLMG (MLMGT::solve over several AMR levels, refinement ratio
+// 2, MLPoisson): host orchestration of MLMGT::oneIter (AMReX_MLMG.H:1227-1293)
+// over one engine per AMR level, with the coarse/fine kernels of
+// amr_kernels.cuh.  FP64 throughout, or (precision 1) FP32 corrections --
+// the V-cycle of AMR level 0, the fine levels' smoothing sweeps and the
+// correction residuals -- inside the FP64 composite residual, reflux,
+// average-down, solution update and norms.
+#include "amr.hpp"
+#include "engine_impl.cuh"
+#include "amr_kernels.cuh"
+
+#include <cmath>
+#include <map>
+
+namespace mlmg {
+
+namespace {
+
+template <typename T>
+void upload_or_keep (DevBuf<T>& b, const std::vector<T>& v, cudaStream_t st)
+{
+    if (!v.empty()) { b.upload(v, st); }
+}
+
+unsigned blocks_for (long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+} // namespace
+
+// One AMR level: its engine and, towards the next coarser level (l > 0) or
+// the next finer one (l < finest), the coupling tables.
+struct AmrLevelData {
+    std::unique_ptr<Engine> eng;
+    Engine::Impl* I = nullptr;
+    // -- as the fine level of level l-1 --
+    std::vector<PatchDesc> h_cfd;           // coarse buffer layout per fine patch (coarsened patch + 1 ghost)
+    DevBuf<PatchDesc> cfd;
+    long long cf_n = 0;
+    DevBuf<double> cf64;
+    DevBuf<float> cf32;
+    DevBuf<CopyTag> gtags;                  // gather: dst fine patch, src coarse patch
+    DevBuf<long long> gstart;
+    int ngtag = 0;
+    long long ngcell = 0;
+    DevBuf<int2> cff;                       // coarse/fine (patch, face) pairs
+    DevBuf<long long> cffstart;
+    GhostWork cfw{};                        // face-cell walk over them (no copy tags)
+    DevBuf<int8_t> bflags;                  // per Dirichlet-value slot: BF_* bits
+    DevBuf<double> bcor;                    // boundary values of the correction (physical slots 0)
+    DevBuf<double> hold64;                  // cor_hold of the AMR level
+    DevBuf<float> hold32;
+    void* cor_p = nullptr;                  // the level's correction buffer (swapped with the hold)
+    void* hold_p = nullptr;
+    // -- as the coarse level of level l+1 --
+    DevBuf<CopyTag> atags;                  // average-down: dst coarse patch, src fine patch
+    DevBuf<long long> astart;
+    int natag = 0;
+    long long nacell = 0;
+    DevBuf<int8_t> covered;                 // per element: 1 where the finer level covers the cell
+    DevBuf<RefluxCell> rcells;
+    DevBuf<RefluxFace> rfaces;
+    int nrcell = 0;
+    RefluxParams rprm{};
+};
+
+struct AmrEngine::Impl {
+    AmrEngine& A;
+    AmrProblem prob;
+    std::vector<AmrLevelData> lev;
+    int nl = 0;
+    int own_launches = 0;
+    PinnedBuf<double> h_norm;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_launches = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+    explicit Impl (AmrEngine& a) : A(a) {}
+    ~Impl () {
+        if (graph_exec) { cudaGraphExecDestroy(graph_exec); }
+        if (ev0) { cudaEventDestroy(ev0); }
+        if (ev1) { cudaEventDestroy(ev1); }
+    }
+    cudaStream_t st () const { return A.m_stream; }
+    bool mixed () const { return A.m_opt.precision == 1; }
+    void launched (int n = 1) { own_launches += n; }
+    LevelData& L (int l) { return lev[l].I->lev[0]; }
+
+    void build ();
+    void build_fine_tables (int l);
+    void build_coarse_tables (int c);
+
+    // operations
+    void solution_residual (int l, bool update);
+    void reflux (int c);
+    void avgdown (int c, const double* fine, double* crse);
+    template <typename T> void gather (int l, const T* crse);
+    template <typename T> T* cor (int l);
+    template <typename T> T* hold (int l);
+    template <typename T> T* res_t (int l);
+    template <typename T> T* rescor_t (int l);
+    template <typename T> void mini_cycle (int l, bool convert_res);
+    template <typename T> void correction_residual (int l, bool inhomog);
+    template <typename T> void one_iter (int iter);
+    void norm_start (int l, const double* x, bool masked, int slot);
+    void fine_residual_and_norm ();
+};
+
+template <> double* AmrEngine::Impl::cor<double> (int l) { return (double*)lev[l].cor_p; }
+template <> float* AmrEngine::Impl::cor<float> (int l) { return (float*)lev[l].cor_p; }
+template <> double* AmrEngine::Impl::hold<double> (int l) { return (double*)lev[l].hold_p; }
+template <> float* AmrEngine::Impl::hold<float> (int l) { return (float*)lev[l].hold_p; }
+template <> double* AmrEngine::Impl::res_t<double> (int l) { return L(l).res.p; }
+template <> float* AmrEngine::Impl::res_t<float> (int l) { return L(l).res32.p; }
+template <> double* AmrEngine::Impl::rescor_t<double> (int l) { return L(l).rescor.p; }
+template <> float* AmrEngine::Impl::rescor_t<float> (int l) { return L(l).rescor32.p; }
+
+// ------------------------------------------------------------------ build --
+void AmrEngine::Impl::build ()
+{
+    nl = (int)prob.levels.size();
+    MLMG_REQUIRE(nl >= 2 && nl <= 8, ERR_ARGS, "an AMR solve needs 2 to 8 levels");
+    for (int d = 0; d < 3; ++d) {
+        MLMG_REQUIRE(!prob.geom.periodic[d], ERR_UNSUPPORTED, "AMR composite solves support non-periodic domains only");
+    }
+    lev.resize(nl);
+    for (int l = 0; l < nl; ++l) {
+        SolveProblem pr;
+        SolveSpec& S = pr.spec;
+        S.geom = prob.geom;
+        S.geom.domain = refine(prob.geom.domain, 1 << l);
+        if (l == 0) {
+            S.levels = define_grids(S.geom, prob.levels[0].boxes, prob.info);
+        } else {
+            LevelGrids G;
+            G.geom = S.geom;
+            G.boxes = prob.levels[l].boxes;
+            G.derived = 1;
+            S.levels.push_back(G);
+            for (const auto& b : G.boxes) {
+                MLMG_REQUIRE(S.geom.domain.contains(b.lo[0], b.lo[1], b.lo[2]) &&
+                             S.geom.domain.contains(b.hi[0], b.hi[1], b.hi[2]), ERR_ARGS,
+                             "AMR level box outside its domain");
+                MLMG_REQUIRE(refine(coarsen(b, 2), 2) == b, ERR_ARGS,
+                             "AMR level boxes must be coarsenable by the refinement ratio 2");
+            }
+        }
+        for (int d = 0; d < 3; ++d) {
+            S.lobc[d] = prob.lobc[d]; S.hibc[d] = prob.hibc[d];
+            S.dx0[d] = (S.geom.prob_hi[d] - S.geom.prob_lo[d]) / (double)S.geom.domain.len(d);
+        }
+        S.maxorder = prob.maxorder;
+        S.is_abec = 0; S.alpha = 0.0; S.beta = 1.0;
+        S.crse_ratio = (l > 0) ? 2 : 1;
+        S.amr_fine = (l > 0) ? 1 : 0;
+        pr.boxes = prob.levels[l].boxes;
+        pr.levelbc = prob.levels[l].levelbc;
+        EngineOptions o = A.m_opt;
+        o.max_fmg_iter = 0;
+        o.transpose = 0;
+        std::vector<SolveProblem> probs{pr};
+        lev[l].eng = std::make_unique<Engine>(std::move(probs), o, st());
+        lev[l].I = &lev[l].eng->impl();
+    }
+    // proper nesting: a fine box coarsened and grown by one lies in the
+    // coarser level (or outside the domain), which the coarse/fine
+    // interpolation, the reflux and the correction interpolation rely on
+    for (int l = 1; l < nl; ++l) {
+        const BoxLocator cl(prob.levels[l - 1].boxes);
+        const Box3 cdom = refine(prob.geom.domain, 1 << (l - 1));
+        for (const auto& b : prob.levels[l].boxes) {
+            const Box3 g = grow(coarsen(b, 2), 1);
+            for (int k = g.lo[2]; k <= g.hi[2]; ++k)
+            for (int j = g.lo[1]; j <= g.hi[1]; ++j)
+            for (int i = g.lo[0]; i <= g.hi[0]; ++i) {
+                if (!cdom.contains(i, j, k)) { continue; }
+                MLMG_REQUIRE(cl.find(i, j, k) >= 0, ERR_ARGS,
+                             "AMR levels are not properly nested (a coarsened fine box grown by one leaves the coarser level)");
+            }
+        }
+    }
+    for (int l = 0; l < nl; ++l) {
+        AmrLevelData& D = lev[l];
+        LevelData& Ld = L(l);
+        const size_t n = (size_t)Ld.meta.nelem;
+        if (mixed()) {
+            D.cor_p = Ld.cor32.p;
+            if (l > 0 && l < nl - 1) { D.hold32.alloc(n); D.hold32.zero(st()); D.hold_p = D.hold32.p; }
+        } else {
+            D.cor_p = Ld.cor.p;
+            if (l > 0 && l < nl - 1) { D.hold64.alloc(n); D.hold64.zero(st()); D.hold_p = D.hold64.p; }
+        }
+        if (l > 0) { build_fine_tables(l); }
+        if (l < nl - 1) { build_coarse_tables(l); }
+    }
+    h_norm.alloc(4 * (size_t)nl + 4);
+    MLMG_CUDA_CHECK(cudaEventCreate(&ev0));
+    MLMG_CUDA_CHECK(cudaEventCreate(&ev1));
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st()));
+}
+
+void AmrEngine::Impl::build_fine_tables (int l)
+{
+    AmrLevelData& D = lev[l];
+    const PatchLevel& Mf = L(l).meta;
+    const PatchLevel& Mc = L(l - 1).meta;
+    // coarse buffers: the coarsened fine patch and one ghost layer
+    long long cursor = 0;
+    D.h_cfd.clear();
+    for (const PatchDesc& P : Mf.patches) {
+        Box3 pb;
+        for (int d = 0; d < 3; ++d) { pb.lo[d] = P.lo[d]; pb.hi[d] = P.hi[d]; }
+        const Box3 cb = coarsen(pb, 2);
+        PatchDesc G{};
+        for (int d = 0; d < 3; ++d) { G.lo[d] = cb.lo[d]; G.hi[d] = cb.hi[d]; }
+        G.sx = cb.len(0) + 2;
+        G.sxy = (long long)G.sx * (cb.len(1) + 2);
+        G.base = cursor + G.sxy + G.sx + 1;
+        cursor += G.sxy * (cb.len(2) + 2);
+        D.h_cfd.push_back(G);
+    }
+    D.cf_n = std::max<long long>(cursor, 1);
+    D.cfd.upload(D.h_cfd, st());
+    D.cf64.alloc((size_t)D.cf_n);
+    if (mixed()) { D.cf32.alloc((size_t)D.cf_n); }
+    // gather tags: every coarse patch's valid cells inside each grown buffer
+    std::vector<CopyTag> tags;
+    std::vector<long long> start{0};
+    for (int p = 0; p < (int)Mf.patches.size(); ++p) {
+        Box3 g;
+        for (int d = 0; d < 3; ++d) { g.lo[d] = D.h_cfd[p].lo[d] - 1; g.hi[d] = D.h_cfd[p].hi[d] + 1; }
+        for (int cp = 0; cp < (int)Mc.patches.size(); ++cp) {
+            Box3 cb;
+            for (int d = 0; d < 3; ++d) { cb.lo[d] = Mc.patches[cp].lo[d]; cb.hi[d] = Mc.patches[cp].hi[d]; }
+            const Box3 is = intersect(g, cb);
+            if (!is.ok()) { continue; }
+            CopyTag t{};
+            t.dst = p; t.src = cp; t.box = is;
+            tags.push_back(t);
+            start.push_back(start.back() + is.npts());
+        }
+    }
+    D.ngtag = (int)tags.size();
+    D.ngcell = start.back();
+    upload_or_keep(D.gtags, tags, st());
+    D.gstart.upload(start, st());
+    // coarse/fine faces and the neighbourhood flags of their ghost cells
+    const Box3 fdom = refine(prob.geom.domain, 1 << l);
+    const BoxLocator floc(prob.levels[l].boxes);
+    auto notcov = [&] (int i, int j, int k) { return fdom.contains(i, j, k) && floc.find(i, j, k) < 0; };
+    std::vector<int8_t> flags(L(l).bcval.n, 0);
+    std::vector<int2> faces;
+    std::vector<long long> fstart{0};
+    for (int p = 0; p < (int)Mf.patches.size(); ++p) {
+        const PatchDesc& P = Mf.patches[p];
+        for (int f = 0; f < 6; ++f) {
+            const FaceBC& F = P.face[f];
+            if (F.on_domain) { continue; }      // physical face: the level's own BC values
+            const int d = f % 3;
+            const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
+            const int g = (f >= 3) ? P.hi[d] + 1 : P.lo[d] - 1;
+            const int n1 = P.hi[t1] - P.lo[t1] + 1, n2 = P.hi[t2] - P.lo[t2] + 1;
+            faces.push_back(make_int2(p, f));
+            fstart.push_back(fstart.back() + (long long)n1 * n2);
+            for (int v2 = 0; v2 < n2; ++v2)
+            for (int v1 = 0; v1 < n1; ++v1) {
+                int c[3];
+                c[d] = g; c[t1] = P.lo[t1] + v1; c[t2] = P.lo[t2] + v2;
+                int fl = 0;
+                if (notcov(c[0], c[1], c[2])) {
+                    fl |= BF_SELF;
+                    auto nc_at = [&] (int a1, int a2) {
+                        int e[3] = {c[0], c[1], c[2]};
+                        e[t1] += a1; e[t2] += a2;
+                        return notcov(e[0], e[1], e[2]);
+                    };
+                    if (nc_at(-2, 0)) { fl |= BF_T1LO; }
+                    if (nc_at(2, 0)) { fl |= BF_T1HI; }
+                    if (nc_at(0, -2)) { fl |= BF_T2LO; }
+                    if (nc_at(0, 2)) { fl |= BF_T2HI; }
+                    if (nc_at(-2, -2) && nc_at(2, -2) && nc_at(-2, 2) && nc_at(2, 2)) { fl |= BF_CROSS; }
+                }
+                flags[(size_t)(F.bcval_off + (long long)v2 * n1 + v1)] = (int8_t)fl;
+            }
+        }
+    }
+    upload_or_keep(D.cff, faces, st());
+    D.cffstart.upload(fstart, st());
+    D.cfw = GhostWork{D.cff.p, D.cffstart.p, (int)faces.size(), nullptr, nullptr, 0, fstart.back(), 0};
+    D.bflags.upload(flags, st());
+    D.bcor.alloc(L(l).bcval.n);
+    D.bcor.zero(st());
+}
+
+void AmrEngine::Impl::build_coarse_tables (int c)
+{
+    AmrLevelData& D = lev[c];
+    const PatchLevel& Mc = L(c).meta;
+    const PatchLevel& Mf = L(c + 1).meta;
+    auto pbox = [] (const PatchDesc& P) {
+        Box3 b;
+        for (int d = 0; d < 3; ++d) { b.lo[d] = P.lo[d]; b.hi[d] = P.hi[d]; }
+        return b;
+    };
+    // average-down tags and the covered mask
+    std::vector<CopyTag> tags;
+    std::vector<long long> start{0};
+    std::vector<int8_t> cov((size_t)Mc.nelem, 0);
+    std::vector<Box3> cfboxes;
+    for (int fp = 0; fp < (int)Mf.patches.size(); ++fp) {
+        const Box3 cb = coarsen(pbox(Mf.patches[fp]), 2);
+        cfboxes.push_back(cb);
+        for (int cp = 0; cp < (int)Mc.patches.size(); ++cp) {
+            const Box3 is = intersect(cb, pbox(Mc.patches[cp]));
+            if (!is.ok()) { continue; }
+            CopyTag t{};
+            t.dst = cp; t.src = fp; t.box = is;
+            tags.push_back(t);
+            start.push_back(start.back() + is.npts());
+            const PatchDesc& C = Mc.patches[cp];
+            for (int k = is.lo[2]; k <= is.hi[2]; ++k)
+            for (int j = is.lo[1]; j <= is.hi[1]; ++j)
+            for (int i = is.lo[0]; i <= is.hi[0]; ++i) { cov[(size_t)cidx(C, i, j, k)] = 1; }
+        }
+    }
+    D.natag = (int)tags.size();
+    D.nacell = start.back();
+    upload_or_keep(D.atags, tags, st());
+    D.astart.upload(start, st());
+    D.covered.upload(cov, st());
+    // reflux: every (uncovered coarse cell, face) pair next to a coarsened fine patch
+    std::vector<Box3> cpboxes;
+    for (const auto& P : Mc.patches) { cpboxes.push_back(pbox(P)); }
+    const BoxLocator cfl(cfboxes), cpl(cpboxes);
+    const Box3 cdom = refine(prob.geom.domain, 1 << c);
+    struct E { long long q; int key; RefluxFace f; };
+    std::vector<E> ent;
+    for (int fp = 0; fp < (int)Mf.patches.size(); ++fp) {
+        const Box3& cb = cfboxes[fp];
+        const PatchDesc& F = Mf.patches[fp];
+        for (int f = 0; f < 6; ++f) {
+            const int d = f % 3;
+            Box3 ab = cb;
+            if (f >= 3) { ab.lo[d] = ab.hi[d] = cb.hi[d] + 1; } else { ab.lo[d] = ab.hi[d] = cb.lo[d] - 1; }
+            const int side = (f < 3) ? 1 : 0;     // the coarsened patch lies at +d of a cell below its low face
+            for (int k = ab.lo[2]; k <= ab.hi[2]; ++k)
+            for (int j = ab.lo[1]; j <= ab.hi[1]; ++j)
+            for (int i = ab.lo[0]; i <= ab.hi[0]; ++i) {
+                if (!cdom.contains(i, j, k) || cfl.find(i, j, k) >= 0) { continue; }
+                const int cp = cpl.find(i, j, k);
+                int n[3] = {i, j, k};
+                n[d] += side ? 1 : -1;
+                const int cpn = cpl.find(n[0], n[1], n[2]);
+                MLMG_REQUIRE(cp >= 0 && cpn >= 0, ERR_ARGS, "AMR levels are not properly nested");
+                int fi[3] = {2 * i, 2 * j, 2 * k};
+                fi[d] = side ? 2 * n[d] : 2 * n[d] + 1;
+                E e;
+                e.q = cidx(Mc.patches[cp], i, j, k);
+                e.key = 2 * d + side;
+                e.f.qn = cidx(Mc.patches[cpn], n[0], n[1], n[2]);
+                e.f.qf = cidx(F, fi[0], fi[1], fi[2]);
+                e.f.fp = fp;
+                e.f.dir = d;
+                e.f.side = side;
+                ent.push_back(e);
+            }
+        }
+    }
+    std::sort(ent.begin(), ent.end(), [] (const E& a, const E& b) { return a.q != b.q ? a.q < b.q : a.key < b.key; });
+    std::vector<RefluxCell> cells;
+    std::vector<RefluxFace> rf;
+    for (size_t e = 0; e < ent.size(); ++e) {
+        if (cells.empty() || cells.back().q != ent[e].q) { cells.push_back(RefluxCell{ent[e].q, (int)e, 0}); }
+        cells.back().ne++;
+        rf.push_back(ent[e].f);
+    }
+    D.nrcell = (int)cells.size();
+    upload_or_keep(D.rcells, cells, st());
+    upload_or_keep(D.rfaces, rf, st());
+    for (int d = 0; d < 3; ++d) {
+        D.rprm.dxinv_c[d] = Mc.patches[0].dxinv[d];
+        D.rprm.dxinv_f[d] = Mf.patches[0].dxinv[d];
+    }
+}
+
+// ------------------------------------------------------------- operations --
+template <> void AmrEngine::Impl::gather<double> (int l, const double* crse)
+{
+    AmrLevelData& D = lev[l];
+    MLMG_CUDA_CHECK(cudaMemsetAsync(D.cf64.p, 0, sizeof(double) * (size_t)D.cf_n, st()));
+    if (D.ngcell > 0) {
+        k_amr_gather<double><<<blocks_for(D.ngcell, 256), 256, 0, st()>>>(L(l - 1).dl, D.cfd.p, D.gtags.p, D.gstart.p,
+                                                                         D.ngtag, D.ngcell, crse, D.cf64.p);
+        launched();
+    }
+}
+
+template <> void AmrEngine::Impl::gather<float> (int l, const float* crse)
+{
+    AmrLevelData& D = lev[l];
+    MLMG_CUDA_CHECK(cudaMemsetAsync(D.cf32.p, 0, sizeof(float) * (size_t)D.cf_n, st()));
+    if (D.ngcell > 0) {
+        k_amr_gather<float><<<blocks_for(D.ngcell, 256), 256, 0, st()>>>(L(l - 1).dl, D.cfd.p, D.gtags.p, D.gstart.p,
+                                                                        D.ngtag, D.ngcell, crse, D.cf32.p);
+        launched();
+    }
+}
+
+// MLCellLinOpT::solutionResidual (AMReX_MLCellLinOp.H:1219-1236); on a fine
+// level with update, the boundary values are first refreshed from the
+// coarser level's solution (updateSolBC, :651-664)
+void AmrEngine::Impl::solution_residual (int l, bool update)
+{
+    LevelData& Ld = L(l);
+    AmrLevelData& D = lev[l];
+    const double* bcv = nullptr;
+    if (l > 0) {
+        if (update) {
+            gather<double>(l, L(l - 1).sol.p);
+            if (D.cfw.nfacecells > 0) {
+                k_amr_bndry<double><<<blocks_for(D.cfw.nfacecells, 256), 256, 0, st()>>>(Ld.dl, D.cfw, D.cfd.p,
+                    D.cf64.p, D.bflags.p, Ld.bcval.p);
+                launched();
+            }
+        }
+        bcv = Ld.bcval.p;
+    }
+    D.I->ghost<double>(0, Ld.sol.p, true, true, bcv);
+    k_residual<double, double, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res.p, Ld.sol.p,
+        Ld.rhs.p, nullptr, nullptr, nullptr, nullptr, nullptr);
+    launched();
+}
+
+// MLCellLinOpT::reflux (AMReX_MLCellLinOp.H:1272-1346) into res of level c
+void AmrEngine::Impl::reflux (int c)
+{
+    LevelData& Lf = L(c + 1);
+    LevelData& Lc = L(c);
+    AmrLevelData& D = lev[c];
+    lev[c + 1].I->ghost<double>(0, Lf.sol.p, true, true, Lf.bcval.p);
+    if (D.nrcell > 0) {
+        k_amr_reflux<<<blocks_for(D.nrcell, 128), 128, 0, st()>>>(Lf.dl, D.rcells.p, D.rfaces.p, D.nrcell, D.rprm,
+                                                                  Lc.sol.p, Lf.sol.p, Lc.res.p);
+        launched();
+    }
+}
+
+void AmrEngine::Impl::avgdown (int c, const double* fine, double* crse)
+{
+    AmrLevelData& D = lev[c];
+    if (D.nacell == 0) { return; }
+    k_amr_avgdown<double, double><<<blocks_for(D.nacell, 256), 256, 0, st()>>>(L(c).dl, L(c + 1).dl, D.atags.p,
+        D.astart.p, D.natag, D.nacell, fine, crse);
+    launched();
+}
+
+// the mini-cycle of a fine AMR level (mgVcycle with one MG level,
+// AMReX_MLMG.H:1306-1415): nu1 smoothing sweeps from zero
+template <typename T>
+void AmrEngine::Impl::mini_cycle (int l, bool convert_res)
+{
+    LevelData& Ld = L(l);
+    if constexpr (std::is_same_v<T, float>) {
+        if (convert_res) {
+            k_amr_copy<float, double><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res32.p, Ld.res.p);
+            launched();
+        }
+    }
+    T* x = cor<T>(l);
+    MLMG_CUDA_CHECK(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)Ld.meta.nelem, st()));
+    for (int i = 0; i < A.m_opt.nu1; ++i) { lev[l].I->smooth<T>(0, x, res_t<T>(l), i == 0); }
+}
+
+// rescor = res - L(cor): homogeneous, or (inhomog) with the coarse/fine
+// values of the coarser level's correction, which gather() has just loaded
+// (updateCorBC, AMReX_MLCellLinOp.H:666-680, 1246-1270)
+template <typename T>
+void AmrEngine::Impl::correction_residual (int l, bool inhomog)
+{
+    LevelData& Ld = L(l);
+    AmrLevelData& D = lev[l];
+    T* x = cor<T>(l);
+    if (inhomog) {
+        const T* cf;
+        if constexpr (std::is_same_v<T, float>) { cf = D.cf32.p; } else { cf = D.cf64.p; }
+        if (D.cfw.nfacecells > 0) {
+            k_amr_bndry<T><<<blocks_for(D.cfw.nfacecells, 256), 256, 0, st()>>>(Ld.dl, D.cfw, D.cfd.p, cf,
+                                                                               D.bflags.p, D.bcor.p);
+            launched();
+        }
+        D.I->ghost<T>(0, x, true, true, D.bcor.p);
+    } else {
+        D.I->ghost<T>(0, x, false, true);
+    }
+    k_residual<T, T, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), rescor_t<T>(l), x,
+        res_t<T>(l), nullptr, nullptr, nullptr, nullptr, nullptr);
+    launched();
+}
+
+// max|x| of level l (masked: cells under the finer level excluded) into h_norm[slot]
+void AmrEngine::Impl::norm_start (int l, const double* x, bool masked, int slot)
+{
+    LevelData& Ld = L(l);
+    Engine::Impl& I = *lev[l].I;
+    k_amr_norm<double><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), x,
+        masked ? lev[l].covered.p : nullptr, I.partial.p);
+    k_reduce_final<<<1, 256, 0, st()>>>(I.partial.p, Ld.all.solve_begin.p, RED_MAXABS, I.red_out.p);
+    launched(2);
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(h_norm.p + slot, I.red_out.p, sizeof(double), cudaMemcpyDeviceToHost, st()));
+}
+
+// MLMGT::computeResidual(finest) and its unmasked norm into h_norm[0]
+void AmrEngine::Impl::fine_residual_and_norm ()
+{
+    const int fin = nl - 1;
+    solution_residual(fin, true);
+    norm_start(fin, L(fin).res.p, false, 0);
+}
+
+// MLMGT::oneIter (AMReX_MLMG.H:1227-1293) followed by the convergence
+// residual of the finest level (:436-441)
+template <typename T>
+void AmrEngine::Impl::one_iter (int iter)
+{
+    const int fin = nl - 1;
+    Engine::Impl& I0 = *lev[0].I;
+    I0.bslot = 0;
+    for (int l = fin; l > 0; --l) {
+        LevelData& Ld = L(l);
+        mini_cycle<T>(l, true);
+        k_add_to<double, T><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), nullptr);
+        launched();
+        // computeResWithCrseSolFineCor(l-1, l), AMReX_MLMG.H:1660-1690
+        solution_residual(l - 1, l - 1 > 0);
+        correction_residual<T>(l, false);
+        k_amr_copy<double, T><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res.p, rescor_t<T>(l));
+        launched();
+        reflux(l - 1);
+        avgdown(l - 1, Ld.res.p, L(l - 1).res.p);
+        if (l != fin) { std::swap(lev[l].cor_p, lev[l].hold_p); }
+    }
+    {
+        LevelData& L0 = L(0);
+        if constexpr (std::is_same_v<T, float>) {
+            k_amr_copy<float, double><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.res32.p, L0.res.p);
+            launched();
+        }
+        if (iter < A.m_opt.max_fmg_iter) { I0.fcycle<T>(); } else { I0.vcycle<T>(0); }
+        k_add_to<double, T><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.sol.p, cor<T>(0), nullptr);
+        launched();
+    }
+    for (int l = 1; l <= fin; ++l) {
+        LevelData& Ld = L(l);
+        AmrLevelData& D = lev[l];
+        const unsigned g = (unsigned)Ld.all.ntiles;
+        // interpCorrection(l), AMReX_MLMG.H:1719-1750
+        gather<T>(l, cor<T>(l - 1));
+        const T* cf;
+        if constexpr (std::is_same_v<T, float>) { cf = D.cf32.p; } else { cf = D.cf64.p; }
+        k_amr_interp<T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), D.cfd.p, cf, cor<T>(l));
+        k_add_to<double, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), nullptr);
+        launched(2);
+        if (l != fin) {
+            k_add_to<T, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), hold<T>(l), cor<T>(l), nullptr);
+            launched();
+        }
+        // computeResWithCrseCorFineCor(l), AMReX_MLMG.H:1693-1715
+        if constexpr (std::is_same_v<T, float>) {
+            k_amr_copy<float, double><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res32.p, Ld.res.p);
+            launched();
+        }
+        correction_residual<T>(l, true);
+        k_amr_copy<T, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), res_t<T>(l), rescor_t<T>(l));
+        launched();
+        mini_cycle<T>(l, false);
+        k_add_to<double, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), nullptr);
+        launched();
+        if (l != fin) {
+            k_add_to<T, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), cor<T>(l), hold<T>(l), nullptr);
+            launched();
+        }
+    }
+    // averageDownAndSync, AMReX_MLCellLinOp.H:2102-2122
+    for (int l = fin; l > 0; --l) { avgdown(l - 1, L(l).sol.p, L(l - 1).sol.p); }
+    fine_residual_and_norm();
+}
+
+// ----------------------------------------------------------------- AmrEngine --
+AmrEngine::AmrEngine (const AmrProblem& prob, const EngineOptions& opt, cudaStream_t stream)
+    : m_opt(opt), m_stream(stream)
+{
+    m_opt.time_kernels = 0;
+    m_impl = std::make_unique<Impl>(*this);
+    m_impl->prob = prob;
+    m_impl->build();
+}
+
+AmrEngine::~AmrEngine () = default;
+
+int AmrEngine::kernel_launches () const
+{
+    int n = m_impl->own_launches;
+    for (const auto& D : m_impl->lev) { n += D.eng->kernel_launches(); }
+    return n;
+}
+
+void AmrEngine::reset_launch_count ()
+{
+    m_impl->own_launches = 0;
+    for (auto& D : m_impl->lev) { D.eng->reset_launch_count(); }
+}
+
+int AmrEngine::namr () const { return m_impl->nl; }
+int AmrEngine::num_mg_levels () const { return m_impl->lev[0].eng->nlevels(0); }
+
+void AmrEngine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<FabSet*>& sol_out,
+                       const std::vector<const FabSet*>& rhs, double tol_rel, double tol_abs)
+{
+    Impl& M = *m_impl;
+    const int nl = M.nl, fin = nl - 1;
+    MLMG_REQUIRE((int)sol_in.size() == nl && (int)sol_out.size() == nl && (int)rhs.size() == nl, ERR_ARGS,
+                 "one sol and one rhs per AMR level");
+    MLMG_REQUIRE(!M.lev[0].I->singular[0], ERR_UNSUPPORTED, "singular AMR composite solves are not supported");
+    m_report = SolveReport{};
+    for (int l = 0; l < nl; ++l) {
+        LevelData& Ld = M.L(l);
+        Engine::Impl& I = *M.lev[l].I;
+        MLMG_CUDA_CHECK(cudaMemsetAsync(Ld.sol.p, 0, Ld.sol.n * sizeof(double), m_stream));
+        MLMG_CUDA_CHECK(cudaMemsetAsync(Ld.rhs.p, 0, Ld.rhs.n * sizeof(double), m_stream));
+        I.xfer(I.items_for(*sol_in[l], 0, 0, -1), *sol_in[l], Ld.sol.p, false, 0);
+        I.xfer(I.items_for(*rhs[l], 0, 0, -1), *rhs[l], Ld.rhs.p, false, 0);
+    }
+    MLMG_CUDA_CHECK(cudaEventRecord(M.ev0, m_stream));
+    // prepareForSolve: averageDownSolutionRHS (AMReX_MLMG.H:1025-1028)
+    for (int l = fin; l > 0; --l) {
+        M.avgdown(l - 1, M.L(l).sol.p, M.L(l - 1).sol.p);
+        M.avgdown(l - 1, M.L(l).rhs.p, M.L(l - 1).rhs.p);
+    }
+    // computeMLResidual(finest) and the masked norms (AMReX_MLMG.H:391-396, 1632-1648)
+    auto ml_residual = [&] (int lmax) {
+        for (int l = lmax; l >= 0; --l) {
+            M.solution_residual(l, l > 0);
+            if (l < fin) { M.reflux(l); }
+        }
+    };
+    ml_residual(fin);
+    for (int l = 0; l < nl; ++l) {
+        M.norm_start(l, M.L(l).res.p, l < fin, 1 + l);
+        M.norm_start(l, M.L(l).rhs.p, l < fin, 1 + nl + l);
+    }
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
+    double resnorm0 = 0, rhsnorm0 = 0;
+    for (int l = 0; l < nl; ++l) {
+        resnorm0 = std::max(resnorm0, M.h_norm.p[1 + l]);
+        rhsnorm0 = std::max(rhsnorm0, M.h_norm.p[1 + nl + l]);
+    }
+    SolveReport& R = m_report;
+    R.init_resid = resnorm0;
+    R.rhs_norm = rhsnorm0;
+    const double max_norm = (m_opt.always_use_bnorm || rhsnorm0 >= resnorm0) ? rhsnorm0 : resnorm0;
+    const double target = std::max(tol_abs, std::max(tol_rel, 1.e-16) * max_norm);
+    R.final_resid = resnorm0;
+    if (m_opt.verbose >= 1) {
+        std::printf("MLMG: Initial rhs               = %.10g\nMLMG: Initial residual (resid0) = %.10g\n",
+                    rhsnorm0, resnorm0);
+    }
+    // the first swap of every intermediate level's correction buffers
+    // happens inside the iteration; their contents never carry over
+    const int niters = m_opt.fixed_iter ? m_opt.fixed_iter : m_opt.max_iter;
+    bool converged = false;
+    int graph_bslots = 1;
+    Engine::Impl& I0 = *M.lev[0].I;
+    if (resnorm0 > target) {
+        for (int iter = 0; iter < niters; ++iter) {
+            const bool fmg = iter < m_opt.max_fmg_iter;
+            if (!fmg && m_opt.use_graph) {
+                if (M.graph_exec == nullptr) {
+                    const int before = kernel_launches();
+                    cudaGraph_t g;
+                    MLMG_CUDA_CHECK(cudaStreamBeginCapture(m_stream, cudaStreamCaptureModeThreadLocal));
+                    I0.capturing = true;
+                    if (M.mixed()) { M.one_iter<float>(iter); } else { M.one_iter<double>(iter); }
+                    I0.capturing = false;
+                    graph_bslots = I0.bslot;
+                    MLMG_CUDA_CHECK(cudaStreamEndCapture(m_stream, &g));
+                    MLMG_CUDA_CHECK(cudaGraphInstantiate(&M.graph_exec, g, 0));
+                    MLMG_CUDA_CHECK(cudaGraphDestroy(g));
+                    M.graph_launches = kernel_launches() - before;
+                    M.own_launches -= M.graph_launches;
+                }
+                MLMG_CUDA_CHECK(cudaGraphLaunch(M.graph_exec, m_stream));
+                M.own_launches += M.graph_launches;
+                I0.bslot = graph_bslots;
+            } else {
+                if (M.mixed()) { M.one_iter<float>(iter); } else { M.one_iter<double>(iter); }
+            }
+            MLMG_CUDA_CHECK(cudaGetLastError());
+            MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
+            const double fine = M.h_norm.p[0];
+            R.history.push_back(fine);
+            for (int q = 0; q < I0.bslot && q < I0.nlev_max + 2; ++q) { R.cg_iters.push_back(I0.h_iters.p[q]); }
+            R.niters++;
+            R.final_resid = fine;
+            if (m_opt.verbose >= 2) {
+                std::printf("MLMG: Iteration %3d Fine resid/%s = %.10g\n", iter + 1,
+                            (max_norm == rhsnorm0) ? "bnorm" : "resid0", fine / max_norm);
+            }
+            if (!std::isfinite(fine)) { R.status = ERR_NONFINITE; break; }
+            if (fine <= target) {
+                // the finest level has converged: test the coarser levels (AMReX_MLMG.H:450-467)
+                ml_residual(fin - 1);
+                for (int l = 0; l < fin; ++l) { M.norm_start(l, M.L(l).res.p, true, 1 + l); }
+                MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
+                double crse = 0;
+                for (int l = 0; l < fin; ++l) { crse = std::max(crse, M.h_norm.p[1 + l]); }
+                R.final_resid = std::max(fine, crse);
+                if (crse <= target) { converged = true; break; }
+            }
+            if (R.final_resid > 1.e20 * max_norm) { R.status = ERR_DIVERGED; break; }
+        }
+        if (!converged && R.status == OK && m_opt.fixed_iter == 0) { R.status = NOT_CONVERGED; }
+    }
+    MLMG_CUDA_CHECK(cudaEventRecord(M.ev1, m_stream));
+    if (m_opt.verbose >= 1) {
+        std::printf("MLMG: Final Iter. %d resid, resid/bnorm = %.10g, %.10g\n", R.niters, R.final_resid,
+                    R.final_resid / max_norm);
+    }
+    for (int l = 0; l < nl; ++l) {
+        FabSet& out = *sol_out[l];
+        Engine::Impl& I = *M.lev[l].I;
+        I.xfer(I.items_for(out, 0, out.ngrow >= 1 ? 1 : 0, -1), out, M.L(l).sol.p, false, 1);
+    }
+    MLMG_CUDA_CHECK(cudaEventSynchronize(M.ev1));
+    float ms = 0;
+    MLMG_CUDA_CHECK(cudaEventElapsedTime(&ms, M.ev0, M.ev1));
+    m_last_ms = ms;
+}
+
+} // namespace mlmg

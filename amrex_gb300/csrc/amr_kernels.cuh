@@ -1,0 +1,280 @@
+// Coarse/fine coupling kernels of the AMR composite solve (refinement ratio
+// 2, MLPoisson).  Every kernel reads index tables built on the host from the
+// two levels' patch layouts, so a launch covers every box of a level.
+#pragma once
+
+#include "stage_kernels.cuh"
+
+namespace mlmg {
+
+// One thread per cell of a list of boxes: prefix `start` over the boxes' cell
+// counts, box w holds cells [start[w], start[w+1]).
+__device__ __forceinline__ void tag_cell (const CopyTag* tags, const long long* start, int ntag, long long t,
+                                          int& w, int& i, int& j, int& k)
+{
+    w = bsearch_ll<int>(start, ntag, t);
+    const CopyTag& C = tags[w];
+    const long long u = t - start[w];
+    const int nx = C.box.hi[0] - C.box.lo[0] + 1, ny = C.box.hi[1] - C.box.lo[1] + 1;
+    i = C.box.lo[0] + (int)(u % nx);
+    j = C.box.lo[1] + (int)((u / nx) % ny);
+    k = C.box.lo[2] + (int)(u / ((long long)nx * ny));
+}
+
+// The coarse level's field (valid cells) into the per-fine-patch coarse
+// buffers over the coarsened fine patch grown by one cell, which were zeroed
+// first: BndryRegisterT::copyFrom and the ParallelCopy of
+// MLMGT::interpCorrection (AMReX_MLMG.H:1719-1750).  Tag dst = fine patch
+// (its coarse buffer descriptor), src = coarse patch.
+template <typename T>
+__global__ void k_amr_gather (DevLevel Lc, const PatchDesc* __restrict__ cfd, const CopyTag* __restrict__ tags,
+                              const long long* __restrict__ start, int ntag, long long ncell,
+                              const T* __restrict__ crse, T* __restrict__ cf)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell) { return; }
+    int w, i, j, k;
+    tag_cell(tags, start, ntag, t, w, i, j, k);
+    const CopyTag& C = tags[w];
+    cf[cidx(cfd[C.dst], i, j, k)] = crse[cidx(Lc.P[C.src], i, j, k)];
+}
+
+// amrex::average_down onto the covered coarse cells (amrex_avgdown,
+// Src/Base/AMReX_MultiFabUtil_3D_C.H:375-392).  Tag dst = coarse patch,
+// src = fine patch, box in coarse index space.
+template <typename TD, typename TS>
+__global__ void k_amr_avgdown (DevLevel Lc, DevLevel Lf, const CopyTag* __restrict__ tags,
+                               const long long* __restrict__ start, int ntag, long long ncell,
+                               const TS* __restrict__ fine, TD* __restrict__ crse)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell) { return; }
+    int w, i, j, k;
+    tag_cell(tags, start, ntag, t, w, i, j, k);
+    const CopyTag& C = tags[w];
+    const PatchDesc& F = Lf.P[C.src];
+    const long long qf = cidx(F, 2 * i, 2 * j, 2 * k);
+    const long long sx = F.sx, sxy = F.sxy;
+    double v = 0;
+    v += (double)fine[qf];            v += (double)fine[qf + 1];
+    v += (double)fine[qf + sx];       v += (double)fine[qf + sx + 1];
+    v += (double)fine[qf + sxy];      v += (double)fine[qf + sxy + 1];
+    v += (double)fine[qf + sxy + sx]; v += (double)fine[qf + sxy + sx + 1];
+    crse[cidx(Lc.P[C.dst], i, j, k)] = TD(0.125 * v);
+}
+
+// fine = trilinear prolongation of the coarse buffer (mlmg_lin_cc_interp_r2,
+// AMReX_MLMG_3D_K.H:7-37) over every valid cell of the fine level:
+// MLCellLinOpT::interpolationAmr (AMReX_MLCellLinOp.H:1094-1181).
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_amr_interp (DevLevel Lf, Subset Sf, const PatchDesc* __restrict__ cfd, const T* __restrict__ cf,
+              T* __restrict__ fine)
+{
+    const TileCoord c = decode_tile(Lf, Sf, blockIdx.x);
+    const PatchDesc& F = Lf.P[c.p];
+    const PatchDesc& G = cfd[c.p];
+    const int j = c.y0 + threadIdx.y;
+    if (j > F.hi[1]) { return; }
+    const long long gx = 1, gy = G.sx, gz = G.sxy;
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > F.hi[2]) { break; }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = c.x0 + threadIdx.x + 32 * h;
+            if (i > F.hi[0]) { continue; }
+            const int ic = i >> 1, jc = j >> 1, kc = k >> 1;
+            const long long di = (i & 1) ? gx : -gx, dj = (j & 1) ? gy : -gy, dk = (k & 1) ? gz : -gz;
+            const long long q = cidx(G, ic, jc, kc);
+            const T v = T(0.421875) * cf[q]
+                      + T(0.140625) * cf[q + di]
+                      + T(0.140625) * cf[q + dj]
+                      + T(0.140625) * cf[q + dk]
+                      + T(0.046875) * cf[q + dj + dk]
+                      + T(0.046875) * cf[q + di + dk]
+                      + T(0.046875) * cf[q + di + dj]
+                      + T(0.015625) * cf[q + di + dj + dk];
+            fine[cidx(F, i, j, k)] = v;
+        }
+    }
+}
+
+// bits of the per-face-cell neighbourhood flags of the boundary interpolation
+enum : int {
+    BF_SELF = 1,        // the ghost cell itself is not covered (a coarse/fine cell)
+    BF_T1LO = 2,        // the ghost cell two fine cells down the first tangential direction is not covered
+    BF_T1HI = 4,        // ... two cells up the first tangential direction
+    BF_T2LO = 8,        // ... down the second tangential direction
+    BF_T2HI = 16,       // ... up the second tangential direction
+    BF_CROSS = 32,      // all four diagonal ghost cells (+-2, +-2) are not covered
+};
+
+// InterpBndryDataT::updateBndryValues (Src/Boundary/AMReX_InterpBndryData.H:
+// 158-267) with interpbndrydata_{x,y,z}_o3 (AMReX_InterpBndryData_3D_K.H:20-120):
+// the Dirichlet value of every not-covered ghost cell on the coarse/fine faces
+// of the fine level, from the coarse buffer: the coarse value at the ghost
+// cell's coarse cell plus tangential slopes and curvatures (one-sided where a
+// neighbouring ghost cell is covered or outside) and the cross term.  Output
+// slots are the faces' Dirichlet-value slots (FaceBC::bcval_off + u).
+template <typename T>
+__global__ void k_amr_bndry (DevLevel Lf, GhostWork W, const PatchDesc* __restrict__ cfd, const T* __restrict__ cf,
+                             const int8_t* __restrict__ flags, double* __restrict__ bcval)
+{
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= W.nfacecells) { return; }
+    const int w = bsearch_ll<int>(W.fstart, W.nface, tid);
+    const int2 pf = W.faces[w];
+    const PatchDesc& P = Lf.P[pf.x];
+    const int f = pf.y;
+    const long long u = tid - W.fstart[w];
+    const long long slot = P.face[f].bcval_off + u;
+    const int fl = flags[slot];
+    if (!(fl & BF_SELF)) { return; }
+    int c[3];
+    face_cell(P, f, u, c[0], c[1], c[2]);
+    const int d = f % 3;
+    const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
+    const PatchDesc& G = cfd[pf.x];
+    const long long st[3] = {1, (long long)G.sx, G.sxy};
+    const int cc[3] = {c[0] >> 1, c[1] >> 1, c[2] >> 1};
+    const long long q = cidx(G, cc[0], cc[1], cc[2]);
+    const double c0 = (double)cf[q];
+    double slope[2], curv[2];
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+        const long long s = st[m == 0 ? t1 : t2];
+        const bool lo_nc = fl & (m == 0 ? BF_T1LO : BF_T2LO);
+        const bool hi_nc = fl & (m == 0 ? BF_T1HI : BF_T2HI);
+        const double vm = (double)cf[q - s], vp = (double)cf[q + s];
+        const double vlo = lo_nc ? vm : c0, vhi = hi_nc ? vp : c0;
+        const double fac = (lo_nc != hi_nc) ? 1.0 : 0.5;
+        slope[m] = fac * (vhi - vlo);
+        curv[m] = (lo_nc && hi_nc) ? 0.5 * (vp - 2.0 * c0 + vm) : 0.0;
+    }
+    double cross = 0.0;
+    if (fl & BF_CROSS) {
+        const long long s1 = st[t1], s2 = st[t2];
+        cross = 0.25 * ((double)cf[q + s1 + s2] - (double)cf[q - s1 + s2] + (double)cf[q - s1 - s2]
+                        - (double)cf[q + s1 - s2]);
+    }
+    const double y = -0.5 + ((double)(c[t1] - 2 * cc[t1]) + 0.5) / 2.0;
+    const double z = -0.5 + ((double)(c[t2] - 2 * cc[t2]) + 0.5) / 2.0;
+    bcval[slot] = c0 + y * slope[0] + (y * y) * curv[0] + z * slope[1] + (z * z) * curv[1] + y * z * cross;
+}
+
+// ----------------------------------------------------------------- reflux --
+// One coarse cell next to the fine level and the faces it shares with it.
+struct RefluxCell {
+    long long q;        // element index of the coarse cell
+    int e0, ne;         // its face entries [e0, e0+ne)
+};
+struct RefluxFace {
+    long long qn;       // element index of the covered coarse neighbour (in its own patch)
+    long long qf;       // element index of the fine cell inside the fine patch at sub-face (0,0)
+    int fp;             // fine patch
+    int dir, side;      // face direction; side 1: the neighbour (and the fine level) lies at +dir
+};
+struct RefluxParams {
+    double dxinv_c[3];  // coarse 1/dx
+    double dxinv_f[3];  // fine 1/dx
+};
+
+// MLCellLinOpT::reflux (AMReX_MLCellLinOp.H:1272-1346) through YAFluxRegister
+// (Src/Boundary/AMReX_YAFluxRegister.H:343-560, AMReX_YAFluxRegister_3D_K.H):
+// res += sum over the cell's coarse/fine faces of the coarse face flux minus
+// the mean of the fine face fluxes, divided by the coarse dx, with MLPoisson's
+// flux F = (phi_hi - phi_lo)/dx.  The fine solution's ghosts must hold the
+// inhomogeneous applyBC values.  Coarse contributions are summed first, in
+// face order, then the fine ones (the register adds its fine patches last).
+__global__ void k_amr_reflux (DevLevel Lf, const RefluxCell* __restrict__ cells, const RefluxFace* __restrict__ faces,
+                              int ncell, RefluxParams prm, const double* __restrict__ sol_c,
+                              const double* __restrict__ sol_f, double* __restrict__ res_c)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell) { return; }
+    const RefluxCell C = cells[t];
+    const double vc = sol_c[C.q];
+    double dc = 0.0;
+    for (int e = C.e0; e < C.e0 + C.ne; ++e) {
+        const RefluxFace& R = faces[e];
+        const double dtdx = prm.dxinv_c[R.dir];
+        const double vn = sol_c[R.qn];
+        if (R.side) { dc += dtdx * (prm.dxinv_c[R.dir] * (vn - vc)); }
+        else { dc -= dtdx * (prm.dxinv_c[R.dir] * (vc - vn)); }
+    }
+    double dfine = 0.0;
+    for (int e = C.e0; e < C.e0 + C.ne; ++e) {
+        const RefluxFace& R = faces[e];
+        const PatchDesc& F = Lf.P[R.fp];
+        const long long st[3] = {1, (long long)F.sx, F.sxy};
+        const int t1 = (R.dir == 0) ? 1 : 0, t2 = (R.dir == 2) ? 1 : 2;
+        const long long sd = st[R.dir];
+        const double dtdx = prm.dxinv_f[R.dir] * 0.125;   // dt / (dx_f * rr^3)
+        double acc = 0.0;
+        for (int o2 = 0; o2 < 2; ++o2)
+        for (int o1 = 0; o1 < 2; ++o1) {
+            const long long qi = R.qf + o1 * st[t1] + o2 * st[t2];
+            if (R.side) {   // fine level above: the fine box's low face, ghost below
+                acc += -dtdx * (prm.dxinv_f[R.dir] * (sol_f[qi] - sol_f[qi - sd]));
+            } else {        // fine level below: the fine box's high face, ghost above
+                acc += dtdx * (prm.dxinv_f[R.dir] * (sol_f[qi + sd] - sol_f[qi]));
+            }
+        }
+        dfine += acc;
+    }
+    res_c[C.q] += dc + dfine;
+}
+
+// per-block max|x| over the valid cells whose `covered` byte is 0 (the
+// norms of a coarse AMR level, MLCellLinOpT::normInf, AMReX_MLCellLinOp.H:2006-2101)
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_amr_norm (DevLevel L, Subset S, const T* __restrict__ x, const int8_t* __restrict__ covered,
+            double* __restrict__ partial)
+{
+    __shared__ double sm[32];
+    const TileCoord c = decode_tile(L, S, blockIdx.x);
+    const PatchDesc& P = L.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    double acc = 0.0;
+    if (j <= P.hi[1]) {
+        for (int kk = 0; kk < TILE_Z; ++kk) {
+            const int k = c.z0 + kk;
+            if (k > P.hi[2]) { break; }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int i = c.x0 + threadIdx.x + 32 * h;
+                if (i > P.hi[0]) { continue; }
+                const long long q = cidx(P, i, j, k);
+                if (covered == nullptr || covered[q] == 0) { acc = fmax(acc, fabs((double)x[q])); }
+            }
+        }
+    }
+    const double red = block_reduce(acc, RED_MAXABS, sm);
+    if (threadIdx.x == 0 && threadIdx.y == 0) { partial[blockIdx.x] = red; }
+}
+
+// dst = src over valid cells, with precision conversion
+template <typename TD, typename TS>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_amr_copy (DevLevel L, Subset S, TD* __restrict__ dst, const TS* __restrict__ src)
+{
+    const TileCoord c = decode_tile(L, S, blockIdx.x);
+    const PatchDesc& P = L.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    if (j > P.hi[1]) { return; }
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > P.hi[2]) { break; }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = c.x0 + threadIdx.x + 32 * h;
+            if (i > P.hi[0]) { continue; }
+            const long long q = cidx(P, i, j, k);
+            dst[q] = TD(src[q]);
+        }
+    }
+}
+
+} // namespace mlmg

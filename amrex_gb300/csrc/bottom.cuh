@@ -106,7 +106,7 @@ __device__ void apply_normalize (const BottomLevelPtrs& B, const BottomJob& J, d
     __syncthreads();
 }
 
-__device__ double reduce (const DevLevel& L, int p0, int np, const double* x, const double* y, int op)
+__device__ inline double reduce (const DevLevel& L, int p0, int np, const double* x, const double* y, int op)
 {
     __shared__ double sm[32];
     __shared__ double result;

@@ -1,6 +1,7 @@
 // C ABI of the GB300 MLMG library (declared in include/mlmg_capi.h).
 #include "../../include/mlmg_capi.h"
 #include "solver.hpp"
+#include "amr.hpp"
 #include "kernels.cuh"
 
 #include <algorithm>
@@ -285,6 +286,12 @@ struct mlmg_linop_s {
     FabSet acoef_fs, bcoef_fs[3], levelbc_fs;
     int struct_version = 0, coef_version = 0;
     std::vector<LevelGrids> levels;
+    // AMR levels (composite MLPoisson): level l's BoxArray and level BC values
+    // (amr_boxes[0] == boxes, amr_levelbc[0] unused: levelbc holds level 0's)
+    int nlev = 1;
+    std::vector<std::vector<Box3>> amr_boxes;
+    std::vector<std::unique_ptr<mlmg_multifab_s>> amr_levelbc;
+    std::vector<FabSet> amr_levelbc_fs;
     void regrid () { levels = define_grids(geom, boxes, info); ++struct_version; }
 };
 
@@ -304,6 +311,9 @@ struct mlmg_solver_s {
     // transposed-operator engine of the adjoint (its own graph and buffers)
     std::unique_ptr<Engine> adj_eng;
     int adj_struct = -1, adj_coef = -1, adj_prec = -1, adj_merge = -1;
+    // composite (multi-AMR-level) engine
+    std::unique_ptr<AmrEngine> amr_eng;
+    int amr_struct = -1, amr_coef = -1, amr_prec = -1, amr_merge = -1;
 };
 
 namespace {
@@ -375,6 +385,8 @@ SolveProblem make_problem (mlmg_linop op)
 Engine& engine_for (mlmg_solver s)
 {
     mlmg_linop op = s->op;
+    MLMG_REQUIRE(op->nlev == 1, ERR_UNSUPPORTED,
+                 "this call works on single-level operators; composite operators solve through mlmg_solve_levels");
     if (!s->eng || s->eng_struct != op->struct_version || s->eng_prec != s->opt.precision ||
         s->eng_merge != s->opt.merge_boxes) {
         s->eng.reset();
@@ -417,6 +429,39 @@ Engine& adjoint_engine_for (mlmg_solver s)
 }
 
 void count_launches (Engine& e) { g_launches += e.kernel_launches(); e.reset_launch_count(); }
+void count_launches (AmrEngine& e) { g_launches += e.kernel_launches(); e.reset_launch_count(); }
+
+AmrEngine& amr_engine_for (mlmg_solver s)
+{
+    mlmg_linop op = s->op;
+    // level BC values are read when the engine is built (setPhysBndryValues):
+    // a new coefficient version rebuilds it
+    if (!s->amr_eng || s->amr_struct != op->struct_version || s->amr_coef != op->coef_version ||
+        s->amr_prec != s->opt.precision || s->amr_merge != s->opt.merge_boxes) {
+        s->amr_eng.reset();
+        AmrProblem P;
+        P.geom = op->geom;
+        for (int d = 0; d < 3; ++d) { P.lobc[d] = op->lobc[d]; P.hibc[d] = op->hibc[d]; }
+        P.maxorder = op->maxorder;
+        P.info = op->info;
+        op->amr_levelbc_fs.assign(op->nlev, FabSet{});
+        for (int l = 0; l < op->nlev; ++l) {
+            AmrLevelProblem L;
+            L.boxes = op->amr_boxes[l];
+            const mlmg_multifab_s* bc = (l == 0) ? op->levelbc.get() : op->amr_levelbc[l].get();
+            if (bc) { op->amr_levelbc_fs[l] = bc->fabset(); L.levelbc = &op->amr_levelbc_fs[l]; }
+            P.levels.push_back(L);
+        }
+        s->amr_eng = std::make_unique<AmrEngine>(P, s->opt, lib_stream());
+        s->amr_struct = op->struct_version;
+        s->amr_coef = op->coef_version;
+        s->amr_prec = s->opt.precision;
+        s->amr_merge = s->opt.merge_boxes;
+    }
+    s->amr_eng->options() = s->opt;
+    s->amr_eng->options().time_kernels = 0;
+    return *s->amr_eng;
+}
 
 void check_solver_mf (mlmg_solver s, mlmg_multifab mf)
 {
@@ -752,7 +797,9 @@ static int linop_new (int is_abec, int nlev, const mlmg_geometry* geom, const ml
 {
     API_BEGIN
     MLMG_REQUIRE(out && geom && ba && dm && geom[0] && ba[0] && dm[0], ERR_ARGS, "null handle");
-    MLMG_REQUIRE(nlev == 1, ERR_UNSUPPORTED, "composite (multi-AMR-level) solves are not implemented");
+    MLMG_REQUIRE(nlev >= 1 && nlev <= 8, ERR_ARGS, "nlev must be in 1..8");
+    MLMG_REQUIRE(nlev == 1 || !is_abec, ERR_UNSUPPORTED,
+                 "composite (multi-AMR-level) solves are implemented for MLPoisson only");
     auto op = std::make_unique<mlmg_linop_s>();
     op->is_abec = is_abec;
     op->geom = geom[0]->g;
@@ -773,6 +820,27 @@ static int linop_new (int is_abec, int nlev, const mlmg_geometry* geom, const ml
     }
     for (int d = 0; d < 3; ++d) {
         if (op->geom.periodic[d]) { op->lobc[d] = op->hibc[d] = BC_PERIODIC; }
+    }
+    op->nlev = nlev;
+    op->amr_boxes.assign(1, op->boxes);
+    op->amr_levelbc.resize(nlev);
+    for (int l = 1; l < nlev; ++l) {
+        MLMG_REQUIRE(geom[l] && ba[l] && dm[l], ERR_ARGS, "null handle");
+        const GeomC& g = geom[l]->g;
+        // refinement ratio 2 between consecutive AMR levels, same physical box
+        MLMG_REQUIRE(g.domain == refine(op->geom.domain, 1 << l), ERR_UNSUPPORTED,
+                     "AMR levels must refine the level-0 domain by 2 per level");
+        for (int d = 0; d < 3; ++d) {
+            MLMG_REQUIRE(g.prob_lo[d] == op->geom.prob_lo[d] && g.prob_hi[d] == op->geom.prob_hi[d] &&
+                         g.periodic[d] == op->geom.periodic[d], ERR_ARGS, "AMR level geometries differ");
+        }
+        MLMG_REQUIRE(dm[l]->nbox == (int)ba[l]->boxes.size(), ERR_ARGS, "DistributionMapping does not match BoxArray");
+        for (const auto& b : ba[l]->boxes) {
+            for (int d = 0; d < 3; ++d) {
+                MLMG_REQUIRE(b.lo[d] >= g.domain.lo[d] && b.hi[d] <= g.domain.hi[d], ERR_ARGS, "box outside the domain");
+            }
+        }
+        op->amr_boxes.push_back(ba[l]->boxes);
     }
     op->regrid();
     *out = op.release();
@@ -814,7 +882,17 @@ int mlmg_linop_set_domain_bc (mlmg_linop op, const int lobc[3], const int hibc[3
 int mlmg_linop_set_level_bc (mlmg_linop op, int amrlev, mlmg_multifab levelbc)
 {
     API_BEGIN
-    MLMG_REQUIRE(op && amrlev == 0, ERR_ARGS, "bad arguments");
+    MLMG_REQUIRE(op && amrlev >= 0 && amrlev < op->nlev, ERR_ARGS, "bad arguments");
+    if (amrlev > 0) {
+        if (levelbc == nullptr) { op->amr_levelbc[amrlev].reset(); }
+        else {
+            MLMG_REQUIRE(levelbc->ngrow >= 1 && levelbc->boxes == op->amr_boxes[amrlev] && levelbc->nodal_dir == -1,
+                         ERR_ARGS, "level BC MultiFab must share the level's BoxArray and have a ghost cell");
+            op->amr_levelbc[amrlev] = clone_mf(*levelbc);
+        }
+        ++op->coef_version;
+        return OK;
+    }
     if (levelbc == nullptr) { op->levelbc.reset(); }
     else {
         MLMG_REQUIRE(levelbc->ngrow >= 1 && levelbc->boxes == op->boxes && levelbc->nodal_dir == -1, ERR_ARGS,
@@ -1016,6 +1094,51 @@ int mlmg_solve (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, double tol_
     API_END
 }
 
+int mlmg_solve_levels (mlmg_solver s, const mlmg_multifab* sol, const mlmg_multifab* rhs, double tol_rel,
+                       double tol_abs, double* final_resid)
+{
+    API_BEGIN
+    MLMG_REQUIRE(s && s->op && sol && rhs, ERR_ARGS, "null handle");
+    mlmg_linop op = s->op;
+    if (op->nlev == 1) { return mlmg_solve(s, sol[0], rhs[0], tol_rel, tol_abs, final_resid); }
+    std::vector<FabSet> fs(op->nlev), fr(op->nlev);
+    std::vector<const FabSet*> in(op->nlev), r(op->nlev);
+    std::vector<FabSet*> out(op->nlev);
+    for (int l = 0; l < op->nlev; ++l) {
+        mlmg_multifab m = sol[l], b = rhs[l];
+        MLMG_REQUIRE(m && b, ERR_ARGS, "null handle");
+        for (mlmg_multifab x : {m, b}) {
+            MLMG_REQUIRE(x->ncomp == 1 && x->nodal_dir == -1 && x->prec == 8, ERR_ARGS,
+                         "solution and rhs must be single-component, cell-centred and double precision");
+            MLMG_REQUIRE(x->boxes == op->amr_boxes[l], ERR_ARGS, "MultiFab BoxArray differs from the level's");
+        }
+        fs[l] = m->fabset();
+        fr[l] = b->fabset();
+        in[l] = &fs[l];
+        out[l] = &fs[l];
+        r[l] = &fr[l];
+    }
+    AmrEngine& e = amr_engine_for(s);
+    e.solve(in, out, r, tol_rel, tol_abs);
+    count_launches(e);
+    s->last = e.report();
+    s->last_ms = e.last_solve_ms();
+    for (int l = 0; l < op->nlev; ++l) {
+        if (sol[l]->ngrow >= 1) {
+            GeomC g = op->geom;
+            g.domain = refine(op->geom.domain, 1 << l);
+            const auto tags = fill_boundary_tags(*sol[l], g);
+            fab_run_tags<double>(*sol[l], tags);
+        }
+    }
+    if (final_resid) { *final_resid = s->last.final_resid; }
+    if (s->last.status == NOT_CONVERGED) { g_err = "MLMG failed to converge"; }
+    if (s->last.status == ERR_DIVERGED) { g_err = "MLMG blew up"; }
+    if (s->last.status == ERR_NONFINITE) { g_err = "MLMG residual is not finite"; }
+    return s->last.status;
+    API_END
+}
+
 int mlmg_adjoint_grad (mlmg_solver s, mlmg_multifab sol, mlmg_multifab dJdphi, double tol_rel, double tol_abs,
                        mlmg_multifab out_dJdf, const mlmg_multifab* out_dJdb, mlmg_multifab out_dJda)
 {
@@ -1201,6 +1324,8 @@ double mlmg_get_final_residual (mlmg_solver s) { return s ? s->last.final_resid 
 double mlmg_get_init_rhs (mlmg_solver s) { return s ? s->last.rhs_norm : -1.0; }
 double mlmg_get_solve_time_ms (mlmg_solver s) { return s ? s->last_ms : -1.0; }
 int mlmg_get_num_mg_levels (mlmg_solver s) { return (s && s->op) ? (int)s->op->levels.size() : ERR_ARGS; }
+
+int mlmg_linop_num_amr_levels (mlmg_linop op) { return op ? op->nlev : ERR_ARGS; }
 
 int mlmg_solve_batched (int n, const mlmg_solver* solvers, const mlmg_multifab* sols, const mlmg_multifab* rhss,
                         double tol_rel, double tol_abs, int* status)

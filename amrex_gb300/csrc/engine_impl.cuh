@@ -1,0 +1,200 @@
+// Internal state of the MLMG engine (Engine::Impl and its per-level data),
+// shared by the single-level engine (solver.cu) and the AMR composite
+// driver (amr.cu).  Not part of the public interface.
+#pragma once
+
+#include "solver.hpp"
+#include "bottom.cuh"
+#include "stencil_kernels.cuh"
+#include "fused_sweep.cuh"
+#include "march_sweep.cuh"
+#include "coarse_vcycle.cuh"
+#include "adjoint_kernels.cuh"
+#include "flux_kernels.cuh"
+#include "fmg_kernels.cuh"
+
+#include <algorithm>
+#include <numeric>
+
+namespace mlmg {
+
+
+struct SubsetData {
+    DevBuf<int> plist, tstart, solve_begin;
+    std::vector<int> h_plist, h_tstart, h_solve_begin;
+    int n = 0, ntiles = 0;
+    Subset dev () const { return Subset{plist.p, tstart.p, n, ntiles}; }
+};
+
+inline int tiles_of (const PatchDesc& P)
+{
+    const int nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1, nz = P.hi[2] - P.lo[2] + 1;
+    return ((nx + TILE_X - 1) / TILE_X) * ((ny + TILE_Y - 1) / TILE_Y) * ((nz + TILE_Z - 1) / TILE_Z);
+}
+
+inline void build_subset (SubsetData& S, const PatchLevel& PL, const std::vector<int>& plist, int nsolve,
+                   cudaStream_t st)
+{
+    S.h_plist = plist;
+    S.n = (int)plist.size();
+    S.h_tstart.assign(S.n + 1, 0);
+    for (int q = 0; q < S.n; ++q) { S.h_tstart[q + 1] = S.h_tstart[q] + tiles_of(PL.patches[plist[q]]); }
+    S.ntiles = S.h_tstart[S.n];
+    S.h_solve_begin.assign(nsolve + 1, 0);
+    // tiles of solve s are [begin[s], begin[s+1]) (patches are grouped by solve)
+    int q = 0;
+    for (int s = 0; s < nsolve; ++s) {
+        S.h_solve_begin[s] = S.h_tstart[q];
+        while (q < S.n && PL.patches[plist[q]].solve == s) { ++q; }
+    }
+    S.h_solve_begin[nsolve] = S.ntiles;
+    if (S.n > 0) {
+        S.plist.upload(S.h_plist, st);
+        S.tstart.upload(S.h_tstart, st);
+    }
+    S.solve_begin.upload(S.h_solve_begin, st);
+}
+
+
+struct LevelData {
+    PatchLevel meta;
+    DevBuf<PatchDesc> P;
+    DevBuf<int8_t> masks;
+    DevBuf<int> sfirst, snp;
+    DevBuf<CopyTag> tags;
+    DevBuf<int2> faces;
+    DevBuf<long long> fstart, tstart;
+    GhostWork gw{};
+    SubsetData all, mg;
+    DevLevel dl{};
+    // FP64 fields
+    DevBuf<double> cor, res, rescor, a, bx, by, bz;
+    DevBuf<double> sol, rhs, bcval;                 // level 0 only
+    DevBuf<double> face_phi, face_out[4];           // level 0 scratch: a solution with ghosts and face outputs
+                                                    // (adjoint gradients, fluxes), allocated on demand
+    DevBuf<double> partner;                         // level 0, periodic image face coefficients (A^T)
+    // FP32 fields (mixed precision)
+    DevBuf<float> cor32, res32, rescor32;
+    // stencil form of the ABec operator (mixed path): FP64 on every level,
+    // FP32 copies for the FP32 V-cycle
+    DevBuf<double> D, sx, sy, sz;
+    DevBuf<float> D32, sx32, sy32, sz32;
+    bool inline_bc = false;   // ghost values computed inside the stencil kernels
+    // fused two-colour sweeps (mixed path): tile map and the second buffer
+    bool fused = false;
+    SubsetData fz;
+    bool march = false;           // fused sweeps by the z-marching kernel
+    SubsetData mz;
+    DevBuf<float> cor32b;
+    DevBuf<int> tfirst_d, tn_d;    // per-solve tag ranges (coarse-level kernel)
+    // F-cycles: the solves' own boxes of this level, interpolation data for
+    // this level as the fine one, and the saved corrections (on demand)
+    DevBuf<Box3> rbox;
+    DevBuf<FmgSolveInfo> fmg;
+    DevBuf<double> cor_hold;
+    DevBuf<float> cor_hold32;
+    // bottom work arrays
+    DevBuf<double> bw[7];
+    bool has_bottom = false;
+    std::vector<int> solve_tag_first, solve_tag_n;  // tags grouped per solve
+};
+
+struct Engine::Impl {
+    Engine& E;
+    int nsolve = 0;
+    int nlev_max = 0;
+    bool abec = false;
+    std::vector<LevelData> lev;
+    std::vector<int> singular;
+    std::vector<double> volinv0, volinv_bottom;
+    DevBuf<double> partial, red_out, volinv0_d;
+    DevBuf<int> active_d, bot_iters, bot_ret;
+    PinnedBuf<double> h_red;
+    PinnedBuf<int> h_iters;
+    DevBuf<BottomLevelPtrs> bot_levels;
+    DevBuf<BottomJob> bot_jobs;
+    int njobs = 0;
+    // one warp when every bottom level is tiny (its block barriers are then
+    // nearly free), else BOTTOM_THREADS
+    int bot_threads = BOTTOM_THREADS;
+    // levels >= lc run inside k_coarse_vcycle (one block per solve); -1: none
+    int lc = -1;
+    DevBuf<CoarseLevelPtrs> coarse_lv;
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_launches = 0;      // kernels in one replay of the iteration graph
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // event pairs around the finest-level smoother launches of one iteration
+    std::vector<cudaEvent_t> kev;
+    int kev_used = 0;
+    bool capturing = false;
+    int bslot = 0;               // bottom solves issued in the current iteration
+
+    explicit Impl (Engine& e) : E(e) {}
+    ~Impl () {
+        if (graph_exec) { cudaGraphExecDestroy(graph_exec); }
+        if (ev0) { cudaEventDestroy(ev0); }
+        if (ev1) { cudaEventDestroy(ev1); }
+        for (auto e : kev) { cudaEventDestroy(e); }
+    }
+
+    void kev_record ()
+    {
+        if (kev_used >= (int)kev.size()) {
+            cudaEvent_t e;
+            MLMG_CUDA_CHECK(cudaEventCreate(&e));
+            kev.push_back(e);
+        }
+        cudaEvent_t e = kev[kev_used++];
+        if (capturing) {
+            MLMG_CUDA_CHECK(cudaEventRecordWithFlags(e, st(), cudaEventRecordExternal));
+        } else {
+            MLMG_CUDA_CHECK(cudaEventRecord(e, st()));
+        }
+    }
+
+    void kev_harvest ()
+    {
+        for (int q = 0; q + 1 < kev_used; q += 2) {
+            float ms = 0;
+            MLMG_CUDA_CHECK(cudaEventElapsedTime(&ms, kev[q], kev[q + 1]));
+            E.m_kstats.total_ms += ms;
+            E.m_kstats.launches += 1;
+        }
+    }
+
+    cudaStream_t st () const { return E.m_stream; }
+    bool mixed () const { return E.m_opt.precision == 1; }
+    void launched (int n = 1) { E.m_launches += n; }
+
+    // ------------------------------------------------------------ setup --
+    void build ();
+    void build_bottom_tables ();
+    void load_level0_field (const FabSet* fs, double* field, double defval, int nodal_dir, int s);
+    void xfer (const std::vector<XferItem>& items, const FabSet& fs, void* field, bool field_is_f32, int dir);
+    std::vector<XferItem> items_for (const FabSet& fs, int s, int ghost_mode, int nodal_dir) const;
+
+    // ------------------------------------------------------- operations --
+    // bcv: Dirichlet values of an inhomogeneous fill (null: the level-0 values)
+    template <typename T> void ghost (int l, T* phi, bool inhomog, bool do_copy, const double* bcv = nullptr);
+    template <typename T> void smooth (int l, T* cor, const T* res, bool skip_fb);
+    template <typename T> void vcycle (int top);
+    template <typename T> void fcycle ();
+    template <typename T> void correction_residual (int l);
+    void bottom_done ();
+    template <typename T> T* field_cor (int l);
+    template <typename T> T* field_res (int l);
+    template <typename T> T* field_rescor (int l);
+    template <typename T> const T* coef (int l, int which);
+    void reduce_per_solve (int l, const SubsetData& S, int op, const double* x, const double* y);
+    StencilPtrs stencil32 (int l) const;
+    StencilPtrs stencil64 (int l) const;
+    void gsrb32 (int l, float* cor, const float* res, int rb);
+    void smooth_fused (int l, int n);
+    void resid32 (int l, float* rescor, float* cor, const float* res);
+    void residual0 (bool to32);   // res[0] (FP64, or FP32 in mixed) and per-block max|r|
+    void one_iteration (bool fmg);
+};
+
+static const dim3 kTileBlock(32, TILE_Y);
+
+} // namespace mlmg

@@ -168,6 +168,43 @@ Box3 adj_cell (const Box3& b, int f)
 
 } // namespace
 
+BoxLocator::BoxLocator (const std::vector<Box3>& boxes) : m_boxes(boxes)
+{
+    if (boxes.empty()) { return; }
+    m_bb = boxes[0];
+    for (const auto& b : boxes) {
+        for (int d = 0; d < 3; ++d) { m_bb.lo[d] = std::min(m_bb.lo[d], b.lo[d]); m_bb.hi[d] = std::max(m_bb.hi[d], b.hi[d]); }
+    }
+    for (int d = 0; d < 3; ++d) { m_nb[d] = (m_bb.len(d) + 7) / 8; }
+    const size_t nbk = (size_t)m_nb[0] * m_nb[1] * m_nb[2];
+    std::vector<int> cnt(nbk + 1, 0);
+    auto each_bucket = [&] (const Box3& b, auto&& fn) {
+        int lo[3], hi[3];
+        for (int d = 0; d < 3; ++d) { lo[d] = (b.lo[d] - m_bb.lo[d]) / 8; hi[d] = (b.hi[d] - m_bb.lo[d]) / 8; }
+        for (int z = lo[2]; z <= hi[2]; ++z)
+        for (int y = lo[1]; y <= hi[1]; ++y)
+        for (int x = lo[0]; x <= hi[0]; ++x) { fn(((size_t)z * m_nb[1] + y) * m_nb[0] + x); }
+    };
+    for (const auto& b : boxes) { each_bucket(b, [&] (size_t q) { cnt[q + 1]++; }); }
+    for (size_t q = 0; q < nbk; ++q) { cnt[q + 1] += cnt[q]; }
+    m_start = cnt;
+    m_list.assign((size_t)cnt[nbk], 0);
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int bi = 0; bi < (int)boxes.size(); ++bi) {
+        each_bucket(boxes[bi], [&] (size_t q) { m_list[(size_t)fill[q]++] = bi; });
+    }
+}
+
+int BoxLocator::find (int i, int j, int k) const
+{
+    if (m_boxes.empty() || !m_bb.contains(i, j, k)) { return -1; }
+    const size_t q = ((size_t)((k - m_bb.lo[2]) / 8) * m_nb[1] + (j - m_bb.lo[1]) / 8) * m_nb[0] + (i - m_bb.lo[0]) / 8;
+    for (int t = m_start[q]; t < m_start[q + 1]; ++t) {
+        if (m_boxes[(size_t)m_list[(size_t)t]].contains(i, j, k)) { return m_list[(size_t)t]; }
+    }
+    return -1;
+}
+
 PatchLevel build_patch_level (const std::vector<const SolveSpec*>& solves, int lev, bool allow_merge)
 {
     PatchLevel PL;
@@ -186,7 +223,8 @@ PatchLevel build_patch_level (const std::vector<const SolveSpec*>& solves, int l
         PL.solve_rbox_n[s] = (int)LG.boxes.size();
         PL.solve_derived[s] = LG.derived;
         PL.rboxes.insert(PL.rboxes.end(), LG.boxes.begin(), LG.boxes.end());
-        const bool is_bottom = (lev == (int)S.levels.size() - 1);
+        const bool is_bottom = (lev == (int)S.levels.size() - 1) && !S.amr_fine;
+        const BoxLocator loc(LG.boxes);
         double dx[3], dxinv[3];
         LG.geom.cell_size(dx, dxinv);
 
@@ -249,7 +287,7 @@ PatchLevel build_patch_level (const std::vector<const SolveSpec*>& solves, int l
                     bcl = 0.0;
                 } else {
                     F.type = BC_DIRICHLET;            // coarse/fine BC type
-                    bcl = 0.5 * 1.0 * S.dx0[d];       // ratio 1 at AMR level 0
+                    bcl = 0.5 * (double)S.crse_ratio * S.dx0[d];
                 }
                 F.coef[0] = F.coef[1] = F.coef[2] = F.coef[3] = 0.0;
                 F.nx = 0;
@@ -275,9 +313,7 @@ PatchLevel build_patch_level (const std::vector<const SolveSpec*>& solves, int l
                     else {
                         // covered by a box of the same level (original boxes, which
                         // cover the same cells as the patches)
-                        bool cov = false;
-                        for (const auto& b : LG.boxes) { if (b.contains(c[0], c[1], c[2])) { cov = true; break; } }
-                        v = cov ? MASK_COVERED : MASK_NOT_COVERED;
+                        v = (loc.find(c[0], c[1], c[2]) >= 0) ? MASK_COVERED : MASK_NOT_COVERED;
                     }
                     m.push_back((int8_t)v);
                 }

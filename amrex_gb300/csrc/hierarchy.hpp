@@ -49,6 +49,9 @@ struct SolveSpec {
     double alpha = 0.0, beta = 1.0;
     int is_abec = 0;
     double dx0[3];                    // level-0 cell size (BC location of internal faces)
+    int crse_ratio = 1;               // refinement ratio to the next coarser AMR level (1 at AMR level 0):
+                                      // coarse/fine faces sit 0.5 * crse_ratio * dx0 outside the box
+    int amr_fine = 0;                 // a finer AMR level: one MG level that is smoothed, never bottom-solved
 };
 
 // Ghost-copy tag: copy region `box` (destination index space) of patch `dst`
@@ -77,6 +80,20 @@ struct PatchLevel {
 
 struct BoxToPatch {                        // level-0 user box -> patch location
     int patch;
+};
+
+// Which box of a BoxArray holds a cell: boxes bucketed on a coarse grid of
+// 8^3-cell buckets over their bounding box, so a query checks only the few
+// boxes that touch the cell's bucket.
+class BoxLocator {
+public:
+    explicit BoxLocator (const std::vector<Box3>& boxes);
+    int find (int i, int j, int k) const;   // box index, -1 if none
+private:
+    std::vector<Box3> m_boxes;
+    Box3 m_bb;
+    int m_nb[3] = {0, 0, 0};
+    std::vector<int> m_start, m_list;
 };
 
 // Build the patch layout of level `lev` for every solve in `solves`.

@@ -117,6 +117,7 @@ public:
     void reset_smoother_stats () { m_kstats.total_ms = 0; m_kstats.launches = 0; }
 
     struct Impl;
+    Impl& impl () { return *m_impl; }   // engine internals (AMR composite driver)
 private:
     std::vector<SolveProblem> m_problems;
     EngineOptions m_opt;

@@ -281,7 +281,7 @@ k_reduce (DevLevel L, Subset S, const T* __restrict__ x, const T* __restrict__ y
 }
 
 // one block per solve: combine the partials of blocks [begin[s], begin[s+1])
-__global__ void k_reduce_final (const double* __restrict__ partial, const int* __restrict__ begin, int op,
+static __global__ void k_reduce_final (const double* __restrict__ partial, const int* __restrict__ begin, int op,
                                 double* __restrict__ out)
 {
     __shared__ double sm[32];

@@ -37,7 +37,7 @@ struct StencilPtrs {            // per-level stencil arrays (null for constant c
 };
 
 // build D, s in FP64 from the FP64 a, bX, bY, bZ of a level; optional FP32 copies
-__global__ void __launch_bounds__(TILE_THREADS)
+static __global__ void __launch_bounds__(TILE_THREADS)
 k_build_stencil (DevLevel L, Subset S, const double* __restrict__ a, const double* __restrict__ bx,
                  const double* __restrict__ by, const double* __restrict__ bz, double* __restrict__ D,
                  double* __restrict__ sx, double* __restrict__ sy, double* __restrict__ sz,

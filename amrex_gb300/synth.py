@@ -48,6 +48,27 @@ def gaussian_rhs(n, seed, nblobs=16, wmin=0.02, wmax=0.1):
     return out
 
 
+def gaussian_rhs_box(n, seed, box, nblobs=16, wmin=0.02, wmax=0.1):
+    """``gaussian_rhs(n, seed)`` on the cells of one box ((lo, hi) or a
+    6-tuple lo+hi), shape (nz, ny, nx) of the box; the same values, bit for
+    bit, without forming the whole-domain array."""
+    n = _as3(n)
+    lo, hi = (tuple(box[:3]), tuple(box[3:])) if len(box) == 6 else (tuple(box[0]), tuple(box[1]))
+    rng = np.random.Generator(np.random.PCG64(seed))
+    c = rng.uniform(0.0, 1.0, size=(nblobs, 3))
+    w = rng.uniform(wmin, wmax, size=nblobs)
+    amp = rng.standard_normal(nblobs)
+    x, y, z = cell_centres(n)
+    x, y, z = x[lo[0]:hi[0] + 1], y[lo[1]:hi[1] + 1], z[lo[2]:hi[2] + 1]
+    out = np.zeros((len(z), len(y), len(x)), dtype=np.float64)
+    for k in range(nblobs):
+        gx = np.exp(-((x - c[k, 0]) ** 2) / (2 * w[k] ** 2))
+        gy = np.exp(-((y - c[k, 1]) ** 2) / (2 * w[k] ** 2))
+        gz = np.exp(-((z - c[k, 2]) ** 2) / (2 * w[k] ** 2))
+        out += amp[k] * gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
+    return out
+
+
 def gaussian_random_field(shape_zyx, seed, sigma_cells=5.0):
     """White noise convolved (periodically, via FFT) with a Gaussian of
     ``sigma_cells`` cells, normalised to zero mean and unit variance."""

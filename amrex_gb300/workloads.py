@@ -7,6 +7,10 @@
 * ``batch_specs(nsolve, seed)``: the batch of independent solves of uneven
   sizes -- cube edges drawn uniformly from {32, 48, ..., 128}, solve i with
   RHS and b seeds ``seed + 1 + i``.
+* ``amr_problem(n, grids, rhs_seed)``: the composite MLPoisson over AMR
+  levels (base n^3 unit cube, refinement ratio 2, level l's boxes
+  ``grids[l]``), Gaussian-blob RHS sampled at each level's cell centres,
+  homogeneous Dirichlet, zero initial guess.
 """
 from __future__ import annotations
 
@@ -62,3 +66,36 @@ def adjoint_objective(n, phi_scale, target_seed=3003):
     q = n // 4
     region = (slice(q, n - q),) * 3
     return tgt, region
+
+
+def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_grid_size=32, con_grid_size=32):
+    """Composite MLPoisson over len(grids) AMR levels: per-level geometry,
+    BoxArray, DistributionMapping, solution (1 ghost, zero) and RHS
+    MultiFabs, the operator and the MLMG solver.  ``grids[l]`` holds level l's
+    boxes as (lo0, lo1, lo2, hi0, hi1, hi2)."""
+    geoms, bas, dms, sols, rhss = [], [], [], [], []
+    for lev, g in enumerate(grids):
+        m = n << lev
+        dom = ag.Box((0, 0, 0), (m - 1, m - 1, m - 1))
+        ba = ag.BoxArray([ag.Box(b[:3], b[3:]) for b in g])
+        dm = ag.DistributionMapping(ba)
+        sol = ag.MultiFab(ba, dm, 1, 1)
+        sol.setVal(0.0)
+        rhs = ag.MultiFab(ba, dm, 1, 0)
+        for i, b in enumerate(g):
+            rhs.set_fab(i, synth.gaussian_rhs_box(m, rhs_seed, b))
+        geoms.append(ag.Geometry(dom))
+        bas.append(ba)
+        dms.append(dm)
+        sols.append(sol)
+        rhss.append(rhs)
+    info = ag.LPInfo().setAgglomerationGridSize(agg_grid_size).setConsolidationGridSize(con_grid_size)
+    op = ag.MLPoisson(geoms, bas, dms, info)
+    op.setDomainBC((ag.LinOpBCType.Dirichlet,) * 3, (ag.LinOpBCType.Dirichlet,) * 3)
+    for lev in range(len(grids)):
+        op.setLevelBC(lev, sols[lev])
+    mlmg = ag.MLMG(op)
+    mlmg.setMaxIter(max_iter)
+    mlmg.setPrecision(precision)
+    mlmg.setGraph(graph)
+    return dict(geoms=geoms, bas=bas, dms=dms, sols=sols, rhss=rhss, op=op, mlmg=mlmg)

@@ -120,7 +120,13 @@ int mlmg_multifab_norminf_noalloc(mlmg_multifab mf, double* out);
 
 /* ------------------------------------------------- linear operators -----
  * replace amrex_fi_new_poisson (Src/F_Interfaces/LinearSolvers/AMReX_poisson_fi.cpp:8-30)
- * and amrex_fi_new_abeclaplacian (AMReX_abeclaplacian_fi.cpp:8-49); nlev must be 1 */
+ * and amrex_fi_new_abeclaplacian (AMReX_abeclaplacian_fi.cpp:8-49).  geom, ba
+ * and dm hold nlev entries, one per AMR level (MLPoissonT(Vector<Geometry>,
+ * Vector<BoxArray>, ...), AMReX_MLPoisson.H:21-40).  nlev > 1 (a composite
+ * solve, up to 8 levels) is implemented for MLPoisson with refinement ratio 2
+ * on a non-periodic domain: level l's domain is level 0's refined by 2^l, its
+ * boxes coarsen by 2 and nest properly in level l-1 (a box coarsened and
+ * grown by one cell stays in level l-1 or outside the domain). */
 int mlmg_linop_new_poisson(int nlev, const mlmg_geometry* geom, const mlmg_boxarray* ba, const mlmg_distromap* dm,
                            const mlmg_lpinfo* info, mlmg_linop* out);
 int mlmg_linop_new_abeclap(int nlev, const mlmg_geometry* geom, const mlmg_boxarray* ba, const mlmg_distromap* dm,
@@ -128,7 +134,9 @@ int mlmg_linop_new_abeclap(int nlev, const mlmg_geometry* geom, const mlmg_boxar
 int mlmg_linop_delete(mlmg_linop op);
 /* amrex_fi_linop_set_domain_bc / _level_bc / _maxorder (AMReX_linop_fi.cpp:8-40) */
 int mlmg_linop_set_domain_bc(mlmg_linop op, const int lobc[3], const int hibc[3]);
-int mlmg_linop_set_level_bc(mlmg_linop op, int amrlev, mlmg_multifab levelbc);  /* NULL: homogeneous */
+/* the Dirichlet values of AMR level amrlev in its ghost cells (taken at this
+ * call); NULL: homogeneous */
+int mlmg_linop_set_level_bc(mlmg_linop op, int amrlev, mlmg_multifab levelbc);
 int mlmg_linop_set_maxorder(mlmg_linop op, int maxorder);
 /* amrex_fi_abeclap_set_scalars / _acoeffs / _bcoeffs (AMReX_abeclaplacian_fi.cpp:20-49) */
 int mlmg_abeclap_set_scalars(mlmg_linop op, double alpha, double beta);
@@ -138,6 +146,8 @@ int mlmg_abeclap_set_bcoeffs(mlmg_linop op, int amrlev, const mlmg_multifab b[3]
 int mlmg_abeclap_set_bcoeffs_const(mlmg_linop op, int amrlev, double b);
 /* number of MG levels of AMR level 0 (built from the LPInfo) */
 int mlmg_linop_num_mg_levels(mlmg_linop op);
+/* number of AMR levels (MLLinOpT::NAMRLevels, AMReX_MLLinOp.H:309) */
+int mlmg_linop_num_amr_levels(mlmg_linop op);
 
 /* ------------------------------------------------------------- solver ----
  * replace amrex_fi_new_multigrid / amrex_fi_multigrid_solve / setters
@@ -180,6 +190,17 @@ int mlmg_get_smoother_stats(mlmg_solver s, double* total_ms, long long* launches
  * right-hand side; returns a status, final_resid gets the final max-norm */
 int mlmg_solve(mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, double tol_rel, double tol_abs,
                double* final_resid);
+/* MLMGT::solve(Vector<MultiFab*>, Vector<MultiFab const*>, ...) (AMReX_MLMG.H:
+ * 353-541) and amrex_fi_multigrid_solve (AMReX_multigrid_fi.cpp:40-50): sol
+ * and rhs hold one MultiFab per AMR level of the operator, on the level's
+ * BoxArray.  The composite solve iterates MLMGT::oneIter over the levels and
+ * converges when the finest level's residual and then the masked residual of
+ * the coarser levels reach the target; final_resid gets the composite
+ * max-norm.  With one level this is mlmg_solve.  The single-level calls
+ * (mlmg_solve, mlmg_apply, fluxes, adjoint, autotune, batching) return -4 on
+ * a composite operator. */
+int mlmg_solve_levels(mlmg_solver s, const mlmg_multifab* sol, const mlmg_multifab* rhs, double tol_rel,
+                      double tol_abs, double* final_resid);
 /* MLMGT::apply (AMReX_MLMG.H:858-932): out = L(in) with the level BC values */
 int mlmg_apply(mlmg_solver s, mlmg_multifab out, mlmg_multifab in);
 /* MLMGT::getFluxes(a_flux, a_sol, loc) (AMReX_MLMG.H:627-655) and

@@ -15,8 +15,9 @@ from amrex_gb300 import synth
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 CASES = {
-    # the 3-level composite configuration: base 128^3, max_grid_size 64 (grids only)
-    "c2": dict(n=128, nlev=3, max_grid_size=64, rhs_seed=1002, solve=False),
+    # the 3-level composite configuration: base 128^3, max_grid_size 64
+    # (solution kept as per-level statistics and samples)
+    "c2": dict(n=128, nlev=3, max_grid_size=64, rhs_seed=1002, solve="summary"),
     # small composite solves for parity
     "c2_n32": dict(n=32, nlev=3, max_grid_size=16, rhs_seed=1002),
     "c2_n16_2lev": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1012),
@@ -26,6 +27,12 @@ CASES = {
 def level_rhs(case, lev):
     """RHS on the whole domain of level lev, shape (m, m, m), m = n 2^lev."""
     return synth.gaussian_rhs(case["n"] << lev, case["rhs_seed"])
+
+
+def sample_index(size, lev, count=4096):
+    """seeded sample of positions into a level's box-packed phi"""
+    rng = np.random.Generator(np.random.PCG64(7000 + lev))
+    return np.sort(rng.choice(size, size=min(count, size), replace=False))
 
 
 def parse_grids(text):

@@ -5,8 +5,9 @@
   level tags the cells where |RHS| exceeds the 90th percentile of |RHS| on
   that level (blocking factor 8, max_grid_size, n_error_buf 1, grid_eff 0.7);
 * ``amrsolve_<name>.npz``: the reference's composite multi-level MLPoisson
-  solve on those grids -- phi on every level's boxes, residual history and
-  bottom iteration counts.
+  solve on those grids -- phi on every level's boxes (for the configuration-
+  size case only per-level statistics and phi at seeded sample cells),
+  residual history and bottom iteration counts.
 
     python tests/golden/make_amr_golden.py [name-prefix ...]
 """
@@ -53,6 +54,7 @@ def make(name, case):
         print("wrote amrgrids", name, [len(g) for g in grids])
         if not case.get("solve", True):
             return
+        summary = case.get("solve") == "summary"
         lines = base + [f"tol_rel {case.get('tol_rel', 1e-10)}", "tol_abs 0.0",
                         f"agg_grid_size {case.get('agg_grid_size', 32)}",
                         f"con_grid_size {case.get('con_grid_size', 32)}"]
@@ -64,7 +66,15 @@ def make(name, case):
         for lev, g in enumerate(grids):
             m = n << lev
             phi = np.fromfile(os.path.join(d, f"phi_l{lev}.bin"), dtype=np.float64).reshape(m, m, m)
-            payload[f"phi_l{lev}"] = amr_cases.pack_boxes(phi, g)
+            flat = amr_cases.pack_boxes(phi, g)
+            if summary:
+                # too large to store: the level's max|phi|, sum and sum of
+                # squares, and phi at seeded sample cells of its boxes
+                idx = amr_cases.sample_index(flat.size, lev)
+                payload[f"phi_l{lev}_stats"] = np.array([np.abs(flat).max(), flat.sum(), (flat * flat).sum()])
+                payload[f"phi_l{lev}_sample"] = flat[idx]
+            else:
+                payload[f"phi_l{lev}"] = flat
         np.savez_compressed(os.path.join(HERE, f"amrsolve_{name}.npz"), **payload)
         print("wrote amrsolve", name)
 

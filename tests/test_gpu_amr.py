@@ -1,0 +1,111 @@
+"""GPU composite (multi-AMR-level) MLPoisson solves through the C ABI against
+the reference's own composite solves on AmrMesh grids (tests/golden/
+amrsolve_*.npz) and, at the configuration size, against per-level
+statistics and sampled values of the reference solution."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import amrex_gb300 as ag
+from amrex_gb300 import workloads
+from tests.golden import amr_cases as ac
+
+pytestmark = pytest.mark.gpu
+
+SMALL = ["c2_n16_2lev", "c2_n32"]
+
+
+def _solve(name, precision=0, graph=False, tol_rel=None):
+    g = ac.load("amrsolve", name)
+    case, grids = g["case"], g["grids"]
+    P = workloads.amr_problem(case["n"], grids, case["rhs_seed"], precision=precision, graph=graph,
+                              agg_grid_size=case.get("agg_grid_size", 32), con_grid_size=case.get("con_grid_size", 32))
+    resid = P["mlmg"].solve(P["sols"], P["rhss"], tol_rel or case.get("tol_rel", 1e-10), 0.0)
+    phis = []
+    for lev, boxes in enumerate(grids):
+        sol = P["sols"][lev]
+        phis.append(np.concatenate([sol.get_fab(i)[1:-1, 1:-1, 1:-1].ravel() for i in range(len(boxes))]))
+    return g, P, resid, phis
+
+
+@pytest.mark.parametrize("name", SMALL)
+def test_amr_fp64_matches_reference(name):
+    g, P, resid, phis = _solve(name, precision=0)
+    ref = g["result"]
+    m = P["mlmg"]
+    assert m.getNumIters() == ref["niters"]
+    assert m.getNumCGIters() == ref["cg_iters"]
+    assert m.getInitResidual() == pytest.approx(ref["init_resid"], rel=1e-12)
+    assert m.getInitRHS() == pytest.approx(ref["rhs_norm"], rel=1e-12)
+    # fine residual history: relative 1e-6 down to roundoff near 1e-10 * |rhs|
+    np.testing.assert_allclose(m.getResidualHistory(), ref["history"], rtol=1e-4, atol=1e-14 * ref["rhs_norm"])
+    assert resid <= 1e-10 * ref["rhs_norm"]
+    for lev in range(len(phis)):
+        want = g[f"phi_l{lev}"]
+        err = np.abs(phis[lev] - want).max() / np.abs(want).max()
+        assert err < 1e-10, (lev, err)
+
+
+@pytest.mark.parametrize("name", SMALL)
+@pytest.mark.parametrize("graph", [False, True])
+def test_amr_mixed_reaches_target(name, graph):
+    """FP32 corrections inside the FP64 composite residual reach the same
+    1e-10 relative composite residual; the solution agrees with the
+    reference's FP64 solution to within the discretisation-free tolerance
+    that a 1e-10 residual allows."""
+    g, P, resid, phis = _solve(name, precision=1, graph=graph)
+    ref = g["result"]
+    assert resid <= 1e-10 * ref["rhs_norm"]
+    assert P["mlmg"].getNumIters() <= ref["niters"] + 3
+    for lev in range(len(phis)):
+        want = g[f"phi_l{lev}"]
+        err = np.abs(phis[lev] - want).max() / np.abs(want).max()
+        assert err < 1e-8, (lev, err)
+
+
+def test_amr_graph_replay_matches_eager_fp64():
+    _, P0, r0, phis0 = _solve("c2_n32", precision=0, graph=False)
+    _, P1, r1, phis1 = _solve("c2_n32", precision=0, graph=True)
+    assert P0["mlmg"].getNumIters() == P1["mlmg"].getNumIters()
+    for a, b in zip(phis0, phis1):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_amr_config_size_against_reference_summary():
+    """The 3-level composite configuration (base 128^3, 57 and 495 boxes on
+    levels 1 and 2): FP64 iteration and bottom counts equal the reference's,
+    per-level statistics and sampled solution values agree to 1e-9; the mixed
+    solve reaches the same residual target and agrees to 1e-8."""
+    g = ac.load("amrsolve", "c2")
+    ref = g["result"]
+    for precision, tol in ((0, 1e-9), (1, 1e-8)):
+        _, P, resid, phis = _solve("c2", precision=precision, graph=True)
+        m = P["mlmg"]
+        assert resid <= 1e-10 * ref["rhs_norm"]
+        if precision == 0:
+            assert m.getNumIters() == ref["niters"]
+            assert m.getNumCGIters() == ref["cg_iters"]
+        for lev in range(len(phis)):
+            st = g[f"phi_l{lev}_stats"]
+            scale = st[0]
+            assert np.abs(phis[lev]).max() == pytest.approx(st[0], rel=tol)
+            idx = ac.sample_index(phis[lev].size, lev)
+            err = np.abs(phis[lev][idx] - g[f"phi_l{lev}_sample"]).max() / scale
+            assert err < tol, (precision, lev, err)
+
+
+def test_amr_rejects_unsupported_and_bad_nesting():
+    n = 16
+    grids = ac.load("amrgrids", "c2_n16_2lev")["grids"]
+    # a fine box whose coarsening grown by one leaves level 0
+    bad = [[(0, 0, 0, 7, 7, 7)], [(0, 0, 0, 15, 15, 15)]]
+    P = workloads.amr_problem(n, bad, 1012)
+    with pytest.raises(ag.MLMGError) as e:
+        P["mlmg"].solve(P["sols"], P["rhss"], 1e-10, 0.0)
+    assert e.value.code == -1
+    # single-level calls on a composite operator
+    P = workloads.amr_problem(n, grids, 1012)
+    with pytest.raises(ag.MLMGError) as e:
+        P["mlmg"].solve(P["sols"][0], P["rhss"][0], 1e-10, 0.0)
+    assert e.value.code in (-1, -4)

@@ -61,3 +61,13 @@ def test_amr_grids_are_properly_nested():
                 assert all(v % 2 == 0 for v in b[:3]) and all(v % 2 == 1 for v in b[3:])
                 blk = cov[lo[2]:hi[2] + 3, lo[1]:hi[1] + 3, lo[0]:hi[0] + 3]
                 assert blk.all(), (name, lev, b)
+
+
+def test_box_rhs_matches_whole_domain_rhs():
+    """The box-restricted RHS generator the GPU workloads use gives the
+    whole-domain generator's values bit for bit."""
+    from amrex_gb300 import synth
+    full = synth.gaussian_rhs(32, 1002)
+    for b in [(0, 0, 0, 7, 7, 7), (8, 16, 4, 23, 31, 11), (5, 3, 30, 5, 9, 31)]:
+        box = synth.gaussian_rhs_box(32, 1002, b)
+        np.testing.assert_array_equal(box, full[b[2]:b[5] + 1, b[1]:b[4] + 1, b[0]:b[3] + 1])
