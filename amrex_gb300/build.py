@@ -21,6 +21,7 @@ LIB = os.path.join(HERE, "libamrex_gb300.so")
 SOURCES = ["hierarchy.cpp", "solver.cu", "amr.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+         "-Xcompiler", "-D_GLIBCXX_ASSERTIONS",
          "--expt-relaxed-constexpr"]
 
 

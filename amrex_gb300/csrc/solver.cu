@@ -871,6 +871,10 @@ void Engine::set_coefficients ()
                     for (size_t b = 0; b < fs.boxes.size(); ++b) {
                         const Box3& vb = fs.boxes[b];
                         if ((hi ? vb.hi[d] : vb.lo[d]) != (hi ? P.hi[d] : P.lo[d])) { continue; }
+                        // only the boxes of this patch (others may share the face plane)
+                        bool inside = true;
+                        for (int e = 0; e < 3; ++e) { if (vb.lo[e] < P.lo[e] || vb.hi[e] > P.hi[e]) { inside = false; } }
+                        if (!inside) { continue; }
                         const Box3 fab = grow(vb, fs.ngrow);
                         for (int v1 = vb.lo[e1]; v1 <= vb.hi[e1]; ++v1)
                         for (int v0 = vb.lo[e0]; v0 <= vb.hi[e0]; ++v0) {
