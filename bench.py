@@ -326,6 +326,62 @@ def bench_adjoint(stream, n=128):
     return out
 
 
+def bench_amr(stream, reps=3):
+    """The 3-level AMR composite MLPoisson (base 128^3, refinement ratio 2,
+    AmrMesh grids tagged where |RHS| exceeds its 90th percentile, blocking
+    factor 8, max_grid_size 64), FP64 and mixed, CUDA-graph iterations,
+    device time per solve from a zero initial guess."""
+    import torch
+    import amrex_gb300 as ag
+    from amrex_gb300 import workloads
+    from tests.golden import amr_cases
+    g = amr_cases.load("amrgrids", "c2")
+    grids, case = g["grids"], g["case"]
+    P = workloads.amr_problem(case["n"], grids, case["rhs_seed"], precision=0, graph=True)
+    cells = [sum((b[3] - b[0] + 1) * (b[4] - b[1] + 1) * (b[5] - b[2] + 1) for b in lv) for lv in grids]
+    out = {"workload": f"3-level AMR composite MLPoisson, base {case['n']}^3, ratio 2, blocking factor 8, "
+                       f"max_grid_size {case['max_grid_size']}, levels tagged where |RHS| > p90 (seed "
+                       f"{case['rhs_seed']}), Dirichlet, tol_rel 1e-10",
+           "boxes": [len(lv) for lv in grids], "cells": cells}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    phis = {}
+    for prec in ("fp64", "mixed"):
+        m = P["mlmg"] if prec == "fp64" else ag.MLMG(P["op"])
+        m.setPrecision(prec)
+        m.setGraph(True)
+
+        def step():
+            for x in P["sols"]:
+                x.setVal(0.0)
+            return m.solve(P["sols"], P["rhss"], TOL_REL, 0.0)
+
+        step()
+        ag.kernel_launches(reset=True)
+        e0.record(stream)
+        for _ in range(reps):
+            resid = step()
+        e1.record(stream)
+        e1.synchronize()
+        out[f"{prec}_ms"] = e0.elapsed_time(e1) / reps
+        out[f"{prec}_iters"] = m.getNumIters()
+        out[f"{prec}_final_resid_rel"] = resid / m.getInitRHS()
+        out[f"{prec}_launches_per_solve"] = ag.kernel_launches() // reps
+        phis[prec] = [np.concatenate([x.get_fab(i)[1:-1, 1:-1, 1:-1].ravel() for i in range(len(lv))])
+                      for x, lv in zip(P["sols"], grids)]
+    out["speedup_mixed_vs_fp64"] = out["fp64_ms"] / out["mixed_ms"]
+    out["phi_rel_diff_mixed_vs_fp64"] = max(float(np.abs(a - b).max() / np.abs(b).max())
+                                            for a, b in zip(phis["mixed"], phis["fp64"]))
+    try:
+        ref = amr_cases.load("amrsolve", "c2")
+        out["reference_fp64_iters"] = ref["result"]["niters"]
+        out["phi_rel_diff_fp64_vs_reference_samples"] = max(
+            float(np.abs(phis["fp64"][lv][amr_cases.sample_index(phis["fp64"][lv].size, lv)]
+                         - ref[f"phi_l{lv}_sample"]).max() / ref[f"phi_l{lv}_stats"][0]) for lv in range(len(grids)))
+    except FileNotFoundError:
+        pass
+    return out
+
+
 def run_gb300(args, ws, rank, local):
     import torch
     import amrex_gb300 as ag
@@ -447,6 +503,7 @@ def run_gb300(args, ws, rank, local):
     if not args.no_batch:
         line["batch"] = bench_batch(stream)
         line["adjoint"] = bench_adjoint(stream)
+        line["amr"] = bench_amr(stream)
     if rank == 0 and ws == 1 and not args.no_cpu:
         import multiprocessing
         os.environ.setdefault("OMP_NUM_THREADS", str(multiprocessing.cpu_count()))
