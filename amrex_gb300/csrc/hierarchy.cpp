@@ -3,6 +3,8 @@
 #include "hierarchy.hpp"
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <cmath>
 #include <cstring>
 
@@ -205,6 +207,38 @@ int BoxLocator::find (int i, int j, int k) const
     return -1;
 }
 
+std::vector<Box3> merge_face_neighbours (std::vector<Box3> b)
+{
+    std::vector<char> alive(b.size(), 1);
+    bool changed = true;
+    while (changed) {
+        changed = false;
+        for (int d = 0; d < 3; ++d) {
+            const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
+            auto key = [&] (const Box3& x, int pos) {
+                return std::array<int, 5>{x.lo[t1], x.hi[t1], x.lo[t2], x.hi[t2], pos};
+            };
+            std::map<std::array<int, 5>, int> by_lo;
+            for (int i = 0; i < (int)b.size(); ++i) { if (alive[i]) { by_lo[key(b[i], b[i].lo[d])] = i; } }
+            for (int i = 0; i < (int)b.size(); ++i) {
+                if (!alive[i]) { continue; }
+                for (;;) {
+                    auto it = by_lo.find(key(b[i], b[i].hi[d] + 1));
+                    if (it == by_lo.end() || it->second == i) { break; }
+                    const int j = it->second;
+                    b[i].hi[d] = b[j].hi[d];
+                    alive[j] = 0;
+                    by_lo.erase(it);
+                    changed = true;
+                }
+            }
+        }
+    }
+    std::vector<Box3> out;
+    for (size_t i = 0; i < b.size(); ++i) { if (alive[i]) { out.push_back(b[i]); } }
+    return out;
+}
+
 PatchLevel build_patch_level (const std::vector<const SolveSpec*>& solves, int lev, bool allow_merge)
 {
     PatchLevel PL;
@@ -228,21 +262,16 @@ PatchLevel build_patch_level (const std::vector<const SolveSpec*>& solves, int l
         double dx[3], dxinv[3];
         LG.geom.cell_size(dx, dxinv);
 
-        // merge decision
+        // merge decision: boxes that share a whole face join one patch while
+        // every box is at least maxorder-1 cells long, so that each Dirichlet
+        // closure keeps its interpolation points
         std::vector<Box3> pboxes = LG.boxes;
         if (allow_merge && LG.boxes.size() > 1) {
-            Box3 bb = LG.boxes[0];
-            long long np = 0;
             int minlen = 1 << 30;
             for (const auto& b : LG.boxes) {
-                np += b.npts();
-                for (int d = 0; d < 3; ++d) {
-                    bb.lo[d] = std::min(bb.lo[d], b.lo[d]);
-                    bb.hi[d] = std::max(bb.hi[d], b.hi[d]);
-                    minlen = std::min(minlen, b.len(d));
-                }
+                for (int d = 0; d < 3; ++d) { minlen = std::min(minlen, b.len(d)); }
             }
-            if (np == bb.npts() && minlen >= S.maxorder - 1) { pboxes.assign(1, bb); }
+            if (minlen >= S.maxorder - 1) { pboxes = merge_face_neighbours(LG.boxes); }
         }
 
         PL.solve_first_patch[s] = (int)PL.patches.size();

@@ -96,9 +96,13 @@ private:
     std::vector<int> m_start, m_list;
 };
 
+// Join boxes that share a whole face, repeatedly along x, y and z, into
+// larger boxes covering the same cells (the patches of a level).
+std::vector<Box3> merge_face_neighbours (std::vector<Box3> boxes);
+
 // Build the patch layout of level `lev` for every solve in `solves`.
-// Boxes of one solve's level are merged into one patch when their union is
-// their bounding box and the merge leaves every Dirichlet closure unchanged.
+// Boxes of one solve's level that share whole faces are merged into larger
+// patches when the merge leaves every Dirichlet closure unchanged.
 PatchLevel build_patch_level (const std::vector<const SolveSpec*>& solves, int lev, bool allow_merge);
 
 // index of cell (i,j,k) of patch p
