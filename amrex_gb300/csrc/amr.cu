@@ -89,16 +89,14 @@ struct AmrEngine::Impl {
     void build_coarse_tables (int c);
 
     // operations
-    void solution_residual (int l, bool update);
+    void solution_residual (int l, bool update, double* partial = nullptr);
     void reflux (int c);
     void avgdown (int c, const double* fine, double* crse);
     template <typename T> void gather (int l, const T* crse);
     template <typename T> T* cor (int l);
     template <typename T> T* hold (int l);
-    template <typename T> T* res_t (int l);
-    template <typename T> T* rescor_t (int l);
-    template <typename T> void mini_cycle (int l, bool convert_res);
-    template <typename T> void correction_residual (int l, bool inhomog);
+    template <typename T> void mini_cycle (int l, const T* rhs);
+    template <typename T, typename TB, typename TO> void cor_residual (int l, bool inhomog, const TB* b, TO* out);
     template <typename T> void one_iter (int iter);
     void norm_start (int l, const double* x, bool masked, int slot);
     void fine_residual_and_norm ();
@@ -108,10 +106,6 @@ template <> double* AmrEngine::Impl::cor<double> (int l) { return (double*)lev[l
 template <> float* AmrEngine::Impl::cor<float> (int l) { return (float*)lev[l].cor_p; }
 template <> double* AmrEngine::Impl::hold<double> (int l) { return (double*)lev[l].hold_p; }
 template <> float* AmrEngine::Impl::hold<float> (int l) { return (float*)lev[l].hold_p; }
-template <> double* AmrEngine::Impl::res_t<double> (int l) { return L(l).res.p; }
-template <> float* AmrEngine::Impl::res_t<float> (int l) { return L(l).res32.p; }
-template <> double* AmrEngine::Impl::rescor_t<double> (int l) { return L(l).rescor.p; }
-template <> float* AmrEngine::Impl::rescor_t<float> (int l) { return L(l).rescor32.p; }
 
 // ------------------------------------------------------------------ build --
 void AmrEngine::Impl::build ()
@@ -407,7 +401,7 @@ template <> void AmrEngine::Impl::gather<float> (int l, const float* crse)
 // MLCellLinOpT::solutionResidual (AMReX_MLCellLinOp.H:1219-1236); on a fine
 // level with update, the boundary values are first refreshed from the
 // coarser level's solution (updateSolBC, :651-664)
-void AmrEngine::Impl::solution_residual (int l, bool update)
+void AmrEngine::Impl::solution_residual (int l, bool update, double* partial)
 {
     LevelData& Ld = L(l);
     AmrLevelData& D = lev[l];
@@ -425,7 +419,7 @@ void AmrEngine::Impl::solution_residual (int l, bool update)
     }
     D.I->ghost<double>(0, Ld.sol.p, true, true, bcv);
     k_residual<double, double, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res.p, Ld.sol.p,
-        Ld.rhs.p, nullptr, nullptr, nullptr, nullptr, nullptr);
+        Ld.rhs.p, nullptr, nullptr, nullptr, nullptr, partial);
     launched();
 }
 
@@ -453,27 +447,21 @@ void AmrEngine::Impl::avgdown (int c, const double* fine, double* crse)
 }
 
 // the mini-cycle of a fine AMR level (mgVcycle with one MG level,
-// AMReX_MLMG.H:1306-1415): nu1 smoothing sweeps from zero
+// AMReX_MLMG.H:1306-1415): nu1 smoothing sweeps from zero on right-hand side rhs
 template <typename T>
-void AmrEngine::Impl::mini_cycle (int l, bool convert_res)
+void AmrEngine::Impl::mini_cycle (int l, const T* rhs)
 {
-    LevelData& Ld = L(l);
-    if constexpr (std::is_same_v<T, float>) {
-        if (convert_res) {
-            k_amr_copy<float, double><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res32.p, Ld.res.p);
-            launched();
-        }
-    }
     T* x = cor<T>(l);
-    MLMG_CUDA_CHECK(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)Ld.meta.nelem, st()));
-    for (int i = 0; i < A.m_opt.nu1; ++i) { lev[l].I->smooth<T>(0, x, res_t<T>(l), i == 0); }
+    MLMG_CUDA_CHECK(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)L(l).meta.nelem, st()));
+    for (int i = 0; i < A.m_opt.nu1; ++i) { lev[l].I->smooth<T>(0, x, rhs, i == 0); }
 }
 
-// rescor = res - L(cor): homogeneous, or (inhomog) with the coarse/fine
-// values of the coarser level's correction, which gather() has just loaded
-// (updateCorBC, AMReX_MLCellLinOp.H:666-680, 1246-1270)
-template <typename T>
-void AmrEngine::Impl::correction_residual (int l, bool inhomog)
+// out = b - L(cor): homogeneous, or (inhomog) with the coarse/fine values of
+// the coarser level's correction, which gather() has just loaded
+// (MLCellLinOpT::correctionResidual with updateCorBC, AMReX_MLCellLinOp.H:
+// 666-680, 1246-1270).  L(cor) in the correction's precision.
+template <typename T, typename TB, typename TO>
+void AmrEngine::Impl::cor_residual (int l, bool inhomog, const TB* b, TO* out)
 {
     LevelData& Ld = L(l);
     AmrLevelData& D = lev[l];
@@ -490,8 +478,7 @@ void AmrEngine::Impl::correction_residual (int l, bool inhomog)
     } else {
         D.I->ghost<T>(0, x, false, true);
     }
-    k_residual<T, T, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), rescor_t<T>(l), x,
-        res_t<T>(l), nullptr, nullptr, nullptr, nullptr, nullptr);
+    k_amr_resid<T, TB, TO><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), out, x, b);
     launched();
 }
 
@@ -502,39 +489,56 @@ void AmrEngine::Impl::norm_start (int l, const double* x, bool masked, int slot)
     Engine::Impl& I = *lev[l].I;
     k_amr_norm<double><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), x,
         masked ? lev[l].covered.p : nullptr, I.partial.p);
-    k_reduce_final<<<1, 256, 0, st()>>>(I.partial.p, Ld.all.solve_begin.p, RED_MAXABS, I.red_out.p);
+    k_reduce_final<<<1, 1024, 0, st()>>>(I.partial.p, Ld.all.solve_begin.p, RED_MAXABS, I.red_out.p);
     launched(2);
     MLMG_CUDA_CHECK(cudaMemcpyAsync(h_norm.p + slot, I.red_out.p, sizeof(double), cudaMemcpyDeviceToHost, st()));
 }
 
-// MLMGT::computeResidual(finest) and its unmasked norm into h_norm[0]
+// MLMGT::computeResidual(finest) with its (unmasked) norm from the residual
+// kernel's block maxima, into h_norm[0]
 void AmrEngine::Impl::fine_residual_and_norm ()
 {
     const int fin = nl - 1;
-    solution_residual(fin, true);
-    norm_start(fin, L(fin).res.p, false, 0);
+    Engine::Impl& I = *lev[fin].I;
+    solution_residual(fin, true, I.partial.p);
+    k_reduce_final<<<1, 1024, 0, st()>>>(I.partial.p, L(fin).all.solve_begin.p, RED_MAXABS, I.red_out.p);
+    launched();
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(h_norm.p, I.red_out.p, sizeof(double), cudaMemcpyDeviceToHost, st()));
 }
 
 // MLMGT::oneIter (AMReX_MLMG.H:1227-1293) followed by the convergence
-// residual of the finest level (:436-441)
+// residual of the finest level (:436-441).  The residual a fine level ends
+// its down-sweep with (fine_res after computeResWithCrseSolFineCor) lives in
+// `dres` until the up-sweep takes it as b; the up-sweep's residual goes to a
+// second buffer, whose only reader is that level's mini-cycle.
 template <typename T>
 void AmrEngine::Impl::one_iter (int iter)
 {
     const int fin = nl - 1;
     Engine::Impl& I0 = *lev[0].I;
     I0.bslot = 0;
+    std::vector<double*> dres(nl, nullptr);
     for (int l = fin; l > 0; --l) {
         LevelData& Ld = L(l);
-        mini_cycle<T>(l, true);
-        k_add_to<double, T><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), nullptr);
+        const unsigned g = (unsigned)Ld.all.ntiles;
+        const T* rhs;
+        if constexpr (std::is_same_v<T, float>) {
+            k_amr_copy<float, double><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res32.p, Ld.res.p);
+            launched();
+            rhs = Ld.res32.p;
+            dres[l] = Ld.res.p;
+        } else {
+            rhs = Ld.res.p;
+            dres[l] = Ld.rescor.p;
+        }
+        mini_cycle<T>(l, rhs);
+        k_add_to<double, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), nullptr);
         launched();
         // computeResWithCrseSolFineCor(l-1, l), AMReX_MLMG.H:1660-1690
         solution_residual(l - 1, l - 1 > 0);
-        correction_residual<T>(l, false);
-        k_amr_copy<double, T><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res.p, rescor_t<T>(l));
-        launched();
+        cor_residual<T, T, double>(l, false, rhs, dres[l]);
         reflux(l - 1);
-        avgdown(l - 1, Ld.res.p, L(l - 1).res.p);
+        avgdown(l - 1, dres[l], L(l - 1).res.p);
         if (l != fin) { std::swap(lev[l].cor_p, lev[l].hold_p); }
     }
     {
@@ -551,32 +555,20 @@ void AmrEngine::Impl::one_iter (int iter)
         LevelData& Ld = L(l);
         AmrLevelData& D = lev[l];
         const unsigned g = (unsigned)Ld.all.ntiles;
-        // interpCorrection(l), AMReX_MLMG.H:1719-1750
+        T* hold_l = (l != fin) ? hold<T>(l) : nullptr;
+        // interpCorrection(l) (AMReX_MLMG.H:1719-1750), sol += cor, hold += cor
         gather<T>(l, cor<T>(l - 1));
         const T* cf;
         if constexpr (std::is_same_v<T, float>) { cf = D.cf32.p; } else { cf = D.cf64.p; }
-        k_amr_interp<T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), D.cfd.p, cf, cor<T>(l));
-        k_add_to<double, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), nullptr);
-        launched(2);
-        if (l != fin) {
-            k_add_to<T, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), hold<T>(l), cor<T>(l), nullptr);
-            launched();
-        }
+        k_amr_interp_add<T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), D.cfd.p, cf, cor<T>(l), Ld.sol.p, hold_l);
+        launched();
         // computeResWithCrseCorFineCor(l), AMReX_MLMG.H:1693-1715
-        if constexpr (std::is_same_v<T, float>) {
-            k_amr_copy<float, double><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res32.p, Ld.res.p);
-            launched();
-        }
-        correction_residual<T>(l, true);
-        k_amr_copy<T, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), res_t<T>(l), rescor_t<T>(l));
+        T* ures;
+        if constexpr (std::is_same_v<T, float>) { ures = Ld.rescor32.p; } else { ures = Ld.res.p; }
+        cor_residual<T, double, T>(l, true, dres[l], ures);
+        mini_cycle<T>(l, ures);
+        k_amr_finish<T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), hold_l);
         launched();
-        mini_cycle<T>(l, false);
-        k_add_to<double, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), nullptr);
-        launched();
-        if (l != fin) {
-            k_add_to<T, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), cor<T>(l), hold<T>(l), nullptr);
-            launched();
-        }
     }
     // averageDownAndSync, AMReX_MLCellLinOp.H:2102-2122
     for (int l = fin; l > 0; --l) { avgdown(l - 1, L(l).sol.p, L(l - 1).sol.p); }

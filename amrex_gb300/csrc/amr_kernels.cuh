@@ -63,43 +63,6 @@ __global__ void k_amr_avgdown (DevLevel Lc, DevLevel Lf, const CopyTag* __restri
     crse[cidx(Lc.P[C.dst], i, j, k)] = TD(0.125 * v);
 }
 
-// fine = trilinear prolongation of the coarse buffer (mlmg_lin_cc_interp_r2,
-// AMReX_MLMG_3D_K.H:7-37) over every valid cell of the fine level:
-// MLCellLinOpT::interpolationAmr (AMReX_MLCellLinOp.H:1094-1181).
-template <typename T>
-__global__ void __launch_bounds__(TILE_THREADS)
-k_amr_interp (DevLevel Lf, Subset Sf, const PatchDesc* __restrict__ cfd, const T* __restrict__ cf,
-              T* __restrict__ fine)
-{
-    const TileCoord c = decode_tile(Lf, Sf, blockIdx.x);
-    const PatchDesc& F = Lf.P[c.p];
-    const PatchDesc& G = cfd[c.p];
-    const int j = c.y0 + threadIdx.y;
-    if (j > F.hi[1]) { return; }
-    const long long gx = 1, gy = G.sx, gz = G.sxy;
-    for (int kk = 0; kk < TILE_Z; ++kk) {
-        const int k = c.z0 + kk;
-        if (k > F.hi[2]) { break; }
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int i = c.x0 + threadIdx.x + 32 * h;
-            if (i > F.hi[0]) { continue; }
-            const int ic = i >> 1, jc = j >> 1, kc = k >> 1;
-            const long long di = (i & 1) ? gx : -gx, dj = (j & 1) ? gy : -gy, dk = (k & 1) ? gz : -gz;
-            const long long q = cidx(G, ic, jc, kc);
-            const T v = T(0.421875) * cf[q]
-                      + T(0.140625) * cf[q + di]
-                      + T(0.140625) * cf[q + dj]
-                      + T(0.140625) * cf[q + dk]
-                      + T(0.046875) * cf[q + dj + dk]
-                      + T(0.046875) * cf[q + di + dk]
-                      + T(0.046875) * cf[q + di + dj]
-                      + T(0.015625) * cf[q + di + dj + dk];
-            fine[cidx(F, i, j, k)] = v;
-        }
-    }
-}
-
 // bits of the per-face-cell neighbourhood flags of the boundary interpolation
 enum : int {
     BF_SELF = 1,        // the ghost cell itself is not covered (a coarse/fine cell)
@@ -253,6 +216,98 @@ k_amr_norm (DevLevel L, Subset S, const T* __restrict__ x, const int8_t* __restr
     }
     const double red = block_reduce(acc, RED_MAXABS, sm);
     if (threadIdx.x == 0 && threadIdx.y == 0) { partial[blockIdx.x] = red; }
+}
+
+// r = b - A x over valid cells (MLPoisson, BCs already in x's ghosts), with A x
+// evaluated in x's precision: the correction residuals of the composite
+// iteration, b and r in either precision
+template <typename TX, typename TB, typename TO>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_amr_resid (DevLevel L, Subset S, TO* __restrict__ r, const TX* __restrict__ x, const TB* __restrict__ b)
+{
+    const TileCoord c = decode_tile(L, S, blockIdx.x);
+    const PatchDesc& P = L.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    if (j > P.hi[1]) { return; }
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > P.hi[2]) { break; }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = c.x0 + threadIdx.x + 32 * h;
+            if (i > P.hi[0]) { continue; }
+            const long long q = cidx(P, i, j, k);
+            const TX ax = adotx_cell<TX, false>(P, q, x, nullptr, nullptr, nullptr, nullptr);
+            r[q] = TO(TX(b[q]) - ax);
+        }
+    }
+}
+
+// fine = trilinear prolongation of the coarse buffer (mlmg_lin_cc_interp_r2,
+// AMReX_MLMG_3D_K.H:7-37; MLCellLinOpT::interpolationAmr,
+// AMReX_MLCellLinOp.H:1094-1181), then sol += fine and,
+// for an intermediate level, hold += fine (MLMGT::oneIter's up-sweep,
+// AMReX_MLMG.H:1266-1276)
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_amr_interp_add (DevLevel Lf, Subset Sf, const PatchDesc* __restrict__ cfd, const T* __restrict__ cf,
+                  T* __restrict__ fine, double* __restrict__ sol, T* __restrict__ hold)
+{
+    const TileCoord c = decode_tile(Lf, Sf, blockIdx.x);
+    const PatchDesc& F = Lf.P[c.p];
+    const PatchDesc& G = cfd[c.p];
+    const int j = c.y0 + threadIdx.y;
+    if (j > F.hi[1]) { return; }
+    const long long gx = 1, gy = G.sx, gz = G.sxy;
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > F.hi[2]) { break; }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = c.x0 + threadIdx.x + 32 * h;
+            if (i > F.hi[0]) { continue; }
+            const int ic = i >> 1, jc = j >> 1, kc = k >> 1;
+            const long long di = (i & 1) ? gx : -gx, dj = (j & 1) ? gy : -gy, dk = (k & 1) ? gz : -gz;
+            const long long q = cidx(G, ic, jc, kc);
+            const T v = T(0.421875) * cf[q]
+                      + T(0.140625) * cf[q + di]
+                      + T(0.140625) * cf[q + dj]
+                      + T(0.140625) * cf[q + dk]
+                      + T(0.046875) * cf[q + dj + dk]
+                      + T(0.046875) * cf[q + di + dk]
+                      + T(0.046875) * cf[q + di + dj]
+                      + T(0.015625) * cf[q + di + dj + dk];
+            const long long qf = cidx(F, i, j, k);
+            fine[qf] = v;
+            sol[qf] += double(v);
+            if (hold != nullptr) { hold[qf] += v; }
+        }
+    }
+}
+
+// sol += cor and, for an intermediate level, cor += hold (the end of the
+// up-sweep at one level, AMReX_MLMG.H:1283-1289)
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_amr_finish (DevLevel L, Subset S, double* __restrict__ sol, T* __restrict__ cor, const T* __restrict__ hold)
+{
+    const TileCoord c = decode_tile(L, S, blockIdx.x);
+    const PatchDesc& P = L.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    if (j > P.hi[1]) { return; }
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > P.hi[2]) { break; }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = c.x0 + threadIdx.x + 32 * h;
+            if (i > P.hi[0]) { continue; }
+            const long long q = cidx(P, i, j, k);
+            const T v = cor[q];
+            sol[q] += double(v);
+            if (hold != nullptr) { cor[q] = v + hold[q]; }
+        }
+    }
 }
 
 // dst = src over valid cells, with precision conversion
