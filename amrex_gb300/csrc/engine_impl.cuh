@@ -7,6 +7,7 @@
 #include "bottom.cuh"
 #include "stencil_kernels.cuh"
 #include "fused_sweep.cuh"
+#include "fused_sweep2.cuh"
 #include "march_sweep.cuh"
 #include "coarse_vcycle.cuh"
 #include "adjoint_kernels.cuh"

@@ -1,0 +1,239 @@
+// Fused two-colour Gauss-Seidel sweep, second form: one code path for every
+// tile, little integer work per cell.
+//
+// Same arithmetic and the same staging as k_sweep_fused (fused_sweep.cuh):
+// phi_in on the 32x8x8 tile grown by two cells in shared memory (A), the
+// first colour ((i+j+k) even) on the tile grown by one (N), the second colour
+// on the tile, both written out of place.  What differs:
+//
+// * Patch faces are handled by rewriting ghost values in shared memory
+//   instead of testing every cell: after staging, the ghost layer next to each
+//   patch face inside the tile gets the closure of the two cells next to the
+//   face (what applyBC stores before the first colour pass); after the first
+//   colour, the same layer of N gets the closure of the current values (what
+//   applyBC stores before the second pass: new first-colour values, old
+//   second-colour values).  Both colour loops then read neighbours without
+//   branches.  Cells of the tile + 1 outside the patch are not updated.
+// * Tiles that touch no patch face (block-uniform flag) skip the inside test
+//   and the smoother's boundary correction, which every other tile evaluates
+//   with six register comparisons in tile-local coordinates.
+// * Thread -> cell maps advance incrementally (no division per cell); global
+//   offsets are 32-bit from the tile's first cell; each thread writes one
+//   8-byte pair (one cell of each colour).
+#pragma once
+
+#include "fused_sweep.cuh"
+
+namespace mlmg {
+
+template <bool VARC>
+__global__ void __launch_bounds__(FS_THREADS, 5)
+k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
+                const float* __restrict__ rhs, StencilPtrs Sc)
+{
+    __shared__ __align__(16) float A[FS_AZ][FS_AY][FS_AX];   // phi_in, local (x-4..x+35, y-2..y+9, z-2..z+9)
+    __shared__ float N[FS_NZ][FS_NY][FS_NX];                  // first colour, local (x-1..x+32, y-1..y+8, z-1..z+8)
+    __shared__ PatchLite SP;
+
+    const int tid = threadIdx.y * FS_TX + threadIdx.x;
+    int x0, y0, z0;
+    {
+        const TileCoord c = decode_fused_tile(L, S, blockIdx.x);
+        x0 = c.x0; y0 = c.y0; z0 = c.z0;
+        if (tid == 0) {
+            const PatchDesc& P = L.P[c.p];
+            for (int d = 0; d < 3; ++d) { SP.lo[d] = P.lo[d]; SP.hi[d] = P.hi[d]; }
+            SP.sx = P.sx; SP.sxy = P.sxy; SP.base = P.base;
+            SP.dhx = float(P.dha[0]); SP.dhy = float(P.dha[1]); SP.dhz = float(P.dha[2]);
+            for (int f = 0; f < 6; ++f) {
+                SP.f[f].type = P.face[f].type;
+                SP.f[f].nx = P.face[f].nx;
+                SP.f[f].c1 = float(P.face[f].coef[1]);
+                SP.f[f].c2 = float(P.face[f].coef[2]);
+                SP.f[f].fco = float(P.face[f].fco);
+            }
+        }
+    }
+    __syncthreads();
+    const PatchLite& P = SP;
+    // patch bounds in tile-local coordinates (lo <= 0 since tiles start inside the patch)
+    const int pxl = P.lo[0] - x0, pxh = P.hi[0] - x0;
+    const int pyl = P.lo[1] - y0, pyh = P.hi[1] - y0;
+    const int pzl = P.lo[2] - z0, pzh = P.hi[2] - z0;
+    // the tile + 1 holds a face cell of the patch (or reaches past it)
+    const bool touches = (pxl >= -1) || (pxh <= FS_TX) || (pyl >= -1) || (pyh <= FS_TY) || (pzl >= -1) ||
+                         (pzh <= FS_TZ);
+
+    // ---- stage phi_in: 12 x 12 rows of 10 16-byte chunks; 250 threads, (ly, lz) advanced incrementally
+    constexpr int CH = FS_AX / 4;                    // 10
+    constexpr int RSTEP = (FS_THREADS / CH);         // 25 rows per round
+    if (tid < RSTEP * CH) {
+        const int ch = tid % CH;
+        int ly = (tid / CH) % FS_AY, lz = (tid / CH) / FS_AY;
+        const int i = x0 - 4 + 4 * ch;
+        const bool x_ok = (i + 3 >= P.lo[0]) && (i <= P.hi[0]);
+        for (int row = tid / CH; row < FS_AZ * FS_AY; row += RSTEP) {
+            const int j = y0 - 2 + ly, k = z0 - 2 + lz;
+            float* dst = &A[lz][ly][4 * ch];
+            if (x_ok && j >= P.lo[1] && j <= P.hi[1] && k >= P.lo[2] && k <= P.hi[2]) {
+                cp_async16(dst, phi_in + P.idx(i, j, k));
+            } else {
+                *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+            ly += RSTEP % FS_AY; lz += RSTEP / FS_AY;
+            if (ly >= FS_AY) { ly -= FS_AY; lz += 1; }
+        }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+
+    // local (lx, ly, lz) -> A / N element, and the patch-inside test
+    auto aat = [&] (int lx, int ly, int lz) -> float& { return A[lz + 2][ly + 2][lx + 4]; };
+    auto nat = [&] (int lx, int ly, int lz) -> float& { return N[lz + 1][ly + 1][lx + 1]; };
+
+    // ghost layers of the patch faces inside the tile + 1 region (lx in -1..32,
+    // ly, lz in -1..8), restricted to the patch's extent along the face.
+    // fn(face, ghost, face cell, inner cell) with local coordinates.
+    auto for_face_ghosts = [&] (auto&& fn) {
+        const int lim[3] = {FS_TX, FS_TY, FS_TZ};
+        const int plo[3] = {pxl, pyl, pzl}, phi[3] = {pxh, pyh, pzh};
+        for (int f = 0; f < 6; ++f) {
+            const int d = f % 3;
+            const int g = (f < 3) ? plo[d] - 1 : phi[d] + 1;
+            if (g < -1 || g > lim[d]) { continue; }
+            const int s = (f < 3) ? 1 : -1;          // from the ghost into the patch
+            const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
+            const int a1 = max(-1, plo[t1]), b1 = min(lim[t1], phi[t1]);
+            const int a2 = max(-1, plo[t2]), b2 = min(lim[t2], phi[t2]);
+            const int n1 = b1 - a1 + 1, n2 = b2 - a2 + 1;
+            if (n1 <= 0 || n2 <= 0) { continue; }
+            for (int u = tid; u < n1 * n2; u += FS_THREADS) {
+                int c[3];
+                c[d] = g; c[t1] = a1 + u % n1; c[t2] = a2 + u / n1;
+                int cf[3] = {c[0], c[1], c[2]}, ci[3] = {c[0], c[1], c[2]};
+                cf[d] += s; ci[d] += 2 * s;
+                fn(f, c, cf, ci);
+            }
+        }
+    };
+
+    if (touches) {
+        // applyBC before the first colour: closure of the old values
+        for_face_ghosts([&] (int f, const int* c, const int* cf, const int* ci) {
+            aat(c[0], c[1], c[2]) = P.closure(f, aat(cf[0], cf[1], cf[2]), aat(ci[0], ci[1], ci[2]));
+        });
+        __syncthreads();
+    }
+
+    const long long q0 = P.idx(x0, y0, z0);
+    const int sx = P.sx, sxy = (int)P.sxy;
+    const float* __restrict__ rh = rhs + q0;
+    const float *Dp = nullptr, *SXp = nullptr, *SYp = nullptr, *SZp = nullptr;
+    if constexpr (VARC) {
+        Dp = static_cast<const float*>(Sc.D) + q0;
+        SXp = static_cast<const float*>(Sc.sx) + q0;
+        SYp = static_cast<const float*>(Sc.sy) + q0;
+        SZp = static_cast<const float*>(Sc.sz) + q0;
+    }
+    const float cdx = -P.dhx, cdy = -P.dhy, cdz = -P.dhz, cd = -2.0f * (P.dhx + P.dhy + P.dhz);
+    const float fco0 = P.f[0].fco, fco1 = P.f[1].fco, fco2 = P.f[2].fco;
+    const float fco3 = P.f[3].fco, fco4 = P.f[4].fco, fco5 = P.f[5].fco;
+    // Gauss-Seidel update of local cell (lx, ly, lz) at global offset o from q0
+    auto update = [&] (int lx, int ly, int lz, int o, float pc, float xm, float xp, float ym, float yp, float zm,
+                       float zp) {
+        float d, sxl, sxh, syl, syh, szl, szh;
+        if constexpr (VARC) {
+            d = __ldg(Dp + o);
+            sxl = __ldg(SXp + o); sxh = __ldg(SXp + o + 1);
+            syl = __ldg(SYp + o); syh = __ldg(SYp + o + sx);
+            szl = __ldg(SZp + o); szh = __ldg(SZp + o + sxy);
+        } else {
+            d = cd; sxl = sxh = cdx; syl = syh = cdy; szl = szh = cdz;
+        }
+        float gmd = d;
+        if (touches) {
+            float corr = 0.0f;
+            if (lx == pxl) { corr += sxl * fco0; }
+            if (lx == pxh) { corr += sxh * fco3; }
+            if (ly == pyl) { corr += syl * fco1; }
+            if (ly == pyh) { corr += syh * fco4; }
+            if (lz == pzl) { corr += szl * fco2; }
+            if (lz == pzh) { corr += szh * fco5; }
+            gmd = d - corr;
+        }
+        const float rho = sxl * xm + sxh * xp + syl * ym + syh * yp + szl * zm + szh * zp;
+        const float res = __ldg(rh + o) - (d * pc - rho);
+        return pc + relax_factor(gmd) * res;
+    };
+
+    // ---- first colour on the tile + 1: 17 cells per row, 10 x 10 rows;
+    // 255 threads = 17 columns x 15 row streams
+    {
+        constexpr int RS = FS_THREADS / FS_RED_ROW;      // 15
+        const int par0 = (x0 - 1 + y0 - 1 + z0 - 1) & 1;  // parity of local (-1, -1, -1)
+        if (tid < RS * FS_RED_ROW) {
+            const int r = tid % FS_RED_ROW;
+            int ry = (tid / FS_RED_ROW) % FS_NY, rz = (tid / FS_RED_ROW) / FS_NY;   // row indices 0..9
+            for (int row = tid / FS_RED_ROW; row < FS_NZ * FS_NY; row += RS) {
+                const int ly = ry - 1, lz = rz - 1;
+                // (x+y+z) even: local lx = 2r - 1 + ((par0 + ry + rz) & 1)
+                const int lx = 2 * r - 1 + ((par0 + ry + rz) & 1);
+                const bool in = !touches || (lx >= pxl && lx <= pxh && ly >= pyl && ly <= pyh && lz >= pzl &&
+                                             lz <= pzh);
+                if (in) {
+                    const int o = lz * sxy + ly * sx + lx;
+                    nat(lx, ly, lz) = update(lx, ly, lz, o, aat(lx, ly, lz), aat(lx - 1, ly, lz), aat(lx + 1, ly, lz),
+                                             aat(lx, ly - 1, lz), aat(lx, ly + 1, lz), aat(lx, ly, lz - 1),
+                                             aat(lx, ly, lz + 1));
+                }
+                ry += RS % FS_NY; rz += RS / FS_NY;
+                if (ry >= FS_NY) { ry -= FS_NY; rz += 1; }
+            }
+        }
+    }
+    __syncthreads();
+    if (touches) {
+        // applyBC before the second colour: closure of the current values
+        // (new first-colour values in N, old second-colour values in A)
+        const int par0 = (x0 + y0 + z0) & 1;      // parity of local (0, 0, 0)
+        auto cur = [&] (const int* c) -> float {
+            return (((par0 + c[0] + c[1] + c[2]) & 1) == 0) ? nat(c[0], c[1], c[2]) : aat(c[0], c[1], c[2]);
+        };
+        for_face_ghosts([&] (int f, const int* c, const int* cf, const int* ci) {
+            nat(c[0], c[1], c[2]) = P.closure(f, cur(cf), cur(ci));
+        });
+        __syncthreads();
+    }
+
+    // ---- second colour on the tile; each thread writes one (even x, odd x)
+    // pair: 16 pairs per row, 8 x 8 rows, 4 rounds
+    {
+        const int r = tid % (FS_TX / 2);
+        const int ly = (tid / (FS_TX / 2)) % FS_TY;
+        const int lzs = (tid / (FS_TX / 2)) / FS_TY;     // 0..1
+        const int par0 = (x0 + y0 + z0) & 1;
+#pragma unroll
+        for (int lz = lzs; lz < FS_TZ; lz += 2) {
+            const int lxe = 2 * r;                       // pair (lxe, lxe + 1)
+            const bool first_at_even = ((par0 + lxe + ly + lz) & 1) == 0;
+            const int lx2 = first_at_even ? lxe + 1 : lxe;   // the second-colour cell of the pair
+            const int o = lz * sxy + ly * sx + lx2;
+            const bool in2 = !touches || (lx2 <= pxh && ly <= pyh && lz <= pzh);
+            float v2 = 0.0f;
+            if (in2) {
+                v2 = update(lx2, ly, lz, o, aat(lx2, ly, lz), nat(lx2 - 1, ly, lz), nat(lx2 + 1, ly, lz),
+                            nat(lx2, ly - 1, lz), nat(lx2, ly + 1, lz), nat(lx2, ly, lz - 1), nat(lx2, ly, lz + 1));
+            }
+            const int lx1 = first_at_even ? lxe : lxe + 1;
+            const float v1 = nat(lx1, ly, lz);
+            const long long qp = q0 + (long long)(lz * sxy + ly * sx + lxe);
+            if (!touches || (lxe + 1 <= pxh && ly <= pyh && lz <= pzh)) {
+                *reinterpret_cast<float2*>(phi_out + qp) = first_at_even ? make_float2(v1, v2) : make_float2(v2, v1);
+            } else if (lxe <= pxh && ly <= pyh && lz <= pzh) {
+                phi_out[qp] = first_at_even ? v1 : v2;
+            }
+        }
+    }
+}
+
+} // namespace mlmg

@@ -479,6 +479,12 @@ void Engine::Impl::smooth_fused (int l, int n)
                 k_sweep_march<false><<<L.mz.ntiles, blk, march_smem_floats(false) * sizeof(float), st()>>>(
                     L.dl, L.mz.dev(), a, b, L.res32.p, S, E.m_opt.march_tz);
             }
+        } else if (E.m_opt.fused_v2) {
+            if (abec) {
+                k_sweep_fused2<true><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);
+            } else {
+                k_sweep_fused2<false><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);
+            }
         } else if (abec) {
             k_sweep_fused<true><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);
         } else {

@@ -71,6 +71,7 @@ k_build_stencil (DevLevel L, Subset S, const double* __restrict__ a, const doubl
             if (i == P.hi[0]) { put(sx, sx32, q + 1, dhx * bx[q + 1]); }
             if (j == P.hi[1]) { put(sy, sy32, q + P.sx, dhy * by[q + P.sx]); }
             if (k == P.hi[2]) { put(sz, sz32, q + P.sxy, dhz * bz[q + P.sxy]); }
+
         }
     }
 }

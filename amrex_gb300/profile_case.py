@@ -86,12 +86,19 @@ def main():
     for kv in args.opt:
         k, v = kv.split("=")
         m.setOption(k, float(v))
+    m.setTimeKernels(True)
     for s in range(args.solves):
         sol.setVal(0.0)
         t = time.perf_counter()
         r = m.solve(sol, rhs, 1e-10, 0.0)
         print(f"solve {s}: {m.getNumIters()} iters, resid {r:.3e}, device {m.solveTimeMs():.2f} ms, "
               f"wall {(time.perf_counter() - t) * 1e3:.2f} ms")
+        if s == 0:
+            m.smootherStats(reset=True)
+    ms, n_l, nbytes = m.smootherStats(reset=True)
+    if n_l:
+        print(f"finest-level smoother: {n_l} launches, {ms / n_l * 1e3:.1f} us each, "
+              f"{nbytes / (ms / n_l * 1e-3) / 1e9:.0f} GB/s algorithmic")
     print("kernel launches:", ag.kernel_launches())
     return 0
 
