@@ -711,6 +711,7 @@ void AmrEngine::solve (const std::vector<const FabSet*>& sol_in, const std::vect
         if (!converged && R.status == OK && m_opt.fixed_iter == 0) { R.status = NOT_CONVERGED; }
     }
     MLMG_CUDA_CHECK(cudaEventRecord(M.ev1, m_stream));
+    M.lev[0].I->check_device_error();
     if (m_opt.verbose >= 1) {
         std::printf("MLMG: Final Iter. %d resid, resid/bnorm = %.10g, %.10g\n", R.niters, R.final_resid,
                     R.final_resid / max_norm);

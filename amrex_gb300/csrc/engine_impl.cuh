@@ -84,6 +84,7 @@ struct LevelData {
     // fused two-colour sweeps (mixed path): tile map and the second buffer
     bool fused = false;
     SubsetData fz;
+    DevBuf<CUtensorMap> tm_a, tm_b;   // per patch: tensor maps of the 40x12x12 staging box over cor32 / cor32b
     bool march = false;           // fused sweeps by the z-marching kernel
     SubsetData mz;
     DevBuf<float> cor32b;
@@ -110,6 +111,7 @@ struct Engine::Impl {
     std::vector<double> volinv0, volinv_bottom;
     DevBuf<double> partial, red_out, volinv0_d;
     DevBuf<int> active_d, bot_iters, bot_ret;
+    DevBuf<int> err_d;           // device-side error report of bounded waits (0: none)
     PinnedBuf<double> h_red;
     PinnedBuf<int> h_iters;
     DevBuf<BottomLevelPtrs> bot_levels;
@@ -194,6 +196,18 @@ struct Engine::Impl {
     void resid32 (int l, float* rescor, float* cor, const float* res);
     void residual0 (bool to32);   // res[0] (FP64, or FP32 in mixed) and per-block max|r|
     void one_iteration (bool fmg);
+    // reads (and clears) the device-side error report of bounded waits; throws if set
+    void check_device_error ()
+    {
+        int h = 0;
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(&h, err_d.p, sizeof(int), cudaMemcpyDeviceToHost, st()));
+        MLMG_CUDA_CHECK(cudaStreamSynchronize(st()));
+        if (h != 0) {
+            MLMG_CUDA_CHECK(cudaMemsetAsync(err_d.p, 0, sizeof(int), st()));
+            MLMG_REQUIRE(h != tma::ERR_TMA_TIMEOUT, ERR_TIMEOUT, "a fused-sweep tile's TMA copy did not complete");
+            MLMG_REQUIRE(false, ERR_INTERNAL, "a fused-sweep tile's TMA box was not 16-byte aligned");
+        }
+    }
 };
 
 static const dim3 kTileBlock(32, TILE_Y);

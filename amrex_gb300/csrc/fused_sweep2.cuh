@@ -23,23 +23,36 @@
 #pragma once
 
 #include "fused_sweep.cuh"
+#include "tma.cuh"
 
 namespace mlmg {
 
-template <bool VARC>
+//
+// With TMA, phi_in is staged by one Tensor Memory Accelerator load per tile
+// (cp.async.bulk.tensor.3d) instead of 16-byte cp.async copies: a 3-D tensor
+// map over the patch's allocation (x with its row padding, y and z with their
+// ghost layers) delivers the 40 x 12 x 12 box into A and signals an mbarrier.
+// The box's x coordinate (x0 - lo + 4) is a multiple of 4 floats, so the copy
+// starts on a 16-byte boundary (checked; a violation is reported in *err and
+// the copy is not issued).  Cells of the box outside the patch hold whatever
+// the allocation holds there (zero past its end): the sweep reads them only
+// through the ghost layers it rewrites.  The wait is bounded; on expiry the
+// block reports ERR_TMA_TIMEOUT, waits once more (bounded) for its copy and
+// leaves.
+template <bool VARC, bool TMA = false>
 __global__ void __launch_bounds__(FS_THREADS, 5)
 k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
-                const float* __restrict__ rhs, StencilPtrs Sc)
+                const float* __restrict__ rhs, StencilPtrs Sc, const CUtensorMap* __restrict__ maps, int* err)
 {
-    __shared__ __align__(16) float A[FS_AZ][FS_AY][FS_AX];   // phi_in, local (x-4..x+35, y-2..y+9, z-2..z+9)
+    __shared__ __align__(128) float A[FS_AZ][FS_AY][FS_AX];   // phi_in, local (x-4..x+35, y-2..y+9, z-2..z+9)
     __shared__ float N[FS_NZ][FS_NY][FS_NX];                  // first colour, local (x-1..x+32, y-1..y+8, z-1..z+8)
     __shared__ PatchLite SP;
 
     const int tid = threadIdx.y * FS_TX + threadIdx.x;
-    int x0, y0, z0;
+    int x0, y0, z0, pid;
     {
         const TileCoord c = decode_fused_tile(L, S, blockIdx.x);
-        x0 = c.x0; y0 = c.y0; z0 = c.z0;
+        x0 = c.x0; y0 = c.y0; z0 = c.z0; pid = c.p;
         if (tid == 0) {
             const PatchDesc& P = L.P[c.p];
             for (int d = 0; d < 3; ++d) { SP.lo[d] = P.lo[d]; SP.hi[d] = P.hi[d]; }
@@ -64,6 +77,27 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
     const bool touches = (pxl >= -1) || (pxh <= FS_TX) || (pyl >= -1) || (pyh <= FS_TY) || (pzl >= -1) ||
                          (pzh <= FS_TZ);
 
+    if constexpr (TMA) {
+        __shared__ unsigned long long bar;
+        const int cx = x0 - P.lo[0] + XOFF - 4, cy = y0 - P.lo[1] - 1, cz = z0 - P.lo[2] - 1;
+        const bool aligned = (cx & 3) == 0;
+        if (tid == 0) { tma::mbar_init(&bar, 1); }
+        __syncthreads();
+        if (!aligned) {
+            if (tid == 0) { atomicExch(err, tma::ERR_TMA_ALIGN); }
+            return;
+        }
+        if (tid == 0) {
+            tma::mbar_expect_tx(&bar, (unsigned)sizeof(A));
+            tma::load_3d(&A[0][0][0], maps + pid, &bar, cx, cy, cz);
+        }
+        const bool late = !tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
+        if (__syncthreads_or(late)) {
+            if (tid == 0) { atomicExch(err, tma::ERR_TMA_TIMEOUT); }
+            tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
+            return;
+        }
+    } else {
     // ---- stage phi_in: 12 x 12 rows of 10 16-byte chunks; 250 threads, (ly, lz) advanced incrementally
     constexpr int CH = FS_AX / 4;                    // 10
     constexpr int RSTEP = (FS_THREADS / CH);         // 25 rows per round
@@ -86,6 +120,7 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
     }
     cp_async_wait_all();
     __syncthreads();
+    }
 
     // local (lx, ly, lz) -> A / N element, and the patch-inside test
     auto aat = [&] (int lx, int ly, int lz) -> float& { return A[lz + 2][ly + 2][lx + 4]; };

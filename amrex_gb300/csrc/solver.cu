@@ -1,11 +1,51 @@
 // The batched MLMG engine: host orchestration of the V-cycle stages.
 #include "engine_impl.cuh"
 
+#include <cudaTypedefs.h>
+
 #include <cmath>
 #include <cstring>
 
 namespace mlmg {
 
+
+// ------------------------------------------------------------ tensor maps --
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder ()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (fn == nullptr) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        MLMG_CUDA_CHECK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        MLMG_REQUIRE(q == cudaDriverEntryPointSuccess && p != nullptr, ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// 3-D tiled tensor map over the allocation of patch P inside an FP32 level
+// field: x over the whole padded row (sx), y and z over the rows and planes
+// with their ghost layers; box = the fused sweep's staging box
+CUtensorMap patch_tensor_map (const float* field, const PatchDesc& P)
+{
+    const long long start = P.base - P.sxy - P.sx - XOFF;      // first element of the patch's allocation
+    const int ny = P.hi[1] - P.lo[1] + 1, nz = P.hi[2] - P.lo[2] + 1;
+    MLMG_REQUIRE(start % 4 == 0 && P.sx % 4 == 0 && P.sxy % 4 == 0, ERR_INTERNAL, "patch layout not 16-byte aligned");
+    cuuint64_t dims[3] = {(cuuint64_t)P.sx, (cuuint64_t)(ny + 2), (cuuint64_t)(nz + 2)};
+    cuuint64_t strides[2] = {(cuuint64_t)P.sx * sizeof(float), (cuuint64_t)P.sxy * sizeof(float)};
+    cuuint32_t box[3] = {(cuuint32_t)FS_AX, (cuuint32_t)FS_AY, (cuuint32_t)FS_AZ};
+    cuuint32_t estride[3] = {1, 1, 1};
+    CUtensorMap m;
+    const CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+        const_cast<float*>(field + start), dims, strides, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    MLMG_REQUIRE(r == CUDA_SUCCESS, ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return m;
+}
+
+} // namespace
 
 // -------------------------------------------------------------- fields ----
 template <> double* Engine::Impl::field_cor<double> (int l) { return lev[l].cor.p; }
@@ -154,7 +194,19 @@ void Engine::Impl::build ()
             alloc0(L.cor); if (l > 0) { alloc0(L.res); } alloc0(L.rescor);
         }
         if (L.has_bottom) { for (auto& b : L.bw) { alloc0(b); } }
+        // tensor maps of the fused sweep's TMA staging, one per patch of the level
+        if (L.fused && !L.march && E.m_opt.fused_v2 && E.m_opt.fused_tma) {
+            std::vector<CUtensorMap> ta(M.patches.size()), tb(M.patches.size());
+            for (size_t p = 0; p < M.patches.size(); ++p) {
+                ta[p] = patch_tensor_map(L.cor32.p, M.patches[p]);
+                tb[p] = patch_tensor_map(L.cor32b.p, M.patches[p]);
+            }
+            L.tm_a.upload(ta, st());
+            L.tm_b.upload(tb, st());
+        }
     }
+    err_d.alloc(1);
+    err_d.zero(st());
     partial.alloc(max_tiles + 1);
     red_out.alloc((size_t)nsolve * 4 + 4);
     h_red.alloc((size_t)nsolve * 4 + 4);
@@ -467,6 +519,9 @@ void Engine::Impl::smooth_fused (int l, int n)
     const bool timed = E.m_opt.time_kernels && l == 0;
     float* a = L.cor32.p;
     float* b = L.cor32b.p;
+    const CUtensorMap* ma = L.tm_a.p;      // tensor maps over a and b (TMA staging)
+    const CUtensorMap* mb = L.tm_b.p;
+    const bool use_tma = ma != nullptr;
     const StencilPtrs S = stencil32(l);
     for (int i = 0; i < n; ++i) {
         if (timed) { kev_record(); }
@@ -480,10 +535,14 @@ void Engine::Impl::smooth_fused (int l, int n)
                     L.dl, L.mz.dev(), a, b, L.res32.p, S, E.m_opt.march_tz);
             }
         } else if (E.m_opt.fused_v2) {
-            if (abec) {
-                k_sweep_fused2<true><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);
+            const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
+            if (use_tma) {
+                if (abec) { k_sweep_fused2<true, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p); }
+                else { k_sweep_fused2<false, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p); }
+            } else if (abec) {
+                k_sweep_fused2<true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p);
             } else {
-                k_sweep_fused2<false><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);
+                k_sweep_fused2<false><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p);
             }
         } else if (abec) {
             k_sweep_fused<true><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);
@@ -493,6 +552,7 @@ void Engine::Impl::smooth_fused (int l, int n)
         launched();
         if (timed) { kev_record(); }
         std::swap(a, b);
+        std::swap(ma, mb);
     }
     if (a != L.cor32.p) {
         MLMG_CUDA_CHECK(cudaMemcpyAsync(L.cor32.p, a, sizeof(float) * (size_t)L.meta.nelem, cudaMemcpyDeviceToDevice,
@@ -1143,6 +1203,7 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
         for (int a : active) { if (a) { any_active = true; } }
     }
     MLMG_CUDA_CHECK(cudaEventRecord(I.ev1, m_stream));
+    I.check_device_error();
     for (int s = 0; s < ns; ++s) {
         if (active[s] && m_opt.fixed_iter == 0) { m_reports[s].status = NOT_CONVERGED; }
         if (m_opt.verbose >= 1) {

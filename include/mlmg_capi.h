@@ -179,8 +179,9 @@ int mlmg_set_fused_smoother(mlmg_solver s, int on);      /* fused two-colour Gau
  * "merge_boxes" (0/1), "fuse_resid_restrict" (0/1), "march_sweep" (0/1: fused
  * sweeps by the z-marching kernel), "march_min_tiles" (levels with fewer
  * marching tiles use the tiled fused sweep), "fused_v2" (0/1: the tiled fused
- * sweep with face ghosts rewritten in shared memory, default 1); -4 for an
- * unknown name */
+ * sweep with face ghosts rewritten in shared memory, default 1), "fused_tma"
+ * (0/1: that sweep stages each tile by one TMA tensor load, default 1); -4
+ * for an unknown name */
 int mlmg_set_option(mlmg_solver s, const char* name, double value);
 /* time every finest-level smoother launch with CUDA events on the library
  * stream (graph replays included); the stats accumulate until reset */
