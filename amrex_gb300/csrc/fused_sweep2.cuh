@@ -209,6 +209,7 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
         if (tid < RS * FS_RED_ROW) {
             const int r = tid % FS_RED_ROW;
             int ry = (tid / FS_RED_ROW) % FS_NY, rz = (tid / FS_RED_ROW) / FS_NY;   // row indices 0..9
+#pragma unroll 2
             for (int row = tid / FS_RED_ROW; row < FS_NZ * FS_NY; row += RS) {
                 const int ly = ry - 1, lz = rz - 1;
                 // (x+y+z) even: local lx = 2r - 1 + ((par0 + ry + rz) & 1)
