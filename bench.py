@@ -210,6 +210,8 @@ def _tuned_options(chosen):
         opts += [("coarse_block", 1), ("coarse_cells", 512 if "8^3" in chosen else 4096)]
     else:
         opts.append(("coarse_block", 0))
+    opts.append(("fused_v2", 0 if "per-cell face tests" in chosen else 1))
+    opts.append(("fused_tma", 0 if ("cp.async" in chosen or "per-cell" in chosen) else 1))
     return opts
 
 
@@ -235,7 +237,7 @@ def bench_batch(stream, nsolve=64):
     # tile / slab shapes picked by the autotuner on the largest solve of the
     # batch; the batch runs with the settings of its first solver
     big = max(range(nsolve), key=lambda q: specs[q].n)
-    _, tune_report = mixed[big].autotune(sols[big], rhss[big], vcycles=2)
+    _, tune_report = mixed[big].autotune(sols[big], rhss[big], vcycles=4)
     chosen = tune_report.strip().splitlines()[-1].replace("chosen: ", "")
     mixed[0].setFusedSmoother(not chosen.startswith("colour passes"))
     for name, val in _tuned_options(chosen):
@@ -486,7 +488,7 @@ def run_gb300(args, ws, rank, local):
         "config": workload_config(),
         "iters": iters, "fp64_ms": fp64_ms, "fp64_iters": fp64_iters, "speedup_vs_fp64": fp64_ms / ms,
         "phi_rel_diff_vs_fp64": rel_diff,
-        "roofline": {"kernel": "finest-level fused two-colour Gauss-Seidel sweep (FP32, k_sweep_fused)",
+        "roofline": {"kernel": "finest-level fused two-colour Gauss-Seidel sweep (FP32, k_sweep_fused2, TMA staging)",
                      "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
