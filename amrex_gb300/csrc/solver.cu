@@ -27,15 +27,15 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder ()
 
 // 3-D tiled tensor map over the allocation of patch P inside an FP32 level
 // field: x over the whole padded row (sx), y and z over the rows and planes
-// with their ghost layers; box = the fused sweep's staging box
-CUtensorMap patch_tensor_map (const float* field, const PatchDesc& P)
+// with their ghost layers; box 40 x by x bz floats (a fused sweep's staging box)
+CUtensorMap patch_tensor_map (const float* field, const PatchDesc& P, int by = FS_AY, int bz = FS_AZ)
 {
     const long long start = P.base - P.sxy - P.sx - XOFF;      // first element of the patch's allocation
     const int ny = P.hi[1] - P.lo[1] + 1, nz = P.hi[2] - P.lo[2] + 1;
     MLMG_REQUIRE(start % 4 == 0 && P.sx % 4 == 0 && P.sxy % 4 == 0, ERR_INTERNAL, "patch layout not 16-byte aligned");
     cuuint64_t dims[3] = {(cuuint64_t)P.sx, (cuuint64_t)(ny + 2), (cuuint64_t)(nz + 2)};
     cuuint64_t strides[2] = {(cuuint64_t)P.sx * sizeof(float), (cuuint64_t)P.sxy * sizeof(float)};
-    cuuint32_t box[3] = {(cuuint32_t)FS_AX, (cuuint32_t)FS_AY, (cuuint32_t)FS_AZ};
+    cuuint32_t box[3] = {(cuuint32_t)FS_AX, (cuuint32_t)by, (cuuint32_t)bz};
     cuuint32_t estride[3] = {1, 1, 1};
     CUtensorMap m;
     const CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
@@ -203,6 +203,33 @@ void Engine::Impl::build ()
             }
             L.tm_a.upload(ta, st());
             L.tm_b.upload(tb, st());
+        }
+        // the third form's maps: phi (both buffers), rhs and the stencil arrays, per patch
+        if (L.fused && !L.march && E.m_opt.fused_v3) {
+            std::vector<CUtensorMap> t3((size_t)F3_NMAP * M.patches.size());
+            std::memset(t3.data(), 0, t3.size() * sizeof(CUtensorMap));
+            for (size_t p = 0; p < M.patches.size(); ++p) {
+                CUtensorMap* m = &t3[p * F3_NMAP];
+                const PatchDesc& P = M.patches[p];
+                m[F3_PHI_A] = patch_tensor_map(L.cor32.p, P, 12, 12);
+                m[F3_PHI_B] = patch_tensor_map(L.cor32b.p, P, 12, 12);
+                m[F3_RHS] = patch_tensor_map(L.res32.p, P, 10, 10);
+                if (abec) {
+                    m[F3_D] = patch_tensor_map(L.D32.p, P, 10, 10);
+                    m[F3_SX] = patch_tensor_map(L.sx32.p, P, 10, 10);
+                    m[F3_SY] = patch_tensor_map(L.sy32.p, P, 11, 10);
+                    m[F3_SZ] = patch_tensor_map(L.sz32.p, P, 10, 11);
+                }
+            }
+            L.tm3.upload(t3, st());
+            static bool attr3 = false;
+            if (!attr3) {
+                MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_fused3<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     Fs3Plan::bytes(true)));
+                MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_fused3<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     Fs3Plan::bytes(false)));
+                attr3 = true;
+            }
         }
     }
     err_d.alloc(1);
@@ -522,6 +549,7 @@ void Engine::Impl::smooth_fused (int l, int n)
     const CUtensorMap* ma = L.tm_a.p;      // tensor maps over a and b (TMA staging)
     const CUtensorMap* mb = L.tm_b.p;
     const bool use_tma = ma != nullptr;
+    int pa = F3_PHI_A, pb = F3_PHI_B;       // the third form's phi maps of a and b
     const StencilPtrs S = stencil32(l);
     for (int i = 0; i < n; ++i) {
         if (timed) { kev_record(); }
@@ -533,6 +561,15 @@ void Engine::Impl::smooth_fused (int l, int n)
             } else {
                 k_sweep_march<false><<<L.mz.ntiles, blk, march_smem_floats(false) * sizeof(float), st()>>>(
                     L.dl, L.mz.dev(), a, b, L.res32.p, S, E.m_opt.march_tz);
+            }
+        } else if (L.tm3.p != nullptr) {
+            const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
+            if (abec) {
+                k_sweep_fused3<true><<<g, blk, Fs3Plan::bytes(true), st()>>>(L.dl, L.fz.dev(), a, b, S, L.tm3.p, pa,
+                                                                             err_d.p);
+            } else {
+                k_sweep_fused3<false><<<g, blk, Fs3Plan::bytes(false), st()>>>(L.dl, L.fz.dev(), a, b, S, L.tm3.p, pa,
+                                                                               err_d.p);
             }
         } else if (E.m_opt.fused_v2) {
             const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
@@ -553,6 +590,7 @@ void Engine::Impl::smooth_fused (int l, int n)
         if (timed) { kev_record(); }
         std::swap(a, b);
         std::swap(ma, mb);
+        std::swap(pa, pb);
     }
     if (a != L.cor32.p) {
         MLMG_CUDA_CHECK(cudaMemcpyAsync(L.cor32.p, a, sizeof(float) * (size_t)L.meta.nelem, cudaMemcpyDeviceToDevice,

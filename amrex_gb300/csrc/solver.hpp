@@ -49,6 +49,7 @@ struct EngineOptions {
     int fused_v2 = 1;           // fused sweeps by k_sweep_fused2 (face ghosts rewritten in shared memory,
                                 // one path for every tile) instead of k_sweep_fused
     int fused_tma = 1;          // ... staging each tile by one TMA tensor load
+    int fused_v3 = 0;           // fused sweeps by k_sweep_fused3 (every input of a tile staged by TMA)
     int max_fmg_iter = 0;       // F-cycles (MLMGT::mgFcycle) for the first max_fmg_iter iterations
     int transpose = 0;          // solve A^T x = rhs (homogeneous BCs): the outer residual uses A^T,
                                 // the V-cycle of A is the correction operator (adjoint solves)

@@ -107,14 +107,16 @@ def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
 
 @pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_mixed_bc", "solve_abec_48",
                                   "solve_poisson_periodic_x", "solve_abec_mo4"])
-@pytest.mark.parametrize("variant", ["tiled", "tiled_v1", "march"])
+@pytest.mark.parametrize("variant", ["tiled", "tiled_v1", "tiled_v3", "march"])
 def test_fused_sweep_matches_colour_passes(name, variant):
     """The fused two-colour sweep (tiled with face ghosts rewritten in shared
-    memory, the earlier tiled form, or marching along z) performs the same
-    arithmetic as two colour passes with ghost refreshes in between."""
+    memory, the earlier tiled form, the tiled form with every input staged by
+    TMA, or marching along z) performs the same arithmetic as two colour
+    passes with ghost refreshes in between."""
     c = load.load(name)["case"]
     inp = cases.inputs(c)
-    opts = {"march_sweep": int(variant == "march"), "march_min_tiles": 0, "fused_v2": int(variant == "tiled")}
+    opts = {"march_sweep": int(variant == "march"), "march_min_tiles": 0,
+            "fused_v2": int(variant in ("tiled", "tiled_v3")), "fused_v3": int(variant == "tiled_v3")}
     p1 = helpers.make_problem(c, inp, precision="mixed", fused=False)
     p2 = helpers.make_problem(c, inp, precision="mixed", fused=True, options=opts)
     p1["mlmg"].solve(p1["sol"], p1["rhs"], 1e-10, 0)
