@@ -46,6 +46,8 @@ struct AmrLevelData {
     GhostWork cfw{};                        // face-cell walk over them (no copy tags)
     DevBuf<int8_t> bflags;                  // per Dirichlet-value slot: BF_* bits
     DevBuf<double> bcor;                    // boundary values of the correction (physical slots 0)
+    DevBuf<long long> nbr;                  // per Dirichlet-value slot: element of the covering patch's cell, or -1
+                                            // (colour passes without ghost fills; empty if a closure has 4 points)
     DevBuf<double> hold64;                  // cor_hold of the AMR level
     DevBuf<float> hold32;
     void* cor_p = nullptr;                  // the level's correction buffer (swapped with the hold)
@@ -89,7 +91,7 @@ struct AmrEngine::Impl {
     void build_coarse_tables (int c);
 
     // operations
-    void solution_residual (int l, bool update, double* partial = nullptr);
+    void solution_residual (int l, bool update, bool want_norm = false);
     void reflux (int c);
     void avgdown (int c, const double* fine, double* crse);
     template <typename T> void gather (int l, const T* crse);
@@ -282,6 +284,36 @@ void AmrEngine::Impl::build_fine_tables (int l)
     D.bflags.upload(flags, st());
     D.bcor.alloc(L(l).bcval.n);
     D.bcor.zero(st());
+    // neighbour table of the ghost-free colour passes: every copy-tag cell
+    // (a ghost covered by another patch) points at its source cell
+    bool short_closures = true;
+    for (const PatchDesc& P : Mf.patches) {
+        for (int f = 0; f < 6; ++f) {
+            if (P.face[f].type == BC_DIRICHLET && P.face[f].nx > 3) { short_closures = false; }
+        }
+    }
+    if (short_closures) {
+        std::vector<long long> nb(L(l).bcval.n, -1);
+        for (const CopyTag& t : Mf.tags) {
+            const PatchDesc& P = Mf.patches[t.dst];
+            const PatchDesc& Q = Mf.patches[t.src];
+            for (int k = t.box.lo[2]; k <= t.box.hi[2]; ++k)
+            for (int j = t.box.lo[1]; j <= t.box.hi[1]; ++j)
+            for (int i = t.box.lo[0]; i <= t.box.hi[0]; ++i) {
+                int f;
+                if (i < P.lo[0]) { f = 0; } else if (i > P.hi[0]) { f = 3; }
+                else if (j < P.lo[1]) { f = 1; } else if (j > P.hi[1]) { f = 4; }
+                else if (k < P.lo[2]) { f = 2; } else { f = 5; }
+                const int nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1;
+                const int d = f % 3;
+                const long long u = (d == 0) ? (long long)(k - P.lo[2]) * ny + (j - P.lo[1])
+                                  : (d == 1) ? (long long)(k - P.lo[2]) * nx + (i - P.lo[0])
+                                             : (long long)(j - P.lo[1]) * nx + (i - P.lo[0]);
+                nb[(size_t)(P.face[f].bcval_off + u)] = cidx(Q, i - t.shift[0], j - t.shift[1], k - t.shift[2]);
+            }
+        }
+        D.nbr.upload(nb, st());
+    }
 }
 
 void AmrEngine::Impl::build_coarse_tables (int c)
@@ -401,7 +433,7 @@ template <> void AmrEngine::Impl::gather<float> (int l, const float* crse)
 // MLCellLinOpT::solutionResidual (AMReX_MLCellLinOp.H:1219-1236); on a fine
 // level with update, the boundary values are first refreshed from the
 // coarser level's solution (updateSolBC, :651-664)
-void AmrEngine::Impl::solution_residual (int l, bool update, double* partial)
+void AmrEngine::Impl::solution_residual (int l, bool update, bool want_norm)
 {
     LevelData& Ld = L(l);
     AmrLevelData& D = lev[l];
@@ -418,9 +450,24 @@ void AmrEngine::Impl::solution_residual (int l, bool update, double* partial)
         bcv = Ld.bcval.p;
     }
     D.I->ghost<double>(0, Ld.sol.p, true, true, bcv);
-    k_residual<double, double, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res.p, Ld.sol.p,
-        Ld.rhs.p, nullptr, nullptr, nullptr, nullptr, partial);
-    launched();
+    Engine::Impl& I = *D.I;
+    if (mixed()) {
+        // stencil form (D x - sum s x_nb: 8 FP64 operations per cell instead of
+        // 14), with the level's max|r| by atomic max into red_out[0]
+        if (want_norm) { MLMG_CUDA_CHECK(cudaMemsetAsync(I.red_out.p, 0, sizeof(double), st())); }
+        k_residual_s<double, double, false, false, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl,
+            Ld.all.dev(), Ld.res.p, Ld.sol.p, Ld.rhs.p, StencilPtrs{}, nullptr, want_norm ? I.red_out.p : nullptr);
+        launched();
+    } else {
+        // the reference's operation order (MLPoissonT::Fapply), block maxima for the norm
+        k_residual<double, double, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res.p,
+            Ld.sol.p, Ld.rhs.p, nullptr, nullptr, nullptr, nullptr, want_norm ? I.partial.p : nullptr);
+        launched();
+        if (want_norm) {
+            k_reduce_final<<<1, 1024, 0, st()>>>(I.partial.p, Ld.all.solve_begin.p, RED_MAXABS, I.red_out.p);
+            launched();
+        }
+    }
 }
 
 // MLCellLinOpT::reflux (AMReX_MLCellLinOp.H:1272-1346) into res of level c
@@ -452,7 +499,18 @@ template <typename T>
 void AmrEngine::Impl::mini_cycle (int l, const T* rhs)
 {
     T* x = cor<T>(l);
-    MLMG_CUDA_CHECK(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)L(l).meta.nelem, st()));
+    LevelData& Ld = L(l);
+    MLMG_CUDA_CHECK(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)Ld.meta.nelem, st()));
+    if (lev[l].nbr.p != nullptr) {
+        // colour passes reading covered neighbours directly: no ghost fills
+        for (int i = 0; i < A.m_opt.nu1; ++i) {
+            for (int rb = 0; rb < 2; ++rb) {
+                k_gsrb_nbr<T><<<Ld.mg.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.mg.dev(), x, rhs, lev[l].nbr.p, rb);
+                launched();
+            }
+        }
+        return;
+    }
     for (int i = 0; i < A.m_opt.nu1; ++i) { lev[l].I->smooth<T>(0, x, rhs, i == 0); }
 }
 
@@ -500,9 +558,7 @@ void AmrEngine::Impl::fine_residual_and_norm ()
 {
     const int fin = nl - 1;
     Engine::Impl& I = *lev[fin].I;
-    solution_residual(fin, true, I.partial.p);
-    k_reduce_final<<<1, 1024, 0, st()>>>(I.partial.p, L(fin).all.solve_begin.p, RED_MAXABS, I.red_out.p);
-    launched();
+    solution_residual(fin, true, true);
     MLMG_CUDA_CHECK(cudaMemcpyAsync(h_norm.p, I.red_out.p, sizeof(double), cudaMemcpyDeviceToHost, st()));
 }
 

@@ -3,7 +3,7 @@
 // two levels' patch layouts, so a launch covers every box of a level.
 #pragma once
 
-#include "stage_kernels.cuh"
+#include "stencil_kernels.cuh"
 
 namespace mlmg {
 
@@ -307,6 +307,62 @@ k_amr_finish (DevLevel L, Subset S, double* __restrict__ sol, T* __restrict__ co
             sol[q] += double(v);
             if (hold != nullptr) { cor[q] = v + hold[q]; }
         }
+    }
+}
+
+// ---------------------------------------------- colour pass without ghosts --
+// Neighbour value across face f of patch cell (i,j,k) for a homogeneous colour
+// pass of a level with several patches: where the ghost is covered by another
+// patch (nbr >= 0, indexed like the face's Dirichlet slots) the neighbour's
+// current value, else the inline closure of the cell and its inner neighbour.
+// In a colour pass both are cells of the other colour or the cell itself, so
+// this equals what a ghost fill before the pass would have stored.
+template <typename T>
+__device__ __forceinline__ T nbr_ghost (const PatchDesc& P, int f, int i, int j, int k, const T* phi, T pc, T pin,
+                                        const long long* __restrict__ nbr)
+{
+    const long long v = nbr[P.face[f].bcval_off + face_local(P, f, i, j, k)];
+    return (v >= 0) ? phi[v] : inline_ghost<T, false>(P, f, pc, pin, nullptr, 0);
+}
+
+// one colour pass of MLPoisson's Gauss-Seidel (mlpoisson_gsrb,
+// AMReX_MLPoisson_3D_K.H:153-196) reading patch-face neighbours through nbr
+// instead of a ghost fill
+template <typename T>
+__global__ void __launch_bounds__(TILE_THREADS)
+k_gsrb_nbr (DevLevel L, Subset Sb, T* __restrict__ phi, const T* __restrict__ rhs, const long long* __restrict__ nbr,
+            int rb)
+{
+    const TileCoord c = decode_tile(L, Sb, blockIdx.x);
+    const PatchDesc& P = L.P[c.p];
+    const int j = c.y0 + threadIdx.y;
+    if (j > P.hi[1]) { return; }
+    const long long sx = P.sx, sxy = P.sxy;
+    const T dhx = T(P.dhs[0]), dhy = T(P.dhs[1]), dhz = T(P.dhs[2]);
+    const T gamma = T(-2.0) * (dhx + dhy + dhz);
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+        const int k = c.z0 + kk;
+        if (k > P.hi[2]) { break; }
+        const int i = c.x0 + ((c.x0 + j + k + rb) & 1) + 2 * threadIdx.x;
+        if (i > P.hi[0]) { continue; }
+        const long long q = cidx(P, i, j, k);
+        const T pc = phi[q];
+        const T xm = (i == P.lo[0]) ? nbr_ghost<T>(P, 0, i, j, k, phi, pc, phi[q + 1], nbr) : phi[q - 1];
+        const T xp = (i == P.hi[0]) ? nbr_ghost<T>(P, 3, i, j, k, phi, pc, phi[q - 1], nbr) : phi[q + 1];
+        const T ym = (j == P.lo[1]) ? nbr_ghost<T>(P, 1, i, j, k, phi, pc, phi[q + sx], nbr) : phi[q - sx];
+        const T yp = (j == P.hi[1]) ? nbr_ghost<T>(P, 4, i, j, k, phi, pc, phi[q - sx], nbr) : phi[q + sx];
+        const T zm = (k == P.lo[2]) ? nbr_ghost<T>(P, 2, i, j, k, phi, pc, phi[q + sxy], nbr) : phi[q - sxy];
+        const T zp = (k == P.hi[2]) ? nbr_ghost<T>(P, 5, i, j, k, phi, pc, phi[q - sxy], nbr) : phi[q + sxy];
+        T cf0 = 0, cf1 = 0, cf2 = 0, cf3 = 0, cf4 = 0, cf5 = 0;
+        if (i == P.lo[0]) { cf0 = T(face_cf(L, P, 0, i, j, k)); }
+        if (j == P.lo[1]) { cf1 = T(face_cf(L, P, 1, i, j, k)); }
+        if (k == P.lo[2]) { cf2 = T(face_cf(L, P, 2, i, j, k)); }
+        if (i == P.hi[0]) { cf3 = T(face_cf(L, P, 3, i, j, k)); }
+        if (j == P.hi[1]) { cf4 = T(face_cf(L, P, 4, i, j, k)); }
+        if (k == P.hi[2]) { cf5 = T(face_cf(L, P, 5, i, j, k)); }
+        const T g_m_d = gamma + dhx * (cf0 + cf3) + dhy * (cf1 + cf4) + dhz * (cf2 + cf5);
+        const T res = rhs[q] - gamma * pc - dhx * (xm + xp) - dhy * (ym + yp) - dhz * (zm + zp);
+        phi[q] = pc + relax_factor(g_m_d) * res;
     }
 }
 
