@@ -33,7 +33,7 @@ def run_amr(args):
         else:
             grids[-1].append(tuple(int(v) for v in p))
     P = workloads.amr_problem(case["n"], grids, case["rhs_seed"], precision={"fp64": 0, "mixed": 1}[args.mode],
-                              graph=args.graph)
+                              graph=args.graph, fused=args.fused)
     m = P["mlmg"]
     for s in range(args.solves):
         for x in P["sols"]:

@@ -68,7 +68,8 @@ def adjoint_objective(n, phi_scale, target_seed=3003):
     return tgt, region
 
 
-def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_grid_size=32, con_grid_size=32):
+def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_grid_size=32, con_grid_size=32,
+                fused=False):
     """Composite MLPoisson over len(grids) AMR levels: per-level geometry,
     BoxArray, DistributionMapping, solution (1 ghost, zero) and RHS
     MultiFabs, the operator and the MLMG solver.  ``grids[l]`` holds level l's
@@ -98,4 +99,5 @@ def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_
     mlmg.setMaxIter(max_iter)
     mlmg.setPrecision(precision)
     mlmg.setGraph(graph)
+    mlmg.setFusedSmoother(fused)
     return dict(geoms=geoms, bas=bas, dms=dms, sols=sols, rhss=rhss, op=op, mlmg=mlmg)

@@ -351,6 +351,7 @@ def bench_amr(stream, reps=3):
         m = P["mlmg"] if prec == "fp64" else ag.MLMG(P["op"])
         m.setPrecision(prec)
         m.setGraph(True)
+        m.setFusedSmoother(prec == "mixed")      # fused sweeps on AMR level 0's V-cycle
 
         def step():
             for x in P["sols"]:

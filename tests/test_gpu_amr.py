@@ -16,11 +16,12 @@ pytestmark = pytest.mark.gpu
 SMALL = ["c2_n16_2lev", "c2_n32"]
 
 
-def _solve(name, precision=0, graph=False, tol_rel=None):
+def _solve(name, precision=0, graph=False, tol_rel=None, fused=False):
     g = ac.load("amrsolve", name)
     case, grids = g["case"], g["grids"]
     P = workloads.amr_problem(case["n"], grids, case["rhs_seed"], precision=precision, graph=graph,
-                              agg_grid_size=case.get("agg_grid_size", 32), con_grid_size=case.get("con_grid_size", 32))
+                              agg_grid_size=case.get("agg_grid_size", 32), con_grid_size=case.get("con_grid_size", 32),
+                              fused=fused)
     resid = P["mlmg"].solve(P["sols"], P["rhss"], tol_rel or case.get("tol_rel", 1e-10), 0.0)
     phis = []
     for lev, boxes in enumerate(grids):
@@ -48,13 +49,13 @@ def test_amr_fp64_matches_reference(name):
 
 
 @pytest.mark.parametrize("name", SMALL)
-@pytest.mark.parametrize("graph", [False, True])
-def test_amr_mixed_reaches_target(name, graph):
+@pytest.mark.parametrize("graph,fused", [(False, False), (True, False), (True, True)])
+def test_amr_mixed_reaches_target(name, graph, fused):
     """FP32 corrections inside the FP64 composite residual reach the same
     1e-10 relative composite residual; the solution agrees with the
     reference's FP64 solution to within the discretisation-free tolerance
     that a 1e-10 residual allows."""
-    g, P, resid, phis = _solve(name, precision=1, graph=graph)
+    g, P, resid, phis = _solve(name, precision=1, graph=graph, fused=fused)
     ref = g["result"]
     assert resid <= 1e-10 * ref["rhs_norm"]
     assert P["mlmg"].getNumIters() <= ref["niters"] + 3
@@ -80,7 +81,7 @@ def test_amr_config_size_against_reference_summary():
     g = ac.load("amrsolve", "c2")
     ref = g["result"]
     for precision, tol in ((0, 1e-9), (1, 1e-8)):
-        _, P, resid, phis = _solve("c2", precision=precision, graph=True)
+        _, P, resid, phis = _solve("c2", precision=precision, graph=True, fused=precision == 1)
         m = P["mlmg"]
         assert resid <= 1e-10 * ref["rhs_norm"]
         if precision == 0:
