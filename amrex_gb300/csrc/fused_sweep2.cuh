@@ -152,124 +152,130 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
         }
     };
 
-    if (touches) {
-        // applyBC before the first colour: closure of the old values
-        for_face_ghosts([&] (int f, const int* c, const int* cf, const int* ci) {
-            aat(c[0], c[1], c[2]) = P.closure(f, aat(cf[0], cf[1], cf[2]), aat(ci[0], ci[1], ci[2]));
-        });
-        __syncthreads();
-    }
+    // the rest of the sweep, compiled separately for tiles that touch a patch
+    // face (ghost rewrites, inside tests, boundary correction) and for the others
+    auto sweep = [&] (auto touch_tag) {
+        constexpr bool TOUCH = decltype(touch_tag)::value;
+        if constexpr (TOUCH) {
+            // applyBC before the first colour: closure of the old values
+            for_face_ghosts([&] (int f, const int* c, const int* cf, const int* ci) {
+                aat(c[0], c[1], c[2]) = P.closure(f, aat(cf[0], cf[1], cf[2]), aat(ci[0], ci[1], ci[2]));
+            });
+            __syncthreads();
+        }
 
-    const long long q0 = P.idx(x0, y0, z0);
-    const int sx = P.sx, sxy = (int)P.sxy;
-    const float* __restrict__ rh = rhs + q0;
-    const float *Dp = nullptr, *SXp = nullptr, *SYp = nullptr, *SZp = nullptr;
-    if constexpr (VARC) {
-        Dp = static_cast<const float*>(Sc.D) + q0;
-        SXp = static_cast<const float*>(Sc.sx) + q0;
-        SYp = static_cast<const float*>(Sc.sy) + q0;
-        SZp = static_cast<const float*>(Sc.sz) + q0;
-    }
-    const float cdx = -P.dhx, cdy = -P.dhy, cdz = -P.dhz, cd = -2.0f * (P.dhx + P.dhy + P.dhz);
-    const float fco0 = P.f[0].fco, fco1 = P.f[1].fco, fco2 = P.f[2].fco;
-    const float fco3 = P.f[3].fco, fco4 = P.f[4].fco, fco5 = P.f[5].fco;
-    // Gauss-Seidel update of local cell (lx, ly, lz) at global offset o from q0
-    auto update = [&] (int lx, int ly, int lz, int o, float pc, float xm, float xp, float ym, float yp, float zm,
-                       float zp) {
-        float d, sxl, sxh, syl, syh, szl, szh;
+        const long long q0 = P.idx(x0, y0, z0);
+        const int sx = P.sx, sxy = (int)P.sxy;
+        const float* __restrict__ rh = rhs + q0;
+        const float *Dp = nullptr, *SXp = nullptr, *SYp = nullptr, *SZp = nullptr;
         if constexpr (VARC) {
-            d = __ldg(Dp + o);
-            sxl = __ldg(SXp + o); sxh = __ldg(SXp + o + 1);
-            syl = __ldg(SYp + o); syh = __ldg(SYp + o + sx);
-            szl = __ldg(SZp + o); szh = __ldg(SZp + o + sxy);
-        } else {
-            d = cd; sxl = sxh = cdx; syl = syh = cdy; szl = szh = cdz;
+            Dp = static_cast<const float*>(Sc.D) + q0;
+            SXp = static_cast<const float*>(Sc.sx) + q0;
+            SYp = static_cast<const float*>(Sc.sy) + q0;
+            SZp = static_cast<const float*>(Sc.sz) + q0;
         }
-        float gmd = d;
-        if (touches) {
-            float corr = 0.0f;
-            if (lx == pxl) { corr += sxl * fco0; }
-            if (lx == pxh) { corr += sxh * fco3; }
-            if (ly == pyl) { corr += syl * fco1; }
-            if (ly == pyh) { corr += syh * fco4; }
-            if (lz == pzl) { corr += szl * fco2; }
-            if (lz == pzh) { corr += szh * fco5; }
-            gmd = d - corr;
-        }
-        const float rho = sxl * xm + sxh * xp + syl * ym + syh * yp + szl * zm + szh * zp;
-        const float res = __ldg(rh + o) - (d * pc - rho);
-        return pc + relax_factor(gmd) * res;
-    };
-
-    // ---- first colour on the tile + 1: 17 cells per row, 10 x 10 rows;
-    // 255 threads = 17 columns x 15 row streams
-    {
-        constexpr int RS = FS_THREADS / FS_RED_ROW;      // 15
-        const int par0 = (x0 - 1 + y0 - 1 + z0 - 1) & 1;  // parity of local (-1, -1, -1)
-        if (tid < RS * FS_RED_ROW) {
-            const int r = tid % FS_RED_ROW;
-            int ry = (tid / FS_RED_ROW) % FS_NY, rz = (tid / FS_RED_ROW) / FS_NY;   // row indices 0..9
-#pragma unroll 2
-            for (int row = tid / FS_RED_ROW; row < FS_NZ * FS_NY; row += RS) {
-                const int ly = ry - 1, lz = rz - 1;
-                // (x+y+z) even: local lx = 2r - 1 + ((par0 + ry + rz) & 1)
-                const int lx = 2 * r - 1 + ((par0 + ry + rz) & 1);
-                const bool in = !touches || (lx >= pxl && lx <= pxh && ly >= pyl && ly <= pyh && lz >= pzl &&
-                                             lz <= pzh);
-                if (in) {
-                    const int o = lz * sxy + ly * sx + lx;
-                    nat(lx, ly, lz) = update(lx, ly, lz, o, aat(lx, ly, lz), aat(lx - 1, ly, lz), aat(lx + 1, ly, lz),
-                                             aat(lx, ly - 1, lz), aat(lx, ly + 1, lz), aat(lx, ly, lz - 1),
-                                             aat(lx, ly, lz + 1));
-                }
-                ry += RS % FS_NY; rz += RS / FS_NY;
-                if (ry >= FS_NY) { ry -= FS_NY; rz += 1; }
+        const float cdx = -P.dhx, cdy = -P.dhy, cdz = -P.dhz, cd = -2.0f * (P.dhx + P.dhy + P.dhz);
+        const float fco0 = P.f[0].fco, fco1 = P.f[1].fco, fco2 = P.f[2].fco;
+        const float fco3 = P.f[3].fco, fco4 = P.f[4].fco, fco5 = P.f[5].fco;
+        // Gauss-Seidel update of local cell (lx, ly, lz) at global offset o from q0
+        auto update = [&] (int lx, int ly, int lz, int o, float pc, float xm, float xp, float ym, float yp, float zm,
+                           float zp) {
+            float d, sxl, sxh, syl, syh, szl, szh;
+            if constexpr (VARC) {
+                d = __ldg(Dp + o);
+                sxl = __ldg(SXp + o); sxh = __ldg(SXp + o + 1);
+                syl = __ldg(SYp + o); syh = __ldg(SYp + o + sx);
+                szl = __ldg(SZp + o); szh = __ldg(SZp + o + sxy);
+            } else {
+                d = cd; sxl = sxh = cdx; syl = syh = cdy; szl = szh = cdz;
             }
-        }
-    }
-    __syncthreads();
-    if (touches) {
-        // applyBC before the second colour: closure of the current values
-        // (new first-colour values in N, old second-colour values in A)
-        const int par0 = (x0 + y0 + z0) & 1;      // parity of local (0, 0, 0)
-        auto cur = [&] (const int* c) -> float {
-            return (((par0 + c[0] + c[1] + c[2]) & 1) == 0) ? nat(c[0], c[1], c[2]) : aat(c[0], c[1], c[2]);
+            float gmd = d;
+            if constexpr (TOUCH) {
+                float corr = 0.0f;
+                if (lx == pxl) { corr += sxl * fco0; }
+                if (lx == pxh) { corr += sxh * fco3; }
+                if (ly == pyl) { corr += syl * fco1; }
+                if (ly == pyh) { corr += syh * fco4; }
+                if (lz == pzl) { corr += szl * fco2; }
+                if (lz == pzh) { corr += szh * fco5; }
+                gmd = d - corr;
+            }
+            const float rho = sxl * xm + sxh * xp + syl * ym + syh * yp + szl * zm + szh * zp;
+            const float res = __ldg(rh + o) - (d * pc - rho);
+            return pc + relax_factor(gmd) * res;
         };
-        for_face_ghosts([&] (int f, const int* c, const int* cf, const int* ci) {
-            nat(c[0], c[1], c[2]) = P.closure(f, cur(cf), cur(ci));
-        });
-        __syncthreads();
-    }
 
-    // ---- second colour on the tile; each thread writes one (even x, odd x)
-    // pair: 16 pairs per row, 8 x 8 rows, 4 rounds
-    {
-        const int r = tid % (FS_TX / 2);
-        const int ly = (tid / (FS_TX / 2)) % FS_TY;
-        const int lzs = (tid / (FS_TX / 2)) / FS_TY;     // 0..1
-        const int par0 = (x0 + y0 + z0) & 1;
-#pragma unroll
-        for (int lz = lzs; lz < FS_TZ; lz += 2) {
-            const int lxe = 2 * r;                       // pair (lxe, lxe + 1)
-            const bool first_at_even = ((par0 + lxe + ly + lz) & 1) == 0;
-            const int lx2 = first_at_even ? lxe + 1 : lxe;   // the second-colour cell of the pair
-            const int o = lz * sxy + ly * sx + lx2;
-            const bool in2 = !touches || (lx2 <= pxh && ly <= pyh && lz <= pzh);
-            float v2 = 0.0f;
-            if (in2) {
-                v2 = update(lx2, ly, lz, o, aat(lx2, ly, lz), nat(lx2 - 1, ly, lz), nat(lx2 + 1, ly, lz),
-                            nat(lx2, ly - 1, lz), nat(lx2, ly + 1, lz), nat(lx2, ly, lz - 1), nat(lx2, ly, lz + 1));
-            }
-            const int lx1 = first_at_even ? lxe : lxe + 1;
-            const float v1 = nat(lx1, ly, lz);
-            const long long qp = q0 + (long long)(lz * sxy + ly * sx + lxe);
-            if (!touches || (lxe + 1 <= pxh && ly <= pyh && lz <= pzh)) {
-                *reinterpret_cast<float2*>(phi_out + qp) = first_at_even ? make_float2(v1, v2) : make_float2(v2, v1);
-            } else if (lxe <= pxh && ly <= pyh && lz <= pzh) {
-                phi_out[qp] = first_at_even ? v1 : v2;
+        // ---- first colour on the tile + 1: 17 cells per row, 10 x 10 rows;
+        // 255 threads = 17 columns x 15 row streams
+        {
+            constexpr int RS = FS_THREADS / FS_RED_ROW;      // 15
+            const int par0 = (x0 - 1 + y0 - 1 + z0 - 1) & 1;  // parity of local (-1, -1, -1)
+            if (tid < RS * FS_RED_ROW) {
+                const int r = tid % FS_RED_ROW;
+                int ry = (tid / FS_RED_ROW) % FS_NY, rz = (tid / FS_RED_ROW) / FS_NY;   // row indices 0..9
+    #pragma unroll 2
+                for (int row = tid / FS_RED_ROW; row < FS_NZ * FS_NY; row += RS) {
+                    const int ly = ry - 1, lz = rz - 1;
+                    // (x+y+z) even: local lx = 2r - 1 + ((par0 + ry + rz) & 1)
+                    const int lx = 2 * r - 1 + ((par0 + ry + rz) & 1);
+                    const bool in = !TOUCH || (lx >= pxl && lx <= pxh && ly >= pyl && ly <= pyh && lz >= pzl &&
+                                                 lz <= pzh);
+                    if (in) {
+                        const int o = lz * sxy + ly * sx + lx;
+                        nat(lx, ly, lz) = update(lx, ly, lz, o, aat(lx, ly, lz), aat(lx - 1, ly, lz), aat(lx + 1, ly, lz),
+                                                 aat(lx, ly - 1, lz), aat(lx, ly + 1, lz), aat(lx, ly, lz - 1),
+                                                 aat(lx, ly, lz + 1));
+                    }
+                    ry += RS % FS_NY; rz += RS / FS_NY;
+                    if (ry >= FS_NY) { ry -= FS_NY; rz += 1; }
+                }
             }
         }
-    }
+        __syncthreads();
+        if constexpr (TOUCH) {
+            // applyBC before the second colour: closure of the current values
+            // (new first-colour values in N, old second-colour values in A)
+            const int par0 = (x0 + y0 + z0) & 1;      // parity of local (0, 0, 0)
+            auto cur = [&] (const int* c) -> float {
+                return (((par0 + c[0] + c[1] + c[2]) & 1) == 0) ? nat(c[0], c[1], c[2]) : aat(c[0], c[1], c[2]);
+            };
+            for_face_ghosts([&] (int f, const int* c, const int* cf, const int* ci) {
+                nat(c[0], c[1], c[2]) = P.closure(f, cur(cf), cur(ci));
+            });
+            __syncthreads();
+        }
+
+        // ---- second colour on the tile; each thread writes one (even x, odd x)
+        // pair: 16 pairs per row, 8 x 8 rows, 4 rounds
+        {
+            const int r = tid % (FS_TX / 2);
+            const int ly = (tid / (FS_TX / 2)) % FS_TY;
+            const int lzs = (tid / (FS_TX / 2)) / FS_TY;     // 0..1
+            const int par0 = (x0 + y0 + z0) & 1;
+    #pragma unroll
+            for (int lz = lzs; lz < FS_TZ; lz += 2) {
+                const int lxe = 2 * r;                       // pair (lxe, lxe + 1)
+                const bool first_at_even = ((par0 + lxe + ly + lz) & 1) == 0;
+                const int lx2 = first_at_even ? lxe + 1 : lxe;   // the second-colour cell of the pair
+                const int o = lz * sxy + ly * sx + lx2;
+                const bool in2 = !TOUCH || (lx2 <= pxh && ly <= pyh && lz <= pzh);
+                float v2 = 0.0f;
+                if (in2) {
+                    v2 = update(lx2, ly, lz, o, aat(lx2, ly, lz), nat(lx2 - 1, ly, lz), nat(lx2 + 1, ly, lz),
+                                nat(lx2, ly - 1, lz), nat(lx2, ly + 1, lz), nat(lx2, ly, lz - 1), nat(lx2, ly, lz + 1));
+                }
+                const int lx1 = first_at_even ? lxe : lxe + 1;
+                const float v1 = nat(lx1, ly, lz);
+                const long long qp = q0 + (long long)(lz * sxy + ly * sx + lxe);
+                if (!TOUCH || (lxe + 1 <= pxh && ly <= pyh && lz <= pzh)) {
+                    *reinterpret_cast<float2*>(phi_out + qp) = first_at_even ? make_float2(v1, v2) : make_float2(v2, v1);
+                } else if (lxe <= pxh && ly <= pyh && lz <= pzh) {
+                    phi_out[qp] = first_at_even ? v1 : v2;
+                }
+            }
+        }
+    };
+    if (touches) { sweep(std::true_type{}); } else { sweep(std::false_type{}); }
 }
 
 } // namespace mlmg
