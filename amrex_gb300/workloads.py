@@ -69,11 +69,13 @@ def adjoint_objective(n, phi_scale, target_seed=3003):
 
 
 def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_grid_size=32, con_grid_size=32,
-                fused=False):
+                fused=False, solbc=None, max_fmg_iter=0):
     """Composite MLPoisson over len(grids) AMR levels: per-level geometry,
     BoxArray, DistributionMapping, solution (1 ghost, zero) and RHS
     MultiFabs, the operator and the MLMG solver.  ``grids[l]`` holds level l's
-    boxes as (lo0, lo1, lo2, hi0, hi1, hi2)."""
+    boxes as (lo0, lo1, lo2, hi0, hi1, hi2); ``solbc[l]`` (optional) is a
+    grown level-domain array with the initial guess in the valid cells and the
+    Dirichlet values in the ghosts."""
     geoms, bas, dms, sols, rhss = [], [], [], [], []
     for lev, g in enumerate(grids):
         m = n << lev
@@ -82,6 +84,8 @@ def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_
         dm = ag.DistributionMapping(ba)
         sol = ag.MultiFab(ba, dm, 1, 1)
         sol.setVal(0.0)
+        if solbc is not None and solbc[lev] is not None:
+            sol.set_global(solbc[lev], lo=(-1, -1, -1))
         rhs = ag.MultiFab(ba, dm, 1, 0)
         for i, b in enumerate(g):
             rhs.set_fab(i, synth.gaussian_rhs_box(m, rhs_seed, b))
@@ -97,6 +101,8 @@ def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_
         op.setLevelBC(lev, sols[lev])
     mlmg = ag.MLMG(op)
     mlmg.setMaxIter(max_iter)
+    if max_fmg_iter:
+        mlmg.setMaxFmgIter(max_fmg_iter)
     mlmg.setPrecision(precision)
     mlmg.setGraph(graph)
     mlmg.setFusedSmoother(fused)

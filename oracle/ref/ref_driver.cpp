@@ -262,6 +262,12 @@ int run_amr (const std::string& mode, const std::string& dir)
         rhs[l].define(ba[l], dm[l], 1, 0);
         const int gx = dom[l].length(0), gy = dom[l].length(1), gz = dom[l].length(2);
         Global gs{gx+2, gy+2, gz+2, -1, -1, -1, std::vector<double>((size_t)(gx+2)*(gy+2)*(gz+2), 0.0)};
+        // optional initial guess and Dirichlet values in the ghosts (grown level domain)
+        const std::string bcf = dir + "/solbc_l" + std::to_string(l) + ".bin";
+        if (std::FILE* tf = std::fopen(bcf.c_str(), "rb")) {
+            std::fclose(tf);
+            gs.v = read_bin(bcf, (size_t)(gx+2)*(gy+2)*(gz+2));
+        }
         fill_from_global(sol[l], gs, 1);
         Global gr{gx, gy, gz, 0, 0, 0, read_bin(dir + "/rhs_l" + std::to_string(l) + ".bin", (size_t)gx*gy*gz)};
         fill_from_global(rhs[l], gr, 0);
@@ -271,6 +277,7 @@ int run_amr (const std::string& mode, const std::string& dir)
     mlmg.setVerbose(c.geti("verbose", 0));
     mlmg.setMaxIter(c.geti("max_iter", 200));
     if (c.geti("fixed_iter", 0) > 0) { mlmg.setFixedIter(c.geti("fixed_iter", 0)); }
+    if (c.geti("max_fmg_iter", 0) > 0) { mlmg.setMaxFmgIter(c.geti("max_fmg_iter", 0)); }
     auto t0 = std::chrono::steady_clock::now();
     const Real resid = mlmg.solve(GetVecOfPtrs(sol), GetVecOfConstPtrs(rhs), c.getd("tol_rel", 1e-10),
                                   c.getd("tol_abs", 0.0));

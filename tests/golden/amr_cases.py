@@ -21,6 +21,10 @@ CASES = {
     # small composite solves for parity
     "c2_n32": dict(n=32, nlev=3, max_grid_size=16, rhs_seed=1002),
     "c2_n16_2lev": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1012),
+    # inhomogeneous Dirichlet values on every level and a non-zero initial guess
+    "c2_n16_2lev_bc": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1012, bc=True),
+    # F-cycles on AMR level 0 for the first two iterations
+    "c2_n32_fmg": dict(n=32, nlev=3, max_grid_size=16, rhs_seed=1002, max_fmg_iter=2, solve="summary"),
 }
 
 
@@ -33,6 +37,23 @@ def sample_index(size, lev, count=4096):
     """seeded sample of positions into a level's box-packed phi"""
     rng = np.random.Generator(np.random.PCG64(7000 + lev))
     return np.sort(rng.choice(size, size=min(count, size), replace=False))
+
+
+def level_solbc(case, lev):
+    """Grown level-domain array (m+2)^3 of a case with ``bc``: the initial
+    guess in the valid cells, the Dirichlet boundary values in the ghost
+    cells, both from smooth functions of the cell centres; None otherwise."""
+    if not case.get("bc"):
+        return None
+    m = case["n"] << lev
+    c = (np.arange(-1, m + 1) + 0.5) / m
+    z, y, x = np.meshgrid(c, c, c, indexing="ij")
+    bc = np.sin(3.0 * x) + 0.5 * np.cos(2.0 * y) + z * z
+    out = 0.01 * np.cos(x + y - z)
+    ghost = np.ones(out.shape, dtype=bool)
+    ghost[1:-1, 1:-1, 1:-1] = False
+    out[ghost] = bc[ghost]
+    return out
 
 
 def parse_grids(text):

@@ -43,6 +43,9 @@ def make(name, case):
         rhs = [amr_cases.level_rhs(case, lev) for lev in range(nlev)]
         for lev in range(nlev):
             rhs[lev].astype(np.float64).tofile(os.path.join(d, f"rhs_l{lev}.bin"))
+            sb = amr_cases.level_solbc(case, lev)
+            if sb is not None:
+                sb.astype(np.float64).tofile(os.path.join(d, f"solbc_l{lev}.bin"))
         thresh = [float(np.percentile(np.abs(r), 90)) for r in rhs]
         base = [f"n {n} {n} {n}", f"nlev {nlev}", f"max_grid_size {case['max_grid_size']}",
                 f"blocking_factor {case.get('blocking_factor', 8)}", "n_error_buf 1", "grid_eff 0.7",
@@ -57,7 +60,8 @@ def make(name, case):
         summary = case.get("solve") == "summary"
         lines = base + [f"tol_rel {case.get('tol_rel', 1e-10)}", "tol_abs 0.0",
                         f"agg_grid_size {case.get('agg_grid_size', 32)}",
-                        f"con_grid_size {case.get('con_grid_size', 32)}"]
+                        f"con_grid_size {case.get('con_grid_size', 32)}",
+                        f"max_fmg_iter {case.get('max_fmg_iter', 0)}"]
         for lev, g in enumerate(grids):
             lines.append(f"boxes_l{lev} " + " ".join(str(v) for b in g for v in b))
         _run("amrsolve", d, lines)
