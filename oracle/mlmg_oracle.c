@@ -1069,7 +1069,7 @@ static void free_solver(Solver* S) {
     if (S->rhs.fab) mf_free(&S->rhs);
 }
 
-static void set_coeffs(Solver* S, const OracleProblem* P) {
+static void load_coeffs(Solver* S, const OracleProblem* P) {
     Hier* H = &S->H;
     Level* L0 = &H->lev[0];
     if (!H->is_abec) return;
@@ -1081,8 +1081,18 @@ static void set_coeffs(Solver* S, const OracleProblem* P) {
         if (bp[d]) copy_global_to_mf(L0, &L0->bcoef[d], bp[d], 0, d); else mf_setval(&L0->bcoef[d], 1.0);
     }
     if (H->alpha == 0.0) mf_setval(&L0->acoef, 0.0);
-    /* averageDownCoeffsSameAmrLevel, AMReX_MLABecLaplacian.H:628-690 */
+}
+
+/* averageDownCoeffsSameAmrLevel, AMReX_MLABecLaplacian.H:628-690 */
+static void restrict_all_coeffs(Solver* S) {
+    Hier* H = &S->H;
+    if (!H->is_abec) return;
     for (int l = 1; l < H->nlev; ++l) restrict_coeffs(H, &H->lev[l - 1], &H->lev[l]);
+}
+
+static void set_coeffs(Solver* S, const OracleProblem* P) {
+    load_coeffs(S, P);
+    restrict_all_coeffs(S);
 }
 
 static int is_singular(const Solver* S) {
@@ -1484,6 +1494,47 @@ static void amr_average_down(Amr* M, int c, const MF* fine, MF* crse) {
     }
 }
 
+/* averageDownCoeffsToCoarseAmrLevel (AMReX_MLABecLaplacian.H:693-712):
+ * a (unless alpha is 0) by amr_average_down, and b by average_down_faces
+ * with the crse geometry (Src/Base/AMReX_MultiFabUtil.H:958-968): every coarse
+ * face of a coarsened fine box, its boundary faces included, takes the mean of
+ * the rr^2 fine faces on it (amrex_avgdown_faces,
+ * Src/Base/AMReX_MultiFabUtil_3D_C.H:170-225, same summation order). */
+static void amr_average_down_coeffs(Amr* M, int c) {
+    Hier* Hc = &M->S[c].H;
+    Level* Lc = &Hc->lev[0];
+    const Level* Lf = &M->S[c + 1].H.lev[0];
+    if (Hc->alpha != 0.0) amr_average_down(M, c, &Lf->acoef, &Lc->acoef);
+    for (int d = 0; d < 3; ++d) {
+        for (int b = 0; b < Lc->nbox; ++b) {
+            Fab* cf = &Lc->bcoef[d].fab[b];
+            FOR_VALID(cf, i, j, k) {
+                int lo[3] = {i, j, k};
+                lo[d] -= 1;
+                if (!covered_by_fine(M, c, i, j, k) && !covered_by_fine(M, c, lo[0], lo[1], lo[2])) continue;
+                double s = 0;
+                for (int r1 = 0; r1 < 2; ++r1)
+                for (int r0 = 0; r0 < 2; ++r0) {
+                    int f[3] = {2 * i, 2 * j, 2 * k};
+                    if (d == 0) { f[1] += r0; f[2] += r1; }
+                    else if (d == 1) { f[0] += r0; f[2] += r1; }
+                    else { f[0] += r0; f[1] += r1; }
+                    /* a fine box holding the cell on either side of the face holds the face */
+                    int wi, wj, wk;
+                    int fb = locate(Lf, Hc->periodic, f[0], f[1], f[2], &wi, &wj, &wk);
+                    if (fb < 0) {
+                        int g[3] = {f[0], f[1], f[2]};
+                        g[d] -= 1;
+                        fb = locate(Lf, Hc->periodic, g[0], g[1], g[2], &wi, &wj, &wk);
+                    }
+                    s += A(&Lf->bcoef[d].fab[fb], f[0], f[1], f[2]);
+                }
+                A(cf, i, j, k) = s * (1.0 / 4.0);
+            }
+        }
+    }
+}
+
 /* MLCellLinOpT::reflux (AMReX_MLCellLinOp.H:1272-1346) through YAFluxRegister
  * (Src/Boundary/AMReX_YAFluxRegister.H:125-335, 343-560; yafluxreg_crseadd /
  * yafluxreg_fineadd, AMReX_YAFluxRegister_3D_K.H): every coarse cell of level
@@ -1519,8 +1570,21 @@ static void amr_reflux(Amr* M, int c, MF* res) {
                     if (!covered_by_fine(M, c, n[0], n[1], n[2])) continue;
                     const double vc = cell_value(Hc, Lc, &Sc->sol, i, j, k);
                     const double vn = cell_value(Hc, Lc, &Sc->sol, n[0], n[1], n[2]);
-                    /* face flux on the face between the cell and its neighbour */
-                    const double fx = side ? Lc->dxinv[q] * (vn - vc) : Lc->dxinv[q] * (vc - vn);
+                    /* face flux on the face between the cell and its neighbour:
+                     * MLPoisson's dxinv (phi_i - phi_i-1) (mlpoisson_flux_x,
+                     * AMReX_MLPoisson_3D_K.H:36-50), MLABecLaplacian's
+                     * -beta dxinv b (phi_i - phi_i-1) (mlabeclap_flux_x,
+                     * AMReX_MLABecLap_3D_K.H:79-95) */
+                    double fx;
+                    if (Hc->is_abec) {
+                        int fc[3] = {i, j, k};
+                        if (side) fc[q] += 1;
+                        const double fac = Hc->beta * Lc->dxinv[q];
+                        const double bf = A(&Lc->bcoef[q].fab[b], fc[0], fc[1], fc[2]);
+                        fx = side ? -fac * bf * (vn - vc) : -fac * bf * (vc - vn);
+                    } else {
+                        fx = side ? Lc->dxinv[q] * (vn - vc) : Lc->dxinv[q] * (vc - vn);
+                    }
                     if (side) A(d, i, j, k) += dtdx * fx; else A(d, i, j, k) -= dtdx * fx;
                 }
             }
@@ -1558,7 +1622,14 @@ static void amr_reflux(Amr* M, int c, MF* res) {
                         fi[t2] = 2 * cc3[t2] + o2;
                         int lo3[3] = {fi[0], fi[1], fi[2]};
                         lo3[q] -= 1;
-                        const double ff = Lf->dxinv[q] * (A(fs, fi[0], fi[1], fi[2]) - A(fs, lo3[0], lo3[1], lo3[2]));
+                        double ff;
+                        if (Hf->is_abec) {
+                            const double fac = Hf->beta * Lf->dxinv[q];
+                            const double bf = A(&Lf->bcoef[q].fab[fb], fi[0], fi[1], fi[2]);
+                            ff = -fac * bf * (A(fs, fi[0], fi[1], fi[2]) - A(fs, lo3[0], lo3[1], lo3[2]));
+                        } else {
+                            ff = Lf->dxinv[q] * (A(fs, fi[0], fi[1], fi[2]) - A(fs, lo3[0], lo3[1], lo3[2]));
+                        }
                         const double tmp = side ? dtdx * ff : -dtdx * ff;
                         A(&patch, i, j, k) += tmp;
                     }
@@ -1712,7 +1783,8 @@ int oracle_solve_amr(int nlev, const OracleProblem* P, const OracleOptions* o, d
                      OracleResult* R) {
     if (nlev < 1 || nlev > AMR_MAX) return -1;
     for (int l = 0; l < nlev; ++l) {
-        if (P[l].is_abec) return -2;
+        if (P[l].is_abec != P[0].is_abec ||
+            (P[0].is_abec && (P[l].alpha != P[0].alpha || P[l].beta != P[0].beta))) return -2;
         for (int d = 0; d < 3; ++d) if (P[l].periodic[d]) return -3;
     }
     Amr* M = (Amr*)calloc(1, sizeof(Amr));
@@ -1722,7 +1794,7 @@ int oracle_solve_amr(int nlev, const OracleProblem* P, const OracleOptions* o, d
         OracleOptions ol = *o;
         if (l > 0) ol.max_coarsening_level = 0;
         setup_ratio(S, &P[l], &ol, l > 0 ? 2 : 1);
-        set_coeffs(S, &P[l]);
+        load_coeffs(S, &P[l]);
         Hier* H = &S->H;
         Level* L0 = &H->lev[0];
         S->bcval.v = P[l].sol; for (int d = 0; d < 3; ++d) S->bcval.n[d] = P[l].n[d];
@@ -1749,8 +1821,14 @@ int oracle_solve_amr(int nlev, const OracleProblem* P, const OracleOptions* o, d
         }
     }
     Solver* S0 = &M->S[0];
-    S0->singular = is_singular(S0);
     const int finest = nlev - 1;
+    /* MLABecLaplacianT::averageDownCoeffs (AMReX_MLABecLaplacian.H:610-626):
+     * finest to coarsest across AMR levels, then the MG levels of level 0 */
+    if (S0->H.is_abec) {
+        for (int l = finest; l > 0; --l) amr_average_down_coeffs(M, l - 1);
+        restrict_all_coeffs(S0);
+    }
+    S0->singular = is_singular(S0);
     /* prepareForSolve: averageDownSolutionRHS, AMReX_MLMG.H:1025-1028 */
     for (int l = finest; l > 0; --l) {
         amr_average_down(M, l - 1, &M->S[l].sol, &M->S[l - 1].sol);

@@ -192,10 +192,12 @@ def solve(case, arrays):
 
 
 def solve_amr(case, levels):
-    """Composite solve over AMR levels (ratio 2, MLPoisson).  ``case`` holds
-    the level-0 settings (n, bc, solver options); ``levels`` is a list of
-    dicts with "boxes", "rhs" (level domain, z-major) and optionally "sol"
-    (grown level domain: initial guess + boundary values; zero by default).
+    """Composite solve over AMR levels (ratio 2, MLPoisson, or MLABecLaplacian
+    with case["op"] == "abec" and its alpha, beta).  ``case`` holds the
+    level-0 settings (n, bc, solver options); ``levels`` is a list of dicts
+    with "boxes", "rhs" (level domain, z-major), optionally "sol" (grown level
+    domain: initial guess + boundary values; zero by default) and, for
+    MLABecLaplacian, "a", "bx", "by", "bz" over the level domain.
     Returns (list of level-domain phi arrays, info dict)."""
     nlev = len(levels)
     probs = (Problem * nlev)()
@@ -207,7 +209,11 @@ def solve_amr(case, levels):
         sol = L.get("sol")
         if sol is None:
             sol = np.zeros((n[2] + 2, n[1] + 2, n[0] + 2))
-        p, k = make_problem(c, {"sol": sol, "rhs": L["rhs"]})
+        arrays = {"sol": sol, "rhs": L["rhs"]}
+        for key in ("a", "bx", "by", "bz"):
+            if L.get(key) is not None:
+                arrays[key] = L[key]
+        p, k = make_problem(c, arrays)
         keep.append(k)
         probs[lev] = p
         phis.append(np.zeros((n[2], n[1], n[0])))

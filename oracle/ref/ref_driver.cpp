@@ -13,7 +13,7 @@
 //            solve  : MLMG::solve                                  -> phi.bin, result.txt
 //            flux   : solve, then getFluxes / getGradSolution    -> also f[xyz].bin, g[xyz].bin
 //            amrgrids : AmrMesh::MakeNewGrids tagging |rhs_l| > thresh_l -> grids.txt
-//            amrsolve : composite multi-level MLPoisson solve          -> phi_l<lev>.bin, result.txt
+//            amrsolve : composite multi-level MLPoisson / MLABecLaplacian solve -> phi_l<lev>.bin, result.txt
 //
 // case.txt holds "key value..." lines; binary inputs are little-endian
 // float64 arrays over the whole domain, x fastest.
@@ -254,8 +254,37 @@ int run_amr (const std::string& mode, const std::string& dir)
         dm[l] = DistributionMapping(ba[l]);
     }
     LPInfo info = make_info(c);
-    MLPoisson pois(geom, ba, dm, info);
-    setup_op(pois, c);
+    // MLPoisson, or (op abec) MLABecLaplacian with per-level a (a_l<lev>.bin)
+    // and face b (b[xyz]_l<lev>.bin) over each level's whole domain
+    const bool is_abec = c.gets("op", "poisson") == "abec";
+    std::unique_ptr<MLCellLinOp> linop;
+    if (is_abec) {
+        auto* abec = new MLABecLaplacian(geom, ba, dm, info);
+        setup_op(*abec, c);
+        abec->setScalars(c.getd("alpha", 1.0), c.getd("beta", 1.0));
+        for (int l = 0; l < nlev; ++l) {
+            const int gx = dom[l].length(0), gy = dom[l].length(1), gz = dom[l].length(2);
+            const std::string sl = "_l" + std::to_string(l) + ".bin";
+            MultiFab acoef(ba[l], dm[l], 1, 0);
+            Global ga{gx, gy, gz, 0, 0, 0, read_bin(dir + "/a" + sl, (size_t)gx*gy*gz)};
+            fill_from_global(acoef, ga, 0);
+            abec->setACoeffs(l, acoef);
+            Array<MultiFab,3> face;
+            for (int d = 0; d < 3; ++d) {
+                face[d].define(amrex::convert(ba[l], IntVect::TheDimensionVector(d)), dm[l], 1, 0);
+                Global gb{gx + (d==0), gy + (d==1), gz + (d==2), 0, 0, 0, {}};
+                gb.v = read_bin(dir + "/b" + std::string(1, char('x'+d)) + sl, (size_t)gb.nx*gb.ny*gb.nz);
+                fill_from_global(face[d], gb, 0);
+            }
+            abec->setBCoeffs(l, amrex::GetArrOfConstPtrs(face));
+        }
+        linop.reset(abec);
+    } else {
+        auto* p = new MLPoisson(geom, ba, dm, info);
+        setup_op(*p, c);
+        linop.reset(p);
+    }
+    MLCellLinOp& pois = *linop;
     Vector<MultiFab> sol(nlev), rhs(nlev);
     for (int l = 0; l < nlev; ++l) {
         sol[l].define(ba[l], dm[l], 1, 1);

@@ -1,8 +1,10 @@
 """AMR composite-solve cases: a base level of n^3 cells, refinement ratio 2,
 levels tagged where |RHS| exceeds the 90th percentile of |RHS| on that level
 (RHS: the seeded sum of 16 Gaussian blobs sampled at each level's cell
-centres), homogeneous Dirichlet on the domain, MLPoisson.  Grids come from the
-reference's AmrMesh (tests/golden/make_amr_golden.py)."""
+centres), homogeneous Dirichlet on the domain (or, with ``bc``, seeded
+Dirichlet values and initial guess), MLPoisson (or, with ``abec``,
+MLABecLaplacian).  Grids come from the reference's AmrMesh
+(tests/golden/make_amr_golden.py)."""
 from __future__ import annotations
 
 import ast
@@ -25,6 +27,11 @@ CASES = {
     "c2_n16_2lev_bc": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1012, bc=True),
     # F-cycles on AMR level 0 for the first two iterations
     "c2_n32_fmg": dict(n=32, nlev=3, max_grid_size=16, rhs_seed=1002, max_fmg_iter=2, solve="summary"),
+    # MLABecLaplacian with per-level a and face b (level_abec): coefficients
+    # averaged down across AMR levels, fluxes beta b grad(phi) in the reflux
+    "c2_n16_2lev_abec": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1012, abec=(0.75, 1.25)),
+    "c2_n32_abec": dict(n=32, nlev=3, max_grid_size=16, rhs_seed=1002, abec=(0.75, 1.25), bc=True,
+                        solve="summary"),
 }
 
 
@@ -54,6 +61,30 @@ def level_solbc(case, lev):
     ghost[1:-1, 1:-1, 1:-1] = False
     out[ghost] = bc[ghost]
     return out
+
+
+def level_abec(case, lev):
+    """(alpha, beta, a, bx, by, bz) of a case with ``abec``: a at the cell
+    centres, (m, m, m); b_d at the face centres normal to d, m+1 faces along
+    d (arrays indexed z, y, x) -- smooth positive functions of position with
+    an order-one variation, so that the coarse and fine samplings differ;
+    None otherwise."""
+    if not case.get("abec"):
+        return None
+    alpha, beta = case["abec"]
+    m = case["n"] << lev
+    cc = (np.arange(m) + 0.5) / m
+    fc = np.arange(m + 1) / m
+    z, y, x = np.meshgrid(cc, cc, cc, indexing="ij")
+    a = 1.0 + 0.5 * np.sin(5.0 * x + 1.0) * np.cos(3.0 * y) + 0.25 * z
+
+    def b(x, y, z):
+        return 1.0 + 0.6 * np.cos(4.0 * x - 1.0) * np.sin(3.0 * y + z) + 0.3 * x * z
+
+    bx = b(*np.meshgrid(cc, cc, fc, indexing="ij")[::-1])
+    by = b(*np.meshgrid(cc, fc, cc, indexing="ij")[::-1])
+    bz = b(*np.meshgrid(fc, cc, cc, indexing="ij")[::-1])
+    return alpha, beta, a, bx, by, bz
 
 
 def parse_grids(text):

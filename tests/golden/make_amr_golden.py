@@ -5,7 +5,7 @@
   level tags the cells where |RHS| exceeds the 90th percentile of |RHS| on
   that level (blocking factor 8, max_grid_size, n_error_buf 1, grid_eff 0.7);
 * ``amrsolve_<name>.npz``: the reference's composite multi-level MLPoisson
-  solve on those grids -- phi on every level's boxes (for the configuration-
+  (or MLABecLaplacian) solve on those grids -- phi on every level's boxes (for the configuration-
   size case only per-level statistics and phi at seeded sample cells),
   residual history and bottom iteration counts.
 
@@ -46,6 +46,10 @@ def make(name, case):
             sb = amr_cases.level_solbc(case, lev)
             if sb is not None:
                 sb.astype(np.float64).tofile(os.path.join(d, f"solbc_l{lev}.bin"))
+            co = amr_cases.level_abec(case, lev)
+            if co is not None:
+                for key, arr in zip(("a", "bx", "by", "bz"), co[2:]):
+                    arr.astype(np.float64).tofile(os.path.join(d, f"{key}_l{lev}.bin"))
         thresh = [float(np.percentile(np.abs(r), 90)) for r in rhs]
         base = [f"n {n} {n} {n}", f"nlev {nlev}", f"max_grid_size {case['max_grid_size']}",
                 f"blocking_factor {case.get('blocking_factor', 8)}", "n_error_buf 1", "grid_eff 0.7",
@@ -62,6 +66,8 @@ def make(name, case):
                         f"agg_grid_size {case.get('agg_grid_size', 32)}",
                         f"con_grid_size {case.get('con_grid_size', 32)}",
                         f"max_fmg_iter {case.get('max_fmg_iter', 0)}"]
+        if case.get("abec"):
+            lines += ["op abec", f"alpha {case['abec'][0]!r}", f"beta {case['abec'][1]!r}"]
         for lev, g in enumerate(grids):
             lines.append(f"boxes_l{lev} " + " ".join(str(v) for b in g for v in b))
         _run("amrsolve", d, lines)

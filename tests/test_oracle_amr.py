@@ -1,5 +1,5 @@
 """The oracle's AMR composite solve (MLMG over several AMR levels, refinement
-ratio 2, MLPoisson) against the reference's own composite solves on
+ratio 2, MLPoisson and MLABecLaplacian) against the reference's own composite solves on
 AmrMesh-generated grids (tests/golden/amrsolve_*.npz)."""
 from __future__ import annotations
 
@@ -12,9 +12,12 @@ from tests.golden import amr_cases as ac
 
 def oracle_case(case):
     n = case["n"]
-    return dict(n=(n, n, n), tol_rel=case.get("tol_rel", 1e-10), tol_abs=0.0,
-                agg_grid_size=case.get("agg_grid_size", 32), con_grid_size=case.get("con_grid_size", 32),
-                max_fmg_iter=case.get("max_fmg_iter", 0))
+    out = dict(n=(n, n, n), tol_rel=case.get("tol_rel", 1e-10), tol_abs=0.0,
+               agg_grid_size=case.get("agg_grid_size", 32), con_grid_size=case.get("con_grid_size", 32),
+               max_fmg_iter=case.get("max_fmg_iter", 0))
+    if case.get("abec"):
+        out.update(op="abec", alpha=case["abec"][0], beta=case["abec"][1])
+    return out
 
 
 def levels_of(case, grids):
@@ -24,16 +27,22 @@ def levels_of(case, grids):
         sb = ac.level_solbc(case, lev)
         if sb is not None:
             L["sol"] = sb
+        co = ac.level_abec(case, lev)
+        if co is not None:
+            L.update(zip(("a", "bx", "by", "bz"), co[2:]))
         out.append(L)
     return out
 
 
-@pytest.mark.parametrize("name", ["c2_n16_2lev", "c2_n32", "c2_n16_2lev_bc", "c2_n32_fmg"])
+@pytest.mark.parametrize("name", ["c2_n16_2lev", "c2_n32", "c2_n16_2lev_bc", "c2_n32_fmg", "c2_n16_2lev_abec",
+                                  "c2_n32_abec"])
 def test_oracle_amr_matches_reference(name):
     """Iteration and bottom counts, norms, residual history and phi (every
     cell, or per-level statistics and seeded samples for summary fixtures);
     the cases cover 2 and 3 levels, inhomogeneous Dirichlet values with a
-    non-zero initial guess, and F-cycles on AMR level 0."""
+    non-zero initial guess, F-cycles on AMR level 0, and MLABecLaplacian with
+    per-level coefficients (averaged down across levels before level 0's MG
+    restriction)."""
     g = ac.load("amrsolve", name)
     case, grids, ref = g["case"], g["grids"], g["result"]
     phis, info = oracle.solve_amr(oracle_case(case), levels_of(case, grids))
@@ -60,7 +69,7 @@ def test_amr_grids_are_properly_nested():
     """Every fixture's finer boxes sit inside the next coarser level grown by
     one coarse cell (AmrMesh proper nesting), the premise of the oracle's and
     the engine's coarse/fine boundary interpolation."""
-    for name in ("c2", "c2_n32", "c2_n16_2lev"):
+    for name in ("c2", "c2_n32", "c2_n16_2lev", "c2_n16_2lev_abec", "c2_n32_abec"):
         g = ac.load("amrgrids", name)
         n = g["case"]["n"]
         grids = g["grids"]
