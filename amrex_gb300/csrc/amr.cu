@@ -1,5 +1,5 @@
 // AMR composite MLMG (MLMGT::solve over several AMR levels, refinement ratio
-// 2, MLPoisson): host orchestration of MLMGT::oneIter (AMReX_MLMG.H:1227-1293)
+// 2, MLPoisson or MLABecLaplacian): host orchestration of MLMGT::oneIter (AMReX_MLMG.H:1227-1293)
 // over one engine per AMR level, with the coarse/fine kernels of
 // amr_kernels.cuh.  FP64 throughout, or (precision 1) FP32 corrections --
 // the V-cycle of AMR level 0, the fine levels' smoothing sweeps and the
@@ -62,6 +62,12 @@ struct AmrLevelData {
     DevBuf<RefluxFace> rfaces;
     int nrcell = 0;
     RefluxParams rprm{};
+    // MLABecLaplacian: face average-down tags per direction (coarse faces of
+    // the coarsened fine patches)
+    DevBuf<CopyTag> ftags[3];
+    DevBuf<long long> fstart[3];
+    int nftag[3] = {0, 0, 0};
+    long long nfcell[3] = {0, 0, 0};
 };
 
 struct AmrEngine::Impl {
@@ -86,9 +92,12 @@ struct AmrEngine::Impl {
     void launched (int n = 1) { own_launches += n; }
     LevelData& L (int l) { return lev[l].I->lev[0]; }
 
+    bool abec () const { return prob.is_abec != 0; }
     void build ();
     void build_fine_tables (int l);
     void build_coarse_tables (int c);
+    void average_down_coefficients ();
+    RefluxCoef reflux_coef (int c);
 
     // operations
     void solution_residual (int l, bool update, bool want_norm = false);
@@ -144,11 +153,17 @@ void AmrEngine::Impl::build ()
             S.dx0[d] = (S.geom.prob_hi[d] - S.geom.prob_lo[d]) / (double)S.geom.domain.len(d);
         }
         S.maxorder = prob.maxorder;
-        S.is_abec = 0; S.alpha = 0.0; S.beta = 1.0;
+        S.is_abec = prob.is_abec;
+        S.alpha = prob.is_abec ? prob.alpha : 0.0;
+        S.beta = prob.is_abec ? prob.beta : 1.0;
         S.crse_ratio = (l > 0) ? 2 : 1;
         S.amr_fine = (l > 0) ? 1 : 0;
         pr.boxes = prob.levels[l].boxes;
         pr.levelbc = prob.levels[l].levelbc;
+        if (prob.is_abec) {
+            pr.acoef = prob.levels[l].acoef;
+            for (int d = 0; d < 3; ++d) { pr.bcoef[d] = prob.levels[l].bcoef[d]; }
+        }
         EngineOptions o = A.m_opt;
         o.max_fmg_iter = 0;
         o.transpose = 0;
@@ -187,6 +202,7 @@ void AmrEngine::Impl::build ()
         if (l > 0) { build_fine_tables(l); }
         if (l < nl - 1) { build_coarse_tables(l); }
     }
+    if (abec()) { average_down_coefficients(); }
     h_norm.alloc(4 * (size_t)nl + 4);
     MLMG_CUDA_CHECK(cudaEventCreate(&ev0));
     MLMG_CUDA_CHECK(cudaEventCreate(&ev1));
@@ -286,7 +302,7 @@ void AmrEngine::Impl::build_fine_tables (int l)
     D.bcor.zero(st());
     // neighbour table of the ghost-free colour passes: every copy-tag cell
     // (a ghost covered by another patch) points at its source cell
-    bool short_closures = true;
+    bool short_closures = !abec();     // the ghost-free passes have MLPoisson's stencil
     for (const PatchDesc& P : Mf.patches) {
         for (int f = 0; f < 6; ++f) {
             if (P.face[f].type == BC_DIRICHLET && P.face[f].nx > 3) { short_closures = false; }
@@ -382,6 +398,9 @@ void AmrEngine::Impl::build_coarse_tables (int c)
                 e.q = cidx(Mc.patches[cp], i, j, k);
                 e.key = 2 * d + side;
                 e.f.qn = cidx(Mc.patches[cpn], n[0], n[1], n[2]);
+                int fc[3] = {i, j, k};
+                if (side) { fc[d] += 1; }
+                e.f.qb = cidx(Mc.patches[cp], fc[0], fc[1], fc[2]);
                 e.f.qf = cidx(F, fi[0], fi[1], fi[2]);
                 e.f.fp = fp;
                 e.f.dir = d;
@@ -405,6 +424,74 @@ void AmrEngine::Impl::build_coarse_tables (int c)
         D.rprm.dxinv_c[d] = Mc.patches[0].dxinv[d];
         D.rprm.dxinv_f[d] = Mf.patches[0].dxinv[d];
     }
+    // face average-down tags: the faces of each coarsened fine patch (its
+    // boundary faces included) within the faces of each coarse patch
+    if (abec()) {
+        for (int d = 0; d < 3; ++d) {
+            std::vector<CopyTag> ft;
+            std::vector<long long> fs{0};
+            for (int fp = 0; fp < (int)Mf.patches.size(); ++fp) {
+                Box3 fb = cfboxes[fp];
+                fb.hi[d] += 1;
+                for (int cp = 0; cp < (int)Mc.patches.size(); ++cp) {
+                    Box3 cb = pbox(Mc.patches[cp]);
+                    cb.hi[d] += 1;
+                    const Box3 is = intersect(fb, cb);
+                    if (!is.ok()) { continue; }
+                    CopyTag t{};
+                    t.dst = cp; t.src = fp; t.box = is;
+                    ft.push_back(t);
+                    fs.push_back(fs.back() + is.npts());
+                }
+            }
+            D.nftag[d] = (int)ft.size();
+            D.nfcell[d] = fs.back();
+            upload_or_keep(D.ftags[d], ft, st());
+            D.fstart[d].upload(fs, st());
+        }
+    }
+}
+
+// MLABecLaplacianT::averageDownCoeffs (AMReX_MLABecLaplacian.H:610-626): from
+// the finest AMR level down, a (unless alpha is 0) onto the covered cells and
+// b onto the faces of the coarsened fine patches of the next coarser level
+// (averageDownCoeffsToCoarseAmrLevel, :693-712); then every level's own MG
+// restriction and stencil form again from the averaged coefficients.
+void AmrEngine::Impl::average_down_coefficients ()
+{
+    for (int c = nl - 2; c >= 0; --c) {
+        AmrLevelData& D = lev[c];
+        LevelData& Lc = L(c);
+        LevelData& Lf = L(c + 1);
+        if (prob.alpha != 0.0 && D.nacell > 0) {
+            k_amr_avgdown<double, double><<<blocks_for(D.nacell, 256), 256, 0, st()>>>(Lc.dl, Lf.dl, D.atags.p,
+                D.astart.p, D.natag, D.nacell, Lf.a.p, Lc.a.p);
+            launched();
+        }
+        const double* fb[3] = {Lf.bx.p, Lf.by.p, Lf.bz.p};
+        double* cb[3] = {Lc.bx.p, Lc.by.p, Lc.bz.p};
+        for (int d = 0; d < 3; ++d) {
+            if (D.nfcell[d] == 0) { continue; }
+            k_amr_avgdown_faces<<<blocks_for(D.nfcell[d], 256), 256, 0, st()>>>(Lc.dl, Lf.dl, D.ftags[d].p,
+                D.fstart[d].p, D.nftag[d], D.nfcell[d], d, fb[d], cb[d]);
+            launched();
+        }
+    }
+    MLMG_CUDA_CHECK(cudaGetLastError());
+    for (int l = 0; l < nl - 1; ++l) { lev[l].eng->restrict_coefficients(); }
+}
+
+RefluxCoef AmrEngine::Impl::reflux_coef (int c)
+{
+    RefluxCoef co{};
+    if (abec()) {
+        LevelData& Lc = L(c);
+        LevelData& Lf = L(c + 1);
+        co.bc[0] = Lc.bx.p; co.bc[1] = Lc.by.p; co.bc[2] = Lc.bz.p;
+        co.bf[0] = Lf.bx.p; co.bf[1] = Lf.by.p; co.bf[2] = Lf.bz.p;
+        co.beta = prob.beta;
+    }
+    return co;
 }
 
 // ------------------------------------------------------------- operations --
@@ -455,13 +542,24 @@ void AmrEngine::Impl::solution_residual (int l, bool update, bool want_norm)
         // stencil form (D x - sum s x_nb: 8 FP64 operations per cell instead of
         // 14), with the level's max|r| by atomic max into red_out[0]
         if (want_norm) { MLMG_CUDA_CHECK(cudaMemsetAsync(I.red_out.p, 0, sizeof(double), st())); }
-        k_residual_s<double, double, false, false, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl,
-            Ld.all.dev(), Ld.res.p, Ld.sol.p, Ld.rhs.p, StencilPtrs{}, nullptr, want_norm ? I.red_out.p : nullptr);
+        if (abec()) {
+            k_residual_s<double, double, true, false, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl,
+                Ld.all.dev(), Ld.res.p, Ld.sol.p, Ld.rhs.p, I.stencil64(0), nullptr, want_norm ? I.red_out.p : nullptr);
+        } else {
+            k_residual_s<double, double, false, false, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl,
+                Ld.all.dev(), Ld.res.p, Ld.sol.p, Ld.rhs.p, StencilPtrs{}, nullptr, want_norm ? I.red_out.p : nullptr);
+        }
         launched();
     } else {
-        // the reference's operation order (MLPoissonT::Fapply), block maxima for the norm
-        k_residual<double, double, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res.p,
-            Ld.sol.p, Ld.rhs.p, nullptr, nullptr, nullptr, nullptr, want_norm ? I.partial.p : nullptr);
+        // the reference's operation order (MLPoissonT::Fapply / MLABecLaplacianT::Fapply),
+        // block maxima for the norm
+        if (abec()) {
+            k_residual<double, double, true><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res.p,
+                Ld.sol.p, Ld.rhs.p, Ld.a.p, Ld.bx.p, Ld.by.p, Ld.bz.p, want_norm ? I.partial.p : nullptr);
+        } else {
+            k_residual<double, double, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res.p,
+                Ld.sol.p, Ld.rhs.p, nullptr, nullptr, nullptr, nullptr, want_norm ? I.partial.p : nullptr);
+        }
         launched();
         if (want_norm) {
             k_reduce_final<<<1, 1024, 0, st()>>>(I.partial.p, Ld.all.solve_begin.p, RED_MAXABS, I.red_out.p);
@@ -478,8 +576,13 @@ void AmrEngine::Impl::reflux (int c)
     AmrLevelData& D = lev[c];
     lev[c + 1].I->ghost<double>(0, Lf.sol.p, true, true, Lf.bcval.p);
     if (D.nrcell > 0) {
-        k_amr_reflux<<<blocks_for(D.nrcell, 128), 128, 0, st()>>>(Lf.dl, D.rcells.p, D.rfaces.p, D.nrcell, D.rprm,
-                                                                  Lc.sol.p, Lf.sol.p, Lc.res.p);
+        if (abec()) {
+            k_amr_reflux<true><<<blocks_for(D.nrcell, 128), 128, 0, st()>>>(Lf.dl, D.rcells.p, D.rfaces.p, D.nrcell,
+                D.rprm, reflux_coef(c), Lc.sol.p, Lf.sol.p, Lc.res.p);
+        } else {
+            k_amr_reflux<false><<<blocks_for(D.nrcell, 128), 128, 0, st()>>>(Lf.dl, D.rcells.p, D.rfaces.p, D.nrcell,
+                D.rprm, RefluxCoef{}, Lc.sol.p, Lf.sol.p, Lc.res.p);
+        }
         launched();
     }
 }
@@ -536,7 +639,14 @@ void AmrEngine::Impl::cor_residual (int l, bool inhomog, const TB* b, TO* out)
     } else {
         D.I->ghost<T>(0, x, false, true);
     }
-    k_amr_resid<T, TB, TO><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), out, x, b);
+    if (abec()) {
+        const StencilPtrs sp = std::is_same_v<T, float> ? D.I->stencil32(0) : StencilPtrs{};
+        k_amr_resid<T, TB, TO, true><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), out, x, b, Ld.a.p,
+            Ld.bx.p, Ld.by.p, Ld.bz.p, sp);
+    } else {
+        k_amr_resid<T, TB, TO, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), out, x, b, nullptr,
+            nullptr, nullptr, nullptr, StencilPtrs{});
+    }
     launched();
 }
 

@@ -1,5 +1,5 @@
 // The AMR composite MLMG solve: MLMGT::solve over several AMR levels
-// (refinement ratio 2, MLPoisson).  AMR level 0 is a full single-level
+// (refinement ratio 2, MLPoisson or MLABecLaplacian).  AMR level 0 is a full single-level
 // engine (its own MG hierarchy, bottom solve, graphs); each finer AMR level is
 // an engine of one MG level that is only smoothed.  The coarse/fine coupling
 // (boundary-value interpolation, flux-register reflux, average-down,
@@ -16,6 +16,8 @@ namespace mlmg {
 struct AmrLevelProblem {
     std::vector<Box3> boxes;            // the AMR level's BoxArray (level-l index space)
     const FabSet* levelbc = nullptr;    // Dirichlet values in its ghost cells; null = 0
+    const FabSet* acoef = nullptr;      // MLABecLaplacian: cell-centred a; null = 1
+    const FabSet* bcoef[3] = {nullptr, nullptr, nullptr};  // face b; null = 1
 };
 
 struct AmrProblem {
@@ -23,6 +25,8 @@ struct AmrProblem {
     int lobc[3] = {BC_DIRICHLET, BC_DIRICHLET, BC_DIRICHLET};
     int hibc[3] = {BC_DIRICHLET, BC_DIRICHLET, BC_DIRICHLET};
     int maxorder = 3;
+    int is_abec = 0;                    // MLABecLaplacian (alpha a - beta div b grad) or MLPoisson
+    double alpha = 0.0, beta = 1.0;
     LPInfoC info;                       // MG coarsening of AMR level 0
     std::vector<AmrLevelProblem> levels;
 };

@@ -1,5 +1,5 @@
 // Coarse/fine coupling kernels of the AMR composite solve (refinement ratio
-// 2, MLPoisson).  Every kernel reads index tables built on the host from the
+// 2, MLPoisson or MLABecLaplacian).  Every kernel reads index tables built on the host from the
 // two levels' patch layouts, so a launch covers every box of a level.
 #pragma once
 
@@ -61,6 +61,33 @@ __global__ void k_amr_avgdown (DevLevel Lc, DevLevel Lf, const CopyTag* __restri
     v += (double)fine[qf + sxy];      v += (double)fine[qf + sxy + 1];
     v += (double)fine[qf + sxy + sx]; v += (double)fine[qf + sxy + sx + 1];
     crse[cidx(Lc.P[C.dst], i, j, k)] = TD(0.125 * v);
+}
+
+// average_down_faces with the coarse geometry (Src/Base/AMReX_MultiFabUtil.H:
+// 958-968; amrex_avgdown_faces, AMReX_MultiFabUtil_3D_C.H:170-225) of the face
+// coefficient b_dir: every coarse face of a coarsened fine patch, its boundary
+// faces included, takes the mean of the 2x2 fine faces on it, summed with the
+// second tangential offset outermost.  Tag dst = coarse patch, src = fine
+// patch, box = coarse faces (face i stored at cell index i of the patch).
+__global__ void k_amr_avgdown_faces (DevLevel Lc, DevLevel Lf, const CopyTag* __restrict__ tags,
+                                     const long long* __restrict__ start, int ntag, long long ncell, int dir,
+                                     const double* __restrict__ fine, double* __restrict__ crse)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell) { return; }
+    int w, i, j, k;
+    tag_cell(tags, start, ntag, t, w, i, j, k);
+    const CopyTag& C = tags[w];
+    const PatchDesc& F = Lf.P[C.src];
+    const long long st[3] = {1, (long long)F.sx, F.sxy};
+    const int t1 = (dir == 0) ? 1 : 0, t2 = (dir == 2) ? 1 : 2;
+    const long long qf = cidx(F, 2 * i, 2 * j, 2 * k);
+    double c = 0.0;
+    c += fine[qf];
+    c += fine[qf + st[t1]];
+    c += fine[qf + st[t2]];
+    c += fine[qf + st[t1] + st[t2]];
+    crse[cidx(Lc.P[C.dst], i, j, k)] = c * 0.25;
 }
 
 // bits of the per-face-cell neighbourhood flags of the boundary interpolation
@@ -135,12 +162,18 @@ struct RefluxCell {
 struct RefluxFace {
     long long qn;       // element index of the covered coarse neighbour (in its own patch)
     long long qf;       // element index of the fine cell inside the fine patch at sub-face (0,0)
+    long long qb;       // element index of the coarse face in the cell's patch (face coefficients)
     int fp;             // fine patch
     int dir, side;      // face direction; side 1: the neighbour (and the fine level) lies at +dir
 };
 struct RefluxParams {
     double dxinv_c[3];  // coarse 1/dx
     double dxinv_f[3];  // fine 1/dx
+};
+struct RefluxCoef {     // MLABecLaplacian: beta and the face b of both levels
+    const double* bc[3];
+    const double* bf[3];
+    double beta;
 };
 
 // MLCellLinOpT::reflux (AMReX_MLCellLinOp.H:1272-1346) through YAFluxRegister
@@ -150,8 +183,12 @@ struct RefluxParams {
 // flux F = (phi_hi - phi_lo)/dx.  The fine solution's ghosts must hold the
 // inhomogeneous applyBC values.  Coarse contributions are summed first, in
 // face order, then the fine ones (the register adds its fine patches last).
+// The face flux is MLPoisson's dxinv (phi_i - phi_i-1) (mlpoisson_flux_x,
+// AMReX_MLPoisson_3D_K.H:36-50) or MLABecLaplacian's
+// -beta dxinv b_i (phi_i - phi_i-1) (mlabeclap_flux_x, AMReX_MLABecLap_3D_K.H:79-95).
+template <bool ABEC>
 __global__ void k_amr_reflux (DevLevel Lf, const RefluxCell* __restrict__ cells, const RefluxFace* __restrict__ faces,
-                              int ncell, RefluxParams prm, const double* __restrict__ sol_c,
+                              int ncell, RefluxParams prm, RefluxCoef co, const double* __restrict__ sol_c,
                               const double* __restrict__ sol_f, double* __restrict__ res_c)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -163,8 +200,10 @@ __global__ void k_amr_reflux (DevLevel Lf, const RefluxCell* __restrict__ cells,
         const RefluxFace& R = faces[e];
         const double dtdx = prm.dxinv_c[R.dir];
         const double vn = sol_c[R.qn];
-        if (R.side) { dc += dtdx * (prm.dxinv_c[R.dir] * (vn - vc)); }
-        else { dc -= dtdx * (prm.dxinv_c[R.dir] * (vc - vn)); }
+        double fac = prm.dxinv_c[R.dir];
+        if constexpr (ABEC) { fac = -(co.beta * prm.dxinv_c[R.dir]) * co.bc[R.dir][R.qb]; }
+        if (R.side) { dc += dtdx * (fac * (vn - vc)); }
+        else { dc -= dtdx * (fac * (vc - vn)); }
     }
     double dfine = 0.0;
     for (int e = C.e0; e < C.e0 + C.ne; ++e) {
@@ -178,10 +217,13 @@ __global__ void k_amr_reflux (DevLevel Lf, const RefluxCell* __restrict__ cells,
         for (int o2 = 0; o2 < 2; ++o2)
         for (int o1 = 0; o1 < 2; ++o1) {
             const long long qi = R.qf + o1 * st[t1] + o2 * st[t2];
+            double fac = prm.dxinv_f[R.dir];
             if (R.side) {   // fine level above: the fine box's low face, ghost below
-                acc += -dtdx * (prm.dxinv_f[R.dir] * (sol_f[qi] - sol_f[qi - sd]));
+                if constexpr (ABEC) { fac = -(co.beta * prm.dxinv_f[R.dir]) * co.bf[R.dir][qi]; }
+                acc += -dtdx * (fac * (sol_f[qi] - sol_f[qi - sd]));
             } else {        // fine level below: the fine box's high face, ghost above
-                acc += dtdx * (prm.dxinv_f[R.dir] * (sol_f[qi + sd] - sol_f[qi]));
+                if constexpr (ABEC) { fac = -(co.beta * prm.dxinv_f[R.dir]) * co.bf[R.dir][qi + sd]; }
+                acc += dtdx * (fac * (sol_f[qi + sd] - sol_f[qi]));
             }
         }
         dfine += acc;
@@ -218,12 +260,15 @@ k_amr_norm (DevLevel L, Subset S, const T* __restrict__ x, const int8_t* __restr
     if (threadIdx.x == 0 && threadIdx.y == 0) { partial[blockIdx.x] = red; }
 }
 
-// r = b - A x over valid cells (MLPoisson, BCs already in x's ghosts), with A x
-// evaluated in x's precision: the correction residuals of the composite
-// iteration, b and r in either precision
-template <typename TX, typename TB, typename TO>
+// r = b - A x over valid cells (BCs already in x's ghosts), with A x evaluated
+// in x's precision: the correction residuals of the composite iteration, b
+// and r in either precision.  MLABecLaplacian reads a and b in FP64, or the
+// FP32 stencil form for FP32 corrections.
+template <typename TX, typename TB, typename TO, bool ABEC>
 __global__ void __launch_bounds__(TILE_THREADS)
-k_amr_resid (DevLevel L, Subset S, TO* __restrict__ r, const TX* __restrict__ x, const TB* __restrict__ b)
+k_amr_resid (DevLevel L, Subset S, TO* __restrict__ r, const TX* __restrict__ x, const TB* __restrict__ b,
+             const double* __restrict__ a, const double* __restrict__ bx, const double* __restrict__ by,
+             const double* __restrict__ bz, StencilPtrs sp)
 {
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchDesc& P = L.P[c.p];
@@ -237,7 +282,18 @@ k_amr_resid (DevLevel L, Subset S, TO* __restrict__ r, const TX* __restrict__ x,
             const int i = c.x0 + threadIdx.x + 32 * h;
             if (i > P.hi[0]) { continue; }
             const long long q = cidx(P, i, j, k);
-            const TX ax = adotx_cell<TX, false>(P, q, x, nullptr, nullptr, nullptr, nullptr);
+            TX ax;
+            if constexpr (!ABEC) {
+                ax = adotx_cell<TX, false>(P, q, x, nullptr, nullptr, nullptr, nullptr);
+            } else if constexpr (std::is_same_v<TX, double>) {
+                ax = adotx_cell<double, true>(P, q, x, a, bx, by, bz);
+            } else {
+                // FP32 corrections: the stencil form D x - sum s x_nb
+                const Coef7<TX, true> cf = load_coef<TX, true>(P, q, sp);
+                const long long sx = P.sx, sxy = P.sxy;
+                ax = cf.d * x[q] - (cf.sxl * x[q - 1] + cf.sxh * x[q + 1] + cf.syl * x[q - sx] + cf.syh * x[q + sx]
+                                    + cf.szl * x[q - sxy] + cf.szh * x[q + sxy]);
+            }
             r[q] = TO(TX(b[q]) - ax);
         }
     }

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -286,12 +287,20 @@ struct mlmg_linop_s {
     FabSet acoef_fs, bcoef_fs[3], levelbc_fs;
     int struct_version = 0, coef_version = 0;
     std::vector<LevelGrids> levels;
-    // AMR levels (composite MLPoisson): level l's BoxArray and level BC values
-    // (amr_boxes[0] == boxes, amr_levelbc[0] unused: levelbc holds level 0's)
+    // AMR levels (composite solves): level l's BoxArray, level BC values and
+    // (MLABecLaplacian) coefficients; entry 0 of amr_levelbc / amr_acoef /
+    // amr_bcoef is unused, levelbc / acoef / bcoef hold level 0's
     int nlev = 1;
     std::vector<std::vector<Box3>> amr_boxes;
     std::vector<std::unique_ptr<mlmg_multifab_s>> amr_levelbc;
     std::vector<FabSet> amr_levelbc_fs;
+    std::vector<std::unique_ptr<mlmg_multifab_s>> amr_acoef;
+    std::vector<std::array<std::unique_ptr<mlmg_multifab_s>, 3>> amr_bcoef;
+    std::vector<FabSet> amr_acoef_fs;
+    std::vector<std::array<FabSet, 3>> amr_bcoef_fs;
+    const std::vector<Box3>& level_boxes (int l) const { return l == 0 ? boxes : amr_boxes[l]; }
+    std::unique_ptr<mlmg_multifab_s>& level_acoef (int l) { return l == 0 ? acoef : amr_acoef[l]; }
+    std::unique_ptr<mlmg_multifab_s>& level_bcoef (int l, int d) { return l == 0 ? bcoef[d] : amr_bcoef[l][d]; }
     void regrid () { levels = define_grids(geom, boxes, info); ++struct_version; }
 };
 
@@ -444,12 +453,29 @@ AmrEngine& amr_engine_for (mlmg_solver s)
         for (int d = 0; d < 3; ++d) { P.lobc[d] = op->lobc[d]; P.hibc[d] = op->hibc[d]; }
         P.maxorder = op->maxorder;
         P.info = op->info;
+        P.is_abec = op->is_abec;
+        if (op->is_abec) {
+            MLMG_REQUIRE(!std::isnan(op->alpha) && !std::isnan(op->beta), ERR_ARGS,
+                         "MLABecLaplacian: setScalars has not been called");
+            P.alpha = op->alpha; P.beta = op->beta;
+        }
         op->amr_levelbc_fs.assign(op->nlev, FabSet{});
+        op->amr_acoef_fs.assign(op->nlev, FabSet{});
+        op->amr_bcoef_fs.assign(op->nlev, std::array<FabSet, 3>{});
         for (int l = 0; l < op->nlev; ++l) {
             AmrLevelProblem L;
             L.boxes = op->amr_boxes[l];
             const mlmg_multifab_s* bc = (l == 0) ? op->levelbc.get() : op->amr_levelbc[l].get();
             if (bc) { op->amr_levelbc_fs[l] = bc->fabset(); L.levelbc = &op->amr_levelbc_fs[l]; }
+            if (op->is_abec) {
+                if (auto& a = op->level_acoef(l)) { op->amr_acoef_fs[l] = a->fabset(); L.acoef = &op->amr_acoef_fs[l]; }
+                for (int d = 0; d < 3; ++d) {
+                    if (auto& b = op->level_bcoef(l, d)) {
+                        op->amr_bcoef_fs[l][d] = b->fabset();
+                        L.bcoef[d] = &op->amr_bcoef_fs[l][d];
+                    }
+                }
+            }
             P.levels.push_back(L);
         }
         s->amr_eng = std::make_unique<AmrEngine>(P, s->opt, lib_stream());
@@ -798,8 +824,6 @@ static int linop_new (int is_abec, int nlev, const mlmg_geometry* geom, const ml
     API_BEGIN
     MLMG_REQUIRE(out && geom && ba && dm && geom[0] && ba[0] && dm[0], ERR_ARGS, "null handle");
     MLMG_REQUIRE(nlev >= 1 && nlev <= 8, ERR_ARGS, "nlev must be in 1..8");
-    MLMG_REQUIRE(nlev == 1 || !is_abec, ERR_UNSUPPORTED,
-                 "composite (multi-AMR-level) solves are implemented for MLPoisson only");
     auto op = std::make_unique<mlmg_linop_s>();
     op->is_abec = is_abec;
     op->geom = geom[0]->g;
@@ -824,6 +848,8 @@ static int linop_new (int is_abec, int nlev, const mlmg_geometry* geom, const ml
     op->nlev = nlev;
     op->amr_boxes.assign(1, op->boxes);
     op->amr_levelbc.resize(nlev);
+    op->amr_acoef.resize(nlev);
+    op->amr_bcoef.resize(nlev);
     for (int l = 1; l < nlev; ++l) {
         MLMG_REQUIRE(geom[l] && ba[l] && dm[l], ERR_ARGS, "null handle");
         const GeomC& g = geom[l]->g;
@@ -924,10 +950,10 @@ int mlmg_abeclap_set_scalars (mlmg_linop op, double alpha, double beta)
 int mlmg_abeclap_set_acoeffs (mlmg_linop op, int amrlev, mlmg_multifab a)
 {
     API_BEGIN
-    MLMG_REQUIRE(op && op->is_abec && amrlev == 0 && a, ERR_ARGS, "bad arguments");
-    MLMG_REQUIRE(a->boxes == op->boxes && a->nodal_dir == -1 && a->ncomp == 1, ERR_ARGS,
-                 "a must be a one-component cell-centred MultiFab on the operator's BoxArray");
-    op->acoef = clone_mf(*a);
+    MLMG_REQUIRE(op && op->is_abec && amrlev >= 0 && amrlev < op->nlev && a, ERR_ARGS, "bad arguments");
+    MLMG_REQUIRE(a->boxes == op->level_boxes(amrlev) && a->nodal_dir == -1 && a->ncomp == 1, ERR_ARGS,
+                 "a must be a one-component cell-centred MultiFab on the level's BoxArray");
+    op->level_acoef(amrlev) = clone_mf(*a);
     ++op->coef_version;
     API_END
 }
@@ -935,9 +961,9 @@ int mlmg_abeclap_set_acoeffs (mlmg_linop op, int amrlev, mlmg_multifab a)
 int mlmg_abeclap_set_acoeffs_const (mlmg_linop op, int amrlev, double a)
 {
     API_BEGIN
-    MLMG_REQUIRE(op && op->is_abec && amrlev == 0, ERR_ARGS, "bad arguments");
-    op->acoef = new_mf(op->boxes, 1, 0, -1, 8);
-    mlmg_multifab_setval(op->acoef.get(), a);
+    MLMG_REQUIRE(op && op->is_abec && amrlev >= 0 && amrlev < op->nlev, ERR_ARGS, "bad arguments");
+    op->level_acoef(amrlev) = new_mf(op->level_boxes(amrlev), 1, 0, -1, 8);
+    mlmg_multifab_setval(op->level_acoef(amrlev).get(), a);
     ++op->coef_version;
     API_END
 }
@@ -945,12 +971,13 @@ int mlmg_abeclap_set_acoeffs_const (mlmg_linop op, int amrlev, double a)
 int mlmg_abeclap_set_bcoeffs (mlmg_linop op, int amrlev, const mlmg_multifab b[3])
 {
     API_BEGIN
-    MLMG_REQUIRE(op && op->is_abec && amrlev == 0 && b && b[0] && b[1] && b[2], ERR_ARGS, "bad arguments");
+    MLMG_REQUIRE(op && op->is_abec && amrlev >= 0 && amrlev < op->nlev && b && b[0] && b[1] && b[2], ERR_ARGS,
+                 "bad arguments");
     for (int d = 0; d < 3; ++d) {
-        MLMG_REQUIRE(b[d]->boxes == op->boxes && b[d]->nodal_dir == d && b[d]->ncomp == 1, ERR_ARGS,
-                     "b[d] must be a one-component face MultiFab (nodal in d) on the operator's BoxArray");
+        MLMG_REQUIRE(b[d]->boxes == op->level_boxes(amrlev) && b[d]->nodal_dir == d && b[d]->ncomp == 1, ERR_ARGS,
+                     "b[d] must be a one-component face MultiFab (nodal in d) on the level's BoxArray");
     }
-    for (int d = 0; d < 3; ++d) { op->bcoef[d] = clone_mf(*b[d]); }
+    for (int d = 0; d < 3; ++d) { op->level_bcoef(amrlev, d) = clone_mf(*b[d]); }
     ++op->coef_version;
     API_END
 }
@@ -958,10 +985,10 @@ int mlmg_abeclap_set_bcoeffs (mlmg_linop op, int amrlev, const mlmg_multifab b[3
 int mlmg_abeclap_set_bcoeffs_const (mlmg_linop op, int amrlev, double b)
 {
     API_BEGIN
-    MLMG_REQUIRE(op && op->is_abec && amrlev == 0, ERR_ARGS, "bad arguments");
+    MLMG_REQUIRE(op && op->is_abec && amrlev >= 0 && amrlev < op->nlev, ERR_ARGS, "bad arguments");
     for (int d = 0; d < 3; ++d) {
-        op->bcoef[d] = new_mf(op->boxes, 1, 0, d, 8);
-        mlmg_multifab_setval(op->bcoef[d].get(), b);
+        op->level_bcoef(amrlev, d) = new_mf(op->level_boxes(amrlev), 1, 0, d, 8);
+        mlmg_multifab_setval(op->level_bcoef(amrlev, d).get(), b);
     }
     ++op->coef_version;
     API_END

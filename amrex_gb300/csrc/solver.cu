@@ -996,6 +996,13 @@ void Engine::set_coefficients ()
             MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
         }
     }
+    restrict_coefficients();
+}
+
+void Engine::restrict_coefficients ()
+{
+    Impl& I = *m_impl;
+    LevelData& L0 = I.lev[0];
     // restrict a and b to every MG level (averageDownCoeffsSameAmrLevel)
     if (I.abec) {
         int a_zero = 1;

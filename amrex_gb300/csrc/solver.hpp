@@ -89,6 +89,11 @@ public:
     // (Re)load coefficients and BC values from the problems' FabSets and
     // restrict them to every MG level.
     void set_coefficients ();
+    // Restrict the level-0 a and b held on the device to every MG level and
+    // rebuild the stencil form (the second half of set_coefficients; a
+    // composite solve calls it after averaging finer AMR levels' coefficients
+    // into level 0's).
+    void restrict_coefficients ();
 
     // MLMGT::solve on every solve of the batch.  sol[s] (ngrow >= 0) holds the
     // initial guess and receives the solution; rhs[s] the right-hand side.

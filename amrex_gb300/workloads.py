@@ -7,10 +7,11 @@
 * ``batch_specs(nsolve, seed)``: the batch of independent solves of uneven
   sizes -- cube edges drawn uniformly from {32, 48, ..., 128}, solve i with
   RHS and b seeds ``seed + 1 + i``.
-* ``amr_problem(n, grids, rhs_seed)``: the composite MLPoisson over AMR
-  levels (base n^3 unit cube, refinement ratio 2, level l's boxes
-  ``grids[l]``), Gaussian-blob RHS sampled at each level's cell centres,
-  homogeneous Dirichlet, zero initial guess.
+* ``amr_problem(n, grids, rhs_seed)``: the composite MLPoisson (or, given
+  per-level coefficients, MLABecLaplacian) over AMR levels (base n^3 unit
+  cube, refinement ratio 2, level l's boxes ``grids[l]``), Gaussian-blob RHS
+  sampled at each level's cell centres, homogeneous Dirichlet and a zero
+  initial guess unless given.
 """
 from __future__ import annotations
 
@@ -69,13 +70,15 @@ def adjoint_objective(n, phi_scale, target_seed=3003):
 
 
 def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_grid_size=32, con_grid_size=32,
-                fused=False, solbc=None, max_fmg_iter=0):
+                fused=False, solbc=None, max_fmg_iter=0, abec=None):
     """Composite MLPoisson over len(grids) AMR levels: per-level geometry,
     BoxArray, DistributionMapping, solution (1 ghost, zero) and RHS
     MultiFabs, the operator and the MLMG solver.  ``grids[l]`` holds level l's
     boxes as (lo0, lo1, lo2, hi0, hi1, hi2); ``solbc[l]`` (optional) is a
     grown level-domain array with the initial guess in the valid cells and the
-    Dirichlet values in the ghosts."""
+    Dirichlet values in the ghosts.  With ``abec[l] = (alpha, beta, a, bx, by,
+    bz)`` (level-domain arrays, z-major) the operator is MLABecLaplacian with
+    those per-level coefficients."""
     geoms, bas, dms, sols, rhss = [], [], [], [], []
     for lev, g in enumerate(grids):
         m = n << lev
@@ -95,10 +98,26 @@ def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_
         sols.append(sol)
         rhss.append(rhs)
     info = ag.LPInfo().setAgglomerationGridSize(agg_grid_size).setConsolidationGridSize(con_grid_size)
-    op = ag.MLPoisson(geoms, bas, dms, info)
+    coefs = []
+    if abec is not None:
+        op = ag.MLABecLaplacian(geoms, bas, dms, info)
+        op.setScalars(abec[0][0], abec[0][1])
+    else:
+        op = ag.MLPoisson(geoms, bas, dms, info)
     op.setDomainBC((ag.LinOpBCType.Dirichlet,) * 3, (ag.LinOpBCType.Dirichlet,) * 3)
     for lev in range(len(grids)):
         op.setLevelBC(lev, sols[lev])
+        if abec is not None:
+            a = ag.MultiFab(bas[lev], dms[lev], 1, 0)
+            a.set_global(abec[lev][2])
+            op.setACoeffs(lev, a)
+            faces = []
+            for d in range(3):
+                f = ag.MultiFab(bas[lev], dms[lev], 1, 0, nodal_dir=d)
+                f.set_global(abec[lev][3 + d])
+                faces.append(f)
+            op.setBCoeffs(lev, faces)
+            coefs.append((a, faces))
     mlmg = ag.MLMG(op)
     mlmg.setMaxIter(max_iter)
     if max_fmg_iter:
@@ -106,4 +125,4 @@ def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_
     mlmg.setPrecision(precision)
     mlmg.setGraph(graph)
     mlmg.setFusedSmoother(fused)
-    return dict(geoms=geoms, bas=bas, dms=dms, sols=sols, rhss=rhss, op=op, mlmg=mlmg)
+    return dict(geoms=geoms, bas=bas, dms=dms, sols=sols, rhss=rhss, op=op, mlmg=mlmg, coefs=coefs)

@@ -123,10 +123,14 @@ int mlmg_multifab_norminf_noalloc(mlmg_multifab mf, double* out);
  * and amrex_fi_new_abeclaplacian (AMReX_abeclaplacian_fi.cpp:8-49).  geom, ba
  * and dm hold nlev entries, one per AMR level (MLPoissonT(Vector<Geometry>,
  * Vector<BoxArray>, ...), AMReX_MLPoisson.H:21-40).  nlev > 1 (a composite
- * solve, up to 8 levels) is implemented for MLPoisson with refinement ratio 2
- * on a non-periodic domain: level l's domain is level 0's refined by 2^l, its
- * boxes coarsen by 2 and nest properly in level l-1 (a box coarsened and
- * grown by one cell stays in level l-1 or outside the domain). */
+ * solve, up to 8 levels) is implemented for MLPoisson and MLABecLaplacian
+ * with refinement ratio 2 on a non-periodic domain: level l's domain is level
+ * 0's refined by 2^l, its boxes coarsen by 2 and nest properly in level l-1
+ * (a box coarsened and grown by one cell stays in level l-1 or outside the
+ * domain).  MLABecLaplacian takes a and b per AMR level (amrlev of the
+ * coefficient setters); the solve averages each finer level's a and b onto
+ * the next coarser level before restricting them to level 0's MG levels
+ * (MLABecLaplacianT::averageDownCoeffs, AMReX_MLABecLaplacian.H:610-712). */
 int mlmg_linop_new_poisson(int nlev, const mlmg_geometry* geom, const mlmg_boxarray* ba, const mlmg_distromap* dm,
                            const mlmg_lpinfo* info, mlmg_linop* out);
 int mlmg_linop_new_abeclap(int nlev, const mlmg_geometry* geom, const mlmg_boxarray* ba, const mlmg_distromap* dm,
@@ -138,7 +142,9 @@ int mlmg_linop_set_domain_bc(mlmg_linop op, const int lobc[3], const int hibc[3]
  * call); NULL: homogeneous */
 int mlmg_linop_set_level_bc(mlmg_linop op, int amrlev, mlmg_multifab levelbc);
 int mlmg_linop_set_maxorder(mlmg_linop op, int maxorder);
-/* amrex_fi_abeclap_set_scalars / _acoeffs / _bcoeffs (AMReX_abeclaplacian_fi.cpp:20-49) */
+/* amrex_fi_abeclap_set_scalars / _acoeffs / _bcoeffs (AMReX_abeclaplacian_fi.cpp:20-49);
+ * amrlev in 0..nlev-1, the MultiFabs on that level's BoxArray; a level whose
+ * a or b is never set takes 1 */
 int mlmg_abeclap_set_scalars(mlmg_linop op, double alpha, double beta);
 int mlmg_abeclap_set_acoeffs(mlmg_linop op, int amrlev, mlmg_multifab a);
 int mlmg_abeclap_set_acoeffs_const(mlmg_linop op, int amrlev, double a);

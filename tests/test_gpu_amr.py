@@ -1,7 +1,7 @@
-"""GPU composite (multi-AMR-level) MLPoisson solves through the C ABI against
-the reference's own composite solves on AmrMesh grids (tests/golden/
-amrsolve_*.npz) and, at the configuration size, against per-level
-statistics and sampled values of the reference solution."""
+"""GPU composite (multi-AMR-level) MLPoisson and MLABecLaplacian solves
+through the C ABI against the reference's own composite solves on AmrMesh
+grids (tests/golden/amrsolve_*.npz) and, at the configuration size, against
+per-level statistics and sampled values of the reference solution."""
 from __future__ import annotations
 
 import numpy as np
@@ -13,7 +13,8 @@ from tests.golden import amr_cases as ac
 
 pytestmark = pytest.mark.gpu
 
-SMALL = ["c2_n16_2lev", "c2_n32", "c2_n16_2lev_bc"]
+SMALL = ["c2_n16_2lev", "c2_n32", "c2_n16_2lev_bc", "c2_n16_2lev_abec"]
+SUMMARY = ["c2_n32_fmg", "c2_n32_abec"]
 
 
 def _phi_error(g, lev, got):
@@ -30,9 +31,10 @@ def _solve(name, precision=0, graph=False, tol_rel=None, fused=False):
     g = ac.load("amrsolve", name)
     case, grids = g["case"], g["grids"]
     solbc = [ac.level_solbc(case, lev) for lev in range(len(grids))]
+    abec = [ac.level_abec(case, lev) for lev in range(len(grids))] if case.get("abec") else None
     P = workloads.amr_problem(case["n"], grids, case["rhs_seed"], precision=precision, graph=graph,
                               agg_grid_size=case.get("agg_grid_size", 32), con_grid_size=case.get("con_grid_size", 32),
-                              fused=fused, solbc=solbc, max_fmg_iter=case.get("max_fmg_iter", 0))
+                              fused=fused, solbc=solbc, max_fmg_iter=case.get("max_fmg_iter", 0), abec=abec)
     resid = P["mlmg"].solve(P["sols"], P["rhss"], tol_rel or case.get("tol_rel", 1e-10), 0.0)
     phis = []
     for lev, boxes in enumerate(grids):
@@ -41,7 +43,7 @@ def _solve(name, precision=0, graph=False, tol_rel=None, fused=False):
     return g, P, resid, phis
 
 
-@pytest.mark.parametrize("name", SMALL + ["c2_n32_fmg"])
+@pytest.mark.parametrize("name", SMALL + SUMMARY)
 def test_amr_fp64_matches_reference(name):
     g, P, resid, phis = _solve(name, precision=0)
     ref = g["result"]
@@ -58,7 +60,7 @@ def test_amr_fp64_matches_reference(name):
         assert err < 1e-10, (lev, err)
 
 
-@pytest.mark.parametrize("name", SMALL + ["c2_n32_fmg"])
+@pytest.mark.parametrize("name", SMALL + SUMMARY)
 @pytest.mark.parametrize("graph,fused", [(False, False), (True, False), (True, True)])
 def test_amr_mixed_reaches_target(name, graph, fused):
     """FP32 corrections inside the FP64 composite residual reach the same
