@@ -51,8 +51,10 @@ def test_oracle_amr_matches_reference(name):
     assert info["cg_iters"] == ref["cg_iters"]
     assert info["init_resid"] == pytest.approx(ref["init_resid"], rel=1e-13)
     assert info["rhs_norm"] == pytest.approx(ref["rhs_norm"], rel=1e-13)
-    # residuals near 1e-10 carry roundoff from the order of the flux-register sums
-    np.testing.assert_allclose(info["history"], ref["history"], rtol=1e-4, atol=1e-14 * ref["rhs_norm"])
+    # the convergence path to 1e-6 (it pins the coefficient average-down of the
+    # MLABecLaplacian cases); residuals near 1e-10 carry roundoff from the
+    # order of the flux-register sums
+    ac.check_history(info["history"], ref)
     for lev in range(len(grids)):
         got = ac.pack_boxes(phis[lev], grids[lev])
         if f"phi_l{lev}" in g:
