@@ -1050,6 +1050,8 @@ int mlmg_set_option (mlmg_solver s, const char* name, double value)
     else if (n == "fused_v2") { s->opt.fused_v2 = value != 0.0; }
     else if (n == "fused_tma") { s->opt.fused_tma = value != 0.0; }
     else if (n == "fused_v3") { s->opt.fused_v3 = value != 0.0; }
+    else if (n == "fused_prefetch") { s->opt.fused_prefetch = value != 0.0; }
+    else if (n == "march_tma") { s->opt.march_tma = value != 0.0; }
     else if (n == "march_tz") {
         MLMG_REQUIRE(value >= 1 && value <= 4096, ERR_ARGS, "march_tz must be in 1..4096");
         s->opt.march_tz = (int)value;

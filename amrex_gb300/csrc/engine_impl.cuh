@@ -87,6 +87,8 @@ struct LevelData {
     SubsetData fz;
     DevBuf<CUtensorMap> tm_a, tm_b;   // per patch: tensor maps of the 40x12x12 staging box over cor32 / cor32b
     DevBuf<CUtensorMap> tm3;          // per patch: the third form's F3_NMAP maps (phi a/b, rhs, stencil)
+    DevBuf<CUtensorMap> tm_pf;        // per patch: FS_PF_NMAP L2-prefetch maps (rhs, D, sX, sY, sZ)
+    DevBuf<CUtensorMap> tm_m;         // per patch: MT_NMAP plane maps of the TMA z-march
     bool march = false;           // fused sweeps by the z-marching kernel
     SubsetData mz;
     DevBuf<float> cor32b;

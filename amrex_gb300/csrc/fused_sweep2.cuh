@@ -39,10 +39,19 @@ namespace mlmg {
 // through the ghost layers it rewrites.  The wait is bounded; on expiry the
 // block reports ERR_TMA_TIMEOUT, waits once more (bounded) for its copy and
 // leaves.
+//
+// With `pf` (FS_PF_NMAP maps per patch over rhs, D, sX, sY, sZ), the block
+// also asks the TMA unit to prefetch into L2 the boxes of those arrays that
+// its colour passes read (the tile grown by one, x widened to the 16-byte
+// aligned 40 columns of the phi box), so that their per-thread loads, issued
+// once phi has arrived, find the lines in L2 rather than in DRAM.
+enum : int { FS_PF_RHS = 0, FS_PF_D = 1, FS_PF_SX = 2, FS_PF_SY = 3, FS_PF_SZ = 4, FS_PF_NMAP = 5 };
+
 template <bool VARC, bool TMA = false>
 __global__ void __launch_bounds__(FS_THREADS, 5)
 k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
-                const float* __restrict__ rhs, StencilPtrs Sc, const CUtensorMap* __restrict__ maps, int* err)
+                const float* __restrict__ rhs, StencilPtrs Sc, const CUtensorMap* __restrict__ maps, int* err,
+                const CUtensorMap* __restrict__ pf = nullptr)
 {
     __shared__ __align__(128) float A[FS_AZ][FS_AY][FS_AX];   // phi_in, local (x-4..x+35, y-2..y+9, z-2..z+9)
     __shared__ float N[FS_NZ][FS_NY][FS_NX];                  // first colour, local (x-1..x+32, y-1..y+8, z-1..z+8)
@@ -90,6 +99,10 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
         if (tid == 0) {
             tma::mbar_expect_tx(&bar, (unsigned)sizeof(A));
             tma::load_3d(&A[0][0][0], maps + pid, &bar, cx, cy, cz);
+        }
+        if (pf != nullptr && tid >= 32 && tid < 32 + (VARC ? FS_PF_NMAP : 1)) {
+            // coordinates of the tile grown by one: never negative
+            tma::prefetch_3d(pf + (size_t)pid * FS_PF_NMAP + (tid - 32), cx, cy + 1, cz + 1);
         }
         const bool late = !tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
         if (__syncthreads_or(late)) {

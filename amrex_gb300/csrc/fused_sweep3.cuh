@@ -51,80 +51,26 @@ struct Fs3Plan {
 // tensor maps of one patch for the third form, in this order
 enum : int { F3_PHI_A = 0, F3_PHI_B, F3_RHS, F3_D, F3_SX, F3_SY, F3_SZ, F3_NMAP };
 
-template <bool VARC>
-__global__ void __launch_bounds__(FS_THREADS, 2)
-k_sweep_fused3 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
-                StencilPtrs Sc, const CUtensorMap* __restrict__ maps, int phi_map, int* err)
+// Both colours and the write of one tile whose inputs sit in shared memory
+// at `sm` (Fs3Plan layout), by NT threads that all call it (block barriers
+// inside).
+template <bool VARC, int NT>
+__device__ __forceinline__ void fs3_tile (const PatchLite& P, int x0, int y0, int z0, float* __restrict__ sm,
+                                          float* __restrict__ phi_out, int tid)
 {
-    extern __shared__ unsigned char fs3_raw[];
-    __shared__ PatchLite SP;
-    __shared__ unsigned long long bar;
+    static_assert(NT % ((FS_TX / 2) * FS_TY) == 0 && NT >= FS_RED_ROW, "thread count");
     using PL = Fs3Plan;
-    float* const sm = reinterpret_cast<float*>((reinterpret_cast<size_t>(fs3_raw) + 127) & ~size_t(127));
     float* const As = sm + PL::oA;
     float* const Ds = sm + PL::oD;
     float* const Rs = sm + PL::oR;
     float* const SXs = sm + PL::oSX;
     float* const SYs = sm + PL::oSY;
     float* const SZs = sm + PL::oSZ;
-
-    const int tid = threadIdx.y * FS_TX + threadIdx.x;
-    int x0, y0, z0, pid;
-    {
-        const TileCoord c = decode_fused_tile(L, S, blockIdx.x);
-        x0 = c.x0; y0 = c.y0; z0 = c.z0; pid = c.p;
-        if (tid == 0) {
-            const PatchDesc& P = L.P[c.p];
-            for (int d = 0; d < 3; ++d) { SP.lo[d] = P.lo[d]; SP.hi[d] = P.hi[d]; }
-            SP.sx = P.sx; SP.sxy = P.sxy; SP.base = P.base;
-            SP.dhx = float(P.dha[0]); SP.dhy = float(P.dha[1]); SP.dhz = float(P.dha[2]);
-            for (int f = 0; f < 6; ++f) {
-                SP.f[f].type = P.face[f].type;
-                SP.f[f].nx = P.face[f].nx;
-                SP.f[f].c1 = float(P.face[f].coef[1]);
-                SP.f[f].c2 = float(P.face[f].coef[2]);
-                SP.f[f].fco = float(P.face[f].fco);
-            }
-            tma::mbar_init(&bar, 1);
-        }
-    }
-    __syncthreads();
-    const PatchLite& P = SP;
     const int pxl = P.lo[0] - x0, pxh = P.hi[0] - x0;
     const int pyl = P.lo[1] - y0, pyh = P.hi[1] - y0;
     const int pzl = P.lo[2] - z0, pzh = P.hi[2] - z0;
     const bool touches = (pxl >= -1) || (pxh <= FS_TX) || (pyl >= -1) || (pyh <= FS_TY) || (pzl >= -1) ||
                          (pzh <= FS_TZ);
-
-    // ---- stage every input with TMA
-    {
-        const int cx = x0 - P.lo[0] + XOFF - 4;                 // tensor x of local x = -4
-        const int cy1 = y0 - P.lo[1], cz1 = z0 - P.lo[2];       // tensor y, z of local -1
-        if ((cx & 3) != 0) {
-            if (tid == 0) { atomicExch(err, tma::ERR_TMA_ALIGN); }
-            return;
-        }
-        if (tid == 0) {
-            const CUtensorMap* M = maps + (size_t)pid * F3_NMAP;
-            unsigned bytes = (unsigned)(PL::A_N + PL::C_N) * 4u;
-            if constexpr (VARC) { bytes += (unsigned)(2 * PL::C_N + PL::SY_N + PL::SZ_N) * 4u; }
-            tma::mbar_expect_tx(&bar, bytes);
-            tma::load_3d(As, M + phi_map, &bar, cx, cy1 - 1, cz1 - 1);
-            tma::load_3d(Rs, M + F3_RHS, &bar, cx, cy1, cz1);
-            if constexpr (VARC) {
-                tma::load_3d(Ds, M + F3_D, &bar, cx, cy1, cz1);
-                tma::load_3d(SXs, M + F3_SX, &bar, cx, cy1, cz1);
-                tma::load_3d(SYs, M + F3_SY, &bar, cx, cy1, cz1);
-                tma::load_3d(SZs, M + F3_SZ, &bar, cx, cy1, cz1);
-            }
-        }
-        const bool late = !tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
-        if (__syncthreads_or(late)) {
-            if (tid == 0) { atomicExch(err, tma::ERR_TMA_TIMEOUT); }
-            tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
-            return;
-        }
-    }
 
     // local (lx, ly, lz) -> shared element
     auto a_at = [&] (int lx, int ly, int lz) -> float& { return As[((lz + 2) * 12 + (ly + 2)) * PL::AX + lx + 4]; };
@@ -145,7 +91,7 @@ k_sweep_fused3 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
             const int a2 = max(-1, plo[t2]), b2 = min(lim[t2], phi[t2]);
             const int n1 = b1 - a1 + 1, n2 = b2 - a2 + 1;
             if (n1 <= 0 || n2 <= 0) { continue; }
-            for (int u = tid; u < n1 * n2; u += FS_THREADS) {
+            for (int u = tid; u < n1 * n2; u += NT) {
                 int c[3];
                 c[d] = g; c[t1] = a1 + u % n1; c[t2] = a2 + u / n1;
                 int cf[3] = {c[0], c[1], c[2]}, ci[3] = {c[0], c[1], c[2]};
@@ -199,7 +145,7 @@ k_sweep_fused3 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
 
     // ---- first colour ((i+j+k) even) on the tile + 1, in place
     {
-        constexpr int RS = FS_THREADS / FS_RED_ROW;      // 15 row streams x 17 columns
+        constexpr int RS = NT / FS_RED_ROW;              // row streams x 17 columns
         const int par0 = (x0 - 1 + y0 - 1 + z0 - 1) & 1;
         if (tid < RS * FS_RED_ROW) {
             const int r = tid % FS_RED_ROW;
@@ -221,12 +167,13 @@ k_sweep_fused3 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
 
     // ---- second colour on the tile, in place: 16 cells per row, 8 x 8 rows
     {
+        constexpr int ZST = NT / ((FS_TX / 2) * FS_TY);   // z streams
         const int r = tid % (FS_TX / 2);
         const int ly = (tid / (FS_TX / 2)) % FS_TY;
         const int lzs = (tid / (FS_TX / 2)) / FS_TY;
         const int par0 = (x0 + y0 + z0) & 1;
 #pragma unroll
-        for (int lz = lzs; lz < FS_TZ; lz += 2) {
+        for (int lz = lzs; lz < FS_TZ; lz += ZST) {
             const int lx = 2 * r + (((par0 + ly + lz) & 1) ^ 1);   // (x+y+z) odd
             const bool in = !touches || (lx <= pxh && ly <= pyh && lz <= pzh);
             if (in) { update(lx, ly, lz); }
@@ -239,7 +186,7 @@ k_sweep_fused3 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
         const long long q0 = P.idx(x0, y0, z0);
         const int sx = P.sx, sxy = (int)P.sxy;
         const bool full = !touches || (pxh >= FS_TX - 1 && pyh >= FS_TY - 1 && pzh >= FS_TZ - 1);
-        for (int u = tid; u < FS_TZ * FS_TY * (FS_TX / 4); u += FS_THREADS) {
+        for (int u = tid; u < FS_TZ * FS_TY * (FS_TX / 4); u += NT) {
             const int c4 = u % (FS_TX / 4), row = u / (FS_TX / 4);
             const int ly = row % FS_TY, lz = row / FS_TY;
             const float* src = &a_at(4 * c4, ly, lz);
@@ -251,6 +198,79 @@ k_sweep_fused3 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
             }
         }
     }
+}
+
+template <bool VARC>
+__global__ void __launch_bounds__(FS_THREADS, 2)
+k_sweep_fused3 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
+                StencilPtrs Sc, const CUtensorMap* __restrict__ maps, int phi_map, int* err)
+{
+    extern __shared__ unsigned char fs3_raw[];
+    __shared__ PatchLite SP;
+    __shared__ unsigned long long bar;
+    using PL = Fs3Plan;
+    float* const sm = reinterpret_cast<float*>((reinterpret_cast<size_t>(fs3_raw) + 127) & ~size_t(127));
+    float* const As = sm + PL::oA;
+    float* const Ds = sm + PL::oD;
+    float* const Rs = sm + PL::oR;
+    float* const SXs = sm + PL::oSX;
+    float* const SYs = sm + PL::oSY;
+    float* const SZs = sm + PL::oSZ;
+
+    const int tid = threadIdx.y * FS_TX + threadIdx.x;
+    int x0, y0, z0, pid;
+    {
+        const TileCoord c = decode_fused_tile(L, S, blockIdx.x);
+        x0 = c.x0; y0 = c.y0; z0 = c.z0; pid = c.p;
+        if (tid == 0) {
+            const PatchDesc& P = L.P[c.p];
+            for (int d = 0; d < 3; ++d) { SP.lo[d] = P.lo[d]; SP.hi[d] = P.hi[d]; }
+            SP.sx = P.sx; SP.sxy = P.sxy; SP.base = P.base;
+            SP.dhx = float(P.dha[0]); SP.dhy = float(P.dha[1]); SP.dhz = float(P.dha[2]);
+            for (int f = 0; f < 6; ++f) {
+                SP.f[f].type = P.face[f].type;
+                SP.f[f].nx = P.face[f].nx;
+                SP.f[f].c1 = float(P.face[f].coef[1]);
+                SP.f[f].c2 = float(P.face[f].coef[2]);
+                SP.f[f].fco = float(P.face[f].fco);
+            }
+            tma::mbar_init(&bar, 1);
+        }
+    }
+    __syncthreads();
+    const PatchLite& P = SP;
+
+    // ---- stage every input with TMA
+    {
+        const int cx = x0 - P.lo[0] + XOFF - 4;                 // tensor x of local x = -4
+        const int cy1 = y0 - P.lo[1], cz1 = z0 - P.lo[2];       // tensor y, z of local -1
+        if ((cx & 3) != 0) {
+            if (tid == 0) { atomicExch(err, tma::ERR_TMA_ALIGN); }
+            return;
+        }
+        if (tid == 0) {
+            const CUtensorMap* M = maps + (size_t)pid * F3_NMAP;
+            unsigned bytes = (unsigned)(PL::A_N + PL::C_N) * 4u;
+            if constexpr (VARC) { bytes += (unsigned)(2 * PL::C_N + PL::SY_N + PL::SZ_N) * 4u; }
+            tma::mbar_expect_tx(&bar, bytes);
+            tma::load_3d(As, M + phi_map, &bar, cx, cy1 - 1, cz1 - 1);
+            tma::load_3d(Rs, M + F3_RHS, &bar, cx, cy1, cz1);
+            if constexpr (VARC) {
+                tma::load_3d(Ds, M + F3_D, &bar, cx, cy1, cz1);
+                tma::load_3d(SXs, M + F3_SX, &bar, cx, cy1, cz1);
+                tma::load_3d(SYs, M + F3_SY, &bar, cx, cy1, cz1);
+                tma::load_3d(SZs, M + F3_SZ, &bar, cx, cy1, cz1);
+            }
+        }
+        const bool late = !tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
+        if (__syncthreads_or(late)) {
+            if (tid == 0) { atomicExch(err, tma::ERR_TMA_TIMEOUT); }
+            tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
+            return;
+        }
+    }
+
+    fs3_tile<VARC, FS_THREADS>(P, x0, y0, z0, sm, phi_out, tid);
 }
 
 } // namespace mlmg

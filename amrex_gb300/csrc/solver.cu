@@ -27,15 +27,16 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder ()
 
 // 3-D tiled tensor map over the allocation of patch P inside an FP32 level
 // field: x over the whole padded row (sx), y and z over the rows and planes
-// with their ghost layers; box 40 x by x bz floats (a fused sweep's staging box)
-CUtensorMap patch_tensor_map (const float* field, const PatchDesc& P, int by = FS_AY, int bz = FS_AZ)
+// with their ghost layers; box bx x by x bz floats (default: a fused sweep's
+// 40 x 12 x 12 staging box)
+CUtensorMap patch_tensor_map (const float* field, const PatchDesc& P, int by = FS_AY, int bz = FS_AZ, int bx = FS_AX)
 {
     const long long start = P.base - P.sxy - P.sx - XOFF;      // first element of the patch's allocation
     const int ny = P.hi[1] - P.lo[1] + 1, nz = P.hi[2] - P.lo[2] + 1;
     MLMG_REQUIRE(start % 4 == 0 && P.sx % 4 == 0 && P.sxy % 4 == 0, ERR_INTERNAL, "patch layout not 16-byte aligned");
     cuuint64_t dims[3] = {(cuuint64_t)P.sx, (cuuint64_t)(ny + 2), (cuuint64_t)(nz + 2)};
     cuuint64_t strides[2] = {(cuuint64_t)P.sx * sizeof(float), (cuuint64_t)P.sxy * sizeof(float)};
-    cuuint32_t box[3] = {(cuuint32_t)FS_AX, (cuuint32_t)by, (cuuint32_t)bz};
+    cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
     cuuint32_t estride[3] = {1, 1, 1};
     CUtensorMap m;
     const CUresult r = tensor_map_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
@@ -173,6 +174,10 @@ void Engine::Impl::build ()
                                                          march_smem_floats(true) * (int)sizeof(float)));
                     MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_march<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                          march_smem_floats(false) * (int)sizeof(float)));
+                    MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_march_tma<true>,
+                        cudaFuncAttributeMaxDynamicSharedMemorySize, march_tma_smem_floats(true) * (int)sizeof(float)));
+                    MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_march_tma<false>,
+                        cudaFuncAttributeMaxDynamicSharedMemorySize, march_tma_smem_floats(false) * (int)sizeof(float)));
                     attr_set = true;
                 }
             }
@@ -203,6 +208,42 @@ void Engine::Impl::build ()
             }
             L.tm_a.upload(ta, st());
             L.tm_b.upload(tb, st());
+            // L2-prefetch maps: the tile grown by one (40 x 10 x 10; the y / z
+            // face arrays one row / plane more)
+            std::vector<CUtensorMap> tp((size_t)FS_PF_NMAP * M.patches.size());
+            std::memset(tp.data(), 0, tp.size() * sizeof(CUtensorMap));
+            for (size_t p = 0; p < M.patches.size(); ++p) {
+                CUtensorMap* m = &tp[p * FS_PF_NMAP];
+                const PatchDesc& P = M.patches[p];
+                m[FS_PF_RHS] = patch_tensor_map(L.res32.p, P, 10, 10);
+                if (abec) {
+                    m[FS_PF_D] = patch_tensor_map(L.D32.p, P, 10, 10);
+                    m[FS_PF_SX] = patch_tensor_map(L.sx32.p, P, 10, 10);
+                    m[FS_PF_SY] = patch_tensor_map(L.sy32.p, P, 11, 10);
+                    m[FS_PF_SZ] = patch_tensor_map(L.sz32.p, P, 10, 11);
+                }
+            }
+            L.tm_pf.upload(tp, st());
+        }
+        // the TMA z-march's maps: one plane (72 x 20 of phi, 72 x 19 of rhs and
+        // the stencil arrays) per load, per patch
+        if (L.march && E.m_opt.march_tma) {
+            std::vector<CUtensorMap> tm((size_t)MT_NMAP * M.patches.size());
+            std::memset(tm.data(), 0, tm.size() * sizeof(CUtensorMap));
+            for (size_t p = 0; p < M.patches.size(); ++p) {
+                CUtensorMap* m = &tm[p * MT_NMAP];
+                const PatchDesc& P = M.patches[p];
+                m[MT_PHI_A] = patch_tensor_map(L.cor32.p, P, MS_XR, 1, MS_RP);
+                m[MT_PHI_B] = patch_tensor_map(L.cor32b.p, P, MS_XR, 1, MS_RP);
+                m[MT_RHS] = patch_tensor_map(L.res32.p, P, MS_CR, 1, MS_RP);
+                if (abec) {
+                    m[MT_D] = patch_tensor_map(L.D32.p, P, MS_CR, 1, MS_RP);
+                    m[MT_SX] = patch_tensor_map(L.sx32.p, P, MS_CR, 1, MS_RP);
+                    m[MT_SY] = patch_tensor_map(L.sy32.p, P, MS_CR, 1, MS_RP);
+                    m[MT_SZ] = patch_tensor_map(L.sz32.p, P, MS_CR, 1, MS_RP);
+                }
+            }
+            L.tm_m.upload(tm, st());
         }
         // the third form's maps: phi (both buffers), rhs and the stencil arrays, per patch
         if (L.fused && !L.march && E.m_opt.fused_v3) {
@@ -553,7 +594,17 @@ void Engine::Impl::smooth_fused (int l, int n)
     const StencilPtrs S = stencil32(l);
     for (int i = 0; i < n; ++i) {
         if (timed) { kev_record(); }
-        if (L.march) {
+        if (L.march && L.tm_m.p != nullptr) {
+            const dim3 blk(MS_TX / 2, MS_TY);
+            const int pm = (a == L.cor32.p) ? MT_PHI_A : MT_PHI_B;
+            if (abec) {
+                k_sweep_march_tma<true><<<L.mz.ntiles, blk, march_tma_smem_floats(true) * sizeof(float), st()>>>(
+                    L.dl, L.mz.dev(), b, L.tm_m.p, pm, E.m_opt.march_tz, err_d.p);
+            } else {
+                k_sweep_march_tma<false><<<L.mz.ntiles, blk, march_tma_smem_floats(false) * sizeof(float), st()>>>(
+                    L.dl, L.mz.dev(), b, L.tm_m.p, pm, E.m_opt.march_tz, err_d.p);
+            }
+        } else if (L.march) {
             const dim3 blk(MS_TX / 2, MS_TY);
             if (abec) {
                 k_sweep_march<true><<<L.mz.ntiles, blk, march_smem_floats(true) * sizeof(float), st()>>>(
@@ -574,8 +625,13 @@ void Engine::Impl::smooth_fused (int l, int n)
         } else if (E.m_opt.fused_v2) {
             const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
             if (use_tma) {
-                if (abec) { k_sweep_fused2<true, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p); }
-                else { k_sweep_fused2<false, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p); }
+                const CUtensorMap* pf = E.m_opt.fused_prefetch ? L.tm_pf.p : nullptr;
+                if (abec) {
+                    k_sweep_fused2<true, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p, pf);
+                } else {
+                    k_sweep_fused2<false, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
+                                                                     pf);
+                }
             } else if (abec) {
                 k_sweep_fused2<true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p);
             } else {

@@ -46,10 +46,12 @@ struct EngineOptions {
                                 // (measured slower than the tiled fused sweep: 0.27 vs 0.18 ms at 256^3)
     int march_min_tiles = 304;  // ... at least this many (column, z-chunk) tiles
     int march_tz = 16;          // planes per z-slab of the marching sweep
+    int march_tma = 1;          // ... staging its planes by TMA tensor loads (else 16-byte cp.async)
     int fused_v2 = 1;           // fused sweeps by k_sweep_fused2 (face ghosts rewritten in shared memory,
                                 // one path for every tile) instead of k_sweep_fused
     int fused_tma = 1;          // ... staging each tile by one TMA tensor load
     int fused_v3 = 0;           // fused sweeps by k_sweep_fused3 (every input of a tile staged by TMA)
+    int fused_prefetch = 1;     // TMA sweeps also prefetch each tile's rhs and stencil boxes into L2
     int max_fmg_iter = 0;       // F-cycles (MLMGT::mgFcycle) for the first max_fmg_iter iterations
     int transpose = 0;          // solve A^T x = rhs (homogeneous BCs): the outer residual uses A^T,
                                 // the V-cycle of A is the correction operator (adjoint solves)

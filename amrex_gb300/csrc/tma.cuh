@@ -29,6 +29,14 @@ __device__ __forceinline__ void load_3d (void* dst, const void* map, unsigned lo
                  :: "r"(smem_addr(dst)), "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar)) : "memory");
 }
 
+// prefetch a tensor-map box into L2 (no shared memory, no barrier); parts of
+// the box outside the tensor are not fetched
+__device__ __forceinline__ void prefetch_3d (const void* map, int c0, int c1, int c2)
+{
+    asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];\n"
+                 :: "l"(map), "r"(c0), "r"(c1), "r"(c2) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait (unsigned long long* bar, unsigned parity)
 {
     unsigned ok;

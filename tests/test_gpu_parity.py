@@ -81,7 +81,8 @@ MIXED_CASES = ["solve_poisson_32", "solve_abec_32", "solve_abec_48", "solve_abec
 
 @pytest.mark.parametrize("name", MIXED_CASES)
 @pytest.mark.parametrize("graph,fused,coarse,march", [(False, False, 1, 0), (True, False, 1, 0), (True, True, 1, 0),
-                                                      (False, False, 0, 0), (True, True, 0, 0), (True, True, 0, 1)])
+                                                      (False, False, 0, 0), (True, True, 0, 0), (True, True, 0, 1),
+                                                      (True, True, 0, 2)])
 def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
     """FP32 V-cycles inside FP64 refinement reach the same 1e-10 relative
     residual (the residual is evaluated in FP64); phi agrees with the
@@ -91,7 +92,8 @@ def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
     c = g["case"]
     opts = {"coarse_block": coarse}
     if march:
-        opts["march_min_tiles"] = 0          # the z-marching sweep on every fused level
+        # the z-marching sweep on every fused level: TMA staging (1) or cp.async (2)
+        opts.update(march_sweep=1, march_min_tiles=0, march_tma=int(march == 1))
     prob = helpers.make_problem(c, cases.inputs(c), precision="mixed", graph=graph, fused=fused, options=opts)
     resid = prob["mlmg"].solve(prob["sol"], prob["rhs"], c["tol_rel"], c["tol_abs"])
     r = g["result"]
@@ -107,16 +109,19 @@ def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
 
 @pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_mixed_bc", "solve_abec_48",
                                   "solve_poisson_periodic_x", "solve_abec_mo4"])
-@pytest.mark.parametrize("variant", ["tiled", "tiled_v1", "tiled_v3", "march"])
+@pytest.mark.parametrize("variant", ["tiled", "tiled_noprefetch", "tiled_v1", "tiled_v3", "march", "march_cpasync"])
 def test_fused_sweep_matches_colour_passes(name, variant):
     """The fused two-colour sweep (tiled with face ghosts rewritten in shared
-    memory, the earlier tiled form, the tiled form with every input staged by
-    TMA, or marching along z) performs the same arithmetic as two colour
-    passes with ghost refreshes in between."""
+    memory, with or without L2 prefetch of its coefficient boxes; the earlier
+    tiled form; the tiled form with every input staged by TMA; or marching
+    along z with its planes staged by TMA or by cp.async) performs the same
+    arithmetic as two colour passes with ghost refreshes in between."""
     c = load.load(name)["case"]
     inp = cases.inputs(c)
-    opts = {"march_sweep": int(variant == "march"), "march_min_tiles": 0,
-            "fused_v2": int(variant in ("tiled", "tiled_v3")), "fused_v3": int(variant == "tiled_v3")}
+    march = variant.startswith("march")
+    opts = {"march_sweep": int(march), "march_min_tiles": 0, "march_tma": int(variant == "march"),
+            "fused_v2": int(variant in ("tiled", "tiled_noprefetch", "tiled_v3")),
+            "fused_v3": int(variant == "tiled_v3"), "fused_prefetch": int(variant != "tiled_noprefetch")}
     p1 = helpers.make_problem(c, inp, precision="mixed", fused=False)
     p2 = helpers.make_problem(c, inp, precision="mixed", fused=True, options=opts)
     p1["mlmg"].solve(p1["sol"], p1["rhs"], 1e-10, 0)
