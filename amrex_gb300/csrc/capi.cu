@@ -231,10 +231,27 @@ std::vector<FabTag> fill_boundary_tags (const mlmg_multifab_s& mf, const GeomC& 
     return tags;
 }
 
+// grow-only device scratch of the whole-array transfers: fab_global holds
+// g_xfer_mutex until its stream has drained, so one set of buffers serves
+// every call (never freed: they live as long as the process)
+std::mutex g_xfer_mutex;
+
+template <typename T>
+T* scratch (int slot, size_t count)
+{
+    static DevBuf<unsigned char>* bufs[3] = {new DevBuf<unsigned char>(), new DevBuf<unsigned char>(),
+                                             new DevBuf<unsigned char>()};
+    DevBuf<unsigned char>& b = *bufs[slot];
+    const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    if (b.n < bytes) { b.alloc(bytes); }
+    return reinterpret_cast<T*>(b.p);
+}
+
 template <typename T>
 void fab_global (mlmg_multifab_s& mf, void* host, const int glo[3], const int gn[3], int dir)
 {
     cudaStream_t st = lib_stream();
+    std::lock_guard<std::mutex> lk(g_xfer_mutex);
     const Box3 gbox{{glo[0], glo[1], glo[2]}, {glo[0] + gn[0] - 1, glo[1] + gn[1] - 1, glo[2] + gn[2] - 1}};
     std::vector<Box3> regions;
     std::vector<long long> start{0};
@@ -252,21 +269,22 @@ void fab_global (mlmg_multifab_s& mf, void* host, const int glo[3], const int gn
         start.push_back(start.back() + (r.ok() ? r.npts() : 0));
     }
     const long long ng = (long long)gn[0] * gn[1] * gn[2];
-    DevBuf<T> stage(ng);
-    DevBuf<Box3> dr; DevBuf<long long> ds;
-    dr.upload(regions, st);
-    ds.upload(start, st);
+    T* const stage = scratch<T>(0, (size_t)ng);
+    Box3* const dr = scratch<Box3>(1, regions.size());
+    long long* const ds = scratch<long long>(2, start.size());
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(dr, regions.data(), regions.size() * sizeof(Box3), cudaMemcpyHostToDevice, st));
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(ds, start.data(), start.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
     // the host array enters the stage for an upload, and for a download that
     // leaves cells of the array uncovered (those keep the host's values)
     if (dir == 0 || start.back() < ng) {
-        MLMG_CUDA_CHECK(cudaMemcpyAsync(stage.p, host, ng * sizeof(T), cudaMemcpyHostToDevice, st));
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(stage, host, ng * sizeof(T), cudaMemcpyHostToDevice, st));
     }
     if (start.back() > 0) {
-        k_fab_global<T><<<grid_for(start.back(), 256), 256, 0, st>>>(mf.dinfo.p, dr.p, ds.p, (int)regions.size(),
-            start.back(), (T*)mf.data.p, stage.p, glo[0], glo[1], glo[2], gn[0], gn[1], dir);
+        k_fab_global<T><<<grid_for(start.back(), 256), 256, 0, st>>>(mf.dinfo.p, dr, ds, (int)regions.size(),
+            start.back(), (T*)mf.data.p, stage, glo[0], glo[1], glo[2], gn[0], gn[1], dir);
         g_launches++;
     }
-    if (dir == 1) { MLMG_CUDA_CHECK(cudaMemcpyAsync(host, stage.p, ng * sizeof(T), cudaMemcpyDeviceToHost, st)); }
+    if (dir == 1) { MLMG_CUDA_CHECK(cudaMemcpyAsync(host, stage, ng * sizeof(T), cudaMemcpyDeviceToHost, st)); }
     MLMG_CUDA_CHECK(cudaGetLastError());
     MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
 }
