@@ -201,7 +201,6 @@ void Engine::Impl::build ()
         if (L.has_bottom) { for (auto& b : L.bw) { alloc0(b); } }
         // tensor maps of the fused sweep's TMA staging, one per patch of the level
         if (L.fused && !L.march && E.m_opt.fused_v2 && E.m_opt.fused_tma) {
-
             std::vector<CUtensorMap> ta(M.patches.size()), tb(M.patches.size());
             for (size_t p = 0; p < M.patches.size(); ++p) {
                 ta[p] = patch_tensor_map(L.cor32.p, M.patches[p]);
