@@ -186,8 +186,12 @@ int mlmg_set_fused_smoother(mlmg_solver s, int on);      /* fused two-colour Gau
  * sweeps by the z-marching kernel), "march_min_tiles" (levels with fewer
  * marching tiles use the tiled fused sweep), "fused_v2" (0/1: the tiled fused
  * sweep with face ghosts rewritten in shared memory, default 1), "fused_tma"
- * (0/1: that sweep stages each tile by one TMA tensor load, default 1); -4
- * for an unknown name */
+ * (0/1: that sweep stages each tile by one TMA tensor load, default 1),
+ * "fused_prefetch" (0/1: ... and prefetches the tile's rhs and stencil boxes
+ * into L2, default 1), "fused_v3" (0/1: every input of a tile staged by TMA),
+ * "march_tz" (planes per z-slab of the marching sweep), "march_tma" (0/1: the
+ * marching sweep stages its planes by TMA tensor loads, default 1); -4 for an
+ * unknown name */
 int mlmg_set_option(mlmg_solver s, const char* name, double value);
 /* time every finest-level smoother launch with CUDA events on the library
  * stream (graph replays included); the stats accumulate until reset */
