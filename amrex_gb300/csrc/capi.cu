@@ -146,6 +146,17 @@ struct mlmg_multifab_s {
     long long total = 0;
     DevBuf<char> data;
     DevBuf<FabInfo> dinfo;
+    // FillBoundary copy tags on the device for the domain / periodicity they
+    // were last built for (the boxes of a MultiFab never change)
+    struct FbCache {
+        bool valid = false;
+        Box3 domain{};
+        int periodic[3] = {0, 0, 0};
+        int ntag = 0;
+        long long ncell = 0;
+        DevBuf<FabTag> tags;
+        DevBuf<long long> start;
+    } fb;
     Box3 fab_box (int b) const {
         Box3 f = grow(boxes[b], ngrow);
         if (nodal_dir >= 0) { f.hi[nodal_dir] += 1; }
@@ -161,22 +172,6 @@ struct mlmg_multifab_s {
 
 namespace {
 
-template <typename T>
-void fab_run_tags (mlmg_multifab_s& mf, const std::vector<FabTag>& tags)
-{
-    if (tags.empty()) { return; }
-    std::vector<long long> start{0};
-    for (const auto& t : tags) { start.push_back(start.back() + t.box.npts()); }
-    DevBuf<FabTag> dt; DevBuf<long long> ds;
-    cudaStream_t st = lib_stream();
-    dt.upload(tags, st);
-    ds.upload(start, st);
-    k_fab_tags<T><<<grid_for(start.back(), 256), 256, 0, st>>>(mf.dinfo.p, dt.p, ds.p, (int)tags.size(), start.back(),
-                                                              (T*)mf.data.p);
-    g_launches++;
-    MLMG_CUDA_CHECK(cudaGetLastError());
-    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
-}
 
 // FillBoundary tags: every ghost cell of every FAB covered by the valid
 // region of a box (periodic images included).  On one rank the reference's
@@ -229,6 +224,42 @@ std::vector<FabTag> fill_boundary_tags (const mlmg_multifab_s& mf, const GeomC& 
         }
     }
     return tags;
+}
+
+// FabArray::FillBoundary on one rank: the copy tags of the MultiFab's
+// geometry (built once per MultiFab and geometry, kept on the device), then
+// one launch over every tagged ghost cell
+void fill_boundary (mlmg_multifab_s& mf, const GeomC& geom)
+{
+    if (mf.ngrow == 0) { return; }
+    auto& C = mf.fb;
+    const bool same = C.valid && C.domain == geom.domain && C.periodic[0] == geom.periodic[0] &&
+                      C.periodic[1] == geom.periodic[1] && C.periodic[2] == geom.periodic[2];
+    cudaStream_t st = lib_stream();
+    if (!same) {
+        const auto tags = fill_boundary_tags(mf, geom);
+        std::vector<long long> start{0};
+        for (const auto& t : tags) { start.push_back(start.back() + t.box.npts()); }
+        C.tags.upload(tags, st);
+        C.start.upload(start, st);
+        C.ntag = (int)tags.size();
+        C.ncell = start.back();
+        C.domain = geom.domain;
+        for (int d = 0; d < 3; ++d) { C.periodic[d] = geom.periodic[d]; }
+        C.valid = true;
+    }
+    if (C.ncell > 0) {
+        if (mf.prec == 8) {
+            k_fab_tags<double><<<grid_for(C.ncell, 256), 256, 0, st>>>(mf.dinfo.p, C.tags.p, C.start.p, C.ntag, C.ncell,
+                                                                       (double*)mf.data.p);
+        } else {
+            k_fab_tags<float><<<grid_for(C.ncell, 256), 256, 0, st>>>(mf.dinfo.p, C.tags.p, C.start.p, C.ntag, C.ncell,
+                                                                      (float*)mf.data.p);
+        }
+        g_launches++;
+        MLMG_CUDA_CHECK(cudaGetLastError());
+    }
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
 }
 
 // grow-only device scratch of the whole-array transfers: fab_global holds
@@ -701,8 +732,7 @@ int mlmg_multifab_fill_boundary (mlmg_multifab mf, mlmg_geometry geom, int cross
     MLMG_REQUIRE(mf != nullptr && geom != nullptr, ERR_ARGS, "null handle");
     MLMG_REQUIRE(mf->ncomp == 1, ERR_UNSUPPORTED, "FillBoundary of multi-component MultiFabs");
     if (mf->ngrow == 0) { return OK; }
-    const auto tags = fill_boundary_tags(*mf, geom->g);
-    if (mf->prec == 8) { fab_run_tags<double>(*mf, tags); } else { fab_run_tags<float>(*mf, tags); }
+    fill_boundary(*mf, geom->g);
     API_END
 }
 
@@ -1133,8 +1163,7 @@ int mlmg_solve (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, double tol_
     if (sol->ngrow >= 1) {
         // ghost cells between boxes, as the reference's final FillBoundary leaves them
         GeomC g = s->op->geom;
-        const auto tags = fill_boundary_tags(*sol, g);
-        fab_run_tags<double>(*sol, tags);
+        fill_boundary(*sol, g);
     }
     if (final_resid) { *final_resid = s->last.final_resid; }
     if (s->last.status == NOT_CONVERGED) { g_err = "MLMG failed to converge"; }
@@ -1177,8 +1206,7 @@ int mlmg_solve_levels (mlmg_solver s, const mlmg_multifab* sol, const mlmg_multi
         if (sol[l]->ngrow >= 1) {
             GeomC g = op->geom;
             g.domain = refine(op->geom.domain, 1 << l);
-            const auto tags = fill_boundary_tags(*sol[l], g);
-            fab_run_tags<double>(*sol[l], tags);
+            fill_boundary(*sol[l], g);
         }
     }
     if (final_resid) { *final_resid = s->last.final_resid; }
@@ -1428,8 +1456,7 @@ int mlmg_solve_batched (int n, const mlmg_solver* solvers, const mlmg_multifab* 
         if (status) { status[i] = e.reports()[i].status; }
         if (e.reports()[i].status != OK) { worst = (worst == OK || e.reports()[i].status < worst) ? e.reports()[i].status : worst; }
         if (sols[i]->ngrow >= 1) {
-            const auto tags = fill_boundary_tags(*sols[i], solvers[i]->op->geom);
-            fab_run_tags<double>(*sols[i], tags);
+            fill_boundary(*sols[i], solvers[i]->op->geom);
         }
     }
     return worst;

@@ -179,6 +179,11 @@ struct Engine::Impl {
     void load_level0_field (const FabSet* fs, double* field, double defval, int nodal_dir, int s);
     void xfer (const std::vector<XferItem>& items, const FabSet& fs, void* field, bool field_is_f32, int dir);
     std::vector<XferItem> items_for (const FabSet& fs, int s, int ghost_mode, int nodal_dir) const;
+    // transfer tables: grow-only device copies, and per solve a locator of
+    // its level-0 patches (built on first use)
+    DevBuf<XferItem> xfer_items;
+    DevBuf<long long> xfer_start;
+    mutable std::vector<std::unique_ptr<BoxLocator>> xfer_loc;
 
     // ------------------------------------------------------- operations --
     // bcv: Dirichlet values of an inhomogeneous fill (null: the level-0 values)

@@ -421,13 +421,19 @@ std::vector<XferItem> Engine::Impl::items_for (const FabSet& fs, int s, int ghos
     std::vector<XferItem> items;
     const PatchLevel& M = lev[0].meta;
     const int p0 = M.solve_first_patch[s], np = M.solve_npatch[s];
-    for (size_t b = 0; b < fs.boxes.size(); ++b) {
-        const Box3& vb = fs.boxes[b];
-        int pid = -1;
+    if ((int)xfer_loc.size() < nsolve) { xfer_loc.resize(nsolve); }
+    if (!xfer_loc[s]) {
+        std::vector<Box3> pbs;
         for (int p = p0; p < p0 + np; ++p) {
             Box3 pb; for (int d = 0; d < 3; ++d) { pb.lo[d] = M.patches[p].lo[d]; pb.hi[d] = M.patches[p].hi[d]; }
-            if (pb.contains(vb.lo[0], vb.lo[1], vb.lo[2])) { pid = p; break; }
+            pbs.push_back(pb);
         }
+        xfer_loc[s] = std::make_unique<BoxLocator>(pbs);
+    }
+    for (size_t b = 0; b < fs.boxes.size(); ++b) {
+        const Box3& vb = fs.boxes[b];
+        const int loc = xfer_loc[s]->find(vb.lo[0], vb.lo[1], vb.lo[2]);
+        const int pid = (loc >= 0) ? p0 + loc : -1;
         MLMG_REQUIRE(pid >= 0, ERR_ARGS, "MultiFab box outside the operator's BoxArray");
         Box3 fab = grow(vb, fs.ngrow);
         if (fs.nodal_dir >= 0) { fab.hi[fs.nodal_dir] += 1; }
@@ -464,26 +470,28 @@ void Engine::Impl::xfer (const std::vector<XferItem>& items, const FabSet& fs, v
     if (items.empty()) { return; }
     std::vector<long long> start{0};
     for (const auto& X : items) { start.push_back(start.back() + X.region.npts()); }
-    DevBuf<XferItem> d_items;
-    DevBuf<long long> d_start;
-    d_items.upload(items, st());
-    d_start.upload(start, st());
+    // grow-only tables (no allocation once large enough); stream order keeps
+    // the next transfer's upload behind this one's kernel
+    xfer_items.upload(items, st());
+    xfer_start.upload(start, st());
+    const XferItem* d_items = xfer_items.p;
+    const long long* d_start = xfer_start.p;
     const long long n = start.back();
     const int threads = 256;
     const unsigned blocks = (unsigned)((n + threads - 1) / threads);
     const DevLevel& dl = lev[0].dl;
     if (fs.prec == 8 && !field_is_f32) {
-        k_xfer<double, double><<<blocks, threads, 0, st()>>>(dl, d_items.p, d_start.p, (int)items.size(), n,
+        k_xfer<double, double><<<blocks, threads, 0, st()>>>(dl, d_items, d_start, (int)items.size(), n,
             (double*)const_cast<void*>(fs.data), (double*)field, dir);
     } else if (fs.prec == 4 && !field_is_f32) {
-        k_xfer<float, double><<<blocks, threads, 0, st()>>>(dl, d_items.p, d_start.p, (int)items.size(), n,
+        k_xfer<float, double><<<blocks, threads, 0, st()>>>(dl, d_items, d_start, (int)items.size(), n,
             (float*)const_cast<void*>(fs.data), (double*)field, dir);
     } else {
         MLMG_REQUIRE(false, ERR_UNSUPPORTED, "unsupported transfer precision");
     }
     launched();
     MLMG_CUDA_CHECK(cudaGetLastError());
-    MLMG_CUDA_CHECK(cudaStreamSynchronize(st()));   // items are freed on return
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st()));
 }
 
 void Engine::Impl::load_level0_field (const FabSet* fs, double* field, double defval, int nodal_dir, int s)
