@@ -202,8 +202,10 @@ __device__ __forceinline__ void atomic_max_nonneg (double* addr, double v)
     atomicMax(reinterpret_cast<unsigned long long*>(addr), (unsigned long long)__double_as_longlong(v));
 }
 
-// r = b - A x in stencil form; optional per-solve max|r| by atomicMax into
-// norm[solve] (zeroed beforehand; a maximum does not depend on the order)
+// r = b - A x in stencil form (the mixed-precision paths' residuals; the FP64
+// path keeps the reference's operation order in k_residual); optional
+// per-solve max|r| by atomicMax into norm[solve] (zeroed beforehand; a
+// maximum does not depend on the order)
 template <typename T, typename TO, bool VARC, bool INLINE_BC, bool INHOMOG>
 __global__ void __launch_bounds__(TILE_THREADS)
 k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x, const T* __restrict__ b,
@@ -227,8 +229,19 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
                 T xm, xp, ym, yp, zm, zp;
                 neighbours<T, INLINE_BC, INHOMOG>(P, i, j, k, q, x, xc, bcval, xm, xp, ym, yp, zm, zp);
                 const Coef7<T, VARC> cf = load_coef<T, VARC>(P, q, S);
-                const T nb = cf.sxl * xm + cf.sxh * xp + cf.syl * ym + cf.syh * yp + cf.szl * zm + cf.szh * zp;
-                const T v = b[q] - (cf.d * xc - nb);
+                T v;
+                if constexpr (std::is_same_v<T, double>) {
+                    // seven FMAs (b - D x, then + s x_nb): GB300's FP64 rate
+                    // bounds this kernel, and the FMA chain needs one FP64
+                    // operation less per cell than D x - sum s x_nb
+                    v = fma(-cf.d, xc, b[q]);
+                    v = fma(cf.sxl, xm, v); v = fma(cf.sxh, xp, v);
+                    v = fma(cf.syl, ym, v); v = fma(cf.syh, yp, v);
+                    v = fma(cf.szl, zm, v); v = fma(cf.szh, zp, v);
+                } else {
+                    const T nb = cf.sxl * xm + cf.sxh * xp + cf.syl * ym + cf.syh * yp + cf.szl * zm + cf.szh * zp;
+                    v = b[q] - (cf.d * xc - nb);
+                }
                 r[q] = TO(v);
                 mx = fmax(mx, fabs((double)v));
             }
