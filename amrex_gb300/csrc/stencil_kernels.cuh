@@ -202,6 +202,32 @@ __device__ __forceinline__ void atomic_max_nonneg (double* addr, double v)
     atomicMax(reinterpret_cast<unsigned long long*>(addr), (unsigned long long)__double_as_longlong(v));
 }
 
+// block maximum of non-negative doubles held as bit patterns (integer
+// compares; a NaN pattern orders above every number), valid in thread 0
+__device__ __forceinline__ unsigned long long block_max_bits (unsigned long long v, double* sm)
+{
+    unsigned long long* smb = reinterpret_cast<unsigned long long*>(sm);
+    const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+    const int warp = (threadIdx.y * blockDim.x + threadIdx.x) >> 5;
+    const int nwarp = (blockDim.x * blockDim.y + 31) >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+        v = (w > v) ? w : v;
+    }
+    __syncthreads();
+    if (lane == 0) { smb[warp] = v; }
+    __syncthreads();
+    unsigned long long r = 0ull;
+    if (warp == 0) {
+        r = (lane < nwarp) ? smb[lane] : 0ull;
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long w = __shfl_down_sync(0xffffffffu, r, o);
+            r = (w > r) ? w : r;
+        }
+    }
+    return r;
+}
+
 // r = b - A x in stencil form (the mixed-precision paths' residuals; the FP64
 // path keeps the reference's operation order in k_residual); optional
 // per-solve max|r| by atomicMax into norm[solve] (zeroed beforehand; a
@@ -216,6 +242,7 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
     const PatchDesc& P = L.P[c.p];
     const int j = c.y0 + threadIdx.y;
     double mx = 0.0;
+    unsigned long long mxb = 0ull;       // FP64: max |r| as the max of the sign-cleared bit patterns
     if (j <= P.hi[1]) {
         for (int kk = 0; kk < TILE_Z; ++kk) {
             const int k = c.z0 + kk;
@@ -243,12 +270,25 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
                     v = b[q] - (cf.d * xc - nb);
                 }
                 r[q] = TO(v);
-                mx = fmax(mx, fabs((double)v));
+                if constexpr (std::is_same_v<T, double>) {
+                    // integer max on the bit patterns of |v| keeps the FP64 pipe
+                    // free (non-negative doubles order like their bits; a NaN
+                    // residual orders above every number and reaches the norm)
+                    const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+                    mxb = (ab > mxb) ? ab : mxb;
+                } else {
+                    mx = fmax(mx, fabs((double)v));
+                }
             }
         }
     }
     if (norm != nullptr) {
-        const double red = block_reduce(mx, RED_MAXABS, sm);
+        double red;
+        if constexpr (std::is_same_v<T, double>) {
+            red = __longlong_as_double((long long)block_max_bits(mxb, sm));
+        } else {
+            red = block_reduce(mx, RED_MAXABS, sm);
+        }
         if (threadIdx.x == 0 && threadIdx.y == 0) { atomic_max_nonneg(&norm[P.solve], red); }
     }
 }
