@@ -1217,8 +1217,12 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
                                                                           I.red_out.p + ns, I.volinv0_d.p);
         I.launched(3);
     }
-    // initial residual and norms (AMReX_MLMG.H:391-420)
-    I.residual0(false);
+    // initial residual and norms (AMReX_MLMG.H:391-420); the mixed forward
+    // solve takes the norm from its stencil-form FP64 residual, which also
+    // leaves the FP32 copy the first V-cycle reads (the FP64 path keeps the
+    // reference's operation order)
+    const bool fused_init = I.mixed() && !m_opt.transpose;
+    I.residual0(fused_init);
     MLMG_CUDA_CHECK(cudaMemcpyAsync(I.h_red.p, I.red_out.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, m_stream));
     I.reduce_per_solve(0, L0.all, RED_MAXABS, L0.rhs.p, nullptr);
     MLMG_CUDA_CHECK(cudaMemcpyAsync(I.h_red.p + ns, I.red_out.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, m_stream));
@@ -1238,9 +1242,9 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
                         R.rhs_norm, R.init_resid);
         }
     }
-    // when the first residual already meets the target, the mixed path needs
-    // its FP32 copy of the residual for the next iteration anyway
-    if (I.mixed()) { I.residual0(true); }
+    // the transposed (adjoint) mixed solve takes its norm from the FP64
+    // residual above and makes the FP32 copy for its first V-cycle here
+    if (I.mixed() && !fused_init) { I.residual0(true); }
     MLMG_CUDA_CHECK(cudaMemcpyAsync(I.active_d.p, active.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, m_stream));
     const int niters = m_opt.fixed_iter ? m_opt.fixed_iter : m_opt.max_iter;
     bool any_active = false;
