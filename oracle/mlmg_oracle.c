@@ -1607,9 +1607,9 @@ static void amr_reflux(Amr* M, int c, MF* res) {
                 for (int j = ab.lo[1]; j <= ab.hi[1]; ++j)
                 for (int i = ab.lo[0]; i <= ab.hi[0]; ++i) {
                     const int cc3[3] = {i, j, k};
-                    int indom = 1;
+                    int indom = 1;   /* periodic directions wrap (covered_by_fine does) */
                     for (int e = 0; e < 3; ++e)
-                        if (cc3[e] < Lc->domain.lo[e] || cc3[e] > Lc->domain.hi[e]) indom = 0;
+                        if (!Hc->periodic[e] && (cc3[e] < Lc->domain.lo[e] || cc3[e] > Lc->domain.hi[e])) indom = 0;
                     if (!indom || covered_by_fine(M, c, i, j, k)) continue;
                     /* the rr^2 fine faces on the coarse cell's face shared with the fine box */
                     const int t1 = (q == 0) ? 1 : 0, t2 = (q == 2) ? 1 : 2;
@@ -1636,12 +1636,14 @@ static void amr_reflux(Amr* M, int c, MF* res) {
                 }
             }
         }
-        /* add the patch into the register over the uncovered cells of grow(cb,1) */
+        /* add the patch into the register over the uncovered cells of grow(cb,1),
+         * through the periodic images (the register's ParallelAdd with the
+         * coarse geometry's periodicity) */
         FOR_VALID(&patch, i, j, k) {
             const int cc3[3] = {i, j, k};
             int indom = 1;
             for (int e = 0; e < 3; ++e)
-                if (cc3[e] < Lc->domain.lo[e] || cc3[e] > Lc->domain.hi[e]) indom = 0;
+                if (!Hc->periodic[e] && (cc3[e] < Lc->domain.lo[e] || cc3[e] > Lc->domain.hi[e])) indom = 0;
             if (!indom || covered_by_fine(M, c, i, j, k)) continue;
             int wi, wj, wk;
             int db = locate(Lc, Hc->periodic, i, j, k, &wi, &wj, &wk);
@@ -1775,7 +1777,7 @@ static void amr_one_iter(Amr* M, int iter) {
 }
 
 /* MLMGT::solve, AMReX_MLMG.H:353-541, several AMR levels (refinement ratio 2,
- * MLPoisson, non-periodic).  P[l] describes AMR level l: its domain
+ * MLPoisson or MLABecLaplacian, any periodicity shared by the levels).  P[l] describes AMR level l: its domain
  * (n = n_0 2^l), boxes, right-hand side over its domain and initial guess
  * with boundary values in the ghosts (grown domain).  phi_out[l] receives the
  * level's solution on its boxes' cells (level-domain array). */
@@ -1785,7 +1787,7 @@ int oracle_solve_amr(int nlev, const OracleProblem* P, const OracleOptions* o, d
     for (int l = 0; l < nlev; ++l) {
         if (P[l].is_abec != P[0].is_abec ||
             (P[0].is_abec && (P[l].alpha != P[0].alpha || P[l].beta != P[0].beta))) return -2;
-        for (int d = 0; d < 3; ++d) if (P[l].periodic[d]) return -3;
+        for (int d = 0; d < 3; ++d) if (P[l].periodic[d] != P[0].periodic[d]) return -3;
     }
     Amr* M = (Amr*)calloc(1, sizeof(Amr));
     M->nlev = nlev;

@@ -210,7 +210,7 @@ int run_amr (const std::string& mode, const std::string& dir)
     const int nlev = c.geti("nlev", 1);
     const int nx = c.geti("n", 32, 0), ny = c.geti("n", 32, 1), nz = c.geti("n", 32, 2);
     RealBox rb({0., 0., 0.}, {1., 1., 1.});
-    Array<int,3> is_per{0, 0, 0};
+    Array<int,3> is_per{c.geti("periodic", 0, 0), c.geti("periodic", 0, 1), c.geti("periodic", 0, 2)};
     std::vector<Box> dom;
     Vector<Geometry> geom;
     for (int l = 0; l < nlev; ++l) {

@@ -1,10 +1,10 @@
 """AMR composite-solve cases: a base level of n^3 cells, refinement ratio 2,
-levels tagged where |RHS| exceeds the 90th percentile of |RHS| on that level
-(RHS: the seeded sum of 16 Gaussian blobs sampled at each level's cell
-centres), homogeneous Dirichlet on the domain (or, with ``bc``, seeded
-Dirichlet values and initial guess), MLPoisson (or, with ``abec``,
-MLABecLaplacian).  Grids come from the reference's AmrMesh
-(tests/golden/make_amr_golden.py)."""
+levels tagged where |RHS| exceeds the 90th (or ``tag_pct``-th) percentile of
+|RHS| on that level (RHS: the seeded sum of 16 Gaussian blobs sampled at each
+level's cell centres), homogeneous Dirichlet on the domain (or, with ``bc``,
+seeded Dirichlet values and initial guess; ``periodic`` makes directions
+periodic), MLPoisson (or, with ``abec``, MLABecLaplacian).  Grids come from
+the reference's AmrMesh (tests/golden/make_amr_golden.py)."""
 from __future__ import annotations
 
 import ast
@@ -32,6 +32,11 @@ CASES = {
     "c2_n16_2lev_abec": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1012, abec=(0.75, 1.25)),
     "c2_n32_abec": dict(n=32, nlev=3, max_grid_size=16, rhs_seed=1002, abec=(0.75, 1.25), bc=True,
                         solve="summary"),
+    # periodic in x and y (Dirichlet in z): coarse/fine boundaries, reflux and
+    # interpolation across the periodic faces
+    "c2_n16_2lev_per": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1013, periodic=(1, 1, 0), tag_pct=98),
+    "c2_n32_per": dict(n=32, nlev=3, max_grid_size=16, rhs_seed=1004, periodic=(1, 1, 0), tag_pct=97,
+                       solve="summary"),
 }
 
 

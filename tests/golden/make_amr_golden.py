@@ -2,8 +2,8 @@
 (oracle/_ref/ref_driver, built by oracle/ref/Makefile):
 
 * ``amrgrids_<name>.npz``: the grids AmrMesh::MakeNewGrids makes when every
-  level tags the cells where |RHS| exceeds the 90th percentile of |RHS| on
-  that level (blocking factor 8, max_grid_size, n_error_buf 1, grid_eff 0.7);
+  level tags the cells where |RHS| exceeds the 90th (or the case's
+  ``tag_pct``-th) percentile of |RHS| on that level (blocking factor 8, max_grid_size, n_error_buf 1, grid_eff 0.7);
 * ``amrsolve_<name>.npz``: the reference's composite multi-level MLPoisson
   (or MLABecLaplacian) solve on those grids -- phi on every level's boxes (for the configuration-
   size case only per-level statistics and phi at seeded sample cells),
@@ -50,10 +50,13 @@ def make(name, case):
             if co is not None:
                 for key, arr in zip(("a", "bx", "by", "bz"), co[2:]):
                     arr.astype(np.float64).tofile(os.path.join(d, f"{key}_l{lev}.bin"))
-        thresh = [float(np.percentile(np.abs(r), 90)) for r in rhs]
+        thresh = [float(np.percentile(np.abs(r), case.get("tag_pct", 90))) for r in rhs]
+        per = case.get("periodic", (0, 0, 0))
+        bc = " ".join("200" if p else "101" for p in per)   # LinOpBCType: Periodic 200, Dirichlet 101
         base = [f"n {n} {n} {n}", f"nlev {nlev}", f"max_grid_size {case['max_grid_size']}",
                 f"blocking_factor {case.get('blocking_factor', 8)}", "n_error_buf 1", "grid_eff 0.7",
-                "thresh " + " ".join(repr(t) for t in thresh)]
+                "thresh " + " ".join(repr(t) for t in thresh),
+                "periodic " + " ".join(str(int(p)) for p in per), f"lobc {bc}", f"hibc {bc}"]
         _run("amrgrids", d, base)
         grids = amr_cases.parse_grids(open(os.path.join(d, "grids.txt")).read())
         np.savez_compressed(os.path.join(HERE, f"amrgrids_{name}.npz"), case=np.array(repr(case)),

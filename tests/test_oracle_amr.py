@@ -17,6 +17,10 @@ def oracle_case(case):
                max_fmg_iter=case.get("max_fmg_iter", 0))
     if case.get("abec"):
         out.update(op="abec", alpha=case["abec"][0], beta=case["abec"][1])
+    if case.get("periodic"):
+        per = tuple(case["periodic"])
+        bc = tuple(200 if p else 101 for p in per)
+        out.update(periodic=per, lobc=bc, hibc=bc)
     return out
 
 
@@ -35,14 +39,15 @@ def levels_of(case, grids):
 
 
 @pytest.mark.parametrize("name", ["c2_n16_2lev", "c2_n32", "c2_n16_2lev_bc", "c2_n32_fmg", "c2_n16_2lev_abec",
-                                  "c2_n32_abec"])
+                                  "c2_n32_abec", "c2_n16_2lev_per", "c2_n32_per"])
 def test_oracle_amr_matches_reference(name):
     """Iteration and bottom counts, norms, residual history and phi (every
     cell, or per-level statistics and seeded samples for summary fixtures);
     the cases cover 2 and 3 levels, inhomogeneous Dirichlet values with a
-    non-zero initial guess, F-cycles on AMR level 0, and MLABecLaplacian with
+    non-zero initial guess, F-cycles on AMR level 0, MLABecLaplacian with
     per-level coefficients (averaged down across levels before level 0's MG
-    restriction)."""
+    restriction), and domains periodic in x and y with fine boxes on the
+    periodic faces."""
     g = ac.load("amrsolve", name)
     case, grids, ref = g["case"], g["grids"], g["result"]
     phis, info = oracle.solve_amr(oracle_case(case), levels_of(case, grids))
