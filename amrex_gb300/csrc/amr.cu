@@ -9,6 +9,7 @@
 #include "engine_impl.cuh"
 #include "amr_kernels.cuh"
 
+#include <array>
 #include <cmath>
 #include <map>
 
@@ -23,6 +24,35 @@ void upload_or_keep (DevBuf<T>& b, const std::vector<T>& v, cudaStream_t st)
 }
 
 unsigned blocks_for (long long n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// wrap cell c into the level domain `dom` along the periodic directions;
+// false if it lies outside along a non-periodic one
+bool wrap_cell (const Box3& dom, const int* periodic, int* c)
+{
+    for (int d = 0; d < 3; ++d) {
+        if (c[d] >= dom.lo[d] && c[d] <= dom.hi[d]) { continue; }
+        if (!periodic[d]) { return false; }
+        const int n = dom.len(d);
+        c[d] = dom.lo[d] + (((c[d] - dom.lo[d]) % n) + n) % n;
+    }
+    return true;
+}
+
+// the periodic image shifts of a level domain (0 included): multiples -1, 0, 1
+// of the domain length along each periodic direction
+std::vector<std::array<int, 3>> image_shifts (const Box3& dom, const int* periodic)
+{
+    std::vector<std::array<int, 3>> out;
+    for (int sz = -1; sz <= 1; ++sz)
+    for (int sy = -1; sy <= 1; ++sy)
+    for (int sx = -1; sx <= 1; ++sx) {
+        const int sv[3] = {sx, sy, sz};
+        bool ok = true;
+        for (int d = 0; d < 3; ++d) { if (sv[d] != 0 && !periodic[d]) { ok = false; } }
+        if (ok) { out.push_back({sx * dom.len(0), sy * dom.len(1), sz * dom.len(2)}); }
+    }
+    return out;
+}
 
 } // namespace
 
@@ -123,9 +153,6 @@ void AmrEngine::Impl::build ()
 {
     nl = (int)prob.levels.size();
     MLMG_REQUIRE(nl >= 2 && nl <= 8, ERR_ARGS, "an AMR solve needs 2 to 8 levels");
-    for (int d = 0; d < 3; ++d) {
-        MLMG_REQUIRE(!prob.geom.periodic[d], ERR_UNSUPPORTED, "AMR composite solves support non-periodic domains only");
-    }
     lev.resize(nl);
     for (int l = 0; l < nl; ++l) {
         SolveProblem pr;
@@ -182,8 +209,9 @@ void AmrEngine::Impl::build ()
             for (int k = g.lo[2]; k <= g.hi[2]; ++k)
             for (int j = g.lo[1]; j <= g.hi[1]; ++j)
             for (int i = g.lo[0]; i <= g.hi[0]; ++i) {
-                if (!cdom.contains(i, j, k)) { continue; }
-                MLMG_REQUIRE(cl.find(i, j, k) >= 0, ERR_ARGS,
+                int c[3] = {i, j, k};
+                if (!wrap_cell(cdom, prob.geom.periodic, c)) { continue; }
+                MLMG_REQUIRE(cl.find(c[0], c[1], c[2]) >= 0, ERR_ARGS,
                              "AMR levels are not properly nested (a coarsened fine box grown by one leaves the coarser level)");
             }
         }
@@ -233,7 +261,10 @@ void AmrEngine::Impl::build_fine_tables (int l)
     D.cfd.upload(D.h_cfd, st());
     D.cf64.alloc((size_t)D.cf_n);
     if (mixed()) { D.cf32.alloc((size_t)D.cf_n); }
-    // gather tags: every coarse patch's valid cells inside each grown buffer
+    // gather tags: every coarse patch's valid cells (and their periodic
+    // images: source cell = buffer cell - shift) inside each grown buffer
+    const Box3 cdom = refine(prob.geom.domain, 1 << (l - 1));
+    const auto cshifts = image_shifts(cdom, prob.geom.periodic);
     std::vector<CopyTag> tags;
     std::vector<long long> start{0};
     for (int p = 0; p < (int)Mf.patches.size(); ++p) {
@@ -242,12 +273,15 @@ void AmrEngine::Impl::build_fine_tables (int l)
         for (int cp = 0; cp < (int)Mc.patches.size(); ++cp) {
             Box3 cb;
             for (int d = 0; d < 3; ++d) { cb.lo[d] = Mc.patches[cp].lo[d]; cb.hi[d] = Mc.patches[cp].hi[d]; }
-            const Box3 is = intersect(g, cb);
-            if (!is.ok()) { continue; }
-            CopyTag t{};
-            t.dst = p; t.src = cp; t.box = is;
-            tags.push_back(t);
-            start.push_back(start.back() + is.npts());
+            for (const auto& sh : cshifts) {
+                const Box3 is = intersect(g, shift(cb, sh.data()));
+                if (!is.ok()) { continue; }
+                CopyTag t{};
+                t.dst = p; t.src = cp; t.box = is;
+                for (int d = 0; d < 3; ++d) { t.shift[d] = sh[d]; }
+                tags.push_back(t);
+                start.push_back(start.back() + is.npts());
+            }
         }
     }
     D.ngtag = (int)tags.size();
@@ -257,7 +291,10 @@ void AmrEngine::Impl::build_fine_tables (int l)
     // coarse/fine faces and the neighbourhood flags of their ghost cells
     const Box3 fdom = refine(prob.geom.domain, 1 << l);
     const BoxLocator floc(prob.levels[l].boxes);
-    auto notcov = [&] (int i, int j, int k) { return fdom.contains(i, j, k) && floc.find(i, j, k) < 0; };
+    auto notcov = [&] (int i, int j, int k) {
+        int c[3] = {i, j, k};
+        return wrap_cell(fdom, prob.geom.periodic, c) && floc.find(c[0], c[1], c[2]) < 0;
+    };
     std::vector<int8_t> flags(L(l).bcval.n, 0);
     std::vector<int2> faces;
     std::vector<long long> fstart{0};
@@ -265,8 +302,8 @@ void AmrEngine::Impl::build_fine_tables (int l)
         const PatchDesc& P = Mf.patches[p];
         for (int f = 0; f < 6; ++f) {
             const FaceBC& F = P.face[f];
-            if (F.on_domain) { continue; }      // physical face: the level's own BC values
             const int d = f % 3;
+            if (F.on_domain && !prob.geom.periodic[d]) { continue; }   // physical face: the level's own BC values
             const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
             const int g = (f >= 3) ? P.hi[d] + 1 : P.lo[d] - 1;
             const int n1 = P.hi[t1] - P.lo[t1] + 1, n2 = P.hi[t2] - P.lo[t2] + 1;
@@ -373,6 +410,7 @@ void AmrEngine::Impl::build_coarse_tables (int c)
     for (const auto& P : Mc.patches) { cpboxes.push_back(pbox(P)); }
     const BoxLocator cfl(cfboxes), cpl(cpboxes);
     const Box3 cdom = refine(prob.geom.domain, 1 << c);
+    auto cfl_find = [&] (const int* w) { return cfl.find(w[0], w[1], w[2]); };
     struct E { long long q; int key; RefluxFace f; };
     std::vector<E> ent;
     for (int fp = 0; fp < (int)Mf.patches.size(); ++fp) {
@@ -386,8 +424,11 @@ void AmrEngine::Impl::build_coarse_tables (int c)
             for (int k = ab.lo[2]; k <= ab.hi[2]; ++k)
             for (int j = ab.lo[1]; j <= ab.hi[1]; ++j)
             for (int i = ab.lo[0]; i <= ab.hi[0]; ++i) {
-                if (!cdom.contains(i, j, k) || cfl.find(i, j, k) >= 0) { continue; }
-                const int cp = cpl.find(i, j, k);
+                // the coarse cell taking the reflux: (i,j,k) or, past a
+                // periodic face, its image inside the domain
+                int w[3] = {i, j, k};
+                if (!wrap_cell(cdom, prob.geom.periodic, w) || cfl_find(w) >= 0) { continue; }
+                const int cp = cpl.find(w[0], w[1], w[2]);
                 int n[3] = {i, j, k};
                 n[d] += side ? 1 : -1;
                 const int cpn = cpl.find(n[0], n[1], n[2]);
@@ -395,10 +436,10 @@ void AmrEngine::Impl::build_coarse_tables (int c)
                 int fi[3] = {2 * i, 2 * j, 2 * k};
                 fi[d] = side ? 2 * n[d] : 2 * n[d] + 1;
                 E e;
-                e.q = cidx(Mc.patches[cp], i, j, k);
+                e.q = cidx(Mc.patches[cp], w[0], w[1], w[2]);
                 e.key = 2 * d + side;
                 e.f.qn = cidx(Mc.patches[cpn], n[0], n[1], n[2]);
-                int fc[3] = {i, j, k};
+                int fc[3] = {w[0], w[1], w[2]};
                 if (side) { fc[d] += 1; }
                 e.f.qb = cidx(Mc.patches[cp], fc[0], fc[1], fc[2]);
                 e.f.qf = cidx(F, fi[0], fi[1], fi[2]);
@@ -427,6 +468,10 @@ void AmrEngine::Impl::build_coarse_tables (int c)
     // face average-down tags: the faces of each coarsened fine patch (its
     // boundary faces included) within the faces of each coarse patch
     if (abec()) {
+        // (box in the fine patch's frame; the coarse face is box - shift, so a
+        // face on a periodic boundary also reaches its image, as the
+        // reference's ParallelCopy with the coarse periodicity does)
+        const auto cshifts = image_shifts(cdom, prob.geom.periodic);
         for (int d = 0; d < 3; ++d) {
             std::vector<CopyTag> ft;
             std::vector<long long> fs{0};
@@ -436,12 +481,15 @@ void AmrEngine::Impl::build_coarse_tables (int c)
                 for (int cp = 0; cp < (int)Mc.patches.size(); ++cp) {
                     Box3 cb = pbox(Mc.patches[cp]);
                     cb.hi[d] += 1;
-                    const Box3 is = intersect(fb, cb);
-                    if (!is.ok()) { continue; }
-                    CopyTag t{};
-                    t.dst = cp; t.src = fp; t.box = is;
-                    ft.push_back(t);
-                    fs.push_back(fs.back() + is.npts());
+                    for (const auto& sh : cshifts) {
+                        const Box3 is = intersect(fb, shift(cb, sh.data()));
+                        if (!is.ok()) { continue; }
+                        CopyTag t{};
+                        t.dst = cp; t.src = fp; t.box = is;
+                        for (int e = 0; e < 3; ++e) { t.shift[e] = sh[e]; }
+                        ft.push_back(t);
+                        fs.push_back(fs.back() + is.npts());
+                    }
                 }
             }
             D.nftag[d] = (int)ft.size();

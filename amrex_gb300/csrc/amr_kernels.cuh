@@ -25,7 +25,8 @@ __device__ __forceinline__ void tag_cell (const CopyTag* tags, const long long* 
 // buffers over the coarsened fine patch grown by one cell, which were zeroed
 // first: BndryRegisterT::copyFrom and the ParallelCopy of
 // MLMGT::interpCorrection (AMReX_MLMG.H:1719-1750).  Tag dst = fine patch
-// (its coarse buffer descriptor), src = coarse patch.
+// (its coarse buffer descriptor), src = coarse patch, whose cell is the
+// buffer cell minus the tag's periodic shift.
 template <typename T>
 __global__ void k_amr_gather (DevLevel Lc, const PatchDesc* __restrict__ cfd, const CopyTag* __restrict__ tags,
                               const long long* __restrict__ start, int ntag, long long ncell,
@@ -36,7 +37,7 @@ __global__ void k_amr_gather (DevLevel Lc, const PatchDesc* __restrict__ cfd, co
     int w, i, j, k;
     tag_cell(tags, start, ntag, t, w, i, j, k);
     const CopyTag& C = tags[w];
-    cf[cidx(cfd[C.dst], i, j, k)] = crse[cidx(Lc.P[C.src], i, j, k)];
+    cf[cidx(cfd[C.dst], i, j, k)] = crse[cidx(Lc.P[C.src], i - C.shift[0], j - C.shift[1], k - C.shift[2])];
 }
 
 // amrex::average_down onto the covered coarse cells (amrex_avgdown,
@@ -68,7 +69,8 @@ __global__ void k_amr_avgdown (DevLevel Lc, DevLevel Lf, const CopyTag* __restri
 // coefficient b_dir: every coarse face of a coarsened fine patch, its boundary
 // faces included, takes the mean of the 2x2 fine faces on it, summed with the
 // second tangential offset outermost.  Tag dst = coarse patch, src = fine
-// patch, box = coarse faces (face i stored at cell index i of the patch).
+// patch, box = coarse faces in the fine patch's frame (face i stored at cell
+// index i of a patch); the coarse patch's face is box - shift (periodic images).
 __global__ void k_amr_avgdown_faces (DevLevel Lc, DevLevel Lf, const CopyTag* __restrict__ tags,
                                      const long long* __restrict__ start, int ntag, long long ncell, int dir,
                                      const double* __restrict__ fine, double* __restrict__ crse)
@@ -87,7 +89,7 @@ __global__ void k_amr_avgdown_faces (DevLevel Lc, DevLevel Lf, const CopyTag* __
     c += fine[qf + st[t1]];
     c += fine[qf + st[t2]];
     c += fine[qf + st[t1] + st[t2]];
-    crse[cidx(Lc.P[C.dst], i, j, k)] = c * 0.25;
+    crse[cidx(Lc.P[C.dst], i - C.shift[0], j - C.shift[1], k - C.shift[2])] = c * 0.25;
 }
 
 // bits of the per-face-cell neighbourhood flags of the boundary interpolation

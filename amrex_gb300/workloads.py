@@ -70,7 +70,7 @@ def adjoint_objective(n, phi_scale, target_seed=3003):
 
 
 def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_grid_size=32, con_grid_size=32,
-                fused=False, solbc=None, max_fmg_iter=0, abec=None):
+                fused=False, solbc=None, max_fmg_iter=0, abec=None, periodic=(0, 0, 0)):
     """Composite MLPoisson over len(grids) AMR levels: per-level geometry,
     BoxArray, DistributionMapping, solution (1 ghost, zero) and RHS
     MultiFabs, the operator and the MLMG solver.  ``grids[l]`` holds level l's
@@ -78,7 +78,8 @@ def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_
     grown level-domain array with the initial guess in the valid cells and the
     Dirichlet values in the ghosts.  With ``abec[l] = (alpha, beta, a, bx, by,
     bz)`` (level-domain arrays, z-major) the operator is MLABecLaplacian with
-    those per-level coefficients."""
+    those per-level coefficients; ``periodic`` makes those directions periodic
+    (Dirichlet on the others)."""
     geoms, bas, dms, sols, rhss = [], [], [], [], []
     for lev, g in enumerate(grids):
         m = n << lev
@@ -92,7 +93,7 @@ def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_
         rhs = ag.MultiFab(ba, dm, 1, 0)
         for i, b in enumerate(g):
             rhs.set_fab(i, synth.gaussian_rhs_box(m, rhs_seed, b))
-        geoms.append(ag.Geometry(dom))
+        geoms.append(ag.Geometry(dom, is_periodic=tuple(periodic)))
         bas.append(ba)
         dms.append(dm)
         sols.append(sol)
@@ -104,7 +105,8 @@ def amr_problem(n, grids, rhs_seed, precision=0, graph=False, max_iter=200, agg_
         op.setScalars(abec[0][0], abec[0][1])
     else:
         op = ag.MLPoisson(geoms, bas, dms, info)
-    op.setDomainBC((ag.LinOpBCType.Dirichlet,) * 3, (ag.LinOpBCType.Dirichlet,) * 3)
+    bc = tuple(ag.LinOpBCType.Periodic if p else ag.LinOpBCType.Dirichlet for p in periodic)
+    op.setDomainBC(bc, bc)
     for lev in range(len(grids)):
         op.setLevelBC(lev, sols[lev])
         if abec is not None:

@@ -124,10 +124,10 @@ int mlmg_multifab_norminf_noalloc(mlmg_multifab mf, double* out);
  * and dm hold nlev entries, one per AMR level (MLPoissonT(Vector<Geometry>,
  * Vector<BoxArray>, ...), AMReX_MLPoisson.H:21-40).  nlev > 1 (a composite
  * solve, up to 8 levels) is implemented for MLPoisson and MLABecLaplacian
- * with refinement ratio 2 on a non-periodic domain: level l's domain is level
- * 0's refined by 2^l, its boxes coarsen by 2 and nest properly in level l-1
- * (a box coarsened and grown by one cell stays in level l-1 or outside the
- * domain).  MLABecLaplacian takes a and b per AMR level (amrlev of the
+ * with refinement ratio 2, periodic or not: level l's domain is level 0's
+ * refined by 2^l (same periodicity), its boxes coarsen by 2 and nest properly
+ * in level l-1 (a box coarsened and grown by one cell stays in level l-1, its
+ * periodic images included, or outside the domain).  MLABecLaplacian takes a and b per AMR level (amrlev of the
  * coefficient setters); the solve averages each finer level's a and b onto
  * the next coarser level before restricting them to level 0's MG levels
  * (MLABecLaplacianT::averageDownCoeffs, AMReX_MLABecLaplacian.H:610-712). */

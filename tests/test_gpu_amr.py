@@ -13,8 +13,8 @@ from tests.golden import amr_cases as ac
 
 pytestmark = pytest.mark.gpu
 
-SMALL = ["c2_n16_2lev", "c2_n32", "c2_n16_2lev_bc", "c2_n16_2lev_abec"]
-SUMMARY = ["c2_n32_fmg", "c2_n32_abec"]
+SMALL = ["c2_n16_2lev", "c2_n32", "c2_n16_2lev_bc", "c2_n16_2lev_abec", "c2_n16_2lev_per"]
+SUMMARY = ["c2_n32_fmg", "c2_n32_abec", "c2_n32_per"]
 
 
 def _phi_error(g, lev, got):
@@ -34,7 +34,8 @@ def _solve(name, precision=0, graph=False, tol_rel=None, fused=False):
     abec = [ac.level_abec(case, lev) for lev in range(len(grids))] if case.get("abec") else None
     P = workloads.amr_problem(case["n"], grids, case["rhs_seed"], precision=precision, graph=graph,
                               agg_grid_size=case.get("agg_grid_size", 32), con_grid_size=case.get("con_grid_size", 32),
-                              fused=fused, solbc=solbc, max_fmg_iter=case.get("max_fmg_iter", 0), abec=abec)
+                              fused=fused, solbc=solbc, max_fmg_iter=case.get("max_fmg_iter", 0), abec=abec,
+                              periodic=case.get("periodic", (0, 0, 0)))
     resid = P["mlmg"].solve(P["sols"], P["rhss"], tol_rel or case.get("tol_rel", 1e-10), 0.0)
     phis = []
     for lev, boxes in enumerate(grids):
