@@ -1519,15 +1519,19 @@ static void amr_average_down_coeffs(Amr* M, int c) {
                     if (d == 0) { f[1] += r0; f[2] += r1; }
                     else if (d == 1) { f[0] += r0; f[2] += r1; }
                     else { f[0] += r0; f[1] += r1; }
-                    /* a fine box holding the cell on either side of the face holds the face */
-                    int wi, wj, wk;
-                    int fb = locate(Lf, Hc->periodic, f[0], f[1], f[2], &wi, &wj, &wk);
+                    /* a fine box holding the cell on either side of the face
+                     * holds the face: its image's index when the cell lies
+                     * past a periodic face (the box stores the face at the
+                     * wrapped cell, or one above the wrapped low-side cell) */
+                    int w[3];
+                    int fb = locate(Lf, Hc->periodic, f[0], f[1], f[2], &w[0], &w[1], &w[2]);
                     if (fb < 0) {
                         int g[3] = {f[0], f[1], f[2]};
                         g[d] -= 1;
-                        fb = locate(Lf, Hc->periodic, g[0], g[1], g[2], &wi, &wj, &wk);
+                        fb = locate(Lf, Hc->periodic, g[0], g[1], g[2], &w[0], &w[1], &w[2]);
+                        w[d] += 1;
                     }
-                    s += A(&Lf->bcoef[d].fab[fb], f[0], f[1], f[2]);
+                    s += A(&Lf->bcoef[d].fab[fb], w[0], w[1], w[2]);
                 }
                 A(cf, i, j, k) = s * (1.0 / 4.0);
             }

@@ -37,6 +37,8 @@ CASES = {
     "c2_n16_2lev_per": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1013, periodic=(1, 1, 0), tag_pct=98),
     "c2_n32_per": dict(n=32, nlev=3, max_grid_size=16, rhs_seed=1004, periodic=(1, 1, 0), tag_pct=97,
                        solve="summary"),
+    "c2_n16_2lev_per_abec": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1013, periodic=(1, 1, 0), tag_pct=98,
+                                 abec=(0.75, 1.25)),
 }
 
 
@@ -85,6 +87,15 @@ def level_abec(case, lev):
 
     def b(x, y, z):
         return 1.0 + 0.6 * np.cos(4.0 * x - 1.0) * np.sin(3.0 * y + z) + 0.3 * x * z
+
+    if case.get("periodic"):
+        # periodic along the periodic directions, so that the two stored
+        # copies of a face on a periodic boundary hold the same b
+        tp = 2.0 * np.pi
+        a = 1.0 + 0.5 * np.sin(tp * x + 1.0) * np.cos(tp * y) + 0.25 * z
+
+        def b(x, y, z):
+            return 1.0 + 0.6 * np.cos(tp * x - 1.0) * np.sin(tp * y + z) + 0.3 * z * np.cos(tp * x)
 
     bx = b(*np.meshgrid(cc, cc, fc, indexing="ij")[::-1])
     by = b(*np.meshgrid(cc, fc, cc, indexing="ij")[::-1])

@@ -39,7 +39,7 @@ def levels_of(case, grids):
 
 
 @pytest.mark.parametrize("name", ["c2_n16_2lev", "c2_n32", "c2_n16_2lev_bc", "c2_n32_fmg", "c2_n16_2lev_abec",
-                                  "c2_n32_abec", "c2_n16_2lev_per", "c2_n32_per"])
+                                  "c2_n32_abec", "c2_n16_2lev_per", "c2_n32_per", "c2_n16_2lev_per_abec"])
 def test_oracle_amr_matches_reference(name):
     """Iteration and bottom counts, norms, residual history and phi (every
     cell, or per-level statistics and seeded samples for summary fixtures);
