@@ -39,6 +39,8 @@ CASES = {
                        solve="summary"),
     "c2_n16_2lev_per_abec": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1013, periodic=(1, 1, 0), tag_pct=98,
                                  abec=(0.75, 1.25)),
+    # four levels: two intermediate levels with their correction holds
+    "c2_n16_4lev": dict(n=16, nlev=4, max_grid_size=16, rhs_seed=1002, tag_pct=95, solve="summary"),
 }
 
 

@@ -14,7 +14,7 @@ from tests.golden import amr_cases as ac
 pytestmark = pytest.mark.gpu
 
 SMALL = ["c2_n16_2lev", "c2_n32", "c2_n16_2lev_bc", "c2_n16_2lev_abec", "c2_n16_2lev_per", "c2_n16_2lev_per_abec"]
-SUMMARY = ["c2_n32_fmg", "c2_n32_abec", "c2_n32_per"]
+SUMMARY = ["c2_n32_fmg", "c2_n32_abec", "c2_n32_per", "c2_n16_4lev"]
 
 
 def _phi_error(g, lev, got):

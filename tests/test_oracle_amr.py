@@ -39,11 +39,12 @@ def levels_of(case, grids):
 
 
 @pytest.mark.parametrize("name", ["c2_n16_2lev", "c2_n32", "c2_n16_2lev_bc", "c2_n32_fmg", "c2_n16_2lev_abec",
-                                  "c2_n32_abec", "c2_n16_2lev_per", "c2_n32_per", "c2_n16_2lev_per_abec"])
+                                  "c2_n32_abec", "c2_n16_2lev_per", "c2_n32_per", "c2_n16_2lev_per_abec",
+                                  "c2_n16_4lev"])
 def test_oracle_amr_matches_reference(name):
     """Iteration and bottom counts, norms, residual history and phi (every
     cell, or per-level statistics and seeded samples for summary fixtures);
-    the cases cover 2 and 3 levels, inhomogeneous Dirichlet values with a
+    the cases cover 2, 3 and 4 levels, inhomogeneous Dirichlet values with a
     non-zero initial guess, F-cycles on AMR level 0, MLABecLaplacian with
     per-level coefficients (averaged down across levels before level 0's MG
     restriction), and domains periodic in x and y with fine boxes on the
