@@ -1,5 +1,6 @@
 // The AMR composite MLMG solve: MLMGT::solve over several AMR levels
-// (refinement ratio 2, MLPoisson or MLABecLaplacian).  AMR level 0 is a full single-level
+// (refinement ratio 2, MLPoisson or MLABecLaplacian, periodic or not).  AMR
+// level 0 is a full single-level
 // engine (its own MG hierarchy, bottom solve, graphs); each finer AMR level is
 // an engine of one MG level that is only smoothed.  The coarse/fine coupling
 // (boundary-value interpolation, flux-register reflux, average-down,

@@ -1316,8 +1316,8 @@ int oracle_solve(const OracleProblem* P, const OracleOptions* o, double* phi_out
 
 /* ======================================================================
  * AMR composite solve: MLMGT::solve over several AMR levels
- * (AMReX_MLMG.H:353-541, oneIter :1227-1293), MLPoisson, refinement ratio 2,
- * non-periodic domain.  AMR level 0 keeps its full MG hierarchy; each finer
+ * (AMReX_MLMG.H:353-541, oneIter :1227-1293), MLPoisson or MLABecLaplacian,
+ * refinement ratio 2, periodic or not.  AMR level 0 keeps its full MG hierarchy; each finer
  * AMR level has one MG level (MLLinOpT::defineGrids, AMReX_MLLinOp.H:843-880),
  * so its mini-cycle is nu1 smoothing sweeps from zero (mgVcycle,
  * AMReX_MLMG.H:1306-1415, amrlev > 0 branch).
