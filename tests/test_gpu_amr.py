@@ -123,3 +123,25 @@ def test_amr_rejects_unsupported_and_bad_nesting():
     with pytest.raises(ag.MLMGError) as e:
         P["mlmg"].solve(P["sols"][0], P["rhss"][0], 1e-10, 0.0)
     assert e.value.code in (-1, -4)
+
+
+def test_amr_abec_coefficient_arguments():
+    """Per-level coefficients of a composite MLABecLaplacian: a MultiFab on
+    another level's BoxArray, or an AMR level out of range, is rejected (-1)
+    before any solve."""
+    g = ac.load("amrsolve", "c2_n16_2lev_abec")
+    case, grids = g["case"], g["grids"]
+    abec = [ac.level_abec(case, lev) for lev in range(len(grids))]
+    P = workloads.amr_problem(case["n"], grids, case["rhs_seed"], abec=abec)
+    op = P["op"]
+    wrong = ag.MultiFab(P["bas"][0], P["dms"][0], 1, 0)      # level 0's BoxArray offered for level 1
+    with pytest.raises(ag.MLMGError) as e:
+        op.setACoeffs(1, wrong)
+    assert e.value.code == -1
+    with pytest.raises(ag.MLMGError) as e:
+        op.setACoeffs(len(grids), 1.0)
+    assert e.value.code == -1
+    # the rejected calls left the operator as it was: the solve still matches the reference
+    resid = P["mlmg"].solve(P["sols"], P["rhss"], 1e-10, 0.0)
+    assert P["mlmg"].getNumIters() == g["result"]["niters"]
+    assert resid <= 1e-10 * max(g["result"]["rhs_norm"], g["result"]["init_resid"])
