@@ -226,28 +226,50 @@ def bench_batch(stream, nsolve=64):
     specs = workloads.batch_specs(nsolve, 4000)
     probs = [workloads.abec_problem(s.n, 32, s.rhs_seed, s.b_seed) for s in specs]
     cells = sum(s.n ** 3 for s in specs)
-    mixed = []
-    for p in probs:
-        m = ag.MLMG(p["op"])
-        m.setPrecision("mixed")
-        m.setGraph(True)
-        m.setFusedSmoother(True)
-        mixed.append(m)
-    sols, rhss = [p["sol"] for p in probs], [p["rhs"] for p in probs]
-    # tile / slab shapes picked by the autotuner on the largest solve of the
-    # batch; the batch runs with the settings of its first solver
-    big = max(range(nsolve), key=lambda q: specs[q].n)
-    _, tune_report = mixed[big].autotune(sols[big], rhss[big], vcycles=4)
-    chosen = tune_report.strip().splitlines()[-1].replace("chosen: ", "")
-    mixed[0].setFusedSmoother(not chosen.startswith("colour passes"))
-    for name, val in _tuned_options(chosen):
-        mixed[0].setOption(name, val)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
-    def batched():
+    def make_mixed():
+        out = []
+        for p in probs:
+            m = ag.MLMG(p["op"])
+            m.setPrecision("mixed")
+            m.setGraph(True)
+            m.setFusedSmoother(True)
+            out.append(m)
+        return out
+
+    sols, rhss = [p["sol"] for p in probs], [p["rhs"] for p in probs]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # two candidate settings for the batch, each on its own solvers (a batch
+    # engine is built once for its settings; the batch runs with the settings
+    # of its first solver): the autotuner's pick on the largest solve, and the
+    # default tiled TMA sweep; one timed batched call each keeps the faster
+    big = max(range(nsolve), key=lambda q: specs[q].n)
+    tuned = make_mixed()
+    _, tune_report = tuned[big].autotune(sols[big], rhss[big], vcycles=4)
+    chosen = tune_report.strip().splitlines()[-1].replace("chosen: ", "")
+    tuned[0].setFusedSmoother(not chosen.startswith("colour passes"))
+    for name, val in _tuned_options(chosen):
+        tuned[0].setOption(name, val)
+    cands = [(chosen, tuned), ("fused sweep, 32x8x8 tiles, TMA staging (default)", make_mixed())]
+
+    def run_batch(ms):
         for x in sols:
             x.setVal(0.0)
-        return ag.solve_batched(mixed, sols, rhss, TOL_REL, 0.0)
+        return ag.solve_batched(ms, sols, rhss, TOL_REL, 0.0)
+
+    trial = []
+    for label, ms in cands:
+        run_batch(ms)
+        e0.record(stream)
+        run_batch(ms)
+        e1.record(stream)
+        e1.synchronize()
+        trial.append((e0.elapsed_time(e1), label, ms))
+    _, chosen, mixed = min(trial, key=lambda t: t[0])
+    del cands, tuned, trial
+
+    def batched():
+        return run_batch(mixed)
 
     batched()
     reps = 3
@@ -286,7 +308,7 @@ def bench_batch(stream, nsolve=64):
             "speedup": seq_ms / batch_ms, "all_converged": all(v == 0 for v in st),
             "iters_mixed": [min(iters_b), max(iters_b)],
             "iters_fp64": [min(m.getNumIters() for m in fp64), max(m.getNumIters() for m in fp64)],
-            "phi_rel_diff_vs_fp64_max": err, "autotuned": chosen}
+            "phi_rel_diff_vs_fp64_max": err, "settings": chosen}
 
 
 def bench_adjoint(stream, n=128):
