@@ -385,9 +385,10 @@ __device__ __forceinline__ T nbr_ghost (const PatchDesc& P, int f, int i, int j,
 
 // one colour pass of MLPoisson's Gauss-Seidel (mlpoisson_gsrb,
 // AMReX_MLPoisson_3D_K.H:153-196) reading patch-face neighbours through nbr
-// instead of a ghost fill
+// instead of a ghost fill.  Latency-bound on those dependent loads: capped at
+// 40 registers for twelve 128-thread blocks per SM (48 warps)
 template <typename T>
-__global__ void __launch_bounds__(TILE_THREADS)
+__global__ void __launch_bounds__(TILE_THREADS, 12)
 k_gsrb_nbr (DevLevel L, Subset Sb, T* __restrict__ phi, const T* __restrict__ rhs, const long long* __restrict__ nbr,
             int rb)
 {
