@@ -47,14 +47,26 @@ namespace mlmg {
 // once phi has arrived, find the lines in L2 rather than in DRAM.
 enum : int { FS_PF_RHS = 0, FS_PF_D = 1, FS_PF_SX = 2, FS_PF_SY = 3, FS_PF_SZ = 4, FS_PF_NMAP = 5 };
 
-template <bool VARC, bool TMA = false>
-__global__ void __launch_bounds__(FS_THREADS, 5)
+// VAR selects the order and storage of the first colour (the arithmetic, and
+// so every result, is the same bit for bit):
+//   bit 0  its rows run from the last z plane of the tile + 1 to the first,
+//          so that the second colour, which runs from the first plane up,
+//          starts on the coefficient lines the first colour touched last;
+//   bit 1  its values are written in place into A (a first-colour update reads
+//          only second-colour cells and its own), with no separate N buffer:
+//          13.6 KB less shared memory per block, left to L1;
+//   bits 2-3  5 + (VAR >> 2) blocks per SM asked of the register allocator
+//          (VAR 6: 40 registers, 6 blocks; VAR 14: 32 registers, 8 blocks; both
+//          fit the in-place form's 23 KB of shared memory).
+template <bool VARC, bool TMA = false, int VAR = 0>
+__global__ void __launch_bounds__(FS_THREADS, 5 + ((VAR >> 2) & 3))
 k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
                 const float* __restrict__ rhs, StencilPtrs Sc, const CUtensorMap* __restrict__ maps, int* err,
                 const CUtensorMap* __restrict__ pf = nullptr)
 {
     __shared__ __align__(128) float A[FS_AZ][FS_AY][FS_AX];   // phi_in, local (x-4..x+35, y-2..y+9, z-2..z+9)
-    __shared__ float N[FS_NZ][FS_NY][FS_NX];                  // first colour, local (x-1..x+32, y-1..y+8, z-1..z+8)
+    constexpr bool DESC = (VAR & 1) != 0, INPL = (VAR & 2) != 0;
+    __shared__ float N[INPL ? 1 : FS_NZ][INPL ? 1 : FS_NY][INPL ? 1 : FS_NX];   // first colour, local (x-1..x+32, y-1..y+8, z-1..z+8)
     __shared__ PatchLite SP;
 
     const int tid = threadIdx.y * FS_TX + threadIdx.x;
@@ -137,7 +149,9 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
 
     // local (lx, ly, lz) -> A / N element, and the patch-inside test
     auto aat = [&] (int lx, int ly, int lz) -> float& { return A[lz + 2][ly + 2][lx + 4]; };
-    auto nat = [&] (int lx, int ly, int lz) -> float& { return N[lz + 1][ly + 1][lx + 1]; };
+    auto nat = [&] (int lx, int ly, int lz) -> float& {
+        if constexpr (INPL) { return A[lz + 2][ly + 2][lx + 4]; } else { return N[lz + 1][ly + 1][lx + 1]; }
+    };
 
     // ghost layers of the patch faces inside the tile + 1 region (lx in -1..32,
     // ly, lz in -1..8), restricted to the patch's extent along the face.
@@ -225,7 +239,9 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
             const int par0 = (x0 - 1 + y0 - 1 + z0 - 1) & 1;  // parity of local (-1, -1, -1)
             if (tid < RS * FS_RED_ROW) {
                 const int r = tid % FS_RED_ROW;
-                int ry = (tid / FS_RED_ROW) % FS_NY, rz = (tid / FS_RED_ROW) / FS_NY;   // row indices 0..9
+                // row indices 0..9; DESC walks the rows from the last (9, 9) down
+                const int row0 = DESC ? FS_NZ * FS_NY - 1 - tid / FS_RED_ROW : tid / FS_RED_ROW;
+                int ry = row0 % FS_NY, rz = row0 / FS_NY;
     #pragma unroll 2
                 for (int row = tid / FS_RED_ROW; row < FS_NZ * FS_NY; row += RS) {
                     const int ly = ry - 1, lz = rz - 1;
@@ -239,8 +255,13 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
                                                  aat(lx, ly - 1, lz), aat(lx, ly + 1, lz), aat(lx, ly, lz - 1),
                                                  aat(lx, ly, lz + 1));
                     }
-                    ry += RS % FS_NY; rz += RS / FS_NY;
-                    if (ry >= FS_NY) { ry -= FS_NY; rz += 1; }
+                    if constexpr (DESC) {
+                        ry -= RS % FS_NY; rz -= RS / FS_NY;
+                        if (ry < 0) { ry += FS_NY; rz -= 1; }
+                    } else {
+                        ry += RS % FS_NY; rz += RS / FS_NY;
+                        if (ry >= FS_NY) { ry -= FS_NY; rz += 1; }
+                    }
                 }
             }
         }

@@ -5,6 +5,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 namespace mlmg {
 
@@ -634,11 +635,23 @@ void Engine::Impl::smooth_fused (int l, int n)
             const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
             if (use_tma) {
                 const CUtensorMap* pf = E.m_opt.fused_prefetch ? L.tm_pf.p : nullptr;
-                if (abec) {
-                    k_sweep_fused2<true, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p, pf);
-                } else {
-                    k_sweep_fused2<false, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
-                                                                     pf);
+                auto launch = [&] (auto var) {
+                    constexpr int V = decltype(var)::value;
+                    if (abec) {
+                        k_sweep_fused2<true, true, V><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma,
+                                                                           err_d.p, pf);
+                    } else {
+                        k_sweep_fused2<false, true, V><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma,
+                                                                            err_d.p, pf);
+                    }
+                };
+                switch (E.m_opt.fused_var) {
+                    case 1: launch(std::integral_constant<int, 1>{}); break;
+                    case 2: launch(std::integral_constant<int, 2>{}); break;
+                    case 3: launch(std::integral_constant<int, 3>{}); break;
+                    case 6: launch(std::integral_constant<int, 6>{}); break;
+                    case 14: launch(std::integral_constant<int, 14>{}); break;
+                    default: launch(std::integral_constant<int, 0>{}); break;
                 }
             } else if (abec) {
                 k_sweep_fused2<true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p);
