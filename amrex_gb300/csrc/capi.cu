@@ -1100,8 +1100,8 @@ int mlmg_set_option (mlmg_solver s, const char* name, double value)
     else if (n == "fused_v3") { s->opt.fused_v3 = value != 0.0; }
     else if (n == "fused_prefetch") { s->opt.fused_prefetch = value != 0.0; }
     else if (n == "fused_var") {
-        MLMG_REQUIRE(value == 0 || value == 1 || value == 2 || value == 3 || value == 6 || value == 14,
-                     ERR_ARGS, "fused_var must be one of 0, 1, 2, 3, 6, 14");
+        MLMG_REQUIRE(value == 0 || value == 1 || value == 2 || value == 3 || value == 6 || value == 14 ||
+                     value == 16 || value == 18, ERR_ARGS, "fused_var must be one of 0, 1, 2, 3, 6, 14, 16, 18");
         s->opt.fused_var = (int)value;
     }
     else if (n == "march_tma") { s->opt.march_tma = value != 0.0; }

@@ -57,7 +57,12 @@ enum : int { FS_PF_RHS = 0, FS_PF_D = 1, FS_PF_SX = 2, FS_PF_SY = 3, FS_PF_SZ = 
 //          13.6 KB less shared memory per block, left to L1;
 //   bits 2-3  5 + (VAR >> 2) blocks per SM asked of the register allocator
 //          (VAR 6: 40 registers, 6 blocks; VAR 14: 32 registers, 8 blocks; both
-//          fit the in-place form's 23 KB of shared memory).
+//          fit the in-place form's 23 KB of shared memory);
+//   bit 4  the first colour skips the cells of the tile + 1 with two or three
+//          coordinates outside the tile (its edges and corners): no
+//          second-colour cell of the tile has them as neighbours, so the
+//          tile's output is unchanged and their coefficient sectors are not
+//          loaded.
 template <bool VARC, bool TMA = false, int VAR = 0>
 __global__ void __launch_bounds__(FS_THREADS, 5 + ((VAR >> 2) & 3))
 k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
@@ -65,7 +70,7 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
                 const CUtensorMap* __restrict__ pf = nullptr)
 {
     __shared__ __align__(128) float A[FS_AZ][FS_AY][FS_AX];   // phi_in, local (x-4..x+35, y-2..y+9, z-2..z+9)
-    constexpr bool DESC = (VAR & 1) != 0, INPL = (VAR & 2) != 0;
+    constexpr bool DESC = (VAR & 1) != 0, INPL = (VAR & 2) != 0, SKIPE = (VAR & 16) != 0;
     __shared__ float N[INPL ? 1 : FS_NZ][INPL ? 1 : FS_NY][INPL ? 1 : FS_NX];   // first colour, local (x-1..x+32, y-1..y+8, z-1..z+8)
     __shared__ PatchLite SP;
 
@@ -247,8 +252,13 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
                     const int ly = ry - 1, lz = rz - 1;
                     // (x+y+z) even: local lx = 2r - 1 + ((par0 + ry + rz) & 1)
                     const int lx = 2 * r - 1 + ((par0 + ry + rz) & 1);
-                    const bool in = !TOUCH || (lx >= pxl && lx <= pxh && ly >= pyl && ly <= pyh && lz >= pzl &&
-                                                 lz <= pzh);
+                    bool in = !TOUCH || (lx >= pxl && lx <= pxh && ly >= pyl && ly <= pyh && lz >= pzl &&
+                                           lz <= pzh);
+                    if constexpr (SKIPE) {
+                        const int nout = int(lx < 0 || lx >= FS_TX) + int(ly < 0 || ly >= FS_TY) +
+                                         int(lz < 0 || lz >= FS_TZ);
+                        in = in && nout <= 1;
+                    }
                     if (in) {
                         const int o = lz * sxy + ly * sx + lx;
                         nat(lx, ly, lz) = update(lx, ly, lz, o, aat(lx, ly, lz), aat(lx - 1, ly, lz), aat(lx + 1, ly, lz),

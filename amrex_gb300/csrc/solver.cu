@@ -651,6 +651,8 @@ void Engine::Impl::smooth_fused (int l, int n)
                     case 3: launch(std::integral_constant<int, 3>{}); break;
                     case 6: launch(std::integral_constant<int, 6>{}); break;
                     case 14: launch(std::integral_constant<int, 14>{}); break;
+                    case 16: launch(std::integral_constant<int, 16>{}); break;
+                    case 18: launch(std::integral_constant<int, 18>{}); break;
                     default: launch(std::integral_constant<int, 0>{}); break;
                 }
             } else if (abec) {

@@ -108,14 +108,15 @@ def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
 
 
 # k_sweep_fused2's first-colour order and storage: descending z rows (1), in
-# place in the staged tile (2), both (3)
-FUSED_VAR = {"tiled_desc": 1, "tiled_inplace": 2, "tiled_desc_inplace": 3}
+# place in the staged tile (2), both (3), every halo cell (0; the default, 16,
+# skips the halo's edges and corners)
+FUSED_VAR = {"tiled_desc": 1, "tiled_inplace": 2, "tiled_desc_inplace": 3, "tiled_all_halo": 0}
 
 
 @pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_mixed_bc", "solve_abec_48",
                                   "solve_poisson_periodic_x", "solve_abec_mo4"])
 @pytest.mark.parametrize("variant", ["tiled", "tiled_noprefetch", "tiled_v1", "tiled_v3", "march", "march_cpasync",
-                                     "tiled_desc", "tiled_inplace", "tiled_desc_inplace"])
+                                     "tiled_desc", "tiled_inplace", "tiled_desc_inplace", "tiled_all_halo"])
 def test_fused_sweep_matches_colour_passes(name, variant):
     """The fused two-colour sweep (tiled with face ghosts rewritten in shared
     memory, with or without L2 prefetch of its coefficient boxes; the earlier
@@ -127,8 +128,9 @@ def test_fused_sweep_matches_colour_passes(name, variant):
     march = variant.startswith("march")
     opts = {"march_sweep": int(march), "march_min_tiles": 0, "march_tma": int(variant == "march"),
             "fused_v2": int(variant in ("tiled", "tiled_noprefetch", "tiled_v3") or variant in FUSED_VAR),
-            "fused_v3": int(variant == "tiled_v3"), "fused_prefetch": int(variant != "tiled_noprefetch"),
-            "fused_var": FUSED_VAR.get(variant, 0)}
+            "fused_v3": int(variant == "tiled_v3"), "fused_prefetch": int(variant != "tiled_noprefetch")}
+    if variant in FUSED_VAR:
+        opts["fused_var"] = FUSED_VAR[variant]
     p1 = helpers.make_problem(c, inp, precision="mixed", fused=False)
     p2 = helpers.make_problem(c, inp, precision="mixed", fused=True, options=opts)
     p1["mlmg"].solve(p1["sol"], p1["rhs"], 1e-10, 0)
@@ -141,13 +143,13 @@ def test_fused_sweep_matches_colour_passes(name, variant):
 
 
 @pytest.mark.parametrize("name", ["solve_abec_32", "solve_abec_48", "solve_abec_mixed_bc", "solve_poisson_periodic_x"])
-@pytest.mark.parametrize("var", [1, 2, 3, 6, 14])
+@pytest.mark.parametrize("var", [1, 2, 3, 6, 14, 16, 18])
 def test_fused_sweep_order_variants_bitwise(name, var):
     """The first colour's row order and its in-place storage change no
     arithmetic: the solution is bit for bit the default sweep's."""
     c = load.load(name)["case"]
     inp = cases.inputs(c)
-    p1 = helpers.make_problem(c, inp, precision="mixed", fused=True)
+    p1 = helpers.make_problem(c, inp, precision="mixed", fused=True, options={"fused_var": 0})
     p2 = helpers.make_problem(c, inp, precision="mixed", fused=True, options={"fused_var": var})
     p1["mlmg"].solve(p1["sol"], p1["rhs"], 1e-10, 0)
     p2["mlmg"].solve(p2["sol"], p2["rhs"], 1e-10, 0)
