@@ -311,7 +311,7 @@ class MLMG:
     def setTimeKernels(self, on): self._set("mlmg_set_time_kernels", int(bool(on)))
 
     def setOption(self, name, value):
-        """Engine tuning knob (coarse_block, coarse_cells, merge_boxes, fuse_resid_restrict)."""
+        """Engine tuning knob by name (coarse_block, coarse_cells, merge_boxes, march_sweep, ...)."""
         check(capi.lib().mlmg_set_option(self._h, name.encode(), float(value)))
 
     def smootherStats(self, reset=False):

@@ -1093,18 +1093,9 @@ int mlmg_set_option (mlmg_solver s, const char* name, double value)
         s->opt.coarse_cells = (int)value;
     }
     else if (n == "merge_boxes") { s->opt.merge_boxes = value != 0.0; }
-    else if (n == "fuse_resid_restrict") { s->opt.fuse_resid_restrict = value != 0.0; }
     else if (n == "march_sweep") { s->opt.march_sweep = value != 0.0; }
-    else if (n == "fused_v2") { s->opt.fused_v2 = value != 0.0; }
     else if (n == "fused_tma") { s->opt.fused_tma = value != 0.0; }
-    else if (n == "fused_v3") { s->opt.fused_v3 = value != 0.0; }
     else if (n == "fused_prefetch") { s->opt.fused_prefetch = value != 0.0; }
-    else if (n == "fused_var") {
-        MLMG_REQUIRE(value == 0 || value == 1 || value == 2 || value == 3 || value == 6 || value == 14 ||
-                     value == 16 || value == 18, ERR_ARGS, "fused_var must be one of 0, 1, 2, 3, 6, 14, 16, 18");
-        s->opt.fused_var = (int)value;
-    }
-    else if (n == "march_tma") { s->opt.march_tma = value != 0.0; }
     else if (n == "march_tz") {
         MLMG_REQUIRE(value >= 1 && value <= 4096, ERR_ARGS, "march_tz must be in 1..4096");
         s->opt.march_tz = (int)value;
@@ -1313,17 +1304,16 @@ int mlmg_autotune (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, int vcyc
     check_solver_mf(s, sol);
     check_solver_mf(s, rhs);
     MLMG_REQUIRE(vcycles >= 1, ERR_ARGS, "vcycles must be >= 1");
-    struct Cand { const char* name; int fused, march, tz, coarse, cells, v2, tma; };
+    struct Cand { const char* name; int fused, march, tz, coarse, cells, tma; };
     static const Cand cands[] = {
-        {"colour passes", 0, 0, 16, 0, 512, 1, 1},
-        {"fused sweep, 32x8x8 tiles, TMA staging", 1, 0, 16, 0, 512, 1, 1},
-        {"fused sweep, 32x8x8 tiles, cp.async staging", 1, 0, 16, 0, 512, 1, 0},
-        {"fused sweep, 32x8x8 tiles, per-cell face tests", 1, 0, 16, 0, 512, 0, 0},
-        {"fused sweep, 64x16 columns, z-slab 8", 1, 1, 8, 0, 512, 1, 1},
-        {"fused sweep, 64x16 columns, z-slab 16", 1, 1, 16, 0, 512, 1, 1},
-        {"fused sweep, 64x16 columns, z-slab 32", 1, 1, 32, 0, 512, 1, 1},
-        {"fused sweep, 32x8x8 tiles, coarse levels <= 8^3 in one block", 1, 0, 16, 1, 512, 1, 1},
-        {"fused sweep, 32x8x8 tiles, coarse levels <= 16^3 in one block", 1, 0, 16, 1, 4096, 1, 1},
+        {"colour passes", 0, 0, 16, 0, 512, 1},
+        {"fused sweep, 32x8x8 tiles, TMA staging", 1, 0, 16, 0, 512, 1},
+        {"fused sweep, 32x8x8 tiles, cp.async staging", 1, 0, 16, 0, 512, 0},
+        {"fused sweep, 64x16 columns, z-slab 8", 1, 1, 8, 0, 512, 1},
+        {"fused sweep, 64x16 columns, z-slab 16", 1, 1, 16, 0, 512, 1},
+        {"fused sweep, 64x16 columns, z-slab 32", 1, 1, 32, 0, 512, 1},
+        {"fused sweep, 32x8x8 tiles, coarse levels <= 8^3 in one block", 1, 0, 16, 1, 512, 1},
+        {"fused sweep, 32x8x8 tiles, coarse levels <= 16^3 in one block", 1, 0, 16, 1, 4096, 1},
     };
     const EngineOptions saved = s->opt;
     auto scratch = clone_mf(*sol);
@@ -1340,7 +1330,6 @@ int mlmg_autotune (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, int vcyc
         s->opt.march_tz = cands[c].tz;
         s->opt.coarse_block = cands[c].coarse;
         s->opt.coarse_cells = cands[c].cells;
-        s->opt.fused_v2 = cands[c].v2;
         s->opt.fused_tma = cands[c].tma;
         s->opt.fixed_iter = vcycles;
         s->eng.reset();
@@ -1366,7 +1355,6 @@ int mlmg_autotune (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, int vcyc
         s->opt.march_tz = cands[bi].tz;
         s->opt.coarse_block = cands[bi].coarse;
         s->opt.coarse_cells = cands[bi].cells;
-        s->opt.fused_v2 = cands[bi].v2;
         s->opt.fused_tma = cands[bi].tma;
     }
     s->eng.reset();

@@ -8,7 +8,6 @@
 #include "stencil_kernels.cuh"
 #include "fused_sweep.cuh"
 #include "fused_sweep2.cuh"
-#include "fused_sweep3.cuh"
 #include "march_sweep.cuh"
 #include "coarse_vcycle.cuh"
 #include "adjoint_kernels.cuh"
@@ -86,7 +85,6 @@ struct LevelData {
     bool fused = false;
     SubsetData fz;
     DevBuf<CUtensorMap> tm_a, tm_b;   // per patch: tensor maps of the 40x12x12 staging box over cor32 / cor32b
-    DevBuf<CUtensorMap> tm3;          // per patch: the third form's F3_NMAP maps (phi a/b, rhs, stencil)
     DevBuf<CUtensorMap> tm_pf;        // per patch: FS_PF_NMAP L2-prefetch maps (rhs, D, sX, sY, sZ)
     DevBuf<CUtensorMap> tm_m;         // per patch: MT_NMAP plane maps of the TMA z-march
     bool march = false;           // fused sweeps by the z-marching kernel

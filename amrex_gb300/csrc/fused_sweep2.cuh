@@ -1,10 +1,9 @@
-// Fused two-colour Gauss-Seidel sweep, second form: one code path for every
-// tile, little integer work per cell.
+// Fused two-colour Gauss-Seidel sweep on 32x8x8 tiles: one code path for
+// every tile, little integer work per cell.
 //
-// Same arithmetic and the same staging as k_sweep_fused (fused_sweep.cuh):
 // phi_in on the 32x8x8 tile grown by two cells in shared memory (A), the
 // first colour ((i+j+k) even) on the tile grown by one (N), the second colour
-// on the tile, both written out of place.  What differs:
+// on the tile, both written out of place.  Measured choices:
 //
 // * Patch faces are handled by rewriting ghost values in shared memory
 //   instead of testing every cell: after staging, the ghost layer next to each
@@ -47,31 +46,18 @@ namespace mlmg {
 // once phi has arrived, find the lines in L2 rather than in DRAM.
 enum : int { FS_PF_RHS = 0, FS_PF_D = 1, FS_PF_SX = 2, FS_PF_SY = 3, FS_PF_SZ = 4, FS_PF_NMAP = 5 };
 
-// VAR selects the order and storage of the first colour (the arithmetic, and
-// so every result, is the same bit for bit):
-//   bit 0  its rows run from the last z plane of the tile + 1 to the first,
-//          so that the second colour, which runs from the first plane up,
-//          starts on the coefficient lines the first colour touched last;
-//   bit 1  its values are written in place into A (a first-colour update reads
-//          only second-colour cells and its own), with no separate N buffer:
-//          13.6 KB less shared memory per block, left to L1;
-//   bits 2-3  5 + (VAR >> 2) blocks per SM asked of the register allocator
-//          (VAR 6: 40 registers, 6 blocks; VAR 14: 32 registers, 8 blocks; both
-//          fit the in-place form's 23 KB of shared memory);
-//   bit 4  the first colour skips the cells of the tile + 1 with two or three
-//          coordinates outside the tile (its edges and corners): no
-//          second-colour cell of the tile has them as neighbours, so the
-//          tile's output is unchanged and their coefficient sectors are not
-//          loaded.
-template <bool VARC, bool TMA = false, int VAR = 0>
-__global__ void __launch_bounds__(FS_THREADS, 5 + ((VAR >> 2) & 3))
+// The first colour skips the cells of the tile + 1 with two or three
+// coordinates outside the tile (its edges and corners): no second-colour cell
+// of the tile has them as neighbours, so the tile's output is unchanged and
+// their coefficient sectors are not loaded.
+template <bool VARC, bool TMA = false>
+__global__ void __launch_bounds__(FS_THREADS, 5)
 k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
                 const float* __restrict__ rhs, StencilPtrs Sc, const CUtensorMap* __restrict__ maps, int* err,
                 const CUtensorMap* __restrict__ pf = nullptr)
 {
     __shared__ __align__(128) float A[FS_AZ][FS_AY][FS_AX];   // phi_in, local (x-4..x+35, y-2..y+9, z-2..z+9)
-    constexpr bool DESC = (VAR & 1) != 0, INPL = (VAR & 2) != 0, SKIPE = (VAR & 16) != 0;
-    __shared__ float N[INPL ? 1 : FS_NZ][INPL ? 1 : FS_NY][INPL ? 1 : FS_NX];   // first colour, local (x-1..x+32, y-1..y+8, z-1..z+8)
+    __shared__ float N[FS_NZ][FS_NY][FS_NX];                    // first colour, local (x-1..x+32, y-1..y+8, z-1..z+8)
     __shared__ PatchLite SP;
 
     const int tid = threadIdx.y * FS_TX + threadIdx.x;
@@ -154,9 +140,7 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
 
     // local (lx, ly, lz) -> A / N element, and the patch-inside test
     auto aat = [&] (int lx, int ly, int lz) -> float& { return A[lz + 2][ly + 2][lx + 4]; };
-    auto nat = [&] (int lx, int ly, int lz) -> float& {
-        if constexpr (INPL) { return A[lz + 2][ly + 2][lx + 4]; } else { return N[lz + 1][ly + 1][lx + 1]; }
-    };
+    auto nat = [&] (int lx, int ly, int lz) -> float& { return N[lz + 1][ly + 1][lx + 1]; };
 
     // ghost layers of the patch faces inside the tile + 1 region (lx in -1..32,
     // ly, lz in -1..8), restricted to the patch's extent along the face.
@@ -244,34 +228,24 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
             const int par0 = (x0 - 1 + y0 - 1 + z0 - 1) & 1;  // parity of local (-1, -1, -1)
             if (tid < RS * FS_RED_ROW) {
                 const int r = tid % FS_RED_ROW;
-                // row indices 0..9; DESC walks the rows from the last (9, 9) down
-                const int row0 = DESC ? FS_NZ * FS_NY - 1 - tid / FS_RED_ROW : tid / FS_RED_ROW;
-                int ry = row0 % FS_NY, rz = row0 / FS_NY;
+                int ry = (tid / FS_RED_ROW) % FS_NY, rz = (tid / FS_RED_ROW) / FS_NY;
     #pragma unroll 2
                 for (int row = tid / FS_RED_ROW; row < FS_NZ * FS_NY; row += RS) {
                     const int ly = ry - 1, lz = rz - 1;
                     // (x+y+z) even: local lx = 2r - 1 + ((par0 + ry + rz) & 1)
                     const int lx = 2 * r - 1 + ((par0 + ry + rz) & 1);
-                    bool in = !TOUCH || (lx >= pxl && lx <= pxh && ly >= pyl && ly <= pyh && lz >= pzl &&
-                                           lz <= pzh);
-                    if constexpr (SKIPE) {
-                        const int nout = int(lx < 0 || lx >= FS_TX) + int(ly < 0 || ly >= FS_TY) +
-                                         int(lz < 0 || lz >= FS_TZ);
-                        in = in && nout <= 1;
-                    }
+                    const int nout = int(lx < 0 || lx >= FS_TX) + int(ly < 0 || ly >= FS_TY) +
+                                     int(lz < 0 || lz >= FS_TZ);
+                    const bool in = nout <= 1 && (!TOUCH || (lx >= pxl && lx <= pxh && ly >= pyl && ly <= pyh &&
+                                                              lz >= pzl && lz <= pzh));
                     if (in) {
                         const int o = lz * sxy + ly * sx + lx;
                         nat(lx, ly, lz) = update(lx, ly, lz, o, aat(lx, ly, lz), aat(lx - 1, ly, lz), aat(lx + 1, ly, lz),
                                                  aat(lx, ly - 1, lz), aat(lx, ly + 1, lz), aat(lx, ly, lz - 1),
                                                  aat(lx, ly, lz + 1));
                     }
-                    if constexpr (DESC) {
-                        ry -= RS % FS_NY; rz -= RS / FS_NY;
-                        if (ry < 0) { ry += FS_NY; rz -= 1; }
-                    } else {
-                        ry += RS % FS_NY; rz += RS / FS_NY;
-                        if (ry >= FS_NY) { ry -= FS_NY; rz += 1; }
-                    }
+                    ry += RS % FS_NY; rz += RS / FS_NY;
+                    if (ry >= FS_NY) { ry -= FS_NY; rz += 1; }
                 }
             }
         }

@@ -1,22 +1,23 @@
 // Fused two-colour Gauss-Seidel sweep that marches along z (FP32, stencil form).
 //
-// The same update as k_sweep_fused (both colour passes of
+// The same update as k_sweep_fused2 (both colour passes of
 // MLCellLinOpT::smooth, AMReX_MLCellLinOp.H:1204-1217, with the arithmetic of
-// abec_gsrb / mlpoisson_gsrb and the inline ghost closures), organised to
-// keep HBM busy instead of the issue slots:
+// abec_gsrb / mlpoisson_gsrb and the inline ghost closures), organised as a
+// march instead of independent tiles:
 //
 // * a block owns an MS_TX x MS_TY column of cells and walks tz planes of
 //   it; the first colour is recomputed only on a one-cell ring in x and y and
 //   on one plane above and below the chunk, not on a halo around every tile;
 // * every array (phi_in, rhs, D, sX, sY, sZ) is staged plane by plane into
-//   shared-memory rings with 16-byte cp.async copies issued one plane ahead,
-//   so each value crosses HBM once and the arithmetic reads shared memory;
+//   shared-memory rings, so each value crosses HBM once and the arithmetic
+//   reads shared memory;
 // * thread (tx, ty) owns the cell pair x0+2tx, x0+2tx+1 of row y0+ty -- one
 //   cell of each colour -- and writes it with one 8-byte store.
 //
 // Step kr of the march computes the first colour ((i+j+k) even) on plane kr
 // over the column plus its ring, then the second colour on plane kr-1 from
-// the first colour's planes kr-2, kr-1, kr, and writes plane kr-1.
+// the first colour's planes kr-2, kr-1, kr, and writes plane kr-1.  It is an
+// autotuner candidate (slower than the tiled sweep on the 256^3 benchmark).
 #pragma once
 
 #include "fused_sweep.cuh"
@@ -40,13 +41,6 @@ constexpr int MS_ZS = 4;                   // sZ planes kr-1 .. kr+2
 constexpr int MS_XPLANE = MS_XR * MS_RP;
 constexpr int MS_RPLANE = MS_RR * MS_RP;
 constexpr int MS_CPLANE = MS_CR * MS_RP;
-
-// shared floats of one block
-constexpr int march_smem_floats (bool varc)
-{
-    return MS_XS * MS_XPLANE + MS_RS * MS_RPLANE + (varc ? 4 : 1) * MS_CS * MS_CPLANE +
-           (varc ? MS_ZS * MS_CPLANE : 0);
-}
 
 inline int march_tiles_of (const PatchDesc& P, int tz)
 {
@@ -75,31 +69,6 @@ __device__ __forceinline__ TileCoord decode_march_tile (const DevLevel& L, const
 
 __device__ __forceinline__ int ring (int k, int n) { return ((k % n) + n) % n; }
 
-// Stage plane k of `src` (rows row0 .. row0+nrows-1, x from x0-4) into dst.
-// Chunks are copied where the plane lies in [klo, khi], the row in
-// [jlo, jhi] and the chunk overlaps [ilo, ihi]; everything else is zeroed.
-// Every copied chunk lies inside its row of the patch allocation (rows keep
-// XOFF cells before lo and at least 7 after hi).
-__device__ __forceinline__ void march_stage (float* __restrict__ dst, int nrows, int row0, const float* __restrict__ src,
-                                             const PatchLite& P, int k, int klo, int khi, int jlo, int jhi, int ilo,
-                                             int ihi, int x0, int tid)
-{
-    const bool k_ok = k >= klo && k <= khi;
-    for (int u = tid; u < nrows * MS_CH; u += MS_THREADS) {
-        const int row = u / MS_CH, ch = u - row * MS_CH;
-        const int j = row0 + row, i = x0 - 4 + 4 * ch;
-        float* d = dst + row * MS_RP + 4 * ch;
-        if (k_ok && j >= jlo && j <= jhi && i + 3 >= ilo && i <= ihi) {
-            cp_async16(d, src + P.idx(i, j, k));
-        } else {
-            *reinterpret_cast<float4*>(d) = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-    }
-}
-
-__device__ __forceinline__ void cp_async_commit () { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait0 () { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
-
 // one Gauss-Seidel update with the boundary correction of the smoother's
 // diagonal (abec_gsrb / mlpoisson_gsrb in stencil form)
 __device__ __forceinline__ float ms_update (const PatchLite& P, int i, int j, int k, float pc, float xm, float xp,
@@ -119,176 +88,10 @@ __device__ __forceinline__ float ms_update (const PatchLite& P, int i, int j, in
     return pc + relax_factor(gmd) * res;
 }
 
-template <bool VARC>
-__global__ void __launch_bounds__(MS_THREADS, 1)
-k_sweep_march (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
-               const float* __restrict__ rhs, StencilPtrs Sc, int tz)
-{
-    extern __shared__ __align__(16) float ms_smem[];
-    __shared__ PatchLite SP;
-    float* const Xs = ms_smem;                                        // [MS_XS][MS_XR][MS_RP] phi_in
-    float* const Rs = Xs + MS_XS * MS_XPLANE;                         // [MS_RS][MS_RR][MS_RP] first colour
-    float* const Cs = Rs + MS_RS * MS_RPLANE;                         // [rhs, D, sX, sY][MS_CS][MS_CR][MS_RP]
-    float* const Zs = Cs + (VARC ? 4 : 1) * MS_CS * MS_CPLANE;        // [MS_ZS][MS_CR][MS_RP] sZ
-    const int tid = threadIdx.y * (MS_TX / 2) + threadIdx.x;
-    int x0, y0, z0;
-    {
-        const TileCoord c = decode_march_tile(L, S, blockIdx.x, tz);
-        x0 = c.x0; y0 = c.y0; z0 = c.z0;
-        if (tid == 0) {
-            const PatchDesc& Q = L.P[c.p];
-            for (int d = 0; d < 3; ++d) { SP.lo[d] = Q.lo[d]; SP.hi[d] = Q.hi[d]; }
-            SP.sx = Q.sx; SP.sxy = Q.sxy; SP.base = Q.base;
-            SP.dhx = float(Q.dha[0]); SP.dhy = float(Q.dha[1]); SP.dhz = float(Q.dha[2]);
-            for (int f = 0; f < 6; ++f) {
-                SP.f[f].type = Q.face[f].type;
-                SP.f[f].nx = Q.face[f].nx;
-                SP.f[f].c1 = float(Q.face[f].coef[1]);
-                SP.f[f].c2 = float(Q.face[f].coef[2]);
-                SP.f[f].fco = float(Q.face[f].fco);
-            }
-        }
-    }
-    __syncthreads();
-    const PatchLite& P = SP;
-    const int lo0 = P.lo[0], lo1 = P.lo[1], lo2 = P.lo[2], hi0 = P.hi[0], hi1 = P.hi[1], hi2 = P.hi[2];
-    const int ks = z0, ke = min(z0 + tz, hi2 + 1);                    // output planes [ks, ke)
-    const float* const Dg = static_cast<const float*>(Sc.D);
-    const float* const SXg = static_cast<const float*>(Sc.sx);
-    const float* const SYg = static_cast<const float*>(Sc.sy);
-    const float* const SZg = static_cast<const float*>(Sc.sz);
-
-    auto stage_x = [&] (int k) {
-        march_stage(Xs + ring(k, MS_XS) * MS_XPLANE, MS_XR, y0 - 2, phi_in, P, k, lo2, hi2, lo1, hi1, lo0, hi0, x0,
-                    tid);
-    };
-    auto stage_c = [&] (int k) {
-        const int s = ring(k, MS_CS) * MS_CPLANE;
-        march_stage(Cs + s, MS_CR, y0 - 1, rhs, P, k, lo2, hi2, lo1, hi1, lo0, hi0, x0, tid);
-        if constexpr (VARC) {
-            march_stage(Cs + 1 * MS_CS * MS_CPLANE + s, MS_CR, y0 - 1, Dg, P, k, lo2, hi2, lo1, hi1, lo0, hi0, x0, tid);
-            march_stage(Cs + 2 * MS_CS * MS_CPLANE + s, MS_CR, y0 - 1, SXg, P, k, lo2, hi2, lo1, hi1, lo0, hi0 + 1, x0,
-                        tid);
-            march_stage(Cs + 3 * MS_CS * MS_CPLANE + s, MS_CR, y0 - 1, SYg, P, k, lo2, hi2, lo1, hi1 + 1, lo0, hi0, x0,
-                        tid);
-        }
-    };
-    auto stage_z = [&] (int k) {
-        if constexpr (VARC) {
-            march_stage(Zs + ring(k, MS_ZS) * MS_CPLANE, MS_CR, y0 - 1, SZg, P, k, lo2, hi2 + 1, lo1, hi1, lo0, hi0,
-                        x0, tid);
-        }
-    };
-    const float cd = -2.0f * (P.dhx + P.dhy + P.dhz);
-
-    // prologue: phi planes ks-2 .. ks, coefficients of plane ks-1, sZ planes ks-1, ks
-    stage_x(ks - 2); stage_x(ks - 1); stage_x(ks);
-    stage_c(ks - 1);
-    stage_z(ks - 1); stage_z(ks);
-    cp_async_commit();
-
-    constexpr int NRED = (MS_TX + 2) / 2;                             // first-colour cells per ring row
-    for (int kr = ks - 1; kr <= ke; ++kr) {
-        cp_async_wait0();
-        __syncthreads();
-        if (kr + 1 <= ke) { stage_x(kr + 2); stage_c(kr + 1); stage_z(kr + 2); }
-        cp_async_commit();
-
-        // ---- first colour ((i+j+k) even) on plane kr, column + ring
-        if (kr >= lo2 && kr <= hi2) {
-            const float* const Xm = Xs + ring(kr - 1, MS_XS) * MS_XPLANE;
-            const float* const Xc = Xs + ring(kr, MS_XS) * MS_XPLANE;
-            const float* const Xp = Xs + ring(kr + 1, MS_XS) * MS_XPLANE;
-            const int cs = ring(kr, MS_CS) * MS_CPLANE;
-            const float* const Zc = Zs + ring(kr, MS_ZS) * MS_CPLANE;
-            const float* const Zp = Zs + ring(kr + 1, MS_ZS) * MS_CPLANE;
-            float* const Rw = Rs + ring(kr, MS_RS) * MS_RPLANE;
-            for (int u = tid; u < MS_RR * NRED; u += MS_THREADS) {
-                const int row = u / NRED, r = u - row * NRED;
-                const int j = y0 - 1 + row;
-                const int i = x0 - 1 + 2 * r + ((x0 - 1 + j + kr) & 1);
-                if (i < lo0 || i > hi0 || j < lo1 || j > hi1) { continue; }
-                const int cx = i - (x0 - 4);
-                const int xo = (j - (y0 - 2)) * MS_RP + cx;
-                const int co = row * MS_RP + cx;
-                const float pc = Xc[xo];
-                const float xm = (i == lo0) ? P.closure(0, pc, Xc[xo + 1]) : Xc[xo - 1];
-                const float xp = (i == hi0) ? P.closure(3, pc, Xc[xo - 1]) : Xc[xo + 1];
-                const float ym = (j == lo1) ? P.closure(1, pc, Xc[xo + MS_RP]) : Xc[xo - MS_RP];
-                const float yp = (j == hi1) ? P.closure(4, pc, Xc[xo - MS_RP]) : Xc[xo + MS_RP];
-                const float zm = (kr == lo2) ? P.closure(2, pc, Xp[xo]) : Xm[xo];
-                const float zp = (kr == hi2) ? P.closure(5, pc, Xm[xo]) : Xp[xo];
-                float d, sxl, sxh, syl, syh, szl, szh;
-                if constexpr (VARC) {
-                    d = Cs[1 * MS_CS * MS_CPLANE + cs + co];
-                    sxl = Cs[2 * MS_CS * MS_CPLANE + cs + co]; sxh = Cs[2 * MS_CS * MS_CPLANE + cs + co + 1];
-                    syl = Cs[3 * MS_CS * MS_CPLANE + cs + co]; syh = Cs[3 * MS_CS * MS_CPLANE + cs + co + MS_RP];
-                    szl = Zc[co]; szh = Zp[co];
-                } else {
-                    d = cd; sxl = sxh = -P.dhx; syl = syh = -P.dhy; szl = szh = -P.dhz;
-                }
-                Rw[co] = ms_update(P, i, j, kr, pc, xm, xp, ym, yp, zm, zp, d, sxl, sxh, syl, syh, szl, szh,
-                                   Cs[cs + co]);
-            }
-        }
-        __syncthreads();
-
-        // ---- second colour on plane kb = kr-1 and the output of that plane
-        const int kb = kr - 1;
-        if (kb >= ks && kb < ke) {
-            const int j = y0 + threadIdx.y;
-            const int i0 = x0 + 2 * threadIdx.x;
-            if (j <= hi1 && i0 <= hi0) {
-                const bool red0 = ((i0 + j + kb) & 1) == 0;
-                const int ib = red0 ? i0 + 1 : i0;
-                const int ir = red0 ? i0 : i0 + 1;
-                const int row = j - (y0 - 1);
-                const float* const Rc = Rs + ring(kb, MS_RS) * MS_RPLANE + row * MS_RP;
-                float vb = 0.0f;
-                if (ib <= hi0) {
-                    const int cx = ib - (x0 - 4);
-                    const int co = row * MS_RP + cx;
-                    const float pc = Xs[ring(kb, MS_XS) * MS_XPLANE + (j - (y0 - 2)) * MS_RP + cx];
-                    const float* const R0 = Rc + cx;
-                    const float xm = (ib == lo0) ? P.closure(0, pc, R0[1]) : R0[-1];
-                    const float xp = (ib == hi0) ? P.closure(3, pc, R0[-1]) : R0[1];
-                    const float ym = (j == lo1) ? P.closure(1, pc, R0[MS_RP]) : R0[-MS_RP];
-                    const float yp = (j == hi1) ? P.closure(4, pc, R0[-MS_RP]) : R0[MS_RP];
-                    const float rm = Rs[ring(kb - 1, MS_RS) * MS_RPLANE + co];
-                    const float rp = Rs[ring(kb + 1, MS_RS) * MS_RPLANE + co];
-                    const float zm = (kb == lo2) ? P.closure(2, pc, rp) : rm;
-                    const float zp = (kb == hi2) ? P.closure(5, pc, rm) : rp;
-                    const int cs = ring(kb, MS_CS) * MS_CPLANE;
-                    float d, sxl, sxh, syl, syh, szl, szh;
-                    if constexpr (VARC) {
-                        d = Cs[1 * MS_CS * MS_CPLANE + cs + co];
-                        sxl = Cs[2 * MS_CS * MS_CPLANE + cs + co]; sxh = Cs[2 * MS_CS * MS_CPLANE + cs + co + 1];
-                        syl = Cs[3 * MS_CS * MS_CPLANE + cs + co]; syh = Cs[3 * MS_CS * MS_CPLANE + cs + co + MS_RP];
-                        szl = Zs[ring(kb, MS_ZS) * MS_CPLANE + co]; szh = Zs[ring(kb + 1, MS_ZS) * MS_CPLANE + co];
-                    } else {
-                        d = cd; sxl = sxh = -P.dhx; syl = syh = -P.dhy; szl = szh = -P.dhz;
-                    }
-                    vb = ms_update(P, ib, j, kb, pc, xm, xp, ym, yp, zm, zp, d, sxl, sxh, syl, syh, szl, szh,
-                                   Cs[cs + co]);
-                }
-                const float vr = Rc[ir - (x0 - 4)];
-                float* const out = phi_out + P.idx(i0, j, kb);
-                if (i0 + 1 <= hi0) {
-                    *reinterpret_cast<float2*>(out) = red0 ? make_float2(vr, vb) : make_float2(vb, vr);
-                } else {
-                    out[0] = red0 ? vr : vb;
-                }
-            }
-        }
-    }
-}
-
 // ---------------------------------------------------------------------------
-// The z-march with every plane staged by the Tensor Memory Accelerator.
-//
-// Same column, chunk and arithmetic as k_sweep_march; the staging differs:
-// each plane of phi_in (72 x 20 floats from (x0-4, y0-2)) and of rhs, D, sX,
-// sY, sZ (72 x 19 from (x0-4, y0-1)) arrives by one cp.async.bulk.tensor.3d
+// Staging by the Tensor Memory Accelerator: each plane of phi_in (72 x 20
+// floats from (x0-4, y0-2)) and of rhs, D, sX, sY, sZ (72 x 19 from
+// (x0-4, y0-1)) arrives by one cp.async.bulk.tensor.3d
 // load of a per-patch tensor map, issued by one thread, MT_LA steps ahead of
 // the plane being computed, so that about MT_LA x 33 KB per SM are in flight
 // while the block computes.  Group g = {phi plane g+1, rhs/D/sX/sY plane g,

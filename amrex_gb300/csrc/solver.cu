@@ -171,10 +171,6 @@ void Engine::Impl::build ()
                 Z.tstart.upload(Z.h_tstart, st());
                 static bool attr_set = false;
                 if (!attr_set) {
-                    MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_march<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                         march_smem_floats(true) * (int)sizeof(float)));
-                    MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_march<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                         march_smem_floats(false) * (int)sizeof(float)));
                     MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_march_tma<true>,
                         cudaFuncAttributeMaxDynamicSharedMemorySize, march_tma_smem_floats(true) * (int)sizeof(float)));
                     MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_march_tma<false>,
@@ -201,7 +197,7 @@ void Engine::Impl::build ()
         }
         if (L.has_bottom) { for (auto& b : L.bw) { alloc0(b); } }
         // tensor maps of the fused sweep's TMA staging, one per patch of the level
-        if (L.fused && !L.march && E.m_opt.fused_v2 && E.m_opt.fused_tma) {
+        if (L.fused && !L.march && E.m_opt.fused_tma) {
             std::vector<CUtensorMap> ta(M.patches.size()), tb(M.patches.size());
             for (size_t p = 0; p < M.patches.size(); ++p) {
                 ta[p] = patch_tensor_map(L.cor32.p, M.patches[p]);
@@ -228,7 +224,7 @@ void Engine::Impl::build ()
         }
         // the TMA z-march's maps: one plane (72 x 20 of phi, 72 x 19 of rhs and
         // the stencil arrays) per load, per patch
-        if (L.march && E.m_opt.march_tma) {
+        if (L.march) {
             std::vector<CUtensorMap> tm((size_t)MT_NMAP * M.patches.size());
             std::memset(tm.data(), 0, tm.size() * sizeof(CUtensorMap));
             for (size_t p = 0; p < M.patches.size(); ++p) {
@@ -245,33 +241,6 @@ void Engine::Impl::build ()
                 }
             }
             L.tm_m.upload(tm, st());
-        }
-        // the third form's maps: phi (both buffers), rhs and the stencil arrays, per patch
-        if (L.fused && !L.march && E.m_opt.fused_v3) {
-            std::vector<CUtensorMap> t3((size_t)F3_NMAP * M.patches.size());
-            std::memset(t3.data(), 0, t3.size() * sizeof(CUtensorMap));
-            for (size_t p = 0; p < M.patches.size(); ++p) {
-                CUtensorMap* m = &t3[p * F3_NMAP];
-                const PatchDesc& P = M.patches[p];
-                m[F3_PHI_A] = patch_tensor_map(L.cor32.p, P, 12, 12);
-                m[F3_PHI_B] = patch_tensor_map(L.cor32b.p, P, 12, 12);
-                m[F3_RHS] = patch_tensor_map(L.res32.p, P, 10, 10);
-                if (abec) {
-                    m[F3_D] = patch_tensor_map(L.D32.p, P, 10, 10);
-                    m[F3_SX] = patch_tensor_map(L.sx32.p, P, 10, 10);
-                    m[F3_SY] = patch_tensor_map(L.sy32.p, P, 11, 10);
-                    m[F3_SZ] = patch_tensor_map(L.sz32.p, P, 10, 11);
-                }
-            }
-            L.tm3.upload(t3, st());
-            static bool attr3 = false;
-            if (!attr3) {
-                MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_fused3<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     Fs3Plan::bytes(true)));
-                MLMG_CUDA_CHECK(cudaFuncSetAttribute(k_sweep_fused3<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     Fs3Plan::bytes(false)));
-                attr3 = true;
-            }
         }
     }
     err_d.alloc(1);
@@ -599,11 +568,10 @@ void Engine::Impl::smooth_fused (int l, int n)
     const CUtensorMap* ma = L.tm_a.p;      // tensor maps over a and b (TMA staging)
     const CUtensorMap* mb = L.tm_b.p;
     const bool use_tma = ma != nullptr;
-    int pa = F3_PHI_A, pb = F3_PHI_B;       // the third form's phi maps of a and b
     const StencilPtrs S = stencil32(l);
     for (int i = 0; i < n; ++i) {
         if (timed) { kev_record(); }
-        if (L.march && L.tm_m.p != nullptr) {
+        if (L.march) {
             const dim3 blk(MS_TX / 2, MS_TY);
             const int pm = (a == L.cor32.p) ? MT_PHI_A : MT_PHI_B;
             if (abec) {
@@ -613,63 +581,26 @@ void Engine::Impl::smooth_fused (int l, int n)
                 k_sweep_march_tma<false><<<L.mz.ntiles, blk, march_tma_smem_floats(false) * sizeof(float), st()>>>(
                     L.dl, L.mz.dev(), b, L.tm_m.p, pm, E.m_opt.march_tz, err_d.p);
             }
-        } else if (L.march) {
-            const dim3 blk(MS_TX / 2, MS_TY);
+        } else if (use_tma) {
+            const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
+            const CUtensorMap* pf = E.m_opt.fused_prefetch ? L.tm_pf.p : nullptr;
             if (abec) {
-                k_sweep_march<true><<<L.mz.ntiles, blk, march_smem_floats(true) * sizeof(float), st()>>>(
-                    L.dl, L.mz.dev(), a, b, L.res32.p, S, E.m_opt.march_tz);
+                k_sweep_fused2<true, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p, pf);
             } else {
-                k_sweep_march<false><<<L.mz.ntiles, blk, march_smem_floats(false) * sizeof(float), st()>>>(
-                    L.dl, L.mz.dev(), a, b, L.res32.p, S, E.m_opt.march_tz);
+                k_sweep_fused2<false, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p, pf);
             }
-        } else if (L.tm3.p != nullptr) {
+        } else {
             const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
             if (abec) {
-                k_sweep_fused3<true><<<g, blk, Fs3Plan::bytes(true), st()>>>(L.dl, L.fz.dev(), a, b, S, L.tm3.p, pa,
-                                                                             err_d.p);
-            } else {
-                k_sweep_fused3<false><<<g, blk, Fs3Plan::bytes(false), st()>>>(L.dl, L.fz.dev(), a, b, S, L.tm3.p, pa,
-                                                                               err_d.p);
-            }
-        } else if (E.m_opt.fused_v2) {
-            const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
-            if (use_tma) {
-                const CUtensorMap* pf = E.m_opt.fused_prefetch ? L.tm_pf.p : nullptr;
-                auto launch = [&] (auto var) {
-                    constexpr int V = decltype(var)::value;
-                    if (abec) {
-                        k_sweep_fused2<true, true, V><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma,
-                                                                           err_d.p, pf);
-                    } else {
-                        k_sweep_fused2<false, true, V><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma,
-                                                                            err_d.p, pf);
-                    }
-                };
-                switch (E.m_opt.fused_var) {
-                    case 1: launch(std::integral_constant<int, 1>{}); break;
-                    case 2: launch(std::integral_constant<int, 2>{}); break;
-                    case 3: launch(std::integral_constant<int, 3>{}); break;
-                    case 6: launch(std::integral_constant<int, 6>{}); break;
-                    case 14: launch(std::integral_constant<int, 14>{}); break;
-                    case 16: launch(std::integral_constant<int, 16>{}); break;
-                    case 18: launch(std::integral_constant<int, 18>{}); break;
-                    default: launch(std::integral_constant<int, 0>{}); break;
-                }
-            } else if (abec) {
                 k_sweep_fused2<true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p);
             } else {
                 k_sweep_fused2<false><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p);
             }
-        } else if (abec) {
-            k_sweep_fused<true><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);
-        } else {
-            k_sweep_fused<false><<<L.fz.ntiles, dim3(FS_TX, FS_TY), 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S);
         }
         launched();
         if (timed) { kev_record(); }
         std::swap(a, b);
         std::swap(ma, mb);
-        std::swap(pa, pb);
     }
     if (a != L.cor32.p) {
         MLMG_CUDA_CHECK(cudaMemcpyAsync(L.cor32.p, a, sizeof(float) * (size_t)L.meta.nelem, cudaMemcpyDeviceToDevice,
@@ -762,22 +693,6 @@ void Engine::Impl::vcycle (int top)
             smooth_fused(l, o.nu1);
         } else {
             for (int i = 0; i < o.nu1; ++i) { smooth<T>(l, cor, res, i == 0); }
-        }
-        if constexpr (std::is_same_v<T, float>) {
-            if (L.inline_bc && E.m_opt.fuse_resid_restrict) {
-                // fused with the restriction below: the fine residual is never stored
-                LevelData& C = lev[l + 1];
-                const StencilPtrs S = stencil32(l);
-                if (abec) {
-                    k_resid_restrict<true><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), cor, res, S,
-                                                                                 field_res<T>(l + 1));
-                } else {
-                    k_resid_restrict<false><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), cor, res,
-                                                                                  S, field_res<T>(l + 1));
-                }
-                launched();
-                continue;
-            }
         }
         correction_residual<T>(l);
         LevelData& C = lev[l + 1];

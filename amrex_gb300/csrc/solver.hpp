@@ -37,7 +37,6 @@ struct EngineOptions {
     int fused_smoother = 0;     // fused two-colour sweeps where a level allows
     int merge_boxes = 1;        // merge a level's boxes into one patch where exact
     int time_kernels = 0;       // time every finest-level smoother launch with CUDA events
-    int fuse_resid_restrict = 0;  // correction residual and restriction in one kernel (slower on GB300)
     int coarse_block = 0;       // run the coarse levels of each V-cycle in one thread block per solve
                                 // (slower than graph-replayed grid-wide launches on GB300 at every
                                 // threshold from 2^3 to 32^3 cells)
@@ -46,16 +45,9 @@ struct EngineOptions {
                                 // (measured slower than the tiled fused sweep: 0.27 vs 0.18 ms at 256^3)
     int march_min_tiles = 304;  // ... at least this many (column, z-chunk) tiles
     int march_tz = 16;          // planes per z-slab of the marching sweep
-    int march_tma = 1;          // ... staging its planes by TMA tensor loads (else 16-byte cp.async)
-    int fused_v2 = 1;           // fused sweeps by k_sweep_fused2 (face ghosts rewritten in shared memory,
-                                // one path for every tile) instead of k_sweep_fused
-    int fused_tma = 1;          // ... staging each tile by one TMA tensor load
-    int fused_v3 = 0;           // fused sweeps by k_sweep_fused3 (every input of a tile staged by TMA)
+    int fused_tma = 1;          // tiled fused sweeps stage each tile by one TMA tensor load (else 16-byte
+                                // cp.async copies)
     int fused_prefetch = 1;     // TMA sweeps also prefetch each tile's rhs and stencil boxes into L2
-    int fused_var = 16;         // TMA sweeps: first colour skips the tile + 1's edges and corners (16,
-                                // default: 147.7 -> 145.7 us at 256^3), in descending z (bit 0) and/or
-                                // in place in the staged tile (bit 1), in place with 6 (var 6) or 8
-                                // (var 14) blocks per SM; the tile's output is the same bit for bit
     int max_fmg_iter = 0;       // F-cycles (MLMGT::mgFcycle) for the first max_fmg_iter iterations
     int transpose = 0;          // solve A^T x = rhs (homogeneous BCs): the outer residual uses A^T,
                                 // the V-cycle of A is the correction operator (adjoint solves)

@@ -293,46 +293,4 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
     }
 }
 
-// crse_res = R(res - L cor): computeResOfCorrection followed by restriction
-// (mgVcycle, AMReX_MLMG.H:1334-1343) in one pass, so the fine residual is
-// never written.  Each coarse cell sums its 2x2x2 fine residuals in the
-// order of amrex_avgdown (k outer, i inner) and scales by 1/8.  Homogeneous
-// BCs, computed inline (the fine level has inline ghosts).
-template <bool VARC>
-__global__ void __launch_bounds__(TILE_THREADS)
-k_resid_restrict (DevLevel Lf, DevLevel Lc, Subset Sc, const float* __restrict__ cor, const float* __restrict__ res,
-                  StencilPtrs S, float* __restrict__ crse)
-{
-    const TileCoord c = decode_tile(Lc, Sc, blockIdx.x);
-    const PatchDesc& C = Lc.P[c.p];
-    const int jc = c.y0 + threadIdx.y;
-    if (jc > C.hi[1]) { return; }
-    const int s = C.solve;
-    const float volfrac = 1.0f / 8.0f;
-    for (int kk = 0; kk < TILE_Z; ++kk) {
-        const int kc = c.z0 + kk;
-        if (kc > C.hi[2]) { break; }
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int ic = c.x0 + threadIdx.x + 32 * h;
-            if (ic > C.hi[0]) { continue; }
-            const PatchDesc& F = Lf.P[find_patch(Lf, s, 2 * ic, 2 * jc, 2 * kc)];
-            float sum = 0.0f;
-            for (int kr = 0; kr < 2; ++kr)
-            for (int jr = 0; jr < 2; ++jr)
-            for (int ir = 0; ir < 2; ++ir) {
-                const int i = 2 * ic + ir, j = 2 * jc + jr, k = 2 * kc + kr;
-                const long long q = cidx(F, i, j, k);
-                const float xc = cor[q];
-                float xm, xp, ym, yp, zm, zp;
-                neighbours<float, true, false>(F, i, j, k, q, cor, xc, nullptr, xm, xp, ym, yp, zm, zp);
-                const Coef7<float, VARC> cf = load_coef<float, VARC>(F, q, S);
-                const float nb = cf.sxl * xm + cf.sxh * xp + cf.syl * ym + cf.syh * yp + cf.szl * zm + cf.szh * zp;
-                sum += res[q] - (cf.d * xc - nb);
-            }
-            crse[cidx(C, ic, jc, kc)] = volfrac * sum;
-        }
-    }
-}
-
 } // namespace mlmg

@@ -210,8 +210,7 @@ def _tuned_options(chosen):
         opts += [("coarse_block", 1), ("coarse_cells", 512 if "8^3" in chosen else 4096)]
     else:
         opts.append(("coarse_block", 0))
-    opts.append(("fused_v2", 0 if "per-cell face tests" in chosen else 1))
-    opts.append(("fused_tma", 0 if ("cp.async" in chosen or "per-cell" in chosen) else 1))
+    opts.append(("fused_tma", 0 if "cp.async" in chosen else 1))
     return opts
 
 

@@ -182,21 +182,13 @@ int mlmg_set_fused_smoother(mlmg_solver s, int on);      /* fused two-colour Gau
 /* engine tuning knobs by name: "coarse_block" (0/1: run the coarse levels of
  * each V-cycle in one thread block per solve), "coarse_cells" (a level is
  * coarse when every solve has at most this many cells on it),
- * "merge_boxes" (0/1), "fuse_resid_restrict" (0/1), "march_sweep" (0/1: fused
- * sweeps by the z-marching kernel), "march_min_tiles" (levels with fewer
- * marching tiles use the tiled fused sweep), "fused_v2" (0/1: the tiled fused
- * sweep with face ghosts rewritten in shared memory, default 1), "fused_tma"
- * (0/1: that sweep stages each tile by one TMA tensor load, default 1),
- * "fused_prefetch" (0/1: ... and prefetches the tile's rhs and stencil boxes
- * into L2, default 1), "fused_var" (0, 1, 2, 3, 6, 14, 16, 18: the TMA sweep's
- * first colour in descending z (bit 0) and/or in place in the staged tile
- * (bit 1); 6 and 14 are in place with 6 or 8 blocks per SM; 16 skips the
- * first colour on the tile + 1's edges and corners, which no tile cell reads,
- * 18 does so in place; same results bit for bit, default 16), "fused_v3"
- * (0/1: every input of a tile staged by TMA),
- * "march_tz" (planes per z-slab of the marching sweep), "march_tma" (0/1: the
- * marching sweep stages its planes by TMA tensor loads, default 1); -4 for an
- * unknown name */
+ * "merge_boxes" (0/1), "march_sweep" (0/1: fused sweeps by the z-marching
+ * kernel), "march_min_tiles" (levels with fewer marching tiles use the tiled
+ * fused sweep), "march_tz" (planes per z-slab of the marching sweep),
+ * "fused_tma" (0/1: the tiled fused sweep stages each tile by one TMA tensor
+ * load, else by 16-byte cp.async copies; default 1), "fused_prefetch" (0/1:
+ * ... and prefetches the tile's rhs and stencil boxes into L2, default 1);
+ * -4 for an unknown name */
 int mlmg_set_option(mlmg_solver s, const char* name, double value);
 /* time every finest-level smoother launch with CUDA events on the library
  * stream (graph replays included); the stats accumulate until reset */

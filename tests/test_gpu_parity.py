@@ -81,8 +81,7 @@ MIXED_CASES = ["solve_poisson_32", "solve_abec_32", "solve_abec_48", "solve_abec
 
 @pytest.mark.parametrize("name", MIXED_CASES)
 @pytest.mark.parametrize("graph,fused,coarse,march", [(False, False, 1, 0), (True, False, 1, 0), (True, True, 1, 0),
-                                                      (False, False, 0, 0), (True, True, 0, 0), (True, True, 0, 1),
-                                                      (True, True, 0, 2)])
+                                                      (False, False, 0, 0), (True, True, 0, 0), (True, True, 0, 1)])
 def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
     """FP32 V-cycles inside FP64 refinement reach the same 1e-10 relative
     residual (the residual is evaluated in FP64); phi agrees with the
@@ -92,8 +91,8 @@ def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
     c = g["case"]
     opts = {"coarse_block": coarse}
     if march:
-        # the z-marching sweep on every fused level: TMA staging (1) or cp.async (2)
-        opts.update(march_sweep=1, march_min_tiles=0, march_tma=int(march == 1))
+        # the z-marching sweep on every fused level
+        opts.update(march_sweep=1, march_min_tiles=0)
     prob = helpers.make_problem(c, cases.inputs(c), precision="mixed", graph=graph, fused=fused, options=opts)
     resid = prob["mlmg"].solve(prob["sol"], prob["rhs"], c["tol_rel"], c["tol_abs"])
     r = g["result"]
@@ -107,30 +106,19 @@ def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
     assert np.abs(phi - ref).max() <= 1e-8 * np.abs(ref).max()
 
 
-# k_sweep_fused2's first-colour order and storage: descending z rows (1), in
-# place in the staged tile (2), both (3), every halo cell (0; the default, 16,
-# skips the halo's edges and corners)
-FUSED_VAR = {"tiled_desc": 1, "tiled_inplace": 2, "tiled_desc_inplace": 3, "tiled_all_halo": 0}
-
-
 @pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_mixed_bc", "solve_abec_48",
                                   "solve_poisson_periodic_x", "solve_abec_mo4"])
-@pytest.mark.parametrize("variant", ["tiled", "tiled_noprefetch", "tiled_v1", "tiled_v3", "march", "march_cpasync",
-                                     "tiled_desc", "tiled_inplace", "tiled_desc_inplace", "tiled_all_halo"])
+@pytest.mark.parametrize("variant", ["tiled", "tiled_noprefetch", "tiled_cpasync", "march"])
 def test_fused_sweep_matches_colour_passes(name, variant):
-    """The fused two-colour sweep (tiled with face ghosts rewritten in shared
-    memory, with or without L2 prefetch of its coefficient boxes; the earlier
-    tiled form; the tiled form with every input staged by TMA; or marching
-    along z with its planes staged by TMA or by cp.async) performs the same
-    arithmetic as two colour passes with ghost refreshes in between."""
+    """The fused two-colour sweep (tiled, staged by TMA with or without the
+    L2 prefetch of its coefficient boxes, or by cp.async; or marching along z
+    with its planes staged by TMA) performs the same arithmetic as two colour
+    passes with ghost refreshes in between."""
     c = load.load(name)["case"]
     inp = cases.inputs(c)
     march = variant.startswith("march")
-    opts = {"march_sweep": int(march), "march_min_tiles": 0, "march_tma": int(variant == "march"),
-            "fused_v2": int(variant in ("tiled", "tiled_noprefetch", "tiled_v3") or variant in FUSED_VAR),
-            "fused_v3": int(variant == "tiled_v3"), "fused_prefetch": int(variant != "tiled_noprefetch")}
-    if variant in FUSED_VAR:
-        opts["fused_var"] = FUSED_VAR[variant]
+    opts = {"march_sweep": int(march), "march_min_tiles": 0, "fused_tma": int(variant != "tiled_cpasync"),
+            "fused_prefetch": int(variant != "tiled_noprefetch")}
     p1 = helpers.make_problem(c, inp, precision="mixed", fused=False)
     p2 = helpers.make_problem(c, inp, precision="mixed", fused=True, options=opts)
     p1["mlmg"].solve(p1["sol"], p1["rhs"], 1e-10, 0)
@@ -143,18 +131,19 @@ def test_fused_sweep_matches_colour_passes(name, variant):
 
 
 @pytest.mark.parametrize("name", ["solve_abec_32", "solve_abec_48", "solve_abec_mixed_bc", "solve_poisson_periodic_x"])
-@pytest.mark.parametrize("var", [1, 2, 3, 6, 14, 16, 18])
-def test_fused_sweep_order_variants_bitwise(name, var):
-    """The first colour's row order and its in-place storage change no
-    arithmetic: the solution is bit for bit the default sweep's."""
+def test_fused_sweep_staging_bitwise(name):
+    """Staging a tile by one TMA tensor load or by cp.async copies, with or
+    without the L2 prefetch, changes no arithmetic: the solution is bit for
+    bit the same."""
     c = load.load(name)["case"]
     inp = cases.inputs(c)
-    p1 = helpers.make_problem(c, inp, precision="mixed", fused=True, options={"fused_var": 0})
-    p2 = helpers.make_problem(c, inp, precision="mixed", fused=True, options={"fused_var": var})
+    p1 = helpers.make_problem(c, inp, precision="mixed", fused=True, options={"fused_tma": 0})
     p1["mlmg"].solve(p1["sol"], p1["rhs"], 1e-10, 0)
-    p2["mlmg"].solve(p2["sol"], p2["rhs"], 1e-10, 0)
-    assert p1["mlmg"].getNumIters() == p2["mlmg"].getNumIters()
-    assert np.array_equal(helpers.solution(p1, c), helpers.solution(p2, c))
+    for opts in ({"fused_tma": 1, "fused_prefetch": 0}, {"fused_tma": 1, "fused_prefetch": 1}):
+        p2 = helpers.make_problem(c, inp, precision="mixed", fused=True, options=opts)
+        p2["mlmg"].solve(p2["sol"], p2["rhs"], 1e-10, 0)
+        assert p1["mlmg"].getNumIters() == p2["mlmg"].getNumIters()
+        assert np.array_equal(helpers.solution(p1, c), helpers.solution(p2, c))
 
 
 @pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_48", "solve_abec_mixed_bc",
