@@ -20,16 +20,28 @@ namespace {
 
 thread_local std::string g_err;
 std::atomic<long long> g_launches{0};
-cudaStream_t g_stream = nullptr;
+constexpr int kMaxDevices = 256;
+cudaStream_t g_stream[kMaxDevices] = {};
 std::mutex g_mutex;
 
+int current_device ()
+{
+    int dev = -1;
+    MLMG_CUDA_CHECK(cudaGetDevice(&dev));
+    MLMG_REQUIRE(dev >= 0 && dev < kMaxDevices, ERR_UNSUPPORTED, "device index out of range");
+    return dev;
+}
+
+// the library's non-blocking stream on the current device (one per device,
+// created on first use with that device current)
 cudaStream_t lib_stream ()
 {
+    const int dev = current_device();
     std::lock_guard<std::mutex> lk(g_mutex);
-    if (g_stream == nullptr) {
-        MLMG_CUDA_CHECK(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+    if (g_stream[dev] == nullptr) {
+        MLMG_CUDA_CHECK(cudaStreamCreateWithFlags(&g_stream[dev], cudaStreamNonBlocking));
     }
-    return g_stream;
+    return g_stream[dev];
 }
 
 int fail (int code, const std::string& msg) { g_err = msg; return code; }
@@ -141,6 +153,7 @@ struct mlmg_geometry_s { GeomC g; };
 struct mlmg_multifab_s {
     std::vector<Box3> boxes;
     int ncomp = 1, ngrow = 0, nodal_dir = -1, prec = 8;
+    int device = 0;       // the device current when the MultiFab was made (its data lives there)
     std::vector<long long> off;
     std::vector<FabInfo> info;
     long long total = 0;
@@ -382,6 +395,7 @@ std::unique_ptr<mlmg_multifab_s> new_mf (const std::vector<Box3>& boxes, int nco
     MLMG_REQUIRE(ncomp >= 1 && ngrow >= 0 && nodal_dir >= -1 && nodal_dir <= 2, ERR_ARGS, "bad MultiFab shape");
     auto mf = std::make_unique<mlmg_multifab_s>();
     mf->boxes = boxes; mf->ncomp = ncomp; mf->ngrow = ngrow; mf->nodal_dir = nodal_dir; mf->prec = prec;
+    mf->device = current_device();
     long long off = 0;
     for (int b = 0; b < (int)boxes.size(); ++b) {
         const Box3 f = mf->fab_box(b);
@@ -790,8 +804,7 @@ constexpr size_t kNoAllocBytes = kNoAllocResultOff + 256;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 std::mutex g_noalloc_mutex;
-constexpr int kNoAllocMaxDevices = 256;
-void* g_noalloc_dptr[kNoAllocMaxDevices] = {};      // device address of the array, per device
+void* g_noalloc_dptr[kMaxDevices] = {};             // device address of the array, per device
 Box3 g_noalloc_regions[kNoAllocMaxBoxes];            // host staging of the tables
 long long g_noalloc_start[kNoAllocMaxBoxes + 1];
 
@@ -799,9 +812,7 @@ long long g_noalloc_start[kNoAllocMaxBoxes + 1];
 // device current (the array's name is only a stand-in in host code)
 char* noalloc_scratch_for_current_device ()
 {
-    int dev = -1;
-    MLMG_CUDA_CHECK(cudaGetDevice(&dev));
-    MLMG_REQUIRE(dev >= 0 && dev < kNoAllocMaxDevices, ERR_UNSUPPORTED, "device index out of range");
+    const int dev = current_device();
     if (g_noalloc_dptr[dev] == nullptr) {
         void* p = nullptr;
         MLMG_CUDA_CHECK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
@@ -823,6 +834,9 @@ int mlmg_multifab_norminf_noalloc (mlmg_multifab mf, double* out)
     MLMG_REQUIRE(nbox <= kNoAllocMaxBoxes, ERR_ARGS,
                  "mlmg_multifab_norminf_noalloc handles at most 4096 boxes; this MultiFab has " +
                  std::to_string(nbox));
+    MLMG_REQUIRE(current_device() == mf->device, ERR_ARGS,
+                 "mlmg_multifab_norminf_noalloc: make the MultiFab's device (" + std::to_string(mf->device) +
+                 ") current before the call");
     std::lock_guard<std::mutex> lk(g_noalloc_mutex);
     char* base = noalloc_scratch_for_current_device();
     Box3* d_regions = reinterpret_cast<Box3*>(base + kNoAllocRegionsOff);

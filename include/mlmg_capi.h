@@ -111,8 +111,11 @@ int mlmg_multifab_norminf(mlmg_multifab mf, double* out);                /* vali
  * allocates nothing: its scratch (box table and result word) is a static
  * device array of 131,584 bytes that every GPU loading the library keeps
  * until the process exits.  At most 4096 boxes (more returns -1 with a
- * message).  The first call on a device looks up that array's device address
- * with the device current; make that first call before any stream capture.
+ * message).  The MultiFab's device (the one current when it was made) must
+ * be current (-1 otherwise); the library keeps one stream per device and
+ * the call runs on that device's.  The first call on a device looks up that
+ * array's device address with the device current; make that first call
+ * before any stream capture.
  * Every call shares the array, which keeps the last call's contents; each
  * call clears the result word before use, and calls that overlap on the GPU
  * race (calls through this library are serialised by a lock). */
