@@ -32,19 +32,19 @@ N = 256
 MGS = 64
 RHS_SEED, B_SEED = 1001, 2001
 TOL_REL = 1e-10
-# V-cycles the reference AMReX CPU MLMG needs on this workload (measured with
-# the reference built from its sources, 16 iterations to 2.67e-11); used to
-# scale the CPU baseline's timed sample of V-cycles to a full solve
-REF_ITERS = 16
-CPU_SAMPLE_VCYCLES = 2
+# the reference's own solve of this workload (iterations, residual history,
+# phi statistics and samples), generated by tests/golden/make_large_golden.py
+REF_FIXTURE = "large_c1_256"
 METRIC = "MLMG time-to-1e-10 residual, 256^3 variable-coefficient ABecLaplacian, mixed FP32/FP64"
 
 
 def workload_config():
+    """The workload both arms time (the implementation is described by each
+    line's own keys)."""
     return {"workload": f"MLABecLaplacian {N}^3, max_grid_size {MGS} ({(N // MGS) ** 3} boxes), log-normal b "
                         f"(contrast 1e3, 5-cell Gaussian field), Gaussian-blob RHS, Dirichlet, tol_rel 1e-10",
             "n": N, "max_grid_size": MGS, "rhs_seed": RHS_SEED, "b_seed": B_SEED,
-            "precision": "FP32 V-cycle in FP64 iterative refinement", "cuda_graph": True,
+            "agg_grid_size": 32, "con_grid_size": 32,
             "l2": "inputs larger than L2 (134 MB FP64 arrays vs 129 MB L2), no flush"}
 
 
@@ -93,12 +93,13 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = None
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.f = open(self.path, "w")
+            import tempfile
+            fd, self.path = tempfile.mkstemp(prefix="mlmg_clocks_", suffix=".csv")
+            self.f = os.fdopen(fd, "w")
             q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -119,10 +120,13 @@ class ClockSampler:
             self.f.close()
 
     def summary(self):
-        if self.proc is None or not os.path.exists(self.path):
+        if self.proc is None or self.path is None or not os.path.exists(self.path):
             return None
         rows = []
-        for line in open(self.path):
+        with open(self.path) as f:
+            lines = f.readlines()
+        os.unlink(self.path)
+        for line in lines:
             p = [x.strip() for x in line.split(",")]
             if len(p) >= 9:
                 try:
@@ -162,42 +166,183 @@ def traffic_per_launch(mode):
     return float(e["bytes_per_cell"]) * N ** 3
 
 
-def cpu_baseline(rhs, bcoef):
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def reference_fixture():
+    from tests.golden import load
+    try:
+        return load.load(REF_FIXTURE)
+    except FileNotFoundError:
+        return None
+
+
+def reference_solves(nsolve, threads):
+    """Full MLMG::solve calls of the reference's own CPU MLMG (built from its
+    sources by oracle/reference.py) on this workload: one process, the MG
+    hierarchy set up by the first call, ``nsolve`` solves from a zero initial
+    guess.  Returns the MLMG "Solve" timer of each call in ms (the first one
+    includes the setup), the run's iteration count, or None with the reason
+    when the reference cannot be built here."""
+    import re
+    import tempfile
+    from oracle import reference
+    from tests.golden import cases
+    t0 = time.perf_counter()
+    exe = reference.driver()
+    build_s = time.perf_counter() - t0
+    if exe is None:
+        return None, reference.driver.reason
+    case = dict(cases.LARGE_CASES[REF_FIXTURE], repeat=nsolve, verbose=1)
+    with tempfile.TemporaryDirectory() as d:
+        files = cases.write_inputs(case, d)
+        with open(os.path.join(d, "case.txt"), "w") as f:
+            f.write(cases.case_text(case, files))
+        out = reference.run("solve", d, threads=threads, capture=True).stdout
+        from tests.golden import load
+        res = load.parse_result(open(os.path.join(d, "result.txt")).read())
+    timers = [float(v) * 1e3 for v in re.findall(r"MLMG: Timers: Solve = ([0-9.eE+-]+)", out)]
+    if len(timers) != nsolve:        # no timer lines: the harness's wall clock around solve()
+        timers = [v * 1e3 for v in res["solve_seconds"]]
+    return {"solve_ms": timers, "niters": res["niters"], "threads": res["threads"], "build_s": build_s,
+            "final_resid_rel": res["final_resid"] / max(res["rhs_norm"], res["init_resid"])}, ""
+
+
+def port_solve(rhs, bcoef, threads):
     """The C restatement of the reference MLMG (oracle) on the host cores:
-    a sample of CPU_SAMPLE_VCYCLES V-cycles of the same solve, scaled to the
-    reference's REF_ITERS V-cycles."""
-    import multiprocessing
-    cores = multiprocessing.cpu_count()
+    one full FP64 solve of this workload, setup excluded (ms)."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
     from oracle import oracle
     from tests.golden import cases
-    c = cases._c(mode="solve", op="abec", n=(N, N, N), max_grid_size=MGS, fixed_iter=CPU_SAMPLE_VCYCLES)
+    c = cases._c(mode="solve", op="abec", n=(N, N, N), max_grid_size=MGS)
     arrays = {"sol": np.zeros((N + 2,) * 3), "rhs": rhs, "a": np.ones((N,) * 3),
               "bx": bcoef[0], "by": bcoef[1], "bz": bcoef[2]}
     _, info = oracle.solve(c, arrays)
-    per_iter = info["iter_seconds"] / CPU_SAMPLE_VCYCLES
-    return {"value": per_iter * REF_ITERS * 1e3, "unit": "ms", "cores": cores, "kind": "port",
-            "sample": f"{CPU_SAMPLE_VCYCLES} V-cycles of the {N}^3 FP64 solve (setup excluded), OpenMP on "
-                      f"{cores} threads, scaled to the reference's {REF_ITERS} V-cycles"}
+    return info["iter_seconds"] * 1e3, info["niters"]
+
+
+def cpu_baseline(rhs, bcoef):
+    """One full solve of this workload by the reference's own CPU MLMG on all
+    host cores (its "Solve" timer, setup excluded); the oracle port when the
+    reference cannot be built here."""
+    cores = os.cpu_count() or 1
+    r, why = reference_solves(2, cores)
+    if r is not None:
+        return {"value": r["solve_ms"][1], "unit": "ms", "cores": r["threads"], "kind": "reference",
+                "cpu_model": cpu_model(), "iters": r["niters"],
+                "sample": f"one full {N}^3 FP64 MLMG::solve to 1e-10 ({r['niters']} V-cycles; MLMG Solve timer, "
+                          f"setup excluded: a first solve built the hierarchy), OpenMP on {r['threads']} threads"}
+    ms, iters = port_solve(rhs, bcoef, cores)
+    return {"value": ms, "unit": "ms", "cores": cores, "kind": "port", "cpu_model": cpu_model(), "iters": iters,
+            "sample": f"one full {N}^3 FP64 solve to 1e-10 by the C restatement of the reference ({iters} "
+                      f"V-cycles, setup excluded), OpenMP on {cores} threads; the reference itself: {why}"}
 
 
 def run_reference(args, ws, rank):
+    """The reference arm: full solves of the reference's own CPU MLMG on the
+    host cores, rank 0 only (the other ranks return at once)."""
     if rank != 0:
         return
-    import multiprocessing
-    os.environ.setdefault("OMP_NUM_THREADS", str(multiprocessing.cpu_count()))
-    rhs, bcoef = make_inputs()
-    vals = []
-    for s in range(args.warmup + args.steps):
-        cb = cpu_baseline(rhs, bcoef)
-        if s >= args.warmup:
-            vals.append(cb["value"])
-    v = statistics.median(vals)
-    cb["value"] = v
+    cores = os.cpu_count() or 1
+    r, why = reference_solves(args.warmup + args.steps, cores)
+    extra = {}
+    if r is not None:
+        timed = r["solve_ms"][args.warmup:]
+        steady = r["solve_ms"][1:] or r["solve_ms"]
+        extra = {"setup_ms": r["solve_ms"][0] - statistics.median(steady), "iters": r["niters"],
+                 "final_resid_rel": r["final_resid_rel"], "build_s": r["build_s"], "solve_ms_all": r["solve_ms"]}
+        kind = "reference"
+        sample = (f"{args.steps} full {N}^3 FP64 MLMG::solve calls to 1e-10 after {args.warmup} warm-up calls "
+                  f"(the first builds the MG hierarchy), MLMG Solve timer, OpenMP on {r['threads']} threads")
+        threads = r["threads"]
+        if not args.no_one_thread:
+            one, _ = reference_solves(2, 1)
+            if one is not None:
+                extra["one_thread_ms"] = one["solve_ms"][1]
+    else:
+        rhs, bcoef = make_inputs()
+        timed = [port_solve(rhs, bcoef, cores)[0] for _ in range(args.warmup + args.steps)][args.warmup:]
+        kind, threads = "port", cores
+        sample = (f"{args.steps} full {N}^3 FP64 solves by the C restatement of the reference (setup excluded), "
+                  f"OpenMP on {cores} threads; the reference itself: {why}")
+    v = statistics.median(timed)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": workload_config(),
-            "cpu_baseline": cb, "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "warmup": args.warmup, "ms_per_step": statistics.mean(timed), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": workload_config(),
+            "implementation": "the reference's CPU MLMG (FP64, OpenMP) compiled from its sources with g++ -O2",
+            "cpu_baseline": {"value": v, "unit": "ms", "cores": threads, "kind": kind, "cpu_model": cpu_model(),
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    line.update(extra)
     print(json.dumps(line), flush=True)
+
+
+def reference_parity(phi64, fp64_iters, phim):
+    """The GPU's FP64 and mixed solutions against the reference's own solve
+    of this workload (iteration count, phi statistics and 4096 seeded
+    samples; tests/test_gpu_large.py asserts the same)."""
+    g = reference_fixture()
+    if g is None:
+        return None
+    from tests.golden import cases
+    mx = float(g["phi_stats"][0])
+    idx = cases.large_sample_index(phi64.size)
+
+    def diff(phi):
+        return float(np.abs(phi.ravel()[idx] - g["phi_sample"]).max() / mx)
+    return {"reference_iters": g["result"]["niters"], "fp64_iters": fp64_iters,
+            "phi_rel_diff_fp64_vs_reference_samples": diff(phi64),
+            "phi_rel_diff_mixed_vs_reference_samples": diff(phim)}
+
+
+def bench_c0(stream, reps=5):
+    """The 64^3 constant-coefficient MLPoisson (max_grid_size 32, 8 boxes,
+    Gaussian-blob RHS seed 1000, Dirichlet), FP64 and mixed (graph, fused
+    sweeps), device time per solve from a zero initial guess."""
+    import torch
+    import amrex_gb300 as ag
+    n = 64
+    from amrex_gb300 import synth
+    domain = ag.Box((0, 0, 0), (n - 1, n - 1, n - 1))
+    ba = ag.BoxArray(domain).maxSize(32)
+    dm = ag.DistributionMapping(ba)
+    geom = ag.Geometry(domain)
+    sol = ag.MultiFab(ba, dm, 1, 1)
+    rhs = ag.MultiFab(ba, dm, 1, 0)
+    rhs.set_global(synth.gaussian_rhs(n, 1000))
+    op = ag.MLPoisson(geom, ba, dm)
+    op.setDomainBC((101,) * 3, (101,) * 3)
+    op.setLevelBC(0, None)
+    out = {"workload": "MLPoisson 64^3, max_grid_size 32 (8 boxes), Gaussian-blob RHS (seed 1000), Dirichlet, "
+                       "tol_rel 1e-10"}
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for prec in ("fp64", "mixed"):
+        m = ag.MLMG(op)
+        m.setPrecision(prec)
+        m.setGraph(True)
+        m.setFusedSmoother(prec == "mixed")
+        for _ in range(2):
+            sol.setVal(0.0)
+            m.solve(sol, rhs, TOL_REL, 0.0)
+        e0.record(stream)
+        for _ in range(reps):
+            sol.setVal(0.0)
+            m.solve(sol, rhs, TOL_REL, 0.0)
+        e1.record(stream)
+        e1.synchronize()
+        out[f"{prec}_ms"] = e0.elapsed_time(e1) / reps
+        out[f"{prec}_iters"] = m.getNumIters()
+    return out
 
 
 def _tuned_options(chosen):
@@ -464,6 +609,20 @@ def run_gb300(args, ws, rank, local):
     fp64_iters = fp64.getNumIters()
     fp64_sm = fp64.smootherStats(reset=True)
     phi64 = sol.get_global((N, N, N))
+    # the same FP64 solve with each iteration replayed as a CUDA graph (no
+    # launch overhead in the comparison)
+    fp64g = ag.MLMG(op)
+    fp64g.setPrecision("fp64")
+    fp64g.setGraph(True)
+    for _ in range(2):
+        step(fp64g)
+    e0.record(stream)
+    for _ in range(nfp):
+        step(fp64g)
+    e1.record(stream)
+    e1.synchronize()
+    fp64_graph_ms = e0.elapsed_time(e1) / nfp
+    del fp64g
 
     # --- mixed + graph: the headline
     for _ in range(args.warmup):
@@ -485,6 +644,7 @@ def run_gb300(args, ws, rank, local):
     iters = mixed.getNumIters()
     phim = sol.get_global((N, N, N))
     rel_diff = float(np.abs(phim - phi64).max() / np.abs(phi64).max())
+    ref = reference_parity(phi64, fp64_iters, phim)
 
     # --- end to end through the C ABI with host buffers (pinned, as a host
     # code would keep its input and output arrays)
@@ -514,8 +674,12 @@ def run_gb300(args, ws, rank, local):
         "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 V-cycle / f64 residual", "data": "synthetic (seeded generators, no dataset)",
         "config": workload_config(),
-        "iters": iters, "fp64_ms": fp64_ms, "fp64_iters": fp64_iters, "speedup_vs_fp64": fp64_ms / ms,
-        "phi_rel_diff_vs_fp64": rel_diff,
+        "implementation": {"precision": "FP32 V-cycles (fused two-colour sweeps) in FP64 iterative refinement",
+                           "cuda_graph": True, "fp64_comparator": "the same engine in FP64 throughout, eager "
+                           "launches (fp64_ms) and graph-replayed iterations (fp64_graph_ms)"},
+        "iters": iters, "fp64_ms": fp64_ms, "fp64_graph_ms": fp64_graph_ms, "fp64_iters": fp64_iters,
+        "speedup_vs_fp64": fp64_ms / ms, "speedup_vs_fp64_graph": fp64_graph_ms / ms,
+        "phi_rel_diff_vs_fp64": rel_diff, "reference_parity": ref,
         "roofline": {"kernel": "finest-level fused two-colour Gauss-Seidel sweep (FP32, k_sweep_fused2, TMA staging)",
                      "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -531,12 +695,11 @@ def run_gb300(args, ws, rank, local):
         "clocks": clk.summary(),
     }
     if not args.no_batch:
+        line["c0"] = bench_c0(stream)
         line["batch"] = bench_batch(stream)
         line["adjoint"] = bench_adjoint(stream)
         line["amr"] = bench_amr(stream)
     if rank == 0 and ws == 1 and not args.no_cpu:
-        import multiprocessing
-        os.environ.setdefault("OMP_NUM_THREADS", str(multiprocessing.cpu_count()))
         line["cpu_baseline"] = cpu_baseline(rhs_h, bcoef_h)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -550,6 +713,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-one-thread", action="store_true", help="reference arm: skip the 1-thread solve")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

@@ -4,7 +4,8 @@
 // tests/golden/make_golden.py and writes the reference's outputs back into it.
 //
 // Test infrastructure only: it is built by oracle/ref/Makefile into
-// oracle/_ref/ and used to generate golden fixtures and the CPU baseline.
+// oracle/_ref/<machine>/ and used to generate golden fixtures and as the
+// timed CPU baseline.
 //
 //   ref_driver <mode> <case_dir>
 //     mode = hier   : MG hierarchy box lists (per MG level)       -> hier.txt

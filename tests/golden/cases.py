@@ -97,6 +97,27 @@ CASES = {
 }
 
 
+# --- full-size solves, kept as statistics and seeded samples of phi -------
+# (make_large_golden.py): the 256^3 variable-coefficient benchmark (max grid
+# size 64) and four solves of the 64-solve batch (cube edges from
+# {32, 48, ..., 128}, max grid size 32, solve i with seeds 4001 + i: solves 0,
+# 1, 5 and 7 are 128^3, 80^3, 48^3 and 112^3; 80, 48 and 112 chop into ragged
+# boxes of 32 + 32 + 16, 32 + 16 and 32 + 32 + 32 + 16 cells)
+LARGE_CASES = {
+    "large_c1_256": _c(mode="solve", op="abec", n=(256, 256, 256), max_grid_size=64, rhs_seed=1001, b_seed=2001),
+    "large_c4_128": _c(mode="solve", op="abec", n=(128, 128, 128), max_grid_size=32, rhs_seed=4001, b_seed=4001),
+    "large_c4_80": _c(mode="solve", op="abec", n=(80, 80, 80), max_grid_size=32, rhs_seed=4002, b_seed=4002),
+    "large_c4_48": _c(mode="solve", op="abec", n=(48, 48, 48), max_grid_size=32, rhs_seed=4006, b_seed=4006),
+    "large_c4_112": _c(mode="solve", op="abec", n=(112, 112, 112), max_grid_size=32, rhs_seed=4008, b_seed=4008),
+}
+
+
+def large_sample_index(size, count=4096):
+    """seeded sample of positions into a whole-domain phi (x fastest)"""
+    rng = np.random.Generator(np.random.PCG64(7100))
+    return np.sort(rng.choice(size, size=min(count, size), replace=False))
+
+
 def sol_grown(case):
     """Initial guess (valid cells) and Dirichlet values (ghost cells) on the
     domain grown by one cell, shape (nz+2, ny+2, nx+2)."""
@@ -207,7 +228,7 @@ def case_text(case, files):
     lines = []
     for k in ("op", "n", "max_grid_size", "lobc", "hibc", "maxorder", "agg", "agg_grid_size", "con",
               "con_grid_size", "periodic", "alpha", "beta", "tol_rel", "tol_abs", "max_iter", "fixed_iter",
-              "cross", "max_fmg_iter"):
+              "cross", "max_fmg_iter", "bottom_solver", "repeat", "verbose"):
         if k in case:
             v = case[k]
             lines.append(k + " " + (" ".join(str(x) for x in v) if isinstance(v, (tuple, list)) else str(v)))

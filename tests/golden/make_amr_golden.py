@@ -1,5 +1,5 @@
 """Generate the AMR golden fixtures in this folder with the reference AMReX
-(oracle/_ref/ref_driver, built by oracle/ref/Makefile):
+(oracle/_ref/<machine>/ref_driver, built by oracle/ref/Makefile):
 
 * ``amrgrids_<name>.npz``: the grids AmrMesh::MakeNewGrids makes when every
   level tags the cells where |RHS| exceeds the 90th (or the case's
@@ -27,7 +27,9 @@ sys.path.insert(0, ROOT)
 from amrex_gb300 import synth  # noqa: E402
 from tests.golden import amr_cases  # noqa: E402
 
-DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+from oracle import reference  # noqa: E402
+
+DRIVER = reference.driver_path()
 
 
 def _run(mode, d, lines):

@@ -1,6 +1,6 @@
 """Generate the golden fixtures in this folder by running the reference AMReX
 CPU MLMG (built from the reference sources by ``oracle/ref/Makefile`` into
-``oracle/_ref/ref_driver``) on seeded synthetic inputs.
+``oracle/_ref/<machine>/ref_driver``) on seeded synthetic inputs.
 
     make -C oracle/ref -j8          # needs the reference source tree
     python tests/golden/make_golden.py [name-prefix ...]
@@ -26,7 +26,9 @@ sys.path.insert(0, ROOT)
 from amrex_gb300 import synth  # noqa: E402
 from tests.golden import cases  # noqa: E402
 
-DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+from oracle import reference  # noqa: E402
+
+DRIVER = reference.driver_path()
 
 
 def run_case(mode, case):

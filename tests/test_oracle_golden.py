@@ -76,3 +76,23 @@ def test_oracle_fluxes_match_reference(name):
         for d, k in enumerate(keys):
             ref = g[k].reshape(shapes[d])
             assert np.array_equal(out[d], ref), (mode, d, np.abs(out[d] - ref).max())
+
+
+@pytest.mark.parametrize("name", ["large_c4_48", "large_c4_80", "large_c4_112", "large_c4_128"])
+def test_solve_matches_reference_batch_shapes(name):
+    """The batch solves with ragged max-grid-size-32 boxes (48 -> 32+16,
+    80 -> 32+32+16, 112 -> 32+32+32+16) at full size: the reference's
+    iteration and bottom counts, its history, and its phi samples and
+    statistics."""
+    g = load.load(name)
+    c, r = g["case"], g["result"]
+    phi, info = oracle.solve(c, cases.inputs(c))
+    assert info["status"] == 0
+    assert info["niters"] == r["niters"]
+    assert info["cg_iters"] == r["cg_iters"]
+    np.testing.assert_allclose(info["history"], r["history"], rtol=1e-6,
+                               atol=1e-13 * max(r["rhs_norm"], r["init_resid"]))
+    flat = phi.ravel()
+    mx = float(g["phi_stats"][0])
+    assert np.abs(flat[cases.large_sample_index(flat.size)] - g["phi_sample"]).max() <= 1e-10 * mx
+    assert abs(np.abs(flat).max() - mx) <= 1e-10 * mx
