@@ -244,6 +244,11 @@ class _LinOp:
     def setMaxOrder(self, o):
         check(capi.lib().mlmg_linop_set_maxorder(self._h, int(o)))
 
+    def setCoarseFineBC(self, crse, crse_ratio):
+        """MLLinOp::setCoarseFineBC: coarse data for the coarse/fine faces of
+        a level that does not cover its domain (values taken at this call)."""
+        check(capi.lib().mlmg_linop_set_coarse_fine_bc(self._h, None if crse is None else crse._h, int(crse_ratio)))
+
     def NMGLevels(self, amrlev=0):
         return capi.lib().mlmg_linop_num_mg_levels(self._h)
 
@@ -305,6 +310,7 @@ class MLMG:
     def setBottomTolerance(self, t): self._set("mlmg_set_bottom_tolerance", float(t))
     def setBottomToleranceAbs(self, t): self._set("mlmg_set_bottom_tolerance_abs", float(t))
     def setAlwaysUseBNorm(self, f): self._set("mlmg_set_always_use_bnorm", int(f))
+    def setFinalFillBC(self, f): self._set("mlmg_set_final_fill_bc", int(f))
     def setPrecision(self, mode): self._set("mlmg_set_precision", {"fp64": 0, "mixed": 1}.get(mode, mode))
     def setGraph(self, on): self._set("mlmg_set_graph", int(bool(on)))
     def setFusedSmoother(self, on): self._set("mlmg_set_fused_smoother", int(bool(on)))
@@ -375,6 +381,13 @@ class MLMG:
         if rc != 0:
             raise MLMGError(rc, capi.lib().mlmg_last_error().decode())
         return capi.lib().mlmg_get_final_residual(self._h)
+
+    def compResidual(self, res, sol, rhs):
+        """MLMG::compResidual: res = rhs - L(sol) on every AMR level (lists
+        of one MultiFab per level, or single MultiFabs)."""
+        lists = [x if isinstance(x, (list, tuple)) else [x] for x in (res, sol, rhs)]
+        arrs = [(ctypes.c_void_p * len(v))(*[m._h for m in v]) for v in lists]
+        check(capi.lib().mlmg_comp_residual(self._h, *arrs))
 
     def apply(self, out, inp):
         outs = out if isinstance(out, (list, tuple)) else [out]

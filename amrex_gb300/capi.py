@@ -57,6 +57,7 @@ SIGNATURES = {
     "mlmg_linop_set_domain_bc": (c_int, [c_void_p, I3, I3]),
     "mlmg_linop_set_level_bc": (c_int, [c_void_p, c_int, c_void_p]),
     "mlmg_linop_set_maxorder": (c_int, [c_void_p, c_int]),
+    "mlmg_linop_set_coarse_fine_bc": (c_int, [c_void_p, c_void_p, c_int]),
     "mlmg_abeclap_set_scalars": (c_int, [c_void_p, c_double, c_double]),
     "mlmg_abeclap_set_acoeffs": (c_int, [c_void_p, c_int, c_void_p]),
     "mlmg_abeclap_set_acoeffs_const": (c_int, [c_void_p, c_int, c_double]),
@@ -79,6 +80,7 @@ SIGNATURES = {
     "mlmg_set_bottom_tolerance": (c_int, [c_void_p, c_double]),
     "mlmg_set_bottom_tolerance_abs": (c_int, [c_void_p, c_double]),
     "mlmg_set_always_use_bnorm": (c_int, [c_void_p, c_int]),
+    "mlmg_set_final_fill_bc": (c_int, [c_void_p, c_int]),
     "mlmg_set_precision": (c_int, [c_void_p, c_int]),
     "mlmg_set_graph": (c_int, [c_void_p, c_int]),
     "mlmg_set_fused_smoother": (c_int, [c_void_p, c_int]),
@@ -88,6 +90,7 @@ SIGNATURES = {
     "mlmg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_double, P(c_double)]),
     "mlmg_solve_levels": (c_int, [c_void_p, P(c_void_p), P(c_void_p), c_double, c_double, P(c_double)]),
     "mlmg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "mlmg_comp_residual": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "mlmg_get_fluxes": (c_int, [c_void_p, c_void_p, P(c_void_p)]),
     "mlmg_get_grad_solution": (c_int, [c_void_p, c_void_p, P(c_void_p)]),
     "mlmg_get_num_iters": (c_int, [c_void_p]),

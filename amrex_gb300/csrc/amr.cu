@@ -130,7 +130,9 @@ struct AmrEngine::Impl {
     RefluxCoef reflux_coef (int c);
 
     // operations
-    void solution_residual (int l, bool update, bool want_norm = false);
+    // exact: the reference's operation order (MLMGT::compResidual) even in
+    // mixed precision
+    void solution_residual (int l, bool update, bool want_norm = false, bool exact = false);
     void reflux (int c);
     void avgdown (int c, const double* fine, double* crse);
     template <typename T> void gather (int l, const T* crse);
@@ -568,7 +570,7 @@ template <> void AmrEngine::Impl::gather<float> (int l, const float* crse)
 // MLCellLinOpT::solutionResidual (AMReX_MLCellLinOp.H:1219-1236); on a fine
 // level with update, the boundary values are first refreshed from the
 // coarser level's solution (updateSolBC, :651-664)
-void AmrEngine::Impl::solution_residual (int l, bool update, bool want_norm)
+void AmrEngine::Impl::solution_residual (int l, bool update, bool want_norm, bool exact)
 {
     LevelData& Ld = L(l);
     AmrLevelData& D = lev[l];
@@ -586,7 +588,7 @@ void AmrEngine::Impl::solution_residual (int l, bool update, bool want_norm)
     }
     D.I->ghost<double>(0, Ld.sol.p, true, true, bcv);
     Engine::Impl& I = *D.I;
-    if (mixed()) {
+    if (mixed() && !exact) {
         // stencil form (D x - sum s x_nb: 8 FP64 operations per cell instead of
         // 14), with the level's max|r| by atomic max into red_out[0]
         if (want_norm) { MLMG_CUDA_CHECK(cudaMemsetAsync(I.red_out.p, 0, sizeof(double), st())); }
@@ -939,6 +941,181 @@ void AmrEngine::solve (const std::vector<const FabSet*>& sol_in, const std::vect
     float ms = 0;
     MLMG_CUDA_CHECK(cudaEventElapsedTime(&ms, M.ev0, M.ev1));
     m_last_ms = ms;
+}
+
+void AmrEngine::comp_residual (const std::vector<const FabSet*>& sol, const std::vector<const FabSet*>& rhs,
+                               const std::vector<FabSet*>& res)
+{
+    Impl& M = *m_impl;
+    const int nl = M.nl, fin = nl - 1;
+    MLMG_REQUIRE((int)sol.size() == nl && (int)rhs.size() == nl && (int)res.size() == nl, ERR_ARGS,
+                 "one res, one sol and one rhs per AMR level");
+    for (int l = 0; l < nl; ++l) {
+        LevelData& Ld = M.L(l);
+        Engine::Impl& I = *M.lev[l].I;
+        MLMG_CUDA_CHECK(cudaMemsetAsync(Ld.sol.p, 0, Ld.sol.n * sizeof(double), m_stream));
+        MLMG_CUDA_CHECK(cudaMemsetAsync(Ld.rhs.p, 0, Ld.rhs.n * sizeof(double), m_stream));
+        I.xfer(I.items_for(*sol[l], 0, 0, -1), *sol[l], Ld.sol.p, false, 0);
+        I.xfer(I.items_for(*rhs[l], 0, 0, -1), *rhs[l], Ld.rhs.p, false, 0);
+    }
+    // AMReX_MLMG.H:821-845: from the finest level down, the solution residual
+    // (fine levels with the coarse/fine values of the next coarser solution),
+    // the reflux of the finer level's fluxes and the average-down of its
+    // residual onto the covered cells
+    for (int l = fin; l >= 0; --l) {
+        M.solution_residual(l, l > 0, false, true);
+        if (l < fin) {
+            M.reflux(l);
+            M.avgdown(l, M.L(l + 1).res.p, M.L(l).res.p);
+        }
+    }
+    for (int l = 0; l < nl; ++l) {
+        Engine::Impl& I = *M.lev[l].I;
+        I.xfer(I.items_for(*res[l], 0, 0, -1), *res[l], M.L(l).res.p, false, 1);
+    }
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
+}
+
+// MLLinOpT::setCoarseFineBC (AMReX_MLLinOp.H:1427-1441) as
+// MLCellLinOpT::setLevelBC applies it at AMR level 0 (AMReX_MLCellLinOp.H:
+// 537-566): a level whose boxes do not cover its domain takes, on its
+// coarse/fine faces, Dirichlet values interpolated from the coarse data
+// (InterpBndryDataT::setBndryValues, o3, AMReX_InterpBndryData.H:158-244),
+// after the coarse FABs' valid cells (and their periodic images) are copied
+// into each fine patch's coarsened box grown by one cell
+// (BndryRegisterT::copyFrom; cells no FAB reaches hold 0).  Refinement ratio 2.
+void coarse_fine_bc_values (Engine::Impl& I, int s, const SolveSpec& S, const FabSet& crse)
+{
+    MLMG_REQUIRE(S.crse_ratio == 2, ERR_UNSUPPORTED, "coarse/fine boundary values need refinement ratio 2");
+    MLMG_REQUIRE(crse.nodal_dir < 0, ERR_ARGS, "the coarse data must be cell-centred");
+    cudaStream_t st = I.st();
+    LevelData& L0 = I.lev[0];
+    const PatchLevel& Mf = L0.meta;
+    const int p0 = Mf.solve_first_patch[s], np = Mf.solve_npatch[s];
+    const int npatch = (int)Mf.patches.size();
+    // coarse buffers (indexed by level patch; patches of other solves get none)
+    std::vector<PatchDesc> cfd(npatch);
+    long long cursor = 0;
+    for (int p = p0; p < p0 + np; ++p) {
+        const PatchDesc& P = Mf.patches[p];
+        Box3 pb;
+        for (int d = 0; d < 3; ++d) { pb.lo[d] = P.lo[d]; pb.hi[d] = P.hi[d]; }
+        const Box3 cb = coarsen(pb, 2);
+        PatchDesc& G = cfd[p];
+        for (int d = 0; d < 3; ++d) { G.lo[d] = cb.lo[d]; G.hi[d] = cb.hi[d]; }
+        G.sx = cb.len(0) + 2;
+        G.sxy = (long long)G.sx * (cb.len(1) + 2);
+        G.base = cursor + G.sxy + G.sx + 1;
+        cursor += G.sxy * (cb.len(2) + 2);
+    }
+    // the coarse FABs as patch descriptors (valid box; index of its lower
+    // corner inside the grown FAB)
+    const int nfab = (int)crse.boxes.size();
+    std::vector<PatchDesc> cdesc(std::max(nfab, 1));
+    for (int b = 0; b < nfab; ++b) {
+        const Box3& vb = crse.boxes[b];
+        const Box3 fb = grow(vb, crse.ngrow);
+        PatchDesc& G = cdesc[b];
+        for (int d = 0; d < 3; ++d) { G.lo[d] = vb.lo[d]; G.hi[d] = vb.hi[d]; }
+        G.sx = fb.len(0);
+        G.sxy = (long long)fb.len(0) * fb.len(1);
+        G.base = crse.off[b] + (long long)crse.ngrow * (G.sxy + G.sx + 1);
+    }
+    // gather tags
+    const Box3 cdom = coarsen(S.geom.domain, 2);
+    const auto cshifts = image_shifts(cdom, S.geom.periodic);
+    std::vector<CopyTag> tags;
+    std::vector<long long> start{0};
+    for (int p = p0; p < p0 + np; ++p) {
+        Box3 g;
+        for (int d = 0; d < 3; ++d) { g.lo[d] = cfd[p].lo[d] - 1; g.hi[d] = cfd[p].hi[d] + 1; }
+        for (int b = 0; b < nfab; ++b) {
+            for (const auto& sh : cshifts) {
+                const Box3 is = intersect(g, shift(crse.boxes[b], sh.data()));
+                if (!is.ok()) { continue; }
+                CopyTag t{};
+                t.dst = p; t.src = b; t.box = is;
+                for (int d = 0; d < 3; ++d) { t.shift[d] = sh[d]; }
+                tags.push_back(t);
+                start.push_back(start.back() + is.npts());
+            }
+        }
+    }
+    // coarse/fine faces and the neighbourhood flags of their ghost cells
+    const Box3 fdom = S.geom.domain;
+    const BoxLocator floc(S.levels[0].boxes);
+    auto notcov = [&] (int i, int j, int k) {
+        int c[3] = {i, j, k};
+        return wrap_cell(fdom, S.geom.periodic, c) && floc.find(c[0], c[1], c[2]) < 0;
+    };
+    std::vector<int8_t> flags(L0.bcval.n, 0);
+    std::vector<int2> faces;
+    std::vector<long long> fstart{0};
+    for (int p = p0; p < p0 + np; ++p) {
+        const PatchDesc& P = Mf.patches[p];
+        for (int f = 0; f < 6; ++f) {
+            const FaceBC& F = P.face[f];
+            const int d = f % 3;
+            if (F.on_domain && !S.geom.periodic[d]) { continue; }   // physical face: the level BC values
+            const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
+            const int g = (f >= 3) ? P.hi[d] + 1 : P.lo[d] - 1;
+            const int n1 = P.hi[t1] - P.lo[t1] + 1, n2 = P.hi[t2] - P.lo[t2] + 1;
+            faces.push_back(make_int2(p, f));
+            fstart.push_back(fstart.back() + (long long)n1 * n2);
+            for (int v2 = 0; v2 < n2; ++v2)
+            for (int v1 = 0; v1 < n1; ++v1) {
+                int c[3];
+                c[d] = g; c[t1] = P.lo[t1] + v1; c[t2] = P.lo[t2] + v2;
+                int fl = 0;
+                if (notcov(c[0], c[1], c[2])) {
+                    fl |= BF_SELF;
+                    auto nc_at = [&] (int a1, int a2) {
+                        int e[3] = {c[0], c[1], c[2]};
+                        e[t1] += a1; e[t2] += a2;
+                        return notcov(e[0], e[1], e[2]);
+                    };
+                    if (nc_at(-2, 0)) { fl |= BF_T1LO; }
+                    if (nc_at(2, 0)) { fl |= BF_T1HI; }
+                    if (nc_at(0, -2)) { fl |= BF_T2LO; }
+                    if (nc_at(0, 2)) { fl |= BF_T2HI; }
+                    if (nc_at(-2, -2) && nc_at(2, -2) && nc_at(-2, 2) && nc_at(2, 2)) { fl |= BF_CROSS; }
+                }
+                flags[(size_t)(F.bcval_off + (long long)v2 * n1 + v1)] = (int8_t)fl;
+            }
+        }
+    }
+    if (faces.empty()) { return; }
+    DevBuf<PatchDesc> d_cfd, d_cdesc;
+    DevBuf<CopyTag> d_tags;
+    DevBuf<long long> d_start, d_fstart;
+    DevBuf<int2> d_faces;
+    DevBuf<int8_t> d_flags;
+    d_cfd.upload(cfd, st);
+    d_cdesc.upload(cdesc, st);
+    d_start.upload(start, st);
+    d_faces.upload(faces, st);
+    d_fstart.upload(fstart, st);
+    d_flags.upload(flags, st);
+    if (!tags.empty()) { d_tags.upload(tags, st); }
+    const DevLevel Lc{d_cdesc.p, nullptr, nullptr, nullptr, nfab};
+    const GhostWork W{d_faces.p, d_fstart.p, (int)faces.size(), nullptr, nullptr, 0, fstart.back(), 0};
+    auto run = [&] (auto tag) {
+        using T = decltype(tag);
+        DevBuf<T> cf;
+        cf.alloc((size_t)std::max<long long>(cursor, 1));
+        cf.zero(st);
+        if (!tags.empty()) {
+            k_amr_gather<T><<<blocks_for(start.back(), 256), 256, 0, st>>>(Lc, d_cfd.p, d_tags.p, d_start.p,
+                (int)tags.size(), start.back(), static_cast<const T*>(crse.data), cf.p);
+            I.launched();
+        }
+        k_amr_bndry<T><<<blocks_for(W.nfacecells, 256), 256, 0, st>>>(L0.dl, W, d_cfd.p, cf.p, d_flags.p,
+                                                                      L0.bcval.p);
+        I.launched();
+        MLMG_CUDA_CHECK(cudaGetLastError());
+        MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+    };
+    if (crse.prec == 8) { run(double{}); } else { run(float{}); }
 }
 
 } // namespace mlmg

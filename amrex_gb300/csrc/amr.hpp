@@ -44,6 +44,13 @@ public:
     void solve (const std::vector<const FabSet*>& sol_in, const std::vector<FabSet*>& sol_out,
                 const std::vector<const FabSet*>& rhs, double tol_rel, double tol_abs);
 
+    // MLMGT::compResidual (AMReX_MLMG.H:790-856): from the finest level down,
+    // res[l] = rhs[l] - L(sol[l]) with the coarse/fine values interpolated
+    // from sol[l-1], then the reflux of level l+1's fluxes into res[l] and the
+    // average-down of res[l+1] onto the cells of level l it covers
+    void comp_residual (const std::vector<const FabSet*>& sol, const std::vector<const FabSet*>& rhs,
+                        const std::vector<FabSet*>& res);
+
     const SolveReport& report () const { return m_report; }
     EngineOptions& options () { return m_opt; }
     const EngineOptions& options () const { return m_opt; }

@@ -347,6 +347,10 @@ struct mlmg_linop_s {
     double alpha = std::nan(""), beta = std::nan("");
     std::unique_ptr<mlmg_multifab_s> acoef, bcoef[3], levelbc;
     FabSet acoef_fs, bcoef_fs[3], levelbc_fs;
+    // setCoarseFineBC: coarse data (copied at the call) and refinement ratio
+    std::unique_ptr<mlmg_multifab_s> crse_bc;
+    FabSet crse_bc_fs;
+    int crse_ratio = 0;
     int struct_version = 0, coef_version = 0;
     std::vector<LevelGrids> levels;
     // AMR levels (composite solves): level l's BoxArray, level BC values and
@@ -451,6 +455,16 @@ SolveProblem make_problem (mlmg_linop op)
         if (op->bcoef[d]) { op->bcoef_fs[d] = op->bcoef[d]->fabset(); pr.bcoef[d] = &op->bcoef_fs[d]; }
     }
     if (op->levelbc) { op->levelbc_fs = op->levelbc->fabset(); pr.levelbc = &op->levelbc_fs; }
+    // a level that does not cover its domain has coarse/fine faces: their
+    // Dirichlet values sit at 0.5 * ratio * dx, the ratio of setCoarseFineBC
+    // or 2 with zero coarse values (MLCellLinOpT::setLevelBC,
+    // AMReX_MLCellLinOp.H:537-566)
+    long long npts = 0;
+    for (const auto& b : op->boxes) { npts += b.npts(); }
+    if (npts != op->geom.domain.npts()) {
+        S.crse_ratio = op->crse_ratio > 0 ? op->crse_ratio : 2;
+        if (op->crse_bc) { op->crse_bc_fs = op->crse_bc->fabset(); pr.crse_bc = &op->crse_bc_fs; }
+    }
     return pr;
 }
 
@@ -991,6 +1005,31 @@ int mlmg_linop_set_level_bc (mlmg_linop op, int amrlev, mlmg_multifab levelbc)
     API_END
 }
 
+int mlmg_linop_set_coarse_fine_bc (mlmg_linop op, mlmg_multifab crse, int crse_ratio)
+{
+    API_BEGIN
+    MLMG_REQUIRE(op != nullptr, ERR_ARGS, "null handle");
+    MLMG_REQUIRE(op->nlev == 1, ERR_UNSUPPORTED,
+                 "coarse data for the coarse/fine boundary applies to single-level operators (AMR level 0)");
+    if (crse == nullptr) {
+        op->crse_bc.reset();
+        op->crse_ratio = 0;
+    } else {
+        MLMG_REQUIRE(crse_ratio == 2, ERR_UNSUPPORTED, "refinement ratio " + std::to_string(crse_ratio) +
+                     " is not implemented (ratio 2 is)");
+        MLMG_REQUIRE(crse->ncomp == 1 && crse->nodal_dir == -1, ERR_ARGS,
+                     "the coarse MultiFab must be single-component and cell-centred");
+        const Box3 cdom = coarsen(op->geom.domain, crse_ratio);
+        for (const auto& b : crse->boxes) {
+            MLMG_REQUIRE(intersect(b, cdom) == b, ERR_ARGS, "a coarse box lies outside the coarsened domain");
+        }
+        op->crse_bc = clone_mf(*crse);       // values are taken at this call
+        op->crse_ratio = crse_ratio;
+    }
+    ++op->struct_version;
+    API_END
+}
+
 int mlmg_linop_set_maxorder (mlmg_linop op, int maxorder)
 {
     API_BEGIN
@@ -1091,6 +1130,7 @@ SETTER(mlmg_set_bottom_max_iter, bottom_maxiter, int, v >= 1)
 SETTER(mlmg_set_bottom_tolerance, bottom_reltol, double, v > 0)
 SETTER(mlmg_set_bottom_tolerance_abs, bottom_abstol, double, true)
 SETTER(mlmg_set_always_use_bnorm, always_use_bnorm, int, true)
+SETTER(mlmg_set_final_fill_bc, final_fill_bc, int, true)
 SETTER(mlmg_set_precision, precision, int, v == 0 || v == 1)
 SETTER(mlmg_set_graph, use_graph, int, true)
 SETTER(mlmg_set_fused_smoother, fused_smoother, int, true)
@@ -1170,8 +1210,10 @@ int mlmg_solve (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, double tol_
     count_launches(e);
     s->last = e.reports()[0];
     s->last_ms = e.last_solve_ms();
-    if (sol->ngrow >= 1) {
-        // ghost cells between boxes, as the reference's final FillBoundary leaves them
+    if (sol->ngrow == 1) {
+        // ghost cells between boxes, as the reference's final FillBoundary
+        // leaves them in its aliased solution (a solution with more ghost
+        // layers keeps them, but for the first one under final_fill_bc)
         GeomC g = s->op->geom;
         fill_boundary(*sol, g);
     }
@@ -1379,6 +1421,42 @@ int mlmg_autotune (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, int vcyc
 }
 
 const char* mlmg_autotune_report (mlmg_solver s) { return s ? s->tune_report.c_str() : ""; }
+
+int mlmg_comp_residual (mlmg_solver s, const mlmg_multifab* res, const mlmg_multifab* sol, const mlmg_multifab* rhs)
+{
+    API_BEGIN
+    MLMG_REQUIRE(s && s->op && res && sol && rhs, ERR_ARGS, "null handle");
+    mlmg_linop op = s->op;
+    const int nl = op->nlev;
+    std::vector<FabSet> fx(nl), fb(nl), fr(nl);
+    std::vector<const FabSet*> px(nl), pb(nl);
+    std::vector<FabSet*> pr(nl);
+    for (int l = 0; l < nl; ++l) {
+        MLMG_REQUIRE(res[l] && sol[l] && rhs[l], ERR_ARGS, "null handle");
+        for (mlmg_multifab x : {res[l], sol[l], rhs[l]}) {
+            MLMG_REQUIRE(x->ncomp == 1 && x->nodal_dir == -1 && x->prec == 8, ERR_ARGS,
+                         "res, sol and rhs must be single-component, cell-centred and double precision");
+            MLMG_REQUIRE(x->boxes == op->level_boxes(l), ERR_ARGS, "MultiFab BoxArray differs from the level's");
+        }
+        fx[l] = sol[l]->fabset();
+        fb[l] = rhs[l]->fabset();
+        fr[l] = res[l]->fabset();
+        px[l] = &fx[l];
+        pb[l] = &fb[l];
+        pr[l] = &fr[l];
+    }
+    if (nl == 1) {
+        Engine& e = engine_for(s);
+        e.comp_residual(fx[0], fb[0], fr[0]);
+        count_launches(e);
+    } else {
+        AmrEngine& e = amr_engine_for(s);
+        e.comp_residual(px, pb, pr);
+        count_launches(e);
+    }
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(lib_stream()));
+    API_END
+}
 
 int mlmg_apply (mlmg_solver s, mlmg_multifab out, mlmg_multifab in)
 {

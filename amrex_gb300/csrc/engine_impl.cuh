@@ -219,4 +219,9 @@ struct Engine::Impl {
 
 static const dim3 kTileBlock(32, TILE_Y);
 
+// The Dirichlet values of the coarse/fine faces of solve s's level 0 when
+// its boxes do not cover the domain, interpolated from the coarse data
+// `crse` (refinement ratio 2; amr.cu)
+void coarse_fine_bc_values (Engine::Impl& I, int s, const SolveSpec& S, const FabSet& crse);
+
 } // namespace mlmg

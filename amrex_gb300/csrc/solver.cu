@@ -386,8 +386,11 @@ void Engine::Impl::build_bottom_tables ()
 // ----------------------------------------------------- user data transfer --
 std::vector<XferItem> Engine::Impl::items_for (const FabSet& fs, int s, int ghost_mode, int nodal_dir) const
 {
-    // ghost_mode 0: valid cells (nodal-extended for faces); 1: valid + the
-    // face-ghost layers that lie inside the owning patch's ghost shell
+    // ghost_mode 0: valid cells (nodal-extended for faces); 1: valid cells,
+    // the first ghost layer where it lies inside the owning patch (values of
+    // the neighbouring boxes, as FillBoundary leaves them) and the face-ghost
+    // layers on the patch's boundary (its ghost shell: boundary closures and
+    // copies from other patches)
     std::vector<XferItem> items;
     const PatchLevel& M = lev[0].meta;
     const int p0 = M.solve_first_patch[s], np = M.solve_npatch[s];
@@ -415,6 +418,12 @@ std::vector<XferItem> Engine::Impl::items_for (const FabSet& fs, int s, int ghos
         X.fsxy = (long long)fab.len(0) * fab.len(1);
         Box3 reg = vb;
         if (nodal_dir >= 0) { reg.hi[nodal_dir] += 1; }
+        if (ghost_mode == 1 && fs.ngrow >= 1 && nodal_dir < 0) {
+            const PatchDesc& P = M.patches[pid];
+            Box3 pb;
+            for (int d = 0; d < 3; ++d) { pb.lo[d] = P.lo[d]; pb.hi[d] = P.hi[d]; }
+            reg = intersect(grow(vb, 1), pb);
+        }
         X.region = reg;
         items.push_back(X);
         if (ghost_mode == 1 && fs.ngrow >= 1) {
@@ -989,6 +998,8 @@ void Engine::set_coefficients ()
             MLMG_CUDA_CHECK(cudaMemcpyAsync(L0.bcval.p, hb.data(), hb.size() * sizeof(double), cudaMemcpyHostToDevice, m_stream));
             MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
         }
+        // coarse/fine faces of a level that does not cover its domain
+        if (pr.crse_bc != nullptr) { coarse_fine_bc_values(I, s, pr.spec, *pr.crse_bc); }
     }
     restrict_coefficients();
 }
@@ -1039,6 +1050,27 @@ void Engine::apply (const FabSet& in, FabSet& out)
     }
     I.launched();
     I.xfer(I.items_for(out, 0, 0, -1), out, L0.res.p, false, 1);
+}
+
+void Engine::comp_residual (const FabSet& sol, const FabSet& rhs, FabSet& res)
+{
+    Impl& I = *m_impl;
+    MLMG_REQUIRE(I.nsolve == 1, ERR_UNSUPPORTED, "compResidual works on a single solve");
+    LevelData& L0 = I.lev[0];
+    I.xfer(I.items_for(sol, 0, 0, -1), sol, L0.sol.p, false, 0);
+    I.xfer(I.items_for(rhs, 0, 0, -1), rhs, L0.rhs.p, false, 0);
+    // MLCellLinOpT::solutionResidual (AMReX_MLCellLinOp.H:1219-1236): applyBC
+    // with the level's boundary values, Fapply, then Xpay
+    I.ghost<double>(0, L0.sol.p, true, true);
+    if (I.abec) {
+        k_residual<double, double, true><<<L0.all.ntiles, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.res.p,
+            L0.sol.p, L0.rhs.p, L0.a.p, L0.bx.p, L0.by.p, L0.bz.p, nullptr);
+    } else {
+        k_residual<double, double, false><<<L0.all.ntiles, kTileBlock, 0, m_stream>>>(L0.dl, L0.all.dev(), L0.res.p,
+            L0.sol.p, L0.rhs.p, nullptr, nullptr, nullptr, nullptr, nullptr);
+    }
+    I.launched();
+    I.xfer(I.items_for(res, 0, 0, -1), res, L0.res.p, false, 1);
 }
 
 void Engine::face_fluxes (const FabSet& phi, FabSet* const out[3], int mode)
@@ -1254,11 +1286,14 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
                         m_reports[s].final_resid, m_reports[s].final_resid / max_norm[s]);
         }
     }
-    // write back the solution: valid cells and, for one-ghost MultiFabs, the
-    // physical-boundary ghost layer left by the last residual evaluation
+    // write back the solution: valid cells and, for one-ghost MultiFabs (the
+    // reference's aliased solution) or with final_fill_bc (MLMGT::solve,
+    // AMReX_MLMG.H:515-524), the ghost layer left by the last residual
+    // evaluation
     for (int s = 0; s < ns; ++s) {
         FabSet& out = *sol_out[s];
-        I.xfer(I.items_for(out, s, out.ngrow >= 1 ? 1 : 0, -1), out, L0.sol.p, false, 1);
+        const bool ghosts = out.ngrow == 1 || (m_opt.final_fill_bc && out.ngrow >= 1);
+        I.xfer(I.items_for(out, s, ghosts ? 1 : 0, -1), out, L0.sol.p, false, 1);
     }
     MLMG_CUDA_CHECK(cudaEventSynchronize(I.ev1));
     float ms = 0;

@@ -51,6 +51,8 @@ struct EngineOptions {
     int max_fmg_iter = 0;       // F-cycles (MLMGT::mgFcycle) for the first max_fmg_iter iterations
     int transpose = 0;          // solve A^T x = rhs (homogeneous BCs): the outer residual uses A^T,
                                 // the V-cycle of A is the correction operator (adjoint solves)
+    int final_fill_bc = 0;      // MLMGT::setFinalFillBC: a solution with more than one ghost layer also
+                                // gets its first ghost layer written back
 };
 
 // Live timing of the dominant kernel (the finest-level smoother).
@@ -67,6 +69,8 @@ struct SolveProblem {           // one solve of a batch
     const FabSet* acoef = nullptr;       // cell-centred a (ABec); null = 1
     const FabSet* bcoef[3] = {nullptr, nullptr, nullptr};  // face b (ABec); null = 1
     const FabSet* levelbc = nullptr;     // Dirichlet values in its ghost cells; null = 0
+    const FabSet* crse_bc = nullptr;     // coarse data of the coarse/fine faces of a level that does not
+                                         // cover its domain (ratio spec.crse_ratio); null = 0
 };
 
 struct SolveReport {
@@ -100,6 +104,10 @@ public:
 
     // out = L(in) with inhomogeneous BCs (MLMGT::apply)
     void apply (const FabSet& in, FabSet& out);
+
+    // res = rhs - L(sol) with inhomogeneous BCs, in the reference's operation
+    // order (MLMGT::compResidual on one AMR level, AMReX_MLMG.H:790-856)
+    void comp_residual (const FabSet& sol, const FabSet& rhs, FabSet& res);
 
     // After a transposed solve (options().transpose) of a batch of one, whose
     // solution lambda solves A^T lambda = dJ/dphi: the face-gradient

@@ -145,6 +145,17 @@ int mlmg_linop_set_domain_bc(mlmg_linop op, const int lobc[3], const int hibc[3]
  * call); NULL: homogeneous */
 int mlmg_linop_set_level_bc(mlmg_linop op, int amrlev, mlmg_multifab levelbc);
 int mlmg_linop_set_maxorder(mlmg_linop op, int maxorder);
+/* MLLinOpT::setCoarseFineBC(crse, crse_ratio) (AMReX_MLLinOp.H:200-211,
+ * 1427-1441) and amrex_fi_linop_set_coarse_fine_bc (AMReX_linop_fi.cpp:31-34):
+ * a single-level operator whose boxes do not cover its domain (a fine AMR
+ * level solved on its own) takes, on its coarse/fine faces, Dirichlet values
+ * at 0.5 * crse_ratio * dx interpolated (InterpBndryData, third order) from
+ * crse, a cell-centred MultiFab over the domain coarsened by crse_ratio.  The
+ * values are taken at this call (the reference reads them at setLevelBC,
+ * which is called after this).  Without it such a level's coarse/fine values
+ * are zero at ratio 2, as in the reference.  crse_ratio 2 only (-4
+ * otherwise); crse NULL clears it; -4 on a composite operator. */
+int mlmg_linop_set_coarse_fine_bc(mlmg_linop op, mlmg_multifab crse, int crse_ratio);
 /* amrex_fi_abeclap_set_scalars / _acoeffs / _bcoeffs (AMReX_abeclaplacian_fi.cpp:20-49);
  * amrlev in 0..nlev-1, the MultiFabs on that level's BoxArray; a level whose
  * a or b is never set takes 1 */
@@ -177,6 +188,12 @@ int mlmg_set_bottom_max_iter(mlmg_solver s, int n);
 int mlmg_set_bottom_tolerance(mlmg_solver s, double t);
 int mlmg_set_bottom_tolerance_abs(mlmg_solver s, double t);
 int mlmg_set_always_use_bnorm(mlmg_solver s, int flag);
+/* MLMGT::setFinalFillBC (AMReX_MLMG.H:137, 515-524) and
+ * amrex_fi_multigrid_set_final_fill_bc (AMReX_multigrid_fi.cpp:109-112): a
+ * solution MultiFab with more than one ghost layer also receives the first
+ * ghost layer the solve's last residual evaluation filled (neighbouring boxes'
+ * values and boundary closures); a one-ghost solution always does. */
+int mlmg_set_final_fill_bc(mlmg_solver s, int flag);
 /* GB300 additions: 0 = FP64 throughout, 1 = FP32 V-cycles inside FP64
  * iterative refinement (residual, update, bottom solve and norms in FP64) */
 int mlmg_set_precision(mlmg_solver s, int mode);
@@ -214,6 +231,14 @@ int mlmg_solve(mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, double tol_r
  * a composite operator. */
 int mlmg_solve_levels(mlmg_solver s, const mlmg_multifab* sol, const mlmg_multifab* rhs, double tol_rel,
                       double tol_abs, double* final_resid);
+/* MLMGT::compResidual (AMReX_MLMG.H:790-856) and
+ * amrex_fi_multigrid_comp_residual (AMReX_multigrid_fi.cpp:53-60): res, sol
+ * and rhs hold one MultiFab per AMR level; res = rhs - L(sol) with the level
+ * BC values (fine levels: coarse/fine values from the next coarser sol), the
+ * finer level's fluxes refluxed and its residual averaged down onto the cells
+ * it covers, in the reference's FP64 operation order.  Unlike the reference
+ * (whose one-ghost sol is filled in place), sol is not modified. */
+int mlmg_comp_residual(mlmg_solver s, const mlmg_multifab* res, const mlmg_multifab* sol, const mlmg_multifab* rhs);
 /* MLMGT::apply (AMReX_MLMG.H:858-932): out = L(in) with the level BC values */
 int mlmg_apply(mlmg_solver s, mlmg_multifab out, mlmg_multifab in);
 /* MLMGT::getFluxes(a_flux, a_sol, loc) (AMReX_MLMG.H:627-655) and

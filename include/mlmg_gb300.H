@@ -257,6 +257,13 @@ public:
         detail::check(mlmg_linop_set_level_bc(m_h.get(), amrlev, levelbcdata ? levelbcdata->handle() : nullptr));
     }
     void setMaxOrder (int maxorder) { detail::check(mlmg_linop_set_maxorder(m_h.get(), maxorder)); }
+    // MLLinOpT::setCoarseFineBC (AMReX_MLLinOp.H:200-211): coarse data for the
+    // coarse/fine faces of a level that does not cover its domain (Dirichlet
+    // only; the values are taken at this call)
+    void setCoarseFineBC (const MultiFab* crse, int crse_ratio)
+    {
+        detail::check(mlmg_linop_set_coarse_fine_bc(m_h.get(), crse ? crse->handle() : nullptr, crse_ratio));
+    }
     int NAMRLevels () const { return mlmg_linop_num_amr_levels(m_h.get()); }
     int NMGLevels (int /*amrlev*/) const { return mlmg_linop_num_mg_levels(m_h.get()); }
     mlmg_linop handle () const { return m_h.get(); }
@@ -344,6 +351,7 @@ public:
     void setBottomTolerance (Real t) { guard(mlmg_set_bottom_tolerance(m_h.get(), t)); }
     void setBottomToleranceAbs (Real t) { guard(mlmg_set_bottom_tolerance_abs(m_h.get(), t)); }
     void setAlwaysUseBNorm (int f) { guard(mlmg_set_always_use_bnorm(m_h.get(), f)); }
+    void setFinalFillBC (int f) { guard(mlmg_set_final_fill_bc(m_h.get(), f)); }
     // GB300 additions: FP32 V-cycles in FP64 refinement, CUDA-graph iterations, fused sweeps
     void setMixedPrecision (bool on) { guard(mlmg_set_precision(m_h.get(), on ? 1 : 0)); }
     void setCudaGraph (bool on) { guard(mlmg_set_graph(m_h.get(), on ? 1 : 0)); }
@@ -363,6 +371,16 @@ public:
             throw error(std::string("MLMG: ") + mlmg_last_error());
         }
         return resid;
+    }
+    // MLMGT::compResidual (AMReX_MLMG.H:790-856): res = rhs - L(sol) on every AMR level
+    void compResidual (const Vector<MultiFab*>& a_res, const Vector<MultiFab*>& a_sol,
+                       const Vector<MultiFab const*>& a_rhs)
+    {
+        std::vector<mlmg_multifab> r, x, b;
+        for (MultiFab* m : a_res) { r.push_back(m->handle()); }
+        for (MultiFab* m : a_sol) { x.push_back(m->handle()); }
+        for (const MultiFab* m : a_rhs) { b.push_back(m->handle()); }
+        guard(mlmg_comp_residual(m_h.get(), r.data(), x.data(), b.data()));
     }
     // MLMGT::apply (AMReX_MLMG.H:858-932): out = L(in) with the level BC values
     void apply (const Vector<MultiFab*>& out, const Vector<MultiFab*>& in)

@@ -12,9 +12,18 @@
 //            fb     : FillBoundary on a MultiFab with 1 ghost      -> fb_out.bin
 //            apply  : MLMG::apply (out = L phi, inhomogeneous BC)  -> out.bin
 //            solve  : MLMG::solve                                  -> phi.bin, result.txt
+//                     (sol_ngrow != 1: also phi_fabs.bin, every grown FAB in box order)
 //            flux   : solve, then getFluxes / getGradSolution    -> also f[xyz].bin, g[xyz].bin
+//            resid  : MLMG::compResidual of the initial guess       -> res.bin
 //            amrgrids : AmrMesh::MakeNewGrids tagging |rhs_l| > thresh_l -> grids.txt
 //            amrsolve : composite multi-level MLPoisson / MLABecLaplacian solve -> phi_l<lev>.bin, result.txt
+//            amrresid : MLMG::compResidual over the AMR levels of the initial guess -> res_l<lev>.bin
+//
+// Single-level keys beyond the operator's: crse_ratio / crse_file / crse_mgs
+// (MLLinOp::setCoarseFineBC with a coarse MultiFab over the coarsened domain,
+// BoxArray chopped to crse_mgs, filled from a whole-coarse-domain array),
+// sol_ngrow (ghost cells of the solution MultiFab), final_fill_bc
+// (MLMG::setFinalFillBC), bottom_solver (MLMG::BottomSolver code).
 //
 // case.txt holds "key value..." lines; binary inputs are little-endian
 // float64 arrays over the whole domain, x fastest.
@@ -308,6 +317,18 @@ int run_amr (const std::string& mode, const std::string& dir)
     mlmg.setMaxIter(c.geti("max_iter", 200));
     if (c.geti("fixed_iter", 0) > 0) { mlmg.setFixedIter(c.geti("fixed_iter", 0)); }
     if (c.geti("max_fmg_iter", 0) > 0) { mlmg.setMaxFmgIter(c.geti("max_fmg_iter", 0)); }
+    if (mode == "amrresid") {
+        Vector<MultiFab> res(nlev);
+        for (int l = 0; l < nlev; ++l) { res[l].define(ba[l], dm[l], 1, 0); }
+        mlmg.compResidual(GetVecOfPtrs(res), GetVecOfPtrs(sol), GetVecOfConstPtrs(rhs));
+        for (int l = 0; l < nlev; ++l) {
+            const int gx = dom[l].length(0), gy = dom[l].length(1), gz = dom[l].length(2);
+            Global go{gx, gy, gz, 0, 0, 0, std::vector<double>((size_t)gx*gy*gz, 0.0)};
+            copy_to_global(res[l], go);
+            write_bin(dir + "/res_l" + std::to_string(l) + ".bin", go.v);
+        }
+        return 0;
+    }
     auto t0 = std::chrono::steady_clock::now();
     const Real resid = mlmg.solve(GetVecOfPtrs(sol), GetVecOfConstPtrs(rhs), c.getd("tol_rel", 1e-10),
                                   c.getd("tol_abs", 0.0));
@@ -348,7 +369,7 @@ int main (int argc, char* argv[])
         pp.add("verbose", 0);
         pp.add("signal_handling", 0);
     });
-    if (mode == "amrgrids" || mode == "amrsolve") {
+    if (mode == "amrgrids" || mode == "amrsolve" || mode == "amrresid") {
         const int rc = run_amr(mode, dir);
         amrex::Finalize();
         return rc;
@@ -418,17 +439,33 @@ int main (int argc, char* argv[])
             } else {
                 // sol holds the initial guess in its valid cells and the
                 // Dirichlet boundary values in its ghost cells
-                MultiFab sol(ba, dm, 1, 1);
+                const int sol_ngrow = c.geti("sol_ngrow", 1);
+                MultiFab sol(ba, dm, 1, sol_ngrow);
                 MultiFab rhs(ba, dm, 1, 0);
                 Global gs{nx+2, ny+2, nz+2, -1, -1, -1, {}};
                 const size_t ngs = (size_t)(nx+2)*(ny+2)*(nz+2);
                 gs.v = c.has("sol_file") ? read_bin(dir + "/" + c.gets("sol_file", ""), ngs)
                                          : std::vector<double>(ngs, 0.0);
+                sol.setVal(0.0);
                 fill_from_global(sol, gs, 1);
                 Global gr{nx, ny, nz, 0, 0, 0, {}};
                 gr.v = c.has("rhs_file") ? read_bin(dir + "/" + c.gets("rhs_file", ""), (size_t)nx*ny*nz)
                                          : std::vector<double>((size_t)nx*ny*nz, 0.0);
                 fill_from_global(rhs, gr, 0);
+                // coarse data for the coarse/fine faces of a level that does
+                // not cover its domain (set before setLevelBC, which reads it)
+                MultiFab crse;
+                if (c.geti("crse_ratio", 0) > 0) {
+                    const int r = c.geti("crse_ratio", 2);
+                    const Box cdom = amrex::coarsen(domain, r);
+                    BoxArray cba(cdom);
+                    cba.maxSize(c.geti("crse_mgs", 32));
+                    crse.define(cba, DistributionMapping(cba), 1, 0);
+                    Global gc{cdom.length(0), cdom.length(1), cdom.length(2), 0, 0, 0,
+                              read_bin(dir + "/" + c.gets("crse_file", "crse.bin"), (size_t)cdom.numPts())};
+                    fill_from_global(crse, gc, 0);
+                    linop->setCoarseFineBC(&crse, r);
+                }
                 linop->setLevelBC(0, &sol);
                 if (abec) {
                     abec->setScalars(c.getd("alpha", 1.0), c.getd("beta", 1.0));
@@ -461,7 +498,14 @@ int main (int argc, char* argv[])
                 if (c.geti("fixed_iter", 0) > 0) { mlmg.setFixedIter(c.geti("fixed_iter", 0)); }
                 mlmg.setBottomSolver(static_cast<MLMG::BottomSolver>(c.geti("bottom_solver", 2)));
                 mlmg.setBottomVerbose(0);
-                if (mode == "apply") {
+                mlmg.setFinalFillBC(c.geti("final_fill_bc", 0));
+                if (mode == "resid") {
+                    MultiFab res(ba, dm, 1, 0);
+                    mlmg.compResidual({&res}, {&sol}, {&rhs});
+                    Global go{nx, ny, nz, 0, 0, 0, std::vector<double>((size_t)nx*ny*nz)};
+                    copy_to_global(res, go);
+                    write_bin(dir + "/res.bin", go.v);
+                } else if (mode == "apply") {
                     MultiFab out(ba, dm, 1, 0);
                     mlmg.apply({&out}, {&sol});
                     Global go{nx, ny, nz, 0, 0, 0, std::vector<double>((size_t)nx*ny*nz)};
@@ -470,11 +514,11 @@ int main (int argc, char* argv[])
                 } else {
                     const int nrep = c.geti("repeat", 1);
                     std::vector<double> times;
-                    MultiFab sol0(ba, dm, 1, 1);
-                    MultiFab::Copy(sol0, sol, 0, 0, 1, 1);
+                    MultiFab sol0(ba, dm, 1, sol_ngrow);
+                    MultiFab::Copy(sol0, sol, 0, 0, 1, sol_ngrow);
                     Real resid = 0;
                     for (int r = 0; r < nrep; ++r) {
-                        MultiFab::Copy(sol, sol0, 0, 0, 1, 1);
+                        MultiFab::Copy(sol, sol0, 0, 0, 1, sol_ngrow);
                         auto t0 = std::chrono::steady_clock::now();
                         resid = mlmg.solve({&sol}, {&rhs}, c.getd("tol_rel", 1e-10), c.getd("tol_abs", 0.0));
                         auto t1 = std::chrono::steady_clock::now();
@@ -483,6 +527,14 @@ int main (int argc, char* argv[])
                     Global go{nx, ny, nz, 0, 0, 0, std::vector<double>((size_t)nx*ny*nz)};
                     copy_to_global(sol, go);
                     write_bin(dir + "/phi.bin", go.v);
+                    if (sol_ngrow != 1) {
+                        std::vector<double> fabs;
+                        for (int b = 0; b < ba.size(); ++b) {
+                            const FArrayBox& fab = sol[b];
+                            fabs.insert(fabs.end(), fab.dataPtr(), fab.dataPtr() + fab.box().numPts());
+                        }
+                        write_bin(dir + "/phi_fabs.bin", fabs);
+                    }
                     if (mode == "flux") {
                         // MLMG::getFluxes (with the solution passed explicitly) and
                         // MLMG::getGradSolution on face MultiFabs

@@ -41,6 +41,14 @@ CASES = {
                                  abec=(0.75, 1.25)),
     # four levels: two intermediate levels with their correction holds
     "c2_n16_4lev": dict(n=16, nlev=4, max_grid_size=16, rhs_seed=1002, tag_pct=95, solve="summary"),
+    # MLMG::compResidual of a non-zero initial guess with inhomogeneous
+    # Dirichlet values (no solve)
+    "c2_n16_2lev_resid": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1012, bc=True, solve=False, resid=True),
+    "c2_n32_resid": dict(n=32, nlev=3, max_grid_size=16, rhs_seed=1002, bc=True, solve=False, resid=True),
+    "c2_n16_2lev_abec_resid": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1012, abec=(0.75, 1.25), bc=True,
+                                   solve=False, resid=True),
+    "c2_n16_2lev_per_resid": dict(n=16, nlev=2, max_grid_size=8, rhs_seed=1013, periodic=(1, 1, 0), tag_pct=98,
+                                  bc=True, solve=False, resid=True),
 }
 
 

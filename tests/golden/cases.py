@@ -94,6 +94,32 @@ CASES = {
     "flux_poisson_32": _c(mode="flux", n=(32, 32, 32), max_grid_size=16, rhs_seed=1013, sol_seed=3014),
     "flux_poisson_periodic_x": _c(mode="flux", n=(32, 24, 16), max_grid_size=8, rhs_seed=1014,
                                   periodic=(1, 0, 0), lobc=(200, 101, 102), hibc=(200, 102, 101)),
+    # --- MLMG::compResidual of a random initial guess (inhomogeneous BCs) ----
+    "resid_abec_32": _c(mode="resid", op="abec", n=(32, 32, 32), max_grid_size=16, rhs_seed=1001, b_seed=2001,
+                        sol_seed=3021),
+    "resid_abec_mixed_bc": _c(mode="resid", op="abec", n=(32, 24, 16), max_grid_size=8, rhs_seed=1003,
+                              b_seed=2003, a_seed=3003, alpha=0.75, beta=1.5, lobc=(101, 102, 101),
+                              hibc=(102, 101, 101), sol_seed=3022),
+    "resid_poisson_periodic_x": _c(mode="resid", n=(32, 24, 16), max_grid_size=8, rhs_seed=1009,
+                                   periodic=(1, 0, 0), lobc=(200, 101, 102), hibc=(200, 102, 101), sol_seed=3023),
+    # --- a level that does not cover its domain: coarse/fine faces take
+    # Dirichlet values interpolated from a coarse MultiFab
+    # (MLLinOp::setCoarseFineBC, refinement ratio 2), or zero coarse values
+    # at ratio 2 when none is given
+    "cf_solve_poisson": _c(mode="solve", n=(32, 32, 32), boxes=((8, 8, 8, 23, 23, 23),), rhs_seed=1015,
+                             crse_ratio=2, crse_seed=6001, crse_mgs=8),
+    "cf_solve_abec": _c(mode="solve", op="abec", n=(32, 32, 32), rhs_seed=1016, b_seed=2016, sol_seed=3024,
+                          boxes=((0, 8, 8, 15, 23, 23), (16, 8, 8, 31, 23, 23), (0, 24, 8, 15, 31, 23)),
+                          crse_ratio=2, crse_seed=6002, crse_mgs=8),
+    "cf_uncovered_poisson": _c(mode="solve", n=(32, 32, 32), boxes=((8, 8, 8, 23, 23, 23),), rhs_seed=1015),
+    "cf_resid_abec": _c(mode="resid", op="abec", n=(32, 32, 32), rhs_seed=1016, b_seed=2016, sol_seed=3025,
+                          boxes=((0, 8, 8, 15, 23, 23), (16, 8, 8, 31, 23, 23), (0, 24, 8, 15, 31, 23)),
+                          crse_ratio=2, crse_seed=6002, crse_mgs=8),
+    # --- MLMG::setFinalFillBC with a solution of two ghost cells ----------------
+    "ffbc_solve_abec": _c(mode="solve", op="abec", n=(32, 24, 16), max_grid_size=8, rhs_seed=1003, b_seed=2003,
+                          sol_seed=3026, lobc=(101, 102, 101), hibc=(102, 101, 101), sol_ngrow=2, final_fill_bc=1),
+    "ffbc_off_solve_abec": _c(mode="solve", op="abec", n=(32, 24, 16), max_grid_size=8, rhs_seed=1003, b_seed=2003,
+                            sol_seed=3026, lobc=(101, 102, 101), hibc=(102, 101, 101), sol_ngrow=2, final_fill_bc=0),
 }
 
 
@@ -149,6 +175,10 @@ def inputs(case):
             d["a"] = rng.uniform(0.5, 1.5, size=(nz, ny, nx))
         else:
             d["a"] = np.ones((nz, ny, nx))
+    if "crse_seed" in case:
+        # coarse data for the coarse/fine faces over the coarsened domain
+        r = case["crse_ratio"]
+        d["crse"] = synth.gaussian_rhs((nx // r, ny // r, nz // r), case["crse_seed"])
     return d
 
 
@@ -221,6 +251,9 @@ def write_inputs(case, d):
         for k in ("a", "bx", "by", "bz"):
             inp[k].astype(np.float64).tofile(os.path.join(d, k + ".bin"))
             files[k + "_file"] = k + ".bin"
+    if "crse" in inp:
+        inp["crse"].astype(np.float64).tofile(os.path.join(d, "crse.bin"))
+        files["crse_file"] = "crse.bin"
     return files
 
 
@@ -228,7 +261,8 @@ def case_text(case, files):
     lines = []
     for k in ("op", "n", "max_grid_size", "lobc", "hibc", "maxorder", "agg", "agg_grid_size", "con",
               "con_grid_size", "periodic", "alpha", "beta", "tol_rel", "tol_abs", "max_iter", "fixed_iter",
-              "cross", "max_fmg_iter", "bottom_solver", "repeat", "verbose"):
+              "cross", "max_fmg_iter", "bottom_solver", "repeat", "verbose", "crse_ratio", "crse_mgs",
+              "sol_ngrow", "final_fill_bc"):
         if k in case:
             v = case[k]
             lines.append(k + " " + (" ".join(str(x) for x in v) if isinstance(v, (tuple, list)) else str(v)))

@@ -4,6 +4,9 @@
 * ``amrgrids_<name>.npz``: the grids AmrMesh::MakeNewGrids makes when every
   level tags the cells where |RHS| exceeds the 90th (or the case's
   ``tag_pct``-th) percentile of |RHS| on that level (blocking factor 8, max_grid_size, n_error_buf 1, grid_eff 0.7);
+* ``amrresid_<name>.npz`` (cases with ``resid``): MLMG::compResidual of the
+  case's initial guess over every AMR level (solution residuals with the
+  coarse/fine boundary values, reflux, average-down), packed per level;
 * ``amrsolve_<name>.npz``: the reference's composite multi-level MLPoisson
   (or MLABecLaplacian) solve on those grids -- phi on every level's boxes (for the configuration-
   size case only per-level statistics and phi at seeded sample cells),
@@ -64,8 +67,6 @@ def make(name, case):
         np.savez_compressed(os.path.join(HERE, f"amrgrids_{name}.npz"), case=np.array(repr(case)),
                             grids=np.array(open(os.path.join(d, "grids.txt")).read()))
         print("wrote amrgrids", name, [len(g) for g in grids])
-        if not case.get("solve", True):
-            return
         summary = case.get("solve") == "summary"
         lines = base + [f"tol_rel {case.get('tol_rel', 1e-10)}", "tol_abs 0.0",
                         f"agg_grid_size {case.get('agg_grid_size', 32)}",
@@ -75,6 +76,18 @@ def make(name, case):
             lines += ["op abec", f"alpha {case['abec'][0]!r}", f"beta {case['abec'][1]!r}"]
         for lev, g in enumerate(grids):
             lines.append(f"boxes_l{lev} " + " ".join(str(v) for b in g for v in b))
+        if case.get("resid"):
+            # MLMG::compResidual of the initial guess over every AMR level
+            _run("amrresid", d, lines)
+            payload = {"case": np.array(repr(case)), "grids": np.array(open(os.path.join(d, "grids.txt")).read())}
+            for lev, g in enumerate(grids):
+                m = n << lev
+                res = np.fromfile(os.path.join(d, f"res_l{lev}.bin"), dtype=np.float64).reshape(m, m, m)
+                payload[f"res_l{lev}"] = amr_cases.pack_boxes(res, g)
+            np.savez_compressed(os.path.join(HERE, f"amrresid_{name}.npz"), **payload)
+            print("wrote amrresid", name)
+        if not case.get("solve", True):
+            return
         _run("amrsolve", d, lines)
         payload = {"case": np.array(repr(case)), "grids": np.array(open(os.path.join(d, "grids.txt")).read()),
                    "result": np.array(open(os.path.join(d, "result.txt")).read())}

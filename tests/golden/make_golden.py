@@ -42,7 +42,8 @@ def run_case(mode, case):
         res = os.path.join(d, "result.txt")
         if os.path.exists(res):
             out["result"] = open(res).read()
-        for name in ("phi.bin", "out.bin", "fb_out.bin", "fx.bin", "fy.bin", "fz.bin", "gx.bin", "gy.bin", "gz.bin"):
+        for name in ("phi.bin", "out.bin", "fb_out.bin", "fx.bin", "fy.bin", "fz.bin", "gx.bin", "gy.bin", "gz.bin",
+                     "res.bin", "phi_fabs.bin"):
             p = os.path.join(d, name)
             if os.path.exists(p):
                 out[name[:-4]] = np.fromfile(p, dtype=np.float64)
@@ -66,7 +67,7 @@ def main():
             payload["result"] = np.array(out["result"])
         if "hier" in out:
             payload["hier"] = np.array(out["hier"])
-        for k in ("phi", "out", "fb_out", "fx", "fy", "fz", "gx", "gy", "gz"):
+        for k in ("phi", "out", "fb_out", "fx", "fy", "fz", "gx", "gy", "gz", "res", "phi_fabs"):
             if k in out:
                 payload[k] = out[k]
         if mode == "fb":

@@ -96,3 +96,16 @@ def test_solve_matches_reference_batch_shapes(name):
     mx = float(g["phi_stats"][0])
     assert np.abs(flat[cases.large_sample_index(flat.size)] - g["phi_sample"]).max() <= 1e-10 * mx
     assert abs(np.abs(flat).max() - mx) <= 1e-10 * mx
+
+
+@pytest.mark.parametrize("name", load.names("resid_"))
+def test_comp_residual_matches_reference(name):
+    """MLMG::compResidual on one level is rhs - L(sol) with the level's
+    inhomogeneous boundary values: the oracle's apply gives the reference's
+    residual."""
+    g = load.load(name)
+    c = g["case"]
+    inp = cases.inputs(c)
+    out = oracle.apply(c, inp)
+    ref = g["res"].reshape(out.shape)
+    np.testing.assert_allclose(inp["rhs"] - out, ref, rtol=0, atol=1e-13 * np.abs(ref).max())
