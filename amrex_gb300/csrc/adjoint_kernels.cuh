@@ -136,7 +136,7 @@ k_residual_transpose (DevLevel L, Subset S, TO* __restrict__ r, const double* __
                 }
                 const double v = g[q] - row;
                 r[q] = TO(v);
-                mx = fmax(mx, fabs(v));
+                mx = max_nan(mx, fabs(v));
             }
         }
     }

@@ -872,6 +872,7 @@ void AmrEngine::solve (const std::vector<const FabSet*>& sol_in, const std::vect
     }
     // the first swap of every intermediate level's correction buffers
     // happens inside the iteration; their contents never carry over
+    M.lev[0].I->bottom_mode_init();
     const int niters = m_opt.fixed_iter ? m_opt.fixed_iter : m_opt.max_iter;
     bool converged = false;
     int graph_bslots = 1;
@@ -904,7 +905,10 @@ void AmrEngine::solve (const std::vector<const FabSet*>& sol_in, const std::vect
             MLMG_CUDA_CHECK(cudaStreamSynchronize(m_stream));
             const double fine = M.h_norm.p[0];
             R.history.push_back(fine);
-            for (int q = 0; q < I0.bslot && q < I0.nlev_max + 2; ++q) { R.cg_iters.push_back(I0.h_iters.p[q]); }
+            for (int q = 0; q < I0.bslot && q < I0.nlev_max + 2; ++q) {
+                R.cg_iters.push_back(I0.h_iters.p[q]);
+                if (I0.h_iters2.p[q] >= 0) { R.cg_iters.push_back(I0.h_iters2.p[q]); }
+            }
             R.niters++;
             R.final_resid = fine;
             if (m_opt.verbose >= 2) {

@@ -254,7 +254,7 @@ k_amr_norm (DevLevel L, Subset S, const T* __restrict__ x, const int8_t* __restr
                 const int i = c.x0 + threadIdx.x + 32 * h;
                 if (i > P.hi[0]) { continue; }
                 const long long q = cidx(P, i, j, k);
-                if (covered == nullptr || covered[q] == 0) { acc = fmax(acc, fabs((double)x[q])); }
+                if (covered == nullptr || covered[q] == 0) { acc = max_nan(acc, fabs((double)x[q])); }
             }
         }
     }

@@ -1,9 +1,11 @@
-// Bottom solve: one thread block per solve runs the whole Jacobi-
-// preconditioned BiCGStab of MLCGSolverT::solve_bicgstab
-// (AMReX_MLCGSolver.H:96-273) and the follow-up smoothing of
-// MLMGT::actualBottomSolve (AMReX_MLMG.H:1500-1610) on the solve's coarsest
-// level, with FP64 arithmetic, dot products and norms, and no host round
-// trip.  The coarsest level is tiny (2^3..8^3 cells for the benchmark
+// Bottom solve: one thread block per solve runs the whole Krylov bottom
+// solve -- the Jacobi-preconditioned BiCGStab of MLCGSolverT::solve_bicgstab
+// (AMReX_MLCGSolver.H:96-273) or the CG of MLCGSolverT::solve_cg (:275-410),
+// or one then the other (BottomSolver::bicgcg / cgbicg, with the switch to
+// the second kept for later bottom solves once it succeeds) -- and the
+// follow-up smoothing of MLMGT::actualBottomSolve (AMReX_MLMG.H:1500-1610) on
+// the solve's coarsest level, with FP64 arithmetic, dot products and norms,
+// and no host round trip.  The coarsest level is tiny (2^3..8^3 cells for the benchmark
 // configurations), so one block is the right size.  The block-level helpers
 // here are also used by the coarse-level V-cycle kernel.
 #pragma once
@@ -32,11 +34,17 @@ struct BottomJob {
     double volinv;
 };
 
+// MLMG::BottomSolver codes (AMReX_MLLinOp.H:30-31)
+enum BottomKind : int { BK_SMOOTHER = 1, BK_BICGSTAB = 2, BK_CG = 3, BK_BICGCG = 4, BK_CGBICG = 5 };
+
 struct BottomParams {
     int maxiter;
     double eps_rel, eps_abs;
     int nub, nuf;
     int smoother_only;         // bottom_solver == smoother
+    int* mode;                 // per solve: the current BottomKind (bicgcg / cgbicg become cg /
+                               // bicgstab once their second solver succeeds); null: bicgstab
+    int* iters2;               // per solve: the second solver's iterations, -1 if it did not run
 };
 
 namespace bottom_detail {
@@ -94,13 +102,15 @@ __device__ void ghost_fill (const DevLevel& L, const CopyTag* tags, int p0, int 
     __syncthreads();
 }
 
-template <bool ABEC>
+// out = A in (homogeneous BCs), divided by the diagonal (MLABecLaplacianT::
+// normalize, AMReX_MLABecLaplacian.H:1128-1168) when NORM
+template <bool ABEC, bool NORM = true>
 __device__ void apply_normalize (const BottomLevelPtrs& B, const BottomJob& J, double* out, double* in)
 {
     ghost_fill<double>(B.L, B.tags, J.p0, J.np, J.t0, J.nt, in);
     for_cells(B.L, J.p0, J.np, [&] (const PatchDesc& P, int, int, int, long long q) {
         double v = adotx_cell<double, ABEC>(P, q, in, B.a, B.bx, B.by, B.bz);
-        if constexpr (ABEC) { v /= abec_diag<double>(P, q, B.a, B.bx, B.by, B.bz); }
+        if constexpr (ABEC && NORM) { v /= abec_diag<double>(P, q, B.a, B.bx, B.by, B.bz); }
         out[q] = v;
     });
     __syncthreads();
@@ -112,7 +122,7 @@ __device__ inline double reduce (const DevLevel& L, int p0, int np, const double
     __shared__ double result;
     double acc = 0.0;
     for_cells(L, p0, np, [&] (const PatchDesc&, int, int, int, long long q) {
-        if (op == RED_MAXABS) { acc = fmax(acc, fabs(x[q])); }
+        if (op == RED_MAXABS) { acc = max_nan(acc, fabs(x[q])); }
         else if (op == RED_DOT) { acc += x[q] * y[q]; }
         else { acc += x[q]; }
     });
@@ -138,6 +148,145 @@ __device__ void smooth (const BottomLevelPtrs& B, const BottomJob& J, double* x,
     }
 }
 
+// x = 0 and the solver's work vectors p, r = 0, ghosts included
+__device__ inline void zero_work (const BottomLevelPtrs& B, const BottomJob& J)
+{
+    for (int pp = J.p0; pp < J.p0 + J.np; ++pp) {
+        const PatchDesc& P = B.L.P[pp];
+        const long long n0 = P.base - P.sxy - P.sx - XOFF;   // the patch's whole allocation
+        const long long n = P.sxy * (P.hi[2] - P.lo[2] + 3);
+        for (long long u = threadIdx.x; u < n; u += blockDim.x) {
+            B.x[n0 + u] = 0.0; B.p[n0 + u] = 0.0; B.r[n0 + u] = 0.0;
+        }
+    }
+    __syncthreads();
+}
+
+// MLCGSolverT::solve_bicgstab with a zero initial guess (AMReX_MLCGSolver.H:
+// 96-273) on right-hand side bb; returns its code, the iterations in *iters
+template <bool ABEC>
+__device__ int bicgstab (const BottomLevelPtrs& B, const BottomJob& J, const BottomParams& prm, const double* bb,
+                         int* iters)
+{
+    double *x = B.x, *p = B.p, *r = B.r, *rh = B.rh, *v = B.v, *t = B.t;
+    zero_work(B, J);
+    // r = b ; normalize ; rh = r
+    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc& P, int, int, int, long long q) {
+        double val = bb[q];
+        if constexpr (ABEC) { val /= abec_diag<double>(P, q, B.a, B.bx, B.by, B.bz); }
+        r[q] = val;
+    });
+    __syncthreads();
+    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { rh[q] = r[q]; });
+    __syncthreads();
+    double rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
+    const double rnorm0 = rnorm;
+    double rho_1 = 0, alpha = 0, omega = 0;
+    int ret = 0, iter = 1;
+    if (!(rnorm0 == 0 || rnorm0 < prm.eps_abs)) {
+        for (; iter <= prm.maxiter; ++iter) {
+            const double rho = reduce(B.L, J.p0, J.np, rh, r, RED_DOT);
+            if (rho == 0) { ret = 1; break; }
+            if (iter == 1) {
+                for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { p[q] = r[q]; });
+            } else {
+                const double beta = (rho / rho_1) * (alpha / omega);
+                for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
+                    double pv = p[q] + (-omega) * v[q];   // Saxpy
+                    p[q] = r[q] + beta * pv;              // Xpay
+                });
+            }
+            __syncthreads();
+            apply_normalize<ABEC>(B, J, v, p);
+            const double rhTv = reduce(B.L, J.p0, J.np, rh, v, RED_DOT);
+            if (rhTv != 0.0) { alpha = rho / rhTv; } else { ret = 2; break; }
+            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
+                x[q] += alpha * p[q];
+                r[q] += (-alpha) * v[q];
+            });
+            __syncthreads();
+            rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
+            if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
+            apply_normalize<ABEC>(B, J, t, r);
+            const double tt = reduce(B.L, J.p0, J.np, t, t, RED_DOT);
+            const double tr = reduce(B.L, J.p0, J.np, t, r, RED_DOT);
+            if (tt != 0.0) { omega = tr / tt; } else { ret = 3; break; }
+            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
+                x[q] += omega * r[q];
+                r[q] += (-omega) * t[q];
+            });
+            __syncthreads();
+            rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
+            if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
+            if (omega == 0) { ret = 4; break; }
+            rho_1 = rho;
+        }
+        if (ret == 0 && rnorm > prm.eps_rel * rnorm0 && rnorm > prm.eps_abs) { ret = 8; }
+        if ((ret == 0 || ret == 8) && (rnorm < rnorm0)) {
+            if (ret == 8) { ret = 9; }
+        } else {
+            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { x[q] = 0.0; });
+            __syncthreads();
+        }
+    }
+    *iters = iter;
+    return ret;
+}
+
+// MLCGSolverT::solve_cg with a zero initial guess (AMReX_MLCGSolver.H:
+// 275-410): unpreconditioned CG, q = A p with homogeneous BCs; v holds q
+template <bool ABEC>
+__device__ int conj_grad (const BottomLevelPtrs& B, const BottomJob& J, const BottomParams& prm, const double* bb,
+                          int* iters)
+{
+    double *x = B.x, *p = B.p, *r = B.r, *q = B.v;
+    zero_work(B, J);
+    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long c) { r[c] = bb[c]; });
+    __syncthreads();
+    double rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
+    const double rnorm0 = rnorm;
+    double rho_1 = 0;
+    int ret = 0, iter = 1;
+    if (rnorm0 == 0 || rnorm0 < prm.eps_abs) {
+        *iters = iter;
+        return ret;
+    }
+    for (; iter <= prm.maxiter; ++iter) {
+        const double rho = reduce(B.L, J.p0, J.np, r, r, RED_DOT);
+        if (rho == 0) { ret = 1; break; }
+        if (iter == 1) {
+            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long c) { p[c] = r[c]; });
+        } else {
+            const double beta = rho / rho_1;
+            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long c) {
+                p[c] = r[c] + beta * p[c];        // Xpay
+            });
+        }
+        __syncthreads();
+        apply_normalize<ABEC, false>(B, J, q, p);
+        const double pw = reduce(B.L, J.p0, J.np, p, q, RED_DOT);
+        double alpha;
+        if (pw != 0.0) { alpha = rho / pw; } else { ret = 1; break; }
+        for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long c) {
+            x[c] += alpha * p[c];                 // Saxpy
+            r[c] += (-alpha) * q[c];
+        });
+        __syncthreads();
+        rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
+        if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
+        rho_1 = rho;
+    }
+    if (ret == 0 && rnorm > prm.eps_rel * rnorm0 && rnorm > prm.eps_abs) { ret = 8; }
+    if ((ret == 0 || ret == 8) && (rnorm < rnorm0)) {
+        if (ret == 8) { ret = 9; }
+    } else {
+        for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long c) { x[c] = 0.0; });
+        __syncthreads();
+    }
+    *iters = iter;
+    return ret;
+}
+
 } // namespace bottom_detail
 
 // the bottom solve of one solve, executed by the calling block
@@ -146,98 +295,42 @@ __device__ void bottom_solve_block (const BottomLevelPtrs& B, const BottomJob& J
                                     int* __restrict__ out_iters, int* __restrict__ out_ret)
 {
     using namespace bottom_detail;
-    double *x = B.x, *b = B.b, *p = B.p, *r = B.r, *rh = B.rh, *v = B.v, *t = B.t;
+    double *x = B.x, *b = B.b;
     const T* bin = static_cast<const T*>(B.b_in);
     T* xout = static_cast<T*>(B.x_out);
 
-    // x = 0 (ghosts included), b = res (valid)
-    for (int pp = J.p0; pp < J.p0 + J.np; ++pp) {
-        const PatchDesc& P = B.L.P[pp];
-        const long long n0 = P.base - P.sxy - P.sx - XOFF;   // the patch's whole allocation
-        const long long n = P.sxy * (P.hi[2] - P.lo[2] + 3);
-        for (long long u = threadIdx.x; u < n; u += blockDim.x) {
-            x[n0 + u] = 0.0; p[n0 + u] = 0.0; r[n0 + u] = 0.0;
-        }
-    }
-    __syncthreads();
+    zero_work(B, J);
     for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { b[q] = (double)bin[q]; });
     __syncthreads();
 
-    int ret = 0, iter = 0;
+    int ret = 0, iter = 0, iter2 = -1;
     if (prm.smoother_only) {
         for (int i = 0; i < prm.nuf; ++i) { smooth<ABEC>(B, J, x, b); }
     } else {
-        // the solve's b, made solvable for a singular operator (a private copy)
+        // the solve's b, made solvable for a singular operator (the Krylov
+        // solvers' private copy: the smoothing after them takes the level's b)
         const double* bb = b;
         if (J.singular) {
             const double off = reduce(B.L, J.p0, J.np, b, nullptr, RED_SUM) * J.volinv;
-            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { t[q] = b[q] + (-off); });
+            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { b[q] = b[q] + (-off); });
             __syncthreads();
-            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { rh[q] = t[q]; });
-            __syncthreads();
-            bb = rh;   // rh is reloaded below from r, so borrow it to hold b'
         }
-        // r = b ; normalize ; rh = r
-        for_cells(B.L, J.p0, J.np, [&] (const PatchDesc& P, int, int, int, long long q) {
-            double val = bb[q];
-            if constexpr (ABEC) { val /= abec_diag<double>(P, q, B.a, B.bx, B.by, B.bz); }
-            r[q] = val;
-        });
-        __syncthreads();
-        for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { rh[q] = r[q]; });
-        __syncthreads();
-        double rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
-        const double rnorm0 = rnorm;
-        double rho_1 = 0, alpha = 0, omega = 0;
-        iter = 1;
-        if (!(rnorm0 == 0 || rnorm0 < prm.eps_abs)) {
-            for (; iter <= prm.maxiter; ++iter) {
-                const double rho = reduce(B.L, J.p0, J.np, rh, r, RED_DOT);
-                if (rho == 0) { ret = 1; break; }
-                if (iter == 1) {
-                    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { p[q] = r[q]; });
-                } else {
-                    const double beta = (rho / rho_1) * (alpha / omega);
-                    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
-                        double pv = p[q] + (-omega) * v[q];   // Saxpy
-                        p[q] = r[q] + beta * pv;              // Xpay
-                    });
-                }
-                __syncthreads();
-                apply_normalize<ABEC>(B, J, v, p);
-                const double rhTv = reduce(B.L, J.p0, J.np, rh, v, RED_DOT);
-                if (rhTv != 0.0) { alpha = rho / rhTv; } else { ret = 2; break; }
-                for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
-                    x[q] += alpha * p[q];
-                    r[q] += (-alpha) * v[q];
-                });
-                __syncthreads();
-                rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
-                if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
-                apply_normalize<ABEC>(B, J, t, r);
-                const double tt = reduce(B.L, J.p0, J.np, t, t, RED_DOT);
-                const double tr = reduce(B.L, J.p0, J.np, t, r, RED_DOT);
-                if (tt != 0.0) { omega = tr / tt; } else { ret = 3; break; }
-                for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
-                    x[q] += omega * r[q];
-                    r[q] += (-omega) * t[q];
-                });
-                __syncthreads();
-                rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
-                if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
-                if (omega == 0) { ret = 4; break; }
-                rho_1 = rho;
-            }
-            if (ret == 0 && rnorm > prm.eps_rel * rnorm0 && rnorm > prm.eps_abs) { ret = 8; }
-            if ((ret == 0 || ret == 8) && (rnorm < rnorm0)) {
-                if (ret == 8) { ret = 9; }
-            } else {
-                for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { x[q] = 0.0; });
-                __syncthreads();
-            }
+        const int kind = (prm.mode != nullptr) ? prm.mode[J.solve] : BK_BICGSTAB;
+        const bool cg_first = (kind == BK_CG || kind == BK_CGBICG);
+        ret = cg_first ? conj_grad<ABEC>(B, J, prm, bb, &iter) : bicgstab<ABEC>(B, J, prm, bb, &iter);
+        if (ret != 0 && (kind == BK_BICGCG || kind == BK_CGBICG)) {
+            // MLMGT::actualBottomSolve: the other solver from zero; once it
+            // succeeds it is used from then on
+            ret = cg_first ? bicgstab<ABEC>(B, J, prm, bb, &iter2) : conj_grad<ABEC>(B, J, prm, bb, &iter2);
+            if (ret == 0 && threadIdx.x == 0) { prm.mode[J.solve] = cg_first ? BK_BICGSTAB : BK_CG; }
         }
         if (ret != 0 && ret != 9) {
             for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { x[q] = 0.0; });
+            __syncthreads();
+        }
+        if (J.singular) {
+            // the smoother below takes the level's own b
+            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { b[q] = (double)bin[q]; });
             __syncthreads();
         }
         const int n = (ret == 0) ? prm.nub : prm.nuf;
@@ -248,6 +341,7 @@ __device__ void bottom_solve_block (const BottomLevelPtrs& B, const BottomJob& J
     if (threadIdx.x == 0) {
         out_iters[J.solve] = iter;
         out_ret[J.solve] = ret;
+        if (prm.iters2 != nullptr) { prm.iters2[J.solve] = iter2; }
     }
     __syncthreads();
 }

@@ -456,13 +456,15 @@ SolveProblem make_problem (mlmg_linop op)
     }
     if (op->levelbc) { op->levelbc_fs = op->levelbc->fabset(); pr.levelbc = &op->levelbc_fs; }
     // a level that does not cover its domain has coarse/fine faces: their
-    // Dirichlet values sit at 0.5 * ratio * dx, the ratio of setCoarseFineBC
-    // or 2 with zero coarse values (MLCellLinOpT::setLevelBC,
-    // AMReX_MLCellLinOp.H:537-566)
+    // Dirichlet values sit at 0.5 * ratio * dx with the ratio of
+    // setCoarseFineBC; without coarse data they are zero and sit on the face
+    // itself (MLCellLinOpT::setLevelBC, AMReX_MLCellLinOp.H:537-592: the
+    // location then comes from the unset coarse ratio and the default
+    // coarse/fine location 0)
     long long npts = 0;
     for (const auto& b : op->boxes) { npts += b.npts(); }
     if (npts != op->geom.domain.npts()) {
-        S.crse_ratio = op->crse_ratio > 0 ? op->crse_ratio : 2;
+        S.crse_ratio = op->crse_ratio > 0 ? op->crse_ratio : 0;
         if (op->crse_bc) { op->crse_bc_fs = op->crse_bc->fabset(); pr.crse_bc = &op->crse_bc_fs; }
     }
     return pr;
@@ -1150,6 +1152,10 @@ int mlmg_set_option (mlmg_solver s, const char* name, double value)
     else if (n == "march_sweep") { s->opt.march_sweep = value != 0.0; }
     else if (n == "fused_tma") { s->opt.fused_tma = value != 0.0; }
     else if (n == "fused_prefetch") { s->opt.fused_prefetch = value != 0.0; }
+    else if (n == "tma_wait_limit") {
+        MLMG_REQUIRE(value >= -1, ERR_ARGS, "tma_wait_limit must be >= 0 (or -1: the default bound)");
+        s->opt.tma_first_wait = (long long)value;
+    }
     else if (n == "march_tz") {
         MLMG_REQUIRE(value >= 1 && value <= 4096, ERR_ARGS, "march_tz must be in 1..4096");
         s->opt.march_tz = (int)value;
@@ -1192,8 +1198,9 @@ int mlmg_set_bottom_solver (mlmg_solver s, int which)
 {
     API_BEGIN
     MLMG_REQUIRE(s != nullptr, ERR_ARGS, "null handle");
-    MLMG_REQUIRE(which == 0 || which == 1 || which == 2, ERR_UNSUPPORTED,
-                 "bottom solver must be 0 (default), 1 (smoother) or 2 (bicgstab)");
+    MLMG_REQUIRE(which >= 0 && which <= 5, ERR_UNSUPPORTED,
+                 "bottom solver must be 0 (default), 1 (smoother), 2 (bicgstab), 3 (cg), 4 (bicgcg) or 5 (cgbicg); "
+                 "hypre and petsc are not built");
     s->opt.bottom_solver = (which == 0) ? 2 : which;
     API_END
 }

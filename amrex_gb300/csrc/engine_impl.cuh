@@ -113,9 +113,11 @@ struct Engine::Impl {
     std::vector<double> volinv0, volinv_bottom;
     DevBuf<double> partial, red_out, volinv0_d;
     DevBuf<int> active_d, bot_iters, bot_ret;
+    DevBuf<int> bot_iters2, bot_mode;   // second bottom solver's iterations; per solve BottomKind
+    int bot_mode_set = -1;       // the bottom_solver option bot_mode was last initialised from
     DevBuf<int> err_d;           // device-side error report of bounded waits (0: none)
     PinnedBuf<double> h_red;
-    PinnedBuf<int> h_iters;
+    PinnedBuf<int> h_iters, h_iters2;
     DevBuf<BottomLevelPtrs> bot_levels;
     DevBuf<BottomJob> bot_jobs;
     int njobs = 0;
@@ -191,6 +193,8 @@ struct Engine::Impl {
     template <typename T> void fcycle ();
     template <typename T> void correction_residual (int l);
     void bottom_done ();
+    BottomParams bottom_params () const;
+    void bottom_mode_init ();
     template <typename T> T* field_cor (int l);
     template <typename T> T* field_res (int l);
     template <typename T> T* field_rescor (int l);

@@ -35,8 +35,9 @@ namespace mlmg {
 // starts on a 16-byte boundary (checked; a violation is reported in *err and
 // the copy is not issued).  Cells of the box outside the patch hold whatever
 // the allocation holds there (zero past its end): the sweep reads them only
-// through the ghost layers it rewrites.  The wait is bounded; on expiry the
-// block reports ERR_TMA_TIMEOUT, waits once more (bounded) for its copy and
+// through the ghost layers it rewrites.  The wait is bounded (first_wait
+// polls); on expiry the block reports ERR_TMA_TIMEOUT, waits once more, with
+// the full bound, for its own copy so that no copy outlives the block, and
 // leaves.
 //
 // With `pf` (FS_PF_NMAP maps per patch over rhs, D, sX, sY, sZ), the block
@@ -54,7 +55,7 @@ template <bool VARC, bool TMA = false>
 __global__ void __launch_bounds__(FS_THREADS, 5)
 k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
                 const float* __restrict__ rhs, StencilPtrs Sc, const CUtensorMap* __restrict__ maps, int* err,
-                const CUtensorMap* __restrict__ pf = nullptr)
+                long long first_wait, const CUtensorMap* __restrict__ pf = nullptr)
 {
     __shared__ __align__(128) float A[FS_AZ][FS_AY][FS_AX];   // phi_in, local (x-4..x+35, y-2..y+9, z-2..z+9)
     __shared__ float N[FS_NZ][FS_NY][FS_NX];                    // first colour, local (x-1..x+32, y-1..y+8, z-1..z+8)
@@ -107,7 +108,7 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
             // coordinates of the tile grown by one: never negative
             tma::prefetch_3d(pf + (size_t)pid * FS_PF_NMAP + (tid - 32), cx, cy + 1, cz + 1);
         }
-        const bool late = !tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
+        const bool late = !tma::mbar_wait_bounded(&bar, 0, first_wait);
         if (__syncthreads_or(late)) {
             if (tid == 0) { atomicExch(err, tma::ERR_TMA_TIMEOUT); }
             tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);

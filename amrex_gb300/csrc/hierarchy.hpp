@@ -49,8 +49,10 @@ struct SolveSpec {
     double alpha = 0.0, beta = 1.0;
     int is_abec = 0;
     double dx0[3];                    // level-0 cell size (BC location of internal faces)
-    int crse_ratio = 1;               // refinement ratio to the next coarser AMR level (1 at AMR level 0):
-                                      // coarse/fine faces sit 0.5 * crse_ratio * dx0 outside the box
+    int crse_ratio = 1;               // refinement ratio to the next coarser AMR level (1 at AMR level 0;
+                                      // at AMR level 0 of a domain it does not cover, the ratio of
+                                      // setCoarseFineBC, or 0 without one): coarse/fine faces sit
+                                      // 0.5 * crse_ratio * dx0 outside the box
     int amr_fine = 0;                 // a finer AMR level: one MG level that is smoothed, never bottom-solved
 };
 

@@ -251,6 +251,9 @@ void Engine::Impl::build ()
     h_iters.alloc((size_t)nsolve * (nlev_max + 2) + 2);
     bot_iters.alloc(nsolve);
     bot_ret.alloc(nsolve);
+    bot_iters2.alloc(nsolve);
+    bot_mode.alloc(nsolve);
+    h_iters2.alloc((size_t)nsolve * (nlev_max + 2) + 2);
     active_d.alloc(nsolve);
 
     // singular operators (update_singular_flags, AMReX_MLABecLaplacian.H:714-773;
@@ -593,17 +596,22 @@ void Engine::Impl::smooth_fused (int l, int n)
         } else if (use_tma) {
             const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
             const CUtensorMap* pf = E.m_opt.fused_prefetch ? L.tm_pf.p : nullptr;
+            const long long fw = E.m_opt.tma_first_wait < 0 ? tma::WAIT_LIMIT : E.m_opt.tma_first_wait;
             if (abec) {
-                k_sweep_fused2<true, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p, pf);
+                k_sweep_fused2<true, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
+                                                                fw, pf);
             } else {
-                k_sweep_fused2<false, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p, pf);
+                k_sweep_fused2<false, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
+                                                                 fw, pf);
             }
         } else {
             const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
             if (abec) {
-                k_sweep_fused2<true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p);
+                k_sweep_fused2<true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p,
+                                                          tma::WAIT_LIMIT);
             } else {
-                k_sweep_fused2<false><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p);
+                k_sweep_fused2<false><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p,
+                                                           tma::WAIT_LIMIT);
             }
         }
         launched();
@@ -678,8 +686,29 @@ void Engine::Impl::bottom_done ()
     if (bslot < nlev_max + 2) {
         MLMG_CUDA_CHECK(cudaMemcpyAsync(h_iters.p + (size_t)bslot * nsolve, bot_iters.p, sizeof(int) * nsolve,
                                         cudaMemcpyDeviceToHost, st()));
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(h_iters2.p + (size_t)bslot * nsolve, bot_iters2.p, sizeof(int) * nsolve,
+                                        cudaMemcpyDeviceToHost, st()));
     }
     ++bslot;
+}
+
+// the per-solve bottom solver on the device: set from the option at the
+// first solve and whenever the option changes (a bicgcg / cgbicg switch made
+// by an earlier solve is kept otherwise, as MLMGT keeps its bottom_solver)
+void Engine::Impl::bottom_mode_init ()
+{
+    if (bot_mode_set == E.m_opt.bottom_solver) { return; }
+    std::vector<int> m(nsolve, E.m_opt.bottom_solver);
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(bot_mode.p, m.data(), sizeof(int) * nsolve, cudaMemcpyHostToDevice, st()));
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st()));
+    bot_mode_set = E.m_opt.bottom_solver;
+}
+
+BottomParams Engine::Impl::bottom_params () const
+{
+    const EngineOptions& o = E.m_opt;
+    return BottomParams{o.bottom_maxiter, o.bottom_reltol, o.bottom_abstol, o.nub, o.nuf,
+                        o.bottom_solver == BK_SMOOTHER ? 1 : 0, bot_mode.p, bot_iters2.p};
 }
 
 // MLMGT::mgVcycle (AMReX_MLMG.H:1306-1415) from MG level `top`, one stage per
@@ -708,7 +737,7 @@ void Engine::Impl::vcycle (int top)
         k_restrict<T><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), rescor, field_res<T>(l + 1));
         launched();
     }
-    BottomParams prm{o.bottom_maxiter, o.bottom_reltol, o.bottom_abstol, o.nub, o.nuf, o.bottom_solver == 1 ? 1 : 0};
+    const BottomParams prm = bottom_params();
     if (coarse) {
         if (abec) {
             k_coarse_vcycle<true><<<njobs, COARSE_THREADS, 0, st()>>>(coarse_lv.p, lc, bot_levels.p, bot_jobs.p, prm,
@@ -758,7 +787,7 @@ void Engine::Impl::fcycle ()
     }
     {
         const EngineOptions& o = E.m_opt;
-        BottomParams prm{o.bottom_maxiter, o.bottom_reltol, o.bottom_abstol, o.nub, o.nuf, o.bottom_solver == 1 ? 1 : 0};
+        const BottomParams prm = bottom_params();
         if (abec) {
             k_bottom<T, true><<<njobs, bot_threads, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
                                                                   bot_iters.p, bot_ret.p);
@@ -1208,6 +1237,7 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
     // residual above and makes the FP32 copy for its first V-cycle here
     if (I.mixed() && !fused_init) { I.residual0(true); }
     MLMG_CUDA_CHECK(cudaMemcpyAsync(I.active_d.p, active.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, m_stream));
+    I.bottom_mode_init();
     const int niters = m_opt.fixed_iter ? m_opt.fixed_iter : m_opt.max_iter;
     bool any_active = false;
     for (int a : active) { if (a) { any_active = true; } }
@@ -1255,6 +1285,10 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
             R.history.push_back(fine);
             for (int q = 0; q < I.bslot && q < I.nlev_max + 2; ++q) {
                 R.cg_iters.push_back(I.h_iters.p[(size_t)q * ns + s]);
+                // a bicgcg / cgbicg bottom solve that ran its second solver
+                // counts twice, as MLMGT::bottomSolveWithCG records each call
+                const int second = I.h_iters2.p[(size_t)q * ns + s];
+                if (second >= 0) { R.cg_iters.push_back(second); }
             }
             R.niters++;
             R.final_resid = fine;
@@ -1290,6 +1324,15 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
     // reference's aliased solution) or with final_fill_bc (MLMGT::solve,
     // AMReX_MLMG.H:515-524), the ghost layer left by the last residual
     // evaluation
+    bool any_ghosts = false;
+    for (int s = 0; s < ns; ++s) {
+        const FabSet& out = *sol_out[s];
+        any_ghosts = any_ghosts || out.ngrow == 1 || (m_opt.final_fill_bc && out.ngrow >= 1);
+    }
+    // the ghost layer of the final solution: boundary closures with the level
+    // BC values and copies between patches (kernels that evaluate the
+    // closures in registers leave the stored layer behind)
+    if (any_ghosts) { I.ghost<double>(0, L0.sol.p, true, true); }
     for (int s = 0; s < ns; ++s) {
         FabSet& out = *sol_out[s];
         const bool ghosts = out.ngrow == 1 || (m_opt.final_fill_bc && out.ngrow >= 1);

@@ -51,6 +51,8 @@ struct EngineOptions {
     int max_fmg_iter = 0;       // F-cycles (MLMGT::mgFcycle) for the first max_fmg_iter iterations
     int transpose = 0;          // solve A^T x = rhs (homogeneous BCs): the outer residual uses A^T,
                                 // the V-cycle of A is the correction operator (adjoint solves)
+    long long tma_first_wait = -1;  // polls of a tiled sweep's wait for its tile (-1: the default bound);
+                                // a test knob: 0 makes every wait expire, which the solve reports as -7
     int final_fill_bc = 0;      // MLMGT::setFinalFillBC: a solution with more than one ghost layer also
                                 // gets its first ghost layer written back
 };

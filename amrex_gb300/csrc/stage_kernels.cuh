@@ -8,9 +8,13 @@ namespace mlmg {
 // ------------------------------------------------------------ reductions --
 enum RedOp : int { RED_MAXABS = 0, RED_DOT = 1, RED_SUM = 2 };
 
+// maximum that keeps a NaN (fmax drops it), so that a NaN in a residual or a
+// right-hand side reaches the norm and the solve reports it
+__device__ __forceinline__ double max_nan (double a, double b) { return (a > b || a != a) ? a : b; }
+
 __device__ __forceinline__ double red_combine (int op, double a, double b)
 {
-    return (op == RED_MAXABS) ? fmax(a, b) : a + b;
+    return (op == RED_MAXABS) ? max_nan(a, b) : a + b;
 }
 
 // deterministic block reduction over TILE_THREADS (or any multiple of 32 up to 1024) threads
@@ -74,7 +78,7 @@ k_residual (DevLevel L, Subset S, TO* __restrict__ r, const T* __restrict__ x, c
                 // MF::Xpay(resid, -1, b): resid = b + (-1)*resid
                 const T v = (b != nullptr) ? T(b[q] + T(-1.0) * ax) : ax;
                 r[q] = TO(v);
-                mx = fmax(mx, fabs((double)v));
+                mx = max_nan(mx, fabs((double)v));
             }
         }
     }
@@ -270,7 +274,7 @@ k_reduce (DevLevel L, Subset S, const T* __restrict__ x, const T* __restrict__ y
                 if (i > P.hi[0]) { continue; }
                 const long long q = cidx(P, i, j, k);
                 const double xv = (double)x[q];
-                if (op == RED_MAXABS) { acc = fmax(acc, fabs(xv)); }
+                if (op == RED_MAXABS) { acc = max_nan(acc, fabs(xv)); }
                 else if (op == RED_DOT) { acc += xv * (double)y[q]; }
                 else { acc += xv; }
             }

@@ -277,7 +277,7 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
                     const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
                     mxb = (ab > mxb) ? ab : mxb;
                 } else {
-                    mx = fmax(mx, fabs((double)v));
+                    mx = max_nan(mx, fabs((double)v));
                 }
             }
         }

@@ -153,8 +153,8 @@ int mlmg_linop_set_maxorder(mlmg_linop op, int maxorder);
  * crse, a cell-centred MultiFab over the domain coarsened by crse_ratio.  The
  * values are taken at this call (the reference reads them at setLevelBC,
  * which is called after this).  Without it such a level's coarse/fine values
- * are zero at ratio 2, as in the reference.  crse_ratio 2 only (-4
- * otherwise); crse NULL clears it; -4 on a composite operator. */
+ * are zero and located on the face itself, as in the reference.  crse_ratio
+ * 2 only (-4 otherwise); crse NULL clears it; -4 on a composite operator. */
 int mlmg_linop_set_coarse_fine_bc(mlmg_linop op, mlmg_multifab crse, int crse_ratio);
 /* amrex_fi_abeclap_set_scalars / _acoeffs / _bcoeffs (AMReX_abeclaplacian_fi.cpp:20-49);
  * amrlev in 0..nlev-1, the MultiFabs on that level's BoxArray; a level whose
@@ -183,7 +183,12 @@ int mlmg_set_pre_smooth(mlmg_solver s, int n);
 int mlmg_set_post_smooth(mlmg_solver s, int n);
 int mlmg_set_final_smooth(mlmg_solver s, int n);
 int mlmg_set_bottom_smooth(mlmg_solver s, int n);
-int mlmg_set_bottom_solver(mlmg_solver s, int which);   /* 0 default, 1 smoother, 2 bicgstab */
+/* MLMG::BottomSolver codes (AMReX_MLLinOp.H:30-31; amrex_fi_multigrid_set_bottom_solver,
+ * AMReX_multigrid_fi.cpp:82-97): 0 default (bicgstab), 1 smoother, 2 bicgstab, 3 cg,
+ * 4 bicgcg, 5 cgbicg (the second solver runs when the first fails and, once it
+ * succeeds, replaces it for later bottom solves, as MLMGT::actualBottomSolve
+ * does); 6 hypre and 7 petsc return -4 */
+int mlmg_set_bottom_solver(mlmg_solver s, int which);
 int mlmg_set_bottom_max_iter(mlmg_solver s, int n);
 int mlmg_set_bottom_tolerance(mlmg_solver s, double t);
 int mlmg_set_bottom_tolerance_abs(mlmg_solver s, double t);
@@ -207,7 +212,11 @@ int mlmg_set_fused_smoother(mlmg_solver s, int on);      /* fused two-colour Gau
  * fused sweep), "march_tz" (planes per z-slab of the marching sweep),
  * "fused_tma" (0/1: the tiled fused sweep stages each tile by one TMA tensor
  * load, else by 16-byte cp.async copies; default 1), "fused_prefetch" (0/1:
- * ... and prefetches the tile's rhs and stencil boxes into L2, default 1);
+ * ... and prefetches the tile's rhs and stencil boxes into L2, default 1),
+ * "tma_wait_limit" (polls of the tiled TMA sweep's bounded wait for its tile;
+ * -1 the default bound; 0 makes every wait expire -- a test of the failure
+ * path: each block then waits, with the full bound, for its own copy, leaves,
+ * and the solve returns -7; the next solve with the default works);
  * -4 for an unknown name */
 int mlmg_set_option(mlmg_solver s, const char* name, double value);
 /* time every finest-level smoother launch with CUDA events on the library

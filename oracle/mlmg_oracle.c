@@ -765,6 +765,7 @@ typedef struct {
     int bottom_cg_iters_total;
     int singular;
     double volinv0, volinv_bottom;
+    int bottom_mode;               /* MLMGT::bottom_solver, switched by bicgcg / cgbicg */
 } Solver;
 
 static void smooth(Solver* S, int lev, MF* sol, const MF* rhs, int skip_fb) {
@@ -864,6 +865,58 @@ done:
     return ret;
 }
 
+/* MLCGSolverT::solve_cg, AMReX_MLCGSolver.H:275-410 (zero initial guess,
+ * unpreconditioned) */
+static int conj_grad(Solver* S, int lev, MF* sol, const MF* rhs, double eps_rel, double eps_abs, int maxiter,
+                     int* niter) {
+    Level* L = &S->H.lev[lev];
+    Hier* H = &S->H;
+    MF p, r, q;
+    mf_define(&p, L->nbox, L->boxes, 1, -1);
+    mf_define(&r, L->nbox, L->boxes, 0, -1);
+    mf_define(&q, L->nbox, L->boxes, 0, -1);
+    mf_axpy(L, &r, 0, rhs, 0);
+    double rnorm = mf_norminf(L, &r);
+    const double rnorm0 = rnorm;
+    int ret = 0, iter = 1;
+    double rho_1 = 0;
+    if (rnorm0 == 0 || rnorm0 < eps_abs) {
+        *niter = iter;
+        goto done;
+    }
+    for (; iter <= maxiter; ++iter) {
+        const double rho = mf_dot(L, &r, &r);
+        if (rho == 0) { ret = 1; break; }
+        if (iter == 1) {
+            mf_axpy(L, &p, 0, &r, 0);
+        } else {
+            const double beta = rho / rho_1;
+            mf_axpy(L, &p, beta, &r, 3);          /* Xpay: p = r + beta p */
+        }
+        apply_bc(H, L, &p, 0, NULL, 0, NULL);
+        fapply(H, L, &q, &p);
+        const double pw = mf_dot(L, &p, &q);
+        double alpha;
+        if (pw != 0.0) alpha = rho / pw;
+        else { ret = 1; break; }
+        mf_axpy(L, sol, alpha, &p, 2);
+        mf_axpy(L, &r, -alpha, &q, 2);
+        rnorm = mf_norminf(L, &r);
+        if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+        rho_1 = rho;
+    }
+    if (ret == 0 && rnorm > eps_rel * rnorm0 && rnorm > eps_abs) ret = 8;
+    if ((ret == 0 || ret == 8) && (rnorm < rnorm0)) {
+        if (ret == 8) ret = 9;
+    } else {
+        mf_setval(sol, 0.0);
+    }
+    *niter = iter;
+done:
+    mf_free(&p); mf_free(&r); mf_free(&q);
+    return ret;
+}
+
 /* MLMGT::actualBottomSolve, AMReX_MLMG.H:1500-1610 */
 static void bottom_solve(Solver* S) {
     int lev = S->H.nlev - 1;
@@ -886,10 +939,24 @@ static void bottom_solve(Solver* S) {
         make_solvable(S, lev, &bb);
         bottom_b = &bb; own = 1;
     }
+    /* BottomSolver: 2 bicgstab, 3 cg, 4 bicgcg, 5 cgbicg; the second solver of
+     * bicgcg / cgbicg runs when the first fails, and replaces it for good once
+     * it succeeds (AMReX_MLMG.H:1563-1597) */
+    const int kind = S->bottom_mode;
+    const int cg_first = (kind == 3 || kind == 5);
     int it = 0;
-    int ret = bicgstab(S, lev, x, bottom_b, S->o.bottom_reltol, -1.0, S->o.bottom_maxiter, &it);
+    int ret = cg_first ? conj_grad(S, lev, x, bottom_b, S->o.bottom_reltol, -1.0, S->o.bottom_maxiter, &it)
+                       : bicgstab(S, lev, x, bottom_b, S->o.bottom_reltol, -1.0, S->o.bottom_maxiter, &it);
     if (S->ncg < ORACLE_MAX_HIST) S->cg_log[S->ncg] = it;
     S->ncg++;
+    if (ret != 0 && (kind == 4 || kind == 5)) {
+        mf_setval(x, 0.0);
+        ret = cg_first ? bicgstab(S, lev, x, bottom_b, S->o.bottom_reltol, -1.0, S->o.bottom_maxiter, &it)
+                       : conj_grad(S, lev, x, bottom_b, S->o.bottom_reltol, -1.0, S->o.bottom_maxiter, &it);
+        if (S->ncg < ORACLE_MAX_HIST) S->cg_log[S->ncg] = it;
+        S->ncg++;
+        if (ret == 0) S->bottom_mode = cg_first ? 2 : 3;
+    }
     if (ret != 0 && ret != 9) mf_setval(x, 0.0);
     int n = (ret == 0) ? S->o.nub : S->o.nuf;
     for (int i = 0; i < n; ++i) smooth(S, lev, x, b, 0);
@@ -1023,6 +1090,7 @@ static int setup(Solver* S, const OracleProblem* P, const OracleOptions* o) { re
 static int setup_ratio(Solver* S, const OracleProblem* P, const OracleOptions* o, int crse_ratio) {
     memset(S, 0, sizeof(*S));
     S->o = *o;
+    S->bottom_mode = o->bottom_solver;
     Hier* H = &S->H;
     H->crse_ratio = crse_ratio;
     for (int d = 0; d < 3; ++d) {

@@ -117,7 +117,7 @@ def make_options(case):
     o = Options()
     lib().oracle_default_options(ctypes.byref(o))
     for k in ("agg", "con", "agg_grid_size", "con_grid_size", "maxorder", "max_iter", "fixed_iter",
-              "max_coarsening_level", "max_fmg_iter"):
+              "max_coarsening_level", "max_fmg_iter", "bottom_solver", "bottom_maxiter"):
         if k in case:
             setattr(o, k, int(case[k]))
     for k in ("tol_rel", "tol_abs"):

@@ -497,6 +497,7 @@ int main (int argc, char* argv[])
                 mlmg.setMaxFmgIter(c.geti("max_fmg_iter", 0));
                 if (c.geti("fixed_iter", 0) > 0) { mlmg.setFixedIter(c.geti("fixed_iter", 0)); }
                 mlmg.setBottomSolver(static_cast<MLMG::BottomSolver>(c.geti("bottom_solver", 2)));
+                mlmg.setBottomMaxIter(c.geti("bottom_maxiter", 200));
                 mlmg.setBottomVerbose(0);
                 mlmg.setFinalFillBC(c.geti("final_fill_bc", 0));
                 if (mode == "resid") {

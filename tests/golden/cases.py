@@ -85,6 +85,18 @@ CASES = {
                                        max_fmg_iter=200),
     "solve_abec_agg8_fmg": _c(mode="solve", op="abec", n=(32, 32, 32), max_grid_size=8, rhs_seed=1005,
                               b_seed=2005, agg_grid_size=8, con_grid_size=8, max_fmg_iter=200),
+    # --- bottom solvers other than BiCGStab (MLMG::BottomSolver cg, bicgcg,
+    # cgbicg): with a small bottom_maxiter the first solver of bicgcg / cgbicg
+    # fails and the second runs (cgbicg then switches to BiCGStab for good)
+    "solve_abec_cg": _c(mode="solve", op="abec", n=(32, 32, 32), max_grid_size=8, rhs_seed=1005, b_seed=2005,
+                        bottom_solver=3),
+    "solve_poisson_cg": _c(mode="solve", n=(32, 32, 32), max_grid_size=16, rhs_seed=1000, bottom_solver=3),
+    "solve_abec_cgbicg": _c(mode="solve", op="abec", n=(32, 32, 32), max_grid_size=8, rhs_seed=1005, b_seed=2005,
+                            bottom_solver=5, bottom_maxiter=4),
+    "solve_abec_bicgcg": _c(mode="solve", op="abec", n=(32, 32, 32), max_grid_size=8, rhs_seed=1005, b_seed=2005,
+                            bottom_solver=4, bottom_maxiter=3),
+    "solve_poisson_bicgcg": _c(mode="solve", n=(32, 32, 32), max_grid_size=8, rhs_seed=1005, bottom_solver=4,
+                               bottom_maxiter=2),
     # --- MLMG::getFluxes / getGradSolution after a solve ----------------------
     "flux_abec_32": _c(mode="flux", op="abec", n=(32, 32, 32), max_grid_size=16, rhs_seed=1011, b_seed=2011,
                        beta=2.0),
@@ -261,7 +273,7 @@ def case_text(case, files):
     lines = []
     for k in ("op", "n", "max_grid_size", "lobc", "hibc", "maxorder", "agg", "agg_grid_size", "con",
               "con_grid_size", "periodic", "alpha", "beta", "tol_rel", "tol_abs", "max_iter", "fixed_iter",
-              "cross", "max_fmg_iter", "bottom_solver", "repeat", "verbose", "crse_ratio", "crse_mgs",
+              "cross", "max_fmg_iter", "bottom_solver", "bottom_maxiter", "repeat", "verbose", "crse_ratio", "crse_mgs",
               "sol_ngrow", "final_fill_bc"):
         if k in case:
             v = case[k]

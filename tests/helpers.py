@@ -47,6 +47,10 @@ def make_problem(case, arrays, precision=None, graph=False, fused=False, options
         keep += [a] + faces
     mlmg = ag.MLMG(op)
     mlmg.setMaxIter(case.get("max_iter", 200))
+    if "bottom_solver" in case:
+        mlmg.setBottomSolver(case["bottom_solver"])
+    if "bottom_maxiter" in case:
+        mlmg.setBottomMaxIter(case["bottom_maxiter"])
     if case.get("fixed_iter", 0):
         mlmg.setFixedIter(case["fixed_iter"])
     if case.get("max_fmg_iter", 0):

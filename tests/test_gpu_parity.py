@@ -76,7 +76,8 @@ def test_fp64_solve_matches_reference(name):
 MIXED_CASES = ["solve_poisson_32", "solve_abec_32", "solve_abec_48", "solve_abec_mixed_bc", "solve_abec_agg8",
                "solve_poisson_c0", "solve_poisson_periodic", "solve_abec_neumann_singular", "solve_abec_mo4",
                "solve_poisson_periodic_x", "solve_abec_32_fmg", "solve_abec_mixed_bc_fmg",
-               "solve_poisson_periodic_x_fmg", "solve_poisson_c0_fmg"]
+               "solve_poisson_periodic_x_fmg", "solve_poisson_c0_fmg", "solve_abec_cg", "solve_abec_cgbicg",
+               "solve_abec_bicgcg"]
 
 
 @pytest.mark.parametrize("name", MIXED_CASES)
