@@ -82,7 +82,8 @@ MIXED_CASES = ["solve_poisson_32", "solve_abec_32", "solve_abec_48", "solve_abec
 
 @pytest.mark.parametrize("name", MIXED_CASES)
 @pytest.mark.parametrize("graph,fused,coarse,march", [(False, False, 1, 0), (True, False, 1, 0), (True, True, 1, 0),
-                                                      (False, False, 0, 0), (True, True, 0, 0), (True, True, 0, 1)])
+                                                      (False, False, 0, 0), (True, True, 0, 0), (True, True, 0, 1),
+                                                      (True, True, 0, 2)])
 def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
     """FP32 V-cycles inside FP64 refinement reach the same 1e-10 relative
     residual (the residual is evaluated in FP64); phi agrees with the
@@ -91,9 +92,12 @@ def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
     g = load.load(name)
     c = g["case"]
     opts = {"coarse_block": coarse}
-    if march:
+    if march == 1:
         # the z-marching sweep on every fused level
         opts.update(march_sweep=1, march_min_tiles=0)
+    elif march == 2:
+        # the z-march with the stencil in registers, slabs of 8 planes
+        opts.update(plane_sweep=1, plane_tz=8)
     prob = helpers.make_problem(c, cases.inputs(c), precision="mixed", graph=graph, fused=fused, options=opts)
     resid = prob["mlmg"].solve(prob["sol"], prob["rhs"], c["tol_rel"], c["tol_abs"])
     r = g["result"]
@@ -109,17 +113,20 @@ def test_mixed_solve_reaches_target(name, graph, fused, coarse, march):
 
 @pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_mixed_bc", "solve_abec_48",
                                   "solve_poisson_periodic_x", "solve_abec_mo4"])
-@pytest.mark.parametrize("variant", ["tiled", "tiled_noprefetch", "tiled_cpasync", "march"])
+@pytest.mark.parametrize("variant", ["tiled", "tiled_noprefetch", "tiled_cpasync", "march", "plane", "plane_tz3"])
 def test_fused_sweep_matches_colour_passes(name, variant):
     """The fused two-colour sweep (tiled, staged by TMA with or without the
-    L2 prefetch of its coefficient boxes, or by cp.async; or marching along z
-    with its planes staged by TMA) performs the same arithmetic as two colour
-    passes with ghost refreshes in between."""
+    L2 prefetch of its coefficient boxes, or by cp.async; marching along z
+    with its planes staged by TMA; or marching along z with the stencil in
+    registers, in slabs of 32 or 3 planes) performs the same arithmetic as
+    two colour passes with ghost refreshes in between."""
     c = load.load(name)["case"]
     inp = cases.inputs(c)
     march = variant.startswith("march")
     opts = {"march_sweep": int(march), "march_min_tiles": 0, "fused_tma": int(variant != "tiled_cpasync"),
             "fused_prefetch": int(variant != "tiled_noprefetch")}
+    if variant.startswith("plane"):
+        opts.update(plane_sweep=1, plane_tz=3 if variant == "plane_tz3" else 32)
     p1 = helpers.make_problem(c, inp, precision="mixed", fused=False)
     p2 = helpers.make_problem(c, inp, precision="mixed", fused=True, options=opts)
     p1["mlmg"].solve(p1["sol"], p1["rhs"], 1e-10, 0)
