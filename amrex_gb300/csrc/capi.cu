@@ -1152,11 +1152,6 @@ int mlmg_set_option (mlmg_solver s, const char* name, double value)
     else if (n == "march_sweep") { s->opt.march_sweep = value != 0.0; }
     else if (n == "fused_tma") { s->opt.fused_tma = value != 0.0; }
     else if (n == "fused_prefetch") { s->opt.fused_prefetch = value != 0.0; }
-    else if (n == "plane_sweep") { s->opt.plane_sweep = value != 0.0; }
-    else if (n == "plane_tz") {
-        MLMG_REQUIRE(value >= 1 && value <= 4096, ERR_ARGS, "plane_tz must be in 1..4096");
-        s->opt.plane_tz = (int)value;
-    }
     else if (n == "tma_wait_limit") {
         MLMG_REQUIRE(value >= -1, ERR_ARGS, "tma_wait_limit must be >= 0 (or -1: the default bound)");
         s->opt.tma_first_wait = (long long)value;
@@ -1372,19 +1367,16 @@ int mlmg_autotune (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, int vcyc
     check_solver_mf(s, sol);
     check_solver_mf(s, rhs);
     MLMG_REQUIRE(vcycles >= 1, ERR_ARGS, "vcycles must be >= 1");
-    struct Cand { const char* name; int fused, march, tz, coarse, cells, tma, plane, ptz; };
+    struct Cand { const char* name; int fused, march, tz, coarse, cells, tma; };
     static const Cand cands[] = {
-        {"colour passes", 0, 0, 16, 0, 512, 1, 0, 32},
-        {"fused sweep, 32x8x8 tiles, TMA staging", 1, 0, 16, 0, 512, 1, 0, 32},
-        {"fused sweep, 32x8x8 tiles, cp.async staging", 1, 0, 16, 0, 512, 0, 0, 32},
-        {"fused sweep, 64x16 columns, z-slab 8", 1, 1, 8, 0, 512, 1, 0, 32},
-        {"fused sweep, 64x16 columns, z-slab 16", 1, 1, 16, 0, 512, 1, 0, 32},
-        {"fused sweep, 64x16 columns, z-slab 32", 1, 1, 32, 0, 512, 1, 0, 32},
-        {"fused sweep, 64x8 columns, stencil in registers, z-slab 16", 1, 0, 16, 0, 512, 1, 1, 16},
-        {"fused sweep, 64x8 columns, stencil in registers, z-slab 32", 1, 0, 16, 0, 512, 1, 1, 32},
-        {"fused sweep, 64x8 columns, stencil in registers, z-slab 64", 1, 0, 16, 0, 512, 1, 1, 64},
-        {"fused sweep, 32x8x8 tiles, coarse levels <= 8^3 in one block", 1, 0, 16, 1, 512, 1, 0, 32},
-        {"fused sweep, 32x8x8 tiles, coarse levels <= 16^3 in one block", 1, 0, 16, 1, 4096, 1, 0, 32},
+        {"colour passes", 0, 0, 16, 0, 512, 1},
+        {"fused sweep, 32x8x8 tiles, TMA staging", 1, 0, 16, 0, 512, 1},
+        {"fused sweep, 32x8x8 tiles, cp.async staging", 1, 0, 16, 0, 512, 0},
+        {"fused sweep, 64x16 columns, z-slab 8", 1, 1, 8, 0, 512, 1},
+        {"fused sweep, 64x16 columns, z-slab 16", 1, 1, 16, 0, 512, 1},
+        {"fused sweep, 64x16 columns, z-slab 32", 1, 1, 32, 0, 512, 1},
+        {"fused sweep, 32x8x8 tiles, coarse levels <= 8^3 in one block", 1, 0, 16, 1, 512, 1},
+        {"fused sweep, 32x8x8 tiles, coarse levels <= 16^3 in one block", 1, 0, 16, 1, 4096, 1},
     };
     const EngineOptions saved = s->opt;
     auto scratch = clone_mf(*sol);
@@ -1402,8 +1394,6 @@ int mlmg_autotune (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, int vcyc
         s->opt.coarse_block = cands[c].coarse;
         s->opt.coarse_cells = cands[c].cells;
         s->opt.fused_tma = cands[c].tma;
-        s->opt.plane_sweep = cands[c].plane;
-        s->opt.plane_tz = cands[c].ptz;
         s->opt.fixed_iter = vcycles;
         s->eng.reset();
         Engine& e = engine_for(s);
@@ -1429,8 +1419,6 @@ int mlmg_autotune (mlmg_solver s, mlmg_multifab sol, mlmg_multifab rhs, int vcyc
         s->opt.coarse_block = cands[bi].coarse;
         s->opt.coarse_cells = cands[bi].cells;
         s->opt.fused_tma = cands[bi].tma;
-        s->opt.plane_sweep = cands[bi].plane;
-        s->opt.plane_tz = cands[bi].ptz;
     }
     s->eng.reset();
     report += std::string("chosen: ") + cands[bi].name + "\n";

@@ -9,7 +9,6 @@
 #include "fused_sweep.cuh"
 #include "fused_sweep2.cuh"
 #include "march_sweep.cuh"
-#include "plane_sweep.cuh"
 #include "coarse_vcycle.cuh"
 #include "adjoint_kernels.cuh"
 #include "flux_kernels.cuh"
@@ -90,9 +89,6 @@ struct LevelData {
     DevBuf<CUtensorMap> tm_m;         // per patch: MT_NMAP plane maps of the TMA z-march
     bool march = false;           // fused sweeps by the z-marching kernel
     SubsetData mz;
-    bool plane = false;           // fused sweeps by the register-stencil z-march (plane_sweep.cuh)
-    SubsetData pz;
-    DevBuf<CUtensorMap> tm_ps;    // per patch: plane maps (72 x 12) over cor32 and cor32b
     DevBuf<float> cor32b;
     DevBuf<int> tfirst_d, tn_d;    // per-solve tag ranges (coarse-level kernel)
     // F-cycles: the solves' own boxes of this level, interpolation data for

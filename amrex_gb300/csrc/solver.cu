@@ -166,20 +166,6 @@ void Engine::Impl::build ()
             for (int q = 0; q < Z.n; ++q) { Z.h_tstart[q + 1] = Z.h_tstart[q] + march_tiles_of(M.patches[mg[q]], E.m_opt.march_tz); }
             Z.ntiles = Z.h_tstart[Z.n];
             L.march = E.m_opt.march_sweep && Z.ntiles >= E.m_opt.march_min_tiles;
-            // the register-stencil z-march
-            L.plane = E.m_opt.plane_sweep && !L.march;
-            if (L.plane) {
-                SubsetData& Q = L.pz;
-                Q.h_plist = mg;
-                Q.n = (int)mg.size();
-                Q.h_tstart.assign(Q.n + 1, 0);
-                for (int q = 0; q < Q.n; ++q) {
-                    Q.h_tstart[q + 1] = Q.h_tstart[q] + plane_tiles_of(M.patches[mg[q]], E.m_opt.plane_tz);
-                }
-                Q.ntiles = Q.h_tstart[Q.n];
-                Q.plist.upload(Q.h_plist, st());
-                Q.tstart.upload(Q.h_tstart, st());
-            }
             if (L.march) {
                 Z.plist.upload(Z.h_plist, st());
                 Z.tstart.upload(Z.h_tstart, st());
@@ -210,18 +196,8 @@ void Engine::Impl::build ()
             alloc0(L.cor); if (l > 0) { alloc0(L.res); } alloc0(L.rescor);
         }
         if (L.has_bottom) { for (auto& b : L.bw) { alloc0(b); } }
-        // the register-stencil z-march's plane maps (72 x 12 floats from
-        // (x0-4, y0-2)) over cor32 and cor32b, per patch
-        if (L.plane) {
-            std::vector<CUtensorMap> tm(2 * M.patches.size());
-            for (size_t p = 0; p < M.patches.size(); ++p) {
-                tm[2 * p] = patch_tensor_map(L.cor32.p, M.patches[p], PS_RY, 1, PS_RX);
-                tm[2 * p + 1] = patch_tensor_map(L.cor32b.p, M.patches[p], PS_RY, 1, PS_RX);
-            }
-            L.tm_ps.upload(tm, st());
-        }
         // tensor maps of the fused sweep's TMA staging, one per patch of the level
-        if (L.fused && !L.march && !L.plane && E.m_opt.fused_tma) {
+        if (L.fused && !L.march && E.m_opt.fused_tma) {
             std::vector<CUtensorMap> ta(M.patches.size()), tb(M.patches.size());
             for (size_t p = 0; p < M.patches.size(); ++p) {
                 ta[p] = patch_tensor_map(L.cor32.p, M.patches[p]);
@@ -607,17 +583,7 @@ void Engine::Impl::smooth_fused (int l, int n)
     const StencilPtrs S = stencil32(l);
     for (int i = 0; i < n; ++i) {
         if (timed) { kev_record(); }
-        if (L.plane) {
-            const dim3 blk(PS_TX / 2, PS_TY);
-            const int pm = (a == L.cor32.p) ? 0 : 1;
-            if (abec) {
-                k_sweep_planes<true><<<L.pz.ntiles, blk, 0, st()>>>(L.dl, L.pz.dev(), b, L.res32.p, S, L.tm_ps.p, pm,
-                                                                    E.m_opt.plane_tz, err_d.p);
-            } else {
-                k_sweep_planes<false><<<L.pz.ntiles, blk, 0, st()>>>(L.dl, L.pz.dev(), b, L.res32.p, S, L.tm_ps.p,
-                                                                     pm, E.m_opt.plane_tz, err_d.p);
-            }
-        } else if (L.march) {
+        if (L.march) {
             const dim3 blk(MS_TX / 2, MS_TY);
             const int pm = (a == L.cor32.p) ? MT_PHI_A : MT_PHI_B;
             if (abec) {

@@ -45,9 +45,6 @@ struct EngineOptions {
                                 // (measured slower than the tiled fused sweep: 0.27 vs 0.18 ms at 256^3)
     int march_min_tiles = 304;  // ... at least this many (column, z-chunk) tiles
     int march_tz = 16;          // planes per z-slab of the marching sweep
-    int plane_sweep = 0;        // fused sweeps by the z-march with the stencil in registers
-                                // (k_sweep_planes: 64x8 columns, phi planes staged by TMA)
-    int plane_tz = 32;          // planes per z-slab of that sweep
     int fused_tma = 1;          // tiled fused sweeps stage each tile by one TMA tensor load (else 16-byte
                                 // cp.async copies)
     int fused_prefetch = 1;     // TMA sweeps also prefetch each tile's rhs and stencil boxes into L2
