@@ -16,7 +16,8 @@ from . import capi
 from .capi import MLMGError, check
 
 __all__ = ["Box", "BoxArray", "DistributionMapping", "Geometry", "MultiFab", "LPInfo", "LinOpBCType",
-           "MLPoisson", "MLABecLaplacian", "MLMG", "MLMGError", "solve_batched", "kernel_launches"]
+           "MLPoisson", "MLABecLaplacian", "MLMG", "MLMGError", "solve_batched", "kernel_launches",
+           "fp64_fma_rate", "check_bit_conversions"]
 
 
 class LinOpBCType:
@@ -328,6 +329,14 @@ class MLMG:
                                                  int(bool(reset))))
         return ms.value, n.value, b.value
 
+    def residualStats(self, reset=False):
+        """(total ms, launches, algorithmic bytes, FP64 operations per launch)
+        of the mixed path's FP64 outer residual since the last reset."""
+        ms, n, b, f = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
+        check(capi.lib().mlmg_get_residual_stats(self._h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(b),
+                                                 ctypes.byref(f), int(bool(reset))))
+        return ms.value, n.value, b.value, f.value
+
     def solve(self, sol, rhs, tol_rel, tol_abs):
         """Returns the final residual max-norm; raises MLMGError unless the
         solve converged (or ran its fixed iteration count)."""
@@ -441,3 +450,24 @@ def solve_batched(solvers, sols, rhss, tol_rel, tol_abs):
 
 def kernel_launches(reset=False):
     return capi.lib().mlmg_kernel_launches(int(bool(reset)))
+
+
+def check_bit_conversions(n, seed=1):
+    """({kind: mismatches}, {kind: first differing input}) over the device's
+    n test cases of the integer-assembled FP64 -> FP32 and FP32 -> FP64
+    conversions and |x| against the hardware's."""
+    bad = (ctypes.c_longlong * 3)()
+    first = (ctypes.c_ulonglong * 3)()
+    check(capi.lib().mlmg_check_bit_conversions(int(n), int(seed), bad, first))
+    kinds = ("f64_to_f32", "f32_to_f64", "abs")
+    return dict(zip(kinds, list(bad))), {k: hex(v) for k, v in zip(kinds, list(first)) if v}
+
+
+def fp64_fma_rate():
+    """The GPU's FP64 FMA throughput in TFLOP/s, measured by one
+    register-resident FMA kernel (the FP64 roofline of the outer residual)."""
+    v = ctypes.c_double(0.0)
+    rc = capi.lib().mlmg_fp64_fma_rate(ctypes.byref(v))
+    if rc < 0:
+        raise MLMGError(rc, capi.lib().mlmg_last_error().decode())
+    return v.value

@@ -29,6 +29,9 @@ SIGNATURES = {
     "mlmg_version": (c_int, []),
     "mlmg_stream": (c_void_p, []),
     "mlmg_kernel_launches": (ctypes.c_longlong, [c_int]),
+    "mlmg_fp64_fma_rate": (c_int, [P(ctypes.c_double)]),
+    "mlmg_check_bit_conversions": (c_int, [ctypes.c_longlong, ctypes.c_ulonglong, P(ctypes.c_longlong),
+                                           P(ctypes.c_ulonglong)]),
     "mlmg_boxarray_new": (c_int, [P(c_int), c_int, P(c_void_p)]),
     "mlmg_boxarray_new_domain": (c_int, [I3, I3, P(c_void_p)]),
     "mlmg_boxarray_maxsize": (c_int, [c_void_p, I3]),
@@ -87,6 +90,8 @@ SIGNATURES = {
     "mlmg_set_time_kernels": (c_int, [c_void_p, c_int]),
     "mlmg_set_option": (c_int, [c_void_p, ctypes.c_char_p, c_double]),
     "mlmg_get_smoother_stats": (c_int, [c_void_p, P(c_double), P(ctypes.c_longlong), P(c_double), c_int]),
+    "mlmg_get_residual_stats": (c_int, [c_void_p, P(ctypes.c_double), P(ctypes.c_longlong), P(ctypes.c_double),
+                                        P(ctypes.c_double), c_int]),
     "mlmg_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_double, c_double, P(c_double)]),
     "mlmg_solve_levels": (c_int, [c_void_p, P(c_void_p), P(c_void_p), c_double, c_double, P(c_double)]),
     "mlmg_apply": (c_int, [c_void_p, c_void_p, c_void_p]),

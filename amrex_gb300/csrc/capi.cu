@@ -3,6 +3,7 @@
 #include "solver.hpp"
 #include "amr.hpp"
 #include "kernels.cuh"
+#include "stage_kernels.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -594,6 +595,139 @@ long long mlmg_kernel_launches (int reset)
     return v;
 }
 
+// 8 independent FMA chains per thread, iters steps each (x -> a x + c stays
+// bounded for |a| < 1); the sums are stored so nothing is optimised away
+static __global__ void k_fp64_fma_probe (double* out, double a, double c, int iters)
+{
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) { x[q] = 1.0e-3 * (threadIdx.x + q); }
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) { x[q] = fma(a, x[q], c); }
+    }
+    double sum = 0.0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) { sum += x[q]; }
+    out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = sum;
+}
+
+int mlmg_fp64_fma_rate (double* tflops)
+{
+    API_BEGIN
+    MLMG_REQUIRE(tflops != nullptr, ERR_ARGS, "bad arguments");
+    int dev = 0, sms = 0;
+    MLMG_CUDA_CHECK(cudaGetDevice(&dev));
+    MLMG_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    cudaStream_t st = lib_stream();
+    const int threads = 256, blocks = sms * 8, iters = 2048;
+    DevBuf<double> out((size_t)blocks * threads);
+    cudaEvent_t e0, e1;
+    MLMG_CUDA_CHECK(cudaEventCreate(&e0));
+    MLMG_CUDA_CHECK(cudaEventCreate(&e1));
+    k_fp64_fma_probe<<<blocks, threads, 0, st>>>(out.p, 0.9999999, 1.0e-7, iters / 8);
+    MLMG_CUDA_CHECK(cudaEventRecord(e0, st));
+    k_fp64_fma_probe<<<blocks, threads, 0, st>>>(out.p, 0.9999999, 1.0e-7, iters);
+    MLMG_CUDA_CHECK(cudaEventRecord(e1, st));
+    g_launches += 2;
+    MLMG_CUDA_CHECK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    MLMG_CUDA_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1.0e-3) * 1.0e-12;
+    API_END
+}
+
+// splitmix64 (a counter-based generator for the conversion check)
+__device__ __forceinline__ unsigned long long mix64 (unsigned long long x)
+{
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+// binary64 values at the edges of binary32 rounding: zeros, infinities, a
+// NaN, the largest float and the halfway point above it, the smallest normal,
+// the largest subnormal plus half an ulp, the smallest subnormal, halfway
+// points around it (2^-150 and just above), and the smallest double
+__constant__ unsigned long long kConvEdges[] = {
+    0x0000000000000000ull, 0x8000000000000000ull, 0x7ff0000000000000ull, 0xfff0000000000000ull,
+    0x7ff8000000000001ull, 0x47efffffe0000000ull, 0x47effffff0000000ull, 0x3810000000000000ull,
+    0x380ffffff0000000ull, 0x36a0000000000000ull, 0x3690000000000000ull, 0x3690000000000001ull,
+    0xb690000000000000ull, 0x0000000000000001ull, 0x47effffff0000001ull, 0x369fffffffffffffull};
+
+// compares the bit-assembled conversions and |x| with the hardware over n
+// cases: random bit patterns, binary64 values around the binary32 range,
+// halfway points between neighbouring floats (and one ulp either side),
+// subnormal-range values, subnormal and zero floats, and the edge table
+static __global__ void k_check_bit_conversions (long long n, unsigned long long seed, unsigned long long* bad,
+                                                 unsigned long long* first)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const unsigned long long r0 = mix64(seed ^ (2ull * t)), r1 = mix64(seed ^ (2ull * t + 1ull));
+        unsigned long long db;
+        const int nedge = (int)(sizeof(kConvEdges) / sizeof(kConvEdges[0]));
+        if (t < nedge) {
+            db = kConvEdges[t];
+        } else {
+            switch (t & 3) {
+            case 0: db = r0; break;
+            case 1: db = (r0 & 0x800fffffffffffffull) | ((850ull + r1 % 325ull) << 52); break;
+            case 2: db = ((r0 & 0x800fffffe0000000ull) | ((860ull + r1 % 300ull) << 52)) + 0x10000000ull
+                         + (unsigned long long)((long long)((r1 >> 40) % 3ull) - 1); break;
+            default: db = (r0 & 0x800fffffffffffffull) | ((860ull + r1 % 40ull) << 52); break;
+            }
+        }
+        const double d = __longlong_as_double((long long)db);
+        const float fh = __double2float_rn(d), fs = d2f_bits(d);
+        const unsigned fb = (unsigned)(r1 >> 32);
+        const float f = __uint_as_float((t & 4) ? (fb & 0x807fffffu) : fb);
+        const double dh = (double)f, ds = f2d_bits(f);
+        // a NaN only has to stay a NaN; |x| of a NaN only has to order above
+        // +Inf as a bit pattern
+        const bool nan_d = (db & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+        const unsigned long long ah = (unsigned long long)__double_as_longlong(fabs(d)), as = abs_bits(d);
+        const bool ok[3] = {__float_as_uint(fh) == __float_as_uint(fs) || (fh != fh && fs != fs),
+                            __double_as_longlong(dh) == __double_as_longlong(ds) || (dh != dh && ds != ds),
+                            nan_d ? as > 0x7ff0000000000000ull : ah == as};
+        const unsigned long long input[3] = {db, (unsigned long long)__float_as_uint(f), db};
+        for (int c = 0; c < 3; ++c) {
+            if (!ok[c]) {
+                atomicAdd(&bad[c], 1ull);
+                atomicCAS(&first[c], 0ull, input[c] | (c == 1 ? 0x100000000ull : 0ull));
+            }
+        }
+    }
+}
+
+int mlmg_check_bit_conversions (long long n, unsigned long long seed, long long mismatches[3],
+                                unsigned long long first_bad[3])
+{
+    API_BEGIN
+    MLMG_REQUIRE(n >= 0 && mismatches != nullptr, ERR_ARGS, "bad arguments");
+    cudaStream_t st = lib_stream();
+    DevBuf<unsigned long long> bad(6);
+    MLMG_CUDA_CHECK(cudaMemsetAsync(bad.p, 0, 6 * sizeof(unsigned long long), st));
+    int dev = 0, sms = 0;
+    MLMG_CUDA_CHECK(cudaGetDevice(&dev));
+    MLMG_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (n > 0) {
+        k_check_bit_conversions<<<sms * 8, 256, 0, st>>>(n, seed, bad.p, bad.p + 3);
+        g_launches += 1;
+    }
+    unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(h, bad.p, sizeof(h), cudaMemcpyDeviceToHost, st));
+    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
+    for (int c = 0; c < 3; ++c) {
+        mismatches[c] = (long long)h[c];
+        if (first_bad) { first_bad[c] = h[3 + c]; }
+    }
+    API_END
+}
+
 // ------------------------------------------------------------- BoxArray --
 int mlmg_boxarray_new (const int* boxes, int nbox, mlmg_boxarray* out)
 {
@@ -1183,6 +1317,22 @@ int mlmg_get_smoother_stats (mlmg_solver s, double* total_ms, long long* launche
     if (launches) { *launches = k.launches; }
     if (bytes_per_launch) { *bytes_per_launch = k.bytes_per_launch; }
     if (reset) { e->reset_smoother_stats(); }
+    API_END
+}
+
+int mlmg_get_residual_stats (mlmg_solver s, double* total_ms, long long* launches, double* bytes_per_launch,
+                             double* flops_per_launch, int reset)
+{
+    API_BEGIN
+    MLMG_REQUIRE(s != nullptr, ERR_ARGS, "null handle");
+    Engine* e = s->eng ? s->eng.get() : s->batch_eng.get();
+    MLMG_REQUIRE(e != nullptr, ERR_ARGS, "no solve has run on this solver");
+    const KernelStats& k = e->residual_stats();
+    if (total_ms) { *total_ms = k.total_ms; }
+    if (launches) { *launches = k.launches; }
+    if (bytes_per_launch) { *bytes_per_launch = k.bytes_per_launch; }
+    if (flops_per_launch) { *flops_per_launch = k.flops_per_launch; }
+    if (reset) { e->reset_residual_stats(); }
     API_END
 }
 

@@ -128,30 +128,39 @@ struct Engine::Impl {
     int lc = -1;
     DevBuf<CoarseLevelPtrs> coarse_lv;
     cudaGraphExec_t graph_exec = nullptr;
+    EngineOptions graph_opt{};   // the options the graph was captured with
     int graph_launches = 0;      // kernels in one replay of the iteration graph
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // event pairs around the finest-level smoother launches of one iteration
-    std::vector<cudaEvent_t> kev;
-    int kev_used = 0;
+    // event pairs around the finest-level smoother launches (0) and the outer
+    // residual (1) of one iteration
+    std::vector<cudaEvent_t> kev[2];
+    int kev_used[2] = {0, 0};
     bool capturing = false;
     int bslot = 0;               // bottom solves issued in the current iteration
 
     explicit Impl (Engine& e) : E(e) {}
     ~Impl () {
-        if (graph_exec) { cudaGraphExecDestroy(graph_exec); }
+        drop_graphs();
         if (ev0) { cudaEventDestroy(ev0); }
         if (ev1) { cudaEventDestroy(ev1); }
-        for (auto e : kev) { cudaEventDestroy(e); }
+        for (auto& v : kev) { for (auto e : v) { cudaEventDestroy(e); } }
     }
 
-    void kev_record ()
+    void drop_graphs ()
     {
-        if (kev_used >= (int)kev.size()) {
+        if (graph_exec) { cudaGraphExecDestroy(graph_exec); }
+        graph_exec = nullptr;
+    }
+
+    void kev_record (int t = 0)
+    {
+        std::vector<cudaEvent_t>& v = kev[t];
+        if (kev_used[t] >= (int)v.size()) {
             cudaEvent_t e;
             MLMG_CUDA_CHECK(cudaEventCreate(&e));
-            kev.push_back(e);
+            v.push_back(e);
         }
-        cudaEvent_t e = kev[kev_used++];
+        cudaEvent_t e = v[kev_used[t]++];
         if (capturing) {
             MLMG_CUDA_CHECK(cudaEventRecordWithFlags(e, st(), cudaEventRecordExternal));
         } else {
@@ -161,11 +170,14 @@ struct Engine::Impl {
 
     void kev_harvest ()
     {
-        for (int q = 0; q + 1 < kev_used; q += 2) {
-            float ms = 0;
-            MLMG_CUDA_CHECK(cudaEventElapsedTime(&ms, kev[q], kev[q + 1]));
-            E.m_kstats.total_ms += ms;
-            E.m_kstats.launches += 1;
+        KernelStats* out[2] = {&E.m_kstats, &E.m_rstats};
+        for (int t = 0; t < 2; ++t) {
+            for (int q = 0; q + 1 < kev_used[t]; q += 2) {
+                float ms = 0;
+                MLMG_CUDA_CHECK(cudaEventElapsedTime(&ms, kev[t][q], kev[t][q + 1]));
+                out[t]->total_ms += ms;
+                out[t]->launches += 1;
+            }
         }
     }
 
@@ -176,6 +188,7 @@ struct Engine::Impl {
     // ------------------------------------------------------------ setup --
     void build ();
     void build_bottom_tables ();
+    void outer_residual_stats ();
     void load_level0_field (const FabSet* fs, double* field, double defval, int nodal_dir, int s);
     void xfer (const std::vector<XferItem>& items, const FabSet& fs, void* field, bool field_is_f32, int dir);
     std::vector<XferItem> items_for (const FabSet& fs, int s, int ghost_mode, int nodal_dir) const;

@@ -309,6 +309,7 @@ void Engine::Impl::build ()
         E.m_kstats.cells_per_launch = cells;
         E.m_kstats.bytes_per_launch = cells * (abec ? 7.0 : 3.0) * (mixed() ? 4.0 : 8.0);
     }
+    outer_residual_stats();
     MLMG_CUDA_CHECK(cudaEventCreate(&ev0));
     MLMG_CUDA_CHECK(cudaEventCreate(&ev1));
 }
@@ -912,7 +913,8 @@ void Engine::Impl::residual0 (bool to32)
 void Engine::Impl::one_iteration (bool fmg)
 {
     LevelData& L0 = lev[0];
-    kev_used = 0;
+    kev_used[0] = kev_used[1] = 0;
+    const bool timed = E.m_opt.time_kernels != 0;
     bslot = 0;
     bool any_singular = false;
     for (int s : singular) { if (s) { any_singular = true; } }
@@ -930,7 +932,9 @@ void Engine::Impl::one_iteration (bool fmg)
         k_add_to<double, float><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.sol.p, L0.cor32.p,
                                                                         active_d.p);
         launched();
+        if (timed) { kev_record(1); }
         residual0(true);
+        if (timed) { kev_record(1); }
     } else {
         if (any_singular) {
             k_reduce<double><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.res.p, nullptr,
@@ -949,7 +953,40 @@ void Engine::Impl::one_iteration (bool fmg)
     MLMG_CUDA_CHECK(cudaMemcpyAsync(h_red.p, red_out.p, sizeof(double) * nsolve, cudaMemcpyDeviceToHost, st()));
 }
 
+// algorithmic bytes and FP64 operations of one outer residual launch of the
+// mixed path over the whole finest level: phi (8 B), rhs (8 B), the FP64
+// stencil D, sX, sY, sZ (ABec, 32 B) and the FP32 residual (4 B) per cell;
+// FP64 operations: 7 FMAs (14 FLOPs) per cell
+void Engine::Impl::outer_residual_stats ()
+{
+    double cells = 0;
+    for (int p : lev[0].all.h_plist) {
+        const PatchDesc& P = lev[0].meta.patches[p];
+        cells += (double)(P.hi[0] - P.lo[0] + 1) * (P.hi[1] - P.lo[1] + 1) * (P.hi[2] - P.lo[2] + 1);
+    }
+    KernelStats& R = E.m_rstats;
+    R.cells_per_launch = cells;
+    R.bytes_per_launch = cells * (abec ? 52.0 : 20.0);
+    R.flops_per_launch = cells * 14.0;
+}
+
 // ---------------------------------------------------------------- Engine ---
+bool same_iteration (const EngineOptions& a, const EngineOptions& b)
+{
+    return a.max_iter == b.max_iter && a.fixed_iter == b.fixed_iter && a.nu1 == b.nu1 && a.nu2 == b.nu2 &&
+           a.nuf == b.nuf && a.nub == b.nub && a.bottom_solver == b.bottom_solver &&
+           a.bottom_maxiter == b.bottom_maxiter && a.bottom_reltol == b.bottom_reltol &&
+           a.bottom_abstol == b.bottom_abstol && a.always_use_bnorm == b.always_use_bnorm &&
+           a.verbose == b.verbose && a.precision == b.precision && a.use_graph == b.use_graph &&
+           a.fused_smoother == b.fused_smoother && a.merge_boxes == b.merge_boxes &&
+           a.time_kernels == b.time_kernels && a.coarse_block == b.coarse_block &&
+           a.coarse_cells == b.coarse_cells && a.march_sweep == b.march_sweep &&
+           a.march_min_tiles == b.march_min_tiles && a.march_tz == b.march_tz && a.fused_tma == b.fused_tma &&
+           a.fused_prefetch == b.fused_prefetch && a.max_fmg_iter == b.max_fmg_iter &&
+           a.transpose == b.transpose && a.tma_first_wait == b.tma_first_wait &&
+           a.final_fill_bc == b.final_fill_bc;
+}
+
 Engine::Engine (std::vector<SolveProblem> problems, const EngineOptions& opt, cudaStream_t stream)
     : m_problems(std::move(problems)), m_opt(opt), m_stream(stream)
 {
@@ -1183,6 +1220,8 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
     // initial guess (valid cells) and rhs; the solution's ghosts come from BCs
     MLMG_CUDA_CHECK(cudaMemsetAsync(L0.sol.p, 0, L0.sol.n * sizeof(double), m_stream));
     MLMG_CUDA_CHECK(cudaMemsetAsync(L0.rhs.p, 0, L0.rhs.n * sizeof(double), m_stream));
+    // a graph captured under other options is not this iteration
+    if (I.graph_exec != nullptr && !same_iteration(I.graph_opt, m_opt)) { I.drop_graphs(); }
     for (int s = 0; s < ns; ++s) {
         I.xfer(I.items_for(*sol_in[s], s, 0, -1), *sol_in[s], L0.sol.p, false, 0);
         I.xfer(I.items_for(*rhs[s], s, 0, -1), *rhs[s], L0.rhs.p, false, 0);
@@ -1265,6 +1304,7 @@ void Engine::solve (const std::vector<const FabSet*>& sol_in, const std::vector<
                 MLMG_CUDA_CHECK(cudaStreamEndCapture(m_stream, &g));
                 MLMG_CUDA_CHECK(cudaGraphInstantiate(&I.graph_exec, g, 0));
                 MLMG_CUDA_CHECK(cudaGraphDestroy(g));
+                I.graph_opt = m_opt;
                 per_iter_launches = m_launches - before;
                 m_launches = before;
             }

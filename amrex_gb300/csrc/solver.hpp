@@ -57,12 +57,16 @@ struct EngineOptions {
                                 // gets its first ghost layer written back
 };
 
+// true when two option sets capture the same iteration graph
+bool same_iteration (const EngineOptions& a, const EngineOptions& b);
+
 // Live timing of the dominant kernel (the finest-level smoother).
 struct KernelStats {
     double total_ms = 0;        // summed device time of the timed launches
     long long launches = 0;
     double bytes_per_launch = 0;  // algorithmic bytes moved by one launch
     double cells_per_launch = 0;
+    double flops_per_launch = 0;  // algorithmic FP64 operations of one launch (an FMA counts 2)
 };
 
 struct SolveProblem {           // one solve of a batch
@@ -132,6 +136,10 @@ public:
     void reset_launch_count () { m_launches = 0; }
     const KernelStats& smoother_stats () const { return m_kstats; }
     void reset_smoother_stats () { m_kstats.total_ms = 0; m_kstats.launches = 0; }
+    // the FP64 outer residual of the mixed path (with the correction update
+    // where it is fused), timed with the smoother under time_kernels
+    const KernelStats& residual_stats () const { return m_rstats; }
+    void reset_residual_stats () { m_rstats.total_ms = 0; m_rstats.launches = 0; }
 
     struct Impl;
     Impl& impl () { return *m_impl; }   // engine internals (AMR composite driver)
@@ -142,7 +150,7 @@ private:
     std::vector<SolveReport> m_reports;
     double m_last_ms = 0;
     int m_launches = 0;
-    KernelStats m_kstats;
+    KernelStats m_kstats, m_rstats;
     std::unique_ptr<Impl> m_impl;
 };
 

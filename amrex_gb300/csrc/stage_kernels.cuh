@@ -5,6 +5,81 @@
 
 namespace mlmg {
 
+// FP32 <-> FP64 conversions and |x| of an FP64 value on the integer pipe.
+// GB300's FP64 pipe completes 2 operations per clock per SM, and a hardware
+// conversion (or the predicated-off conversion of a guarded fallback, or an
+// FP64 absolute value) occupies it like arithmetic does, so the kernels that
+// FP64 bounds (the outer residual, phi += cor) assemble these results from
+// the IEEE 754 bit fields instead.  Each equals the hardware result for every
+// finite input and for +-Inf (a NaN stays a quiet NaN with the top bits of
+// its payload); mlmg_check_bit_conversions compares them on the device.
+
+// binary32 -> binary64 (exact): rebias the exponent by 1023 - 127 and move the
+// 23 fraction bits to the top of the 52; a subnormal is normalised first
+__device__ __forceinline__ double f2d_bits (float c)
+{
+    const unsigned u = __float_as_uint(c);
+    const unsigned sign = u & 0x80000000u;
+    const unsigned e = (u >> 23) & 0xffu;
+    unsigned m = u & 0x7fffffu;
+    unsigned ed;
+    if (e == 0u) {
+        if (m == 0u) { return __hiloint2double((int)sign, 0); }
+        const int p = 31 - __clz((int)m);              // leading one of the subnormal's fraction
+        ed = (unsigned)(p + 1023 - 149);               // value = 1.f x 2^(p - 149)
+        m = (m << (23 - p)) & 0x7fffffu;
+    } else if (e == 255u) {
+        ed = 2047u;
+        if (m != 0u) { m |= 0x400000u; }               // quiet NaN
+    } else {
+        ed = e + 896u;
+    }
+    return __hiloint2double((int)(sign | (ed << 20) | (m >> 3)), (int)(m << 29));
+}
+
+// binary64 -> binary32, round to nearest even: keep the top 23 fraction bits
+// and round on the 29 dropped ones (above half, or exactly half with an odd
+// kept part); a carry moves into the exponent (the largest finite float
+// rounds up to Inf).  Results below the normal range shift the 53-bit
+// significand right by the subnormal distance and round the same way.
+__device__ __forceinline__ float d2f_bits (double v)
+{
+    const unsigned hi = (unsigned)__double2hiint(v), lo = (unsigned)__double2loint(v);
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned E = (hi >> 20) & 0x7ffu;
+    const int e = (int)E - 896;                        // binary32 biased exponent
+    unsigned f;
+    if (e >= 1 && e <= 254) {
+        f = ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+        const unsigned rem = lo & 0x1fffffffu;
+        f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
+    } else if (E == 2047u) {
+        f = (((hi & 0xfffffu) | lo) != 0u) ? (0x7fc00000u | ((hi & 0xfffffu) << 3) | (lo >> 29)) : 0x7f800000u;
+    } else if (e > 254) {
+        f = 0x7f800000u;                               // overflow
+    } else {
+        const int sh = 926 - (int)E;                   // value = M x 2^-sh in units of 2^-149
+        if (sh >= 64) {
+            f = 0u;
+        } else {
+            const unsigned long long M = (1ull << 52) | ((unsigned long long)(hi & 0xfffffu) << 32) | lo;
+            const unsigned long long q = M >> sh;
+            const unsigned long long rem = M & ((1ull << sh) - 1ull);
+            const unsigned long long half = 1ull << (sh - 1);
+            f = (unsigned)q + ((rem > half || (rem == half && (q & 1ull))) ? 1u : 0u);
+        }
+    }
+    return __uint_as_float(sign | f);
+}
+
+// the bit pattern of |v| as an integer (non-negative doubles order like their
+// bits; a NaN orders above every number), cleared on the high word so that
+// it stays an integer operation rather than an FP64 absolute value
+__device__ __forceinline__ unsigned long long abs_bits (double v)
+{
+    return ((unsigned long long)((unsigned)__double2hiint(v) & 0x7fffffffu) << 32) | (unsigned)__double2loint(v);
+}
+
 // ------------------------------------------------------------ reductions --
 enum RedOp : int { RED_MAXABS = 0, RED_DOT = 1, RED_SUM = 2 };
 
@@ -248,7 +323,11 @@ k_add_to (DevLevel L, Subset S, TD* __restrict__ dst, const TS* __restrict__ src
             const int i = c.x0 + threadIdx.x + 32 * h;
             if (i > P.hi[0]) { continue; }
             const long long q = cidx(P, i, j, k);
-            dst[q] += TD(src[q]);
+            if constexpr (std::is_same_v<TD, double> && std::is_same_v<TS, float>) {
+                dst[q] += f2d_bits(src[q]);
+            } else {
+                dst[q] += TD(src[q]);
+            }
         }
     }
 }

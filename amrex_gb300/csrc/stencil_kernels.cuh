@@ -23,6 +23,7 @@
 
 namespace mlmg {
 
+
 // omega / g for the Gauss-Seidel update (omega = 1.15, abec_gsrb).  The FP32
 // V-cycle is only a preconditioner of the FP64 refinement, so its division
 // uses the fast single-precision intrinsic; FP64 keeps IEEE division.
@@ -258,9 +259,9 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
                 const Coef7<T, VARC> cf = load_coef<T, VARC>(P, q, S);
                 T v;
                 if constexpr (std::is_same_v<T, double>) {
-                    // seven FMAs (b - D x, then + s x_nb): GB300's FP64 rate
-                    // bounds this kernel, and the FMA chain needs one FP64
-                    // operation less per cell than D x - sum s x_nb
+                    // seven FMAs (b - D x, then + s x_nb) and nothing else on
+                    // the FP64 pipe, whose rate bounds this kernel on GB300:
+                    // the FP32 copy and the max-norm are integer operations
                     v = fma(-cf.d, xc, b[q]);
                     v = fma(cf.sxl, xm, v); v = fma(cf.sxh, xp, v);
                     v = fma(cf.syl, ym, v); v = fma(cf.syh, yp, v);
@@ -269,12 +270,16 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
                     const T nb = cf.sxl * xm + cf.sxh * xp + cf.syl * ym + cf.syh * yp + cf.szl * zm + cf.szh * zp;
                     v = b[q] - (cf.d * xc - nb);
                 }
-                r[q] = TO(v);
+                if constexpr (std::is_same_v<T, double> && std::is_same_v<TO, float>) {
+                    r[q] = d2f_bits(v);
+                } else {
+                    r[q] = TO(v);
+                }
                 if constexpr (std::is_same_v<T, double>) {
                     // integer max on the bit patterns of |v| keeps the FP64 pipe
                     // free (non-negative doubles order like their bits; a NaN
                     // residual orders above every number and reaches the norm)
-                    const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+                    const unsigned long long ab = abs_bits(v);
                     mxb = (ab > mxb) ? ab : mxb;
                 } else {
                     mx = max_nan(mx, fabs((double)v));

@@ -628,6 +628,7 @@ def run_gb300(args, ws, rank, local):
     for _ in range(args.warmup):
         step(mixed)
     mixed.smootherStats(reset=True)
+    mixed.residualStats(reset=True)
     ag.kernel_launches(reset=True)
     barrier(ws)
     torch.cuda.synchronize()
@@ -641,6 +642,7 @@ def run_gb300(args, ws, rank, local):
     ms = e0.elapsed_time(e1) / args.steps
     ms = barrier_max(ms, ws)
     sm_ms, sm_n, sm_bytes = mixed.smootherStats(reset=True)
+    r_ms, r_n, r_bytes, r_flops = mixed.residualStats(reset=True)
     iters = mixed.getNumIters()
     phim = sol.get_global((N, N, N))
     rel_diff = float(np.abs(phim - phi64).max() / np.abs(phi64).max())
@@ -665,7 +667,21 @@ def run_gb300(args, ws, rank, local):
     e2e_ms = (time.perf_counter() - t0) * 1e3 / ne2e
     e2e_ms = barrier_max(e2e_ms, ws)
 
+    # FP64 roofline of the outer residual: this GPU's FMA rate, measured by
+    # the library's register-resident FMA kernel
+    fp64_peak = ag.fp64_fma_rate()
+    r_avg = r_ms / max(r_n, 1)
+    outer = {"kernel": "k_update_residual: phi += cor fused into the FP64 outer residual r = f - A phi "
+                       "(stencil form, FP32 copy of r, per-solve max-norm)",
+             "bound": "fp64", "avg_launch_ms": r_avg, "launches_timed": r_n,
+             "flops_per_launch": r_flops, "bytes_per_launch": r_bytes,
+             "achieved_tflops": r_flops / (r_avg * 1e-3) / 1e12 if r_n else None,
+             "fp64_peak_tflops": fp64_peak, "fp64_peak_kind": "measured in-run (FMA chains, mlmg_fp64_fma_rate)",
+             "achieved_gbs": r_bytes / (r_avg * 1e-3) / 1e9 if r_n else None}
+    outer["fp64_frac"] = outer["achieved_tflops"] / fp64_peak if r_n and fp64_peak > 0 else None
+
     peak, peak_kind = peaks()
+    outer["hbm_frac"] = outer["achieved_gbs"] / peak if r_n else None
     avg_launch_ms = sm_ms / max(sm_n, 1)
     achieved = sm_bytes / (avg_launch_ms * 1e-3) / 1e9 if sm_n else None
     traffic = traffic_per_launch("mixed")
@@ -688,7 +704,8 @@ def run_gb300(args, ws, rank, local):
                      "launches_timed": sm_n,
                      "fp64_smoother": {"avg_launch_ms": fp64_sm[0] / max(fp64_sm[1], 1),
                                        "achieved": (fp64_sm[2] / (fp64_sm[0] / max(fp64_sm[1], 1) * 1e-3) / 1e9)
-                                       if fp64_sm[1] else None}},
+                                       if fp64_sm[1] else None},
+                     "outer_residual": outer},
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": int(rhs_h.nbytes),
                 "d2h_bytes_per_step": int(sol_h.nbytes)},
         "gpu_launches": int(launches),

@@ -59,6 +59,20 @@ int mlmg_version(void);
 void* mlmg_stream(void);
 /* number of kernels this library has launched since the last reset */
 long long mlmg_kernel_launches(int reset);
+/* the device's FP64 FMA throughput in TFLOP/s (2 FLOPs per FMA), measured by
+ * one register-resident kernel (8 independent FMA chains per thread, eight
+ * 256-thread blocks per SM) timed with CUDA events on the library stream after
+ * a warm-up launch: the FP64 roofline of the outer residual.  Changes no
+ * device setting. */
+int mlmg_fp64_fma_rate(double* tflops);
+/* the FP64-bound kernels convert FP32 <-> FP64 and take |x| by integer bit
+ * assembly; this compares those results with the hardware's on n device cases
+ * (edge values, random bit patterns, halfway points between floats,
+ * subnormals): mismatches[0..2] = cases that differ for FP64 -> FP32, FP32 ->
+ * FP64 and |x| (0 expected); first_bad (may be null) = an input of each kind
+ * that differed (FP32 inputs with bit 32 set; 0 when none) */
+int mlmg_check_bit_conversions(long long n, unsigned long long seed, long long mismatches[3],
+                               unsigned long long first_bad[3]);
 
 /* ----------------------------------------------------------- BoxArray ----
  * replaces amrex_fi_new_boxarray / amrex_fi_boxarray_maxsize / ..._get_box
@@ -219,11 +233,17 @@ int mlmg_set_fused_smoother(mlmg_solver s, int on);      /* fused two-colour Gau
  * and the solve returns -7; the next solve with the default works);
  * -4 for an unknown name */
 int mlmg_set_option(mlmg_solver s, const char* name, double value);
-/* time every finest-level smoother launch with CUDA events on the library
- * stream (graph replays included); the stats accumulate until reset */
+/* time every finest-level smoother launch and every FP64 outer residual of
+ * the mixed path with CUDA events on the library stream (graph replays
+ * included); the stats accumulate until reset */
 int mlmg_set_time_kernels(mlmg_solver s, int on);
 int mlmg_get_smoother_stats(mlmg_solver s, double* total_ms, long long* launches, double* bytes_per_launch,
                             int reset);
+/* the FP64 outer residual of the mixed path (with the correction update where
+ * it is fused): total ms, launches, algorithmic bytes and FP64 operations
+ * (an FMA counts 2) per launch */
+int mlmg_get_residual_stats(mlmg_solver s, double* total_ms, long long* launches, double* bytes_per_launch,
+                            double* flops_per_launch, int reset);
 
 /* MLMGT::solve (AMReX_MLMG.H:44-51): sol holds the initial guess, rhs the
  * right-hand side; returns a status, final_resid gets the final max-norm */

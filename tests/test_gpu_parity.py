@@ -195,6 +195,15 @@ def test_coarse_block_vcycle_matches_grid_kernels(name, cells):
     assert np.abs(a - b).max() <= 1e-8 * np.abs(a).max()
 
 
+def test_bit_assembled_conversions_match_hardware():
+    """The FP32 <-> FP64 conversions and |x| that the FP64-bound kernels
+    assemble on the integer pipe equal the hardware's on 2^26 device cases
+    (edge values, random patterns, halfway points, subnormals)."""
+    for n, seed in ((1 << 26, 2024), (1 << 20, 7)):
+        bad, first = ag.check_bit_conversions(n, seed=seed)
+        assert sum(bad.values()) == 0, (bad, first)
+
+
 def test_graph_replay_is_bitwise_identical():
     c = load.load("solve_abec_32")["case"]
     inp = cases.inputs(c)
