@@ -67,7 +67,7 @@ k_coarse_vcycle (const CoarseLevelPtrs* __restrict__ lv, int lc, const BottomLev
         for_cells(C.L, p0, np, [&] (const PatchDesc& P, int i, int j, int k, long long q) {
             const float xc = C.cor[q];
             float xm, xp, ym, yp, zm, zp;
-            neighbours<float, false, false>(P, i, j, k, q, C.cor, xc, nullptr, xm, xp, ym, yp, zm, zp);
+            neighbours<float, false, false>(P, P, i, j, k, q, C.cor, xc, nullptr, xm, xp, ym, yp, zm, zp);
             const Coef7<float, ABEC> cf = load_coef<float, ABEC>(P, q, C.S);
             const float nb = cf.sxl * xm + cf.sxh * xp + cf.syl * ym + cf.syh * yp + cf.szl * zm + cf.szh * zp;
             C.rescor[q] = C.res[q] - (cf.d * xc - nb);

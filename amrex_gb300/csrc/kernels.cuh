@@ -55,6 +55,38 @@ __host__ __device__ __forceinline__ long long cidx (const PatchDesc& P, int i, i
     return P.base + (long long)(k - P.lo[2]) * P.sxy + (long long)(j - P.lo[1]) * P.sx + (i - P.lo[0]);
 }
 
+// the index geometry (and MLPoisson factors) of a patch, loaded once into
+// registers by the streaming kernels instead of being read through the
+// descriptor inside their cell loops
+struct PatchGeom {
+    int lo[3], hi[3];
+    long long base, sxy;
+    int sx, solve;
+    double dha[3];
+};
+
+__device__ __forceinline__ PatchGeom geom_of (const PatchDesc& P)
+{
+    PatchGeom g;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) { g.lo[d] = P.lo[d]; g.hi[d] = P.hi[d]; g.dha[d] = P.dha[d]; }
+    g.base = P.base;
+    g.sxy = P.sxy;
+    g.sx = P.sx;
+    g.solve = P.solve;
+    return g;
+}
+
+__host__ __device__ __forceinline__ long long cidx (const PatchGeom& P, int i, int j, int k)
+{
+    return P.base + (long long)(k - P.lo[2]) * P.sxy + (long long)(j - P.lo[1]) * P.sx + (i - P.lo[0]);
+}
+
+__device__ __forceinline__ bool contains (const PatchGeom& P, int i, int j, int k)
+{
+    return i >= P.lo[0] && i <= P.hi[0] && j >= P.lo[1] && j <= P.hi[1] && k >= P.lo[2] && k <= P.hi[2];
+}
+
 // mask value of the outside cell (i,j,k) adjacent to face f of patch P
 __device__ __forceinline__ int face_mask (const DevLevel& L, const PatchDesc& P, int f, int i, int j, int k)
 {

@@ -255,10 +255,17 @@ __global__ void __launch_bounds__(TILE_THREADS)
 k_restrict (DevLevel Lf, DevLevel Lc, Subset Sc, const T* __restrict__ fine, T* __restrict__ crse)
 {
     const TileCoord c = decode_tile(Lc, Sc, blockIdx.x);
-    const PatchDesc& C = Lc.P[c.p];
+    const PatchGeom C = geom_of(Lc.P[c.p]);
+    const int s = C.solve;
+    // the fine patch over the tile's first and last cells; a tile that lies
+    // over one fine patch (nearly all) looks it up once
+    const int xe = min(c.x0 + TILE_X - 1, C.hi[0]), ye = min(c.y0 + TILE_Y - 1, C.hi[1]);
+    const int ze = min(c.z0 + TILE_Z - 1, C.hi[2]);
+    const int pf = find_patch(Lf, s, 2 * c.x0, 2 * c.y0, 2 * c.z0);
+    const PatchGeom F0 = geom_of(Lf.P[pf]);
+    const bool one = contains(F0, 2 * xe + 1, 2 * ye + 1, 2 * ze + 1);
     const int j = c.y0 + threadIdx.y;
     if (j > C.hi[1]) { return; }
-    const int s = C.solve;
     const T volfrac = T(1.0) / T(8);
     for (int kk = 0; kk < TILE_Z; ++kk) {
         const int k = c.z0 + kk;
@@ -267,9 +274,13 @@ k_restrict (DevLevel Lf, DevLevel Lc, Subset Sc, const T* __restrict__ fine, T* 
         for (int h = 0; h < 2; ++h) {
             const int i = c.x0 + threadIdx.x + 32 * h;
             if (i > C.hi[0]) { continue; }
-            const PatchDesc& F = Lf.P[find_patch(Lf, s, 2 * i, 2 * j, 2 * k)];
-            const long long qf = cidx(F, 2 * i, 2 * j, 2 * k);
-            const long long sx = F.sx, sxy = F.sxy;
+            long long qf, sx, sxy;
+            if (one) {
+                qf = cidx(F0, 2 * i, 2 * j, 2 * k); sx = F0.sx; sxy = F0.sxy;
+            } else {
+                const PatchDesc& F = Lf.P[find_patch(Lf, s, 2 * i, 2 * j, 2 * k)];
+                qf = cidx(F, 2 * i, 2 * j, 2 * k); sx = F.sx; sxy = F.sxy;
+            }
             T v = 0;
             v += fine[qf];           v += fine[qf + 1];
             v += fine[qf + sx];      v += fine[qf + sx + 1];
@@ -286,10 +297,17 @@ __global__ void __launch_bounds__(TILE_THREADS)
 k_interp_add (DevLevel Lf, Subset Sf, DevLevel Lc, const T* __restrict__ crse, T* __restrict__ fine)
 {
     const TileCoord c = decode_tile(Lf, Sf, blockIdx.x);
-    const PatchDesc& F = Lf.P[c.p];
+    const PatchGeom F = geom_of(Lf.P[c.p]);
+    const int s = F.solve;
+    // the coarse patch under the tile's first and last cells; a tile that
+    // lies under one coarse patch (nearly all) looks it up once
+    const int xe = min(c.x0 + TILE_X - 1, F.hi[0]), ye = min(c.y0 + TILE_Y - 1, F.hi[1]);
+    const int ze = min(c.z0 + TILE_Z - 1, F.hi[2]);
+    const int pc = find_patch(Lc, s, c.x0 >> 1, c.y0 >> 1, c.z0 >> 1);
+    const PatchGeom C = geom_of(Lc.P[pc]);
+    const bool one = contains(C, xe >> 1, ye >> 1, ze >> 1);
     const int j = c.y0 + threadIdx.y;
     if (j > F.hi[1]) { return; }
-    const int s = F.solve;
     for (int kk = 0; kk < TILE_Z; ++kk) {
         const int k = c.z0 + kk;
         if (k > F.hi[2]) { break; }
@@ -298,8 +316,8 @@ k_interp_add (DevLevel Lf, Subset Sf, DevLevel Lc, const T* __restrict__ crse, T
             const int i = c.x0 + threadIdx.x + 32 * h;
             if (i > F.hi[0]) { continue; }
             const int ic = i >> 1, jc = j >> 1, kc = k >> 1;
-            const PatchDesc& C = Lc.P[find_patch(Lc, s, ic, jc, kc)];
-            fine[cidx(F, i, j, k)] += crse[cidx(C, ic, jc, kc)];
+            const long long qc = one ? cidx(C, ic, jc, kc) : cidx(Lc.P[find_patch(Lc, s, ic, jc, kc)], ic, jc, kc);
+            fine[cidx(F, i, j, k)] += crse[qc];
         }
     }
 }
@@ -311,7 +329,7 @@ __global__ void __launch_bounds__(TILE_THREADS)
 k_add_to (DevLevel L, Subset S, TD* __restrict__ dst, const TS* __restrict__ src, const int* __restrict__ active)
 {
     const TileCoord c = decode_tile(L, S, blockIdx.x);
-    const PatchDesc& P = L.P[c.p];
+    const PatchGeom P = geom_of(L.P[c.p]);
     const int j = c.y0 + threadIdx.y;
     if (j > P.hi[1]) { return; }
     if (active != nullptr && !active[P.solve]) { return; }
@@ -340,7 +358,7 @@ k_reduce (DevLevel L, Subset S, const T* __restrict__ x, const T* __restrict__ y
 {
     __shared__ double sm[32];
     const TileCoord c = decode_tile(L, S, blockIdx.x);
-    const PatchDesc& P = L.P[c.p];
+    const PatchGeom P = geom_of(L.P[c.p]);
     const int j = c.y0 + threadIdx.y;
     double acc = 0.0;
     if (j <= P.hi[1]) {
@@ -384,7 +402,7 @@ k_minus_offset (DevLevel L, Subset S, T* __restrict__ x, const double* __restric
                 const double* __restrict__ volinv)
 {
     const TileCoord c = decode_tile(L, S, blockIdx.x);
-    const PatchDesc& P = L.P[c.p];
+    const PatchGeom P = geom_of(L.P[c.p]);
     const int j = c.y0 + threadIdx.y;
     if (j > P.hi[1]) { return; }
     const T off = T(sums[P.solve] * volinv[P.solve]);

@@ -99,7 +99,8 @@ __device__ __forceinline__ T inline_ghost (const PatchDesc& P, int f, T pc, T pi
 }
 
 // local index of the face cell of face f for the patch cell (i,j,k) next to it
-__device__ __forceinline__ long long face_local (const PatchDesc& P, int f, int i, int j, int k)
+template <typename Geo>
+__device__ __forceinline__ long long face_local (const Geo& P, int f, int i, int j, int k)
 {
     const int d = f % 3;
     const int nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1;
@@ -109,20 +110,23 @@ __device__ __forceinline__ long long face_local (const PatchDesc& P, int f, int 
 }
 
 // the six neighbours of cell q (ghosts inline at patch faces when INLINE_BC)
-template <typename T, bool INLINE_BC, bool INHOMOG>
-__device__ __forceinline__ void neighbours (const PatchDesc& P, int i, int j, int k, long long q, const T* phi, T pc,
-                                            const double* bcval, T& xm, T& xp, T& ym, T& yp, T& zm, T& zp)
+// (Geo: the patch's geometry, PatchDesc or PatchGeom; PD: its descriptor,
+// whose face BCs the closures read)
+template <typename T, bool INLINE_BC, bool INHOMOG, typename Geo>
+__device__ __forceinline__ void neighbours (const Geo& P, const PatchDesc& PD, int i, int j, int k, long long q,
+                                            const T* phi, T pc, const double* bcval,
+                                            T& xm, T& xp, T& ym, T& yp, T& zm, T& zp)
 {
     const long long sx = P.sx, sxy = P.sxy;
     if constexpr (!INLINE_BC) {
         xm = phi[q - 1]; xp = phi[q + 1]; ym = phi[q - sx]; yp = phi[q + sx]; zm = phi[q - sxy]; zp = phi[q + sxy];
     } else {
-        xm = (i == P.lo[0]) ? inline_ghost<T, INHOMOG>(P, 0, pc, phi[q + 1], bcval, face_local(P, 0, i, j, k)) : phi[q - 1];
-        xp = (i == P.hi[0]) ? inline_ghost<T, INHOMOG>(P, 3, pc, phi[q - 1], bcval, face_local(P, 3, i, j, k)) : phi[q + 1];
-        ym = (j == P.lo[1]) ? inline_ghost<T, INHOMOG>(P, 1, pc, phi[q + sx], bcval, face_local(P, 1, i, j, k)) : phi[q - sx];
-        yp = (j == P.hi[1]) ? inline_ghost<T, INHOMOG>(P, 4, pc, phi[q - sx], bcval, face_local(P, 4, i, j, k)) : phi[q + sx];
-        zm = (k == P.lo[2]) ? inline_ghost<T, INHOMOG>(P, 2, pc, phi[q + sxy], bcval, face_local(P, 2, i, j, k)) : phi[q - sxy];
-        zp = (k == P.hi[2]) ? inline_ghost<T, INHOMOG>(P, 5, pc, phi[q - sxy], bcval, face_local(P, 5, i, j, k)) : phi[q + sxy];
+        xm = (i == P.lo[0]) ? inline_ghost<T, INHOMOG>(PD, 0, pc, phi[q + 1], bcval, face_local(P, 0, i, j, k)) : phi[q - 1];
+        xp = (i == P.hi[0]) ? inline_ghost<T, INHOMOG>(PD, 3, pc, phi[q - 1], bcval, face_local(P, 3, i, j, k)) : phi[q + 1];
+        ym = (j == P.lo[1]) ? inline_ghost<T, INHOMOG>(PD, 1, pc, phi[q + sx], bcval, face_local(P, 1, i, j, k)) : phi[q - sx];
+        yp = (j == P.hi[1]) ? inline_ghost<T, INHOMOG>(PD, 4, pc, phi[q - sx], bcval, face_local(P, 4, i, j, k)) : phi[q + sx];
+        zm = (k == P.lo[2]) ? inline_ghost<T, INHOMOG>(PD, 2, pc, phi[q + sxy], bcval, face_local(P, 2, i, j, k)) : phi[q - sxy];
+        zp = (k == P.hi[2]) ? inline_ghost<T, INHOMOG>(PD, 5, pc, phi[q - sxy], bcval, face_local(P, 5, i, j, k)) : phi[q + sxy];
     }
 }
 
@@ -131,8 +135,8 @@ struct Coef7 {
     T d, sxl, sxh, syl, syh, szl, szh;
 };
 
-template <typename T, bool VARC>
-__device__ __forceinline__ Coef7<T, VARC> load_coef (const PatchDesc& P, long long q, const StencilPtrs& S)
+template <typename T, bool VARC, typename Geo>
+__device__ __forceinline__ Coef7<T, VARC> load_coef (const Geo& P, long long q, const StencilPtrs& S)
 {
     Coef7<T, VARC> c;
     if constexpr (VARC) {
@@ -162,7 +166,7 @@ __device__ __forceinline__ void gsrb_s_cell (const DevLevel& L, const PatchDesc&
     const long long q = cidx(P, i, j, k);
     const T pc = phi[q];
     T xm, xp, ym, yp, zm, zp;
-    neighbours<T, INLINE_BC, false>(P, i, j, k, q, phi, pc, nullptr, xm, xp, ym, yp, zm, zp);
+    neighbours<T, INLINE_BC, false>(P, P, i, j, k, q, phi, pc, nullptr, xm, xp, ym, yp, zm, zp);
     const Coef7<T, VARC> c = load_coef<T, VARC>(P, q, S);
     T gmd = c.d;
     const bool face = (i == P.lo[0]) | (i == P.hi[0]) | (j == P.lo[1]) | (j == P.hi[1]) | (k == P.lo[2]) | (k == P.hi[2]);
@@ -255,7 +259,7 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
                 const long long q = cidx(P, i, j, k);
                 const T xc = x[q];
                 T xm, xp, ym, yp, zm, zp;
-                neighbours<T, INLINE_BC, INHOMOG>(P, i, j, k, q, x, xc, bcval, xm, xp, ym, yp, zm, zp);
+                neighbours<T, INLINE_BC, INHOMOG>(P, P, i, j, k, q, x, xc, bcval, xm, xp, ym, yp, zm, zp);
                 const Coef7<T, VARC> cf = load_coef<T, VARC>(P, q, S);
                 T v;
                 if constexpr (std::is_same_v<T, double>) {
