@@ -352,6 +352,8 @@ k_bottom (const BottomLevelPtrs* __restrict__ levels, const BottomJob* __restric
           const int* __restrict__ active, int* __restrict__ out_iters, int* __restrict__ out_ret)
 {
     const BottomJob J = jobs[blockIdx.x];
+    pdl_wait();
+    pdl_trigger();
     if (active != nullptr && !active[J.solve]) { return; }
     bottom_solve_block<T, ABEC>(levels[J.lev], J, prm, out_iters, out_ret);
 }

@@ -1286,6 +1286,7 @@ int mlmg_set_option (mlmg_solver s, const char* name, double value)
     else if (n == "march_sweep") { s->opt.march_sweep = value != 0.0; }
     else if (n == "fused_tma") { s->opt.fused_tma = value != 0.0; }
     else if (n == "fused_prefetch") { s->opt.fused_prefetch = value != 0.0; }
+    else if (n == "pdl") { s->opt.pdl = value != 0.0; }
     else if (n == "tma_wait_limit") {
         MLMG_REQUIRE(value >= -1, ERR_ARGS, "tma_wait_limit must be >= 0 (or -1: the default bound)");
         s->opt.tma_first_wait = (long long)value;

@@ -182,6 +182,24 @@ struct Engine::Impl {
     }
 
     cudaStream_t st () const { return E.m_stream; }
+    // a V-cycle kernel on the engine's stream, as a programmatic dependent
+    // launch (the kernel calls pdl_wait before it reads what the previous
+    // kernel wrote) unless the pdl option is off
+    template <typename... KArgs, typename... Args>
+    void launch (void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, Args&&... args)
+    {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = grid;
+        cfg.blockDim = block;
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st();
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = E.m_opt.pdl ? 1 : 0;
+        MLMG_CUDA_CHECK(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
+    }
     bool mixed () const { return E.m_opt.precision == 1; }
     void launched (int n = 1) { E.m_launches += n; }
 

@@ -81,6 +81,8 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
         }
     }
     __syncthreads();
+    pdl_wait();
+    pdl_trigger();
     const PatchLite& P = SP;
     // patch bounds in tile-local coordinates (lo <= 0 since tiles start inside the patch)
     const int pxl = P.lo[0] - x0, pxh = P.hi[0] - x0;

@@ -14,6 +14,15 @@ constexpr int TILE_Y = 4;         // rows per tile (one per warp)
 constexpr int TILE_Z = 4;         // planes per tile
 constexpr int TILE_THREADS = 128;
 
+// Programmatic dependent launch: the V-cycle's kernels are launched so that a
+// kernel's blocks may start while the previous kernel drains.  Each such
+// kernel reads only static data (tile maps, patch descriptors) before
+// pdl_wait(), which returns once the previous kernel has completed and its
+// writes are visible; pdl_trigger() then lets the next kernel be launched.
+// Both are no-ops for a kernel launched the ordinary way.
+__device__ __forceinline__ void pdl_wait () { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger () { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 struct DevLevel {
     const PatchDesc* P;
     const int8_t* masks;

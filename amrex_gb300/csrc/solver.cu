@@ -552,18 +552,18 @@ void Engine::Impl::resid32 (int l, float* rescor, float* cor, const float* res)
     const unsigned g = (unsigned)L.mg.ntiles;
     if (abec) {
         if (L.inline_bc) {
-            k_residual_s<float, float, true, true, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor,
+            launch(k_residual_s<float, float, true, true, false>, g, kTileBlock, 0, L.dl, L.mg.dev(), rescor, cor,
                                                                                        res, S, nullptr, nullptr);
         } else {
-            k_residual_s<float, float, true, false, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor,
+            launch(k_residual_s<float, float, true, false, false>, g, kTileBlock, 0, L.dl, L.mg.dev(), rescor, cor,
                                                                                         res, S, nullptr, nullptr);
         }
     } else {
         if (L.inline_bc) {
-            k_residual_s<float, float, false, true, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor,
+            launch(k_residual_s<float, float, false, true, false>, g, kTileBlock, 0, L.dl, L.mg.dev(), rescor, cor,
                                                                                         res, S, nullptr, nullptr);
         } else {
-            k_residual_s<float, float, false, false, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor,
+            launch(k_residual_s<float, float, false, false, false>, g, kTileBlock, 0, L.dl, L.mg.dev(), rescor, cor,
                                                                                          res, S, nullptr, nullptr);
         }
     }
@@ -599,20 +599,20 @@ void Engine::Impl::smooth_fused (int l, int n)
             const CUtensorMap* pf = E.m_opt.fused_prefetch ? L.tm_pf.p : nullptr;
             const long long fw = E.m_opt.tma_first_wait < 0 ? tma::WAIT_LIMIT : E.m_opt.tma_first_wait;
             if (abec) {
-                k_sweep_fused2<true, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
+                launch(k_sweep_fused2<true, true>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
                                                                 fw, pf);
             } else {
-                k_sweep_fused2<false, true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
+                launch(k_sweep_fused2<false, true>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
                                                                  fw, pf);
             }
         } else {
             const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
             if (abec) {
-                k_sweep_fused2<true><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p,
-                                                          tma::WAIT_LIMIT);
+                launch(k_sweep_fused2<true>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p,
+                                                          tma::WAIT_LIMIT, nullptr);
             } else {
-                k_sweep_fused2<false><<<g, blk, 0, st()>>>(L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p,
-                                                           tma::WAIT_LIMIT);
+                launch(k_sweep_fused2<false>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p,
+                                                           tma::WAIT_LIMIT, nullptr);
             }
         }
         launched();
@@ -735,7 +735,7 @@ void Engine::Impl::vcycle (int top)
         }
         correction_residual<T>(l);
         LevelData& C = lev[l + 1];
-        k_restrict<T><<<C.all.ntiles, kTileBlock, 0, st()>>>(L.dl, C.dl, C.all.dev(), rescor, field_res<T>(l + 1));
+        launch(k_restrict<T>, C.all.ntiles, kTileBlock, 0, L.dl, C.dl, C.all.dev(), rescor, field_res<T>(l + 1));
         launched();
     }
     const BottomParams prm = bottom_params();
@@ -748,10 +748,10 @@ void Engine::Impl::vcycle (int top)
                                                                        o.nu1, o.nu2, bot_iters.p, bot_ret.p);
         }
     } else if (abec) {
-        k_bottom<T, true><<<njobs, bot_threads, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
+        launch(k_bottom<T, true>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr,
                                                               bot_iters.p, bot_ret.p);
     } else {
-        k_bottom<T, false><<<njobs, bot_threads, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
+        launch(k_bottom<T, false>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr,
                                                                bot_iters.p, bot_ret.p);
     }
     launched();
@@ -760,7 +760,7 @@ void Engine::Impl::vcycle (int top)
         LevelData& L = lev[l];
         if (L.mg.n == 0) { continue; }
         T* cor = field_cor<T>(l);
-        k_interp_add<T><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), lev[l + 1].dl, field_cor<T>(l + 1), cor);
+        launch(k_interp_add<T>, L.mg.ntiles, kTileBlock, 0, L.dl, L.mg.dev(), lev[l + 1].dl, field_cor<T>(l + 1), cor);
         launched();
         if (std::is_same_v<T, float> && L.fused) {
             smooth_fused(l, o.nu2);
@@ -782,7 +782,7 @@ void Engine::Impl::fcycle ()
     for (int l = 1; l <= nb; ++l) {
         LevelData& C = lev[l];
         // avgDownResMG (AMReX_MLLinOp.H:1563-1584)
-        k_restrict<T><<<C.all.ntiles, kTileBlock, 0, st()>>>(lev[l - 1].dl, C.dl, C.all.dev(), field_res<T>(l - 1),
+        launch(k_restrict<T>, C.all.ntiles, kTileBlock, 0, lev[l - 1].dl, C.dl, C.all.dev(), field_res<T>(l - 1),
                                                              field_res<T>(l));
         launched();
     }
@@ -790,10 +790,10 @@ void Engine::Impl::fcycle ()
         const EngineOptions& o = E.m_opt;
         const BottomParams prm = bottom_params();
         if (abec) {
-            k_bottom<T, true><<<njobs, bot_threads, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
+            launch(k_bottom<T, true>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr,
                                                                   bot_iters.p, bot_ret.p);
         } else {
-            k_bottom<T, false><<<njobs, bot_threads, 0, st()>>>(bot_levels.p, bot_jobs.p, prm, nullptr,
+            launch(k_bottom<T, false>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr,
                                                                    bot_iters.p, bot_ret.p);
         }
         launched();
@@ -824,7 +824,7 @@ void Engine::Impl::fcycle ()
         }
         MLMG_CUDA_CHECK(cudaMemcpyAsync(hold, cor, bytes, cudaMemcpyDeviceToDevice, st()));
         vcycle<T>(l);
-        k_add_to<T, T><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, hold, nullptr);
+        launch(k_add_to<T, T>, L.mg.ntiles, kTileBlock, 0, L.dl, L.mg.dev(), cor, hold, nullptr);
         launched();
     }
 }
@@ -877,18 +877,18 @@ void Engine::Impl::residual0 (bool to32)
         const unsigned g = (unsigned)L.all.ntiles;
         if (abec) {
             if (L.inline_bc) {
-                k_residual_s<double, float, true, true, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res32.p,
+                launch(k_residual_s<double, float, true, true, true>, g, kTileBlock, 0, L.dl, L.all.dev(), L.res32.p,
                     L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
             } else {
-                k_residual_s<double, float, true, false, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(),
+                launch(k_residual_s<double, float, true, false, true>, g, kTileBlock, 0, L.dl, L.all.dev(),
                     L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
             }
         } else {
             if (L.inline_bc) {
-                k_residual_s<double, float, false, true, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(),
+                launch(k_residual_s<double, float, false, true, true>, g, kTileBlock, 0, L.dl, L.all.dev(),
                     L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
             } else {
-                k_residual_s<double, float, false, false, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.all.dev(),
+                launch(k_residual_s<double, float, false, false, true>, g, kTileBlock, 0, L.dl, L.all.dev(),
                     L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
             }
         }
@@ -929,7 +929,7 @@ void Engine::Impl::one_iteration (bool fmg)
             launched(3);
         }
         if (fmg) { fcycle<float>(); } else { vcycle<float>(0); }
-        k_add_to<double, float><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.sol.p, L0.cor32.p,
+        launch(k_add_to<double, float>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.sol.p, L0.cor32.p,
                                                                         active_d.p);
         launched();
         if (timed) { kev_record(1); }
@@ -945,7 +945,7 @@ void Engine::Impl::one_iteration (bool fmg)
             launched(3);
         }
         if (fmg) { fcycle<double>(); } else { vcycle<double>(0); }
-        k_add_to<double, double><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.sol.p, L0.cor.p,
+        launch(k_add_to<double, double>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.sol.p, L0.cor.p,
                                                                          active_d.p);
         launched();
         residual0(false);
@@ -984,7 +984,7 @@ bool same_iteration (const EngineOptions& a, const EngineOptions& b)
            a.march_min_tiles == b.march_min_tiles && a.march_tz == b.march_tz && a.fused_tma == b.fused_tma &&
            a.fused_prefetch == b.fused_prefetch && a.max_fmg_iter == b.max_fmg_iter &&
            a.transpose == b.transpose && a.tma_first_wait == b.tma_first_wait &&
-           a.final_fill_bc == b.final_fill_bc;
+           a.final_fill_bc == b.final_fill_bc && a.pdl == b.pdl;
 }
 
 Engine::Engine (std::vector<SolveProblem> problems, const EngineOptions& opt, cudaStream_t stream)

@@ -55,6 +55,7 @@ struct EngineOptions {
                                 // a test knob: 0 makes every wait expire, which the solve reports as -7
     int final_fill_bc = 0;      // MLMGT::setFinalFillBC: a solution with more than one ghost layer also
                                 // gets its first ghost layer written back
+    int pdl = 1;                // V-cycle kernels as programmatic dependent launches
 };
 
 // true when two option sets capture the same iteration graph

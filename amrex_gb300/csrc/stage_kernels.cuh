@@ -264,6 +264,8 @@ k_restrict (DevLevel Lf, DevLevel Lc, Subset Sc, const T* __restrict__ fine, T* 
     const int pf = find_patch(Lf, s, 2 * c.x0, 2 * c.y0, 2 * c.z0);
     const PatchGeom F0 = geom_of(Lf.P[pf]);
     const bool one = contains(F0, 2 * xe + 1, 2 * ye + 1, 2 * ze + 1);
+    pdl_wait();
+    pdl_trigger();
     const int j = c.y0 + threadIdx.y;
     if (j > C.hi[1]) { return; }
     const T volfrac = T(1.0) / T(8);
@@ -306,6 +308,8 @@ k_interp_add (DevLevel Lf, Subset Sf, DevLevel Lc, const T* __restrict__ crse, T
     const int pc = find_patch(Lc, s, c.x0 >> 1, c.y0 >> 1, c.z0 >> 1);
     const PatchGeom C = geom_of(Lc.P[pc]);
     const bool one = contains(C, xe >> 1, ye >> 1, ze >> 1);
+    pdl_wait();
+    pdl_trigger();
     const int j = c.y0 + threadIdx.y;
     if (j > F.hi[1]) { return; }
     for (int kk = 0; kk < TILE_Z; ++kk) {
@@ -330,6 +334,8 @@ k_add_to (DevLevel L, Subset S, TD* __restrict__ dst, const TS* __restrict__ src
 {
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchGeom P = geom_of(L.P[c.p]);
+    pdl_wait();
+    pdl_trigger();
     const int j = c.y0 + threadIdx.y;
     if (j > P.hi[1]) { return; }
     if (active != nullptr && !active[P.solve]) { return; }

@@ -245,6 +245,8 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
     __shared__ double sm[32];
     const TileCoord c = decode_tile(L, Sb, blockIdx.x);
     const PatchDesc& P = L.P[c.p];
+    pdl_wait();
+    pdl_trigger();
     const int j = c.y0 + threadIdx.y;
     double mx = 0.0;
     unsigned long long mxb = 0ull;       // FP64: max |r| as the max of the sign-cleared bit patterns
