@@ -789,6 +789,7 @@ void AmrEngine::Impl::one_iter (int iter)
     // averageDownAndSync, AMReX_MLCellLinOp.H:2102-2122
     for (int l = fin; l > 0; --l) { avgdown(l - 1, L(l).sol.p, L(l - 1).sol.p); }
     fine_residual_and_norm();
+    I0.fetch_bottom_counts();
 }
 
 // ----------------------------------------------------------------- AmrEngine --

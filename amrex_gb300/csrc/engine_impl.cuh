@@ -224,6 +224,8 @@ struct Engine::Impl {
     template <typename T> void fcycle ();
     template <typename T> void correction_residual (int l);
     void bottom_done ();
+    void fetch_bottom_counts ();
+    int bottom_slot () const { return std::min(bslot, nlev_max + 1); }
     BottomParams bottom_params () const;
     void bottom_mode_init ();
     template <typename T> T* field_cor (int l);
@@ -234,9 +236,9 @@ struct Engine::Impl {
     StencilPtrs stencil32 (int l) const;
     StencilPtrs stencil64 (int l) const;
     void gsrb32 (int l, float* cor, const float* res, int rb);
-    void smooth_fused (int l, int n);
+    void smooth_fused (int l, int n, bool from_zero = false);
     void resid32 (int l, float* rescor, float* cor, const float* res);
-    void residual0 (bool to32);   // res[0] (FP64, or FP32 in mixed) and per-block max|r|
+    void residual0 (bool to32, bool norm_zeroed = false);   // res[0] (FP64, or FP32 in mixed) and its max-norm
     void one_iteration (bool fmg);
     // reads (and clears) the device-side error report of bounded waits; throws if set
     void check_device_error ()

@@ -55,7 +55,7 @@ template <bool VARC, bool TMA = false>
 __global__ void __launch_bounds__(FS_THREADS, 5)
 k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
                 const float* __restrict__ rhs, StencilPtrs Sc, const CUtensorMap* __restrict__ maps, int* err,
-                long long first_wait, const CUtensorMap* __restrict__ pf = nullptr)
+                long long first_wait, const CUtensorMap* __restrict__ pf = nullptr, int zero_in = 0)
 {
     __shared__ __align__(128) float A[FS_AZ][FS_AY][FS_AX];   // phi_in, local (x-4..x+35, y-2..y+9, z-2..z+9)
     __shared__ float N[FS_NZ][FS_NY][FS_NX];                    // first colour, local (x-1..x+32, y-1..y+8, z-1..z+8)
@@ -102,7 +102,7 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
             if (tid == 0) { atomicExch(err, tma::ERR_TMA_ALIGN); }
             return;
         }
-        if (tid == 0) {
+        if (tid == 0 && !zero_in) {
             tma::mbar_expect_tx(&bar, (unsigned)sizeof(A));
             tma::load_3d(&A[0][0][0], maps + pid, &bar, cx, cy, cz);
         }
@@ -110,11 +110,18 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
             // coordinates of the tile grown by one: never negative
             tma::prefetch_3d(pf + (size_t)pid * FS_PF_NMAP + (tid - 32), cx, cy + 1, cz + 1);
         }
-        const bool late = !tma::mbar_wait_bounded(&bar, 0, first_wait);
-        if (__syncthreads_or(late)) {
-            if (tid == 0) { atomicExch(err, tma::ERR_TMA_TIMEOUT); }
-            tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
-            return;
+        if (zero_in) {
+            // the first sweep of a V-cycle level starts from a zero correction
+            float* a = &A[0][0][0];
+            for (int u = tid; u < FS_AZ * FS_AY * FS_AX; u += FS_THREADS) { a[u] = 0.f; }
+            __syncthreads();
+        } else {
+            const bool late = !tma::mbar_wait_bounded(&bar, 0, first_wait);
+            if (__syncthreads_or(late)) {
+                if (tid == 0) { atomicExch(err, tma::ERR_TMA_TIMEOUT); }
+                tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
+                return;
+            }
         }
     } else {
     // ---- stage phi_in: 12 x 12 rows of 10 16-byte chunks; 250 threads, (ly, lz) advanced incrementally
@@ -128,7 +135,7 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
         for (int row = tid / CH; row < FS_AZ * FS_AY; row += RSTEP) {
             const int j = y0 - 2 + ly, k = z0 - 2 + lz;
             float* dst = &A[lz][ly][4 * ch];
-            if (x_ok && j >= P.lo[1] && j <= P.hi[1] && k >= P.lo[2] && k <= P.hi[2]) {
+            if (!zero_in && x_ok && j >= P.lo[1] && j <= P.hi[1] && k >= P.lo[2] && k <= P.hi[2]) {
                 cp_async16(dst, phi_in + P.idx(i, j, k));
             } else {
                 *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);

@@ -249,9 +249,10 @@ void Engine::Impl::build ()
     red_out.alloc((size_t)nsolve * 4 + 4);
     h_red.alloc((size_t)nsolve * 4 + 4);
     h_iters.alloc((size_t)nsolve * (nlev_max + 2) + 2);
-    bot_iters.alloc(nsolve);
-    bot_ret.alloc(nsolve);
-    bot_iters2.alloc(nsolve);
+    // one slot of nsolve counts per bottom solve of an iteration
+    bot_iters.alloc((size_t)nsolve * (nlev_max + 2));
+    bot_ret.alloc((size_t)nsolve * (nlev_max + 2));
+    bot_iters2.alloc((size_t)nsolve * (nlev_max + 2));
     bot_mode.alloc(nsolve);
     h_iters2.alloc((size_t)nsolve * (nlev_max + 2) + 2);
     active_d.alloc(nsolve);
@@ -572,7 +573,7 @@ void Engine::Impl::resid32 (int l, float* rescor, float* cor, const float* res)
 
 // n fused two-colour sweeps on level l (mixed path), ping-ponging between
 // cor32 and cor32b and ending in cor32
-void Engine::Impl::smooth_fused (int l, int n)
+void Engine::Impl::smooth_fused (int l, int n, bool from_zero)
 {
     LevelData& L = lev[l];
     const bool timed = E.m_opt.time_kernels && l == 0;
@@ -583,6 +584,7 @@ void Engine::Impl::smooth_fused (int l, int n)
     const bool use_tma = ma != nullptr;
     const StencilPtrs S = stencil32(l);
     for (int i = 0; i < n; ++i) {
+        const int zero = (from_zero && i == 0) ? 1 : 0;
         if (timed) { kev_record(); }
         if (L.march) {
             const dim3 blk(MS_TX / 2, MS_TY);
@@ -600,19 +602,19 @@ void Engine::Impl::smooth_fused (int l, int n)
             const long long fw = E.m_opt.tma_first_wait < 0 ? tma::WAIT_LIMIT : E.m_opt.tma_first_wait;
             if (abec) {
                 launch(k_sweep_fused2<true, true>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
-                                                                fw, pf);
+                                                                fw, pf, zero);
             } else {
                 launch(k_sweep_fused2<false, true>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
-                                                                 fw, pf);
+                                                                 fw, pf, zero);
             }
         } else {
             const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
             if (abec) {
                 launch(k_sweep_fused2<true>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p,
-                                                          tma::WAIT_LIMIT, nullptr);
+                                                          tma::WAIT_LIMIT, nullptr, zero);
             } else {
                 launch(k_sweep_fused2<false>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p,
-                                                           tma::WAIT_LIMIT, nullptr);
+                                                           tma::WAIT_LIMIT, nullptr, zero);
             }
         }
         launched();
@@ -684,13 +686,18 @@ void Engine::Impl::correction_residual (int l)
 // solve number bslot, to the host (MLMGT::m_niters_cg keeps one per solve)
 void Engine::Impl::bottom_done ()
 {
-    if (bslot < nlev_max + 2) {
-        MLMG_CUDA_CHECK(cudaMemcpyAsync(h_iters.p + (size_t)bslot * nsolve, bot_iters.p, sizeof(int) * nsolve,
-                                        cudaMemcpyDeviceToHost, st()));
-        MLMG_CUDA_CHECK(cudaMemcpyAsync(h_iters2.p + (size_t)bslot * nsolve, bot_iters2.p, sizeof(int) * nsolve,
-                                        cudaMemcpyDeviceToHost, st()));
-    }
     ++bslot;
+}
+
+// the bottom iteration counts of the iteration's bottom solves to the host,
+// once at the end of the iteration (a copy between the V-cycle's kernels
+// would stall their dependent launches)
+void Engine::Impl::fetch_bottom_counts ()
+{
+    const size_t n = (size_t)std::min(bslot, nlev_max + 2) * nsolve;
+    if (n == 0) { return; }
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(h_iters.p, bot_iters.p, sizeof(int) * n, cudaMemcpyDeviceToHost, st()));
+    MLMG_CUDA_CHECK(cudaMemcpyAsync(h_iters2.p, bot_iters2.p, sizeof(int) * n, cudaMemcpyDeviceToHost, st()));
 }
 
 // the per-solve bottom solver on the device: set from the option at the
@@ -709,7 +716,8 @@ BottomParams Engine::Impl::bottom_params () const
 {
     const EngineOptions& o = E.m_opt;
     return BottomParams{o.bottom_maxiter, o.bottom_reltol, o.bottom_abstol, o.nub, o.nuf,
-                        o.bottom_solver == BK_SMOOTHER ? 1 : 0, bot_mode.p, bot_iters2.p};
+                        o.bottom_solver == BK_SMOOTHER ? 1 : 0, bot_mode.p,
+                        bot_iters2.p + (size_t)bottom_slot() * nsolve};
 }
 
 // MLMGT::mgVcycle (AMReX_MLMG.H:1306-1415) from MG level `top`, one stage per
@@ -727,9 +735,12 @@ void Engine::Impl::vcycle (int top)
         T* cor = field_cor<T>(l);
         T* res = field_res<T>(l);
         T* rescor = field_rescor<T>(l);
-        MLMG_CUDA_CHECK(cudaMemsetAsync(cor, 0, (size_t)L.meta.nelem * sizeof(T), st()));
+        // the correction starts at zero: a fused level's first sweep takes
+        // that as given, every other level clears the array
+        const bool zero_sweep = std::is_same_v<T, float> && L.fused && !L.march && o.nu1 > 0;
+        if (!zero_sweep) { MLMG_CUDA_CHECK(cudaMemsetAsync(cor, 0, (size_t)L.meta.nelem * sizeof(T), st())); }
         if (std::is_same_v<T, float> && L.fused) {
-            smooth_fused(l, o.nu1);
+            smooth_fused(l, o.nu1, zero_sweep);
         } else {
             for (int i = 0; i < o.nu1; ++i) { smooth<T>(l, cor, res, i == 0); }
         }
@@ -742,17 +753,21 @@ void Engine::Impl::vcycle (int top)
     if (coarse) {
         if (abec) {
             k_coarse_vcycle<true><<<njobs, COARSE_THREADS, 0, st()>>>(coarse_lv.p, lc, bot_levels.p, bot_jobs.p, prm,
-                                                                      o.nu1, o.nu2, bot_iters.p, bot_ret.p);
+                                                                      o.nu1, o.nu2, bot_iters.p + (size_t)bottom_slot() * nsolve,
+                                                                      bot_ret.p + (size_t)bottom_slot() * nsolve);
         } else {
             k_coarse_vcycle<false><<<njobs, COARSE_THREADS, 0, st()>>>(coarse_lv.p, lc, bot_levels.p, bot_jobs.p, prm,
-                                                                       o.nu1, o.nu2, bot_iters.p, bot_ret.p);
+                                                                       o.nu1, o.nu2, bot_iters.p + (size_t)bottom_slot() * nsolve,
+                                                                      bot_ret.p + (size_t)bottom_slot() * nsolve);
         }
     } else if (abec) {
         launch(k_bottom<T, true>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr,
-                                                              bot_iters.p, bot_ret.p);
+                                                              bot_iters.p + (size_t)bottom_slot() * nsolve,
+                   bot_ret.p + (size_t)bottom_slot() * nsolve);
     } else {
         launch(k_bottom<T, false>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr,
-                                                               bot_iters.p, bot_ret.p);
+                                                               bot_iters.p + (size_t)bottom_slot() * nsolve,
+                   bot_ret.p + (size_t)bottom_slot() * nsolve);
     }
     launched();
     bottom_done();
@@ -791,10 +806,12 @@ void Engine::Impl::fcycle ()
         const BottomParams prm = bottom_params();
         if (abec) {
             launch(k_bottom<T, true>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr,
-                                                                  bot_iters.p, bot_ret.p);
+                                                                  bot_iters.p + (size_t)bottom_slot() * nsolve,
+                   bot_ret.p + (size_t)bottom_slot() * nsolve);
         } else {
             launch(k_bottom<T, false>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr,
-                                                                   bot_iters.p, bot_ret.p);
+                                                                   bot_iters.p + (size_t)bottom_slot() * nsolve,
+                   bot_ret.p + (size_t)bottom_slot() * nsolve);
         }
         launched();
         bottom_done();
@@ -824,7 +841,7 @@ void Engine::Impl::fcycle ()
         }
         MLMG_CUDA_CHECK(cudaMemcpyAsync(hold, cor, bytes, cudaMemcpyDeviceToDevice, st()));
         vcycle<T>(l);
-        launch(k_add_to<T, T>, L.mg.ntiles, kTileBlock, 0, L.dl, L.mg.dev(), cor, hold, nullptr);
+        launch(k_add_to<T, T>, L.mg.ntiles, kTileBlock, 0, L.dl, L.mg.dev(), cor, hold, nullptr, nullptr, 0);
         launched();
     }
 }
@@ -839,7 +856,7 @@ void Engine::Impl::reduce_per_solve (int l, const SubsetData& S, int op, const d
 
 // res[0] = rhs - L(sol) with the solution's BCs (solutionResidual,
 // AMReX_MLCellLinOp.H:1219-1236) and per-solve max|res| into red_out
-void Engine::Impl::residual0 (bool to32)
+void Engine::Impl::residual0 (bool to32, bool norm_zeroed)
 {
     LevelData& L = lev[0];
     if (E.m_opt.transpose) {
@@ -871,7 +888,7 @@ void Engine::Impl::residual0 (bool to32)
     if (to32) {
         // mixed path: FP64 residual in stencil form, FP32 copy for the V-cycle,
         // per-solve max-norm by atomic max (zeroed first)
-        MLMG_CUDA_CHECK(cudaMemsetAsync(red_out.p, 0, sizeof(double) * nsolve, st()));
+        if (!norm_zeroed) { MLMG_CUDA_CHECK(cudaMemsetAsync(red_out.p, 0, sizeof(double) * nsolve, st())); }
         if (!L.inline_bc) { ghost<double>(0, L.sol.p, true, true); }
         const StencilPtrs S = stencil64(0);
         const unsigned g = (unsigned)L.all.ntiles;
@@ -929,11 +946,12 @@ void Engine::Impl::one_iteration (bool fmg)
             launched(3);
         }
         if (fmg) { fcycle<float>(); } else { vcycle<float>(0); }
+        // phi += cor, which also clears the norms the residual takes its maximum into
         launch(k_add_to<double, float>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.sol.p, L0.cor32.p,
-                                                                        active_d.p);
+               active_d.p, red_out.p, nsolve);
         launched();
         if (timed) { kev_record(1); }
-        residual0(true);
+        residual0(true, true);
         if (timed) { kev_record(1); }
     } else {
         if (any_singular) {
@@ -946,11 +964,12 @@ void Engine::Impl::one_iteration (bool fmg)
         }
         if (fmg) { fcycle<double>(); } else { vcycle<double>(0); }
         launch(k_add_to<double, double>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.sol.p, L0.cor.p,
-                                                                         active_d.p);
+                                                                         active_d.p, nullptr, 0);
         launched();
         residual0(false);
     }
     MLMG_CUDA_CHECK(cudaMemcpyAsync(h_red.p, red_out.p, sizeof(double) * nsolve, cudaMemcpyDeviceToHost, st()));
+    fetch_bottom_counts();
 }
 
 // algorithmic bytes and FP64 operations of one outer residual launch of the

@@ -330,12 +330,16 @@ k_interp_add (DevLevel Lf, Subset Sf, DevLevel Lc, const T* __restrict__ crse, T
 // whose `active` flag is 0 are left untouched
 template <typename TD, typename TS>
 __global__ void __launch_bounds__(TILE_THREADS)
-k_add_to (DevLevel L, Subset S, TD* __restrict__ dst, const TS* __restrict__ src, const int* __restrict__ active)
+k_add_to (DevLevel L, Subset S, TD* __restrict__ dst, const TS* __restrict__ src, const int* __restrict__ active,
+          double* __restrict__ clear = nullptr, int nclear = 0)
 {
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchGeom P = geom_of(L.P[c.p]);
     pdl_wait();
     pdl_trigger();
+    if (blockIdx.x == 0 && threadIdx.y == 0) {
+        for (int t = threadIdx.x; t < nclear; t += 32) { clear[t] = 0.0; }
+    }
     const int j = c.y0 + threadIdx.y;
     if (j > P.hi[1]) { return; }
     if (active != nullptr && !active[P.solve]) { return; }
