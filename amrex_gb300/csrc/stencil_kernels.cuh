@@ -248,7 +248,7 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
     pdl_wait();
     pdl_trigger();
     const int j = c.y0 + threadIdx.y;
-    double mx = 0.0;
+    float mxf = 0.f;                     // FP32: max |r|
     unsigned long long mxb = 0ull;       // FP64: max |r| as the max of the sign-cleared bit patterns
     if (j <= P.hi[1]) {
         for (int kk = 0; kk < TILE_Z; ++kk) {
@@ -287,8 +287,10 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
                     // residual orders above every number and reaches the norm)
                     const unsigned long long ab = abs_bits(v);
                     mxb = (ab > mxb) ? ab : mxb;
-                } else {
-                    mx = max_nan(mx, fabs((double)v));
+                } else if (norm != nullptr) {
+                    // FP32 max of |v| (NaN kept), widened once per block
+                    const float av = fabsf(v);
+                    mxf = (av > mxf || av != av) ? av : mxf;
                 }
             }
         }
@@ -298,7 +300,7 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
         if constexpr (std::is_same_v<T, double>) {
             red = __longlong_as_double((long long)block_max_bits(mxb, sm));
         } else {
-            red = block_reduce(mx, RED_MAXABS, sm);
+            red = block_reduce((double)mxf, RED_MAXABS, sm);
         }
         if (threadIdx.x == 0 && threadIdx.y == 0) { atomic_max_nonneg(&norm[P.solve], red); }
     }
