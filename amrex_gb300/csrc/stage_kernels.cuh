@@ -312,16 +312,31 @@ k_interp_add (DevLevel Lf, Subset Sf, DevLevel Lc, const T* __restrict__ crse, T
     pdl_trigger();
     const int j = c.y0 + threadIdx.y;
     if (j > F.hi[1]) { return; }
+    // all of the thread's loads first, then the sums and stores
+    T f[TILE_Z][2], v[TILE_Z][2];
+    bool ok[TILE_Z][2];
+    long long qf[TILE_Z][2];
+#pragma unroll
     for (int kk = 0; kk < TILE_Z; ++kk) {
-        const int k = c.z0 + kk;
-        if (k > F.hi[2]) { break; }
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            const int i = c.x0 + threadIdx.x + 32 * h;
-            if (i > F.hi[0]) { continue; }
-            const int ic = i >> 1, jc = j >> 1, kc = k >> 1;
-            const long long qc = one ? cidx(C, ic, jc, kc) : cidx(Lc.P[find_patch(Lc, s, ic, jc, kc)], ic, jc, kc);
-            fine[cidx(F, i, j, k)] += crse[qc];
+            const int i = c.x0 + threadIdx.x + 32 * h, k = c.z0 + kk;
+            ok[kk][h] = (k <= F.hi[2]) && (i <= F.hi[0]);
+            qf[kk][h] = cidx(F, i, j, k);
+            f[kk][h] = T(0); v[kk][h] = T(0);
+            if (ok[kk][h]) {
+                const int ic = i >> 1, jc = j >> 1, kc = k >> 1;
+                const long long qc = one ? cidx(C, ic, jc, kc) : cidx(Lc.P[find_patch(Lc, s, ic, jc, kc)], ic, jc, kc);
+                f[kk][h] = fine[qf[kk][h]];
+                v[kk][h] = crse[qc];
+            }
+        }
+    }
+#pragma unroll
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (ok[kk][h]) { fine[qf[kk][h]] = f[kk][h] + v[kk][h]; }
         }
     }
 }
@@ -343,18 +358,31 @@ k_add_to (DevLevel L, Subset S, TD* __restrict__ dst, const TS* __restrict__ src
     const int j = c.y0 + threadIdx.y;
     if (j > P.hi[1]) { return; }
     if (active != nullptr && !active[P.solve]) { return; }
+    // all of the thread's loads first, then the sums and stores
+    const long long q0 = cidx(P, c.x0 + threadIdx.x, j, c.z0);
+    TD d[TILE_Z][2];
+    TS v[TILE_Z][2];
+    bool ok[TILE_Z][2];
+#pragma unroll
     for (int kk = 0; kk < TILE_Z; ++kk) {
-        const int k = c.z0 + kk;
-        if (k > P.hi[2]) { break; }
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            const int i = c.x0 + threadIdx.x + 32 * h;
-            if (i > P.hi[0]) { continue; }
-            const long long q = cidx(P, i, j, k);
+            ok[kk][h] = (c.z0 + kk <= P.hi[2]) && (c.x0 + threadIdx.x + 32 * h <= P.hi[0]);
+            const long long q = q0 + kk * P.sxy + 32 * h;
+            d[kk][h] = ok[kk][h] ? dst[q] : TD(0);
+            v[kk][h] = ok[kk][h] ? src[q] : TS(0);
+        }
+    }
+#pragma unroll
+    for (int kk = 0; kk < TILE_Z; ++kk) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (!ok[kk][h]) { continue; }
+            const long long q = q0 + kk * P.sxy + 32 * h;
             if constexpr (std::is_same_v<TD, double> && std::is_same_v<TS, float>) {
-                dst[q] += f2d_bits(src[q]);
+                dst[q] = d[kk][h] + f2d_bits(v[kk][h]);
             } else {
-                dst[q] += TD(src[q]);
+                dst[q] = d[kk][h] + TD(v[kk][h]);
             }
         }
     }
