@@ -78,6 +78,14 @@ struct AmrLevelData {
     DevBuf<double> bcor;                    // boundary values of the correction (physical slots 0)
     DevBuf<long long> nbr;                  // per Dirichlet-value slot: element of the covering patch's cell, or -1
                                             // (colour passes without ghost fills; empty if a closure has 4 points)
+    // fused two-colour sweeps of the level (MLPoisson, FP32 corrections): the
+    // fused-sweep tiles whose halo meets no face shared with another patch,
+    // the others (colour passes), the sweeps' second buffer and tensor maps
+    // (per patch, over the correction, the hold and the second buffer)
+    DevBuf<int4> fz_safe, fz_rest;
+    int nsafe = 0, nrest = 0;
+    DevBuf<float> fz_buf;
+    DevBuf<CUtensorMap> fz_maps;
     DevBuf<double> hold64;                  // cor_hold of the AMR level
     DevBuf<float> hold32;
     void* cor_p = nullptr;                  // the level's correction buffer (swapped with the hold)
@@ -139,6 +147,7 @@ struct AmrEngine::Impl {
     template <typename T> T* cor (int l);
     template <typename T> T* hold (int l);
     template <typename T> void mini_cycle (int l, const T* rhs);
+    void build_fused_tiles (int l, const std::vector<long long>& nb);
     template <typename T, typename TB, typename TO> void cor_residual (int l, bool inhomog, const TB* b, TO* out);
     template <typename T> void one_iter (int iter);
     void norm_start (int l, const double* x, bool masked, int slot);
@@ -368,7 +377,65 @@ void AmrEngine::Impl::build_fine_tables (int l)
             }
         }
         D.nbr.upload(nb, st());
+        if (mixed() && A.m_opt.fused_smoother && A.m_opt.fused_fine) { build_fused_tiles(l, nb); }
     }
+}
+
+// The fused-sweep tiles of fine level l: a tile is safe when no face of its
+// patch that its halo (the tile grown by one) reaches has a ghost covered by
+// another patch within that halo's extent; such a tile's two colours can run
+// in one fused sweep.  The others get colour passes.
+void AmrEngine::Impl::build_fused_tiles (int l, const std::vector<long long>& nb)
+{
+    AmrLevelData& D = lev[l];
+    LevelData& Ld = L(l);
+    const PatchLevel& M = Ld.meta;
+    std::vector<int4> safe, rest;
+    for (int p = 0; p < (int)M.patches.size(); ++p) {
+        const PatchDesc& P = M.patches[p];
+        const int nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1;
+        const int tdim[3] = {FS_TX, FS_TY, FS_TZ};
+        for (int z0 = P.lo[2]; z0 <= P.hi[2]; z0 += FS_TZ)
+        for (int y0 = P.lo[1]; y0 <= P.hi[1]; y0 += FS_TY)
+        for (int x0 = P.lo[0]; x0 <= P.hi[0]; x0 += FS_TX) {
+            const int t0[3] = {x0, y0, z0};
+            // the tile + 1 clipped to the patch
+            int a[3], b[3];
+            for (int d = 0; d < 3; ++d) {
+                a[d] = std::max(P.lo[d], t0[d] - 1);
+                b[d] = std::min(P.hi[d], t0[d] + tdim[d]);
+            }
+            bool ok = true;
+            for (int f = 0; f < 6 && ok; ++f) {
+                const int d = f % 3;
+                const bool reach = (f < 3) ? (t0[d] == P.lo[d]) : (t0[d] + tdim[d] >= P.hi[d]);
+                if (!reach) { continue; }
+                const int e1 = (d == 0) ? 1 : 0, e2 = (d == 2) ? 1 : 2;
+                const int n1 = (d == 0) ? ny : nx;
+                for (int v = a[e2]; v <= b[e2] && ok; ++v) {
+                    for (int w = a[e1]; w <= b[e1] && ok; ++w) {
+                        const long long u = (long long)(v - P.lo[e2]) * n1 + (w - P.lo[e1]);
+                        if (nb[(size_t)(P.face[f].bcval_off + u)] >= 0) { ok = false; }
+                    }
+                }
+            }
+            (ok && A.m_opt.fused_fine == 1 ? safe : rest).push_back(make_int4(p, x0, y0, z0));
+        }
+    }
+    D.nsafe = (int)safe.size();
+    D.nrest = (int)rest.size();
+    D.fz_safe.upload(safe, st());
+    D.fz_rest.upload(rest, st());
+    D.fz_buf.alloc((size_t)M.nelem);
+    D.fz_buf.zero(st());
+    const size_t np = M.patches.size();
+    std::vector<CUtensorMap> maps(3 * np);
+    for (size_t p = 0; p < np; ++p) {
+        maps[p] = patch_tensor_map(Ld.cor32.p, M.patches[p]);
+        maps[np + p] = D.hold32.p ? patch_tensor_map(D.hold32.p, M.patches[p]) : maps[p];
+        maps[2 * np + p] = patch_tensor_map(D.fz_buf.p, M.patches[p]);
+    }
+    D.fz_maps.upload(maps, st());
 }
 
 void AmrEngine::Impl::build_coarse_tables (int c)
@@ -654,6 +721,41 @@ void AmrEngine::Impl::mini_cycle (int l, const T* rhs)
     T* x = cor<T>(l);
     LevelData& Ld = L(l);
     MLMG_CUDA_CHECK(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)Ld.meta.nelem, st()));
+    AmrLevelData& D = lev[l];
+    if constexpr (std::is_same_v<T, float>) {
+        if (D.nsafe + D.nrest > 0) {
+            // fused two-colour sweeps on the safe tiles, colour passes on the
+            // rest: both read the old buffer and write the new one, the
+            // second colour of the rest then reads the new buffer
+            const dim3 blk(FS_TX, FS_TY);
+            const size_t np = Ld.meta.patches.size();
+            int* err = lev[0].I->err_d.p;
+            float* a = x;
+            float* b = D.fz_buf.p;
+            auto maps_of = [&] (const float* f) {
+                const size_t w = (f == Ld.cor32.p) ? 0 : ((f == D.hold32.p) ? 1 : 2);
+                return D.fz_maps.p + w * np;
+            };
+            for (int i = 0; i < A.m_opt.nu1; ++i) {
+                if (D.nsafe > 0) {
+                    k_sweep_fused2<false, true><<<D.nsafe, blk, 0, st()>>>(Ld.dl, Ld.mg.dev(), a, b, rhs, StencilPtrs{},
+                        maps_of(a), err, tma::WAIT_LIMIT, nullptr, 0, D.fz_safe.p);
+                    launched();
+                }
+                if (D.nrest > 0) {
+                    k_gsrb_tiles<<<D.nrest, blk, 0, st()>>>(Ld.dl, D.fz_rest.p, a, a, b, rhs, D.nbr.p, 0);
+                    k_gsrb_tiles<<<D.nrest, blk, 0, st()>>>(Ld.dl, D.fz_rest.p, a, b, b, rhs, D.nbr.p, 1);
+                    launched(2);
+                }
+                std::swap(a, b);
+            }
+            if (a != x) {
+                MLMG_CUDA_CHECK(cudaMemcpyAsync(x, a, sizeof(float) * (size_t)Ld.meta.nelem, cudaMemcpyDeviceToDevice,
+                                                st()));
+            }
+            return;
+        }
+    }
     if (lev[l].nbr.p != nullptr) {
         // colour passes reading covered neighbours directly: no ghost fills
         for (int i = 0; i < A.m_opt.nu1; ++i) {

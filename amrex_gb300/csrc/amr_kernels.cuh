@@ -254,7 +254,15 @@ k_amr_norm (DevLevel L, Subset S, const T* __restrict__ x, const int8_t* __restr
                 const int i = c.x0 + threadIdx.x + 32 * h;
                 if (i > P.hi[0]) { continue; }
                 const long long q = cidx(P, i, j, k);
-                if (covered == nullptr || covered[q] == 0) { acc = max_nan(acc, fabs((double)x[q])); }
+                if (covered == nullptr || covered[q] == 0) {
+                    if constexpr (std::is_same_v<T, double>) {
+                        // integer max of the |x| bit patterns (NaN orders above every number)
+                        const unsigned long long ab = abs_bits(x[q]), cur = (unsigned long long)__double_as_longlong(acc);
+                        acc = __longlong_as_double((long long)((ab > cur) ? ab : cur));
+                    } else {
+                        acc = max_nan(acc, fabs((double)x[q]));
+                    }
+                }
             }
         }
     }
@@ -276,6 +284,7 @@ k_amr_resid (DevLevel L, Subset S, TO* __restrict__ r, const TX* __restrict__ x,
     const PatchDesc& P = L.P[c.p];
     const int j = c.y0 + threadIdx.y;
     if (j > P.hi[1]) { return; }
+    const TX pdhx = convert<TX>(P.dha[0]), pdhy = convert<TX>(P.dha[1]), pdhz = convert<TX>(P.dha[2]);
     for (int kk = 0; kk < TILE_Z; ++kk) {
         const int k = c.z0 + kk;
         if (k > P.hi[2]) { break; }
@@ -286,7 +295,12 @@ k_amr_resid (DevLevel L, Subset S, TO* __restrict__ r, const TX* __restrict__ x,
             const long long q = cidx(P, i, j, k);
             TX ax;
             if constexpr (!ABEC) {
-                ax = adotx_cell<TX, false>(P, q, x, nullptr, nullptr, nullptr, nullptr);
+                // adotx_cell's MLPoisson form with the factors converted once per block
+                const long long sx = P.sx, sxy = P.sxy;
+                const TX xc = x[q];
+                ax = pdhx * (x[q - 1] - TX(2.0) * xc + x[q + 1])
+                   + pdhy * (x[q - sx] - TX(2.0) * xc + x[q + sx])
+                   + pdhz * (x[q - sxy] - TX(2.0) * xc + x[q + sxy]);
             } else if constexpr (std::is_same_v<TX, double>) {
                 ax = adotx_cell<double, true>(P, q, x, a, bx, by, bz);
             } else {
@@ -296,7 +310,7 @@ k_amr_resid (DevLevel L, Subset S, TO* __restrict__ r, const TX* __restrict__ x,
                 ax = cf.d * x[q] - (cf.sxl * x[q - 1] + cf.sxh * x[q + 1] + cf.syl * x[q - sx] + cf.syh * x[q + sx]
                                     + cf.szl * x[q - sxy] + cf.szh * x[q + sxy]);
             }
-            r[q] = TO(TX(b[q]) - ax);
+            r[q] = convert<TO>(TX(convert<TX>(b[q])) - ax);
         }
     }
 }

@@ -1287,6 +1287,10 @@ int mlmg_set_option (mlmg_solver s, const char* name, double value)
     else if (n == "fused_tma") { s->opt.fused_tma = value != 0.0; }
     else if (n == "fused_prefetch") { s->opt.fused_prefetch = value != 0.0; }
     else if (n == "pdl") { s->opt.pdl = value != 0.0; }
+    else if (n == "fused_fine") {
+        MLMG_REQUIRE(value >= 0 && value <= 2, ERR_ARGS, "fused_fine must be 0, 1 or 2");
+        s->opt.fused_fine = (int)value;
+    }
     else if (n == "tma_wait_limit") {
         MLMG_REQUIRE(value >= -1, ERR_ARGS, "tma_wait_limit must be >= 0 (or -1: the default bound)");
         s->opt.tma_first_wait = (long long)value;
@@ -1303,6 +1307,7 @@ int mlmg_set_option (mlmg_solver s, const char* name, double value)
     // layout-changing knobs take effect at the next engine build
     s->eng.reset();
     s->batch_eng.reset();
+    s->amr_eng.reset();
     API_END
 }
 

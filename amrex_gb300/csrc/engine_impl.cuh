@@ -57,6 +57,11 @@ inline void build_subset (SubsetData& S, const PatchLevel& PL, const std::vector
 }
 
 
+// 3-D tiled tensor map over the allocation of patch P inside an FP32 level
+// field (the fused sweep's staging box by default)
+CUtensorMap patch_tensor_map (const float* field, const PatchDesc& P, int by = FS_AY, int bz = FS_AZ,
+                              int bx = FS_AX);
+
 struct LevelData {
     PatchLevel meta;
     DevBuf<PatchDesc> P;

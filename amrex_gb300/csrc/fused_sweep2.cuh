@@ -55,7 +55,8 @@ template <bool VARC, bool TMA = false>
 __global__ void __launch_bounds__(FS_THREADS, 5)
 k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* __restrict__ phi_out,
                 const float* __restrict__ rhs, StencilPtrs Sc, const CUtensorMap* __restrict__ maps, int* err,
-                long long first_wait, const CUtensorMap* __restrict__ pf = nullptr, int zero_in = 0)
+                long long first_wait, const CUtensorMap* __restrict__ pf = nullptr, int zero_in = 0,
+                const int4* __restrict__ tiles = nullptr)
 {
     __shared__ __align__(128) float A[FS_AZ][FS_AY][FS_AX];   // phi_in, local (x-4..x+35, y-2..y+9, z-2..z+9)
     __shared__ float N[FS_NZ][FS_NY][FS_NX];                    // first colour, local (x-1..x+32, y-1..y+8, z-1..z+8)
@@ -64,7 +65,11 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
     const int tid = threadIdx.y * FS_TX + threadIdx.x;
     int x0, y0, z0, pid;
     {
-        const TileCoord c = decode_fused_tile(L, S, blockIdx.x);
+        // the tile: from the level's tile map, or (an AMR fine level) from a
+        // list of the tiles whose halo meets no face shared with another patch
+        const TileCoord c = (tiles != nullptr)
+            ? TileCoord{tiles[blockIdx.x].x, tiles[blockIdx.x].y, tiles[blockIdx.x].z, tiles[blockIdx.x].w}
+            : decode_fused_tile(L, S, blockIdx.x);
         x0 = c.x0; y0 = c.y0; z0 = c.z0; pid = c.p;
         if (tid == 0) {
             const PatchDesc& P = L.P[c.p];
@@ -304,6 +309,79 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
         }
     };
     if (touches) { sweep(std::true_type{}); } else { sweep(std::false_type{}); }
+}
+
+// One colour of MLPoisson's Gauss-Seidel sweep over a list of fused-sweep
+// tiles of an AMR fine level (the tiles whose halo meets a face shared with
+// another patch): old cell values from `old` (null: a zero correction),
+// neighbours from `nb` (the old array for the first colour, the new one for
+// the second), results into `out`.  A ghost covered by another patch is that
+// patch's cell (nbr), any other ghost the homogeneous closure; the update is
+// the fused sweep's arithmetic, so a cell gets the value the fused sweep gives
+// it from the same neighbours.  Launched for the first colour over these tiles
+// together with the fused sweep over the others (both read only the old
+// array), then for the second colour.
+static __global__ void __launch_bounds__(FS_THREADS)
+k_gsrb_tiles (DevLevel L, const int4* __restrict__ tiles, const float* __restrict__ old, const float* __restrict__ nb,
+              float* __restrict__ out, const float* __restrict__ rhs, const long long* __restrict__ nbr, int rb)
+{
+    const int4 t = tiles[blockIdx.x];
+    const PatchDesc& P = L.P[t.x];
+    pdl_wait();
+    pdl_trigger();
+    // lanes 0..15 take the 16 cells of the colour in a row of plane lz, lanes
+    // 16..31 those of plane lz + 1
+    const int j = t.z + threadIdx.y;
+    const int half = threadIdx.x >> 4, r = threadIdx.x & 15;
+    if (j > P.hi[1]) { return; }
+    const float dhx = float(P.dha[0]), dhy = float(P.dha[1]), dhz = float(P.dha[2]);
+    const float cdx = -dhx, cdy = -dhy, cdz = -dhz, cd = -2.0f * (dhx + dhy + dhz);
+    const long long sx = P.sx, sxy = P.sxy;
+    auto val = [&] (const float* a, long long q) -> float { return (a != nullptr) ? a[q] : 0.0f; };
+    // the ghost across face f: the covering patch's cell, or the closure
+    // (which also adds the face's diagonal term, s_f * fco_f, to corr)
+    auto ghost = [&] (int f, int i, int k, float pc, long long qin, float s, float& corr) -> float {
+        const long long v = nbr[P.face[f].bcval_off + face_local(P, f, i, j, k)];
+        if (v >= 0) { return val(nb, v); }
+        const FaceBC& F = P.face[f];
+        const float pin = val(nb, qin);
+        float g = 0.0f;
+        if (F.type == BC_DIRICHLET) {
+            const float c1 = float(F.coef[1]), c2 = float(F.coef[2]);
+            g = (F.nx >= 2) ? pc * c1 : 0.0f;
+            if (F.nx >= 3) { g += pin * c2; }
+        } else if (F.type == BC_NEUMANN) {
+            g = pc;
+        } else if (F.type == BC_REFLECT_ODD) {
+            g = -pc;
+        }
+        corr += s * float(F.fco);
+        return g;
+    };
+    for (int lz = half; lz < FS_TZ; lz += 2) {
+        const int k = t.w + lz;
+        if (k > P.hi[2]) { break; }
+        const int i = t.y + 2 * r + ((t.y + j + k + rb) & 1);
+        if (i > P.hi[0]) { continue; }
+        const long long q = cidx(P, i, j, k);
+        const float pc = val(old, q);
+        // the closures' diagonal terms accumulate in the fused sweep's order
+        // (x-lo, x-hi, y-lo, y-hi, z-lo, z-hi)
+        float corr = 0.0f;
+        const float xm = (i == P.lo[0]) ? ghost(0, i, k, pc, q + 1, cdx, corr) : val(nb, q - 1);
+        const float xp = (i == P.hi[0]) ? ghost(3, i, k, pc, q - 1, cdx, corr) : val(nb, q + 1);
+        const float ym = (j == P.lo[1]) ? ghost(1, i, k, pc, q + sx, cdy, corr) : val(nb, q - sx);
+        const float yp = (j == P.hi[1]) ? ghost(4, i, k, pc, q - sx, cdy, corr) : val(nb, q + sx);
+        const float zm = (k == P.lo[2]) ? ghost(2, i, k, pc, q + sxy, cdz, corr) : val(nb, q - sxy);
+        const float zp = (k == P.hi[2]) ? ghost(5, i, k, pc, q - sxy, cdz, corr) : val(nb, q + sxy);
+        const bool face = (i == P.lo[0]) | (i == P.hi[0]) | (j == P.lo[1]) | (j == P.hi[1]) | (k == P.lo[2]) |
+                          (k == P.hi[2]);
+        const float gmd = face ? cd - corr : cd;
+        const float d = cd, sxl = cdx, sxh = cdx, syl = cdy, syh = cdy, szl = cdz, szh = cdz;
+        const float rho = sxl * xm + sxh * xp + syl * ym + syh * yp + szl * zm + szh * zp;
+        const float res = __ldg(rhs + q) - (d * pc - rho);
+        out[q] = pc + relax_factor(gmd) * res;
+    }
 }
 
 } // namespace mlmg

@@ -26,11 +26,14 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder ()
     return fn;
 }
 
+
+} // namespace
+
 // 3-D tiled tensor map over the allocation of patch P inside an FP32 level
 // field: x over the whole padded row (sx), y and z over the rows and planes
 // with their ghost layers; box bx x by x bz floats (default: a fused sweep's
 // 40 x 12 x 12 staging box)
-CUtensorMap patch_tensor_map (const float* field, const PatchDesc& P, int by = FS_AY, int bz = FS_AZ, int bx = FS_AX)
+CUtensorMap patch_tensor_map (const float* field, const PatchDesc& P, int by, int bz, int bx)
 {
     const long long start = P.base - P.sxy - P.sx - XOFF;      // first element of the patch's allocation
     const int ny = P.hi[1] - P.lo[1] + 1, nz = P.hi[2] - P.lo[2] + 1;
@@ -46,8 +49,6 @@ CUtensorMap patch_tensor_map (const float* field, const PatchDesc& P, int by = F
     MLMG_REQUIRE(r == CUDA_SUCCESS, ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     return m;
 }
-
-} // namespace
 
 // -------------------------------------------------------------- fields ----
 template <> double* Engine::Impl::field_cor<double> (int l) { return lev[l].cor.p; }
@@ -602,19 +603,19 @@ void Engine::Impl::smooth_fused (int l, int n, bool from_zero)
             const long long fw = E.m_opt.tma_first_wait < 0 ? tma::WAIT_LIMIT : E.m_opt.tma_first_wait;
             if (abec) {
                 launch(k_sweep_fused2<true, true>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
-                                                                fw, pf, zero);
+                                                                fw, pf, zero, nullptr);
             } else {
                 launch(k_sweep_fused2<false, true>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, ma, err_d.p,
-                                                                 fw, pf, zero);
+                                                                 fw, pf, zero, nullptr);
             }
         } else {
             const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
             if (abec) {
                 launch(k_sweep_fused2<true>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p,
-                                                          tma::WAIT_LIMIT, nullptr, zero);
+                                                          tma::WAIT_LIMIT, nullptr, zero, nullptr);
             } else {
                 launch(k_sweep_fused2<false>, g, blk, 0, L.dl, L.fz.dev(), a, b, L.res32.p, S, nullptr, err_d.p,
-                                                           tma::WAIT_LIMIT, nullptr, zero);
+                                                           tma::WAIT_LIMIT, nullptr, zero, nullptr);
             }
         }
         launched();
@@ -1003,7 +1004,7 @@ bool same_iteration (const EngineOptions& a, const EngineOptions& b)
            a.march_min_tiles == b.march_min_tiles && a.march_tz == b.march_tz && a.fused_tma == b.fused_tma &&
            a.fused_prefetch == b.fused_prefetch && a.max_fmg_iter == b.max_fmg_iter &&
            a.transpose == b.transpose && a.tma_first_wait == b.tma_first_wait &&
-           a.final_fill_bc == b.final_fill_bc && a.pdl == b.pdl;
+           a.final_fill_bc == b.final_fill_bc && a.pdl == b.pdl && a.fused_fine == b.fused_fine;
 }
 
 Engine::Engine (std::vector<SolveProblem> problems, const EngineOptions& opt, cudaStream_t stream)

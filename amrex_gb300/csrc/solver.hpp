@@ -56,6 +56,9 @@ struct EngineOptions {
     int final_fill_bc = 0;      // MLMGT::setFinalFillBC: a solution with more than one ghost layer also
                                 // gets its first ghost layer written back
     int pdl = 1;                // V-cycle kernels as programmatic dependent launches
+    int fused_fine = 1;         // AMR fine levels (MLPoisson, mixed): fused sweeps on the tiles whose halo
+                                // meets no face shared with another patch, colour passes on the rest
+                                // (2: colour passes on every tile; 0: the per-level colour passes)
 };
 
 // true when two option sets capture the same iteration graph

@@ -80,6 +80,19 @@ __device__ __forceinline__ unsigned long long abs_bits (double v)
     return ((unsigned long long)((unsigned)__double2hiint(v) & 0x7fffffffu) << 32) | (unsigned)__double2loint(v);
 }
 
+// TD(v) with the FP32 <-> FP64 cases on the integer pipe
+template <typename TD, typename TS>
+__device__ __forceinline__ TD convert (TS v)
+{
+    if constexpr (std::is_same_v<TD, double> && std::is_same_v<TS, float>) {
+        return f2d_bits(v);
+    } else if constexpr (std::is_same_v<TD, float> && std::is_same_v<TS, double>) {
+        return d2f_bits(v);
+    } else {
+        return TD(v);
+    }
+}
+
 // ------------------------------------------------------------ reductions --
 enum RedOp : int { RED_MAXABS = 0, RED_DOT = 1, RED_SUM = 2 };
 

@@ -248,6 +248,10 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
     pdl_wait();
     pdl_trigger();
     const int j = c.y0 + threadIdx.y;
+    // MLPoisson: the constant stencil, formed once (the cell loop would
+    // otherwise repeat its FP64 arithmetic for every cell)
+    Coef7<T, VARC> cc{};
+    if constexpr (!VARC) { cc = load_coef<T, false>(P, 0, S); }
     float mxf = 0.f;                     // FP32: max |r|
     unsigned long long mxb = 0ull;       // FP64: max |r| as the max of the sign-cleared bit patterns
     if (j <= P.hi[1]) {
@@ -262,7 +266,8 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
                 const T xc = x[q];
                 T xm, xp, ym, yp, zm, zp;
                 neighbours<T, INLINE_BC, INHOMOG>(P, P, i, j, k, q, x, xc, bcval, xm, xp, ym, yp, zm, zp);
-                const Coef7<T, VARC> cf = load_coef<T, VARC>(P, q, S);
+                Coef7<T, VARC> cf;
+                if constexpr (VARC) { cf = load_coef<T, true>(P, q, S); } else { cf = cc; }
                 T v;
                 if constexpr (std::is_same_v<T, double>) {
                     // seven FMAs (b - D x, then + s x_nb) and nothing else on

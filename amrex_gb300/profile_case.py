@@ -35,6 +35,9 @@ def run_amr(args):
     P = workloads.amr_problem(case["n"], grids, case["rhs_seed"], precision={"fp64": 0, "mixed": 1}[args.mode],
                               graph=args.graph, fused=args.fused)
     m = P["mlmg"]
+    for kv in args.opt:
+        k, v = kv.split("=")
+        m.setOption(k, float(v))
     for s in range(args.solves):
         for x in P["sols"]:
             x.setVal(0.0)

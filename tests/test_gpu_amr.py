@@ -27,7 +27,7 @@ def _phi_error(g, lev, got):
     return np.abs(got[ac.sample_index(got.size, lev)] - g[f"phi_l{lev}_sample"]).max() / st[0]
 
 
-def _solve(name, precision=0, graph=False, tol_rel=None, fused=False):
+def _solve(name, precision=0, graph=False, tol_rel=None, fused=False, options=None):
     g = ac.load("amrsolve", name)
     case, grids = g["case"], g["grids"]
     solbc = [ac.level_solbc(case, lev) for lev in range(len(grids))]
@@ -36,6 +36,8 @@ def _solve(name, precision=0, graph=False, tol_rel=None, fused=False):
                               agg_grid_size=case.get("agg_grid_size", 32), con_grid_size=case.get("con_grid_size", 32),
                               fused=fused, solbc=solbc, max_fmg_iter=case.get("max_fmg_iter", 0), abec=abec,
                               periodic=case.get("periodic", (0, 0, 0)))
+    for k, v in (options or {}).items():
+        P["mlmg"].setOption(k, v)
     resid = P["mlmg"].solve(P["sols"], P["rhss"], tol_rel or case.get("tol_rel", 1e-10), 0.0)
     phis = []
     for lev, boxes in enumerate(grids):
@@ -76,6 +78,20 @@ def test_amr_mixed_reaches_target(name, graph, fused):
     for lev in range(len(phis)):
         err = _phi_error(g, lev, phis[lev])
         assert err < 1e-8, (lev, err)
+
+
+@pytest.mark.parametrize("name", ["c2_n16_2lev", "c2_n32", "c2_n16_2lev_bc", "c2_n16_2lev_per", "c2_n32_fmg",
+                                  "c2_n16_4lev"])
+def test_amr_fused_fine_sweeps_bitwise(name):
+    """On the fine AMR levels, fused two-colour sweeps on the tiles whose halo
+    meets no face shared with another patch, with colour passes on the other
+    tiles, give the solution of colour passes on every tile bit for bit."""
+    _, P1, r1, phis1 = _solve(name, precision=1, graph=True, fused=True, options={"fused_fine": 1})
+    _, P2, r2, phis2 = _solve(name, precision=1, graph=True, fused=True, options={"fused_fine": 2})
+    assert P1["mlmg"].getNumIters() == P2["mlmg"].getNumIters()
+    assert r1 == r2
+    for a, b in zip(phis1, phis2):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_amr_graph_replay_matches_eager_fp64():
