@@ -720,10 +720,13 @@ void AmrEngine::Impl::mini_cycle (int l, const T* rhs)
 {
     T* x = cor<T>(l);
     LevelData& Ld = L(l);
-    MLMG_CUDA_CHECK(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)Ld.meta.nelem, st()));
     AmrLevelData& D = lev[l];
+    const bool fused = std::is_same_v<T, float> && D.nsafe + D.nrest > 0 && A.m_opt.nu1 > 0;
+    // the correction starts at zero: the fused sweeps' first one takes that
+    // as given, the other paths clear the array
+    if (!fused) { MLMG_CUDA_CHECK(cudaMemsetAsync(x, 0, sizeof(T) * (size_t)Ld.meta.nelem, st())); }
     if constexpr (std::is_same_v<T, float>) {
-        if (D.nsafe + D.nrest > 0) {
+        if (fused) {
             // fused two-colour sweeps on the safe tiles, colour passes on the
             // rest: both read the old buffer and write the new one, the
             // second colour of the rest then reads the new buffer
@@ -737,14 +740,15 @@ void AmrEngine::Impl::mini_cycle (int l, const T* rhs)
                 return D.fz_maps.p + w * np;
             };
             for (int i = 0; i < A.m_opt.nu1; ++i) {
+                const float* in = (i == 0) ? nullptr : a;      // the first sweep reads a zero correction
                 if (D.nsafe > 0) {
                     k_sweep_fused2<false, true><<<D.nsafe, blk, 0, st()>>>(Ld.dl, Ld.mg.dev(), a, b, rhs, StencilPtrs{},
-                        maps_of(a), err, tma::WAIT_LIMIT, nullptr, 0, D.fz_safe.p);
+                        maps_of(a), err, tma::WAIT_LIMIT, nullptr, i == 0 ? 1 : 0, D.fz_safe.p);
                     launched();
                 }
                 if (D.nrest > 0) {
-                    k_gsrb_tiles<<<D.nrest, blk, 0, st()>>>(Ld.dl, D.fz_rest.p, a, a, b, rhs, D.nbr.p, 0);
-                    k_gsrb_tiles<<<D.nrest, blk, 0, st()>>>(Ld.dl, D.fz_rest.p, a, b, b, rhs, D.nbr.p, 1);
+                    k_gsrb_tiles<<<D.nrest, blk, 0, st()>>>(Ld.dl, D.fz_rest.p, in, in, b, rhs, D.nbr.p, 0);
+                    k_gsrb_tiles<<<D.nrest, blk, 0, st()>>>(Ld.dl, D.fz_rest.p, in, b, b, rhs, D.nbr.p, 1);
                     launched(2);
                 }
                 std::swap(a, b);
