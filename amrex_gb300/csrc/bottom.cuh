@@ -102,13 +102,138 @@ __device__ void ghost_fill (const DevLevel& L, const CopyTag* tags, int p0, int 
     __syncthreads();
 }
 
+// Per-thread cache of a solve's bottom level, built once per bottom solve:
+// the thread's cells (the same cells, in the same order, as for_cells gives
+// it) and its face-ghost entries (as ghost_fill assigns them), so the Krylov
+// loop's many passes skip the index divisions and face walks.  Used when the
+// solve has one patch and every thread's share fits; uniform over the block.
+constexpr int BC_CELLS = 2;
+constexpr int BC_GHOSTS = 6;
+
+struct BotCache {
+    bool cells = false, ghosts = false;
+    const PatchDesc* P = nullptr;
+    int n = 0;
+    long long q[BC_CELLS];
+    int i[BC_CELLS], j[BC_CELLS], k[BC_CELLS];
+    int ng = 0;
+    int gf[BC_GHOSTS];               // the face of each ghost entry
+    long long gq[BC_GHOSTS];         // its ghost cell
+};
+
+struct BottomJobK : BottomJob {
+    BotCache K;
+};
+
+__device__ inline BottomJobK make_job (const BottomLevelPtrs& B, const BottomJob& J0)
+{
+    BottomJobK J;
+    static_cast<BottomJob&>(J) = J0;
+    if (J0.np != 1) { return J; }
+    const PatchDesc& P = B.L.P[J0.p0];
+    const int nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1, nz = P.hi[2] - P.lo[2] + 1;
+    const int ncell = nx * ny * nz;
+    BotCache& K = J.K;
+    K.P = &P;
+    if (ncell <= BC_CELLS * (int)blockDim.x) {
+        K.cells = true;
+#pragma unroll
+        for (int c = 0; c < BC_CELLS; ++c) {
+            const int u = (int)threadIdx.x + c * (int)blockDim.x;
+            K.i[c] = K.j[c] = K.k[c] = 0;
+            K.q[c] = 0;
+            if (u < ncell) {
+                K.n = c + 1;
+                K.i[c] = P.lo[0] + u % nx;
+                K.j[c] = P.lo[1] + (u / nx) % ny;
+                K.k[c] = P.lo[2] + u / (nx * ny);
+                K.q[c] = cidx(P, K.i[c], K.j[c], K.k[c]);
+            }
+        }
+    }
+    // the face walk of ghost_fill: face f's cells u = tid, tid + blockDim, ...
+    int per_thread = 0;
+    const int nf[6] = {ny * nz, nx * nz, nx * ny, ny * nz, nx * nz, nx * ny};
+    for (int f = 0; f < 6; ++f) { per_thread += (nf[f] + (int)blockDim.x - 1) / (int)blockDim.x; }
+    if (per_thread <= BC_GHOSTS) {
+        // entries in the walk's order; with at most one cell per face per
+        // thread (the common case) slot f holds face f's cell, or none
+        K.ghosts = true;
+        int g = 0;
+#pragma unroll
+        for (int s = 0; s < BC_GHOSTS; ++s) { K.gf[s] = -1; K.gq[s] = 0; }
+        for (int f = 0; f < 6; ++f) {
+            for (int u = threadIdx.x; u < nf[f]; u += blockDim.x) {
+                int i, j, k;
+                face_cell(P, f, u, i, j, k);
+                if (face_mask(B.L, P, f, i, j, k) > 0) {
+#pragma unroll
+                    for (int s = 0; s < BC_GHOSTS; ++s) {
+                        if (s == g) { K.gf[s] = f; K.gq[s] = cidx(P, i, j, k); }
+                    }
+                    ++g;
+                }
+            }
+        }
+        K.ng = g;
+    }
+    return J;
+}
+
+// for_cells over the solve's bottom patches, from the cache when it holds them
+template <typename F>
+__device__ __forceinline__ void cells (const BottomJobK& J, const DevLevel& L, F&& f)
+{
+    if (J.K.cells) {
+#pragma unroll
+        for (int c = 0; c < BC_CELLS; ++c) {
+            if (c < J.K.n) { f(*J.K.P, J.K.i[c], J.K.j[c], J.K.k[c], J.K.q[c]); }
+        }
+    } else {
+        for_cells(L, J.p0, J.np, f);
+    }
+}
+
+// ghost_fill of the solve's bottom patches, the closures from the cache when
+// it holds them (the copies between patches keep their walk)
+__device__ inline void ghosts (const BottomJobK& J, const BottomLevelPtrs& B, double* phi)
+{
+    if (!J.K.ghosts) {
+        ghost_fill<double>(B.L, B.tags, J.p0, J.np, J.t0, J.nt, phi);
+        return;
+    }
+    __syncthreads();
+    const PatchDesc& P = *J.K.P;
+#pragma unroll
+    for (int g = 0; g < BC_GHOSTS; ++g) {
+        if (g < J.K.ng) {
+            // homogeneous closures: the Dirichlet value slot index is not read
+            const int f = J.K.gf[g], d = f % 3;
+            const long long stride = (d == 0) ? 1 : ((d == 1) ? (long long)P.sx : P.sxy);
+            bc_ghost<double>(P, f, J.K.gq[g], (f >= 3) ? -stride : stride, phi, 0, nullptr, 0);
+        }
+    }
+    for (int w = J.t0; w < J.t0 + J.nt; ++w) {
+        const CopyTag& C = B.tags[w];
+        const int nx = C.box.hi[0] - C.box.lo[0] + 1, ny = C.box.hi[1] - C.box.lo[1] + 1;
+        const int n = nx * ny * (C.box.hi[2] - C.box.lo[2] + 1);
+        for (int u = threadIdx.x; u < n; u += blockDim.x) {
+            const int i = C.box.lo[0] + u % nx;
+            const int j = C.box.lo[1] + (u / nx) % ny;
+            const int k = C.box.lo[2] + u / (nx * ny);
+            phi[cidx(B.L.P[C.dst], i, j, k)] = phi[cidx(B.L.P[C.src], i - C.shift[0], j - C.shift[1], k - C.shift[2])];
+        }
+    }
+    __syncthreads();
+}
+
 // out = A in (homogeneous BCs), divided by the diagonal (MLABecLaplacianT::
 // normalize, AMReX_MLABecLaplacian.H:1128-1168) when NORM
 template <bool ABEC, bool NORM = true>
-__device__ void apply_normalize (const BottomLevelPtrs& B, const BottomJob& J, double* out, double* in)
+__device__ void apply_normalize (const BottomLevelPtrs& B, const BottomJobK& J, double* out, double* in)
 {
-    ghost_fill<double>(B.L, B.tags, J.p0, J.np, J.t0, J.nt, in);
-    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc& P, int, int, int, long long q) {
+    ghosts(J, B, in);
+    cells(J, B.L, [&] (const PatchDesc& P, int, int, int, long long q) {
         double v = adotx_cell<double, ABEC>(P, q, in, B.a, B.bx, B.by, B.bz);
         if constexpr (ABEC && NORM) { v /= abec_diag<double>(P, q, B.a, B.bx, B.by, B.bz); }
         out[q] = v;
@@ -116,16 +241,24 @@ __device__ void apply_normalize (const BottomLevelPtrs& B, const BottomJob& J, d
     __syncthreads();
 }
 
-__device__ inline double reduce (const DevLevel& L, int p0, int np, const double* x, const double* y, int op)
+__device__ inline double reduce (const BottomJobK& J, const DevLevel& L, const double* x, const double* y, int op)
 {
     __shared__ double sm[32];
     __shared__ double result;
     double acc = 0.0;
-    for_cells(L, p0, np, [&] (const PatchDesc&, int, int, int, long long q) {
+    cells(J, L, [&] (const PatchDesc&, int, int, int, long long q) {
         if (op == RED_MAXABS) { acc = max_nan(acc, fabs(x[q])); }
         else if (op == RED_DOT) { acc += x[q] * y[q]; }
         else { acc += x[q]; }
     });
+    if (blockDim.x == 32) {
+        // one warp: block_reduce's two stages without its barriers (the
+        // second stage combines lane 0's value with five zeros)
+        double v = acc;
+        for (int o = 16; o > 0; o >>= 1) { v = red_combine(op, v, __shfl_down_sync(0xffffffffu, v, o)); }
+        for (int o = 16; o > 0; o >>= 1) { v = red_combine(op, v, 0.0); }
+        return __shfl_sync(0xffffffffu, v, 0);
+    }
     const double r = block_reduce(acc, op, sm);
     if (threadIdx.x == 0) { result = r; }
     __syncthreads();
@@ -135,11 +268,11 @@ __device__ inline double reduce (const DevLevel& L, int p0, int np, const double
 }
 
 template <bool ABEC>
-__device__ void smooth (const BottomLevelPtrs& B, const BottomJob& J, double* x, const double* b)
+__device__ void smooth (const BottomLevelPtrs& B, const BottomJobK& J, double* x, const double* b)
 {
     for (int rb = 0; rb < 2; ++rb) {
-        ghost_fill<double>(B.L, B.tags, J.p0, J.np, J.t0, J.nt, x);
-        for_cells(B.L, J.p0, J.np, [&] (const PatchDesc& P, int i, int j, int k, long long) {
+        ghosts(J, B, x);
+        cells(J, B.L, [&] (const PatchDesc& P, int i, int j, int k, long long) {
             if (((i + j + k + rb) & 1) == 0) {
                 gsrb_cell<double, ABEC>(B.L, P, i, j, k, x, b, B.a, B.bx, B.by, B.bz);
             }
@@ -149,7 +282,7 @@ __device__ void smooth (const BottomLevelPtrs& B, const BottomJob& J, double* x,
 }
 
 // x = 0 and the solver's work vectors p, r = 0, ghosts included
-__device__ inline void zero_work (const BottomLevelPtrs& B, const BottomJob& J)
+__device__ inline void zero_work (const BottomLevelPtrs& B, const BottomJobK& J)
 {
     for (int pp = J.p0; pp < J.p0 + J.np; ++pp) {
         const PatchDesc& P = B.L.P[pp];
@@ -165,58 +298,58 @@ __device__ inline void zero_work (const BottomLevelPtrs& B, const BottomJob& J)
 // MLCGSolverT::solve_bicgstab with a zero initial guess (AMReX_MLCGSolver.H:
 // 96-273) on right-hand side bb; returns its code, the iterations in *iters
 template <bool ABEC>
-__device__ int bicgstab (const BottomLevelPtrs& B, const BottomJob& J, const BottomParams& prm, const double* bb,
+__device__ int bicgstab (const BottomLevelPtrs& B, const BottomJobK& J, const BottomParams& prm, const double* bb,
                          int* iters)
 {
     double *x = B.x, *p = B.p, *r = B.r, *rh = B.rh, *v = B.v, *t = B.t;
     zero_work(B, J);
     // r = b ; normalize ; rh = r
-    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc& P, int, int, int, long long q) {
+    cells(J, B.L, [&] (const PatchDesc& P, int, int, int, long long q) {
         double val = bb[q];
         if constexpr (ABEC) { val /= abec_diag<double>(P, q, B.a, B.bx, B.by, B.bz); }
         r[q] = val;
     });
     __syncthreads();
-    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { rh[q] = r[q]; });
+    cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long q) { rh[q] = r[q]; });
     __syncthreads();
-    double rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
+    double rnorm = reduce(J, B.L, r, nullptr, RED_MAXABS);
     const double rnorm0 = rnorm;
     double rho_1 = 0, alpha = 0, omega = 0;
     int ret = 0, iter = 1;
     if (!(rnorm0 == 0 || rnorm0 < prm.eps_abs)) {
         for (; iter <= prm.maxiter; ++iter) {
-            const double rho = reduce(B.L, J.p0, J.np, rh, r, RED_DOT);
+            const double rho = reduce(J, B.L, rh, r, RED_DOT);
             if (rho == 0) { ret = 1; break; }
             if (iter == 1) {
-                for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { p[q] = r[q]; });
+                cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long q) { p[q] = r[q]; });
             } else {
                 const double beta = (rho / rho_1) * (alpha / omega);
-                for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
+                cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long q) {
                     double pv = p[q] + (-omega) * v[q];   // Saxpy
                     p[q] = r[q] + beta * pv;              // Xpay
                 });
             }
             __syncthreads();
             apply_normalize<ABEC>(B, J, v, p);
-            const double rhTv = reduce(B.L, J.p0, J.np, rh, v, RED_DOT);
+            const double rhTv = reduce(J, B.L, rh, v, RED_DOT);
             if (rhTv != 0.0) { alpha = rho / rhTv; } else { ret = 2; break; }
-            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
+            cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long q) {
                 x[q] += alpha * p[q];
                 r[q] += (-alpha) * v[q];
             });
             __syncthreads();
-            rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
+            rnorm = reduce(J, B.L, r, nullptr, RED_MAXABS);
             if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
             apply_normalize<ABEC>(B, J, t, r);
-            const double tt = reduce(B.L, J.p0, J.np, t, t, RED_DOT);
-            const double tr = reduce(B.L, J.p0, J.np, t, r, RED_DOT);
+            const double tt = reduce(J, B.L, t, t, RED_DOT);
+            const double tr = reduce(J, B.L, t, r, RED_DOT);
             if (tt != 0.0) { omega = tr / tt; } else { ret = 3; break; }
-            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) {
+            cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long q) {
                 x[q] += omega * r[q];
                 r[q] += (-omega) * t[q];
             });
             __syncthreads();
-            rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
+            rnorm = reduce(J, B.L, r, nullptr, RED_MAXABS);
             if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
             if (omega == 0) { ret = 4; break; }
             rho_1 = rho;
@@ -225,7 +358,7 @@ __device__ int bicgstab (const BottomLevelPtrs& B, const BottomJob& J, const Bot
         if ((ret == 0 || ret == 8) && (rnorm < rnorm0)) {
             if (ret == 8) { ret = 9; }
         } else {
-            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { x[q] = 0.0; });
+            cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long q) { x[q] = 0.0; });
             __syncthreads();
         }
     }
@@ -236,14 +369,14 @@ __device__ int bicgstab (const BottomLevelPtrs& B, const BottomJob& J, const Bot
 // MLCGSolverT::solve_cg with a zero initial guess (AMReX_MLCGSolver.H:
 // 275-410): unpreconditioned CG, q = A p with homogeneous BCs; v holds q
 template <bool ABEC>
-__device__ int conj_grad (const BottomLevelPtrs& B, const BottomJob& J, const BottomParams& prm, const double* bb,
+__device__ int conj_grad (const BottomLevelPtrs& B, const BottomJobK& J, const BottomParams& prm, const double* bb,
                           int* iters)
 {
     double *x = B.x, *p = B.p, *r = B.r, *q = B.v;
     zero_work(B, J);
-    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long c) { r[c] = bb[c]; });
+    cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long c) { r[c] = bb[c]; });
     __syncthreads();
-    double rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
+    double rnorm = reduce(J, B.L, r, nullptr, RED_MAXABS);
     const double rnorm0 = rnorm;
     double rho_1 = 0;
     int ret = 0, iter = 1;
@@ -252,27 +385,27 @@ __device__ int conj_grad (const BottomLevelPtrs& B, const BottomJob& J, const Bo
         return ret;
     }
     for (; iter <= prm.maxiter; ++iter) {
-        const double rho = reduce(B.L, J.p0, J.np, r, r, RED_DOT);
+        const double rho = reduce(J, B.L, r, r, RED_DOT);
         if (rho == 0) { ret = 1; break; }
         if (iter == 1) {
-            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long c) { p[c] = r[c]; });
+            cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long c) { p[c] = r[c]; });
         } else {
             const double beta = rho / rho_1;
-            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long c) {
+            cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long c) {
                 p[c] = r[c] + beta * p[c];        // Xpay
             });
         }
         __syncthreads();
         apply_normalize<ABEC, false>(B, J, q, p);
-        const double pw = reduce(B.L, J.p0, J.np, p, q, RED_DOT);
+        const double pw = reduce(J, B.L, p, q, RED_DOT);
         double alpha;
         if (pw != 0.0) { alpha = rho / pw; } else { ret = 1; break; }
-        for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long c) {
+        cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long c) {
             x[c] += alpha * p[c];                 // Saxpy
             r[c] += (-alpha) * q[c];
         });
         __syncthreads();
-        rnorm = reduce(B.L, J.p0, J.np, r, nullptr, RED_MAXABS);
+        rnorm = reduce(J, B.L, r, nullptr, RED_MAXABS);
         if (rnorm < prm.eps_rel * rnorm0 || rnorm < prm.eps_abs) { break; }
         rho_1 = rho;
     }
@@ -280,7 +413,7 @@ __device__ int conj_grad (const BottomLevelPtrs& B, const BottomJob& J, const Bo
     if ((ret == 0 || ret == 8) && (rnorm < rnorm0)) {
         if (ret == 8) { ret = 9; }
     } else {
-        for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long c) { x[c] = 0.0; });
+        cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long c) { x[c] = 0.0; });
         __syncthreads();
     }
     *iters = iter;
@@ -291,16 +424,17 @@ __device__ int conj_grad (const BottomLevelPtrs& B, const BottomJob& J, const Bo
 
 // the bottom solve of one solve, executed by the calling block
 template <typename T, bool ABEC>
-__device__ void bottom_solve_block (const BottomLevelPtrs& B, const BottomJob& J, const BottomParams& prm,
+__device__ void bottom_solve_block (const BottomLevelPtrs& B, const BottomJob& J0, const BottomParams& prm,
                                     int* __restrict__ out_iters, int* __restrict__ out_ret)
 {
     using namespace bottom_detail;
+    const BottomJobK J = make_job(B, J0);
     double *x = B.x, *b = B.b;
     const T* bin = static_cast<const T*>(B.b_in);
     T* xout = static_cast<T*>(B.x_out);
 
     zero_work(B, J);
-    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { b[q] = (double)bin[q]; });
+    cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long q) { b[q] = (double)bin[q]; });
     __syncthreads();
 
     int ret = 0, iter = 0, iter2 = -1;
@@ -311,8 +445,8 @@ __device__ void bottom_solve_block (const BottomLevelPtrs& B, const BottomJob& J
         // solvers' private copy: the smoothing after them takes the level's b)
         const double* bb = b;
         if (J.singular) {
-            const double off = reduce(B.L, J.p0, J.np, b, nullptr, RED_SUM) * J.volinv;
-            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { b[q] = b[q] + (-off); });
+            const double off = reduce(J, B.L, b, nullptr, RED_SUM) * J.volinv;
+            cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long q) { b[q] = b[q] + (-off); });
             __syncthreads();
         }
         const int kind = (prm.mode != nullptr) ? prm.mode[J.solve] : BK_BICGSTAB;
@@ -325,19 +459,19 @@ __device__ void bottom_solve_block (const BottomLevelPtrs& B, const BottomJob& J
             if (ret == 0 && threadIdx.x == 0) { prm.mode[J.solve] = cg_first ? BK_BICGSTAB : BK_CG; }
         }
         if (ret != 0 && ret != 9) {
-            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { x[q] = 0.0; });
+            cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long q) { x[q] = 0.0; });
             __syncthreads();
         }
         if (J.singular) {
             // the smoother below takes the level's own b
-            for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { b[q] = (double)bin[q]; });
+            cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long q) { b[q] = (double)bin[q]; });
             __syncthreads();
         }
         const int n = (ret == 0) ? prm.nub : prm.nuf;
         for (int i = 0; i < n; ++i) { smooth<ABEC>(B, J, x, b); }
     }
     __syncthreads();
-    for_cells(B.L, J.p0, J.np, [&] (const PatchDesc&, int, int, int, long long q) { xout[q] = T(x[q]); });
+    cells(J, B.L, [&] (const PatchDesc&, int, int, int, long long q) { xout[q] = T(x[q]); });
     if (threadIdx.x == 0) {
         out_iters[J.solve] = iter;
         out_ret[J.solve] = ret;
