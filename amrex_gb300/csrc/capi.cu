@@ -314,14 +314,21 @@ void fab_global (mlmg_multifab_s& mf, void* host, const int glo[3], const int gn
         start.push_back(start.back() + (r.ok() ? r.npts() : 0));
     }
     const long long ng = (long long)gn[0] * gn[1] * gn[2];
-    T* const stage = scratch<T>(0, (size_t)ng);
     Box3* const dr = scratch<Box3>(1, regions.size());
     long long* const ds = scratch<long long>(2, start.size());
     MLMG_CUDA_CHECK(cudaMemcpyAsync(dr, regions.data(), regions.size() * sizeof(Box3), cudaMemcpyHostToDevice, st));
     MLMG_CUDA_CHECK(cudaMemcpyAsync(ds, start.data(), start.size() * sizeof(long long), cudaMemcpyHostToDevice, st));
+    // a page-locked host array is read or written by the scatter / gather
+    // kernel itself through its device pointer (over NVLink-C2C), with no
+    // staging copy; any other host array goes through a device stage
+    cudaPointerAttributes pa{};
+    const bool pinned = cudaPointerGetAttributes(&pa, host) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+                        pa.devicePointer != nullptr;
+    if (!pinned) { (void)cudaGetLastError(); }
+    T* stage = pinned ? static_cast<T*>(pa.devicePointer) : scratch<T>(0, (size_t)ng);
     // the host array enters the stage for an upload, and for a download that
     // leaves cells of the array uncovered (those keep the host's values)
-    if (dir == 0 || start.back() < ng) {
+    if (!pinned && (dir == 0 || start.back() < ng)) {
         MLMG_CUDA_CHECK(cudaMemcpyAsync(stage, host, ng * sizeof(T), cudaMemcpyHostToDevice, st));
     }
     if (start.back() > 0) {
@@ -329,7 +336,9 @@ void fab_global (mlmg_multifab_s& mf, void* host, const int glo[3], const int gn
             start.back(), (T*)mf.data.p, stage, glo[0], glo[1], glo[2], gn[0], gn[1], dir);
         g_launches++;
     }
-    if (dir == 1) { MLMG_CUDA_CHECK(cudaMemcpyAsync(host, stage, ng * sizeof(T), cudaMemcpyDeviceToHost, st)); }
+    if (!pinned && dir == 1) {
+        MLMG_CUDA_CHECK(cudaMemcpyAsync(host, stage, ng * sizeof(T), cudaMemcpyDeviceToHost, st));
+    }
     MLMG_CUDA_CHECK(cudaGetLastError());
     MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
 }
