@@ -1296,6 +1296,7 @@ int mlmg_set_option (mlmg_solver s, const char* name, double value)
     else if (n == "fused_tma") { s->opt.fused_tma = value != 0.0; }
     else if (n == "fused_prefetch") { s->opt.fused_prefetch = value != 0.0; }
     else if (n == "pdl") { s->opt.pdl = value != 0.0; }
+    else if (n == "fused_restrict") { s->opt.fused_restrict = value != 0.0; }
     else if (n == "fused_fine") {
         MLMG_REQUIRE(value >= 0 && value <= 2, ERR_ARGS, "fused_fine must be 0, 1 or 2");
         s->opt.fused_fine = (int)value;

@@ -242,6 +242,7 @@ struct Engine::Impl {
     StencilPtrs stencil64 (int l) const;
     void gsrb32 (int l, float* cor, const float* res, int rb);
     void smooth_fused (int l, int n, bool from_zero = false);
+    bool resid_restrict_fused (int l);
     void resid32 (int l, float* rescor, float* cor, const float* res);
     void residual0 (bool to32, bool norm_zeroed = false);   // res[0] (FP64, or FP32 in mixed) and its max-norm
     void one_iteration (bool fmg);

@@ -311,6 +311,161 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
     if (touches) { sweep(std::true_type{}); } else { sweep(std::false_type{}); }
 }
 
+// The correction residual of a fused level and its restriction in one pass
+// (MLMGT::mgVcycle's computeResOfCorrection then restriction,
+// AMReX_MLMG.H:1306-1415; amrex_avgdown, AMReX_MultiFabUtil_3D_C.H:375-392):
+// each 32x8x8 tile stages the correction over the tile grown by two by one
+// TMA load (the box of the fused sweep), closes the patch faces in shared
+// memory (homogeneous closures, as applyBC before the residual), computes
+// r = res - A cor for its cells with the arithmetic of k_residual_s into
+// shared memory, and writes the 16x4x4 coarse right-hand sides as the mean of
+// each 2x2x2 group, summed in k_restrict's order.  The fine residual never
+// goes to memory, and the restriction is no separate launch.  A level is
+// coarsenable, so patches and tiles start on even cells and hold whole groups.
+// Each thread issues the loads of its 8 cells' rhs and stencil values before
+// it waits for the copy (64 values in registers; three blocks per SM), which
+// hides the copy's latency: separate residual and restriction launches took
+// 0.85 ms more per 256^3 solve, loads issued after the wait 0.5 ms more.
+template <bool VARC>
+__global__ void __launch_bounds__(FS_THREADS, 3)
+k_resid_restrict_tma (DevLevel L, Subset S, DevLevel Lc, const float* __restrict__ rhs, StencilPtrs Sc,
+                      const CUtensorMap* __restrict__ maps, float* __restrict__ crse, int* err)
+{
+    __shared__ __align__(128) float A[FS_AZ][FS_AY][FS_AX];   // cor, local (x-4..x+35, y-2..y+9, z-2..z+9)
+    __shared__ float R[FS_TZ][FS_TY][FS_TX];                    // the tile's residuals
+    __shared__ PatchLite SP;
+    __shared__ unsigned long long bar;
+    const int tid = threadIdx.y * FS_TX + threadIdx.x;
+    const TileCoord c = decode_fused_tile(L, S, blockIdx.x);
+    const int x0 = c.x0, y0 = c.y0, z0 = c.z0;
+    const PatchDesc& PD = L.P[c.p];
+    if (tid == 0) {
+        for (int d = 0; d < 3; ++d) { SP.lo[d] = PD.lo[d]; SP.hi[d] = PD.hi[d]; }
+        SP.sx = PD.sx; SP.sxy = PD.sxy; SP.base = PD.base;
+        SP.dhx = float(PD.dha[0]); SP.dhy = float(PD.dha[1]); SP.dhz = float(PD.dha[2]);
+        for (int f = 0; f < 6; ++f) {
+            SP.f[f].type = PD.face[f].type;
+            SP.f[f].nx = PD.face[f].nx;
+            SP.f[f].c1 = float(PD.face[f].coef[1]);
+            SP.f[f].c2 = float(PD.face[f].coef[2]);
+            SP.f[f].fco = float(PD.face[f].fco);
+        }
+        tma::mbar_init(&bar, 1);
+    }
+    // the coarse patch under the tile's first and last cells; a tile that
+    // lies over one coarse patch (nearly all) looks it up once
+    const int pc = find_patch(Lc, PD.solve, x0 >> 1, y0 >> 1, z0 >> 1);
+    const PatchGeom C = geom_of(Lc.P[pc]);
+    const bool one = contains(C, min(x0 + FS_TX - 1, PD.hi[0]) >> 1, min(y0 + FS_TY - 1, PD.hi[1]) >> 1,
+                              min(z0 + FS_TZ - 1, PD.hi[2]) >> 1);
+    __syncthreads();
+    pdl_wait();
+    pdl_trigger();
+    const PatchLite& P = SP;
+    const int cx = x0 - P.lo[0] + XOFF - 4, cy = y0 - P.lo[1] - 1, cz = z0 - P.lo[2] - 1;
+    if ((cx & 3) != 0) {
+        if (tid == 0) { atomicExch(err, tma::ERR_TMA_ALIGN); }
+        return;
+    }
+    if (tid == 0) {
+        tma::mbar_expect_tx(&bar, (unsigned)sizeof(A));
+        tma::load_3d(&A[0][0][0], maps + c.p, &bar, cx, cy, cz);
+    }
+    // patch bounds in tile-local coordinates
+    const int pl[3] = {P.lo[0] - x0, P.lo[1] - y0, P.lo[2] - z0};
+    const int ph[3] = {P.hi[0] - x0, P.hi[1] - y0, P.hi[2] - z0};
+    // the rhs and stencil values of the thread's column of 8 cells, loaded
+    // while the correction's copy is in flight
+    const int lx = threadIdx.x, ly = threadIdx.y;
+    const bool inxy = lx <= ph[0] && ly <= ph[1];
+    const long long q0 = P.idx(x0, y0, z0);
+    const int sx = P.sx, sxy = (int)P.sxy;
+    float rv[FS_TZ], dv[FS_TZ], xl[FS_TZ], xh[FS_TZ], yl[FS_TZ], yh[FS_TZ], zl[FS_TZ], zh[FS_TZ];
+#pragma unroll
+    for (int lz = 0; lz < FS_TZ; ++lz) {
+        const bool in = inxy && lz <= ph[2];
+        const int o = lz * sxy + ly * sx + lx;
+        rv[lz] = in ? __ldg(rhs + q0 + o) : 0.0f;
+        if constexpr (VARC) {
+            const float* Dp = static_cast<const float*>(Sc.D) + q0;
+            const float* SXp = static_cast<const float*>(Sc.sx) + q0;
+            const float* SYp = static_cast<const float*>(Sc.sy) + q0;
+            const float* SZp = static_cast<const float*>(Sc.sz) + q0;
+            dv[lz] = in ? __ldg(Dp + o) : 0.0f;
+            xl[lz] = in ? __ldg(SXp + o) : 0.0f; xh[lz] = in ? __ldg(SXp + o + 1) : 0.0f;
+            yl[lz] = in ? __ldg(SYp + o) : 0.0f; yh[lz] = in ? __ldg(SYp + o + sx) : 0.0f;
+            zl[lz] = in ? __ldg(SZp + o) : 0.0f; zh[lz] = in ? __ldg(SZp + o + sxy) : 0.0f;
+        }
+    }
+    const bool late = !tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
+    if (__syncthreads_or(late)) {
+        if (tid == 0) { atomicExch(err, tma::ERR_TMA_TIMEOUT); }
+        tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
+        return;
+    }
+    auto aat = [&] (int ax, int ay, int az) -> float& { return A[az + 2][ay + 2][ax + 4]; };
+    const int lim[3] = {FS_TX - 1, FS_TY - 1, FS_TZ - 1};
+    // ghost layers of the patch faces next to the tile's cells: the closure
+    // of the face cell and the next inner cell
+    for (int f = 0; f < 6; ++f) {
+        const int d = f % 3;
+        const int g = (f < 3) ? pl[d] - 1 : ph[d] + 1;
+        if (g < -1 || g > lim[d] + 1) { continue; }
+        const int s = (f < 3) ? 1 : -1;
+        const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
+        const int a1 = max(0, pl[t1]), b1 = min(lim[t1], ph[t1]);
+        const int a2 = max(0, pl[t2]), b2 = min(lim[t2], ph[t2]);
+        const int n1 = b1 - a1 + 1, n2 = b2 - a2 + 1;
+        if (n1 <= 0 || n2 <= 0) { continue; }
+        for (int u = tid; u < n1 * n2; u += FS_THREADS) {
+            int cc[3];
+            cc[d] = g; cc[t1] = a1 + u % n1; cc[t2] = a2 + u / n1;
+            int cf[3] = {cc[0], cc[1], cc[2]}, ci[3] = {cc[0], cc[1], cc[2]};
+            cf[d] += s; ci[d] += 2 * s;
+            aat(cc[0], cc[1], cc[2]) = P.closure(f, aat(cf[0], cf[1], cf[2]), aat(ci[0], ci[1], ci[2]));
+        }
+    }
+    __syncthreads();
+    // r = res - A cor for the tile's cells (k_residual_s's arithmetic)
+    {
+        const float dhx = P.dhx, dhy = P.dhy, dhz = P.dhz;
+        const float cdd = float(-2.0) * (dhx + dhy + dhz);
+#pragma unroll
+        for (int lz = 0; lz < FS_TZ; ++lz) {
+            float v = 0.0f;
+            if (inxy && lz <= ph[2]) {
+                float d, sxl, sxh, syl, syh, szl, szh;
+                if constexpr (VARC) {
+                    d = dv[lz]; sxl = xl[lz]; sxh = xh[lz]; syl = yl[lz]; syh = yh[lz]; szl = zl[lz]; szh = zh[lz];
+                } else {
+                    d = cdd; sxl = sxh = -dhx; syl = syh = -dhy; szl = szh = -dhz;
+                }
+                const float xc = aat(lx, ly, lz);
+                const float nb = sxl * aat(lx - 1, ly, lz) + sxh * aat(lx + 1, ly, lz) + syl * aat(lx, ly - 1, lz) +
+                                 syh * aat(lx, ly + 1, lz) + szl * aat(lx, ly, lz - 1) + szh * aat(lx, ly, lz + 1);
+                v = rv[lz] - (d * xc - nb);
+            }
+            R[lz][ly][lx] = v;
+        }
+    }
+    __syncthreads();
+    // the coarse cells of the tile: one per thread (16 x 4 x 4)
+    {
+        const int ux = tid % (FS_TX / 2), uy = (tid / (FS_TX / 2)) % (FS_TY / 2), uz = tid / ((FS_TX / 2) * (FS_TY / 2));
+        const int fx = 2 * ux, fy = 2 * uy, fz = 2 * uz;
+        if (fx <= ph[0] && fy <= ph[1] && fz <= ph[2]) {
+            float v = 0;
+            v += R[fz][fy][fx];         v += R[fz][fy][fx + 1];
+            v += R[fz][fy + 1][fx];     v += R[fz][fy + 1][fx + 1];
+            v += R[fz + 1][fy][fx];     v += R[fz + 1][fy][fx + 1];
+            v += R[fz + 1][fy + 1][fx]; v += R[fz + 1][fy + 1][fx + 1];
+            const int i = (x0 >> 1) + ux, j = (y0 >> 1) + uy, k = (z0 >> 1) + uz;
+            const long long qc = one ? cidx(C, i, j, k) : cidx(Lc.P[find_patch(Lc, C.solve, i, j, k)], i, j, k);
+            crse[qc] = (float(1.0) / float(8)) * v;
+        }
+    }
+}
+
 // One colour of MLPoisson's Gauss-Seidel sweep over a list of fused-sweep
 // tiles of an AMR fine level (the tiles whose halo meets a face shared with
 // another patch): old cell values from `old` (null: a zero correction),

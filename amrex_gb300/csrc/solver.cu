@@ -629,6 +629,28 @@ void Engine::Impl::smooth_fused (int l, int n, bool from_zero)
     }
 }
 
+// computeResOfCorrection and the restriction of the result to the next MG
+// level in one launch over a TMA-swept level's tiles (the correction in
+// cor32, as the fused sweeps leave it); false where the level has no tensor
+// maps or the option is off
+bool Engine::Impl::resid_restrict_fused (int l)
+{
+    LevelData& L = lev[l];
+    if (!E.m_opt.fused_restrict || !L.fused || L.march || L.tm_a.p == nullptr) { return false; }
+    LevelData& C = lev[l + 1];
+    const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
+    const StencilPtrs S = stencil32(l);
+    if (abec) {
+        launch(k_resid_restrict_tma<true>, g, blk, 0, L.dl, L.fz.dev(), C.dl, L.res32.p, S, L.tm_a.p, C.res32.p,
+               err_d.p);
+    } else {
+        launch(k_resid_restrict_tma<false>, g, blk, 0, L.dl, L.fz.dev(), C.dl, L.res32.p, S, L.tm_a.p, C.res32.p,
+               err_d.p);
+    }
+    launched();
+    return true;
+}
+
 template <typename T>
 void Engine::Impl::smooth (int l, T* cor, const T* res, bool skip_fb)
 {
@@ -745,6 +767,7 @@ void Engine::Impl::vcycle (int top)
         } else {
             for (int i = 0; i < o.nu1; ++i) { smooth<T>(l, cor, res, i == 0); }
         }
+        if (std::is_same_v<T, float> && resid_restrict_fused(l)) { continue; }
         correction_residual<T>(l);
         LevelData& C = lev[l + 1];
         launch(k_restrict<T>, C.all.ntiles, kTileBlock, 0, L.dl, C.dl, C.all.dev(), rescor, field_res<T>(l + 1));
@@ -1004,7 +1027,8 @@ bool same_iteration (const EngineOptions& a, const EngineOptions& b)
            a.march_min_tiles == b.march_min_tiles && a.march_tz == b.march_tz && a.fused_tma == b.fused_tma &&
            a.fused_prefetch == b.fused_prefetch && a.max_fmg_iter == b.max_fmg_iter &&
            a.transpose == b.transpose && a.tma_first_wait == b.tma_first_wait &&
-           a.final_fill_bc == b.final_fill_bc && a.pdl == b.pdl && a.fused_fine == b.fused_fine;
+           a.final_fill_bc == b.final_fill_bc && a.pdl == b.pdl && a.fused_fine == b.fused_fine &&
+           a.fused_restrict == b.fused_restrict;
 }
 
 Engine::Engine (std::vector<SolveProblem> problems, const EngineOptions& opt, cudaStream_t stream)

@@ -59,6 +59,8 @@ struct EngineOptions {
     int fused_fine = 1;         // AMR fine levels (MLPoisson, mixed): fused sweeps on the tiles whose halo
                                 // meets no face shared with another patch, colour passes on the rest
                                 // (2: colour passes on every tile; 0: the per-level colour passes)
+    int fused_restrict = 1;     // TMA-swept levels: the V-cycle's correction residual and its restriction
+                                // in one tile kernel (the fine residual stays in shared memory)
 };
 
 // true when two option sets capture the same iteration graph

@@ -175,6 +175,29 @@ def test_fused_sweep_staging_bitwise(name):
 
 
 @pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_48", "solve_abec_mixed_bc",
+                                  "solve_abec_agg8", "solve_poisson_periodic", "solve_poisson_periodic_x",
+                                  "solve_abec_mo4"])
+@pytest.mark.parametrize("merge", [1, 0])
+def test_fused_residual_restriction_bitwise(name, merge):
+    """The correction residual and its restriction computed in one TMA tile
+    kernel (the fine residual kept in shared memory) give the separate
+    residual and restriction launches' coarse right-hand sides bit for bit:
+    the same iterations and the same solution, with merged or unmerged
+    patches."""
+    c = load.load(name)["case"]
+    inp = cases.inputs(c)
+    sols = []
+    for fr in (0, 1):
+        p = helpers.make_problem(c, inp, precision="mixed", fused=True,
+                                 options={"fused_restrict": fr, "merge_boxes": merge})
+        p["mlmg"].solve(p["sol"], p["rhs"], 1e-10, 0)
+        sols.append((p["mlmg"].getNumIters(), list(p["mlmg"].getResidualHistory()), helpers.solution(p, c)))
+    assert sols[0][0] == sols[1][0]
+    assert sols[0][1] == sols[1][1]
+    assert np.array_equal(sols[0][2], sols[1][2])
+
+
+@pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_48", "solve_abec_mixed_bc",
                                   "solve_abec_agg8", "solve_poisson_periodic"])
 @pytest.mark.parametrize("cells", [512, 32768])
 def test_coarse_block_vcycle_matches_grid_kernels(name, cells):
