@@ -129,6 +129,24 @@ struct AmrEngine::Impl {
     bool mixed () const { return A.m_opt.precision == 1; }
     void launched (int n = 1) { own_launches += n; }
     LevelData& L (int l) { return lev[l].I->lev[0]; }
+    // a kernel on the engine's stream, as a programmatic dependent launch
+    // unless the option is off (every kernel of the path starts with
+    // griddepcontrol.wait before it touches the previous kernels' data)
+    template <typename... KArgs, typename... Args>
+    void launch (void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, Args&&... args)
+    {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = grid;
+        cfg.blockDim = block;
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st();
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = A.m_opt.pdl ? 1 : 0;
+        MLMG_CUDA_CHECK(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...));
+    }
 
     bool abec () const { return prob.is_abec != 0; }
     void build ();
@@ -581,7 +599,7 @@ void AmrEngine::Impl::average_down_coefficients ()
         LevelData& Lc = L(c);
         LevelData& Lf = L(c + 1);
         if (prob.alpha != 0.0 && D.nacell > 0) {
-            k_amr_avgdown<double, double><<<blocks_for(D.nacell, 256), 256, 0, st()>>>(Lc.dl, Lf.dl, D.atags.p,
+            launch(k_amr_avgdown<double, double>, blocks_for(D.nacell, 256), 256, 0, Lc.dl, Lf.dl, D.atags.p,
                 D.astart.p, D.natag, D.nacell, Lf.a.p, Lc.a.p);
             launched();
         }
@@ -589,7 +607,7 @@ void AmrEngine::Impl::average_down_coefficients ()
         double* cb[3] = {Lc.bx.p, Lc.by.p, Lc.bz.p};
         for (int d = 0; d < 3; ++d) {
             if (D.nfcell[d] == 0) { continue; }
-            k_amr_avgdown_faces<<<blocks_for(D.nfcell[d], 256), 256, 0, st()>>>(Lc.dl, Lf.dl, D.ftags[d].p,
+            launch(k_amr_avgdown_faces, blocks_for(D.nfcell[d], 256), 256, 0, Lc.dl, Lf.dl, D.ftags[d].p,
                 D.fstart[d].p, D.nftag[d], D.nfcell[d], d, fb[d], cb[d]);
             launched();
         }
@@ -617,7 +635,7 @@ template <> void AmrEngine::Impl::gather<double> (int l, const double* crse)
     AmrLevelData& D = lev[l];
     MLMG_CUDA_CHECK(cudaMemsetAsync(D.cf64.p, 0, sizeof(double) * (size_t)D.cf_n, st()));
     if (D.ngcell > 0) {
-        k_amr_gather<double><<<blocks_for(D.ngcell, 256), 256, 0, st()>>>(L(l - 1).dl, D.cfd.p, D.gtags.p, D.gstart.p,
+        launch(k_amr_gather<double>, blocks_for(D.ngcell, 256), 256, 0, L(l - 1).dl, D.cfd.p, D.gtags.p, D.gstart.p,
                                                                          D.ngtag, D.ngcell, crse, D.cf64.p);
         launched();
     }
@@ -628,7 +646,7 @@ template <> void AmrEngine::Impl::gather<float> (int l, const float* crse)
     AmrLevelData& D = lev[l];
     MLMG_CUDA_CHECK(cudaMemsetAsync(D.cf32.p, 0, sizeof(float) * (size_t)D.cf_n, st()));
     if (D.ngcell > 0) {
-        k_amr_gather<float><<<blocks_for(D.ngcell, 256), 256, 0, st()>>>(L(l - 1).dl, D.cfd.p, D.gtags.p, D.gstart.p,
+        launch(k_amr_gather<float>, blocks_for(D.ngcell, 256), 256, 0, L(l - 1).dl, D.cfd.p, D.gtags.p, D.gstart.p,
                                                                         D.ngtag, D.ngcell, crse, D.cf32.p);
         launched();
     }
@@ -646,7 +664,7 @@ void AmrEngine::Impl::solution_residual (int l, bool update, bool want_norm, boo
         if (update) {
             gather<double>(l, L(l - 1).sol.p);
             if (D.cfw.nfacecells > 0) {
-                k_amr_bndry<double><<<blocks_for(D.cfw.nfacecells, 256), 256, 0, st()>>>(Ld.dl, D.cfw, D.cfd.p,
+                launch(k_amr_bndry<double>, blocks_for(D.cfw.nfacecells, 256), 256, 0, Ld.dl, D.cfw, D.cfd.p,
                     D.cf64.p, D.bflags.p, Ld.bcval.p);
                 launched();
             }
@@ -660,10 +678,10 @@ void AmrEngine::Impl::solution_residual (int l, bool update, bool want_norm, boo
         // 14), with the level's max|r| by atomic max into red_out[0]
         if (want_norm) { MLMG_CUDA_CHECK(cudaMemsetAsync(I.red_out.p, 0, sizeof(double), st())); }
         if (abec()) {
-            k_residual_s<double, double, true, false, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl,
+            launch(k_residual_s<double, double, true, false, false>, Ld.all.ntiles, kTileBlock, 0, Ld.dl,
                 Ld.all.dev(), Ld.res.p, Ld.sol.p, Ld.rhs.p, I.stencil64(0), nullptr, want_norm ? I.red_out.p : nullptr);
         } else {
-            k_residual_s<double, double, false, false, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl,
+            launch(k_residual_s<double, double, false, false, false>, Ld.all.ntiles, kTileBlock, 0, Ld.dl,
                 Ld.all.dev(), Ld.res.p, Ld.sol.p, Ld.rhs.p, StencilPtrs{}, nullptr, want_norm ? I.red_out.p : nullptr);
         }
         launched();
@@ -671,15 +689,15 @@ void AmrEngine::Impl::solution_residual (int l, bool update, bool want_norm, boo
         // the reference's operation order (MLPoissonT::Fapply / MLABecLaplacianT::Fapply),
         // block maxima for the norm
         if (abec()) {
-            k_residual<double, double, true><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res.p,
+            launch(k_residual<double, double, true>, Ld.all.ntiles, kTileBlock, 0, Ld.dl, Ld.all.dev(), Ld.res.p,
                 Ld.sol.p, Ld.rhs.p, Ld.a.p, Ld.bx.p, Ld.by.p, Ld.bz.p, want_norm ? I.partial.p : nullptr);
         } else {
-            k_residual<double, double, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res.p,
+            launch(k_residual<double, double, false>, Ld.all.ntiles, kTileBlock, 0, Ld.dl, Ld.all.dev(), Ld.res.p,
                 Ld.sol.p, Ld.rhs.p, nullptr, nullptr, nullptr, nullptr, want_norm ? I.partial.p : nullptr);
         }
         launched();
         if (want_norm) {
-            k_reduce_final<<<1, 1024, 0, st()>>>(I.partial.p, Ld.all.solve_begin.p, RED_MAXABS, I.red_out.p);
+            launch(k_reduce_final, 1, 1024, 0, I.partial.p, Ld.all.solve_begin.p, RED_MAXABS, I.red_out.p);
             launched();
         }
     }
@@ -691,13 +709,15 @@ void AmrEngine::Impl::reflux (int c)
     LevelData& Lf = L(c + 1);
     LevelData& Lc = L(c);
     AmrLevelData& D = lev[c];
-    lev[c + 1].I->ghost<double>(0, Lf.sol.p, true, true, Lf.bcval.p);
+    // the reflux reads the fine solution's ghosts across the coarse/fine faces
+    // only: the face closures, no copies between the fine patches
+    lev[c + 1].I->ghost<double>(0, Lf.sol.p, true, false, Lf.bcval.p);
     if (D.nrcell > 0) {
         if (abec()) {
-            k_amr_reflux<true><<<blocks_for(D.nrcell, 128), 128, 0, st()>>>(Lf.dl, D.rcells.p, D.rfaces.p, D.nrcell,
+            launch(k_amr_reflux<true>, blocks_for(D.nrcell, 128), 128, 0, Lf.dl, D.rcells.p, D.rfaces.p, D.nrcell,
                 D.rprm, reflux_coef(c), Lc.sol.p, Lf.sol.p, Lc.res.p);
         } else {
-            k_amr_reflux<false><<<blocks_for(D.nrcell, 128), 128, 0, st()>>>(Lf.dl, D.rcells.p, D.rfaces.p, D.nrcell,
+            launch(k_amr_reflux<false>, blocks_for(D.nrcell, 128), 128, 0, Lf.dl, D.rcells.p, D.rfaces.p, D.nrcell,
                 D.rprm, RefluxCoef{}, Lc.sol.p, Lf.sol.p, Lc.res.p);
         }
         launched();
@@ -708,7 +728,7 @@ void AmrEngine::Impl::avgdown (int c, const double* fine, double* crse)
 {
     AmrLevelData& D = lev[c];
     if (D.nacell == 0) { return; }
-    k_amr_avgdown<double, double><<<blocks_for(D.nacell, 256), 256, 0, st()>>>(L(c).dl, L(c + 1).dl, D.atags.p,
+    launch(k_amr_avgdown<double, double>, blocks_for(D.nacell, 256), 256, 0, L(c).dl, L(c + 1).dl, D.atags.p,
         D.astart.p, D.natag, D.nacell, fine, crse);
     launched();
 }
@@ -742,13 +762,13 @@ void AmrEngine::Impl::mini_cycle (int l, const T* rhs)
             for (int i = 0; i < A.m_opt.nu1; ++i) {
                 const float* in = (i == 0) ? nullptr : a;      // the first sweep reads a zero correction
                 if (D.nsafe > 0) {
-                    k_sweep_fused2<false, true><<<D.nsafe, blk, 0, st()>>>(Ld.dl, Ld.mg.dev(), a, b, rhs, StencilPtrs{},
+                    launch(k_sweep_fused2<false, true>, D.nsafe, blk, 0, Ld.dl, Ld.mg.dev(), a, b, rhs, StencilPtrs{},
                         maps_of(a), err, tma::WAIT_LIMIT, nullptr, i == 0 ? 1 : 0, D.fz_safe.p);
                     launched();
                 }
                 if (D.nrest > 0) {
-                    k_gsrb_tiles<<<D.nrest, blk, 0, st()>>>(Ld.dl, D.fz_rest.p, in, in, b, rhs, D.nbr.p, 0);
-                    k_gsrb_tiles<<<D.nrest, blk, 0, st()>>>(Ld.dl, D.fz_rest.p, in, b, b, rhs, D.nbr.p, 1);
+                    launch(k_gsrb_tiles, D.nrest, blk, 0, Ld.dl, D.fz_rest.p, in, in, b, rhs, D.nbr.p, 0);
+                    launch(k_gsrb_tiles, D.nrest, blk, 0, Ld.dl, D.fz_rest.p, in, b, b, rhs, D.nbr.p, 1);
                     launched(2);
                 }
                 std::swap(a, b);
@@ -764,7 +784,7 @@ void AmrEngine::Impl::mini_cycle (int l, const T* rhs)
         // colour passes reading covered neighbours directly: no ghost fills
         for (int i = 0; i < A.m_opt.nu1; ++i) {
             for (int rb = 0; rb < 2; ++rb) {
-                k_gsrb_nbr<T><<<Ld.mg.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.mg.dev(), x, rhs, lev[l].nbr.p, rb);
+                launch(k_gsrb_nbr<T>, Ld.mg.ntiles, kTileBlock, 0, Ld.dl, Ld.mg.dev(), x, rhs, lev[l].nbr.p, rb);
                 launched();
             }
         }
@@ -787,7 +807,7 @@ void AmrEngine::Impl::cor_residual (int l, bool inhomog, const TB* b, TO* out)
         const T* cf;
         if constexpr (std::is_same_v<T, float>) { cf = D.cf32.p; } else { cf = D.cf64.p; }
         if (D.cfw.nfacecells > 0) {
-            k_amr_bndry<T><<<blocks_for(D.cfw.nfacecells, 256), 256, 0, st()>>>(Ld.dl, D.cfw, D.cfd.p, cf,
+            launch(k_amr_bndry<T>, blocks_for(D.cfw.nfacecells, 256), 256, 0, Ld.dl, D.cfw, D.cfd.p, cf,
                                                                                D.bflags.p, D.bcor.p);
             launched();
         }
@@ -797,10 +817,10 @@ void AmrEngine::Impl::cor_residual (int l, bool inhomog, const TB* b, TO* out)
     }
     if (abec()) {
         const StencilPtrs sp = std::is_same_v<T, float> ? D.I->stencil32(0) : StencilPtrs{};
-        k_amr_resid<T, TB, TO, true><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), out, x, b, Ld.a.p,
+        launch(k_amr_resid<T, TB, TO, true>, Ld.all.ntiles, kTileBlock, 0, Ld.dl, Ld.all.dev(), out, x, b, Ld.a.p,
             Ld.bx.p, Ld.by.p, Ld.bz.p, sp);
     } else {
-        k_amr_resid<T, TB, TO, false><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), out, x, b, nullptr,
+        launch(k_amr_resid<T, TB, TO, false>, Ld.all.ntiles, kTileBlock, 0, Ld.dl, Ld.all.dev(), out, x, b, nullptr,
             nullptr, nullptr, nullptr, StencilPtrs{});
     }
     launched();
@@ -811,9 +831,9 @@ void AmrEngine::Impl::norm_start (int l, const double* x, bool masked, int slot)
 {
     LevelData& Ld = L(l);
     Engine::Impl& I = *lev[l].I;
-    k_amr_norm<double><<<Ld.all.ntiles, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), x,
+    launch(k_amr_norm<double>, Ld.all.ntiles, kTileBlock, 0, Ld.dl, Ld.all.dev(), x,
         masked ? lev[l].covered.p : nullptr, I.partial.p);
-    k_reduce_final<<<1, 1024, 0, st()>>>(I.partial.p, Ld.all.solve_begin.p, RED_MAXABS, I.red_out.p);
+    launch(k_reduce_final, 1, 1024, 0, I.partial.p, Ld.all.solve_begin.p, RED_MAXABS, I.red_out.p);
     launched(2);
     MLMG_CUDA_CHECK(cudaMemcpyAsync(h_norm.p + slot, I.red_out.p, sizeof(double), cudaMemcpyDeviceToHost, st()));
 }
@@ -845,7 +865,7 @@ void AmrEngine::Impl::one_iter (int iter)
         const unsigned g = (unsigned)Ld.all.ntiles;
         const T* rhs;
         if constexpr (std::is_same_v<T, float>) {
-            k_amr_copy<float, double><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.res32.p, Ld.res.p);
+            launch(k_amr_copy<float, double>, g, kTileBlock, 0, Ld.dl, Ld.all.dev(), Ld.res32.p, Ld.res.p);
             launched();
             rhs = Ld.res32.p;
             dres[l] = Ld.res.p;
@@ -854,7 +874,7 @@ void AmrEngine::Impl::one_iter (int iter)
             dres[l] = Ld.rescor.p;
         }
         mini_cycle<T>(l, rhs);
-        k_add_to<double, T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), nullptr);
+        launch(k_add_to<double, T>, g, kTileBlock, 0, Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), nullptr, nullptr, 0);
         launched();
         // computeResWithCrseSolFineCor(l-1, l), AMReX_MLMG.H:1660-1690
         solution_residual(l - 1, l - 1 > 0);
@@ -866,11 +886,12 @@ void AmrEngine::Impl::one_iter (int iter)
     {
         LevelData& L0 = L(0);
         if constexpr (std::is_same_v<T, float>) {
-            k_amr_copy<float, double><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.res32.p, L0.res.p);
+            launch(k_amr_copy<float, double>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.res32.p, L0.res.p);
             launched();
         }
         if (iter < A.m_opt.max_fmg_iter) { I0.fcycle<T>(); } else { I0.vcycle<T>(0); }
-        k_add_to<double, T><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.sol.p, cor<T>(0), nullptr);
+        launch(k_add_to<double, T>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.sol.p, cor<T>(0), nullptr,
+               nullptr, 0);
         launched();
     }
     for (int l = 1; l <= fin; ++l) {
@@ -882,14 +903,14 @@ void AmrEngine::Impl::one_iter (int iter)
         gather<T>(l, cor<T>(l - 1));
         const T* cf;
         if constexpr (std::is_same_v<T, float>) { cf = D.cf32.p; } else { cf = D.cf64.p; }
-        k_amr_interp_add<T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), D.cfd.p, cf, cor<T>(l), Ld.sol.p, hold_l);
+        launch(k_amr_interp_add<T>, g, kTileBlock, 0, Ld.dl, Ld.all.dev(), D.cfd.p, cf, cor<T>(l), Ld.sol.p, hold_l);
         launched();
         // computeResWithCrseCorFineCor(l), AMReX_MLMG.H:1693-1715
         T* ures;
         if constexpr (std::is_same_v<T, float>) { ures = Ld.rescor32.p; } else { ures = Ld.res.p; }
         cor_residual<T, double, T>(l, true, dres[l], ures);
         mini_cycle<T>(l, ures);
-        k_amr_finish<T><<<g, kTileBlock, 0, st()>>>(Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), hold_l);
+        launch(k_amr_finish<T>, g, kTileBlock, 0, Ld.dl, Ld.all.dev(), Ld.sol.p, cor<T>(l), hold_l);
         launched();
     }
     // averageDownAndSync, AMReX_MLCellLinOp.H:2102-2122

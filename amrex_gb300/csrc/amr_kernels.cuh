@@ -32,6 +32,8 @@ __global__ void k_amr_gather (DevLevel Lc, const PatchDesc* __restrict__ cfd, co
                               const long long* __restrict__ start, int ntag, long long ncell,
                               const T* __restrict__ crse, T* __restrict__ cf)
 {
+    pdl_wait();
+    pdl_trigger();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ncell) { return; }
     int w, i, j, k;
@@ -48,6 +50,8 @@ __global__ void k_amr_avgdown (DevLevel Lc, DevLevel Lf, const CopyTag* __restri
                                const long long* __restrict__ start, int ntag, long long ncell,
                                const TS* __restrict__ fine, TD* __restrict__ crse)
 {
+    pdl_wait();
+    pdl_trigger();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ncell) { return; }
     int w, i, j, k;
@@ -75,6 +79,8 @@ __global__ void k_amr_avgdown_faces (DevLevel Lc, DevLevel Lf, const CopyTag* __
                                      const long long* __restrict__ start, int ntag, long long ncell, int dir,
                                      const double* __restrict__ fine, double* __restrict__ crse)
 {
+    pdl_wait();
+    pdl_trigger();
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ncell) { return; }
     int w, i, j, k;
@@ -113,6 +119,8 @@ template <typename T>
 __global__ void k_amr_bndry (DevLevel Lf, GhostWork W, const PatchDesc* __restrict__ cfd, const T* __restrict__ cf,
                              const int8_t* __restrict__ flags, double* __restrict__ bcval)
 {
+    pdl_wait();
+    pdl_trigger();
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= W.nfacecells) { return; }
     const int w = bsearch_ll<int>(W.fstart, W.nface, tid);
@@ -193,6 +201,8 @@ __global__ void k_amr_reflux (DevLevel Lf, const RefluxCell* __restrict__ cells,
                               int ncell, RefluxParams prm, RefluxCoef co, const double* __restrict__ sol_c,
                               const double* __restrict__ sol_f, double* __restrict__ res_c)
 {
+    pdl_wait();
+    pdl_trigger();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ncell) { return; }
     const RefluxCell C = cells[t];
@@ -240,6 +250,8 @@ __global__ void __launch_bounds__(TILE_THREADS)
 k_amr_norm (DevLevel L, Subset S, const T* __restrict__ x, const int8_t* __restrict__ covered,
             double* __restrict__ partial)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double sm[32];
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchDesc& P = L.P[c.p];
@@ -280,6 +292,8 @@ k_amr_resid (DevLevel L, Subset S, TO* __restrict__ r, const TX* __restrict__ x,
              const double* __restrict__ a, const double* __restrict__ bx, const double* __restrict__ by,
              const double* __restrict__ bz, StencilPtrs sp)
 {
+    pdl_wait();
+    pdl_trigger();
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchDesc& P = L.P[c.p];
     const int j = c.y0 + threadIdx.y;
@@ -325,6 +339,8 @@ __global__ void __launch_bounds__(TILE_THREADS)
 k_amr_interp_add (DevLevel Lf, Subset Sf, const PatchDesc* __restrict__ cfd, const T* __restrict__ cf,
                   T* __restrict__ fine, double* __restrict__ sol, T* __restrict__ hold)
 {
+    pdl_wait();
+    pdl_trigger();
     const TileCoord c = decode_tile(Lf, Sf, blockIdx.x);
     const PatchDesc& F = Lf.P[c.p];
     const PatchDesc& G = cfd[c.p];
@@ -363,6 +379,8 @@ template <typename T>
 __global__ void __launch_bounds__(TILE_THREADS)
 k_amr_finish (DevLevel L, Subset S, double* __restrict__ sol, T* __restrict__ cor, const T* __restrict__ hold)
 {
+    pdl_wait();
+    pdl_trigger();
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchDesc& P = L.P[c.p];
     const int j = c.y0 + threadIdx.y;
@@ -406,6 +424,8 @@ __global__ void __launch_bounds__(TILE_THREADS, 12)
 k_gsrb_nbr (DevLevel L, Subset Sb, T* __restrict__ phi, const T* __restrict__ rhs, const long long* __restrict__ nbr,
             int rb)
 {
+    pdl_wait();
+    pdl_trigger();
     const TileCoord c = decode_tile(L, Sb, blockIdx.x);
     const PatchDesc& P = L.P[c.p];
     const int j = c.y0 + threadIdx.y;
@@ -444,6 +464,8 @@ template <typename TD, typename TS>
 __global__ void __launch_bounds__(TILE_THREADS)
 k_amr_copy (DevLevel L, Subset S, TD* __restrict__ dst, const TS* __restrict__ src)
 {
+    pdl_wait();
+    pdl_trigger();
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchDesc& P = L.P[c.p];
     const int j = c.y0 + threadIdx.y;

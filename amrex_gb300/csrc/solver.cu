@@ -512,7 +512,7 @@ void Engine::Impl::ghost (int l, T* phi, bool inhomog, bool do_copy, const doubl
     const long long n = L.gw.nfacecells + (do_copy ? L.gw.ntagcells : 0);
     if (n == 0) { return; }
     const int threads = 256;
-    k_ghost<T><<<(unsigned)((n + threads - 1) / threads), threads, 0, st()>>>(
+    launch(k_ghost<T>, (unsigned)((n + threads - 1) / threads), threads, 0, 
         L.dl, L.gw, phi, inhomog ? 1 : 0, bcv ? bcv : ((l == 0) ? L.bcval.p : nullptr), do_copy ? 1 : 0);
     launched();
 }
@@ -536,11 +536,11 @@ void Engine::Impl::gsrb32 (int l, float* cor, const float* res, int rb)
     const StencilPtrs S = stencil32(l);
     const unsigned g = (unsigned)L.mg.ntiles;
     if (abec) {
-        if (L.inline_bc) { k_gsrb_s<float, true, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, S, rb); }
-        else { k_gsrb_s<float, true, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, S, rb); }
+        if (L.inline_bc) { launch(k_gsrb_s<float, true, true>, g, kTileBlock, 0, L.dl, L.mg.dev(), cor, res, S, rb); }
+        else { launch(k_gsrb_s<float, true, false>, g, kTileBlock, 0, L.dl, L.mg.dev(), cor, res, S, rb); }
     } else {
-        if (L.inline_bc) { k_gsrb_s<float, false, true><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, S, rb); }
-        else { k_gsrb_s<float, false, false><<<g, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, S, rb); }
+        if (L.inline_bc) { launch(k_gsrb_s<float, false, true>, g, kTileBlock, 0, L.dl, L.mg.dev(), cor, res, S, rb); }
+        else { launch(k_gsrb_s<float, false, false>, g, kTileBlock, 0, L.dl, L.mg.dev(), cor, res, S, rb); }
     }
     launched();
 }
@@ -669,10 +669,10 @@ void Engine::Impl::smooth (int l, T* cor, const T* res, bool skip_fb)
             gsrb32(l, cor, res, rb);
         } else {
             if (abec) {
-                k_gsrb<T, true><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, coef<T>(l, 0),
+                launch(k_gsrb<T, true>, L.mg.ntiles, kTileBlock, 0, L.dl, L.mg.dev(), cor, res, coef<T>(l, 0),
                     coef<T>(l, 1), coef<T>(l, 2), coef<T>(l, 3), rb);
             } else {
-                k_gsrb<T, false><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), cor, res, nullptr, nullptr,
+                launch(k_gsrb<T, false>, L.mg.ntiles, kTileBlock, 0, L.dl, L.mg.dev(), cor, res, nullptr, nullptr,
                     nullptr, nullptr, rb);
             }
             launched();
@@ -695,10 +695,10 @@ void Engine::Impl::correction_residual (int l)
     } else {
         ghost<T>(l, cor, false, true);
         if (abec) {
-            k_residual<T, T, true><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
+            launch(k_residual<T, T, true>, L.mg.ntiles, kTileBlock, 0, L.dl, L.mg.dev(), rescor, cor, res,
                 coef<T>(l, 0), coef<T>(l, 1), coef<T>(l, 2), coef<T>(l, 3), nullptr);
         } else {
-            k_residual<T, T, false><<<L.mg.ntiles, kTileBlock, 0, st()>>>(L.dl, L.mg.dev(), rescor, cor, res,
+            launch(k_residual<T, T, false>, L.mg.ntiles, kTileBlock, 0, L.dl, L.mg.dev(), rescor, cor, res,
                 nullptr, nullptr, nullptr, nullptr, nullptr);
         }
         launched();
@@ -873,8 +873,8 @@ void Engine::Impl::fcycle ()
 void Engine::Impl::reduce_per_solve (int l, const SubsetData& S, int op, const double* x, const double* y)
 {
     const LevelData& L = lev[l];
-    k_reduce<double><<<S.ntiles, kTileBlock, 0, st()>>>(L.dl, S.dev(), x, y, op, partial.p);
-    k_reduce_final<<<nsolve, 256, 0, st()>>>(partial.p, S.solve_begin.p, op, red_out.p);
+    launch(k_reduce<double>, S.ntiles, kTileBlock, 0, L.dl, S.dev(), x, y, op, partial.p);
+    launch(k_reduce_final, nsolve, 256, 0, partial.p, S.solve_begin.p, op, red_out.p);
     launched(2);
 }
 
@@ -939,13 +939,13 @@ void Engine::Impl::residual0 (bool to32, bool norm_zeroed)
     ghost<double>(0, L.sol.p, true, true);
     const double *a = L.a.p, *bx = L.bx.p, *by = L.by.p, *bz = L.bz.p;
     if (abec) {
-        k_residual<double, double, true><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res.p,
+        launch(k_residual<double, double, true>, L.all.ntiles, kTileBlock, 0, L.dl, L.all.dev(), L.res.p,
             L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
     } else {
-        k_residual<double, double, false><<<L.all.ntiles, kTileBlock, 0, st()>>>(L.dl, L.all.dev(), L.res.p,
+        launch(k_residual<double, double, false>, L.all.ntiles, kTileBlock, 0, L.dl, L.all.dev(), L.res.p,
             L.sol.p, L.rhs.p, a, bx, by, bz, partial.p);
     }
-    k_reduce_final<<<nsolve, 256, 0, st()>>>(partial.p, L.all.solve_begin.p, RED_MAXABS, red_out.p);
+    launch(k_reduce_final, nsolve, 256, 0, partial.p, L.all.solve_begin.p, RED_MAXABS, red_out.p);
     launched(2);
 }
 
@@ -962,10 +962,10 @@ void Engine::Impl::one_iteration (bool fmg)
     if (mixed()) {
         if (any_singular) {
             // makeSolvable on the (FP32) residual: offsets from FP64 sums
-            k_reduce<float><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.res32.p, nullptr,
+            launch(k_reduce<float>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.res32.p, nullptr,
                                                                     RED_SUM, partial.p);
-            k_reduce_final<<<nsolve, 256, 0, st()>>>(partial.p, L0.all.solve_begin.p, RED_SUM, red_out.p + nsolve);
-            k_minus_offset<float><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.res32.p,
+            launch(k_reduce_final, nsolve, 256, 0, partial.p, L0.all.solve_begin.p, RED_SUM, red_out.p + nsolve);
+            launch(k_minus_offset<float>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.res32.p,
                                                                          red_out.p + nsolve, volinv0_d.p);
             launched(3);
         }
@@ -979,10 +979,10 @@ void Engine::Impl::one_iteration (bool fmg)
         if (timed) { kev_record(1); }
     } else {
         if (any_singular) {
-            k_reduce<double><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.res.p, nullptr,
+            launch(k_reduce<double>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.res.p, nullptr,
                                                                      RED_SUM, partial.p);
-            k_reduce_final<<<nsolve, 256, 0, st()>>>(partial.p, L0.all.solve_begin.p, RED_SUM, red_out.p + nsolve);
-            k_minus_offset<double><<<L0.all.ntiles, kTileBlock, 0, st()>>>(L0.dl, L0.all.dev(), L0.res.p,
+            launch(k_reduce_final, nsolve, 256, 0, partial.p, L0.all.solve_begin.p, RED_SUM, red_out.p + nsolve);
+            launch(k_minus_offset<double>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.res.p,
                                                                           red_out.p + nsolve, volinv0_d.p);
             launched(3);
         }

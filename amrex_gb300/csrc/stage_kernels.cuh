@@ -129,6 +129,8 @@ __global__ void __launch_bounds__(TILE_THREADS)
 k_gsrb (DevLevel L, Subset S, T* __restrict__ phi, const T* __restrict__ rhs, const T* __restrict__ a,
         const T* __restrict__ bx, const T* __restrict__ by, const T* __restrict__ bz, int rb)
 {
+    pdl_wait();
+    pdl_trigger();
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchDesc& P = L.P[c.p];
     const int j = c.y0 + threadIdx.y;
@@ -148,6 +150,8 @@ k_residual (DevLevel L, Subset S, TO* __restrict__ r, const T* __restrict__ x, c
             const T* __restrict__ a, const T* __restrict__ bx, const T* __restrict__ by,
             const T* __restrict__ bz, double* __restrict__ partial)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double sm[32];
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchDesc& P = L.P[c.p];
@@ -216,6 +220,8 @@ template <typename T>
 __global__ void k_ghost (DevLevel L, GhostWork W, T* __restrict__ phi, int inhomog,
                          const double* __restrict__ bcval, int do_copy)
 {
+    pdl_wait();
+    pdl_trigger();
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (tid < W.nfacecells) {
         const int w = bsearch_ll<int>(W.fstart, W.nface, tid);
@@ -407,6 +413,8 @@ __global__ void __launch_bounds__(TILE_THREADS)
 k_reduce (DevLevel L, Subset S, const T* __restrict__ x, const T* __restrict__ y, int op,
           double* __restrict__ partial)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double sm[32];
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchGeom P = geom_of(L.P[c.p]);
@@ -436,6 +444,8 @@ k_reduce (DevLevel L, Subset S, const T* __restrict__ x, const T* __restrict__ y
 static __global__ void k_reduce_final (const double* __restrict__ partial, const int* __restrict__ begin, int op,
                                 double* __restrict__ out)
 {
+    pdl_wait();
+    pdl_trigger();
     __shared__ double sm[32];
     const int s = blockIdx.x;
     double acc = 0.0;
@@ -452,6 +462,8 @@ __global__ void __launch_bounds__(TILE_THREADS)
 k_minus_offset (DevLevel L, Subset S, T* __restrict__ x, const double* __restrict__ sums,
                 const double* __restrict__ volinv)
 {
+    pdl_wait();
+    pdl_trigger();
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchGeom P = geom_of(L.P[c.p]);
     const int j = c.y0 + threadIdx.y;

@@ -189,6 +189,8 @@ template <typename T, bool VARC, bool INLINE_BC>
 __global__ void __launch_bounds__(TILE_THREADS)
 k_gsrb_s (DevLevel L, Subset Sb, T* __restrict__ phi, const T* __restrict__ rhs, StencilPtrs S, int rb)
 {
+    pdl_wait();
+    pdl_trigger();
     const TileCoord c = decode_tile(L, Sb, blockIdx.x);
     const PatchDesc& P = L.P[c.p];
     const int j = c.y0 + threadIdx.y;
