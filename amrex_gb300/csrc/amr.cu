@@ -675,14 +675,18 @@ void AmrEngine::Impl::solution_residual (int l, bool update, bool want_norm, boo
     Engine::Impl& I = *D.I;
     if (mixed() && !exact) {
         // stencil form (D x - sum s x_nb: 8 FP64 operations per cell instead of
-        // 14), with the level's max|r| by atomic max into red_out[0]
+        // 14), with the level's max|r| by atomic max into red_out[0]; on the
+        // finest level also the FP32 copy that the next iteration's
+        // correction solve starts from (nothing changes res there before it)
         if (want_norm) { MLMG_CUDA_CHECK(cudaMemsetAsync(I.red_out.p, 0, sizeof(double), st())); }
+        double* nrm = want_norm ? I.red_out.p : nullptr;
+        float* r32 = (l == nl - 1) ? Ld.res32.p : nullptr;
         if (abec()) {
             launch(k_residual_s<double, double, true, false, false>, Ld.all.ntiles, kTileBlock, 0, Ld.dl,
-                Ld.all.dev(), Ld.res.p, Ld.sol.p, Ld.rhs.p, I.stencil64(0), nullptr, want_norm ? I.red_out.p : nullptr);
+                Ld.all.dev(), Ld.res.p, Ld.sol.p, Ld.rhs.p, I.stencil64(0), nullptr, nrm, r32);
         } else {
             launch(k_residual_s<double, double, false, false, false>, Ld.all.ntiles, kTileBlock, 0, Ld.dl,
-                Ld.all.dev(), Ld.res.p, Ld.sol.p, Ld.rhs.p, StencilPtrs{}, nullptr, want_norm ? I.red_out.p : nullptr);
+                Ld.all.dev(), Ld.res.p, Ld.sol.p, Ld.rhs.p, StencilPtrs{}, nullptr, nrm, r32);
         }
         launched();
     } else {
@@ -865,8 +869,11 @@ void AmrEngine::Impl::one_iter (int iter)
         const unsigned g = (unsigned)Ld.all.ntiles;
         const T* rhs;
         if constexpr (std::is_same_v<T, float>) {
-            launch(k_amr_copy<float, double>, g, kTileBlock, 0, Ld.dl, Ld.all.dev(), Ld.res32.p, Ld.res.p);
-            launched();
+            // the finest level's FP32 copy was written with its residual
+            if (l != fin) {
+                launch(k_amr_copy<float, double>, g, kTileBlock, 0, Ld.dl, Ld.all.dev(), Ld.res32.p, Ld.res.p);
+                launched();
+            }
             rhs = Ld.res32.p;
             dres[l] = Ld.res.p;
         } else {

@@ -552,21 +552,22 @@ void Engine::Impl::resid32 (int l, float* rescor, float* cor, const float* res)
     if (!L.inline_bc) { ghost<float>(l, cor, false, true); }
     const StencilPtrs S = stencil32(l);
     const unsigned g = (unsigned)L.mg.ntiles;
+    float* const none = nullptr;
     if (abec) {
         if (L.inline_bc) {
             launch(k_residual_s<float, float, true, true, false>, g, kTileBlock, 0, L.dl, L.mg.dev(), rescor, cor,
-                                                                                       res, S, nullptr, nullptr);
+                   res, S, nullptr, nullptr, none);
         } else {
             launch(k_residual_s<float, float, true, false, false>, g, kTileBlock, 0, L.dl, L.mg.dev(), rescor, cor,
-                                                                                        res, S, nullptr, nullptr);
+                   res, S, nullptr, nullptr, none);
         }
     } else {
         if (L.inline_bc) {
             launch(k_residual_s<float, float, false, true, false>, g, kTileBlock, 0, L.dl, L.mg.dev(), rescor, cor,
-                                                                                        res, S, nullptr, nullptr);
+                   res, S, nullptr, nullptr, none);
         } else {
             launch(k_residual_s<float, float, false, false, false>, g, kTileBlock, 0, L.dl, L.mg.dev(), rescor, cor,
-                                                                                         res, S, nullptr, nullptr);
+                   res, S, nullptr, nullptr, none);
         }
     }
     launched();
@@ -919,18 +920,18 @@ void Engine::Impl::residual0 (bool to32, bool norm_zeroed)
         if (abec) {
             if (L.inline_bc) {
                 launch(k_residual_s<double, float, true, true, true>, g, kTileBlock, 0, L.dl, L.all.dev(), L.res32.p,
-                    L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
+                    L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p, (float*)nullptr);
             } else {
                 launch(k_residual_s<double, float, true, false, true>, g, kTileBlock, 0, L.dl, L.all.dev(),
-                    L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
+                    L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p, (float*)nullptr);
             }
         } else {
             if (L.inline_bc) {
                 launch(k_residual_s<double, float, false, true, true>, g, kTileBlock, 0, L.dl, L.all.dev(),
-                    L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
+                    L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p, (float*)nullptr);
             } else {
                 launch(k_residual_s<double, float, false, false, true>, g, kTileBlock, 0, L.dl, L.all.dev(),
-                    L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p);
+                    L.res32.p, L.sol.p, L.rhs.p, S, L.bcval.p, red_out.p, (float*)nullptr);
             }
         }
         launched();

@@ -238,11 +238,13 @@ __device__ __forceinline__ unsigned long long block_max_bits (unsigned long long
 // r = b - A x in stencil form (the mixed-precision paths' residuals; the FP64
 // path keeps the reference's operation order in k_residual); optional
 // per-solve max|r| by atomicMax into norm[solve] (zeroed beforehand; a
-// maximum does not depend on the order)
+// maximum does not depend on the order); optional FP32 copy of an FP64 r
+// (r32, rounded on the integer pipe)
 template <typename T, typename TO, bool VARC, bool INLINE_BC, bool INHOMOG>
 __global__ void __launch_bounds__(TILE_THREADS)
 k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x, const T* __restrict__ b,
-              StencilPtrs S, const double* __restrict__ bcval, double* __restrict__ norm)
+              StencilPtrs S, const double* __restrict__ bcval, double* __restrict__ norm,
+              float* __restrict__ r32)
 {
     __shared__ double sm[32];
     const TileCoord c = decode_tile(L, Sb, blockIdx.x);
@@ -287,6 +289,9 @@ k_residual_s (DevLevel L, Subset Sb, TO* __restrict__ r, const T* __restrict__ x
                     r[q] = d2f_bits(v);
                 } else {
                     r[q] = TO(v);
+                }
+                if constexpr (std::is_same_v<TO, double>) {
+                    if (r32 != nullptr) { r32[q] = d2f_bits(v); }
                 }
                 if constexpr (std::is_same_v<T, double>) {
                     // integer max on the bit patterns of |v| keeps the FP64 pipe
