@@ -10,6 +10,7 @@
 #include "amr_kernels.cuh"
 
 #include <array>
+#include <climits>
 #include <cmath>
 #include <map>
 
@@ -75,6 +76,8 @@ struct AmrLevelData {
     DevBuf<long long> cffstart;
     GhostWork cfw{};                        // face-cell walk over them (no copy tags)
     DevBuf<int8_t> bflags;                  // per Dirichlet-value slot: BF_* bits
+    DevBuf<int4> bitems;                    // the coarse/fine ghost cells (k_amr_bndry_list)
+    int nbitems = 0;
     DevBuf<double> bcor;                    // boundary values of the correction (physical slots 0)
     DevBuf<long long> nbr;                  // per Dirichlet-value slot: element of the covering patch's cell, or -1
                                             // (colour passes without ghost fills; empty if a closure has 4 points)
@@ -325,6 +328,7 @@ void AmrEngine::Impl::build_fine_tables (int l)
         return wrap_cell(fdom, prob.geom.periodic, c) && floc.find(c[0], c[1], c[2]) < 0;
     };
     std::vector<int8_t> flags(L(l).bcval.n, 0);
+    std::vector<int4> bitems;
     std::vector<int2> faces;
     std::vector<long long> fstart{0};
     for (int p = 0; p < (int)Mf.patches.size(); ++p) {
@@ -355,6 +359,11 @@ void AmrEngine::Impl::build_fine_tables (int l)
                     if (nc_at(0, -2)) { fl |= BF_T2LO; }
                     if (nc_at(0, 2)) { fl |= BF_T2HI; }
                     if (nc_at(-2, -2) && nc_at(2, -2) && nc_at(-2, 2) && nc_at(2, 2)) { fl |= BF_CROSS; }
+                    const long long slot = F.bcval_off + (long long)v2 * n1 + v1;
+                    const long long q = cidx(D.h_cfd[p], c[0] >> 1, c[1] >> 1, c[2] >> 1);
+                    MLMG_REQUIRE(slot < INT_MAX && q < INT_MAX, ERR_UNSUPPORTED, "coarse/fine tables above 2^31 entries");
+                    bitems.push_back(make_int4((int)slot, (int)q, p,
+                                               fl | ((c[t1] & 1) << 6) | ((c[t2] & 1) << 7) | (f << 8)));
                 }
                 flags[(size_t)(F.bcval_off + (long long)v2 * n1 + v1)] = (int8_t)fl;
             }
@@ -364,6 +373,8 @@ void AmrEngine::Impl::build_fine_tables (int l)
     D.cffstart.upload(fstart, st());
     D.cfw = GhostWork{D.cff.p, D.cffstart.p, (int)faces.size(), nullptr, nullptr, 0, fstart.back(), 0};
     D.bflags.upload(flags, st());
+    D.nbitems = (int)bitems.size();
+    upload_or_keep(D.bitems, bitems, st());
     D.bcor.alloc(L(l).bcval.n);
     D.bcor.zero(st());
     // neighbour table of the ghost-free colour passes: every copy-tag cell
@@ -663,9 +674,9 @@ void AmrEngine::Impl::solution_residual (int l, bool update, bool want_norm, boo
     if (l > 0) {
         if (update) {
             gather<double>(l, L(l - 1).sol.p);
-            if (D.cfw.nfacecells > 0) {
-                launch(k_amr_bndry<double>, blocks_for(D.cfw.nfacecells, 256), 256, 0, Ld.dl, D.cfw, D.cfd.p,
-                    D.cf64.p, D.bflags.p, Ld.bcval.p);
+            if (D.nbitems > 0) {
+                launch(k_amr_bndry_list<double>, blocks_for(D.nbitems, 256), 256, 0, (const int4*)D.bitems.p,
+                       D.nbitems, (const PatchDesc*)D.cfd.p, (const double*)D.cf64.p, Ld.bcval.p);
                 launched();
             }
         }
@@ -810,9 +821,9 @@ void AmrEngine::Impl::cor_residual (int l, bool inhomog, const TB* b, TO* out)
     if (inhomog) {
         const T* cf;
         if constexpr (std::is_same_v<T, float>) { cf = D.cf32.p; } else { cf = D.cf64.p; }
-        if (D.cfw.nfacecells > 0) {
-            launch(k_amr_bndry<T>, blocks_for(D.cfw.nfacecells, 256), 256, 0, Ld.dl, D.cfw, D.cfd.p, cf,
-                                                                               D.bflags.p, D.bcor.p);
+        if (D.nbitems > 0) {
+            launch(k_amr_bndry_list<T>, blocks_for(D.nbitems, 256), 256, 0, (const int4*)D.bitems.p, D.nbitems,
+                   (const PatchDesc*)D.cfd.p, cf, D.bcor.p);
             launched();
         }
         D.I->ghost<T>(0, x, true, true, D.bcor.p);

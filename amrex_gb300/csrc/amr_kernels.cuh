@@ -163,6 +163,51 @@ __global__ void k_amr_bndry (DevLevel Lf, GhostWork W, const PatchDesc* __restri
     bcval[slot] = c0 + y * slope[0] + (y * y) * curv[0] + z * slope[1] + (z * z) * curv[1] + y * z * cross;
 }
 
+// The same boundary values over a list of the coarse/fine ghost cells only
+// (built with the flags): x = Dirichlet-value slot, y = element of the ghost
+// cell's coarse cell in the coarse buffer, z = fine patch, w = the BF_* flags
+// | the ghost cell's parity along the first / second tangential direction
+// (bits 6, 7) | the face (bits 8..10).  No search and no covered ghost cells;
+// the arithmetic is k_amr_bndry's.
+template <typename T>
+__global__ void k_amr_bndry_list (const int4* __restrict__ items, int n, const PatchDesc* __restrict__ cfd,
+                                  const T* __restrict__ cf, double* __restrict__ bcval)
+{
+    pdl_wait();
+    pdl_trigger();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) { return; }
+    const int4 it = items[t];
+    const int fl = it.w & 63, f = it.w >> 8;
+    const int d = f % 3;
+    const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
+    const PatchDesc& G = cfd[it.z];
+    const long long st[3] = {1, (long long)G.sx, G.sxy};
+    const long long q = it.y;
+    const double c0 = (double)cf[q];
+    double slope[2], curv[2];
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+        const long long s = st[m == 0 ? t1 : t2];
+        const bool lo_nc = fl & (m == 0 ? BF_T1LO : BF_T2LO);
+        const bool hi_nc = fl & (m == 0 ? BF_T1HI : BF_T2HI);
+        const double vm = (double)cf[q - s], vp = (double)cf[q + s];
+        const double vlo = lo_nc ? vm : c0, vhi = hi_nc ? vp : c0;
+        const double fac = (lo_nc != hi_nc) ? 1.0 : 0.5;
+        slope[m] = fac * (vhi - vlo);
+        curv[m] = (lo_nc && hi_nc) ? 0.5 * (vp - 2.0 * c0 + vm) : 0.0;
+    }
+    double cross = 0.0;
+    if (fl & BF_CROSS) {
+        const long long s1 = st[t1], s2 = st[t2];
+        cross = 0.25 * ((double)cf[q + s1 + s2] - (double)cf[q - s1 + s2] + (double)cf[q - s1 - s2]
+                        - (double)cf[q + s1 - s2]);
+    }
+    const double y = -0.5 + ((double)((it.w >> 6) & 1) + 0.5) / 2.0;
+    const double z = -0.5 + ((double)((it.w >> 7) & 1) + 0.5) / 2.0;
+    bcval[it.x] = c0 + y * slope[0] + (y * y) * curv[0] + z * slope[1] + (z * z) * curv[1] + y * z * cross;
+}
+
 // ----------------------------------------------------------------- reflux --
 // One coarse cell next to the fine level and the faces it shares with it.
 struct RefluxCell {
