@@ -163,7 +163,7 @@ struct AmrEngine::Impl {
     // mixed precision
     void solution_residual (int l, bool update, bool want_norm = false, bool exact = false);
     void reflux (int c);
-    void avgdown (int c, const double* fine, double* crse);
+    void avgdown (int c, const double* fine, double* crse, float* crse32 = nullptr);
     template <typename T> void gather (int l, const T* crse);
     template <typename T> T* cor (int l);
     template <typename T> T* hold (int l);
@@ -611,7 +611,7 @@ void AmrEngine::Impl::average_down_coefficients ()
         LevelData& Lf = L(c + 1);
         if (prob.alpha != 0.0 && D.nacell > 0) {
             launch(k_amr_avgdown<double, double>, blocks_for(D.nacell, 256), 256, 0, Lc.dl, Lf.dl, D.atags.p,
-                D.astart.p, D.natag, D.nacell, Lf.a.p, Lc.a.p);
+                D.astart.p, D.natag, D.nacell, Lf.a.p, Lc.a.p, (float*)nullptr);
             launched();
         }
         const double* fb[3] = {Lf.bx.p, Lf.by.p, Lf.bz.p};
@@ -686,12 +686,12 @@ void AmrEngine::Impl::solution_residual (int l, bool update, bool want_norm, boo
     Engine::Impl& I = *D.I;
     if (mixed() && !exact) {
         // stencil form (D x - sum s x_nb: 8 FP64 operations per cell instead of
-        // 14), with the level's max|r| by atomic max into red_out[0]; on the
-        // finest level also the FP32 copy that the next iteration's
-        // correction solve starts from (nothing changes res there before it)
+        // 14), with the level's max|r| by atomic max into red_out[0], and the
+        // FP32 copy the level's correction solve starts from (the reflux and
+        // the average-down that change res afterwards update it too)
         if (want_norm) { MLMG_CUDA_CHECK(cudaMemsetAsync(I.red_out.p, 0, sizeof(double), st())); }
         double* nrm = want_norm ? I.red_out.p : nullptr;
-        float* r32 = (l == nl - 1) ? Ld.res32.p : nullptr;
+        float* r32 = Ld.res32.p;
         if (abec()) {
             launch(k_residual_s<double, double, true, false, false>, Ld.all.ntiles, kTileBlock, 0, Ld.dl,
                 Ld.all.dev(), Ld.res.p, Ld.sol.p, Ld.rhs.p, I.stencil64(0), nullptr, nrm, r32);
@@ -730,21 +730,21 @@ void AmrEngine::Impl::reflux (int c)
     if (D.nrcell > 0) {
         if (abec()) {
             launch(k_amr_reflux<true>, blocks_for(D.nrcell, 128), 128, 0, Lf.dl, D.rcells.p, D.rfaces.p, D.nrcell,
-                D.rprm, reflux_coef(c), Lc.sol.p, Lf.sol.p, Lc.res.p);
+                D.rprm, reflux_coef(c), Lc.sol.p, Lf.sol.p, Lc.res.p, mixed() ? Lc.res32.p : nullptr);
         } else {
             launch(k_amr_reflux<false>, blocks_for(D.nrcell, 128), 128, 0, Lf.dl, D.rcells.p, D.rfaces.p, D.nrcell,
-                D.rprm, RefluxCoef{}, Lc.sol.p, Lf.sol.p, Lc.res.p);
+                D.rprm, RefluxCoef{}, Lc.sol.p, Lf.sol.p, Lc.res.p, mixed() ? Lc.res32.p : nullptr);
         }
         launched();
     }
 }
 
-void AmrEngine::Impl::avgdown (int c, const double* fine, double* crse)
+void AmrEngine::Impl::avgdown (int c, const double* fine, double* crse, float* crse32)
 {
     AmrLevelData& D = lev[c];
     if (D.nacell == 0) { return; }
     launch(k_amr_avgdown<double, double>, blocks_for(D.nacell, 256), 256, 0, L(c).dl, L(c + 1).dl, D.atags.p,
-        D.astart.p, D.natag, D.nacell, fine, crse);
+        D.astart.p, D.natag, D.nacell, fine, crse, crse32);
     launched();
 }
 
@@ -880,11 +880,7 @@ void AmrEngine::Impl::one_iter (int iter)
         const unsigned g = (unsigned)Ld.all.ntiles;
         const T* rhs;
         if constexpr (std::is_same_v<T, float>) {
-            // the finest level's FP32 copy was written with its residual
-            if (l != fin) {
-                launch(k_amr_copy<float, double>, g, kTileBlock, 0, Ld.dl, Ld.all.dev(), Ld.res32.p, Ld.res.p);
-                launched();
-            }
+            // res32 was written with res (residual, reflux, average-down)
             rhs = Ld.res32.p;
             dres[l] = Ld.res.p;
         } else {
@@ -898,15 +894,11 @@ void AmrEngine::Impl::one_iter (int iter)
         solution_residual(l - 1, l - 1 > 0);
         cor_residual<T, T, double>(l, false, rhs, dres[l]);
         reflux(l - 1);
-        avgdown(l - 1, dres[l], L(l - 1).res.p);
+        avgdown(l - 1, dres[l], L(l - 1).res.p, std::is_same_v<T, float> ? L(l - 1).res32.p : nullptr);
         if (l != fin) { std::swap(lev[l].cor_p, lev[l].hold_p); }
     }
     {
         LevelData& L0 = L(0);
-        if constexpr (std::is_same_v<T, float>) {
-            launch(k_amr_copy<float, double>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.res32.p, L0.res.p);
-            launched();
-        }
         if (iter < A.m_opt.max_fmg_iter) { I0.fcycle<T>(); } else { I0.vcycle<T>(0); }
         launch(k_add_to<double, T>, L0.all.ntiles, kTileBlock, 0, L0.dl, L0.all.dev(), L0.sol.p, cor<T>(0), nullptr,
                nullptr, 0);

@@ -48,7 +48,7 @@ __global__ void k_amr_gather (DevLevel Lc, const PatchDesc* __restrict__ cfd, co
 template <typename TD, typename TS>
 __global__ void k_amr_avgdown (DevLevel Lc, DevLevel Lf, const CopyTag* __restrict__ tags,
                                const long long* __restrict__ start, int ntag, long long ncell,
-                               const TS* __restrict__ fine, TD* __restrict__ crse)
+                               const TS* __restrict__ fine, TD* __restrict__ crse, float* __restrict__ crse32)
 {
     pdl_wait();
     pdl_trigger();
@@ -65,7 +65,9 @@ __global__ void k_amr_avgdown (DevLevel Lc, DevLevel Lf, const CopyTag* __restri
     v += (double)fine[qf + sx];       v += (double)fine[qf + sx + 1];
     v += (double)fine[qf + sxy];      v += (double)fine[qf + sxy + 1];
     v += (double)fine[qf + sxy + sx]; v += (double)fine[qf + sxy + sx + 1];
-    crse[cidx(Lc.P[C.dst], i, j, k)] = TD(0.125 * v);
+    const long long qc = cidx(Lc.P[C.dst], i, j, k);
+    crse[qc] = TD(0.125 * v);
+    if (crse32 != nullptr) { crse32[qc] = d2f_bits(double(TD(0.125 * v))); }
 }
 
 // average_down_faces with the coarse geometry (Src/Base/AMReX_MultiFabUtil.H:
@@ -244,7 +246,8 @@ struct RefluxCoef {     // MLABecLaplacian: beta and the face b of both levels
 template <bool ABEC>
 __global__ void k_amr_reflux (DevLevel Lf, const RefluxCell* __restrict__ cells, const RefluxFace* __restrict__ faces,
                               int ncell, RefluxParams prm, RefluxCoef co, const double* __restrict__ sol_c,
-                              const double* __restrict__ sol_f, double* __restrict__ res_c)
+                              const double* __restrict__ sol_f, double* __restrict__ res_c,
+                              float* __restrict__ res32_c)
 {
     pdl_wait();
     pdl_trigger();
@@ -285,7 +288,9 @@ __global__ void k_amr_reflux (DevLevel Lf, const RefluxCell* __restrict__ cells,
         }
         dfine += acc;
     }
-    res_c[C.q] += dc + dfine;
+    const double nv = res_c[C.q] + (dc + dfine);
+    res_c[C.q] = nv;
+    if (res32_c != nullptr) { res32_c[C.q] = d2f_bits(nv); }
 }
 
 // per-block max|x| over the valid cells whose `covered` byte is 0 (the
