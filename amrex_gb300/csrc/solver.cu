@@ -454,7 +454,10 @@ void Engine::Impl::xfer (const std::vector<XferItem>& items, const FabSet& fs, v
 {
     if (items.empty()) { return; }
     std::vector<long long> start{0};
-    for (const auto& X : items) { start.push_back(start.back() + X.region.npts()); }
+    for (const auto& X : items) {
+        MLMG_REQUIRE(X.region.npts() < (1ll << 32), ERR_UNSUPPORTED, "a FAB of 2^32 cells or more");
+        start.push_back(start.back() + X.region.npts());
+    }
     // grow-only tables (no allocation once large enough); stream order keeps
     // the next transfer's upload behind this one's kernel
     xfer_items.upload(items, st());

@@ -509,11 +509,14 @@ __global__ void k_xfer (DevLevel L, const XferItem* __restrict__ items, const lo
     if (t >= ncell) { return; }
     const int w = bsearch_ll<int>(start, nitem, t);
     const XferItem& X = items[w];
-    const long long u = t - start[w];
-    const int nx = X.region.hi[0] - X.region.lo[0] + 1, ny = X.region.hi[1] - X.region.lo[1] + 1;
-    const int i = X.region.lo[0] + (int)(u % nx);
-    const int j = X.region.lo[1] + (int)((u / nx) % ny);
-    const int k = X.region.lo[2] + (int)(u / ((long long)nx * ny));
+    // a region holds fewer than 2^32 cells: 32-bit index arithmetic (a
+    // 64-bit division costs several times as many instructions)
+    const unsigned u = (unsigned)(t - start[w]);
+    const unsigned nx = X.region.hi[0] - X.region.lo[0] + 1, ny = X.region.hi[1] - X.region.lo[1] + 1;
+    const unsigned row = u / nx;
+    const int i = X.region.lo[0] + (int)(u - row * nx);
+    const int j = X.region.lo[1] + (int)(row % ny);
+    const int k = X.region.lo[2] + (int)(row / ny);
     const long long qm = X.src_off + (long long)(k - X.flo[2]) * X.fsxy + (long long)(j - X.flo[1]) * X.fsx
                        + (i - X.flo[0]);
     const long long qp = cidx(L.P[X.patch], i, j, k);

@@ -526,12 +526,17 @@ def bench_amr(stream, reps=3):
 
         step()
         ag.kernel_launches(reset=True)
+        dev = 0.0
         e0.record(stream)
         for _ in range(reps):
             resid = step()
+            dev += m.solveTimeMs()
         e1.record(stream)
         e1.synchronize()
         out[f"{prec}_ms"] = e0.elapsed_time(e1) / reps
+        # the solve's own device time: its iterations, without the transfers
+        # between the MultiFabs and the level fields and the zero fill
+        out[f"{prec}_solve_device_ms"] = dev / reps
         out[f"{prec}_iters"] = m.getNumIters()
         out[f"{prec}_final_resid_rel"] = resid / m.getInitRHS()
         out[f"{prec}_launches_per_solve"] = ag.kernel_launches() // reps
