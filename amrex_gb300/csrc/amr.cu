@@ -782,8 +782,18 @@ void AmrEngine::Impl::mini_cycle (int l, const T* rhs)
                     launched();
                 }
                 if (D.nrest > 0) {
-                    launch(k_gsrb_tiles, D.nrest, blk, 0, Ld.dl, D.fz_rest.p, in, in, b, rhs, D.nbr.p, 0);
-                    launch(k_gsrb_tiles, D.nrest, blk, 0, Ld.dl, D.fz_rest.p, in, b, b, rhs, D.nbr.p, 1);
+                    const float* bb = b;
+                    if (in == nullptr) {
+                        launch(k_gsrb_tiles<false, false>, D.nrest, blk, 0, Ld.dl, D.fz_rest.p, in, in, b, rhs,
+                               D.nbr.p, 0);
+                        launch(k_gsrb_tiles<false, true>, D.nrest, blk, 0, Ld.dl, D.fz_rest.p, in, bb, b, rhs,
+                               D.nbr.p, 1);
+                    } else {
+                        launch(k_gsrb_tiles<true, true>, D.nrest, blk, 0, Ld.dl, D.fz_rest.p, in, in, b, rhs,
+                               D.nbr.p, 0);
+                        launch(k_gsrb_tiles<true, true>, D.nrest, blk, 0, Ld.dl, D.fz_rest.p, in, bb, b, rhs,
+                               D.nbr.p, 1);
+                    }
                     launched(2);
                 }
                 std::swap(a, b);

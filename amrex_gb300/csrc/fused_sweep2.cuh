@@ -470,36 +470,41 @@ k_resid_restrict_tma (DevLevel L, Subset S, DevLevel Lc, const float* __restrict
 // tiles of an AMR fine level (the tiles whose halo meets a face shared with
 // another patch): old cell values from `old` (null: a zero correction),
 // neighbours from `nb` (the old array for the first colour, the new one for
-// the second), results into `out`.  A ghost covered by another patch is that
+// the second; null: zeros), results into `out`.  A ghost covered by another patch is that
 // patch's cell (nbr), any other ghost the homogeneous closure; the update is
 // the fused sweep's arithmetic, so a cell gets the value the fused sweep gives
 // it from the same neighbours.  Launched for the first colour over these tiles
 // together with the fused sweep over the others (both read only the old
 // array), then for the second colour.
+template <bool OLD, bool NB>
 static __global__ void __launch_bounds__(FS_THREADS)
 k_gsrb_tiles (DevLevel L, const int4* __restrict__ tiles, const float* __restrict__ old, const float* __restrict__ nb,
               float* __restrict__ out, const float* __restrict__ rhs, const long long* __restrict__ nbr, int rb)
 {
     const int4 t = tiles[blockIdx.x];
     const PatchDesc& P = L.P[t.x];
+    // the patch's geometry in registers (as far as the compiler knows, the
+    // stores below could change the descriptor, which it would then reload
+    // for every cell); offsets inside the tile in 32 bits from its first cell
+    const int lo0 = P.lo[0], lo1 = P.lo[1], lo2 = P.lo[2], hi0 = P.hi[0], hi1 = P.hi[1], hi2 = P.hi[2];
+    const int sx = P.sx, sxy = (int)P.sxy;
+    const float dhx = float(P.dha[0]), dhy = float(P.dha[1]), dhz = float(P.dha[2]);
+    const float cdx = -dhx, cdy = -dhy, cdz = -dhz, cd = -2.0f * (dhx + dhy + dhz);
+    const long long q00 = cidx(P, t.y, t.z, t.w);
     pdl_wait();
     pdl_trigger();
     // lanes 0..15 take the 16 cells of the colour in a row of plane lz, lanes
     // 16..31 those of plane lz + 1
     const int j = t.z + threadIdx.y;
     const int half = threadIdx.x >> 4, r = threadIdx.x & 15;
-    if (j > P.hi[1]) { return; }
-    const float dhx = float(P.dha[0]), dhy = float(P.dha[1]), dhz = float(P.dha[2]);
-    const float cdx = -dhx, cdy = -dhy, cdz = -dhz, cd = -2.0f * (dhx + dhy + dhz);
-    const long long sx = P.sx, sxy = P.sxy;
-    auto val = [&] (const float* a, long long q) -> float { return (a != nullptr) ? a[q] : 0.0f; };
+    if (j > hi1) { return; }
     // the ghost across face f: the covering patch's cell, or the closure
     // (which also adds the face's diagonal term, s_f * fco_f, to corr)
     auto ghost = [&] (int f, int i, int k, float pc, long long qin, float s, float& corr) -> float {
-        const long long v = nbr[P.face[f].bcval_off + face_local(P, f, i, j, k)];
-        if (v >= 0) { return val(nb, v); }
         const FaceBC& F = P.face[f];
-        const float pin = val(nb, qin);
+        const long long v = nbr[F.bcval_off + face_local(P, f, i, j, k)];
+        if (v >= 0) { return NB ? nb[v] : 0.0f; }
+        const float pin = NB ? nb[qin] : 0.0f;
         float g = 0.0f;
         if (F.type == BC_DIRICHLET) {
             const float c1 = float(F.coef[1]), c2 = float(F.coef[2]);
@@ -515,22 +520,21 @@ k_gsrb_tiles (DevLevel L, const int4* __restrict__ tiles, const float* __restric
     };
     for (int lz = half; lz < FS_TZ; lz += 2) {
         const int k = t.w + lz;
-        if (k > P.hi[2]) { break; }
+        if (k > hi2) { break; }
         const int i = t.y + 2 * r + ((t.y + j + k + rb) & 1);
-        if (i > P.hi[0]) { continue; }
-        const long long q = cidx(P, i, j, k);
-        const float pc = val(old, q);
+        if (i > hi0) { continue; }
+        const long long q = q00 + (lz * sxy + (int)threadIdx.y * sx + (i - t.y));
+        const float pc = OLD ? old[q] : 0.0f;
         // the closures' diagonal terms accumulate in the fused sweep's order
         // (x-lo, x-hi, y-lo, y-hi, z-lo, z-hi)
         float corr = 0.0f;
-        const float xm = (i == P.lo[0]) ? ghost(0, i, k, pc, q + 1, cdx, corr) : val(nb, q - 1);
-        const float xp = (i == P.hi[0]) ? ghost(3, i, k, pc, q - 1, cdx, corr) : val(nb, q + 1);
-        const float ym = (j == P.lo[1]) ? ghost(1, i, k, pc, q + sx, cdy, corr) : val(nb, q - sx);
-        const float yp = (j == P.hi[1]) ? ghost(4, i, k, pc, q - sx, cdy, corr) : val(nb, q + sx);
-        const float zm = (k == P.lo[2]) ? ghost(2, i, k, pc, q + sxy, cdz, corr) : val(nb, q - sxy);
-        const float zp = (k == P.hi[2]) ? ghost(5, i, k, pc, q - sxy, cdz, corr) : val(nb, q + sxy);
-        const bool face = (i == P.lo[0]) | (i == P.hi[0]) | (j == P.lo[1]) | (j == P.hi[1]) | (k == P.lo[2]) |
-                          (k == P.hi[2]);
+        const float xm = (i == lo0) ? ghost(0, i, k, pc, q + 1, cdx, corr) : (NB ? nb[q - 1] : 0.0f);
+        const float xp = (i == hi0) ? ghost(3, i, k, pc, q - 1, cdx, corr) : (NB ? nb[q + 1] : 0.0f);
+        const float ym = (j == lo1) ? ghost(1, i, k, pc, q + sx, cdy, corr) : (NB ? nb[q - sx] : 0.0f);
+        const float yp = (j == hi1) ? ghost(4, i, k, pc, q - sx, cdy, corr) : (NB ? nb[q + sx] : 0.0f);
+        const float zm = (k == lo2) ? ghost(2, i, k, pc, q + sxy, cdz, corr) : (NB ? nb[q - sxy] : 0.0f);
+        const float zp = (k == hi2) ? ghost(5, i, k, pc, q - sxy, cdz, corr) : (NB ? nb[q + sxy] : 0.0f);
+        const bool face = (i == lo0) | (i == hi0) | (j == lo1) | (j == hi1) | (k == lo2) | (k == hi2);
         const float gmd = face ? cd - corr : cd;
         const float d = cd, sxl = cdx, sxh = cdx, syl = cdy, syh = cdy, szl = cdz, szh = cdz;
         const float rho = sxl * xm + sxh * xp + syl * ym + syh * yp + szl * zm + szh * zp;
