@@ -466,7 +466,7 @@ void Engine::Impl::xfer (const std::vector<XferItem>& items, const FabSet& fs, v
     const long long* d_start = xfer_start.p;
     const long long n = start.back();
     const int threads = 256;
-    const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+    const unsigned blocks = (unsigned)((n + (long long)threads * XF_CELLS - 1) / ((long long)threads * XF_CELLS));
     const DevLevel& dl = lev[0].dl;
     if (fs.prec == 8 && !field_is_f32) {
         k_xfer<double, double><<<blocks, threads, 0, st()>>>(dl, d_items, d_start, (int)items.size(), n,

@@ -500,27 +500,54 @@ struct XferItem {
     long long fsxy;       // FAB x*y extent
 };
 
-// dir 0: MultiFab -> patch field ; dir 1: patch field -> MultiFab
+// dir 0: MultiFab -> patch field ; dir 1: patch field -> MultiFab.  Each
+// thread moves XF_CELLS cells blockDim.x apart (coalesced per step): one
+// search of the item list for the first, then a walk forward (items hold at
+// least one cell, most of them thousands), all loads issued before the stores.
+constexpr int XF_CELLS = 8;
 template <typename TM, typename TP>
 __global__ void k_xfer (DevLevel L, const XferItem* __restrict__ items, const long long* __restrict__ start,
                         int nitem, long long ncell, TM* __restrict__ mf, TP* __restrict__ field, int dir)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ncell) { return; }
-    const int w = bsearch_ll<int>(start, nitem, t);
-    const XferItem& X = items[w];
-    // a region holds fewer than 2^32 cells: 32-bit index arithmetic (a
-    // 64-bit division costs several times as many instructions)
-    const unsigned u = (unsigned)(t - start[w]);
-    const unsigned nx = X.region.hi[0] - X.region.lo[0] + 1, ny = X.region.hi[1] - X.region.lo[1] + 1;
-    const unsigned row = u / nx;
-    const int i = X.region.lo[0] + (int)(u - row * nx);
-    const int j = X.region.lo[1] + (int)(row % ny);
-    const int k = X.region.lo[2] + (int)(row / ny);
-    const long long qm = X.src_off + (long long)(k - X.flo[2]) * X.fsxy + (long long)(j - X.flo[1]) * X.fsx
-                       + (i - X.flo[0]);
-    const long long qp = cidx(L.P[X.patch], i, j, k);
-    if (dir == 0) { field[qp] = TP(mf[qm]); } else { mf[qm] = TM(field[qp]); }
+    const long long t0 = (long long)blockIdx.x * blockDim.x * XF_CELLS + threadIdx.x;
+    if (t0 >= ncell) { return; }
+    int w = bsearch_ll<int>(start, nitem, t0);
+    long long qs[XF_CELLS], qd[XF_CELLS];
+    int m_n = 0;
+#pragma unroll
+    for (int m = 0; m < XF_CELLS; ++m) {
+        const long long t = t0 + (long long)m * blockDim.x;
+        if (t < ncell) {
+            while (w + 1 < nitem && start[w + 1] <= t) { ++w; }
+            const XferItem& X = items[w];
+            // a region holds fewer than 2^32 cells: 32-bit index arithmetic
+            const unsigned u = (unsigned)(t - start[w]);
+            const unsigned nx = X.region.hi[0] - X.region.lo[0] + 1, ny = X.region.hi[1] - X.region.lo[1] + 1;
+            const unsigned row = u / nx;
+            const int i = X.region.lo[0] + (int)(u - row * nx);
+            const int j = X.region.lo[1] + (int)(row % ny);
+            const int k = X.region.lo[2] + (int)(row / ny);
+            const long long qm = X.src_off + (long long)(k - X.flo[2]) * X.fsxy + (long long)(j - X.flo[1]) * X.fsx
+                               + (i - X.flo[0]);
+            const long long qp = cidx(L.P[X.patch], i, j, k);
+            qs[m] = (dir == 0) ? qm : qp;
+            qd[m] = (dir == 0) ? qp : qm;
+            m_n = m + 1;
+        }
+    }
+    if (dir == 0) {
+        TP v[XF_CELLS];
+#pragma unroll
+        for (int m = 0; m < XF_CELLS; ++m) { if (m < m_n) { v[m] = TP(mf[qs[m]]); } }
+#pragma unroll
+        for (int m = 0; m < XF_CELLS; ++m) { if (m < m_n) { field[qd[m]] = v[m]; } }
+    } else {
+        TM v[XF_CELLS];
+#pragma unroll
+        for (int m = 0; m < XF_CELLS; ++m) { if (m < m_n) { v[m] = TM(field[qs[m]]); } }
+#pragma unroll
+        for (int m = 0; m < XF_CELLS; ++m) { if (m < m_n) { mf[qd[m]] = v[m]; } }
+    }
 }
 
 // ------------------------------------------------- coefficient restriction --
