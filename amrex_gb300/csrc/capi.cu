@@ -893,8 +893,9 @@ int mlmg_multifab_setval (mlmg_multifab mf, double v)
     if (mf->prec == 8) { k_fill<double><<<nb, 256, 0, st>>>(n, (double*)mf->data.p, v); }
     else { k_fill<float><<<nb, 256, 0, st>>>(n, (float*)mf->data.p, (float)v); }
     g_launches++;
+    // stream-ordered like every other access to the MultiFab's data (the
+    // downloads synchronise), so the host does not wait here
     MLMG_CUDA_CHECK(cudaGetLastError());
-    MLMG_CUDA_CHECK(cudaStreamSynchronize(st));
     API_END
 }
 
