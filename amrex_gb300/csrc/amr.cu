@@ -976,11 +976,12 @@ void AmrEngine::solve (const std::vector<const FabSet*>& sol_in, const std::vect
                  "one sol and one rhs per AMR level");
     MLMG_REQUIRE(!M.lev[0].I->singular[0], ERR_UNSUPPORTED, "singular AMR composite solves are not supported");
     m_report = SolveReport{};
+    // the valid cells of sol and rhs; their other elements (zero since the
+    // fields were allocated) are written before they are read: the ghost
+    // shells by the fills ahead of every stencil, the padding never
     for (int l = 0; l < nl; ++l) {
         LevelData& Ld = M.L(l);
         Engine::Impl& I = *M.lev[l].I;
-        MLMG_CUDA_CHECK(cudaMemsetAsync(Ld.sol.p, 0, Ld.sol.n * sizeof(double), m_stream));
-        MLMG_CUDA_CHECK(cudaMemsetAsync(Ld.rhs.p, 0, Ld.rhs.n * sizeof(double), m_stream));
         I.xfer(I.items_for(*sol_in[l], 0, 0, -1), *sol_in[l], Ld.sol.p, false, 0);
         I.xfer(I.items_for(*rhs[l], 0, 0, -1), *rhs[l], Ld.rhs.p, false, 0);
     }

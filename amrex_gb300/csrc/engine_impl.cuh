@@ -215,10 +215,21 @@ struct Engine::Impl {
     void load_level0_field (const FabSet* fs, double* field, double defval, int nodal_dir, int s);
     void xfer (const std::vector<XferItem>& items, const FabSet& fs, void* field, bool field_is_f32, int dir);
     std::vector<XferItem> items_for (const FabSet& fs, int s, int ghost_mode, int nodal_dir) const;
-    // transfer tables: grow-only device copies, and per solve a locator of
-    // its level-0 patches (built on first use)
-    DevBuf<XferItem> xfer_items;
-    DevBuf<long long> xfer_start;
+    // transfer tables: device copies kept while a transfer's items recur (a
+    // MultiFab and a level give the same items from call to call, and an
+    // upload from pageable memory makes the host wait for the stream), least
+    // recently used replaced; per solve a locator of its level-0 patches
+    struct XferTables {
+        std::vector<XferItem> items;
+        DevBuf<XferItem> d_items;
+        DevBuf<long long> d_start;
+        long long n = 0;
+        unsigned long long used = 0;
+    };
+    static constexpr size_t XFER_TABLES = 8;
+    std::vector<std::unique_ptr<XferTables>> xfer_tables;
+    unsigned long long xfer_tick = 0;
+    const XferTables& xfer_tables_for (const std::vector<XferItem>& items);
     mutable std::vector<std::unique_ptr<BoxLocator>> xfer_loc;
 
     // ------------------------------------------------------- operations --

@@ -449,22 +449,59 @@ std::vector<XferItem> Engine::Impl::items_for (const FabSet& fs, int s, int ghos
     return items;
 }
 
+namespace {
+bool same_item (const XferItem& a, const XferItem& b)
+{
+    for (int d = 0; d < 3; ++d) {
+        if (a.region.lo[d] != b.region.lo[d] || a.region.hi[d] != b.region.hi[d] || a.flo[d] != b.flo[d]) {
+            return false;
+        }
+    }
+    return a.patch == b.patch && a.src_off == b.src_off && a.fsx == b.fsx && a.fsxy == b.fsxy;
+}
+} // namespace
+
+const Engine::Impl::XferTables& Engine::Impl::xfer_tables_for (const std::vector<XferItem>& items)
+{
+    XferTables* T = nullptr;
+    for (auto& c : xfer_tables) {
+        if (c->items.size() != items.size()) { continue; }
+        bool same = true;
+        for (size_t w = 0; w < items.size() && same; ++w) { same = same_item(c->items[w], items[w]); }
+        if (same) { T = c.get(); break; }
+    }
+    if (T == nullptr) {
+        if (xfer_tables.size() < XFER_TABLES) {
+            xfer_tables.push_back(std::make_unique<XferTables>());
+            T = xfer_tables.back().get();
+        } else {
+            T = xfer_tables[0].get();
+            for (auto& c : xfer_tables) { if (c->used < T->used) { T = c.get(); } }
+        }
+        std::vector<long long> start{0};
+        for (const auto& X : items) {
+            MLMG_REQUIRE(X.region.npts() < (1ll << 32), ERR_UNSUPPORTED, "a FAB of 2^32 cells or more");
+            start.push_back(start.back() + X.region.npts());
+        }
+        // stream order keeps the upload behind the kernels that read the
+        // tables this one replaces
+        T->items = items;
+        T->d_items.upload(items, st());
+        T->d_start.upload(start, st());
+        T->n = start.back();
+    }
+    T->used = ++xfer_tick;
+    return *T;
+}
+
 void Engine::Impl::xfer (const std::vector<XferItem>& items, const FabSet& fs, void* field, bool field_is_f32,
                          int dir)
 {
     if (items.empty()) { return; }
-    std::vector<long long> start{0};
-    for (const auto& X : items) {
-        MLMG_REQUIRE(X.region.npts() < (1ll << 32), ERR_UNSUPPORTED, "a FAB of 2^32 cells or more");
-        start.push_back(start.back() + X.region.npts());
-    }
-    // grow-only tables (no allocation once large enough); stream order keeps
-    // the next transfer's upload behind this one's kernel
-    xfer_items.upload(items, st());
-    xfer_start.upload(start, st());
-    const XferItem* d_items = xfer_items.p;
-    const long long* d_start = xfer_start.p;
-    const long long n = start.back();
+    const XferTables& T = xfer_tables_for(items);
+    const XferItem* d_items = T.d_items.p;
+    const long long* d_start = T.d_start.p;
+    const long long n = T.n;
     const int threads = 256;
     const unsigned blocks = (unsigned)((n + (long long)threads * XF_CELLS - 1) / ((long long)threads * XF_CELLS));
     const DevLevel& dl = lev[0].dl;
