@@ -90,26 +90,51 @@ __global__ void k_fab_tags (const FabInfo* __restrict__ fi, const FabTag* __rest
 }
 
 // global array <-> FAB cells.  dir 0: global -> FAB (cells of the grown box
-// inside the global array); dir 1: FAB valid cells -> global
+// inside the global array); dir 1: FAB valid cells -> global.  The global
+// array may be host memory read or written over NVLink-C2C, which wants many
+// requests in flight: each thread moves FG_CELLS cells blockDim.x apart (one
+// region search, then a walk forward; 32-bit index arithmetic inside a
+// region), all loads before the stores.
+constexpr int FG_CELLS = 8;
 template <typename T>
 __global__ void k_fab_global (const FabInfo* __restrict__ fi, const Box3* __restrict__ regions,
                               const long long* __restrict__ start, int nbox, long long n, T* __restrict__ data,
                               T* __restrict__ glob, int g0, int g1, int g2, int gnx, int gny, int dir)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) { return; }
-    int lo = 0, hi = nbox - 1;
-    while (lo < hi) { const int mid = (lo + hi + 1) >> 1; if (start[mid] <= t) { lo = mid; } else { hi = mid - 1; } }
-    const Box3& R = regions[lo];
-    const FabInfo& F = fi[lo];
-    const long long u = t - start[lo];
-    const int nx = R.hi[0] - R.lo[0] + 1, ny = R.hi[1] - R.lo[1] + 1;
-    const int i = R.lo[0] + (int)(u % nx);
-    const int j = R.lo[1] + (int)((u / nx) % ny);
-    const int k = R.lo[2] + (int)(u / ((long long)nx * ny));
-    const long long qf = F.off + (long long)(k - F.lo[2]) * F.sxy + (long long)(j - F.lo[1]) * F.sx + (i - F.lo[0]);
-    const long long qg = ((long long)(k - g2) * gny + (j - g1)) * gnx + (i - g0);
-    if (dir == 0) { data[qf] = glob[qg]; } else { glob[qg] = data[qf]; }
+    const long long t0 = (long long)blockIdx.x * blockDim.x * FG_CELLS + threadIdx.x;
+    if (t0 >= n) { return; }
+    int w = 0, hi = nbox - 1;
+    while (w < hi) { const int mid = (w + hi + 1) >> 1; if (start[mid] <= t0) { w = mid; } else { hi = mid - 1; } }
+    long long qs[FG_CELLS], qd[FG_CELLS];
+    int m_n = 0;
+#pragma unroll
+    for (int m = 0; m < FG_CELLS; ++m) {
+        const long long t = t0 + (long long)m * blockDim.x;
+        if (t < n) {
+            while (w + 1 < nbox && start[w + 1] <= t) { ++w; }
+            const Box3& R = regions[w];
+            const FabInfo& F = fi[w];
+            const unsigned u = (unsigned)(t - start[w]);
+            const unsigned nx = R.hi[0] - R.lo[0] + 1, ny = R.hi[1] - R.lo[1] + 1;
+            const unsigned row = u / nx;
+            const int i = R.lo[0] + (int)(u - row * nx);
+            const int j = R.lo[1] + (int)(row % ny);
+            const int k = R.lo[2] + (int)(row / ny);
+            const long long qf = F.off + (long long)(k - F.lo[2]) * F.sxy + (long long)(j - F.lo[1]) * F.sx
+                               + (i - F.lo[0]);
+            const long long qg = ((long long)(k - g2) * gny + (j - g1)) * gnx + (i - g0);
+            qs[m] = (dir == 0) ? qg : qf;
+            qd[m] = (dir == 0) ? qf : qg;
+            m_n = m + 1;
+        }
+    }
+    const T* src = (dir == 0) ? glob : data;
+    T* dst = (dir == 0) ? data : glob;
+    T v[FG_CELLS];
+#pragma unroll
+    for (int m = 0; m < FG_CELLS; ++m) { if (m < m_n) { v[m] = src[qs[m]]; } }
+#pragma unroll
+    for (int m = 0; m < FG_CELLS; ++m) { if (m < m_n) { dst[qd[m]] = v[m]; } }
 }
 
 template <typename T>
@@ -310,6 +335,7 @@ void fab_global (mlmg_multifab_s& mf, void* host, const int glo[3], const int gn
             r = intersect(v, gbox);
         }
         if (!r.ok()) { r = Box3{{0, 0, 0}, {-1, -1, -1}}; }
+        MLMG_REQUIRE(!r.ok() || r.npts() < (1ll << 32), ERR_UNSUPPORTED, "a FAB of 2^32 cells or more");
         regions.push_back(r);
         start.push_back(start.back() + (r.ok() ? r.npts() : 0));
     }
@@ -332,7 +358,8 @@ void fab_global (mlmg_multifab_s& mf, void* host, const int glo[3], const int gn
         MLMG_CUDA_CHECK(cudaMemcpyAsync(stage, host, ng * sizeof(T), cudaMemcpyHostToDevice, st));
     }
     if (start.back() > 0) {
-        k_fab_global<T><<<grid_for(start.back(), 256), 256, 0, st>>>(mf.dinfo.p, dr, ds, (int)regions.size(),
+        k_fab_global<T><<<grid_for(start.back(), 256 * FG_CELLS), 256, 0, st>>>(mf.dinfo.p, dr, ds,
+            (int)regions.size(),
             start.back(), (T*)mf.data.p, stage, glo[0], glo[1], glo[2], gn[0], gn[1], dir);
         g_launches++;
     }
