@@ -8,7 +8,10 @@
 // block barriers, and ends with the correction of level lc ready for the
 // grid-wide kernels above it.  Stage arithmetic is that of the grid-wide
 // FP32 kernels (stencil form, ghost values filled as applyBC does); the
-// bottom solve is the FP64 BiCGStab of bottom.cuh.
+// bottom solve is the FP64 BiCGStab of bottom.cuh.  `part` selects the
+// stages: 1 the levels down to the bottom, 2 the levels back up from it, 3
+// all of them with the bottom solve inside this block (1 and 2 leave the
+// bottom solve to the one-warp k_bottom launched between them).
 #pragma once
 
 #include "bottom.cuh"
@@ -31,9 +34,11 @@ template <bool ABEC>
 __global__ void __launch_bounds__(COARSE_THREADS, 1)
 k_coarse_vcycle (const CoarseLevelPtrs* __restrict__ lv, int lc, const BottomLevelPtrs* __restrict__ blev,
                  const BottomJob* __restrict__ jobs, BottomParams prm, int nu1, int nu2,
-                 int* __restrict__ out_iters, int* __restrict__ out_ret)
+                 int* __restrict__ out_iters, int* __restrict__ out_ret, int part)
 {
     using namespace bottom_detail;
+    pdl_wait();
+    pdl_trigger();
     const BottomJob J = jobs[blockIdx.x];
     const int s = J.solve, lb = J.lev;
 
@@ -50,7 +55,7 @@ k_coarse_vcycle (const CoarseLevelPtrs* __restrict__ lv, int lc, const BottomLev
     };
 
     // ---- down
-    for (int l = lc; l < lb; ++l) {
+    for (int l = lc; l < lb && (part & 1); ++l) {
         const CoarseLevelPtrs& C = lv[l];
         const int p0 = C.L.sfirst[s], np = C.L.snp[s], t0 = C.tfirst[s], nt = C.tn[s];
         // cor = 0, ghosts included
@@ -90,10 +95,10 @@ k_coarse_vcycle (const CoarseLevelPtrs* __restrict__ lv, int lc, const BottomLev
     }
 
     // ---- bottom (FP64)
-    bottom_solve_block<float, ABEC>(blev[lb], J, prm, out_iters, out_ret);
+    if (part == 3) { bottom_solve_block<float, ABEC>(blev[lb], J, prm, out_iters, out_ret); }
 
     // ---- up
-    for (int l = lb - 1; l >= lc; --l) {
+    for (int l = lb - 1; l >= lc && (part & 2); --l) {
         const CoarseLevelPtrs& C = lv[l];
         const CoarseLevelPtrs& Cc = lv[l + 1];
         const int p0 = C.L.sfirst[s], np = C.L.snp[s], t0 = C.tfirst[s], nt = C.tn[s];

@@ -815,26 +815,32 @@ void Engine::Impl::vcycle (int top)
         launched();
     }
     const BottomParams prm = bottom_params();
-    if (coarse) {
+    int* const iters_slot = bot_iters.p + (size_t)bottom_slot() * nsolve;
+    int* const ret_slot = bot_ret.p + (size_t)bottom_slot() * nsolve;
+    // the coarse levels' stages in one block per solve, down and up, with the
+    // one-warp bottom solve launched between them
+    auto coarse_part = [&] (int part) {
         if (abec) {
-            k_coarse_vcycle<true><<<njobs, COARSE_THREADS, 0, st()>>>(coarse_lv.p, lc, bot_levels.p, bot_jobs.p, prm,
-                                                                      o.nu1, o.nu2, bot_iters.p + (size_t)bottom_slot() * nsolve,
-                                                                      bot_ret.p + (size_t)bottom_slot() * nsolve);
+            launch(k_coarse_vcycle<true>, njobs, COARSE_THREADS, 0, (const CoarseLevelPtrs*)coarse_lv.p, lc,
+                   (const BottomLevelPtrs*)bot_levels.p, (const BottomJob*)bot_jobs.p, prm, o.nu1, o.nu2, iters_slot,
+                   ret_slot, part);
         } else {
-            k_coarse_vcycle<false><<<njobs, COARSE_THREADS, 0, st()>>>(coarse_lv.p, lc, bot_levels.p, bot_jobs.p, prm,
-                                                                       o.nu1, o.nu2, bot_iters.p + (size_t)bottom_slot() * nsolve,
-                                                                      bot_ret.p + (size_t)bottom_slot() * nsolve);
+            launch(k_coarse_vcycle<false>, njobs, COARSE_THREADS, 0, (const CoarseLevelPtrs*)coarse_lv.p, lc,
+                   (const BottomLevelPtrs*)bot_levels.p, (const BottomJob*)bot_jobs.p, prm, o.nu1, o.nu2, iters_slot,
+                   ret_slot, part);
         }
-    } else if (abec) {
-        launch(k_bottom<T, true>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr,
-                                                              bot_iters.p + (size_t)bottom_slot() * nsolve,
-                   bot_ret.p + (size_t)bottom_slot() * nsolve);
+        launched();
+    };
+    if (coarse) { coarse_part(1); }
+    if (abec) {
+        launch(k_bottom<T, true>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr, iters_slot,
+               ret_slot);
     } else {
-        launch(k_bottom<T, false>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr,
-                                                               bot_iters.p + (size_t)bottom_slot() * nsolve,
-                   bot_ret.p + (size_t)bottom_slot() * nsolve);
+        launch(k_bottom<T, false>, njobs, bot_threads, 0, bot_levels.p, bot_jobs.p, prm, nullptr, iters_slot,
+               ret_slot);
     }
     launched();
+    if (coarse) { coarse_part(2); }
     bottom_done();
     for (int l = top_end - 1; l >= top; --l) {
         LevelData& L = lev[l];
