@@ -322,12 +322,15 @@ k_sweep_fused2 (DevLevel L, Subset S, const float* __restrict__ phi_in, float* _
 // each 2x2x2 group, summed in k_restrict's order.  The fine residual never
 // goes to memory, and the restriction is no separate launch.  A level is
 // coarsenable, so patches and tiles start on even cells and hold whole groups.
-// Each thread issues the loads of its 8 cells' rhs and stencil values before
-// it waits for the copy (64 values in registers; three blocks per SM), which
-// hides the copy's latency: separate residual and restriction launches took
-// 0.85 ms more per 256^3 solve, loads issued after the wait 0.5 ms more.
-template <bool VARC>
-__global__ void __launch_bounds__(FS_THREADS, 3)
+// Each thread computes the residuals of a column of 8 cells; the loads of the
+// first NB planes' rhs and stencil values are issued before it waits for the
+// copy, the rest after it.  Measured on the 256^3 solve (ABec): all 8 planes
+// early (64 values in registers, 3 blocks per SM) 23.34 ms, 4 early at 4 / 5
+// blocks 23.31 / 23.10 ms, 2 early at 5 blocks 22.98 ms, none early at 5 / 6
+// blocks 23.14 / 23.10 ms; the separate residual and restriction launches
+// 23.78 ms.
+template <bool VARC, int NB = FS_TZ, int MINB = 3>
+__global__ void __launch_bounds__(FS_THREADS, MINB)
 k_resid_restrict_tma (DevLevel L, Subset S, DevLevel Lc, const float* __restrict__ rhs, StencilPtrs Sc,
                       const CUtensorMap* __restrict__ maps, float* __restrict__ crse, int* err)
 {
@@ -380,23 +383,29 @@ k_resid_restrict_tma (DevLevel L, Subset S, DevLevel Lc, const float* __restrict
     const bool inxy = lx <= ph[0] && ly <= ph[1];
     const long long q0 = P.idx(x0, y0, z0);
     const int sx = P.sx, sxy = (int)P.sxy;
-    float rv[FS_TZ], dv[FS_TZ], xl[FS_TZ], xh[FS_TZ], yl[FS_TZ], yh[FS_TZ], zl[FS_TZ], zh[FS_TZ];
-#pragma unroll
-    for (int lz = 0; lz < FS_TZ; ++lz) {
+    // the stencil of plane lz of the thread's column (zeros outside the patch)
+    struct Cell8 { float r, d, xl, xh, yl, yh, zl, zh; };
+    auto load = [&] (int lz) {
+        Cell8 c{};
         const bool in = inxy && lz <= ph[2];
         const int o = lz * sxy + ly * sx + lx;
-        rv[lz] = in ? __ldg(rhs + q0 + o) : 0.0f;
+        c.r = in ? __ldg(rhs + q0 + o) : 0.0f;
         if constexpr (VARC) {
             const float* Dp = static_cast<const float*>(Sc.D) + q0;
             const float* SXp = static_cast<const float*>(Sc.sx) + q0;
             const float* SYp = static_cast<const float*>(Sc.sy) + q0;
             const float* SZp = static_cast<const float*>(Sc.sz) + q0;
-            dv[lz] = in ? __ldg(Dp + o) : 0.0f;
-            xl[lz] = in ? __ldg(SXp + o) : 0.0f; xh[lz] = in ? __ldg(SXp + o + 1) : 0.0f;
-            yl[lz] = in ? __ldg(SYp + o) : 0.0f; yh[lz] = in ? __ldg(SYp + o + sx) : 0.0f;
-            zl[lz] = in ? __ldg(SZp + o) : 0.0f; zh[lz] = in ? __ldg(SZp + o + sxy) : 0.0f;
+            c.d = in ? __ldg(Dp + o) : 0.0f;
+            c.xl = in ? __ldg(SXp + o) : 0.0f; c.xh = in ? __ldg(SXp + o + 1) : 0.0f;
+            c.yl = in ? __ldg(SYp + o) : 0.0f; c.yh = in ? __ldg(SYp + o + sx) : 0.0f;
+            c.zl = in ? __ldg(SZp + o) : 0.0f; c.zh = in ? __ldg(SZp + o + sxy) : 0.0f;
         }
-    }
+        return c;
+    };
+    // the first NB planes' loads are issued before the copy's wait
+    Cell8 pre[NB > 0 ? NB : 1];
+#pragma unroll
+    for (int lz = 0; lz < NB; ++lz) { pre[lz] = load(lz); }
     const bool late = !tma::mbar_wait_bounded(&bar, 0, tma::WAIT_LIMIT);
     if (__syncthreads_or(late)) {
         if (tid == 0) { atomicExch(err, tma::ERR_TMA_TIMEOUT); }
@@ -433,17 +442,18 @@ k_resid_restrict_tma (DevLevel L, Subset S, DevLevel Lc, const float* __restrict
 #pragma unroll
         for (int lz = 0; lz < FS_TZ; ++lz) {
             float v = 0.0f;
+            const Cell8 c = (lz < NB) ? pre[lz < NB ? lz : 0] : load(lz);
             if (inxy && lz <= ph[2]) {
                 float d, sxl, sxh, syl, syh, szl, szh;
                 if constexpr (VARC) {
-                    d = dv[lz]; sxl = xl[lz]; sxh = xh[lz]; syl = yl[lz]; syh = yh[lz]; szl = zl[lz]; szh = zh[lz];
+                    d = c.d; sxl = c.xl; sxh = c.xh; syl = c.yl; syh = c.yh; szl = c.zl; szh = c.zh;
                 } else {
                     d = cdd; sxl = sxh = -dhx; syl = syh = -dhy; szl = szh = -dhz;
                 }
                 const float xc = aat(lx, ly, lz);
                 const float nb = sxl * aat(lx - 1, ly, lz) + sxh * aat(lx + 1, ly, lz) + syl * aat(lx, ly - 1, lz) +
                                  syh * aat(lx, ly + 1, lz) + szl * aat(lx, ly, lz - 1) + szh * aat(lx, ly, lz + 1);
-                v = rv[lz] - (d * xc - nb);
+                v = c.r - (d * xc - nb);
             }
             R[lz][ly][lx] = v;
         }

@@ -681,12 +681,14 @@ bool Engine::Impl::resid_restrict_fused (int l)
     LevelData& C = lev[l + 1];
     const dim3 g(L.fz.ntiles), blk(FS_TX, FS_TY);
     const StencilPtrs S = stencil32(l);
+    // ABec: the first two planes' stencil loads before the copy's wait, five
+    // blocks per SM; MLPoisson loads only rhs, all eight planes early
     if (abec) {
-        launch(k_resid_restrict_tma<true>, g, blk, 0, L.dl, L.fz.dev(), C.dl, L.res32.p, S, L.tm_a.p, C.res32.p,
-               err_d.p);
+        launch(k_resid_restrict_tma<true, 2, 5>, g, blk, 0, L.dl, L.fz.dev(), C.dl, L.res32.p, S, L.tm_a.p,
+               C.res32.p, err_d.p);
     } else {
-        launch(k_resid_restrict_tma<false>, g, blk, 0, L.dl, L.fz.dev(), C.dl, L.res32.p, S, L.tm_a.p, C.res32.p,
-               err_d.p);
+        launch(k_resid_restrict_tma<false, 8, 5>, g, blk, 0, L.dl, L.fz.dev(), C.dl, L.res32.p, S, L.tm_a.p,
+               C.res32.p, err_d.p);
     }
     launched();
     return true;
