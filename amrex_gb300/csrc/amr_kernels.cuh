@@ -346,21 +346,24 @@ k_amr_resid (DevLevel L, Subset S, TO* __restrict__ r, const TX* __restrict__ x,
     pdl_trigger();
     const TileCoord c = decode_tile(L, S, blockIdx.x);
     const PatchDesc& P = L.P[c.p];
+    // the geometry in registers, one 64-bit row start per plane
+    const PatchGeom G = geom_of(P);
     const int j = c.y0 + threadIdx.y;
-    if (j > P.hi[1]) { return; }
-    const TX pdhx = convert<TX>(P.dha[0]), pdhy = convert<TX>(P.dha[1]), pdhz = convert<TX>(P.dha[2]);
+    if (j > G.hi[1]) { return; }
+    const TX pdhx = convert<TX>(G.dha[0]), pdhy = convert<TX>(G.dha[1]), pdhz = convert<TX>(G.dha[2]);
     for (int kk = 0; kk < TILE_Z; ++kk) {
         const int k = c.z0 + kk;
-        if (k > P.hi[2]) { break; }
+        if (k > G.hi[2]) { break; }
+        const long long row = cidx(G, G.lo[0], j, k);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int i = c.x0 + threadIdx.x + 32 * h;
-            if (i > P.hi[0]) { continue; }
-            const long long q = cidx(P, i, j, k);
+            if (i > G.hi[0]) { continue; }
+            const long long q = row + (i - G.lo[0]);
             TX ax;
             if constexpr (!ABEC) {
                 // adotx_cell's MLPoisson form with the factors converted once per block
-                const long long sx = P.sx, sxy = P.sxy;
+                const int sx = G.sx, sxy = (int)G.sxy;
                 const TX xc = x[q];
                 ax = pdhx * (x[q - 1] - TX(2.0) * xc + x[q + 1])
                    + pdhy * (x[q - sx] - TX(2.0) * xc + x[q + sx])
@@ -392,21 +395,28 @@ k_amr_interp_add (DevLevel Lf, Subset Sf, const PatchDesc* __restrict__ cfd, con
     pdl_wait();
     pdl_trigger();
     const TileCoord c = decode_tile(Lf, Sf, blockIdx.x);
-    const PatchDesc& F = Lf.P[c.p];
-    const PatchDesc& G = cfd[c.p];
+    // both layouts in registers; per plane one 64-bit row start in each, the
+    // rest 32-bit offsets (a coarse buffer plane holds fewer than 2^31 cells)
+    const PatchGeom F = geom_of(Lf.P[c.p]);
+    const PatchGeom G = geom_of(cfd[c.p]);
     const int j = c.y0 + threadIdx.y;
     if (j > F.hi[1]) { return; }
-    const long long gx = 1, gy = G.sx, gz = G.sxy;
+    const int gy = G.sx, gz = (int)G.sxy;
+    const int jc = j >> 1;
+    const int dj = (j & 1) ? gy : -gy;
     for (int kk = 0; kk < TILE_Z; ++kk) {
         const int k = c.z0 + kk;
         if (k > F.hi[2]) { break; }
+        const int kc = k >> 1;
+        const int dk = (k & 1) ? gz : -gz;
+        const long long grow = cidx(G, G.lo[0], jc, kc), frow = cidx(F, F.lo[0], j, k);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int i = c.x0 + threadIdx.x + 32 * h;
             if (i > F.hi[0]) { continue; }
-            const int ic = i >> 1, jc = j >> 1, kc = k >> 1;
-            const long long di = (i & 1) ? gx : -gx, dj = (j & 1) ? gy : -gy, dk = (k & 1) ? gz : -gz;
-            const long long q = cidx(G, ic, jc, kc);
+            const int ic = i >> 1;
+            const int di = (i & 1) ? 1 : -1;
+            const long long q = grow + (ic - G.lo[0]);
             const T v = T(0.421875) * cf[q]
                       + T(0.140625) * cf[q + di]
                       + T(0.140625) * cf[q + dj]
@@ -415,7 +425,7 @@ k_amr_interp_add (DevLevel Lf, Subset Sf, const PatchDesc* __restrict__ cfd, con
                       + T(0.046875) * cf[q + di + dk]
                       + T(0.046875) * cf[q + di + dj]
                       + T(0.015625) * cf[q + di + dj + dk];
-            const long long qf = cidx(F, i, j, k);
+            const long long qf = frow + (i - F.lo[0]);
             fine[qf] = v;
             sol[qf] += double(v);
             if (hold != nullptr) { hold[qf] += v; }
@@ -432,17 +442,18 @@ k_amr_finish (DevLevel L, Subset S, double* __restrict__ sol, T* __restrict__ co
     pdl_wait();
     pdl_trigger();
     const TileCoord c = decode_tile(L, S, blockIdx.x);
-    const PatchDesc& P = L.P[c.p];
+    const PatchGeom P = geom_of(L.P[c.p]);
     const int j = c.y0 + threadIdx.y;
     if (j > P.hi[1]) { return; }
     for (int kk = 0; kk < TILE_Z; ++kk) {
         const int k = c.z0 + kk;
         if (k > P.hi[2]) { break; }
+        const long long row = cidx(P, P.lo[0], j, k);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int i = c.x0 + threadIdx.x + 32 * h;
             if (i > P.hi[0]) { continue; }
-            const long long q = cidx(P, i, j, k);
+            const long long q = row + (i - P.lo[0]);
             const T v = cor[q];
             sol[q] += double(v);
             if (hold != nullptr) { cor[q] = v + hold[q]; }
