@@ -14,11 +14,13 @@ __device__ __forceinline__ void tag_cell (const CopyTag* tags, const long long* 
 {
     w = bsearch_ll<int>(start, ntag, t);
     const CopyTag& C = tags[w];
-    const long long u = t - start[w];
-    const int nx = C.box.hi[0] - C.box.lo[0] + 1, ny = C.box.hi[1] - C.box.lo[1] + 1;
-    i = C.box.lo[0] + (int)(u % nx);
-    j = C.box.lo[1] + (int)((u / nx) % ny);
-    k = C.box.lo[2] + (int)(u / ((long long)nx * ny));
+    // a box holds fewer than 2^32 cells: 32-bit index arithmetic
+    const unsigned u = (unsigned)(t - start[w]);
+    const unsigned nx = C.box.hi[0] - C.box.lo[0] + 1, ny = C.box.hi[1] - C.box.lo[1] + 1;
+    const unsigned row = u / nx;
+    i = C.box.lo[0] + (int)(u - row * nx);
+    j = C.box.lo[1] + (int)(row % ny);
+    k = C.box.lo[2] + (int)(row / ny);
 }
 
 // The coarse level's field (valid cells) into the per-fine-patch coarse

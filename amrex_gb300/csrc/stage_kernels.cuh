@@ -206,11 +206,12 @@ __device__ __forceinline__ int bsearch_ll (const long long* start, int n, long l
 __device__ __forceinline__ void face_cell (const PatchDesc& P, int f, long long u, int& i, int& j, int& k)
 {
     const int d = f % 3;
-    const int nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1;
+    const unsigned nx = P.hi[0] - P.lo[0] + 1, ny = P.hi[1] - P.lo[1] + 1;
     const int g = (f >= 3) ? P.hi[d] + 1 : P.lo[d] - 1;
-    if (d == 0) { i = g; j = P.lo[1] + (int)(u % ny); k = P.lo[2] + (int)(u / ny); }
-    else if (d == 1) { j = g; i = P.lo[0] + (int)(u % nx); k = P.lo[2] + (int)(u / nx); }
-    else { k = g; i = P.lo[0] + (int)(u % nx); j = P.lo[1] + (int)(u / nx); }
+    const unsigned uu = (unsigned)u;          // a face holds fewer than 2^32 cells
+    if (d == 0) { i = g; j = P.lo[1] + (int)(uu % ny); k = P.lo[2] + (int)(uu / ny); }
+    else if (d == 1) { j = g; i = P.lo[0] + (int)(uu % nx); k = P.lo[2] + (int)(uu / nx); }
+    else { k = g; i = P.lo[0] + (int)(uu % nx); j = P.lo[1] + (int)(uu / nx); }
 }
 
 // FillBoundary (face ghosts) + physical/coarse-fine BC closure, one launch:
@@ -242,11 +243,12 @@ __global__ void k_ghost (DevLevel L, GhostWork W, T* __restrict__ phi, int inhom
         if (t >= W.ntagcells) { return; }
         const int w = bsearch_ll<int>(W.tstart, W.ntag, t);
         const CopyTag& C = W.tags[w];
-        const long long u = t - W.tstart[w];
-        const int nx = C.box.hi[0] - C.box.lo[0] + 1, ny = C.box.hi[1] - C.box.lo[1] + 1;
-        const int i = C.box.lo[0] + (int)(u % nx);
-        const int j = C.box.lo[1] + (int)((u / nx) % ny);
-        const int k = C.box.lo[2] + (int)(u / ((long long)nx * ny));
+        const unsigned u = (unsigned)(t - W.tstart[w]);      // a tag box holds fewer than 2^32 cells
+        const unsigned nx = C.box.hi[0] - C.box.lo[0] + 1, ny = C.box.hi[1] - C.box.lo[1] + 1;
+        const unsigned row = u / nx;
+        const int i = C.box.lo[0] + (int)(u - row * nx);
+        const int j = C.box.lo[1] + (int)(row % ny);
+        const int k = C.box.lo[2] + (int)(row / ny);
         const PatchDesc& D = L.P[C.dst];
         const PatchDesc& Sp = L.P[C.src];
         phi[cidx(D, i, j, k)] = phi[cidx(Sp, i - C.shift[0], j - C.shift[1], k - C.shift[2])];
