@@ -94,6 +94,20 @@ def test_amr_fused_fine_sweeps_bitwise(name):
         np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("name", ["c2_n32", "c2_n16_2lev_bc", "c2_n16_2lev_per", "c2_n16_2lev_abec", "c2_n16_4lev"])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_amr_dependent_launches_bitwise(name, precision):
+    """Programmatic dependent launches (every composite-path kernel waits on
+    its predecessor with griddepcontrol.wait) change only when kernels start:
+    the solutions with and without them are bit for bit the same."""
+    _, P1, r1, phis1 = _solve(name, precision=precision, graph=True, fused=bool(precision), options={"pdl": 1})
+    _, P0, r0, phis0 = _solve(name, precision=precision, graph=True, fused=bool(precision), options={"pdl": 0})
+    assert P1["mlmg"].getNumIters() == P0["mlmg"].getNumIters()
+    assert r1 == r0
+    for a, b in zip(phis1, phis0):
+        np.testing.assert_array_equal(a, b)
+
+
 def test_amr_graph_replay_matches_eager_fp64():
     _, P0, r0, phis0 = _solve("c2_n32", precision=0, graph=False)
     _, P1, r1, phis1 = _solve("c2_n32", precision=0, graph=True)

@@ -262,6 +262,24 @@ def test_graph_replay_is_bitwise_identical():
     assert np.array_equal(helpers.solution(p1, c), helpers.solution(p2, c))
 
 
+@pytest.mark.parametrize("name", ["solve_abec_32", "solve_poisson_32", "solve_abec_mixed_bc", "solve_abec_agg8",
+                                  "solve_poisson_periodic_x"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_dependent_launches_bitwise(name, precision):
+    """Programmatic dependent launches change only when kernels start: the
+    graph solves with and without them are bit for bit the same."""
+    c = load.load(name)["case"]
+    inp = cases.inputs(c)
+    out = []
+    for pdl in (1, 0):
+        p = helpers.make_problem(c, inp, precision=precision, graph=True, fused=precision == "mixed",
+                                 options={"pdl": pdl})
+        p["mlmg"].solve(p["sol"], p["rhs"], 1e-10, 0)
+        out.append((p["mlmg"].getNumIters(), list(p["mlmg"].getResidualHistory()), helpers.solution(p, c)))
+    assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
+    assert np.array_equal(out[0][2], out[1][2])
+
+
 def test_oracle_and_gpu_agree_on_unpinned_shape():
     """A shape with no golden fixture (anisotropic, ragged boxes, Neumann and
     reflect_odd faces): the GPU FP64 solve against the CPU oracle."""
