@@ -113,7 +113,8 @@ int mlmg_multifab_download(mlmg_multifab mf, int box, void* host);
  * out of every box's valid cells -- one host<->device copy and one kernel */
 int mlmg_multifab_upload_global(mlmg_multifab mf, const void* host, const int glo[3], const int gn[3]);
 int mlmg_multifab_download_global(mlmg_multifab mf, void* host, const int glo[3], const int gn[3]);
-int mlmg_multifab_setval(mlmg_multifab mf, double v);                    /* FabArray::setVal, ghosts included */
+int mlmg_multifab_setval(mlmg_multifab mf, double v);                    /* FabArray::setVal, ghosts included;
+                                                                          * stream-ordered, returns without waiting */
 /* FabArray::FillBoundary (Src/Base/AMReX_FabArray.H:1000-1044), one rank */
 int mlmg_multifab_fill_boundary(mlmg_multifab mf, mlmg_geometry geom, int cross);
 int mlmg_multifab_norminf(mlmg_multifab mf, double* out);                /* valid cells */
@@ -231,7 +232,12 @@ int mlmg_set_fused_smoother(mlmg_solver s, int on);      /* fused two-colour Gau
  * -1 the default bound; 0 makes every wait expire -- a test of the failure
  * path: each block then waits, with the full bound, for its own copy, leaves,
  * and the solve returns -7; the next solve with the default works);
- * -4 for an unknown name */
+ * "pdl" (0/1: V-cycle and composite-path kernels as programmatic dependent
+ * launches, default 1), "fused_fine" (0/1/2: AMR fine levels smoothed by
+ * colour passes per level / fused sweeps where the tile allows them, the
+ * default / colour passes on every tile), "fused_restrict" (0/1: the
+ * correction residual and its restriction on TMA-swept levels in one tile
+ * kernel, default 1); -4 for an unknown name */
 int mlmg_set_option(mlmg_solver s, const char* name, double value);
 /* time every finest-level smoother launch and every FP64 outer residual of
  * the mixed path with CUDA events on the library stream (graph replays
